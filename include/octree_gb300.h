@@ -1,0 +1,181 @@
+/*
+ * octree_gb300.h — C-ABI of the GB300 Morton location-code tree (OrthoTree's OctreePoint /
+ * OctreeBox, Create + data-parallel queries) implemented with sm_103a CUDA kernels.
+ *
+ * The boundary takes plain pointers and sizes only. Every function returns an int status
+ * (OTG_OK on success). Each entry point names the reference interface it replaces, with paths
+ * relative to the OrthoTree project root.
+ *
+ * Memory spaces: inputs marked "mem" are host pointers (OTG_MEM_HOST; copied to the device
+ * inside the call) or device pointers (OTG_MEM_DEVICE). Query results stay in device memory,
+ * owned by an otg_result, until copied out with otg_result_copy().
+ *
+ * Scalars: a tree is OTG_SCALAR_F64 (double, the reference default BaseGeometryType) or
+ * OTG_SCALAR_F32 (float); entity, query and plane arrays use the tree's scalar type.
+ * Tolerance arguments are double; a negative tolerance selects the reference default
+ * BASE_TOLERANCE = 100 * epsilon of the tree's scalar type (adapters/general.h:57).
+ *
+ * Layouts (all 3-D, arrays of structs exactly as the reference's types):
+ *   point   : {x, y, z}                               PointND<3>       (adapters/general.h:346-347)
+ *   box     : {min x, min y, min z, max x, max y, max z} BoundingBoxND<3> (adapters/general.h:349-354)
+ *   ray     : {origin x, y, z, direction x, y, z}      RayND<3>         (adapters/general.h:356-361)
+ *   plane   : {origo distance, normal x, y, z}         PlaneND<3>       (adapters/general.h:363-368)
+ *
+ * Streams: `stream` is a cudaStream_t (NULL = legacy default stream). Calls that return sizes to
+ * the host synchronise that stream before returning.
+ */
+#ifndef OCTREE_GB300_H
+#define OCTREE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OTG_OK 0
+#define OTG_ERR_INVALID_ARGUMENT 1 /* misuse that the reference answers with ORTHOTREE_CRASH_IF / assert */
+#define OTG_ERR_CUDA 2             /* a CUDA runtime call failed; see otg_last_error() */
+#define OTG_ERR_OUT_OF_MEMORY 3
+#define OTG_ERR_TIMEOUT 5          /* a bounded device-side wait ran out (never a hang) */
+#define OTG_ERR_NOT_SUPPORTED 6
+#define OTG_ERR_NO_DEVICE 7        /* no CUDA device: there is no CPU fallback */
+
+#define OTG_MEM_HOST 0
+#define OTG_MEM_DEVICE 1
+
+#define OTG_SCALAR_F64 0
+#define OTG_SCALAR_F32 1
+
+/* tree kinds: core/ot_aliases.h:119 (OctreePoint) and :122 (OctreeBox) */
+#define OTG_KIND_POINTS 0 /* loose factor 1.0, MinPoint node geometry (core/configuration.h:104-105) */
+#define OTG_KIND_BOXES 1  /* loose factor 2.0, MBR node geometry      (core/configuration.h:107-108) */
+
+/* RangeSearchMode, core/types.h:83-87 */
+#define OTG_RANGE_INSIDE 0
+#define OTG_RANGE_OVERLAP 1
+
+/* query-kernel variants: the plain one-query-per-thread FP64 kernels, and the batched kernels
+   (warp per query, FP32 outward-rounded filter, FP64 recheck). Both return identical results. */
+#define OTG_ALGO_DEFAULT 0
+#define OTG_ALGO_PLAIN_FP64 1
+#define OTG_ALGO_FILTERED 2
+
+typedef struct otg_tree otg_tree;
+typedef struct otg_result otg_result;
+
+typedef struct otg_tree_info
+{
+  uint64_t entity_count;
+  uint64_t node_count;
+  uint32_t max_depth;   /* maxDepthID after EstimateMaxDepth (detail/utils.h:613-622) */
+  uint32_t scalar;      /* OTG_SCALAR_* */
+  uint32_t kind;        /* OTG_KIND_* */
+  uint32_t reserved;
+  uint64_t max_elements;
+  double space_min[3];  /* the tree's space (given box or the entities' bounding box) */
+  double space_max[3];
+} otg_tree_info;
+
+/* Last error message of the calling thread (empty when none). */
+const char* otg_last_error(void);
+
+/* Number of CUDA devices usable by the library (0: every compute call returns OTG_ERR_NO_DEVICE). */
+int otg_device_count(void);
+
+/* Allocates an empty tree object; replaces the default constructor of
+   DynamicHashOrthoTreeCore (core/ot_dynamic_hash_core.h:333). */
+int otg_tree_new(otg_tree** out, int scalar, int kind);
+void otg_tree_free(otg_tree* tree);
+
+/* (Re)builds the tree from n entities: the entity span of
+   DynamicHashOrthoTreeCore::Create(entities, maxDepth, box, maxElementNo, exec)
+   (core/ot_dynamic_hash_core.h:751-809) and the static Create(tree, ...) (:812-822), also reached
+   through OrthoTreeManaged::Create (core/ot_managed.h:169-228, 318-360).
+   max_depth 0 = estimate (EstimateMaxDepth); box NULL = the entities' bounding box.
+   The entity array is copied into the tree (the Managed form's ownership, ot_managed.h:70-71);
+   queries therefore need no entity argument. Asynchronous on `stream` unless mem == OTG_MEM_HOST,
+   in which case the call returns after the build finished and reports device-side errors. */
+int otg_tree_create(otg_tree* tree, const void* entities, uint64_t n, uint32_t max_depth, const void* box, uint64_t max_elements, int mem,
+                    void* stream);
+
+/* Waits for the tree's last build on `stream` and reports device-side errors (OTG_ERR_TIMEOUT). */
+int otg_tree_sync(otg_tree* tree, void* stream);
+
+int otg_tree_info_get(const otg_tree* tree, otg_tree_info* info);
+
+/* Per-entity location keys (loc << 5 | depth, input order), as MortonGridSpaceIndexing::GetLocation
+   and the compact Location storage produce them (detail/si_mortongrid.h:69-97, detail/si_morton.h:117-143).
+   keys: device or host array of entity_count uint64. */
+int otg_tree_export_locations(const otg_tree* tree, uint64_t* keys, int mem, void* stream);
+
+/* The node set reachable from the root, in breadth-first order: node keys with sentinel bit
+   (detail/si_morton.h:210-235), node min point and size as GetNodeMinPoint / GetNodeSize return them
+   (core/ot_dynamic_hash_core.h:491-519), the node's own entity ids, child counts.
+   keys[node_count], min_size[node_count*6] (double), entity_offsets[node_count+1],
+   entity_ids[entity_count] (every reachable entity once), child_count[node_count]. Host memory. */
+int otg_tree_export_nodes(const otg_tree* tree, uint64_t* keys, double* min_size, uint64_t* entity_offsets, uint32_t* entity_ids,
+                          uint32_t* child_count);
+
+/* ---------------------------------------------------------------- queries (batched) */
+
+/* RangeSearch(range, entities, mode, tol) per query box (core/ot_query.h:476-583). */
+int otg_range_search(const otg_tree* tree, const void* ranges, uint64_t n_queries, int mode, double tol, int algo, otg_result** out, int mem,
+                     void* stream);
+
+/* PickSearch(point, entities, tol) per query point (core/ot_query.h:425-466). */
+int otg_pick_search(const otg_tree* tree, const void* points, uint64_t n_queries, double tol, int algo, otg_result** out, int mem, void* stream);
+
+/* GetNearestNeighbors(point, k, maxDistanceWithin, entities, tol) (core/ot_query.h:1208-1270).
+   k: n_queries uint32 (mem space of the points) or NULL with k_all for every query.
+   max_distance < 0: unbounded (std::numeric_limits<Scalar>::max()). Results by (distance, id);
+   more than k ids are returned when distances tie within the tolerance, as in the reference. */
+int otg_knn(const otg_tree* tree, const void* points, uint64_t n_queries, const uint32_t* k, uint32_t k_all, double max_distance, double tol,
+            int algo, otg_result** out, int mem, void* stream);
+
+/* FrustumCulling(planes, entities, tol) (core/ot_query.h:767-833): planes_per_query planes per query. */
+int otg_frustum_culling(const otg_tree* tree, const void* planes, uint64_t planes_per_query, uint64_t n_queries, double tol, int algo,
+                        otg_result** out, int mem, void* stream);
+
+/* RayIntersectedAll(origin, direction, entities, tol, toleranceIncrement, maxExaminationDistance)
+   (core/ot_query.h:1928-2022). max_distance < 0: unbounded; 0: no limit (reference semantics).
+   Results by (enter distance, id). */
+int otg_ray_all(const otg_tree* tree, const void* rays, uint64_t n_queries, double tol, double tol_increment, double max_distance, int algo,
+                otg_result** out, int mem, void* stream);
+
+/* RayIntersectedFirst(...) (core/ot_query.h:2035-2146). Results by (enter distance, id); the
+   reference returns the same set farthest first. */
+int otg_ray_first(const otg_tree* tree, const void* rays, uint64_t n_queries, double tol, double tol_increment, double max_distance, int algo,
+                  otg_result** out, int mem, void* stream);
+
+/* CollisionDetection(entities, tol, exec) within one box tree (core/ot_query.h:1690-1914).
+   One result "query" whose ids are pairs (i, j), i < j, ascending. */
+int otg_collision_self(const otg_tree* tree, double tol, int algo, otg_result** out, void* stream);
+
+/* CollisionDetection(leftTree, leftEntities, rightTree, rightEntities, tol) (core/ot_query.h:1462-1497).
+   Pairs (left id, right id), ascending. */
+int otg_collision_pair(const otg_tree* left, const otg_tree* right, double tol, int algo, otg_result** out, void* stream);
+
+/* ---------------------------------------------------------------- results */
+int otg_result_info(const otg_result* r, uint64_t* n_queries, uint64_t* n_ids, int* has_distances);
+/* offsets[n_queries+1], ids[n_ids], distances[n_ids] (double; may be NULL). mem: destination space. */
+int otg_result_copy(const otg_result* r, uint64_t* offsets, uint32_t* ids, double* distances, int mem, void* stream);
+/* Device pointers owned by the result (valid until otg_result_free). */
+int otg_result_device_ptrs(const otg_result* r, const uint64_t** offsets, const uint32_t** ids, const double** distances);
+/* Statistics of the last query that produced r: FP32-filter tests and FP64 rechecks. */
+int otg_result_stats(const otg_result* r, uint64_t* filter_tests, uint64_t* fp64_rechecks);
+void otg_result_free(otg_result* r);
+
+/* ---------------------------------------------------------------- instrumentation
+   No counterpart in the reference. When enabled, each otg_tree_create records a CUDA event on
+   its stream before every build phase; after the stream has completed, otg_profile_phase()
+   returns the phase names and their device durations (ms) of the last build. */
+int otg_profile_enable(int on);
+int otg_profile_phase_count(void);
+int otg_profile_phase(int index, char* name, int name_capacity, float* milliseconds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OCTREE_GB300_H */

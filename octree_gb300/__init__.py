@@ -1,0 +1,318 @@
+"""Python host binding of the GB300 Morton location-code tree (C-ABI in include/octree_gb300.h).
+
+The binding mirrors OrthoTree's Managed trees (OctreePointM / OctreeBoxM, core/ot_managed.h): the
+tree owns a device copy of its entities, Create() rebuilds it, and every query is batched (one
+call answers many query geometries). Inputs are numpy arrays (host) or torch CUDA tensors
+(device). There is no CPU path: importing works anywhere, but every compute call raises
+OtgError when the CUDA library or a GPU is missing.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "liboctree_gb300.so")
+
+OTG_OK = 0
+MEM_HOST, MEM_DEVICE = 0, 1
+SCALAR_F64, SCALAR_F32 = 0, 1
+KIND_POINTS, KIND_BOXES = 0, 1
+RANGE_INSIDE, RANGE_OVERLAP = 0, 1
+ALGO_DEFAULT, ALGO_PLAIN_FP64, ALGO_FILTERED = 0, 1, 2
+
+_STATUS = {
+    1: "invalid argument",
+    2: "CUDA error",
+    3: "out of memory",
+    5: "device wait timed out",
+    6: "not supported",
+    7: "no CUDA device",
+}
+
+_vp, _u64, _u32, _dbl, _int = C.c_void_p, C.c_uint64, C.c_uint32, C.c_double, C.c_int
+
+# (name, restype, argtypes) of every exported entry point, in include/octree_gb300.h order
+EXPORTS = [
+    ("otg_last_error", C.c_char_p, []),
+    ("otg_device_count", _int, []),
+    ("otg_tree_new", _int, [C.POINTER(_vp), _int, _int]),
+    ("otg_tree_free", None, [_vp]),
+    ("otg_tree_create", _int, [_vp, _vp, _u64, _u32, _vp, _u64, _int, _vp]),
+    ("otg_tree_sync", _int, [_vp, _vp]),
+    ("otg_tree_info_get", _int, [_vp, _vp]),
+    ("otg_tree_export_locations", _int, [_vp, _vp, _int, _vp]),
+    ("otg_tree_export_nodes", _int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    ("otg_range_search", _int, [_vp, _vp, _u64, _int, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_pick_search", _int, [_vp, _vp, _u64, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_knn", _int, [_vp, _vp, _u64, _vp, _u32, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_frustum_culling", _int, [_vp, _vp, _u64, _u64, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_ray_all", _int, [_vp, _vp, _u64, _dbl, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_ray_first", _int, [_vp, _vp, _u64, _dbl, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_collision_self", _int, [_vp, _dbl, _int, C.POINTER(_vp), _vp]),
+    ("otg_collision_pair", _int, [_vp, _vp, _dbl, _int, C.POINTER(_vp), _vp]),
+    ("otg_result_info", _int, [_vp, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_int)]),
+    ("otg_result_copy", _int, [_vp, _vp, _vp, _vp, _int, _vp]),
+    ("otg_result_device_ptrs", _int, [_vp, _vp, _vp, _vp]),
+    ("otg_result_stats", _int, [_vp, C.POINTER(_u64), C.POINTER(_u64)]),
+    ("otg_result_free", None, [_vp]),
+    ("otg_profile_enable", _int, [_int]),
+    ("otg_profile_phase_count", _int, []),
+    ("otg_profile_phase", _int, [_int, C.c_char_p, _int, C.POINTER(C.c_float)]),
+]
+
+
+class OtgError(RuntimeError):
+    pass
+
+
+class _TreeInfo(C.Structure):
+    _fields_ = [
+        ("entity_count", _u64),
+        ("node_count", _u64),
+        ("max_depth", _u32),
+        ("scalar", _u32),
+        ("kind", _u32),
+        ("reserved", _u32),
+        ("max_elements", _u64),
+        ("space_min", _dbl * 3),
+        ("space_max", _dbl * 3),
+    ]
+
+
+_lib = None
+
+
+def library():
+    """Loads the CUDA library built by __graft_entry__.build(); raises when it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OtgError(f"CUDA library not built: {LIB_PATH} (run __graft_entry__.build())")
+        lib = C.CDLL(LIB_PATH)
+        for name, res, args in EXPORTS:
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _check(rc):
+    if rc != OTG_OK:
+        msg = library().otg_last_error().decode(errors="replace")
+        raise OtgError(f"{_STATUS.get(rc, rc)}: {msg}")
+
+
+def device_count():
+    return library().otg_device_count()
+
+
+def profile_enable(on=True):
+    _check(library().otg_profile_enable(1 if on else 0))
+
+
+def profile_phases():
+    """[(phase name, device ms)] of the last build (after its stream completed)."""
+    lib = library()
+    out = []
+    for i in range(lib.otg_profile_phase_count()):
+        buf = C.create_string_buffer(64)
+        ms = C.c_float()
+        _check(lib.otg_profile_phase(i, buf, 64, C.byref(ms)))
+        out.append((buf.value.decode(), ms.value))
+    return out
+
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+def _arg(a, dtype):
+    """(pointer, mem space, keepalive) of an array argument in the tree's scalar type."""
+    if a is None:
+        return None, MEM_HOST, None
+    if _is_torch(a):
+        import torch
+
+        tdt = torch.float64 if dtype == np.float64 else (torch.float32 if dtype == np.float32 else torch.uint32)
+        if a.dtype != tdt:
+            a = a.to(tdt)
+        a = a.contiguous()
+        return C.c_void_p(a.data_ptr()), (MEM_DEVICE if a.is_cuda else MEM_HOST), a
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a.ctypes.data_as(_vp), MEM_HOST, a
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return C.c_void_p(stream.cuda_stream)
+    return C.c_void_p(int(stream))
+
+
+class Result:
+    """Owner of a device result (CSR offsets + ids [+ distances])."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            library().otg_result_free(self.h)
+            self.h = None
+
+    def sizes(self):
+        nq, nids, hd = _u64(), _u64(), _int()
+        _check(library().otg_result_info(self.h, C.byref(nq), C.byref(nids), C.byref(hd)))
+        return nq.value, nids.value, bool(hd.value)
+
+    def stats(self):
+        a, b = _u64(), _u64()
+        _check(library().otg_result_stats(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def to_host(self, stream=None):
+        nq, nids, hd = self.sizes()
+        off = np.zeros(nq + 1, np.uint64)
+        ids = np.zeros(max(nids, 1), np.uint32)
+        dist = np.zeros(max(nids, 1), np.float64) if hd else None
+        _check(
+            library().otg_result_copy(
+                self.h, off.ctypes.data_as(_vp), ids.ctypes.data_as(_vp), None if dist is None else dist.ctypes.data_as(_vp), MEM_HOST, _stream_ptr(stream)
+            )
+        )
+        return off, ids[:nids], (dist[:nids] if dist is not None else None)
+
+
+class Tree:
+    """A GPU OctreePoint (kind='points') or OctreeBox (kind='boxes', loose factor 2.0)."""
+
+    def __init__(self, kind="points", dtype=np.float64):
+        self.kind = KIND_POINTS if kind == "points" else KIND_BOXES
+        self.dtype = np.dtype(dtype).type
+        self.scalar = SCALAR_F64 if self.dtype == np.float64 else SCALAR_F32
+        h = _vp()
+        _check(library().otg_tree_new(C.byref(h), self.scalar, self.kind))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            library().otg_tree_free(self.h)
+            self.h = None
+
+    # ------------------------------------------------------------------ Create
+    def create(self, entities, max_depth=0, box=None, max_elements=16, stream=None):
+        """OrthoTree Create(entities, maxDepth, box, maxElementNo) — core/ot_dynamic_hash_core.h:751-822."""
+        p, mem, keep = _arg(entities, self.dtype)
+        n = int(entities.shape[0]) if len(entities.shape) else 0
+        bp, bmem, bkeep = _arg(box, self.dtype)
+        if box is not None and bmem != mem:
+            bb = np.ascontiguousarray(box.cpu().numpy() if _is_torch(box) else box, dtype=self.dtype)
+            if mem == MEM_DEVICE:
+                import torch
+
+                bkeep = torch.as_tensor(bb, device="cuda")
+                bp = C.c_void_p(bkeep.data_ptr())
+            else:
+                bkeep = bb
+                bp = bb.ctypes.data_as(_vp)
+        _check(library().otg_tree_create(self.h, p, n, max_depth, bp, max_elements, mem, _stream_ptr(stream)))
+        self._keep = (keep, bkeep)
+        return self
+
+    def sync(self, stream=None):
+        _check(library().otg_tree_sync(self.h, _stream_ptr(stream)))
+
+    def info(self):
+        info = _TreeInfo()
+        _check(library().otg_tree_info_get(self.h, C.byref(info)))
+        return info
+
+    @property
+    def max_depth(self):
+        return self.info().max_depth
+
+    @property
+    def node_count(self):
+        return self.info().node_count
+
+    def location_keys(self):
+        n = self.info().entity_count
+        out = np.zeros(max(n, 1), np.uint64)
+        _check(library().otg_tree_export_locations(self.h, out.ctypes.data_as(_vp), MEM_HOST, None))
+        return out[:n]
+
+    def nodes(self):
+        info = self.info()
+        m, n = info.node_count, info.entity_count
+        keys = np.zeros(m, np.uint64)
+        ms = np.zeros((m, 6), np.float64)
+        eoff = np.zeros(m + 1, np.uint64)
+        eids = np.zeros(max(n, 1), np.uint32)
+        cc = np.zeros(m, np.uint32)
+        _check(
+            library().otg_tree_export_nodes(
+                self.h, keys.ctypes.data_as(_vp), ms.ctypes.data_as(_vp), eoff.ctypes.data_as(_vp), eids.ctypes.data_as(_vp), cc.ctypes.data_as(_vp)
+            )
+        )
+        return dict(keys=keys, min=ms[:, :3], size=ms[:, 3:], eoff=eoff, eids=eids[: int(eoff[-1])], child_count=cc)
+
+    # ------------------------------------------------------------------ queries
+    def _query(self, name, args, mem, stream, raw):
+        out = _vp()
+        fn = getattr(library(), name)
+        _check(fn(self.h, *args, C.byref(out), mem, _stream_ptr(stream)))
+        r = Result(out)
+        return r if raw else r.to_host(stream)
+
+    def range_search(self, ranges, mode=RANGE_INSIDE, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        p, mem, keep = _arg(ranges, self.dtype)
+        return self._query("otg_range_search", [p, int(ranges.shape[0]), mode, tol, algo], mem, stream, raw)
+
+    def pick_search(self, points, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        p, mem, keep = _arg(points, self.dtype)
+        return self._query("otg_pick_search", [p, int(points.shape[0]), tol, algo], mem, stream, raw)
+
+    def knn(self, points, k, max_distance=-1.0, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        p, mem, keep = _arg(points, self.dtype)
+        nq = int(points.shape[0])
+        kp, kall, kkeep = None, 0, None
+        if np.isscalar(k):
+            kall = int(k)
+        else:
+            if _is_torch(k):
+                import torch
+
+                kkeep = k.to(torch.int32).contiguous()
+                kp = C.c_void_p(kkeep.data_ptr())
+            else:
+                kkeep = np.ascontiguousarray(k, dtype=np.uint32)
+                kp = kkeep.ctypes.data_as(_vp)
+        return self._query("otg_knn", [p, nq, kp, kall, max_distance, tol, algo], mem, stream, raw)
+
+    def frustum_culling(self, planes, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        """planes: (n_queries, planes_per_query, 4) as {origo distance, nx, ny, nz}."""
+        p, mem, keep = _arg(planes, self.dtype)
+        return self._query("otg_frustum_culling", [p, int(planes.shape[1]), int(planes.shape[0]), tol, algo], mem, stream, raw)
+
+    def ray_all(self, rays, tol=-1.0, tol_increment=0.0, max_distance=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        p, mem, keep = _arg(rays, self.dtype)
+        return self._query("otg_ray_all", [p, int(rays.shape[0]), tol, tol_increment, max_distance, algo], mem, stream, raw)
+
+    def ray_first(self, rays, tol=-1.0, tol_increment=0.0, max_distance=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        p, mem, keep = _arg(rays, self.dtype)
+        return self._query("otg_ray_first", [p, int(rays.shape[0]), tol, tol_increment, max_distance, algo], mem, stream, raw)
+
+    def collision_self(self, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        out = _vp()
+        _check(library().otg_collision_self(self.h, tol, algo, C.byref(out), _stream_ptr(stream)))
+        r = Result(out)
+        return r if raw else r.to_host(stream)[1].reshape(-1, 2)
+
+    def collision_pair(self, other, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        out = _vp()
+        _check(library().otg_collision_pair(self.h, other.h, tol, algo, C.byref(out), _stream_ptr(stream)))
+        r = Result(out)
+        return r if raw else r.to_host(stream)[1].reshape(-1, 2)

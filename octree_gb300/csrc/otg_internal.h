@@ -1,0 +1,134 @@
+// otg_internal.h — host-side state of a GPU tree and of a query result.
+//
+// HBM layout of a tree with N entities and M nodes (T = double or float):
+//   entities     T[N*W]     the caller's entities in input order (W = 3 points, 6 boxes)
+//   sortedIds    u32[N]     entity ids in tree (Morton key) order — node entity lists are
+//                           contiguous runs of this array, and every subtree is one run
+//   sortedGeom   T[N*W]     entities in tree order, so a node's entities are one coalesced read
+//   sortedKeys   K[N]       location keys in tree order (K = u32 when they fit in 32 bits)
+//   nodeLink     uint4[M]   {firstChild | childCount << 28, ownBegin, ownEnd, subtreeEnd}
+//   nodeKey      u64[M]     node key with sentinel bit
+//   nodeBox      T[M*6]     {min xyz, size xyz} exactly as GetNodeMinPoint / GetNodeSize
+//   nodeMax      T[M*3]     exact max corner of box-tree MBRs (for conservative pruning)
+//   nodeDepth    u8[M]
+// Nodes are stored breadth-first; the children of a node are contiguous.
+#pragma once
+
+#include "../../include/octree_gb300.h"
+#include "otg_device.cuh"
+
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+namespace otg
+{
+
+struct DevBuf
+{
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t need)
+  {
+    if (need <= bytes)
+      return cudaSuccess;
+    if (p)
+      cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, need ? need : 16);
+    if (e == cudaSuccess)
+      bytes = need ? need : 16;
+    return e;
+  }
+  void release()
+  {
+    if (p)
+      cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template<typename X>
+  X* as() const
+  {
+    return reinterpret_cast<X*>(p);
+  }
+};
+
+constexpr u32 kChildShift = 28;
+constexpr u32 kFirstChildMask = (1u << kChildShift) - 1;
+
+struct TreeState
+{
+  int scalar = OTG_SCALAR_F64;
+  int kind = OTG_KIND_POINTS;
+  u64 n = 0;
+  u32 D = 0;
+  u64 maxElem = 16;
+  bool keys32 = false;
+  bool built = false;
+  bool boxGiven = false;
+  u64 maxNodes = 0;
+
+  DevBuf entities, sortedIds, sortedGeom, keysA, keysB, valsB;
+  DevBuf nodeLink, nodeKey, nodeBox, nodeMax, nodeDepth;
+  DevBuf levelCount; // u32[32]: nodes per depth
+  DevBuf space;      // Space<T>
+  DevBuf sortScratch;
+  DevBuf err;        // u32 device error bits
+  DevBuf bboxBits;   // ordered-bit min/max accumulators
+  DevBuf locations;  // u64 per entity (input order), filled on export request
+  DevBuf boxDev;     // the given space box (6 scalars)
+
+  // cached after the build (host copies, filled by sync)
+  u64 nodeCount = 0;
+  bool countsKnown = false;
+  std::vector<u32> levelCountsHost;
+
+  const void* sortedKeys = nullptr; // final sorted keys (keysA or keysB)
+};
+
+struct ResultState
+{
+  u64 nq = 0;
+  u64 nids = 0;
+  bool hasDist = false;
+  DevBuf offsets; // u64[nq+1]
+  DevBuf ids;     // u32[nids]
+  DevBuf dist;    // double[nids]
+  u64 filterTests = 0;
+  u64 rechecks = 0;
+};
+
+void set_error(const std::string& msg);
+
+// build-phase instrumentation (otg_capi.cu): mark() records an event on the stream when enabled
+struct Profiler
+{
+  bool enabled = false;
+  std::vector<std::string> names;
+  std::vector<cudaEvent_t> events;
+  void reset();
+  void mark(const char* name, cudaStream_t st);
+};
+Profiler& profiler();
+int cuda_status(cudaError_t e, const char* what);
+
+// build entry (otg_build.cu)
+int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const void* box, u64 maxElem, int mem, cudaStream_t st);
+int finish_build(TreeState& t, cudaStream_t st);
+int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st);
+int export_nodes(const TreeState& t, u64* keys, double* minSize, u64* eoff, u32* eids, u32* childCount);
+
+// queries (otg_query.cu)
+int query_range(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st);
+int query_pick(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st);
+int query_knn(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAll, double maxDist, double tol, int algo, ResultState& r, int mem,
+              cudaStream_t st);
+int query_frustum(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st);
+int query_ray(const TreeState& t, const void* rays, u64 nq, double tol, double tolInc, double maxDist, bool first, int algo, ResultState& r,
+              int mem, cudaStream_t st);
+int query_collide_self(const TreeState& t, double tol, int algo, ResultState& r, cudaStream_t st);
+int query_collide_pair(const TreeState& a, const TreeState& b, double tol, int algo, ResultState& r, cudaStream_t st);
+
+} // namespace otg

@@ -1,0 +1,1258 @@
+// otg_query.cu — data-parallel queries over a GPU tree.
+//
+// Plain kernels: one query per thread, FP64 (or the tree's scalar) arithmetic in the reference's
+// operation order, explicit depth-first node stack. They prune with exactly the node tests of the
+// reference (same node boxes, same predicates), so the id sets equal the reference's:
+//   RangeSearch         core/ot_query.h:476-583
+//   PickSearch          core/ot_query.h:425-466
+//   FrustumCulling      core/ot_query.h:767-833
+//   GetNearestNeighbors core/ot_query.h:1208-1270
+//   RayIntersectedAll   core/ot_query.h:1928-2022
+//   RayIntersectedFirst core/ot_query.h:2035-2146
+//   CollisionDetection  core/ot_query.h:1308-1497 (two trees), 1690-1914 (one tree)
+//
+// Results are appended as (query << 32 | id) items (plus a distance where the query has one),
+// then ordered with stable radix sorts into CSR form: ids ascending per query, or by
+// (distance, id) for kNN and rays, or (i, j) pairs ascending for collisions.
+#include "otg_internal.h"
+#include "otg_sort.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace otg
+{
+
+constexpr int kStack = 168; // > 7 * 19 + 1 entries: depth-first stack bound for maxDepth <= 19
+
+template<typename T>
+struct TreeView
+{
+  const uint4* link;
+  const T* nodeBox; // {min xyz, size xyz}
+  const T* nodeMax; // box trees: exact max corner
+  const u32* ids;   // sortedIds
+  const T* geom;    // sortedGeom
+  u32 n;
+  int isBox;
+  u32 nNodes;
+};
+
+struct Appender
+{
+  u64* items;      // (query << 32) | id
+  double* dist;    // optional
+  unsigned long long* count;
+  u64 capacity;
+  __device__ __forceinline__ void put(u32 q, u32 id, double d = 0.0)
+  {
+    u64 pos = atomicAdd(count, 1ull);
+    if (pos < capacity)
+    {
+      items[pos] = (u64(q) << 32) | id;
+      if (dist)
+        dist[pos] = d;
+    }
+  }
+  __device__ __forceinline__ u64 reserve(u64 len) { return atomicAdd(count, (unsigned long long)len); }
+};
+
+template<typename T>
+__device__ __forceinline__ void load_box(const T* p, T b[6])
+{
+#pragma unroll
+  for (int c = 0; c < 6; ++c)
+    b[c] = p[c];
+}
+
+// ---------------------------------------------------------------- RangeSearch (plain)
+template<typename T>
+__global__ void __launch_bounds__(128) range_plain_kernel(TreeView<T> tv, const T* __restrict__ ranges, u32 nq, int mode, T tol, Appender out,
+                                                          u32* err)
+{
+  using G = GeoD<T>;
+  const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq)
+    return;
+  T r[6];
+  load_box(ranges + u64(q) * 6, r);
+  // root shortcut (:488-511): the whole root box inside the range -> every entity id
+  {
+    T rb[6];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+    {
+      rb[c] = tv.nodeBox[c];
+      rb[3 + c] = tv.nodeBox[c] + tv.nodeBox[3 + c];
+    }
+    if (G::range_contains_box(r, rb, tol))
+    {
+      u64 pos = out.reserve(tv.n);
+      for (u32 i = 0; i < tv.n; ++i)
+        if (pos + i < out.capacity)
+          out.items[pos + i] = (u64(q) << 32) | i;
+      return;
+    }
+  }
+  // zero-volume range -> empty (:514-519)
+  T vol = T(1);
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    vol *= T(r[3 + c] - r[c]);
+  if (vol <= T(0))
+    return;
+  T rmin[3], rsize[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+  {
+    rmin[c] = r[c];
+    rsize[c] = T(r[3 + c] - r[c]);
+  }
+  u32 stack[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp++] = 0;
+  while (sp > 0)
+  {
+    const u32 node = stack[--sp];
+    const T* nb = tv.nodeBox + u64(node) * 6;
+    T nmin[3], nsize[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+    {
+      nmin[c] = nb[c];
+      nsize[c] = nb[3 + c];
+    }
+    if (!G::overlap_by_min_point(rmin, rsize, nmin, nsize, tol))
+      continue;
+    const uint4 L = tv.link[node];
+    if (L.z > tv.n || L.w > tv.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    if (G::range_contains_min_size(r, nmin, nsize, tol))
+    {
+      // whole subtree without entity tests (:549-567); the subtree is one run of sortedIds
+      const u32 len = L.w - L.y;
+      u64 pos = out.reserve(len);
+      for (u32 i = 0; i < len; ++i)
+        if (pos + i < out.capacity)
+          out.items[pos + i] = (u64(q) << 32) | tv.ids[L.y + i];
+      continue;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      bool ok;
+      if (!tv.isBox)
+        ok = G::box_contains_point(r, tv.geom + u64(e) * 3, tol);
+      else
+      {
+        T b[6];
+        load_box(tv.geom + u64(e) * 6, b);
+        ok = (mode == OTG_RANGE_OVERLAP) ? (G::box_relation(r, b, tol) == -1) : G::contains_box_no_tol(r, b);
+      }
+      if (ok)
+        out.put(q, tv.ids[e]);
+    }
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 c = 0; c < cc; ++c)
+      stack[sp++] = fc + c;
+  }
+}
+
+// ---------------------------------------------------------------- PickSearch (plain)
+template<typename T>
+__global__ void __launch_bounds__(128) pick_plain_kernel(TreeView<T> tv, const T* __restrict__ pts, u32 nq, T tol, Appender out, u32* err)
+{
+  using G = GeoD<T>;
+  const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq)
+    return;
+  T p[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    p[c] = pts[u64(q) * 3 + c];
+  {
+    T rb[6];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+    {
+      rb[c] = tv.nodeBox[c];
+      rb[3 + c] = tv.nodeBox[c] + tv.nodeBox[3 + c];
+    }
+    if (!G::box_contains_point(rb, p, tol)) // :430-431 (DoesBoxContainPointAD box form)
+      return;
+  }
+  u32 stack[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp++] = 0;
+  while (sp > 0)
+  {
+    const u32 node = stack[--sp];
+    const T* nb = tv.nodeBox + u64(node) * 6;
+    if (!G::node_contains_point(nb, nb + 3, p, tol))
+      continue;
+    const uint4 L = tv.link[node];
+    if (L.z > tv.n || L.w > tv.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      bool ok = tv.isBox ? G::box_contains_point(tv.geom + u64(e) * 6, p, tol) : G::points_equal(tv.geom + u64(e) * 3, p, tol);
+      if (ok)
+        out.put(q, tv.ids[e]);
+    }
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 c = 0; c < cc; ++c)
+      stack[sp++] = fc + c;
+  }
+}
+
+// ---------------------------------------------------------------- FrustumCulling (plain)
+template<typename T>
+__global__ void __launch_bounds__(128) frustum_plain_kernel(TreeView<T> tv, const T* __restrict__ planes, u32 np, u32 nq, T tol, Appender out,
+                                                            u32* err)
+{
+  using G = GeoD<T>;
+  const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq || np == 0)
+    return;
+  const T* pl = planes + u64(q) * np * 4;
+  u32 stack[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp++] = 0;
+  while (sp > 0)
+  {
+    const u32 node = stack[--sp];
+    const T* nb = tv.nodeBox + u64(node) * 6;
+    bool select = true;
+    for (u32 i = 0; i < np; ++i) // :779-795 first Hit selects, first Negative prunes
+    {
+      int rel = G::box_plane(nb, nb + 3, pl[4 * i], pl + 4 * i + 1, tol);
+      if (rel == 1)
+        break;
+      if (rel == 0)
+      {
+        select = false;
+        break;
+      }
+    }
+    if (!select)
+      continue;
+    const uint4 L = tv.link[node];
+    if (L.z > tv.n || L.w > tv.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      bool neg = false;
+      for (u32 i = 0; i < np && !neg; ++i)
+      {
+        int rel;
+        if (tv.isBox)
+        {
+          const T* b = tv.geom + u64(e) * 6;
+          T bsize[3] = { T(b[3] - b[0]), T(b[4] - b[1]), T(b[5] - b[2]) };
+          rel = G::box_plane(b, bsize, pl[4 * i], pl + 4 * i + 1, tol);
+        }
+        else
+          rel = G::point_plane(tv.geom + u64(e) * 3, pl[4 * i], pl + 4 * i + 1, tol);
+        neg = rel == 0;
+      }
+      if (!neg)
+        out.put(q, tv.ids[e]);
+    }
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 c = 0; c < cc; ++c)
+      stack[sp++] = fc + c;
+  }
+}
+
+// ---------------------------------------------------------------- kNN (plain)
+// ot_query.h:1033-1036 GetValueWithToleranceUpper
+template<typename T>
+__device__ __forceinline__ T upper_tol(T v, T tol)
+{
+  return fmax(tol, v * (T(1.0) + tol));
+}
+
+template<typename T>
+__device__ __forceinline__ T entity_distance(const TreeView<T>& tv, u32 e, const T* p, T tol)
+{
+  if (tv.isBox)
+  {
+    T mn, mm;
+    GeoD<T>::min_max_distance(p, tv.geom + u64(e) * 6, tol, mn, mm);
+    return mn;
+  }
+  return GeoD<T>::distance(p, tv.geom + u64(e) * 3);
+}
+
+constexpr int kKnnMaxK = 256;
+
+// Pass 1: the k-th smallest distance d_k (points) -> F = U(d_k), the reference's final
+// farthestEntityDistance. Box trees keep the reference's optimistic/pessimistic pair:
+// the pessimistic (minMax) k-th distance sets F, entities qualify by their min distance.
+template<typename T>
+__global__ void __launch_bounds__(128) knn_threshold_kernel(TreeView<T> tv, const T* __restrict__ pts, u32 nq, const u32* __restrict__ kArr, u32 kAll,
+                                                            T F0, T tol, T* __restrict__ Fout, u32* err)
+{
+  using G = GeoD<T>;
+  const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq)
+    return;
+  u32 k = kArr ? kArr[q] : kAll;
+  if (k > kKnnMaxK)
+  {
+    atomicOr(err, kErrCapacity);
+    k = kKnnMaxK;
+  }
+  T p[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    p[c] = pts[u64(q) * 3 + c];
+  T heap[kKnnMaxK]; // max-heap of the k smallest (pessimistic) distances
+  u32 hs = 0;
+  T F = F0;
+  u32 stack[kStack];
+  T sdist[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp] = 0;
+  sdist[sp++] = G::wall_distance(p, tv.nodeBox, tv.nodeBox + 3);
+  while (sp > 0 && k > 0)
+  {
+    --sp;
+    const u32 node = stack[sp];
+    if (sdist[sp] >= F)
+      continue;
+    const uint4 L = tv.link[node];
+    if (L.z > tv.n || L.w > tv.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      T dmin, dmm;
+      if (tv.isBox)
+        G::min_max_distance(p, tv.geom + u64(e) * 6, tol, dmin, dmm);
+      else
+        dmin = dmm = G::distance(p, tv.geom + u64(e) * 3);
+      if (dmin >= F)
+        continue;
+      if (hs < k)
+      {
+        // sift up
+        u32 i = hs++;
+        while (i > 0)
+        {
+          u32 par = (i - 1) >> 1;
+          if (!(heap[par] < dmm))
+            break;
+          heap[i] = heap[par];
+          i = par;
+        }
+        heap[i] = dmm;
+        if (hs == k)
+          F = upper_tol(heap[0], tol); // :1123-1128 (heapify sets F unconditionally)
+      }
+      else if (dmm < heap[0])
+      {
+        // replace the max, sift down
+        u32 i = 0;
+        for (;;)
+        {
+          u32 l = 2 * i + 1, r = l + 1, m = i;
+          T vm = dmm;
+          if (l < hs && vm < heap[l])
+          {
+            m = l;
+            vm = heap[l];
+          }
+          if (r < hs && vm < heap[r])
+          {
+            m = r;
+            vm = heap[r];
+          }
+          if (m == i)
+            break;
+          heap[i] = heap[m];
+          i = m;
+        }
+        heap[i] = dmm;
+        T lim = upper_tol(heap[0], tol);
+        if (lim < F)
+          F = lim;
+      }
+    }
+    // children, nearest popped first
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      break;
+    }
+    const int base = sp;
+    for (u32 c = 0; c < cc; ++c)
+    {
+      const T* nb = tv.nodeBox + u64(fc + c) * 6;
+      T w = G::wall_distance(p, nb, nb + 3);
+      if (w >= F)
+        continue;
+      // insertion keeping [base, sp) sorted by descending distance
+      int j = sp++;
+      while (j > base && sdist[j - 1] < w)
+      {
+        sdist[j] = sdist[j - 1];
+        stack[j] = stack[j - 1];
+        --j;
+      }
+      sdist[j] = w;
+      stack[j] = fc + c;
+    }
+  }
+  Fout[q] = F;
+}
+
+// Pass 2: every entity with (min) distance < F, appended with its distance.
+template<typename T>
+__global__ void __launch_bounds__(128) knn_collect_kernel(TreeView<T> tv, const T* __restrict__ pts, u32 nq, const T* __restrict__ Fin, T tol, Appender out,
+                                                          u32* err)
+{
+  using G = GeoD<T>;
+  const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq)
+    return;
+  const T F = Fin[q];
+  T p[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    p[c] = pts[u64(q) * 3 + c];
+  u32 stack[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp++] = 0;
+  while (sp > 0)
+  {
+    const u32 node = stack[--sp];
+    const T* nb = tv.nodeBox + u64(node) * 6;
+    if (G::wall_distance(p, nb, nb + 3) >= F)
+      continue;
+    const uint4 L = tv.link[node];
+    if (L.z > tv.n || L.w > tv.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      T d = entity_distance(tv, e, p, tol);
+      if (d < F)
+        out.put(q, tv.ids[e], double(d));
+    }
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 c = 0; c < cc; ++c)
+      stack[sp++] = fc + c;
+  }
+}
+
+// ---------------------------------------------------------------- rays (plain)
+template<typename T>
+__device__ __forceinline__ bool entity_hit(const TreeView<T>& tv, const RayD<T>& ray, u32 e, T& en, T& ex)
+{
+  return tv.isBox ? ray.hit_box(tv.geom + u64(e) * 6, en, ex) : ray.hit_point(tv.geom + u64(e) * 3, en, ex);
+}
+
+// RayIntersectedAll: DFS over nodes hit by the ray; entities hit with enter <= maxDist (or maxDist == 0)
+template<typename T>
+__global__ void __launch_bounds__(128) ray_all_plain_kernel(TreeView<T> tv, const T* __restrict__ rays, u32 nq, T tol, T tolInc, T maxDist, Appender out,
+                                                            u32* err)
+{
+  const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq)
+    return;
+  RayD<T> ray;
+  ray.make(rays + u64(q) * 6, rays + u64(q) * 6 + 3, tol, tolInc);
+  if (!ray.valid)
+    return;
+  u32 stack[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp++] = 0;
+  while (sp > 0)
+  {
+    const u32 node = stack[--sp];
+    const T* nb = tv.nodeBox + u64(node) * 6;
+    T en, ex;
+    if (!ray.hit_node(nb, nb + 3, en, ex))
+      continue;
+    const uint4 L = tv.link[node];
+    if (L.z > tv.n || L.w > tv.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      if (!entity_hit(tv, ray, e, en, ex))
+        continue;
+      if (!(maxDist == T(0) || en <= maxDist))
+        continue;
+      out.put(q, tv.ids[e], double(en));
+    }
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 c = 0; c < cc; ++c)
+      stack[sp++] = fc + c;
+  }
+}
+
+// RayIntersectedFirst, pass 1: M = (1 + tolInc) * (smallest exit among hits with enter <= maxDist) + tol'
+// (ot_query.h:2093-2103), never above maxDist; pass 2 collects every hit with enter <= M.
+template<typename T>
+__global__ void __launch_bounds__(128) ray_first_threshold_kernel(TreeView<T> tv, const T* __restrict__ rays, u32 nq, T tol, T tolInc, T maxDist,
+                                                                  T* __restrict__ Mout, u32* err)
+{
+  const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq)
+    return;
+  RayD<T> ray;
+  ray.make(rays + u64(q) * 6, rays + u64(q) * 6 + 3, tol, tolInc);
+  T M = maxDist;
+  if (!ray.valid)
+  {
+    Mout[q] = -Lim<T>::max();
+    return;
+  }
+  const T applied = tol == T(0) ? Lim<T>::eps() : tol;
+  u32 stack[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp++] = 0;
+  while (sp > 0)
+  {
+    const u32 node = stack[--sp];
+    const T* nb = tv.nodeBox + u64(node) * 6;
+    T en, ex;
+    if (!ray.hit_node(nb, nb + 3, en, ex) || en > M)
+      continue;
+    const uint4 L = tv.link[node];
+    if (L.z > tv.n || L.w > tv.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      if (!entity_hit(tv, ray, e, en, ex))
+        continue;
+      if (en > M || ex >= M)
+        continue;
+      M = (T(1) + tolInc) * ex + applied;
+    }
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      break;
+    }
+    for (u32 c = 0; c < cc; ++c)
+      stack[sp++] = fc + c;
+  }
+  Mout[q] = M;
+}
+
+template<typename T>
+__global__ void __launch_bounds__(128) ray_first_collect_kernel(TreeView<T> tv, const T* __restrict__ rays, u32 nq, T tol, T tolInc, const T* __restrict__ Min,
+                                                                Appender out, u32* err)
+{
+  const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq)
+    return;
+  RayD<T> ray;
+  ray.make(rays + u64(q) * 6, rays + u64(q) * 6 + 3, tol, tolInc);
+  if (!ray.valid)
+    return;
+  const T M = Min[q];
+  u32 stack[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp++] = 0;
+  while (sp > 0)
+  {
+    const u32 node = stack[--sp];
+    const T* nb = tv.nodeBox + u64(node) * 6;
+    T en, ex;
+    if (!ray.hit_node(nb, nb + 3, en, ex) || en > M)
+      continue;
+    const uint4 L = tv.link[node];
+    if (L.z > tv.n || L.w > tv.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      if (!entity_hit(tv, ray, e, en, ex))
+        continue;
+      if (en > M)
+        continue;
+      out.put(q, tv.ids[e], double(en));
+    }
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 c = 0; c < cc; ++c)
+      stack[sp++] = fc + c;
+  }
+}
+
+// ---------------------------------------------------------------- collision (plain)
+// One thread per query box; tree B's node MBRs (exact min / max corners) prune conservatively
+// and every candidate pair is decided by GetBoxRelation == Overlapped (general.h:262-294), the
+// predicate of both reference paths. selfMode: only pairs with idB > idA are reported.
+template<typename T>
+__global__ void __launch_bounds__(128) collide_plain_kernel(TreeView<T> ta, TreeView<T> tb, T tol, int selfMode, Appender out, u32* err)
+{
+  using G = GeoD<T>;
+  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ta.n)
+    return;
+  T a[6];
+  load_box(ta.geom + u64(i) * 6, a);
+  const u32 idA = ta.ids[i];
+  u32 stack[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp++] = 0;
+  while (sp > 0)
+  {
+    const u32 node = stack[--sp];
+    const T* nmin = tb.nodeBox + u64(node) * 6;
+    const T* nmax = tb.nodeMax + u64(node) * 3;
+    bool disjoint = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      disjoint |= (a[3 + c] < nmin[c]) || (nmax[c] < a[c]);
+    if (disjoint)
+      continue;
+    const uint4 L = tb.link[node];
+    if (L.z > tb.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      const u32 idB = tb.ids[e];
+      if (selfMode && idB <= idA)
+        continue;
+      T b[6];
+      load_box(tb.geom + u64(e) * 6, b);
+      if (G::box_relation(a, b, tol) == -1)
+        out.put(idA, idB);
+    }
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tb.nNodes) || ++visits > tb.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 c = 0; c < cc; ++c)
+      stack[sp++] = fc + c;
+  }
+}
+
+// ---------------------------------------------------------------- result finishing
+__global__ void split_items_kernel(const u64* __restrict__ items, const u32* __restrict__ perm, u64 m, u32* __restrict__ qOut, u32* __restrict__ idOut)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+  {
+    u64 it = items[perm ? perm[i] : i];
+    if (qOut)
+      qOut[i] = u32(it >> 32);
+    idOut[i] = u32(it);
+  }
+}
+__global__ void gather_u64_kernel(const u64* __restrict__ src, const u32* __restrict__ perm, u64 m, u64* __restrict__ dst)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+    dst[i] = src[perm[i]];
+}
+__global__ void gather_dist_bits_kernel(const double* __restrict__ d, const u32* __restrict__ perm, u64 m, u64* __restrict__ dst)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+    dst[i] = u64(__double_as_longlong(d[perm[i]])); // distances are >= 0: bit order == value order
+}
+__global__ void gather_qid_kernel(const u64* __restrict__ items, const u32* __restrict__ perm, u64 m, u32* __restrict__ dst)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+    dst[i] = u32(items[perm[i]] >> 32);
+}
+__global__ void gather_final_kernel(const u64* __restrict__ items, const double* __restrict__ d, const u32* __restrict__ perm, u64 m,
+                                    u32* __restrict__ idOut, double* __restrict__ dOut)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+  {
+    u32 p = perm[i];
+    idOut[i] = u32(items[p]);
+    if (dOut)
+      dOut[i] = d[p];
+  }
+}
+// offsets[q] = first position whose query id >= q, from sorted query ids
+__global__ void offsets_kernel(const u32* __restrict__ qid, u64 m, u64 nq, u64* __restrict__ offsets)
+{
+  for (u64 q = blockIdx.x * u64(blockDim.x) + threadIdx.x; q <= nq; q += u64(gridDim.x) * blockDim.x)
+  {
+    u64 lo = 0, hi = m;
+    while (lo < hi)
+    {
+      u64 mid = (lo + hi) >> 1;
+      if (u64(qid[mid]) < q)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    offsets[q] = lo;
+  }
+}
+__global__ void iota_kernel(u32* v, u64 m)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+    v[i] = u32(i);
+}
+__global__ void item_ids_kernel(const u64* __restrict__ items, u64 m, u32* __restrict__ dst)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+    dst[i] = u32(items[i]);
+}
+
+static int blocks_for(u64 n, int per = 256)
+{
+  return int(std::max<u64>(1, std::min<u64>((n + per - 1) / per, 152 * 16)));
+}
+
+static u32 bit_count(u64 v)
+{
+  u32 b = 0;
+  while (v)
+  {
+    ++b;
+    v >>= 1;
+  }
+  return b;
+}
+
+// Stable radix sort of (u64 key, u32 value) with temporary buffers; result in (keys, vals).
+static int sort_pairs_u64(u64* keys, u32* vals, u64 m, u32 bits, cudaStream_t st, u32* err)
+{
+  if (m <= 1 || bits == 0)
+    return OTG_OK;
+  const u32 passes = (bits + kRadixBits - 1) / kRadixBits;
+  DevBuf k1, v1, scratch;
+  cudaError_t e;
+  if ((e = k1.ensure(sizeof(u64) * m)) || (e = v1.ensure(sizeof(u32) * m)) || (e = scratch.ensure(SortScratch::bytes(m, passes))))
+    return cuda_status(e, "allocating sort buffers");
+  cudaMemsetAsync(scratch.p, 0, SortScratch::bytes(m, passes), st);
+  SortScratch ss;
+  ss.carve(scratch.p, m, passes);
+  radix_histogram_kernel<u64><<<blocks_for(m), 256, 0, st>>>(keys, m, 0, passes, ss.hist);
+  bool inB = onesweep_passes<u64>(keys, vals, k1.as<u64>(), v1.as<u32>(), m, 0, passes, false, ss, err, st);
+  if (inB)
+  {
+    cudaMemcpyAsync(keys, k1.p, sizeof(u64) * m, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(vals, v1.p, sizeof(u32) * m, cudaMemcpyDeviceToDevice, st);
+  }
+  cudaStreamSynchronize(st);
+  k1.release();
+  v1.release();
+  scratch.release();
+  return cuda_status(cudaGetLastError(), "sorting results");
+}
+
+static int sort_pairs_u32(u32* keys, u32* vals, u64 m, u32 bits, cudaStream_t st, u32* err)
+{
+  if (m <= 1 || bits == 0)
+    return OTG_OK;
+  const u32 passes = (bits + kRadixBits - 1) / kRadixBits;
+  DevBuf k1, v1, scratch;
+  cudaError_t e;
+  if ((e = k1.ensure(sizeof(u32) * m)) || (e = v1.ensure(sizeof(u32) * m)) || (e = scratch.ensure(SortScratch::bytes(m, passes))))
+    return cuda_status(e, "allocating sort buffers");
+  cudaMemsetAsync(scratch.p, 0, SortScratch::bytes(m, passes), st);
+  SortScratch ss;
+  ss.carve(scratch.p, m, passes);
+  radix_histogram_kernel<u32><<<blocks_for(m), 256, 0, st>>>(keys, m, 0, passes, ss.hist);
+  bool inB = onesweep_passes<u32>(keys, vals, k1.as<u32>(), v1.as<u32>(), m, 0, passes, false, ss, err, st);
+  if (inB)
+  {
+    cudaMemcpyAsync(keys, k1.p, sizeof(u32) * m, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(vals, v1.p, sizeof(u32) * m, cudaMemcpyDeviceToDevice, st);
+  }
+  cudaStreamSynchronize(st);
+  k1.release();
+  v1.release();
+  scratch.release();
+  return cuda_status(cudaGetLastError(), "sorting results");
+}
+
+struct Collected
+{
+  DevBuf items, dist, count, err;
+  u64 m = 0;
+};
+
+static int check_err(const DevBuf& err, cudaStream_t st)
+{
+  u32 h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, err.p, sizeof(u32), cudaMemcpyDeviceToHost, st);
+  if (!e)
+    e = cudaStreamSynchronize(st);
+  if (e)
+    return cuda_status(e, "reading query status");
+  if (h & kErrStack)
+  {
+    set_error("traversal stack bound exceeded");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
+  if (h & kErrTimeout)
+  {
+    set_error("a bounded device wait ran out");
+    return OTG_ERR_TIMEOUT;
+  }
+  if (h & kErrCapacity)
+  {
+    set_error("k above the supported maximum of 256");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
+  return OTG_OK;
+}
+
+// Runs launch(appender) until the append buffer was large enough; items end in c.items.
+template<typename F>
+static int collect(Collected& c, bool withDist, u64 guess, F&& launch, cudaStream_t st)
+{
+  cudaError_t e;
+  if ((e = c.count.ensure(sizeof(unsigned long long))) || (e = c.err.ensure(sizeof(u32))))
+    return cuda_status(e, "allocating counters");
+  u64 cap = std::max<u64>(guess, 1024);
+  for (int attempt = 0; attempt < 3; ++attempt)
+  {
+    if ((e = c.items.ensure(sizeof(u64) * cap)) || (withDist && (e = c.dist.ensure(sizeof(double) * cap))))
+      return cuda_status(e, "allocating result buffer");
+    cudaMemsetAsync(c.count.p, 0, sizeof(unsigned long long), st);
+    cudaMemsetAsync(c.err.p, 0, sizeof(u32), st);
+    Appender a{ c.items.as<u64>(), withDist ? c.dist.as<double>() : nullptr, c.count.as<unsigned long long>(), cap };
+    launch(a, c.err.as<u32>());
+    if ((e = cudaGetLastError()))
+      return cuda_status(e, "launching query");
+    unsigned long long m = 0;
+    e = cudaMemcpyAsync(&m, c.count.p, sizeof(m), cudaMemcpyDeviceToHost, st);
+    if (!e)
+      e = cudaStreamSynchronize(st);
+    if (e)
+      return cuda_status(e, "running query");
+    if (int rc = check_err(c.err, st))
+      return rc;
+    if (m <= cap)
+    {
+      c.m = m;
+      return OTG_OK;
+    }
+    cap = m + m / 8 + 1024;
+  }
+  set_error("result buffer sizing did not converge");
+  return OTG_ERR_OUT_OF_MEMORY;
+}
+
+// CSR result with ids ascending per query
+static int finish_sorted_ids(Collected& c, u64 nq, ResultState& r, cudaStream_t st)
+{
+  const u64 m = c.m;
+  r.nq = nq;
+  r.nids = m;
+  r.hasDist = false;
+  cudaError_t e;
+  if ((e = r.offsets.ensure(sizeof(u64) * (nq + 1))) || (e = r.ids.ensure(sizeof(u32) * std::max<u64>(m, 1))))
+    return cuda_status(e, "allocating result");
+  if (m == 0)
+    return cuda_status(cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * (nq + 1), st), "result offsets");
+  DevBuf vals, qid;
+  if ((e = vals.ensure(sizeof(u32) * m)) || (e = qid.ensure(sizeof(u32) * m)))
+    return cuda_status(e, "allocating sort values");
+  if (int rc = sort_pairs_u64(c.items.as<u64>(), vals.as<u32>(), m, 32 + bit_count(nq), st, c.err.as<u32>()))
+    return rc;
+  split_items_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), nullptr, m, qid.as<u32>(), r.ids.as<u32>());
+  offsets_kernel<<<blocks_for(nq + 1), 256, 0, st>>>(qid.as<u32>(), m, nq, r.offsets.as<u64>());
+  e = cudaStreamSynchronize(st);
+  return cuda_status(e ? e : cudaGetLastError(), "finishing result");
+}
+
+// CSR result ordered by (query, distance, id): three stable radix sorts (id, distance, query)
+static int finish_by_distance(Collected& c, u64 nq, u64 nEntities, ResultState& r, cudaStream_t st)
+{
+  const u64 m = c.m;
+  r.nq = nq;
+  r.nids = m;
+  r.hasDist = true;
+  cudaError_t e;
+  if ((e = r.offsets.ensure(sizeof(u64) * (nq + 1))) || (e = r.ids.ensure(sizeof(u32) * std::max<u64>(m, 1))) ||
+      (e = r.dist.ensure(sizeof(double) * std::max<u64>(m, 1))))
+    return cuda_status(e, "allocating result");
+  if (m == 0)
+    return cuda_status(cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * (nq + 1), st), "result offsets");
+  DevBuf perm, k32, k64;
+  if ((e = perm.ensure(sizeof(u32) * m)) || (e = k32.ensure(sizeof(u32) * m)) || (e = k64.ensure(sizeof(u64) * m)))
+    return cuda_status(e, "allocating sort buffers");
+  u32* err = c.err.as<u32>();
+  iota_kernel<<<blocks_for(m), 256, 0, st>>>(perm.as<u32>(), m);
+  item_ids_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), m, k32.as<u32>());
+  if (int rc = sort_pairs_u32(k32.as<u32>(), perm.as<u32>(), m, bit_count(nEntities), st, err))
+    return rc;
+  gather_dist_bits_kernel<<<blocks_for(m), 256, 0, st>>>(c.dist.as<double>(), perm.as<u32>(), m, k64.as<u64>());
+  if (int rc = sort_pairs_u64(k64.as<u64>(), perm.as<u32>(), m, 64, st, err))
+    return rc;
+  gather_qid_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), perm.as<u32>(), m, k32.as<u32>());
+  if (int rc = sort_pairs_u32(k32.as<u32>(), perm.as<u32>(), m, bit_count(nq), st, err))
+    return rc;
+  gather_final_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), c.dist.as<double>(), perm.as<u32>(), m, r.ids.as<u32>(), r.dist.as<double>());
+  offsets_kernel<<<blocks_for(nq + 1), 256, 0, st>>>(k32.as<u32>(), m, nq, r.offsets.as<u64>());
+  e = cudaStreamSynchronize(st);
+  return cuda_status(e ? e : cudaGetLastError(), "finishing result");
+}
+
+// pairs (a << 32 | b) ascending: one "query" holding 2*m ids
+static int finish_pairs(Collected& c, ResultState& r, cudaStream_t st)
+{
+  const u64 m = c.m;
+  r.nq = 1;
+  r.nids = 2 * m;
+  r.hasDist = false;
+  cudaError_t e;
+  if ((e = r.offsets.ensure(sizeof(u64) * 2)) || (e = r.ids.ensure(sizeof(u32) * std::max<u64>(2 * m, 1))))
+    return cuda_status(e, "allocating result");
+  u64 offs[2] = { 0, 2 * m };
+  if ((e = cudaMemcpyAsync(r.offsets.p, offs, sizeof(offs), cudaMemcpyHostToDevice, st)))
+    return cuda_status(e, "result offsets");
+  if (m)
+  {
+    DevBuf vals;
+    if ((e = vals.ensure(sizeof(u32) * m)))
+      return cuda_status(e, "allocating sort values");
+    if (int rc = sort_pairs_u64(c.items.as<u64>(), vals.as<u32>(), m, 64, st, c.err.as<u32>()))
+      return rc;
+    // (a << 32 | b) in little-endian memory is {b, a}: swap into {a, b}
+    e = cudaMemcpyAsync(r.ids.p, c.items.p, sizeof(u64) * m, cudaMemcpyDeviceToDevice, st);
+  }
+  if (!e)
+    e = cudaStreamSynchronize(st);
+  return cuda_status(e, "finishing pairs");
+}
+
+__global__ void swap_pair_halves_kernel(u32* ids, u64 m)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+  {
+    u32 lo = ids[2 * i], hi = ids[2 * i + 1];
+    ids[2 * i] = hi;
+    ids[2 * i + 1] = lo;
+  }
+}
+
+// ---------------------------------------------------------------- host entry points
+template<typename T>
+static TreeView<T> view(const TreeState& t)
+{
+  return TreeView<T>{ t.nodeLink.as<uint4>(), t.nodeBox.as<T>(), t.nodeMax.as<T>(), t.sortedIds.as<u32>(), t.sortedGeom.as<T>(), u32(t.n),
+                      t.kind == OTG_KIND_BOXES ? 1 : 0, u32(t.nodeCount) };
+}
+
+template<typename T>
+static T upper_tol_host(T v, T tol)
+{
+  return std::fmax(tol, v * (T(1.0) + tol));
+}
+
+template<typename T>
+static T tol_of(double tol)
+{
+  return tol < 0 ? base_tol<T>() : T(tol);
+}
+
+// stage a caller array in device memory
+static int stage_input(DevBuf& buf, const void* src, size_t bytes, int mem, cudaStream_t st, const void*& dptr)
+{
+  if (mem == OTG_MEM_DEVICE)
+  {
+    dptr = src;
+    return OTG_OK;
+  }
+  if (cudaError_t e = buf.ensure(bytes))
+    return cuda_status(e, "allocating query input");
+  if (bytes)
+    if (cudaError_t e = cudaMemcpyAsync(buf.p, src, bytes, cudaMemcpyHostToDevice, st))
+      return cuda_status(e, "copying query input");
+  dptr = buf.p;
+  return OTG_OK;
+}
+
+static int empty_result(u64 nq, ResultState& r, bool dist, cudaStream_t st)
+{
+  r.nq = nq;
+  r.nids = 0;
+  r.hasDist = dist;
+  if (cudaError_t e = r.offsets.ensure(sizeof(u64) * (nq + 1)))
+    return cuda_status(e, "allocating result");
+  r.ids.ensure(4);
+  if (dist)
+    r.dist.ensure(8);
+  cudaError_t e = cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * (nq + 1), st);
+  if (!e)
+    e = cudaStreamSynchronize(st);
+  return cuda_status(e, "empty result");
+}
+
+template<typename T>
+static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+{
+  DevBuf in;
+  const void* d;
+  if (int rc = stage_input(in, ranges, sizeof(T) * 6 * nq, mem, st, d))
+    return rc;
+  if (t.n == 0 || nq == 0)
+    return empty_result(nq, r, false, st);
+  Collected c;
+  auto tv = view<T>(t);
+  T tl = tol_of<T>(tol);
+  int rc = collect(
+    c, false, nq * 32,
+    [&](Appender a, u32* err) {
+      range_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), mode, tl, a, err);
+    },
+    st);
+  if (rc)
+    return rc;
+  return finish_sorted_ids(c, nq, r, st);
+}
+
+template<typename T>
+static int pick_impl(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+{
+  DevBuf in;
+  const void* d;
+  if (int rc = stage_input(in, pts, sizeof(T) * 3 * nq, mem, st, d))
+    return rc;
+  if (t.n == 0 || nq == 0)
+    return empty_result(nq, r, false, st);
+  Collected c;
+  auto tv = view<T>(t);
+  T tl = tol_of<T>(tol);
+  int rc = collect(
+    c, false, nq * 8,
+    [&](Appender a, u32* err) { pick_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, a, err); }, st);
+  if (rc)
+    return rc;
+  return finish_sorted_ids(c, nq, r, st);
+}
+
+template<typename T>
+static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+{
+  DevBuf in;
+  const void* d;
+  if (int rc = stage_input(in, planes, sizeof(T) * 4 * np * nq, mem, st, d))
+    return rc;
+  if (t.n == 0 || nq == 0 || np == 0)
+    return empty_result(nq, r, false, st);
+  Collected c;
+  auto tv = view<T>(t);
+  T tl = tol_of<T>(tol);
+  int rc = collect(
+    c, false, std::max<u64>(nq * 64, t.n / 4),
+    [&](Appender a, u32* err) {
+      frustum_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(np), u32(nq), tl, a, err);
+    },
+    st);
+  if (rc)
+    return rc;
+  return finish_sorted_ids(c, nq, r, st);
+}
+
+template<typename T>
+static int knn_impl(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAll, double maxDist, double tol, int algo, ResultState& r, int mem,
+                    cudaStream_t st)
+{
+  DevBuf in, kin, F;
+  const void* d;
+  const void* dk = nullptr;
+  if (int rc = stage_input(in, pts, sizeof(T) * 3 * nq, mem, st, d))
+    return rc;
+  if (k)
+    if (int rc = stage_input(kin, k, sizeof(u32) * nq, mem, st, dk))
+      return rc;
+  if (t.n == 0 || nq == 0)
+    return empty_result(nq, r, true, st);
+  if (cudaError_t e = F.ensure(sizeof(T) * nq))
+    return cuda_status(e, "allocating kNN thresholds");
+  auto tv = view<T>(t);
+  T tl = tol_of<T>(tol);
+  T F0 = maxDist < 0 ? Lim<T>::max() : upper_tol_host(T(maxDist), tl);
+  Collected c;
+  int rc = collect(
+    c, true, nq * 16,
+    [&](Appender a, u32* err) {
+      knn_threshold_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), (const u32*)dk, kAll, F0, tl, F.as<T>(), err);
+      knn_collect_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), F.as<T>(), tl, a, err);
+    },
+    st);
+  if (rc)
+    return rc;
+  return finish_by_distance(c, nq, t.n, r, st);
+}
+
+template<typename T>
+static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, double tolInc, double maxDist, bool first, int algo, ResultState& r,
+                    int mem, cudaStream_t st)
+{
+  DevBuf in, M;
+  const void* d;
+  if (int rc = stage_input(in, rays, sizeof(T) * 6 * nq, mem, st, d))
+    return rc;
+  if (t.n == 0 || nq == 0)
+    return empty_result(nq, r, true, st);
+  auto tv = view<T>(t);
+  T tl = tol_of<T>(tol);
+  T ti = T(tolInc);
+  T md = maxDist < 0 ? Lim<T>::max() : T(maxDist);
+  Collected c;
+  int rc;
+  if (!first)
+  {
+    rc = collect(
+      c, true, nq * 16,
+      [&](Appender a, u32* err) {
+        ray_all_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, ti, md, a, err);
+      },
+      st);
+  }
+  else
+  {
+    if (cudaError_t e = M.ensure(sizeof(T) * nq))
+      return cuda_status(e, "allocating ray thresholds");
+    rc = collect(
+      c, true, nq * 4,
+      [&](Appender a, u32* err) {
+        ray_first_threshold_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, ti, md, M.as<T>(), err);
+        ray_first_collect_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, ti, M.as<T>(), a, err);
+      },
+      st);
+  }
+  if (rc)
+    return rc;
+  return finish_by_distance(c, nq, t.n, r, st);
+}
+
+template<typename T>
+static int collide_impl(const TreeState& a, const TreeState& b, bool self, double tol, int algo, ResultState& r, cudaStream_t st)
+{
+  if (a.n == 0 || b.n == 0)
+  {
+    r.nq = 1;
+    r.nids = 0;
+    r.hasDist = false;
+    r.offsets.ensure(sizeof(u64) * 2);
+    r.ids.ensure(4);
+    return cuda_status(cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * 2, st), "empty result");
+  }
+  Collected c;
+  auto ta = view<T>(a), tb = view<T>(b);
+  T tl = tol_of<T>(tol);
+  int rc = collect(
+    c, false, a.n * 4,
+    [&](Appender ap, u32* err) {
+      collide_plain_kernel<T><<<u32((a.n + 127) / 128), 128, 0, st>>>(ta, tb, tl, self ? 1 : 0, ap, err);
+    },
+    st);
+  if (rc)
+    return rc;
+  rc = finish_pairs(c, r, st);
+  if (rc)
+    return rc;
+  if (c.m)
+    swap_pair_halves_kernel<<<blocks_for(c.m), 256, 0, st>>>(r.ids.as<u32>(), c.m);
+  return cuda_status(cudaStreamSynchronize(st), "finishing pairs");
+}
+
+int query_range(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+{
+  return t.scalar == OTG_SCALAR_F64 ? range_impl<double>(t, ranges, nq, mode, tol, algo, r, mem, st)
+                                    : range_impl<float>(t, ranges, nq, mode, tol, algo, r, mem, st);
+}
+int query_pick(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+{
+  return t.scalar == OTG_SCALAR_F64 ? pick_impl<double>(t, pts, nq, tol, algo, r, mem, st) : pick_impl<float>(t, pts, nq, tol, algo, r, mem, st);
+}
+int query_knn(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAll, double maxDist, double tol, int algo, ResultState& r, int mem,
+              cudaStream_t st)
+{
+  return t.scalar == OTG_SCALAR_F64 ? knn_impl<double>(t, pts, nq, k, kAll, maxDist, tol, algo, r, mem, st)
+                                    : knn_impl<float>(t, pts, nq, k, kAll, maxDist, tol, algo, r, mem, st);
+}
+int query_frustum(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+{
+  return t.scalar == OTG_SCALAR_F64 ? frustum_impl<double>(t, planes, np, nq, tol, algo, r, mem, st)
+                                    : frustum_impl<float>(t, planes, np, nq, tol, algo, r, mem, st);
+}
+int query_ray(const TreeState& t, const void* rays, u64 nq, double tol, double tolInc, double maxDist, bool first, int algo, ResultState& r, int mem,
+              cudaStream_t st)
+{
+  return t.scalar == OTG_SCALAR_F64 ? ray_impl<double>(t, rays, nq, tol, tolInc, maxDist, first, algo, r, mem, st)
+                                    : ray_impl<float>(t, rays, nq, tol, tolInc, maxDist, first, algo, r, mem, st);
+}
+int query_collide_self(const TreeState& t, double tol, int algo, ResultState& r, cudaStream_t st)
+{
+  return t.scalar == OTG_SCALAR_F64 ? collide_impl<double>(t, t, true, tol, algo, r, st) : collide_impl<float>(t, t, true, tol, algo, r, st);
+}
+int query_collide_pair(const TreeState& a, const TreeState& b, double tol, int algo, ResultState& r, cudaStream_t st)
+{
+  return a.scalar == OTG_SCALAR_F64 ? collide_impl<double>(a, b, false, tol, algo, r, st) : collide_impl<float>(a, b, false, tol, algo, r, st);
+}
+
+} // namespace otg

@@ -1,0 +1,281 @@
+// otg_sort.cuh — single-pass-per-digit ("onesweep") LSD radix sort of (key, u32 value) pairs.
+//
+// Sorting replaces the reference's std::sort(par) over (Location, EntityID) in Create
+// (core/ot_dynamic_hash_core.h:791-796); the result is the same key order (the reference's
+// sort is unstable, this one is stable, so equal keys keep ascending entity id).
+//
+// Per pass, every CTA takes the next tile id from a counter (so tiles start in launch order),
+// ranks its 4096 keys by digit with warp match-any, publishes its per-digit counts and looks back
+// over earlier tiles' published counts (decoupled look-back) to get its global offsets, stages the
+// tile in shared memory in digit order and writes it out in runs. Look-back spins are bounded:
+// on timeout the CTA sets an error bit and finishes, so a broken invariant can never hang the GPU.
+#pragma once
+
+#include "otg_device.cuh"
+
+namespace otg
+{
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems; // 4096
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr u32 kStatusAggregate = 1u << 30;
+constexpr u32 kStatusInclusive = 2u << 30;
+constexpr u32 kStatusValueMask = (1u << 30) - 1;
+constexpr u32 kLookbackSpinLimit = 1u << 22;
+
+// error bits reported by device code
+constexpr u32 kErrTimeout = 1u;
+constexpr u32 kErrCapacity = 2u;
+constexpr u32 kErrStack = 4u;
+
+__device__ __forceinline__ u32 lanemask_lt()
+{
+  u32 m;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// exclusive scan of one value per thread over a 256-thread block; returns the block total
+__device__ __forceinline__ u32 block_exclusive_scan_256(u32 v, u32* s_warp, u32& total)
+{
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  u32 x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    u32 y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o)
+      x += y;
+  }
+  if (lane == 31)
+    s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0)
+  {
+    u32 w = lane < kSortWarps ? s_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      u32 y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o)
+        w += y;
+    }
+    if (lane < kSortWarps)
+      s_warp[lane] = w; // inclusive warp totals
+  }
+  __syncthreads();
+  u32 warpPrefix = warp ? s_warp[warp - 1] : 0;
+  total = s_warp[kSortWarps - 1];
+  u32 r = warpPrefix + x - v;
+  __syncthreads();
+  return r;
+}
+
+// All-pass digit histograms of `keys` (shift0 + 8p for p < passes) accumulated into hist[p][256].
+template<typename K>
+__global__ void __launch_bounds__(256) radix_histogram_kernel(const K* __restrict__ keys, u64 n, u32 shift0, u32 passes, u32* __restrict__ hist)
+{
+  __shared__ u32 sh[8][kRadix];
+  for (int i = threadIdx.x; i < 8 * kRadix; i += blockDim.x)
+    (&sh[0][0])[i] = 0;
+  __syncthreads();
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < n; i += u64(gridDim.x) * blockDim.x)
+  {
+    K k = keys[i];
+    for (u32 p = 0; p < passes; ++p)
+      atomicAdd(&sh[p][(k >> (shift0 + kRadixBits * p)) & (kRadix - 1)], 1u);
+  }
+  __syncthreads();
+  for (u32 p = 0; p < passes; ++p)
+    for (int d = threadIdx.x; d < kRadix; d += blockDim.x)
+      if (sh[p][d])
+        atomicAdd(&hist[p * kRadix + d], sh[p][d]);
+}
+
+// One onesweep pass. vin == nullptr means values are the input positions (iota).
+template<typename K>
+__global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(const K* __restrict__ kin, const u32* __restrict__ vin, K* __restrict__ kout,
+                                                                     u32* __restrict__ vout, u32 n, u32 shift, const u32* __restrict__ hist,
+                                                                     u32* __restrict__ status, u32* __restrict__ tileCounter, u32* __restrict__ err)
+{
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  K* s_keys = reinterpret_cast<K*>(s_dyn);
+  u32* s_vals = reinterpret_cast<u32*>(s_dyn + sizeof(K) * kSortTile);
+  __shared__ u32 s_warpHist[kSortWarps][kRadix];
+  __shared__ u32 s_digitStart[kRadix];
+  __shared__ u32 s_globalBase[kRadix];
+  __shared__ u32 s_scan[kSortWarps];
+  __shared__ u32 s_tile;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0)
+    s_tile = atomicAdd(tileCounter, 1u);
+  for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads)
+    (&s_warpHist[0][0])[i] = 0;
+  __syncthreads();
+  const u32 tile = s_tile;
+  const u64 base = u64(tile) * kSortTile;
+
+  K keys[kSortItems];
+  u32 vals[kSortItems];
+  u32 rank[kSortItems];
+  u32 dig[kSortItems];
+  const u64 wbase = base + u64(warp) * (32 * kSortItems);
+#pragma unroll
+  for (int i = 0; i < kSortItems; ++i)
+  {
+    u64 idx = wbase + i * 32 + lane;
+    bool valid = idx < n;
+    keys[i] = valid ? kin[idx] : K(0);
+    vals[i] = vin ? (valid ? vin[idx] : 0u) : u32(idx);
+    dig[i] = valid ? u32((keys[i] >> shift) & (kRadix - 1)) : u32(kRadix);
+  }
+  const u32 ltmask = lanemask_lt();
+#pragma unroll
+  for (int i = 0; i < kSortItems; ++i)
+  {
+    u32 d = dig[i];
+    u32 peers = __match_any_sync(0xffffffffu, d);
+    u32 cnt = 0;
+    if (d < kRadix)
+      cnt = s_warpHist[warp][d];
+    rank[i] = cnt + __popc(peers & ltmask);
+    __syncwarp();
+    if (d < kRadix && lane == __ffs(peers) - 1)
+      s_warpHist[warp][d] = cnt + __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // per digit (thread tid owns digit tid): warp offsets and the tile total
+  u32 total = 0;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w)
+  {
+    u32 c = s_warpHist[w][tid];
+    s_warpHist[w][tid] = total;
+    total += c;
+  }
+
+  // decoupled look-back over earlier tiles for digit tid
+  u32 prefix = 0;
+  volatile u32* vstatus = status;
+  if (tile == 0)
+  {
+    vstatus[tid] = kStatusInclusive | total;
+  }
+  else
+  {
+    vstatus[u64(tile) * kRadix + tid] = kStatusAggregate | total;
+    long long j = (long long)tile - 1;
+    u32 spins = 0;
+    while (j >= 0)
+    {
+      u32 s = vstatus[u64(j) * kRadix + tid];
+      u32 flag = s & ~kStatusValueMask;
+      if (flag == 0)
+      {
+        if (++spins > kLookbackSpinLimit)
+        {
+          atomicOr(err, kErrTimeout);
+          break;
+        }
+        __nanosleep(32);
+        continue;
+      }
+      prefix += s & kStatusValueMask;
+      if (flag == kStatusInclusive)
+        break;
+      --j;
+    }
+    vstatus[u64(tile) * kRadix + tid] = kStatusInclusive | ((prefix + total) & kStatusValueMask);
+  }
+
+  u32 tileTotal;
+  u32 digitStart = block_exclusive_scan_256(total, s_scan, tileTotal);
+  u32 hcount = hist[tid];
+  u32 hsum;
+  u32 histPrefix = block_exclusive_scan_256(hcount, s_scan, hsum);
+  s_digitStart[tid] = digitStart;
+  s_globalBase[tid] = histPrefix + prefix - digitStart;
+  __syncthreads();
+
+#pragma unroll
+  for (int i = 0; i < kSortItems; ++i)
+  {
+    u32 d = dig[i];
+    if (d < kRadix)
+    {
+      u32 pos = s_digitStart[d] + s_warpHist[warp][d] + rank[i];
+      s_keys[pos] = keys[i];
+      s_vals[pos] = vals[i];
+    }
+  }
+  __syncthreads();
+
+  const u32 tileCount = u32(min(u64(kSortTile), u64(n) - base));
+  for (u32 j = tid; j < tileCount; j += kSortThreads)
+  {
+    K k = s_keys[j];
+    u32 d = u32((k >> shift) & (kRadix - 1));
+    u32 pos = s_globalBase[d] + j;
+    if (pos < n)
+    {
+      kout[pos] = k;
+      vout[pos] = s_vals[j];
+    }
+    else
+      atomicOr(err, kErrTimeout);
+  }
+}
+
+// Scratch for a sort of up to n keys over `passes` digits.
+struct SortScratch
+{
+  u32* hist = nullptr;        // passes * 256
+  u32* status = nullptr;      // passes * tiles * 256
+  u32* tileCounters = nullptr; // passes
+  static size_t tiles(u64 n) { return size_t((n + kSortTile - 1) / kSortTile); }
+  static size_t bytes(u64 n, u32 passes) { return sizeof(u32) * (size_t(passes) * kRadix + size_t(passes) * tiles(n) * kRadix + passes + 8); }
+  void carve(void* p, u64 n, u32 passes)
+  {
+    u32* q = reinterpret_cast<u32*>(p);
+    hist = q;
+    q += size_t(passes) * kRadix;
+    status = q;
+    q += size_t(passes) * tiles(n) * kRadix;
+    tileCounters = q;
+  }
+};
+
+template<typename K>
+inline size_t onesweep_smem_bytes()
+{
+  return (sizeof(K) + sizeof(u32)) * kSortTile;
+}
+
+// Runs the passes of a sort whose histograms are already in scratch.hist (zeroed scratch otherwise).
+// Pass p reads buffer (p even ? 0 : 1) and writes the other one; returns true when the sorted
+// result is in (k1, v1). iotaValues: the first pass generates values 0..n-1 instead of reading v0.
+template<typename K>
+inline bool onesweep_passes(K* k0, u32* v0, K* k1, u32* v1, u64 n, u32 shift0, u32 passes, bool iotaValues, SortScratch& s, u32* err, cudaStream_t st)
+{
+  cudaFuncSetAttribute(onesweep_pass_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(onesweep_smem_bytes<K>()));
+  const u32 tiles = u32(SortScratch::tiles(n));
+  for (u32 p = 0; p < passes; ++p)
+  {
+    const bool even = (p % 2) == 0;
+    const K* ki = even ? k0 : k1;
+    const u32* vi = (p == 0 && iotaValues) ? nullptr : (even ? v0 : v1);
+    K* ko = even ? k1 : k0;
+    u32* vo = even ? v1 : v0;
+    onesweep_pass_kernel<K><<<tiles, kSortThreads, onesweep_smem_bytes<K>(), st>>>(ki, vi, ko, vo, u32(n), shift0 + kRadixBits * p, s.hist + p * kRadix,
+                                                                               s.status + size_t(p) * tiles * kRadix, s.tileCounters + p, err);
+  }
+  return (passes % 2) == 1;
+}
+
+} // namespace otg

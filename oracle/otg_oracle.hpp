@@ -1,0 +1,1432 @@
+// otg_oracle.hpp — CPU restatement of OrthoTree's Morton location-code tree (Create + queries).
+//
+// TEST INFRASTRUCTURE ONLY. This header is the checker for the GPU path: only tests/,
+// __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm may build or call it.
+// Nothing in octree_gb300/ includes or links it.
+//
+// It restates, in plain single-threaded C++, the algorithm of the reference library for the
+// paths the GPU build accelerates. Every function names the reference file:line it follows
+// (paths are relative to the OrthoTree project root). The restatement keeps the reference's
+// arithmetic order operation by operation, so it must be compiled with -ffp-contract=off
+// (aarch64 GCC contracts a*b+c into FMA by default, which changes results).
+//
+// Scope (3-D only, contiguous entity ids 0..N-1):
+//   * OctreePoint: loose factor 1.0, MinPoint node geometry (core/configuration.h:104-105).
+//   * OctreeBox:   loose factor 2.0, MBR node geometry      (core/configuration.h:107-108).
+//     Non-loose box trees (loose factor 1.0, MBR) are also restated.
+//   * Scalars: double (the library default) and float.
+#pragma once
+
+#include <algorithm>
+#include <array>
+#include <bit>
+#include <cmath>
+#include <cstdint>
+#include <functional>
+#include <limits>
+#include <numeric>
+#include <optional>
+#include <queue>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+namespace otg_oracle
+{
+using u32 = uint32_t;
+using u64 = uint64_t;
+
+// core/types.h:61-67
+constexpr u32 INVALID_DEPTH = 31;
+constexpr u32 INVALID_GRIDID = 0xFFFFFFFFu;
+
+enum class RangeMode : int { Inside = 0, Overlap = 1 };          // core/types.h:83-87
+enum class PlaneRel : int { Negative = 0, Hit = 1, Positive = 2 }; // core/types.h:91-96
+
+// adapters/general.h:57  BASE_TOLERANCE = epsilon * 100
+template<typename T>
+constexpr T base_tolerance() { return std::numeric_limits<T>::epsilon() * T(100); }
+
+// ---------------------------------------------------------------- Morton helpers
+// detail/si_morton.h:432-471 (Part1By2, 64-bit location) — spread 21 bits two apart.
+inline u64 part1by2(u32 g)
+{
+  u64 x = g;
+  x = (x ^ (x << 32)) & 0xffff00000000ffffULL;
+  x = (x ^ (x << 16)) & 0x00ff0000ff0000ffULL;
+  x = (x ^ (x << 8)) & 0xf00f00f00f00f00fULL;
+  x = (x ^ (x << 4)) & 0x30c30c30c30c30c3ULL;
+  x = (x ^ (x << 2)) & 0x9249249249249249ULL;
+  return x;
+}
+// detail/si_morton.h:519-535 (3-D Encode: x -> bit 0, y -> bit 1, z -> bit 2)
+inline u64 encode3(const u32 g[3]) { return (part1by2(g[2]) << 2) + (part1by2(g[1]) << 1) + part1by2(g[0]); }
+
+// detail/si_morton.h:257-263 (GetDepthID of a sentinel node key)
+inline u32 key_depth(u64 key) { return u32(std::bit_width(key) - 1) / 3; }
+
+// detail/si_morton.h:576-622 (Decode, non-BMI2 branch)
+inline std::array<u32, 3> decode_node(u64 key, u32 maxDepth)
+{
+  std::array<u32, 3> g{ 0, 0, 0 };
+  u32 depth = key_depth(key);
+  u32 shift = 0;
+  for (u32 lvl = maxDepth - depth; lvl < maxDepth; ++lvl)
+    for (u32 d = 0; d < 3; ++d, ++shift)
+      g[d] |= u32((key >> shift) & 1ULL) << lvl;
+  return g;
+}
+
+// detail/si_morton.h:117-143 compact location key (loc << 5) | depth, used for D <= 19 in 3-D
+inline u64 compact_key(u64 loc, u64 depth) { return (loc << 5) | depth; }
+inline u32 key_loc_depth(u64 k) { return u32(k & 31u); }
+inline u64 key_loc(u64 k) { return k >> 5; }
+
+// detail/utils.h:613-622 EstimateMaxDepth (3-D, MAX_THEORETICAL_DEPTH_ID = 21)
+inline u32 estimate_max_depth(size_t n, size_t maxElem)
+{
+  if (n <= maxElem)
+    return 2;
+  size_t nLeaf = n / maxElem;
+  return std::clamp(static_cast<u32>(std::log2(double(nLeaf)) / 3.0), u32(2), u32(21));
+}
+
+// ---------------------------------------------------------------- geometry predicates
+// All follow adapters/general.h and detail/internal_geometry_module.h line by line.
+template<typename T>
+struct Geo
+{
+  static bool is_less(T a, T b, T tol) { return a + tol < b; }                  // general.h:246
+  static bool almost_equal(T a, T b, T tol) { return std::abs(a - b) <= tol; }  // general.h:245
+
+  // general.h:262-289 GetBoxRelation: -1 overlapped, 0 adjacent, 1 separated
+  static int box_relation(const T* e1, const T* e2, T tol)
+  {
+    unsigned rel = 0;
+    for (int d = 0; d < 3; ++d)
+    {
+      T min1 = e1[d], max1 = e1[3 + d], min2 = e2[d], max2 = e2[3 + d];
+      if (is_less(min1, max2, tol) && is_less(min2, max1, tol))
+        rel |= 1u;
+      else if (almost_equal(min1, max2, tol) || almost_equal(max1, min2, tol))
+        rel |= 2u;
+      else if (is_less(max2, min1, tol) || is_less(max1, min2, tol))
+        return 1;
+    }
+    return (rel & 2u) ? 0 : -1;
+  }
+  static bool overlapped_strict(const T* e1, const T* e2, T tol) { return box_relation(e1, e2, tol) == -1; } // general.h:291-294
+
+  // general.h:296-310 AreBoxesOverlapped(e1, e2, true, ...) — containment, tolerance ignored
+  static bool contains_box_no_tol(const T* e1, const T* e2)
+  {
+    for (int d = 0; d < 3; ++d)
+    {
+      if (e1[d] > e2[d] || e2[d] > e1[3 + d])
+        return false;
+      if (e1[d] > e2[3 + d] || e2[3 + d] > e1[3 + d])
+        return false;
+    }
+    return true;
+  }
+
+  // general.h:225-243 DoesBoxContainPoint
+  static bool box_contains_point(const T* box, const T* p, T tol)
+  {
+    if (tol != T(0))
+    {
+      for (int d = 0; d < 3; ++d)
+        if (!(box[d] - tol < p[d] && p[d] < box[3 + d] + tol))
+          return false;
+    }
+    else
+    {
+      for (int d = 0; d < 3; ++d)
+        if (!(box[d] <= p[d] && p[d] <= box[3 + d]))
+          return false;
+    }
+    return true;
+  }
+
+  // general.h:135-146 Distance2 / Distance
+  static T distance2(const T* a, const T* b)
+  {
+    T d2 = T(0);
+    for (int d = 0; d < 3; ++d)
+    {
+      T v = a[d] - b[d];
+      d2 += v * v;
+    }
+    return d2;
+  }
+  static T distance(const T* a, const T* b) { return std::sqrt(distance2(a, b)); }
+
+  // general.h:218-221 ArePointsEqual
+  static bool points_equal(const T* a, const T* b, T tol) { return distance2(a, b) <= tol * tol; }
+
+  // general.h:159-216 MinMaxDistance (box entities in kNN)
+  static std::pair<T, T> min_max_distance(const T* pt, const T* box, T tol)
+  {
+    T dmin = T(0), dminMax = T(0);
+    T farthestInside2 = std::numeric_limits<T>::max();
+    T largestDiff = T(0);
+    bool isInside = true;
+    for (int d = 0; d < 3; ++d)
+    {
+      T v = pt[d], minC = box[d], maxC = box[3 + d];
+      T minDist = v - minC;
+      T maxDist = maxC - v;
+      bool inComp = (-tol <= minDist && -tol <= maxDist);
+      isInside &= inComp;
+      T minDist2 = minDist * minDist;
+      T maxDist2 = maxDist * maxDist;
+      if (maxDist2 < minDist2)
+        std::swap(minDist2, maxDist2);
+      if (isInside)
+        farthestInside2 = std::min(farthestInside2, maxDist2);
+      if (!inComp)
+        dmin += minDist2;
+      largestDiff = std::max(largestDiff, maxDist2 - minDist2);
+      dminMax += maxDist2;
+    }
+    if (isInside)
+    {
+      dmin = T(0);
+      dminMax = farthestInside2;
+    }
+    else
+      dminMax -= largestDiff;
+    return { std::sqrt(dmin), std::sqrt(dminMax) };
+  }
+
+  // general.h:322-335 GetPointPlaneRelation (plane = {origoDistance, n[3]})
+  static PlaneRel point_plane(const T* p, T dist, const T* n, T tol)
+  {
+    T proj = T{};
+    for (int d = 0; d < 3; ++d)
+      proj += n[d] * p[d];
+    if (proj < dist - tol)
+      return PlaneRel::Negative;
+    if (proj > dist + tol)
+      return PlaneRel::Positive;
+    return PlaneRel::Hit;
+  }
+
+  // internal_geometry_module.h:254-280 GetBoxPlaneRelationAD (radius accumulates in double)
+  static PlaneRel box_plane(const T* minPoint, const T* size, T dist, const T* n, T tol)
+  {
+    T center[3], half[3];
+    for (int d = 0; d < 3; ++d)
+    {
+      half[d] = size[d] * T(0.5);
+      center[d] = minPoint[d] + half[d];
+    }
+    double radius = double(tol);
+    for (int d = 0; d < 3; ++d)
+      radius += half[d] * std::abs(n[d]);
+    T dot = T{};
+    for (int d = 0; d < 3; ++d)
+      dot += n[d] * center[d];
+    T cproj = dot - dist;
+    if (cproj + radius < 0.0)
+      return PlaneRel::Negative;
+    if (cproj - radius > 0.0)
+      return PlaneRel::Positive;
+    return PlaneRel::Hit;
+  }
+
+  // internal_geometry_module.h:148-161 AreBoxesOverlappingByMinPoint
+  static bool overlap_by_min_point(const T* minL, const T* sizeL, const T* minR, const T* sizeR, T tol)
+  {
+    for (int d = 0; d < 3; ++d)
+    {
+      T maxL = minL[d] + sizeL[d];
+      T maxR = minR[d] + sizeR[d];
+      if (maxL <= minR[d] - tol || maxR <= minL[d] - tol)
+        return false;
+    }
+    return true;
+  }
+
+  // internal_geometry_module.h:190-199 DoesRangeContainBox (scalar form)
+  static bool range_contains(T rmin, T rmax, T bmin, T bmax, T tol)
+  {
+    if (rmin - tol > bmin || bmin > rmax + tol)
+      return false;
+    if (rmin - tol > bmax || bmax > rmax + tol)
+      return false;
+    return true;
+  }
+  // internal_geometry_module.h:201-237 DoesRangeContainBoxAD(range, box{min,max})
+  static bool range_contains_box(const T* range, const T* box, T tol)
+  {
+    for (int d = 0; d < 3; ++d)
+      if (!range_contains(range[d], range[3 + d], box[d], box[3 + d], tol))
+        return false;
+    return true;
+  }
+  // internal_geometry_module.h:239-252 DoesRangeContainBoxAD(range, minPoint, size)
+  static bool range_contains_min_size(const T* range, const T* minPoint, const T* size, T tol)
+  {
+    for (int d = 0; d < 3; ++d)
+    {
+      T bmax = minPoint[d] + size[d];
+      if (!range_contains(range[d], range[3 + d], minPoint[d], bmax, tol))
+        return false;
+    }
+    return true;
+  }
+  // internal_geometry_module.h:372-396 DoesBoxContainPointAD(box{min,max}, p)
+  static bool box_contains_point_ad(const T* box, const T* p, T tol) { return box_contains_point(box, p, tol); }
+  // internal_geometry_module.h:398-422 DoesBoxContainPointAD(minPoint, size, p) (centre / half form)
+  static bool node_contains_point(const T* minPoint, const T* size, const T* p, T tol)
+  {
+    for (int d = 0; d < 3; ++d)
+    {
+      T half = size[d] * T(0.5);
+      T dist = std::abs(p[d] - minPoint[d] - half);
+      if (tol != T(0))
+      {
+        if (dist >= half + tol)
+          return false;
+      }
+      else if (dist > half)
+        return false;
+    }
+    return true;
+  }
+  // internal_geometry_module.h:424-458 GetBoxWallDistanceAD(..., isInsideConsideredAsZero=true)
+  static T wall_distance(const T* p, const T* minPoint, const T* size)
+  {
+    T cd[3], half[3];
+    bool inside = true;
+    for (int d = 0; d < 3; ++d)
+    {
+      half[d] = size[d] * T(0.5);
+      cd[d] = std::abs(minPoint[d] + half[d] - p[d]);
+      inside &= cd[d] <= half[d];
+    }
+    if (inside)
+      return T{};
+    T d2 = T(0);
+    for (int d = 0; d < 3; ++d)
+    {
+      T v = std::max(T{}, cd[d] - half[d]);
+      d2 += v * v;
+    }
+    return std::sqrt(d2);
+  }
+};
+
+// internal_geometry_module.h:536-723 RayHitTester
+template<typename T>
+struct RayTester
+{
+  T origin[3], dir[3], inv[3];
+  T minTol, tolInc;
+  bool sign[3], zero[3];
+  bool hasNaN = false;
+
+  // internal_geometry_module.h:539-568
+  static std::optional<RayTester> make(const T* o, const T* nd, T minTolerance, T toleranceIncrement)
+  {
+    T s2 = T(0);
+    for (int d = 0; d < 3; ++d)
+      s2 += nd[d] * nd[d];
+    if (!(std::abs(s2 - 1.0) < 0.000001)) // general.h:223 IsNormalizedVector
+      return std::nullopt;
+    RayTester r{};
+    for (int d = 0; d < 3; ++d)
+      r.origin[d] = o[d];
+    r.minTol = minTolerance;
+    r.tolInc = toleranceIncrement;
+    for (int d = 0; d < 3; ++d)
+      r.dir[d] = nd[d];
+    for (int d = 0; d < 3; ++d)
+    {
+      T c = nd[d];
+      bool isNaN = std::fabs(c) < 2.0 * std::numeric_limits<T>::epsilon();
+      r.inv[d] = isNaN ? std::numeric_limits<T>::quiet_NaN() : (T(1) / c);
+      r.sign[d] = c < 0;
+      r.zero[d] = isNaN;
+      r.hasNaN |= isNaN;
+    }
+    return r;
+  }
+
+  // internal_geometry_module.h:631-712 BoxHitTest<true>
+  bool box_hit_test(const T* minDiff, const T* maxDiff, T& enterOut, T& exitOut) const
+  {
+    T enter = -std::numeric_limits<T>::max();
+    T exit = std::numeric_limits<T>::max();
+    T pd[2][3];
+    for (int d = 0; d < 3; ++d)
+      pd[0][d] = minDiff[d] * inv[d];
+    for (int d = 0; d < 3; ++d)
+      pd[1][d] = maxDiff[d] * inv[d];
+    if (hasNaN)
+    {
+      for (int d = 0; d < 3; ++d)
+        if (!zero[d])
+          enter = std::fmax(enter, pd[sign[d] ? 1 : 0][d]);
+      for (int d = 0; d < 3; ++d)
+        if (!zero[d])
+          exit = std::fmin(exit, pd[sign[d] ? 0 : 1][d]);
+    }
+    else
+    {
+      for (int d = 0; d < 3; ++d)
+        enter = std::max(enter, pd[sign[d] ? 1 : 0][d]);
+      for (int d = 0; d < 3; ++d)
+        exit = std::min(exit, pd[sign[d] ? 0 : 1][d]);
+    }
+    T exitTol = std::max(T(0), exit) * tolInc + minTol;
+    enter -= T(0.5) * (std::max(T(0), enter) * tolInc + minTol);
+    exit += T(0.5) * (std::max(T(0), exit) * tolInc + minTol);
+    if (enter >= exit || exit <= T(0))
+      return false;
+    enter = std::max(T(0), enter);
+    if (hasNaN)
+    {
+      for (int d = 0; d < 3; ++d)
+      {
+        if (!zero[d])
+          continue;
+        if (minDiff[d] > exitTol || maxDiff[d] < -exitTol)
+          return false;
+      }
+    }
+    enterOut = enter;
+    exitOut = exit;
+    return true;
+  }
+  // internal_geometry_module.h:576-585 Hit(minPoint, size)
+  bool hit_node(const T* minPoint, const T* size, T& en, T& ex) const
+  {
+    T a[3], b[3];
+    for (int d = 0; d < 3; ++d)
+      a[d] = minPoint[d] - origin[d];
+    for (int d = 0; d < 3; ++d)
+      b[d] = minPoint[d] + size[d] - origin[d];
+    return box_hit_test(a, b, en, ex);
+  }
+  // internal_geometry_module.h:587-597 Hit(box)
+  bool hit_box(const T* box, T& en, T& ex) const
+  {
+    T a[3], b[3];
+    for (int d = 0; d < 3; ++d)
+      a[d] = box[d] - origin[d];
+    for (int d = 0; d < 3; ++d)
+      b[d] = box[3 + d] - origin[d];
+    return box_hit_test(a, b, en, ex);
+  }
+  // internal_geometry_module.h:599-626 Hit(point)
+  bool hit_point(const T* p, T& en, T& ex) const
+  {
+    T v[3];
+    for (int d = 0; d < 3; ++d)
+      v[d] = p[d] - origin[d];
+    T t = T{};
+    for (int d = 0; d < 3; ++d)
+      t += v[d] * dir[d];
+    T len2 = T{};
+    for (int d = 0; d < 3; ++d)
+      len2 += v[d] * v[d];
+    T dist2 = std::max(T(0), len2 - t * t);
+    T tol = std::max(T(0), t) * tolInc + minTol;
+    if (dist2 <= (tol * tol) && t >= -tol)
+    {
+      en = std::max(T(0), t - tol);
+      ex = t + tol;
+      return true;
+    }
+    return false;
+  }
+};
+
+// ---------------------------------------------------------------- the tree
+template<typename T>
+class Tree
+{
+public:
+  using G = Geo<T>;
+  static constexpr T TOL = base_tolerance<T>();
+
+  struct Node
+  {
+    u64 key = 0;
+    std::vector<u64> children; // child node keys in child-id order (ot_dynamic_hash_core.h:190-215)
+    std::vector<u32> entities; // own entity ids in sorted-location order
+    T minPoint[3] = { 0, 0, 0 };
+    T size[3] = { 0, 0, 0 }; // MBR trees only; MinPoint trees take the per-depth table
+    u64 subtreeCount = 0;
+  };
+
+  bool isBox = false;
+  bool loose = false;
+  u32 D = 0;
+  size_t maxElem = 16;
+  size_t N = 0;
+  std::vector<T> geom; // N*3 (points) or N*6 (boxes: min xyz, max xyz)
+
+  // grid space (detail/si_grid.h:65-103)
+  T spaceMin[3]{}, spaceMax[3]{}, sizeT[3]{};
+  bool rasterDouble = true; // float trees with D >= 16 rasterise in double (si_grid.h:70-80)
+  double rsizeD[3]{}, rastD[3]{}, derastD[3]{};
+  float rsizeF[3]{}, rastF[3]{}, derastF[3]{};
+  u32 res = 0, maxRasterID = 0;
+
+  std::vector<std::array<T, 3>> nodeSize; // MinPoint per-depth sizes (core/ot_base.h:121-134)
+  std::unordered_map<u64, Node> nodes;
+  std::vector<u64> locationKeys; // per entity, input order
+
+  const T* ent(u32 id) const { return &geom[size_t(id) * (isBox ? 6 : 3)]; }
+
+  // ------------------------------------------------------------------ space indexing
+  template<typename R>
+  void grid_factors(R* rsize, R* rast, R* derast)
+  {
+    R sub = R(res);
+    for (int d = 0; d < 3; ++d)
+    {
+      rsize[d] = R(sizeT[d]);
+      derast[d] = rsize[d] / sub;
+      bool flat = rsize[d] == 0;
+      rast[d] = flat ? R(1) : (sub / rsize[d]);
+    }
+  }
+
+  // si_grid.h:145-175 GetPointGridID
+  template<typename R>
+  bool point_grid(const T* p, u32 g[3], const R* rsize, const R* rast) const
+  {
+    for (int d = 0; d < 3; ++d)
+    {
+      T pc = T(p[d]) - spaceMin[d];
+      if (pc < -TOL || pc > rsize[d] + TOL)
+        return false;
+      if (pc <= 0)
+        g[d] = 0;
+      else
+      {
+        u32 rid = u32(R(pc) * rast[d]);
+        g[d] = std::min<u32>(maxRasterID, rid);
+      }
+    }
+    return true;
+  }
+
+  // si_grid.h:221-285 GetLooseBoxGridData<2.0>
+  template<typename R>
+  bool loose_box_grid(const T* box, u32 g[3], u32& level, const R* rast) const
+  {
+    T space[6] = { spaceMin[0], spaceMin[1], spaceMin[2], spaceMax[0], spaceMax[1], spaceMax[2] };
+    if (!G::range_contains_box(space, box, TOL))
+      return false;
+    T center[3], bsize[3];
+    for (int d = 0; d < 3; ++d)
+      center[d] = (box[d] + box[3 + d]) * T(0.5); // internal_geometry_module.h:132-138
+    for (int d = 0; d < 3; ++d)
+      bsize[d] = T(box[3 + d] - box[d]); // internal_geometry_module.h:140-146
+    for (int d = 0; d < 3; ++d)
+      g[d] = u32(R(center[d] - spaceMin[d]) * rast[d]);
+    R maxRel = R{};
+    for (int d = 0; d < 3; ++d)
+      maxRel = std::max(maxRel, R(bsize[d]) * rast[d]);
+    u32 maxRelGrid = u32(std::ceil(maxRel));
+    if (maxRelGrid == 0)
+    {
+      level = 0;
+      return true;
+    }
+    level = u32(std::bit_width(maxRelGrid - 1));
+    return true;
+  }
+
+  // si_grid.h:177-219 GetBoxGridID (non-loose trees)
+  template<typename R>
+  bool box_grid_range(const T* box, u32 g0[3], u32 g1[3], const R* rast) const
+  {
+    R zero = R{};
+    R maxR = R(res);
+    for (int d = 0; d < 3; ++d)
+    {
+      T bmin = T(box[d]) - spaceMin[d];
+      T bmax = T(box[3 + d]) - spaceMin[d];
+      if (bmin < -TOL || bmax > sizeT[d] + TOL)
+        return false;
+      R minR = R(bmin) * rast[d];
+      R maxRid = R(bmax) * rast[d];
+      g0[d] = u32(std::clamp(minR, zero, maxR));
+      g1[d] = u32(std::clamp(maxRid, zero, maxR));
+      if ((g0[d] != g1[d] && std::floor(maxRid) == maxRid) || g1[d] >= res)
+        --g1[d];
+    }
+    return true;
+  }
+
+  // si_mortongrid.h:69-97 GetLocation -> compact key (si_morton.h:129-131)
+  template<typename R>
+  u64 location_key(const T* e, const R* rsize, const R* rast) const
+  {
+    u32 g[3];
+    if (!isBox)
+    {
+      if (!point_grid<R>(e, g, rsize, rast))
+        return compact_key(0, 0); // ALLOW_OUT_OF_SPACE_INSERTION: root (si_mortongrid.h:57-62)
+      return compact_key(encode3(g), D);
+    }
+    if (loose)
+    {
+      u32 level = 0;
+      if (!loose_box_grid<R>(e, g, level, rast))
+        return compact_key(0, 0);
+      u32 shift = level * 3;
+      u64 loc = (encode3(g) >> shift) << shift;
+      return compact_key(loc, u64(u32(D - level)));
+    }
+    u32 g1[3];
+    if (!box_grid_range<R>(e, g, g1, rast))
+      return compact_key(0, 0);
+    // si_morton.h:698-722 GetRangeLocation
+    if (g[0] == g1[0] && g[1] == g1[1] && g[2] == g1[2])
+      return compact_key(encode3(g), D);
+    u64 l0 = encode3(g), l1 = encode3(g1);
+    u64 diff = l0 ^ l1;
+    u32 levelID = (u32(std::bit_width(diff)) + 2) / 3;
+    u32 shift = levelID * 3;
+    return compact_key((l0 >> shift) << shift, D - levelID);
+  }
+
+  // si_grid.h:124-143 CalculateGridCellCenter, used by InitNodeGeometry (ot_dynamic_hash_core.h:563-572)
+  template<typename R>
+  void node_center(u64 key, T c[3], const R* derast) const
+  {
+    auto g = decode_node(key, D);
+    u32 depth = key_depth(key);
+    u32 centerLevel = D - depth;
+    R halfGrid = R(u64(1) << centerLevel) * R(0.5);
+    for (int d = 0; d < 3; ++d)
+      c[d] = T((R(g[d]) + halfGrid) * derast[d]) + spaceMin[d];
+  }
+
+  void init_min_point(Node& n) const
+  {
+    T c[3];
+    if (rasterDouble)
+      node_center<double>(n.key, c, derastD);
+    else
+      node_center<float>(n.key, c, derastF);
+    u32 depth = key_depth(n.key);
+    for (int d = 0; d < 3; ++d)
+      n.minPoint[d] = c[d] - nodeSize[depth + 1][d];
+  }
+
+  // ------------------------------------------------------------------ Create
+  // ot_dynamic_hash_core.h:751-809
+  void create(const T* entities, size_t n, u32 maxDepthIn, const T* box, size_t maxElemIn, bool isBoxTree, bool looseTree)
+  {
+    isBox = isBoxTree;
+    loose = isBoxTree && looseTree;
+    N = n;
+    maxElem = maxElemIn;
+    geom.assign(entities, entities + n * (isBox ? 6 : 3));
+    nodes.clear();
+    locationKeys.clear();
+
+    // :759 box space: given, else IGM::GetBoundingBoxAD (internal_geometry_module.h:342-370)
+    if (box)
+    {
+      for (int d = 0; d < 3; ++d)
+      {
+        spaceMin[d] = box[d];
+        spaceMax[d] = box[3 + d];
+      }
+    }
+    else
+    {
+      for (int d = 0; d < 3; ++d)
+      {
+        spaceMin[d] = std::numeric_limits<T>::max();
+        spaceMax[d] = -std::numeric_limits<T>::max();
+      }
+      for (size_t i = 0; i < n; ++i)
+      {
+        const T* e = ent(u32(i));
+        for (int d = 0; d < 3; ++d)
+        {
+          spaceMin[d] = std::min(spaceMin[d], e[d]);
+          spaceMax[d] = std::max(spaceMax[d], isBox ? e[3 + d] : e[d]);
+        }
+      }
+    }
+    // :762-764
+    D = (maxDepthIn == 0) ? estimate_max_depth(n, maxElem) : maxDepthIn;
+
+    // InitBase :611-626 -> si_grid.h:65-103, ot_base.h:102-134
+    res = u32(1) << D;
+    maxRasterID = res - 1;
+    for (int d = 0; d < 3; ++d)
+      sizeT[d] = spaceMax[d] - spaceMin[d];
+    rasterDouble = !(std::is_same_v<T, float> && D < 16);
+    grid_factors<double>(rsizeD, rastD, derastD);
+    grid_factors<float>(rsizeF, rastF, derastF);
+    if (!isBox)
+    {
+      nodeSize.assign(D + 2, {});
+      T lf = T(1.0);
+      for (u32 d = 0; d < D + 2; ++d, lf *= T(0.5))
+        for (int c = 0; c < 3; ++c)
+          nodeSize[d][c] = sizeT[c] * lf;
+    }
+    Node root;
+    root.key = 1;
+    if (!isBox)
+      init_min_point(root);
+    else
+    {
+      // ot_dynamic_hash_core.h:573-576 MBR init: minPoint = {max, 0, 0}, size = 0
+      root.minPoint[0] = std::numeric_limits<T>::max();
+    }
+    if (n == 0)
+    {
+      nodes.emplace(1, root);
+      return;
+    }
+
+    // :774-783 locations
+    locationKeys.resize(n);
+    for (size_t i = 0; i < n; ++i)
+      locationKeys[i] = rasterDouble ? location_key<double>(ent(u32(i)), rsizeD, rastD) : location_key<float>(ent(u32(i)), rsizeF, rastF);
+
+    // :791-796 sort by location (ParExec path). Ties are ordered by id here; the reference's
+    // std::sort leaves them unspecified, so every comparison is made on canonical (sorted) id sets.
+    std::vector<u32> order(n);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](u32 a, u32 b) { return locationKeys[a] < locationKeys[b]; });
+
+    // :717-747 BuildSubtree (depth-first emission)
+    build_subtree(root, 0, order, 0, n);
+
+    // :803-806 node geometry
+    if (isBox)
+      init_mbr(nodes.at(1));
+    else if (box)
+      init_root_box_min_point();
+  }
+
+  // ot_dynamic_hash_core.h:647-747 (ProcessNode / CreateProcessingData / BuildSubtree)
+  void build_subtree(Node node, u32 depth, const std::vector<u32>& order, size_t b, size_t e)
+  {
+    size_t count = e - b;
+    node.subtreeCount = count;
+    size_t it = b;
+    if (count > 0)
+    {
+      size_t stuckEnd = e;
+      if (count > maxElem && depth < D)
+      {
+        // :660-666 partition_point on "entity depth == node depth" (stuck entities come first)
+        stuckEnd = b;
+        while (stuckEnd < e && key_loc_depth(locationKeys[order[stuckEnd]]) == depth)
+          ++stuckEnd;
+      }
+      for (size_t i = b; i < stuckEnd; ++i)
+        node.entities.push_back(order[i]);
+      it = stuckEnd;
+      while (it < e)
+      {
+        // :695-714 child id from bits [3(D-d-1), 3(D-d-1)+3)
+        u32 examined = D - (depth + 1);
+        u64 loc = key_loc(locationKeys[order[it]]);
+        u64 mask = u64(7) << (examined * 3);
+        u64 flag = loc & mask;
+        u64 childID = flag >> (examined * 3);
+        size_t end = it;
+        while (end < e && (key_loc(locationKeys[order[end]]) & mask) == flag)
+          ++end;
+        Node child;
+        child.key = (node.key << 3) | childID;
+        if (!isBox)
+          init_min_point(child);
+        // LinkChild (ot_dynamic_hash_core.h:190-215) overwrites an existing link with the same
+        // child id. That only happens when an entity's location lies outside the 3*D-bit grid (a
+        // degenerate loose box centred on the max face rasterises to 2^D): the reference then
+        // builds a second instance of the child whose final emplace fails, so the entity ends up
+        // in nodes that are not reachable from the root. The restatement does the same.
+        if (std::find(node.children.begin(), node.children.end(), child.key) == node.children.end())
+          node.children.push_back(child.key);
+        build_subtree(child, depth + 1, order, it, end);
+        it = end;
+      }
+    }
+    nodes.emplace(node.key, std::move(node));
+  }
+
+  // ot_dynamic_hash_core.h:1425-1450 InitializeSubtreeMinimalNodeGeometry
+  void init_mbr(Node& node, T outMin[3] = nullptr, T outMax[3] = nullptr)
+  {
+    T bmin[3], bmax[3];
+    for (int d = 0; d < 3; ++d)
+    {
+      bmin[d] = std::numeric_limits<T>::max();
+      bmax[d] = -std::numeric_limits<T>::max();
+    }
+    for (u64 ck : node.children)
+    {
+      T cmin[3], cmax[3];
+      init_mbr(nodes.at(ck), cmin, cmax);
+      for (int d = 0; d < 3; ++d)
+      {
+        bmin[d] = std::min(bmin[d], cmin[d]);
+        bmax[d] = std::max(bmax[d], cmax[d]);
+      }
+    }
+    for (u32 id : node.entities)
+    {
+      const T* e = ent(id);
+      for (int d = 0; d < 3; ++d)
+      {
+        bmin[d] = std::min(bmin[d], e[d]);
+        bmax[d] = std::max(bmax[d], e[3 + d]);
+      }
+    }
+    for (int d = 0; d < 3; ++d)
+    {
+      node.minPoint[d] = bmin[d];
+      node.size[d] = bmax[d] - bmin[d];
+    }
+    if (outMin)
+      for (int d = 0; d < 3; ++d)
+      {
+        outMin[d] = bmin[d];
+        outMax[d] = bmax[d];
+      }
+  }
+
+  // ot_dynamic_hash_core.h:1573-1601 InitializeRootNodeBox (MinPoint, out-of-space allowed)
+  void init_root_box_min_point()
+  {
+    Node& root = nodes.at(1);
+    T bmin[3], bmax[3];
+    for (int d = 0; d < 3; ++d)
+    {
+      bmin[d] = root.minPoint[d];
+      bmax[d] = root.minPoint[d] + nodeSize[0][d];
+    }
+    for (u32 id : root.entities)
+    {
+      const T* p = ent(id);
+      for (int d = 0; d < 3; ++d)
+      {
+        bmin[d] = std::min(bmin[d], p[d]);
+        bmax[d] = std::max(bmax[d], p[d]);
+      }
+    }
+    for (int d = 0; d < 3; ++d)
+    {
+      root.minPoint[d] = bmin[d];
+      nodeSize[0][d] = bmax[d] - bmin[d];
+    }
+  }
+
+  // ------------------------------------------------------------------ node accessors
+  // ot_dynamic_hash_core.h:491-529
+  const T* node_min(const Node& n) const { return n.minPoint; }
+  const T* node_size(const Node& n) const { return isBox ? n.size : nodeSize[key_depth(n.key)].data(); }
+  void node_box(const Node& n, T box[6]) const
+  {
+    const T* mn = node_min(n);
+    const T* sz = node_size(n);
+    for (int d = 0; d < 3; ++d)
+    {
+      box[d] = mn[d];
+      box[3 + d] = mn[d] + sz[d];
+    }
+  }
+  const Node& root() const { return nodes.at(1); }
+
+  template<typename F>
+  void dfs(F&& visit, const Node& start) const
+  {
+    std::vector<const Node*> stack{ &start };
+    while (!stack.empty())
+    {
+      const Node* n = stack.back();
+      stack.pop_back();
+      if (!visit(*n))
+        continue;
+      for (u64 ck : n->children)
+        stack.push_back(&nodes.at(ck));
+    }
+  }
+  void collect_subtree(const Node& n, std::vector<u32>& out) const
+  {
+    dfs(
+      [&](const Node& m) {
+        out.insert(out.end(), m.entities.begin(), m.entities.end());
+        return true;
+      },
+      n);
+  }
+
+  // ------------------------------------------------------------------ queries
+  // ot_query.h:476-583 RangeSearch
+  std::vector<u32> range_search(const T* range, RangeMode mode, T tol) const
+  {
+    std::vector<u32> found;
+    T rootBox[6];
+    node_box(root(), rootBox);
+    if (G::range_contains_box(range, rootBox, tol))
+    {
+      found.resize(N);
+      std::iota(found.begin(), found.end(), 0u);
+      return found;
+    }
+    T vol = T(1.0);
+    for (int d = 0; d < 3; ++d)
+      vol *= T(range[3 + d] - range[d]);
+    if (vol <= 0.0)
+      return found;
+    T rmin[3], rsize[3];
+    for (int d = 0; d < 3; ++d)
+    {
+      rmin[d] = range[d];
+      rsize[d] = T(range[3 + d] - range[d]);
+    }
+    dfs(
+      [&](const Node& n) {
+        const T* mn = node_min(n);
+        const T* sz = node_size(n);
+        if (!G::overlap_by_min_point(rmin, rsize, mn, sz, tol))
+          return false;
+        if (G::range_contains_min_size(range, mn, sz, tol))
+        {
+          collect_subtree(n, found);
+          return false;
+        }
+        for (u32 id : n.entities)
+        {
+          const T* e = ent(id);
+          bool ok;
+          if (!isBox)
+            ok = G::box_contains_point(range, e, tol);
+          else if (mode == RangeMode::Overlap)
+            ok = G::overlapped_strict(range, e, tol);
+          else
+            ok = G::contains_box_no_tol(range, e);
+          if (ok)
+            found.push_back(id);
+        }
+        return true;
+      },
+      root());
+    return found;
+  }
+
+  // ot_query.h:425-466 PickSearch
+  std::vector<u32> pick_search(const T* p, T tol) const
+  {
+    std::vector<u32> found;
+    T rootBox[6];
+    node_box(root(), rootBox);
+    if (!G::box_contains_point_ad(rootBox, p, tol))
+      return found;
+    dfs(
+      [&](const Node& n) {
+        if (!G::node_contains_point(node_min(n), node_size(n), p, tol))
+          return false;
+        for (u32 id : n.entities)
+        {
+          bool ok = isBox ? G::box_contains_point(ent(id), p, tol) : G::points_equal(ent(id), p, tol);
+          if (ok)
+            found.push_back(id);
+        }
+        return true;
+      },
+      root());
+    return found;
+  }
+
+  // ot_query.h:767-833 FrustumCulling (planes: np x {origoDistance, nx, ny, nz})
+  std::vector<u32> frustum(const T* planes, size_t np, T tol) const
+  {
+    std::vector<u32> found;
+    if (np == 0)
+      return found;
+    dfs(
+      [&](const Node& n) {
+        bool select = true;
+        for (size_t i = 0; i < np; ++i)
+        {
+          const T* pl = planes + 4 * i;
+          PlaneRel r = G::box_plane(node_min(n), node_size(n), pl[0], pl + 1, tol);
+          if (r == PlaneRel::Hit)
+          {
+            select = true;
+            break;
+          }
+          if (r == PlaneRel::Negative)
+          {
+            select = false;
+            break;
+          }
+        }
+        if (!select)
+          return false;
+        for (u32 id : n.entities)
+        {
+          bool neg = false;
+          for (size_t i = 0; i < np && !neg; ++i)
+          {
+            const T* pl = planes + 4 * i;
+            PlaneRel r;
+            if (isBox)
+            {
+              const T* b = ent(id);
+              T bsize[3] = { T(b[3] - b[0]), T(b[4] - b[1]), T(b[5] - b[2]) };
+              r = G::box_plane(b, bsize, pl[0], pl + 1, tol);
+            }
+            else
+              r = G::point_plane(ent(id), pl[0], pl + 1, tol);
+            neg = (r == PlaneRel::Negative);
+          }
+          if (!neg)
+            found.push_back(id);
+        }
+        return true;
+      },
+      root());
+    return found;
+  }
+
+  // ot_query.h:235-291 TraverseNodesByPriority
+  template<typename Proc, typename Prio>
+  void traverse_by_priority(Proc&& proc, Prio&& prio) const
+  {
+    struct PN
+    {
+      const Node* node;
+      T priority;
+      auto operator<=>(const PN& o) const { return priority <=> o.priority; }
+      bool operator==(const PN& o) const { return priority == o.priority; }
+    };
+    auto p0 = prio(root());
+    if (!p0)
+      return;
+    std::priority_queue<PN, std::vector<PN>, std::greater<PN>> q;
+    q.push({ &root(), *p0 });
+    while (!q.empty())
+    {
+      auto [n, pr] = q.top();
+      q.pop();
+      int control = proc(*n, pr); // 0 continue, 1 skip children, 2 terminate
+      if (control == 2)
+        return;
+      if (control == 1)
+        continue;
+      for (u64 ck : n->children)
+      {
+        const Node& c = nodes.at(ck);
+        auto pc = prio(c);
+        if (!pc)
+          continue;
+        q.push({ &c, *pc });
+      }
+    }
+  }
+
+  struct EntityDistance
+  {
+    u32 id;
+    T distance;
+    auto operator<=>(const EntityDistance& o) const { return distance <=> o.distance; }
+    bool operator==(const EntityDistance& o) const { return distance == o.distance; }
+  };
+
+  // ot_query.h:1033-1036
+  static T upper_tol(T v, T tol) { return std::fmax(tol, v * (T(1.0) + tol)); }
+
+  // ot_query.h:1058-1164 AddEntityDistance
+  void add_entity_distance(size_t k, const T* q, const std::vector<u32>& ids, T tol, std::vector<EntityDistance>& opt,
+                           std::vector<EntityDistance>& pes, T& farthest) const
+  {
+    for (u32 id : ids)
+    {
+      T dmin, dminMax;
+      if (!isBox)
+      {
+        T dist = G::distance(q, ent(id));
+        dmin = dminMax = dist;
+      }
+      else
+      {
+        auto mm = G::min_max_distance(q, ent(id), tol);
+        dmin = mm.first;
+        dminMax = mm.second;
+      }
+      if (dmin >= farthest)
+        continue;
+      bool shouldHeapify = opt.size() == k - 1;
+      opt.push_back({ id, dmin });
+      pes.push_back({ id, dminMax });
+      if (pes.size() < k)
+        continue;
+      if (shouldHeapify)
+      {
+        std::ranges::make_heap(opt);
+        std::ranges::make_heap(pes);
+        farthest = upper_tol(pes[0].distance, tol);
+      }
+      else
+      {
+        std::ranges::push_heap(opt);
+        std::ranges::push_heap(pes);
+        std::ranges::pop_heap(pes);
+        pes.pop_back();
+        T limit = upper_tol(pes.front().distance, tol);
+        if (limit < farthest)
+        {
+          farthest = limit;
+          bool removed = false;
+          while (opt.front().distance > farthest)
+          {
+            u32 rid = opt.front().id;
+            auto it = std::ranges::find_if(pes, [rid](const EntityDistance& ed) { return ed.id == rid; });
+            if (it != pes.end())
+            {
+              pes.erase(it);
+              removed = true;
+            }
+            std::ranges::pop_heap(opt);
+            opt.pop_back();
+          }
+          if (removed)
+            std::ranges::make_heap(pes);
+        }
+      }
+    }
+  }
+
+  // ot_query.h:1208-1247 GetNearestNeighbors. Returns (id, distance) pairs in the reference's order.
+  std::vector<EntityDistance> knn(const T* q, size_t k, T maxDistanceWithin, T tol) const
+  {
+    std::vector<EntityDistance> opt, pes;
+    if (k == 0)
+      return opt;
+    T farthest = (maxDistanceWithin == std::numeric_limits<T>::max()) ? std::numeric_limits<T>::max() : upper_tol(maxDistanceWithin, tol);
+    traverse_by_priority(
+      [&](const Node& n, T nodeDistance) -> int {
+        if (nodeDistance >= farthest)
+          return 2;
+        add_entity_distance(k, q, n.entities, tol, opt, pes, farthest);
+        return 0;
+      },
+      [&](const Node& n) -> std::optional<T> {
+        T w = G::wall_distance(q, node_min(n), node_size(n));
+        if (w >= farthest)
+          return std::nullopt;
+        return w;
+      });
+    // ot_query.h:1166-1191 ConvertEntityDistanceToList
+    if (opt.empty())
+      return opt;
+    if (opt.size() < k)
+      std::sort(opt.begin(), opt.end());
+    else
+      std::sort_heap(opt.begin(), opt.end());
+    return opt;
+  }
+
+  // ---------------------------------------------------------------- collision detection
+  // ot_query.h:1274-1300 SweepAndPruneDatabase order: by min-x only (std::sort, unstable)
+  std::vector<u32> sorted_by_minx(const std::vector<u32>& ids) const
+  {
+    std::vector<u32> s(ids);
+    std::sort(s.begin(), s.end(), [&](u32 a, u32 b) { return ent(a)[0] < ent(b)[0]; });
+    return s;
+  }
+
+  // ot_query.h:1308-1458 two-tree CollisionDetection (breadth-first node-pair queue)
+  static void collide_trees(const Tree& L, const Node& lroot, const Tree& Rt, const Node& rroot, T tol, std::vector<std::pair<u32, u32>>& out)
+  {
+    struct NS
+    {
+      const Node* n;
+      bool traversed;
+    };
+    std::unordered_map<const Node*, std::vector<u32>> cache[2];
+    bool same = &L == &Rt;
+    auto inOrder = [&](int side, const Node* n) -> const std::vector<u32>& {
+      if (same)
+        side = 0;
+      const Tree& t = side == 0 ? L : Rt;
+      auto it = cache[side].find(n);
+      if (it == cache[side].end())
+        it = cache[side].emplace(n, t.sorted_by_minx(n->entities)).first;
+      return it->second;
+    };
+    std::queue<std::array<NS, 2>> q;
+    q.push({ NS{ &lroot, false }, NS{ &rroot, false } });
+    while (!q.empty())
+    {
+      auto pp = q.front();
+      q.pop();
+      const auto& le = inOrder(0, pp[0].n);
+      const auto& re = inOrder(1, pp[1].n);
+      size_t rn = re.size();
+      size_t rb = 0;
+      for (u32 lid : le)
+      {
+        const T* lg = L.ent(lid);
+        for (; rb < rn; ++rb)
+        {
+          const T* rg = Rt.ent(re[rb]);
+          if (L.isBox ? (rg[3] >= lg[0]) : (rg[0] >= lg[0]))
+            break;
+        }
+        for (size_t ri = rb; ri < rn; ++ri)
+        {
+          u32 rid = re[ri];
+          const T* rg = Rt.ent(rid);
+          if (L.isBox)
+          {
+            if (lg[3] < rg[0])
+              break;
+            if (G::box_relation(lg, rg, tol) == -1)
+              out.emplace_back(lid, rid);
+          }
+          else
+          {
+            if (lg[0] < rg[0])
+              break;
+            if (G::points_equal(lg, rg, tol))
+              out.emplace_back(lid, rid);
+          }
+        }
+      }
+      std::array<std::vector<NS>, 2> ch;
+      for (int s = 0; s < 2; ++s)
+      {
+        if (pp[s].traversed)
+          continue;
+        const Tree& t = s == 0 ? L : Rt;
+        for (u64 ck : pp[s].n->children)
+          ch[s].push_back({ &t.nodes.at(ck), false });
+      }
+      if (ch[0].empty() && ch[1].empty())
+        continue;
+      for (int s = 0; s < 2; ++s)
+        if (!pp[s].n->entities.empty())
+          ch[s].push_back({ pp[s].n, true });
+      for (auto& lc : ch[0])
+        for (auto& rc : ch[1])
+          if (!(lc.n == pp[0].n && rc.n == pp[1].n))
+            if (G::overlap_by_min_point(L.node_min(*lc.n), L.node_size(*lc.n), Rt.node_min(*rc.n), Rt.node_size(*rc.n), tol))
+              q.push({ lc, rc });
+    }
+  }
+
+  // ot_query.h:1500-1687 self collision, sequential path
+  struct Ctx
+  {
+    const Node* n;
+    T box[6];
+    std::vector<u32> ids;
+  };
+  // ot_query.h:1699-1716 comparator: min-x, then id
+  std::vector<u32> sorted_by_minx_id(const std::vector<u32>& ids) const
+  {
+    std::vector<u32> s(ids);
+    std::sort(s.begin(), s.end(), [&](u32 a, u32 b) {
+      T xa = ent(a)[0], xb = ent(b)[0];
+      return xa < xb || (xa == xb && a < b);
+    });
+    return s;
+  }
+  void collide_subtree(const Node& n, std::vector<Ctx>& stack, T tol, std::vector<std::pair<u32, u32>>& out) const
+  {
+    Ctx c;
+    c.n = &n;
+    c.ids = sorted_by_minx_id(n.entities);
+    node_box(n, c.box);
+    stack.push_back(std::move(c));
+    const Ctx& ctx = stack.back();
+    // :1518-1561 inside node
+    size_t m = ctx.ids.size();
+    for (size_t i = 0; i < m; ++i)
+    {
+      const T* bi = ent(ctx.ids[i]);
+      for (size_t j = i + 1; j < m; ++j)
+      {
+        const T* bj = ent(ctx.ids[j]);
+        if (isBox)
+        {
+          if (bi[3] < bj[0])
+            break;
+          if (G::overlapped_strict(bi, bj, tol))
+            out.emplace_back(ctx.ids[i], ctx.ids[j]);
+        }
+        else
+        {
+          if (bi[0] < bj[0])
+            break;
+          if (G::points_equal(bi, bj, tol))
+            out.emplace_back(ctx.ids[i], ctx.ids[j]);
+        }
+      }
+    }
+    // :1563-1653 with parents
+    const T* nmin = ctx.box;
+    const T* nsize = node_size(n);
+    for (size_t pd = 0; pd + 1 < stack.size(); ++pd)
+    {
+      const Ctx& par = stack[pd];
+      size_t ib = 0;
+      for (u32 pid : par.ids)
+      {
+        const T* pg = ent(pid);
+        if (pg[0] > ctx.box[3])
+          break;
+        T pmin[3], psize[3];
+        for (int d = 0; d < 3; ++d)
+        {
+          pmin[d] = pg[d];
+          psize[d] = isBox ? T(pg[3 + d] - pg[d]) : T(0);
+        }
+        if (!G::overlap_by_min_point(nmin, nsize, pmin, psize, tol))
+          continue;
+        for (; ib < m; ++ib)
+        {
+          const T* eg = ent(ctx.ids[ib]);
+          if (isBox ? (eg[3] >= pg[0]) : (eg[0] >= pg[0]))
+            break;
+        }
+        for (size_t ie = ib; ie < m; ++ie)
+        {
+          u32 eid = ctx.ids[ie];
+          const T* eg = ent(eid);
+          if (isBox)
+          {
+            if (pg[3] < eg[0])
+              break;
+            if (G::overlapped_strict(eg, pg, tol))
+              out.emplace_back(eid, pid);
+          }
+          else
+          {
+            if (pg[0] < eg[0])
+              break;
+            if (G::points_equal(pg, eg, tol))
+              out.emplace_back(eid, pid);
+          }
+        }
+      }
+    }
+    for (u64 ck : n.children)
+      collide_subtree(nodes.at(ck), stack, tol, out);
+    // :1672-1684 loose trees: pairwise sibling sub-trees
+    if (loose)
+    {
+      for (size_t a = 0; a < n.children.size(); ++a)
+        for (size_t b = a + 1; b < n.children.size(); ++b)
+          collide_trees(*this, nodes.at(n.children[a]), *this, nodes.at(n.children[b]), tol, out);
+    }
+    stack.pop_back();
+  }
+  // ot_query.h:1690-1731, 1901-1906
+  std::vector<std::pair<u32, u32>> collide_self(T tol) const
+  {
+    std::vector<std::pair<u32, u32>> out;
+    std::vector<Ctx> stack;
+    collide_subtree(root(), stack, tol, out);
+    return out;
+  }
+  // ot_query.h:1462-1485
+  static std::vector<std::pair<u32, u32>> collide_pair(const Tree& a, const Tree& b, T tol)
+  {
+    std::vector<std::pair<u32, u32>> out;
+    collide_trees(a, a.root(), b, b.root(), tol, out);
+    return out;
+  }
+
+  // ---------------------------------------------------------------- rays
+  // ot_query.h:1928-2011 RayIntersectedAll (sorted by enter distance)
+  std::vector<std::pair<u32, T>> ray_all(const T* o, const T* dir, T tol, T tolInc, T maxDist) const
+  {
+    std::vector<std::pair<u32, T>> found;
+    auto rt = RayTester<T>::make(o, dir, tol, tolInc);
+    if (!rt)
+      return found;
+    dfs(
+      [&](const Node& n) {
+        T en, ex;
+        if (!rt->hit_node(node_min(n), node_size(n), en, ex))
+          return false;
+        for (u32 id : n.entities)
+        {
+          bool h = isBox ? rt->hit_box(ent(id), en, ex) : rt->hit_point(ent(id), en, ex);
+          if (!h)
+            continue;
+          if (!(maxDist == 0 || en <= maxDist))
+            continue;
+          found.emplace_back(id, en);
+        }
+        return true;
+      },
+      root());
+    std::sort(found.begin(), found.end(), [](auto& a, auto& b) { return a.second < b.second || (a.second == b.second && a.first < b.first); });
+    return found;
+  }
+
+  // ot_query.h:2035-2122 RayIntersectedFirst (returned farthest first)
+  std::vector<std::pair<u32, T>> ray_first(const T* o, const T* dir, T tol, T tolInc, T maxDistance) const
+  {
+    std::vector<std::pair<u32, T>> res;
+    auto rt = RayTester<T>::make(o, dir, tol, tolInc);
+    if (!rt)
+      return res;
+    struct Cand
+    {
+      u32 id;
+      T enter;
+      auto operator<=>(const Cand& o) const { return enter <=> o.enter; }
+      bool operator==(const Cand& o) const { return enter == o.enter; }
+    };
+    T applied = tol == 0 ? std::numeric_limits<T>::epsilon() : tol;
+    std::priority_queue<Cand, std::vector<Cand>> heap;
+    T maxExam = maxDistance;
+    traverse_by_priority(
+      [&](const Node& n, T nodeEnter) -> int {
+        if (nodeEnter > maxExam)
+          return 2;
+        for (u32 id : n.entities)
+        {
+          T en, ex;
+          bool h = isBox ? rt->hit_box(ent(id), en, ex) : rt->hit_point(ent(id), en, ex);
+          if (!h)
+            continue;
+          if (en > maxExam)
+            continue;
+          heap.push(Cand{ id, en });
+          if (ex >= maxExam)
+            continue;
+          maxExam = (T(1) + tolInc) * ex + applied;
+          while (!heap.empty() && heap.top().enter > maxExam)
+            heap.pop();
+        }
+        return 0;
+      },
+      [&](const Node& n) -> std::optional<T> {
+        T en, ex;
+        if (!rt->hit_node(node_min(n), node_size(n), en, ex))
+          return std::nullopt;
+        return en;
+      });
+    for (; !heap.empty(); heap.pop())
+      res.emplace_back(heap.top().id, heap.top().enter);
+    return res;
+  }
+};
+
+} // namespace otg_oracle

@@ -1,0 +1,418 @@
+// ref_harness.cpp — exposes the UNMODIFIED reference library (OrthoTree headers, compiled from
+// their own location with -I) through the same C-ABI as otg_oracle_capi.cpp, so that the CPU
+// restatement can be pinned against the reference itself and golden fixtures can be generated.
+//
+// TEST INFRASTRUCTURE ONLY. Built by oracle/Makefile into oracle/_ref/ (git-ignored), and only
+// where the reference sources are present. Results are canonicalised exactly like the restatement's.
+#include "orthotree/octree.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <span>
+#include <vector>
+
+using namespace OrthoTree;
+
+namespace
+{
+template<typename T>
+using PointTree = OrthoTreePointND<3, T>;
+template<typename T>
+using LooseBoxTree = OrthoTreeBoxND<3, true, T>;
+template<typename T>
+using BoxTree = OrthoTreeBoxND<3, false, T>;
+
+struct Result
+{
+  std::vector<uint64_t> offsets{ 0 };
+  std::vector<uint32_t> ids;
+  std::vector<double> dist;
+};
+
+struct AnyRef
+{
+  int scalar = 0; // 0 double, 1 float
+  int kind = 0;   // 0 points, 1 loose boxes, 2 boxes
+  uint32_t D = 0;
+  std::vector<double> ed;
+  std::vector<float> ef;
+  std::unique_ptr<PointTree<double>> pd;
+  std::unique_ptr<LooseBoxTree<double>> lbd;
+  std::unique_ptr<BoxTree<double>> bd;
+  std::unique_ptr<PointTree<float>> pf;
+  std::unique_ptr<LooseBoxTree<float>> lbf;
+  std::unique_ptr<BoxTree<float>> bf;
+  std::vector<uint64_t> locKeys;
+};
+
+template<typename T>
+std::span<const PointND<3, T>> pts_span(const std::vector<T>& v)
+{
+  return { reinterpret_cast<const PointND<3, T>*>(v.data()), v.size() / 3 };
+}
+template<typename T>
+std::span<const BoundingBoxND<3, T>> box_span(const std::vector<T>& v)
+{
+  return { reinterpret_cast<const BoundingBoxND<3, T>*>(v.data()), v.size() / 6 };
+}
+
+template<typename T>
+T tol_or_default(double tol)
+{
+  return tol < 0 ? std::numeric_limits<T>::epsilon() * T(100) : T(tol);
+}
+
+// Location keys through the reference's own space indexing (si_mortongrid.h:69-97).
+template<typename Tree, typename Span>
+std::vector<uint64_t> location_keys(Span ents, const typename Tree::TBox* boxIn, uint32_t D)
+{
+  using GA = typename Tree::GA;
+  using IGM = detail::InternalGeometryModule<GA>;
+  using EA = typename Tree::EA;
+  using CONFIG = typename Tree::CONFIG;
+  auto space = boxIn ? IGM::GetBoxAD(*boxIn) : IGM::template GetBoundingBoxAD<EA>(ents);
+  detail::MortonGridSpaceIndexing<GA, CONFIG::ALLOW_OUT_OF_SPACE_INSERTION, CONFIG::LOOSE_FACTOR, CONFIG::MAX_ALLOWED_DEPTH_ID> si(D, space);
+  std::vector<uint64_t> keys(ents.size());
+  for (size_t i = 0; i < ents.size(); ++i)
+  {
+    auto loc = si.GetLocation(ents[i]);
+    keys[i] = (uint64_t(loc.GetLocationID()) << 5) | uint64_t(loc.GetDepthID());
+  }
+  return keys;
+}
+
+template<typename Tree>
+void export_nodes(Tree const& t, uint64_t* keys, double* minp, double* size, uint64_t* eoff, uint32_t* eids)
+{
+  std::vector<uint64_t> ks;
+  for (auto const& kv : t.GetNodes())
+    ks.push_back(uint64_t(kv.first));
+  std::sort(ks.begin(), ks.end());
+  uint64_t off = 0;
+  for (size_t i = 0; i < ks.size(); ++i)
+  {
+    auto nv = t.GetNodeValue(ks[i]);
+    keys[i] = ks[i];
+    auto const& mn = t.GetNodeMinPoint(nv);
+    auto const& sz = t.GetNodeSize(nv);
+    for (int d = 0; d < 3; ++d)
+    {
+      minp[3 * i + d] = double(mn[d]);
+      size[3 * i + d] = double(sz[d]);
+    }
+    eoff[i] = off;
+    std::vector<uint32_t> ids(t.GetNodeEntities(nv).begin(), t.GetNodeEntities(nv).end());
+    std::sort(ids.begin(), ids.end());
+    for (auto id : ids)
+      eids[off++] = id;
+  }
+  eoff[ks.size()] = off;
+}
+
+template<typename F>
+Result* run_queries(uint64_t nq, F&& one)
+{
+  auto* r = new Result();
+  for (uint64_t q = 0; q < nq; ++q)
+  {
+    one(q, *r);
+    r->offsets.push_back(r->ids.size());
+  }
+  return r;
+}
+
+template<typename T, typename Tree, typename Span>
+Result* range_impl(Tree const& t, Span ents, const T* ranges, uint64_t nq, int mode, double tol)
+{
+  return run_queries(nq, [&](uint64_t q, Result& r) {
+    auto const& b = *reinterpret_cast<const BoundingBoxND<3, T>*>(ranges + 6 * q);
+    auto v = t.RangeSearch(b, ents, mode == 1 ? RangeSearchMode::Overlap : RangeSearchMode::Inside, tol_or_default<T>(tol));
+    std::sort(v.begin(), v.end());
+    r.ids.insert(r.ids.end(), v.begin(), v.end());
+  });
+}
+template<typename T, typename Tree, typename Span>
+Result* pick_impl(Tree const& t, Span ents, const T* pts, uint64_t nq, double tol)
+{
+  return run_queries(nq, [&](uint64_t q, Result& r) {
+    auto const& p = *reinterpret_cast<const PointND<3, T>*>(pts + 3 * q);
+    auto v = t.PickSearch(p, ents, tol_or_default<T>(tol));
+    std::sort(v.begin(), v.end());
+    r.ids.insert(r.ids.end(), v.begin(), v.end());
+  });
+}
+template<typename T, typename Tree, typename Span>
+Result* frustum_impl(Tree const& t, Span ents, const T* planes, uint64_t np, uint64_t nq, double tol)
+{
+  return run_queries(nq, [&](uint64_t q, Result& r) {
+    std::vector<PlaneND<3, T>> pl(np);
+    for (uint64_t i = 0; i < np; ++i)
+    {
+      const T* s = planes + 4 * (np * q + i);
+      pl[i].OrigoDistance = s[0];
+      pl[i].Normal = { s[1], s[2], s[3] };
+    }
+    auto v = t.FrustumCulling(std::span<const PlaneND<3, T>>(pl), ents, tol_or_default<T>(tol));
+    std::sort(v.begin(), v.end());
+    r.ids.insert(r.ids.end(), v.begin(), v.end());
+  });
+}
+template<typename T, bool IS_BOX, typename Tree, typename Span>
+Result* knn_impl(Tree const& t, Span ents, const T* pts, uint64_t nq, const uint32_t* k, double maxDist, double tol)
+{
+  using GA = GeneralGeometryAdapterND<3, T>;
+  T md = maxDist < 0 ? std::numeric_limits<T>::max() : T(maxDist);
+  T tl = tol_or_default<T>(tol);
+  return run_queries(nq, [&](uint64_t q, Result& r) {
+    auto const& p = *reinterpret_cast<const PointND<3, T>*>(pts + 3 * q);
+    auto v = t.template GetNearestNeighbors<true>(p, k[q], md, ents, tl);
+    std::vector<std::pair<T, uint32_t>> dv;
+    for (auto id : v)
+    {
+      T dist;
+      if constexpr (IS_BOX)
+        dist = GA::MinMaxDistance(p, ents[id], tl).min;
+      else
+        dist = GA::Distance(p, ents[id]);
+      dv.emplace_back(dist, id);
+    }
+    std::sort(dv.begin(), dv.end());
+    for (auto& e : dv)
+    {
+      r.ids.push_back(e.second);
+      r.dist.push_back(double(e.first));
+    }
+  });
+}
+template<typename T, typename Tree, typename Span>
+Result* ray_impl(Tree const& t, Span ents, const T* rays, uint64_t nq, double tol, double tolInc, double maxDist, bool first)
+{
+  using GA = GeneralGeometryAdapterND<3, T>;
+  using IGM = detail::InternalGeometryModule<GA>;
+  T md = maxDist < 0 ? std::numeric_limits<T>::max() : T(maxDist);
+  T tl = tol_or_default<T>(tol);
+  return run_queries(nq, [&](uint64_t q, Result& r) {
+    auto const& o = *reinterpret_cast<const PointND<3, T>*>(rays + 6 * q);
+    auto const& d = *reinterpret_cast<const PointND<3, T>*>(rays + 6 * q + 3);
+    auto v = first ? t.RayIntersectedFirst(o, d, ents, tl, T(tolInc), md) : t.RayIntersectedAll(o, d, ents, tl, T(tolInc), md);
+    auto rt = IGM::RayHitTester::Make(o, d, tl, T(tolInc));
+    std::vector<std::pair<T, uint32_t>> dv;
+    for (auto id : v)
+    {
+      auto h = rt->Hit(ents[id]);
+      dv.emplace_back(h ? h->enterDistance : T(-1), id);
+    }
+    std::sort(dv.begin(), dv.end());
+    for (auto& e : dv)
+    {
+      r.ids.push_back(e.second);
+      r.dist.push_back(double(e.first));
+    }
+  });
+}
+Result* pairs_result(std::vector<std::pair<uint32_t, uint32_t>> p, bool canonical)
+{
+  if (canonical)
+    for (auto& e : p)
+      if (e.first > e.second)
+        std::swap(e.first, e.second);
+  std::sort(p.begin(), p.end());
+  auto* r = new Result();
+  for (auto& e : p)
+  {
+    r->ids.push_back(e.first);
+    r->ids.push_back(e.second);
+  }
+  r->offsets.push_back(r->ids.size());
+  return r;
+}
+
+// dispatch helper: calls f(tree, span, scalarTag)
+template<typename F>
+auto with_tree(AnyRef* a, F&& f)
+{
+  if (a->scalar == 0)
+  {
+    if (a->kind == 0)
+      return f(*a->pd, pts_span(a->ed), double{}, std::false_type{});
+    if (a->kind == 1)
+      return f(*a->lbd, box_span(a->ed), double{}, std::true_type{});
+    return f(*a->bd, box_span(a->ed), double{}, std::true_type{});
+  }
+  if (a->kind == 0)
+    return f(*a->pf, pts_span(a->ef), float{}, std::false_type{});
+  if (a->kind == 1)
+    return f(*a->lbf, box_span(a->ef), float{}, std::true_type{});
+  return f(*a->bf, box_span(a->ef), float{}, std::true_type{});
+}
+
+template<typename Tree, typename T, typename Span>
+std::unique_ptr<Tree> make_tree(Span ents, uint32_t maxDepth, const T* box, uint64_t maxElem, AnyRef* a)
+{
+  std::optional<typename Tree::TBox> ob;
+  if (box)
+    ob = *reinterpret_cast<const typename Tree::TBox*>(box);
+  std::optional<depth_t> od;
+  if (maxDepth)
+    od = maxDepth;
+  auto t = std::make_unique<Tree>(PAR_EXEC, ents, od, ob, maxElem);
+  a->D = t->GetMaxDepthID();
+  a->locKeys = location_keys<Tree>(ents, box ? &*ob : nullptr, a->D);
+  return t;
+}
+} // namespace
+
+extern "C"
+{
+  void* oro_create(int scalar, int kind, const void* ent, uint64_t n, uint32_t maxDepth, const void* box, uint64_t maxElem)
+  {
+    auto* a = new AnyRef();
+    a->scalar = scalar;
+    a->kind = kind;
+    size_t w = kind == 0 ? 3 : 6;
+    if (scalar == 0)
+    {
+      a->ed.assign((const double*)ent, (const double*)ent + n * w);
+      auto* b = (const double*)box;
+      if (kind == 0)
+        a->pd = make_tree<PointTree<double>>(pts_span(a->ed), maxDepth, b, maxElem, a);
+      else if (kind == 1)
+        a->lbd = make_tree<LooseBoxTree<double>>(box_span(a->ed), maxDepth, b, maxElem, a);
+      else
+        a->bd = make_tree<BoxTree<double>>(box_span(a->ed), maxDepth, b, maxElem, a);
+    }
+    else
+    {
+      a->ef.assign((const float*)ent, (const float*)ent + n * w);
+      auto* b = (const float*)box;
+      if (kind == 0)
+        a->pf = make_tree<PointTree<float>>(pts_span(a->ef), maxDepth, b, maxElem, a);
+      else if (kind == 1)
+        a->lbf = make_tree<LooseBoxTree<float>>(box_span(a->ef), maxDepth, b, maxElem, a);
+      else
+        a->bf = make_tree<BoxTree<float>>(box_span(a->ef), maxDepth, b, maxElem, a);
+    }
+    return a;
+  }
+  void oro_destroy(void* h) { delete (AnyRef*)h; }
+  uint32_t oro_max_depth(void* h) { return ((AnyRef*)h)->D; }
+  uint64_t oro_node_count(void* h)
+  {
+    return with_tree((AnyRef*)h, [](auto& t, auto, auto, auto) { return uint64_t(t.GetNodeCount()); });
+  }
+  void oro_location_keys(void* h, uint64_t* out)
+  {
+    auto* a = (AnyRef*)h;
+    std::memcpy(out, a->locKeys.data(), a->locKeys.size() * sizeof(uint64_t));
+  }
+  void oro_export_nodes(void* h, uint64_t* keys, double* minp, double* size, uint64_t* eoff, uint32_t* eids, uint64_t* subtree)
+  {
+    (void)subtree;
+    with_tree((AnyRef*)h, [&](auto& t, auto, auto, auto) {
+      export_nodes(t, keys, minp, size, eoff, eids);
+      return 0;
+    });
+  }
+  void* oro_range(void* h, const void* ranges, uint64_t nq, int mode, double tol)
+  {
+    return with_tree((AnyRef*)h, [&](auto& t, auto ents, auto s, auto) -> Result* {
+      using T = decltype(s);
+      return range_impl<T>(t, ents, (const T*)ranges, nq, mode, tol);
+    });
+  }
+  void* oro_pick(void* h, const void* pts, uint64_t nq, double tol)
+  {
+    return with_tree((AnyRef*)h, [&](auto& t, auto ents, auto s, auto) -> Result* {
+      using T = decltype(s);
+      return pick_impl<T>(t, ents, (const T*)pts, nq, tol);
+    });
+  }
+  void* oro_frustum(void* h, const void* planes, uint64_t np, uint64_t nq, double tol)
+  {
+    return with_tree((AnyRef*)h, [&](auto& t, auto ents, auto s, auto) -> Result* {
+      using T = decltype(s);
+      return frustum_impl<T>(t, ents, (const T*)planes, np, nq, tol);
+    });
+  }
+  void* oro_knn(void* h, const void* pts, uint64_t nq, const uint32_t* k, double maxDist, double tol)
+  {
+    return with_tree((AnyRef*)h, [&](auto& t, auto ents, auto s, auto isBox) -> Result* {
+      using T = decltype(s);
+      return knn_impl<T, decltype(isBox)::value>(t, ents, (const T*)pts, nq, k, maxDist, tol);
+    });
+  }
+  void* oro_ray(void* h, const void* rays, uint64_t nq, double tol, double tolInc, double maxDist, int first)
+  {
+    return with_tree((AnyRef*)h, [&](auto& t, auto ents, auto s, auto) -> Result* {
+      using T = decltype(s);
+      return ray_impl<T>(t, ents, (const T*)rays, nq, tol, tolInc, maxDist, first != 0);
+    });
+  }
+  void* oro_collide_self(void* h, double tol)
+  {
+    auto* a = (AnyRef*)h;
+    if (a->kind == 0)
+      return pairs_result({}, true);
+    return with_tree(a, [&](auto& t, auto ents, auto s, auto isBox) -> Result* {
+      using T = decltype(s);
+      if constexpr (decltype(isBox)::value)
+        return pairs_result(t.CollisionDetection(ents, tol_or_default<T>(tol), SEQ_EXEC), true);
+      else
+        return pairs_result({}, true);
+    });
+  }
+  // Same as oro_collide_self but through the parallel (task-split) path of the reference.
+  void* oro_collide_self_par(void* h, double tol)
+  {
+    auto* a = (AnyRef*)h;
+    return with_tree(a, [&](auto& t, auto ents, auto s, auto isBox) -> Result* {
+      using T = decltype(s);
+      if constexpr (decltype(isBox)::value)
+        return pairs_result(t.CollisionDetection(ents, tol_or_default<T>(tol), PAR_EXEC), true);
+      else
+        return pairs_result({}, true);
+    });
+  }
+  void* oro_collide_pair(void* h1, void* h2, double tol)
+  {
+    auto* a = (AnyRef*)h1;
+    auto* b = (AnyRef*)h2;
+    if (a->scalar == 0 && a->kind == 1)
+      return pairs_result(LooseBoxTree<double>::CollisionDetection(*a->lbd, box_span(a->ed), *b->lbd, box_span(b->ed), tol_or_default<double>(tol)), false);
+    if (a->scalar == 1 && a->kind == 1)
+      return pairs_result(LooseBoxTree<float>::CollisionDetection(*a->lbf, box_span(a->ef), *b->lbf, box_span(b->ef), tol_or_default<float>(tol)), false);
+    if (a->scalar == 0 && a->kind == 2)
+      return pairs_result(BoxTree<double>::CollisionDetection(*a->bd, box_span(a->ed), *b->bd, box_span(b->ed), tol_or_default<double>(tol)), false);
+    if (a->scalar == 1 && a->kind == 2)
+      return pairs_result(BoxTree<float>::CollisionDetection(*a->bf, box_span(a->ef), *b->bf, box_span(b->ef), tol_or_default<float>(tol)), false);
+    return pairs_result({}, false);
+  }
+  uint64_t oro_res_nq(void* r) { return ((Result*)r)->offsets.size() - 1; }
+  uint64_t oro_res_total(void* r) { return ((Result*)r)->ids.size(); }
+  int oro_res_has_dist(void* r) { return ((Result*)r)->dist.empty() ? 0 : 1; }
+  void oro_res_copy(void* rr, uint64_t* offsets, uint32_t* ids, double* dist)
+  {
+    auto* r = (Result*)rr;
+    std::memcpy(offsets, r->offsets.data(), r->offsets.size() * sizeof(uint64_t));
+    std::memcpy(ids, r->ids.data(), r->ids.size() * sizeof(uint32_t));
+    if (dist && !r->dist.empty())
+      std::memcpy(dist, r->dist.data(), r->dist.size() * sizeof(double));
+  }
+  void oro_res_free(void* r) { delete (Result*)r; }
+
+  // Timed reference Create (OctreePoint, PAR_EXEC) — used for the CPU baseline where the reference is built.
+  double oro_time_create_points(const double* pts, uint64_t n, uint32_t maxDepth, uint64_t maxElem, int reps)
+  {
+    auto span = std::span<const Point3D>(reinterpret_cast<const Point3D*>(pts), n);
+    auto t0 = std::chrono::steady_clock::now();
+    for (int r = 0; r < reps; ++r)
+    {
+      OctreePoint t(PAR_EXEC, span, depth_t(maxDepth), std::nullopt, maxElem);
+      (void)t;
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    return std::chrono::duration<double>(t1 - t0).count();
+  }
+}

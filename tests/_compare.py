@@ -1,0 +1,59 @@
+"""Comparison helpers shared by the oracle and GPU parity tests."""
+import glob
+import os
+
+import numpy as np
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def golden_cases():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
+
+
+def load_golden(name):
+    with np.load(os.path.join(GOLDEN_DIR, name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+def assert_csr_equal(a, b, what):
+    """a, b: (offsets, ids[, dist]) tuples; distances compared exactly unless rel_tol given."""
+    assert np.array_equal(np.asarray(a[0], np.uint64), np.asarray(b[0], np.uint64)), f"{what}: offsets differ"
+    assert np.array_equal(a[1], b[1]), f"{what}: ids differ ({len(a[1])} vs {len(b[1])})"
+    if len(a) > 2 and len(b) > 2 and a[2] is not None and b[2] is not None:
+        assert np.array_equal(a[2], b[2]), f"{what}: distances differ"
+
+
+def assert_dist_close(a, b, rel, what):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    assert a.shape == b.shape, f"{what}: distance count differs"
+    err = np.abs(a - b) <= rel * np.maximum(np.abs(a), np.abs(b))
+    assert err.all(), f"{what}: distances differ beyond {rel} relative"
+
+
+def assert_nodes_equal(gpu, ref, what):
+    """gpu: nodes reachable from the root (any order). ref: every node of the reference's node map,
+    sorted by key. Nodes the reference holds but cannot reach from the root (its orphan nodes for
+    locations outside the 3*D-bit grid) may only hold entities that no reachable node holds."""
+    order = np.argsort(gpu["keys"], kind="stable")
+    gk = gpu["keys"][order]
+    rk = ref["keys"]
+    pos = np.searchsorted(rk, gk)
+    assert (pos < len(rk)).all() and np.array_equal(rk[np.minimum(pos, len(rk) - 1)], gk), f"{what}: node keys differ"
+    assert np.array_equal(gpu["min"][order], ref["min"][pos]), f"{what}: node min points differ"
+    assert np.array_equal(gpu["size"][order], ref["size"][pos]), f"{what}: node sizes differ"
+    reached = set()
+    for gi, ri in zip(order, pos):
+        ge = np.sort(gpu["eids"][int(gpu["eoff"][gi]) : int(gpu["eoff"][gi + 1])])
+        re = ref["eids"][int(ref["eoff"][ri]) : int(ref["eoff"][ri + 1])]
+        assert np.array_equal(ge, re), f"{what}: entities of node {hex(int(gk[list(order).index(gi)]))} differ"
+        reached.update(ge.tolist())
+    extra = np.setdiff1d(np.arange(len(rk)), pos)
+    for ri in extra:
+        re = ref["eids"][int(ref["eoff"][ri]) : int(ref["eoff"][ri + 1])]
+        assert not (set(re.tolist()) & reached), f"{what}: orphan node shares entities"
+
+
+def node_dict(prefix, g):
+    return {k: g[prefix + k] for k in ("keys", "min", "size", "eoff", "eids")}

@@ -1,0 +1,180 @@
+"""ctypes access to the CPU oracle (oracle/otg_oracle_capi.cpp) and, where it was built, to the
+reference harness (oracle/_ref/libref_orthotree.so). Both export the same C-ABI, so every test can
+run the same call against either library. Test infrastructure only."""
+import ctypes as C
+import os
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "libotg_oracle.so")
+REF_SO = os.path.join(ROOT, "oracle", "_ref", "libref_orthotree.so")
+
+KIND_POINTS, KIND_LOOSE_BOXES, KIND_BOXES = 0, 1, 2
+
+_vp = C.c_void_p
+_u64 = C.c_uint64
+_u32 = C.c_uint32
+_dbl = C.c_double
+_int = C.c_int
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_vp)
+
+
+class OracleLib:
+    def __init__(self, path):
+        self.path = path
+        lib = C.CDLL(path)
+        sig = {
+            "oro_create": (_vp, [_int, _int, _vp, _u64, _u32, _vp, _u64]),
+            "oro_destroy": (None, [_vp]),
+            "oro_max_depth": (_u32, [_vp]),
+            "oro_node_count": (_u64, [_vp]),
+            "oro_location_keys": (None, [_vp, _vp]),
+            "oro_export_nodes": (None, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+            "oro_range": (_vp, [_vp, _vp, _u64, _int, _dbl]),
+            "oro_pick": (_vp, [_vp, _vp, _u64, _dbl]),
+            "oro_frustum": (_vp, [_vp, _vp, _u64, _u64, _dbl]),
+            "oro_knn": (_vp, [_vp, _vp, _u64, _vp, _dbl, _dbl]),
+            "oro_ray": (_vp, [_vp, _vp, _u64, _dbl, _dbl, _dbl, _int]),
+            "oro_collide_self": (_vp, [_vp, _dbl]),
+            "oro_collide_pair": (_vp, [_vp, _vp, _dbl]),
+            "oro_res_nq": (_u64, [_vp]),
+            "oro_res_total": (_u64, [_vp]),
+            "oro_res_has_dist": (_int, [_vp]),
+            "oro_res_copy": (None, [_vp, _vp, _vp, _vp]),
+            "oro_res_free": (None, [_vp]),
+            "oro_time_create_points": (_dbl, [_vp, _u64, _u32, _u64, _int]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        if hasattr(lib, "oro_brute_collide"):
+            lib.oro_brute_collide.restype = _vp
+            lib.oro_brute_collide.argtypes = [_int, _vp, _u64, _dbl]
+        if hasattr(lib, "oro_collide_self_par"):
+            lib.oro_collide_self_par.restype = _vp
+            lib.oro_collide_self_par.argtypes = [_vp, _dbl]
+        self.lib = lib
+
+    # -------------------------------------------------------------- trees
+    def create(self, ent, kind, max_depth=0, box=None, max_elem=16):
+        ent = np.ascontiguousarray(ent)
+        scalar = 0 if ent.dtype == np.float64 else 1
+        if box is not None:
+            box = np.ascontiguousarray(box, dtype=ent.dtype)
+        n = ent.shape[0] if ent.size else 0
+        h = self.lib.oro_create(scalar, kind, _ptr(ent), n, max_depth, _ptr(box), max_elem)
+        return OracleTree(self, h, ent, kind)
+
+    def brute_collide(self, boxes, tol=-1.0):
+        boxes = np.ascontiguousarray(boxes)
+        scalar = 0 if boxes.dtype == np.float64 else 1
+        r = self.lib.oro_brute_collide(scalar, _ptr(boxes), boxes.shape[0], tol)
+        off, ids, _ = self._result(r)
+        return ids.reshape(-1, 2)
+
+    def _result(self, r):
+        nq = self.lib.oro_res_nq(r)
+        tot = self.lib.oro_res_total(r)
+        off = np.zeros(nq + 1, np.uint64)
+        ids = np.zeros(tot, np.uint32)
+        dist = np.zeros(tot, np.float64) if (self.lib.oro_res_has_dist(r) or tot == 0) else None
+        self.lib.oro_res_copy(r, _ptr(off), _ptr(ids), _ptr(dist))
+        self.lib.oro_res_free(r)
+        return off, ids, dist
+
+
+class OracleTree:
+    def __init__(self, owner, handle, ent, kind):
+        self.o = owner
+        self.lib = owner.lib
+        self.h = handle
+        self.ent = ent
+        self.kind = kind
+        self.n = ent.shape[0] if ent.size else 0
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.oro_destroy(self.h)
+            self.h = None
+
+    @property
+    def max_depth(self):
+        return self.lib.oro_max_depth(self.h)
+
+    @property
+    def node_count(self):
+        return self.lib.oro_node_count(self.h)
+
+    def location_keys(self):
+        out = np.zeros(self.n, np.uint64)
+        self.lib.oro_location_keys(self.h, _ptr(out))
+        return out
+
+    def nodes(self):
+        """Nodes sorted by key: keys, min (nn,3), size (nn,3), entity offsets, entity ids (ascending per node)."""
+        nn = self.node_count
+        keys = np.zeros(nn, np.uint64)
+        minp = np.zeros((nn, 3), np.float64)
+        size = np.zeros((nn, 3), np.float64)
+        eoff = np.zeros(nn + 1, np.uint64)
+        eids = np.zeros(max(self.n, 1), np.uint32)
+        self.lib.oro_export_nodes(self.h, _ptr(keys), _ptr(minp), _ptr(size), _ptr(eoff), _ptr(eids), None)
+        return dict(keys=keys, min=minp, size=size, eoff=eoff, eids=eids[: int(eoff[-1])])
+
+    def _q(self, arr):
+        return np.ascontiguousarray(arr, dtype=self.ent.dtype)
+
+    def range_search(self, ranges, mode=0, tol=-1.0):
+        ranges = self._q(ranges)
+        return self.o._result(self.lib.oro_range(self.h, _ptr(ranges), ranges.shape[0], mode, tol))[:2]
+
+    def pick_search(self, pts, tol=-1.0):
+        pts = self._q(pts)
+        return self.o._result(self.lib.oro_pick(self.h, _ptr(pts), pts.shape[0], tol))[:2]
+
+    def frustum(self, planes, tol=-1.0):
+        """planes: (nq, np, 4) as {origoDistance, nx, ny, nz}."""
+        planes = self._q(planes)
+        nq, np_ = planes.shape[0], planes.shape[1]
+        return self.o._result(self.lib.oro_frustum(self.h, _ptr(planes), np_, nq, tol))[:2]
+
+    def knn(self, pts, k, max_dist=-1.0, tol=-1.0):
+        pts = self._q(pts)
+        kk = np.ascontiguousarray(np.broadcast_to(np.asarray(k, np.uint32), (pts.shape[0],)))
+        return self.o._result(self.lib.oro_knn(self.h, _ptr(pts), pts.shape[0], _ptr(kk), max_dist, tol))
+
+    def ray(self, rays, first=False, tol=-1.0, tol_inc=0.0, max_dist=-1.0):
+        rays = self._q(rays)
+        return self.o._result(self.lib.oro_ray(self.h, _ptr(rays), rays.shape[0], tol, tol_inc, max_dist, int(first)))
+
+    def collide_self(self, tol=-1.0):
+        return self.o._result(self.lib.oro_collide_self(self.h, tol))[1].reshape(-1, 2)
+
+    def collide_self_par(self, tol=-1.0):
+        return self.o._result(self.lib.oro_collide_self_par(self.h, tol))[1].reshape(-1, 2)
+
+    def collide_pair(self, other, tol=-1.0):
+        return self.o._result(self.lib.oro_collide_pair(self.h, other.h, tol))[1].reshape(-1, 2)
+
+
+_cache = {}
+
+
+def oracle():
+    if "o" not in _cache:
+        if not os.path.exists(ORACLE_SO):
+            raise RuntimeError(f"oracle library missing: {ORACLE_SO} (run __graft_entry__.build())")
+        _cache["o"] = OracleLib(ORACLE_SO)
+    return _cache["o"]
+
+
+def reference():
+    """The reference itself (only where oracle/_ref was built from the reference sources)."""
+    if "r" not in _cache:
+        _cache["r"] = OracleLib(REF_SO) if os.path.exists(REF_SO) else None
+    return _cache["r"]

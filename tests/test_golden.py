@@ -1,0 +1,33 @@
+"""The CPU oracle (oracle/otg_oracle.hpp) against the golden fixtures produced by the reference
+itself (tests/golden/make_golden.py). This pins the restatement to the reference."""
+import numpy as np
+import pytest
+
+from _compare import assert_csr_equal, golden_cases, load_golden, node_dict
+from _oracle_lib import KIND_POINTS, oracle
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_oracle_matches_reference_fixture(name):
+    g = load_golden(name)
+    kind = int(g["kind"])
+    t = oracle().create(g["entities"], kind, int(g["max_depth"]), g.get("box"), int(g["max_elem"]))
+    assert t.max_depth == int(g["depth"])
+    assert np.array_equal(t.location_keys(), g["loc"])
+    nd = t.nodes()
+    ref = node_dict("node_", g)
+    for k in ("keys", "min", "size", "eoff", "eids"):
+        assert np.array_equal(nd[k], ref[k]), f"node field {k}"
+    for mode in (0, 1):
+        assert_csr_equal(t.range_search(g["ranges"], mode), (g[f"range{mode}_off"], g[f"range{mode}_ids"]), f"range{mode}")
+    assert_csr_equal(t.pick_search(g["qpts"]), (g["pick_off"], g["pick_ids"]), "pick")
+    assert_csr_equal(t.knn(g["qpts"], g["k"]), (g["knn_off"], g["knn_ids"], g["knn_dist"]), "knn")
+    assert_csr_equal(t.frustum(g["planes"]), (g["frustum_off"], g["frustum_ids"]), "frustum")
+    for first in (0, 1):
+        assert_csr_equal(
+            t.ray(g["rays"], first=bool(first), tol=float(g["ray_tol"])), (g[f"ray{first}_off"], g[f"ray{first}_ids"], g[f"ray{first}_dist"]), f"ray{first}"
+        )
+    if kind != KIND_POINTS:
+        assert np.array_equal(t.collide_self(), g["collide"])
+        t2 = oracle().create(g["other"], kind, int(g["max_depth"]), None, int(g["max_elem"]))
+        assert np.array_equal(t.collide_pair(t2), g["collide_pair"])

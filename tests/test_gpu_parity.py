@@ -1,0 +1,196 @@
+"""Parity of the CUDA path with the reference (golden fixtures) and with the CPU oracle on seeded
+inputs. Ids must match exactly; ray and kNN distances are compared bit-exact except where stated
+(the benchmark spec tolerance for ray hit distances: 1e-12 relative)."""
+import numpy as np
+import pytest
+
+import octree_gb300 as otg
+from _compare import assert_csr_equal, assert_dist_close, assert_nodes_equal, golden_cases, load_golden, node_dict
+from _oracle_lib import KIND_LOOSE_BOXES, KIND_POINTS, oracle
+
+pytestmark = pytest.mark.gpu
+
+RAY_REL = 1e-12
+
+
+def _gpu_tree(ent, kind, max_depth, box, max_elem):
+    t = otg.Tree("points" if kind == KIND_POINTS else "boxes", ent.dtype)
+    return t.create(ent, max_depth=max_depth, box=box, max_elements=max_elem)
+
+
+def _check_queries(t, o, q, kind, ray_tol, what):
+    for mode in (0, 1):
+        assert_csr_equal(t.range_search(q["ranges"], mode)[:2], o.range_search(q["ranges"], mode), f"{what} range{mode}")
+    assert_csr_equal(t.pick_search(q["qpts"])[:2], o.pick_search(q["qpts"]), f"{what} pick")
+    g = t.knn(q["qpts"], q["k"])
+    r = o.knn(q["qpts"], q["k"])
+    assert_csr_equal(g, r, f"{what} knn")
+    assert_csr_equal(t.frustum_culling(q["planes"])[:2], o.frustum(q["planes"]), f"{what} frustum")
+    for first in (False, True):
+        g = t.ray_first(q["rays"], tol=ray_tol) if first else t.ray_all(q["rays"], tol=ray_tol)
+        r = o.ray(q["rays"], first=first, tol=ray_tol)
+        assert_csr_equal(g[:2], r[:2], f"{what} ray first={first}")
+        assert_dist_close(g[2], r[2], RAY_REL, f"{what} ray first={first}")
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_gpu_matches_reference_fixture(name):
+    g = load_golden(name)
+    kind = int(g["kind"])
+    t = _gpu_tree(g["entities"], kind, int(g["max_depth"]), g.get("box"), int(g["max_elem"]))
+    assert t.max_depth == int(g["depth"])
+    assert np.array_equal(t.location_keys(), g["loc"])
+    assert_nodes_equal(t.nodes(), node_dict("node_", g), name)
+    for mode in (0, 1):
+        assert_csr_equal(t.range_search(g["ranges"], mode)[:2], (g[f"range{mode}_off"], g[f"range{mode}_ids"]), f"range{mode}")
+    assert_csr_equal(t.pick_search(g["qpts"])[:2], (g["pick_off"], g["pick_ids"]), "pick")
+    assert_csr_equal(t.knn(g["qpts"], g["k"]), (g["knn_off"], g["knn_ids"], g["knn_dist"]), "knn")
+    assert_csr_equal(t.frustum_culling(g["planes"])[:2], (g["frustum_off"], g["frustum_ids"]), "frustum")
+    for first in (0, 1):
+        fn = t.ray_first if first else t.ray_all
+        res = fn(g["rays"], tol=float(g["ray_tol"]))
+        assert_csr_equal(res[:2], (g[f"ray{first}_off"], g[f"ray{first}_ids"]), f"ray{first}")
+        assert_dist_close(res[2], g[f"ray{first}_dist"], RAY_REL, f"ray{first}")
+    if kind != KIND_POINTS:
+        assert np.array_equal(t.collision_self(), g["collide"])
+        t2 = _gpu_tree(g["other"], kind, int(g["max_depth"]), None, int(g["max_elem"]))
+        assert np.array_equal(t.collision_pair(t2), g["collide_pair"])
+
+
+def _queries(rng, dtype, scale, nq=400):
+    c = rng.random((nq, 3)) * scale * 1.1 - 0.05 * scale
+    e = rng.random((nq, 3)) * 0.06 * scale
+    ranges = np.concatenate([c - e, c + e], 1).astype(dtype)
+    pts = (rng.random((nq, 3)) * scale).astype(dtype)
+    k = rng.integers(1, 65, nq).astype(np.uint32)
+    nrm = rng.normal(size=(16, 6, 3))
+    nrm /= np.linalg.norm(nrm, axis=2, keepdims=True)
+    planes = np.concatenate([rng.random((16, 6, 1)) * scale * 0.6 - 0.3 * scale, nrm], 2).astype(dtype)
+    dirs = rng.normal(size=(nq, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    rays = np.concatenate([rng.random((nq, 3)) * scale, dirs], 1).astype(dtype)
+    return dict(ranges=ranges, qpts=pts, k=k, planes=planes, rays=rays)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("max_depth,max_elem", [(10, 20), (0, 16), (5, 4), (19, 32)])
+def test_points_random(dtype, max_depth, max_elem):
+    rng = np.random.default_rng(max_depth * 100 + max_elem)
+    pts = (rng.random((200_000, 3)) * 100).astype(dtype)
+    t = _gpu_tree(pts, KIND_POINTS, max_depth, None, max_elem)
+    o = oracle().create(pts, KIND_POINTS, max_depth, None, max_elem)
+    assert t.max_depth == o.max_depth
+    assert np.array_equal(t.location_keys(), o.location_keys())
+    assert_nodes_equal(t.nodes(), o.nodes(), "points")
+    _check_queries(t, o, _queries(rng, dtype, 100), KIND_POINTS, 0.05, "points")
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("max_depth,max_elem", [(8, 32), (0, 16), (4, 2)])
+def test_boxes_random(dtype, max_depth, max_elem):
+    rng = np.random.default_rng(7 + max_depth + max_elem)
+    n = 60_000
+    cen = np.where(rng.random((n, 1)) < 0.5, rng.random((n, 3)) * 1000, rng.normal(500, 10, (n, 3)))
+    half = rng.lognormal(np.log(0.5), 0.6, (n, 3))
+    boxes = np.concatenate([cen - half, cen + half], 1).astype(dtype)
+    t = _gpu_tree(boxes, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    o = oracle().create(boxes, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    assert np.array_equal(t.location_keys(), o.location_keys())
+    assert_nodes_equal(t.nodes(), o.nodes(), "boxes")
+    _check_queries(t, o, _queries(rng, dtype, 1000), KIND_LOOSE_BOXES, 0.0, "boxes")
+    assert np.array_equal(t.collision_self(), o.collide_self())
+    other = boxes.copy()
+    other += dtype(0.4)
+    t2 = _gpu_tree(other, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    o2 = oracle().create(other, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    assert np.array_equal(t.collision_pair(t2), o.collide_pair(o2))
+
+
+EDGE_CASES = {
+    "single": (np.array([[1.0, 2.0, 3.0]]), KIND_POINTS, None),
+    "two_equal": (np.array([[1.0, 2.0, 3.0], [1.0, 2.0, 3.0]]), KIND_POINTS, None),
+    "duplicates": (np.repeat(np.random.default_rng(3).random((40, 3)) * 10, 25, axis=0), KIND_POINTS, None),
+    "flat": (np.c_[np.random.default_rng(4).random((3000, 2)) * 10, np.zeros(3000)], KIND_POINTS, None),
+    "outside_box": (np.random.default_rng(5).random((3000, 3)) * 100, KIND_POINTS, np.array([10.0, 10, 10, 60, 60, 60])),
+    "negative": (np.random.default_rng(6).random((3000, 3)) * 200 - 100, KIND_POINTS, None),
+    "tiny_extent": (np.random.default_rng(8).random((3000, 3)) * 1e-9 + 1e5, KIND_POINTS, None),
+}
+
+
+def _edge_boxes():
+    rng = np.random.default_rng(9)
+    cen = rng.random((2000, 3)) * 50
+    hh = rng.random((2000, 3)) * 4
+    b = np.concatenate([cen - hh, cen + hh], 1)
+    span = b.copy()
+    span[0] = [b[:, 0].min(), b[:, 1].min(), b[:, 2].min(), b[:, 3].max(), b[:, 4].max(), b[:, 5].max()]
+    corner = b.copy()
+    corner[1] = [50, 50, 50, 50, 50, 50]
+    corner[2] = [0, 0, 0, 0, 0, 0]
+    return {
+        "boxes_degenerate": (np.concatenate([cen, cen], 1), KIND_LOOSE_BOXES, None),
+        "box_spans_space": (span, KIND_LOOSE_BOXES, None),
+        "boxes_on_max_corner": (corner, KIND_LOOSE_BOXES, np.array([0.0, 0, 0, 50, 50, 50])),
+        "boxes_outside_box": (b, KIND_LOOSE_BOXES, np.array([10.0, 10, 10, 40, 40, 40])),
+    }
+
+
+@pytest.mark.parametrize("name", list(EDGE_CASES) + list(_edge_boxes()))
+@pytest.mark.parametrize("max_depth,max_elem", [(0, 1), (3, 4), (10, 16)])
+def test_edge_cases(name, max_depth, max_elem):
+    ent, kind, box = {**EDGE_CASES, **_edge_boxes()}[name]
+    t = _gpu_tree(ent, kind, max_depth, box, max_elem)
+    o = oracle().create(ent, kind, max_depth, box, max_elem)
+    assert np.array_equal(t.location_keys(), o.location_keys())
+    assert_nodes_equal(t.nodes(), o.nodes(), name)
+    rng = np.random.default_rng(11)
+    lo = ent[:, :3].min(0)
+    hi = ent[:, 3:].max(0) if kind != KIND_POINTS else ent.max(0)
+    span = np.maximum(hi - lo, 1e-12)
+    c = lo + rng.random((64, 3)) * span
+    e = rng.random((64, 3)) * span * 0.2
+    ranges = np.concatenate([c - e, c + e], 1)
+    ranges[0] = np.concatenate([lo - 1, hi + 1])  # whole-tree range: root shortcut
+    ranges[1] = np.concatenate([c[1], c[1]])  # zero volume
+    for mode in (0, 1):
+        assert_csr_equal(t.range_search(ranges, mode)[:2], o.range_search(ranges, mode), f"{name} range{mode}")
+    q = np.concatenate([ent[:16, :3], c[:16]])
+    assert_csr_equal(t.knn(q, 5), o.knn(q, 5), f"{name} knn")
+    assert_csr_equal(t.pick_search(q)[:2], o.pick_search(q), f"{name} pick")
+    if kind != KIND_POINTS:
+        assert np.array_equal(t.collision_self(), o.collide_self())
+
+
+def test_empty_tree():
+    t = otg.Tree("points").create(np.zeros((0, 3)))
+    off, ids, _ = t.range_search(np.array([[0.0, 0, 0, 1, 1, 1]]))
+    assert len(ids) == 0 and off.tolist() == [0, 0]
+    off, ids, d = t.knn(np.array([[0.0, 0, 0]]), 3)
+    assert len(ids) == 0
+    tb = otg.Tree("boxes").create(np.zeros((0, 6)))
+    assert tb.collision_self().shape == (0, 2)
+
+
+def test_knn_max_distance_and_ties():
+    rng = np.random.default_rng(12)
+    pts = np.round(rng.random((20000, 3)) * 30)  # many exact ties
+    t = _gpu_tree(pts, KIND_POINTS, 6, None, 8)
+    o = oracle().create(pts, KIND_POINTS, 6, None, 8)
+    q = np.round(rng.random((200, 3)) * 30) + 0.5
+    for md in (-1.0, 0.75, 2.0):
+        assert_csr_equal(t.knn(q, 7, max_distance=md), o.knn(q, 7, max_dist=md), f"knn maxdist {md}")
+
+
+def test_device_inputs_match_host_inputs():
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(13)
+    pts = rng.random((100_000, 3)) * 100
+    th = otg.Tree("points").create(pts, max_depth=9, max_elements=20)
+    td = otg.Tree("points").create(torch.as_tensor(pts, device="cuda"), max_depth=9, max_elements=20)
+    td.sync()
+    assert np.array_equal(th.location_keys(), td.location_keys())
+    c = rng.random((100, 3)) * 100
+    ranges = np.concatenate([c - 2, c + 2], 1)
+    a = th.range_search(ranges)
+    b = td.range_search(torch.as_tensor(ranges, device="cuda"))
+    assert_csr_equal(a[:2], b[:2], "device input")

@@ -1,0 +1,51 @@
+"""Random seeded cases: the CPU oracle against the reference library itself. Runs only where the
+reference harness was built from the reference sources (oracle/_ref); elsewhere it is skipped and
+the committed golden fixtures carry the pin."""
+import numpy as np
+import pytest
+
+from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, oracle, reference
+
+pytestmark = pytest.mark.skipif(reference() is None, reason="reference harness not built here")
+
+
+def _same_tree(a, b):
+    na, nb = a.nodes(), b.nodes()
+    return a.max_depth == b.max_depth and np.array_equal(a.location_keys(), b.location_keys()) and all(np.array_equal(na[k], nb[k]) for k in na)
+
+
+@pytest.mark.parametrize("seed", range(4))
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_random_points(seed, dtype):
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(50, 4000))
+    pts = (rng.random((n, 3)) * 100).astype(dtype)
+    D = int(rng.integers(0, 9))
+    me = int(rng.integers(1, 24))
+    a, b = oracle().create(pts, KIND_POINTS, D, None, me), reference().create(pts, KIND_POINTS, D, None, me)
+    assert _same_tree(a, b)
+    c = rng.random((100, 3)) * 100
+    e = rng.random((100, 3)) * 8
+    ranges = np.concatenate([c - e, c + e], 1).astype(dtype)
+    for x, y in zip(a.range_search(ranges), b.range_search(ranges)):
+        assert np.array_equal(x, y)
+    q = (rng.random((100, 3)) * 100).astype(dtype)
+    k = rng.integers(1, 30, 100).astype(np.uint32)
+    for x, y in zip(a.knn(q, k), b.knn(q, k)):
+        assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("seed", range(3))
+@pytest.mark.parametrize("kind", [KIND_LOOSE_BOXES, KIND_BOXES])
+def test_random_boxes(seed, kind):
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(50, 2500))
+    cen = rng.random((n, 3)) * 100
+    half = rng.random((n, 3)) * 3
+    boxes = np.concatenate([cen - half, cen + half], 1)
+    D = int(rng.integers(0, 7))
+    me = int(rng.integers(1, 20))
+    a, b = oracle().create(boxes, kind, D, None, me), reference().create(boxes, kind, D, None, me)
+    assert _same_tree(a, b)
+    assert np.array_equal(a.collide_self(), b.collide_self())
+    assert np.array_equal(b.collide_self(), b.collide_self_par())
