@@ -380,7 +380,7 @@ template<typename T, typename K, bool IS_BOX>
 __global__ void __launch_bounds__(256) emit_level_kernel(u32 d, u64 maxElem, const K* __restrict__ keys, uint4* __restrict__ link,
                                                          u64* __restrict__ nodeKey, T* __restrict__ nodeBox, unsigned char* __restrict__ nodeDepth,
                                                          u32* __restrict__ levelCount, const Space<T>* __restrict__ spg, u64 maxNodes,
-                                                         u32* __restrict__ err)
+                                                         u32* __restrict__ err, u32* __restrict__ ownerNode, u32* __restrict__ nodeParent)
 {
   __shared__ Space<T> s;
   if (threadIdx.x == 0)
@@ -465,9 +465,14 @@ __global__ void __launch_bounds__(256) emit_level_kernel(u32 d, u64 maxElem, con
           nodeKey[ci] = (key << 3) | u64(c);
           link[ci] = make_uint4(0, bounds[c], bounds[c], bounds[c + 1]);
           nodeDepth[ci] = (unsigned char)(d + 1);
+          if (nodeParent)
+            nodeParent[ci] = node;
         }
       }
       link[node] = make_uint4((nchild ? (firstChild & kFirstChildMask) : 0u) | (nchild << kChildShift), b, ownEnd, e);
+      if (ownerNode)
+        for (u32 q = b; q < ownEnd; ++q)
+          ownerNode[q] = node;
       if constexpr (!IS_BOX)
       {
         T mn[3];
@@ -632,7 +637,8 @@ static int build_impl(TreeState& t, const void* box, u64 n, cudaStream_t st)
       (e = t.nodeKey.ensure(sizeof(u64) * maxNodes)) || (e = t.nodeBox.ensure(sizeof(T) * 6 * maxNodes)) ||
       (e = t.nodeDepth.ensure(maxNodes)) || (e = t.levelCount.ensure(sizeof(u32) * 32)) || (e = t.space.ensure(sizeof(Space<T>))) ||
       (e = t.sortScratch.ensure(SortScratch::bytes(n, passes))) || (e = t.bboxBits.ensure(sizeof(B) * 6)) ||
-      (IS_BOX && (e = t.nodeMax.ensure(sizeof(T) * 3 * maxNodes))))
+      (IS_BOX && ((e = t.nodeMax.ensure(sizeof(T) * 3 * maxNodes)) || (e = t.ownerNode.ensure(sizeof(u32) * n)) ||
+                  (e = t.nodeParent.ensure(sizeof(u32) * maxNodes)))))
     return cuda_status(e, "allocating tree buffers");
 
   Profiler& prof = profiler();
@@ -679,7 +685,8 @@ static int build_impl(TreeState& t, const void* box, u64 n, cudaStream_t st)
   const int emitBlocks = grid_blocks(n / std::max<u64>(1, t.maxElem / 2), 256, 152 * 4);
   for (u32 d = 0; d <= D; ++d)
     emit_level_kernel<T, K, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, t.maxElem, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
-                                                                t.nodeDepth.as<unsigned char>(), t.levelCount.as<u32>(), sp, maxNodes, t.err.as<u32>());
+                                                                t.nodeDepth.as<unsigned char>(), t.levelCount.as<u32>(), sp, maxNodes, t.err.as<u32>(),
+                                                                IS_BOX ? t.ownerNode.as<u32>() : nullptr, IS_BOX ? t.nodeParent.as<u32>() : nullptr);
   prof.mark("geometry", st);
   if constexpr (IS_BOX)
   {

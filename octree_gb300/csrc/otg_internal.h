@@ -11,6 +11,8 @@
 //   nodeBox      T[M*6]     {min xyz, size xyz} exactly as GetNodeMinPoint / GetNodeSize
 //   nodeMax      T[M*3]     exact max corner of box-tree MBRs (for conservative pruning)
 //   nodeDepth    u8[M]
+//   nodeParent   u32[M]     (box trees) parent node index
+//   ownerNode    u32[N]     (box trees) node that holds the entity at each sorted position
 // Nodes are stored breadth-first; the children of a node are contiguous.
 #pragma once
 
@@ -24,10 +26,32 @@
 namespace otg
 {
 
+// Owning device allocation (move-only; freed on destruction).
 struct DevBuf
 {
   void* p = nullptr;
   size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes)
+  {
+    o.p = nullptr;
+    o.bytes = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept
+  {
+    if (this != &o)
+    {
+      release();
+      p = o.p;
+      bytes = o.bytes;
+      o.p = nullptr;
+      o.bytes = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
   cudaError_t ensure(size_t need)
   {
     if (need <= bytes)
@@ -72,6 +96,8 @@ struct TreeState
 
   DevBuf entities, sortedIds, sortedGeom, keysA, keysB, valsB;
   DevBuf nodeLink, nodeKey, nodeBox, nodeMax, nodeDepth;
+  DevBuf ownerNode; // u32 per sorted position: the node holding that entity (box trees)
+  DevBuf nodeParent; // u32 per node (box trees)
   DevBuf levelCount; // u32[32]: nodes per depth
   DevBuf space;      // Space<T>
   DevBuf sortScratch;

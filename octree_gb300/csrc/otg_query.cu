@@ -686,7 +686,7 @@ __global__ void __launch_bounds__(128) collide_plain_kernel(TreeView<T> ta, Tree
       T b[6];
       load_box(tb.geom + u64(e) * 6, b);
       if (G::box_relation(a, b, tol) == -1)
-        out.put(idA, idB);
+        out.put(i, e); // sorted positions; collide_filter_kernel maps them to ids
     }
     const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
     if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tb.nNodes) || ++visits > tb.nNodes)
@@ -696,6 +696,107 @@ __global__ void __launch_bounds__(128) collide_plain_kernel(TreeView<T> ta, Tree
     }
     for (u32 c = 0; c < cc; ++c)
       stack[sp++] = fc + c;
+  }
+}
+
+// ---------------------------------------------------------------- collision structure filter
+// The reference compares an overlapping pair only if its tree walk reaches the pair's two nodes,
+// and that walk prunes with AreBoxesOverlappingByMinPoint on node boxes (min, min + size) with the
+// tolerance. For strictly overlapping boxes those tests pass except at rounding level, which in
+// float trees with coordinates far above the tolerance does happen. This filter applies the walk's
+// conditions to every candidate pair exactly:
+//   same node          InsertCollidedEntitiesInsideNode: always compared (ot_query.h:1518-1561)
+//   ancestor entity p   InsertCollidedEntitiesWithParents: p.minX <= node.Box.Max[0] and
+//                       AreBoxesOverlappingByMinPoint(node, p) (ot_query.h:1563-1653)
+//   sibling subtrees    two-tree walk from the sibling pair (first pair untested), then every
+//                       descent pair tested (ot_query.h:1308-1458, called at :1672-1684)
+//   two trees           the same walk from the two roots (ot_query.h:1462-1485)
+template<typename T>
+struct StructTree
+{
+  const T* nodeBox;
+  const u32* owner;
+  const u32* parent;
+  const unsigned char* depth;
+  const T* geom;
+  const u32* ids;
+};
+
+template<typename T>
+__device__ __forceinline__ int ancestors(const StructTree<T>& t, u32 x, u32* anc)
+{
+  int d = t.depth[x];
+  if (d > 20)
+    d = 20;
+  anc[d] = x;
+  for (int k = d; k > 0; --k)
+    anc[k - 1] = t.parent[anc[k]];
+  return d;
+}
+
+template<typename T>
+__device__ __forceinline__ bool node_overlap(const StructTree<T>& ta, u32 a, const StructTree<T>& tb, u32 b, T tol)
+{
+  const T* na = ta.nodeBox + u64(a) * 6;
+  const T* nb = tb.nodeBox + u64(b) * 6;
+  return GeoD<T>::overlap_by_min_point(na, na + 3, nb, nb + 3, tol);
+}
+
+template<typename T>
+__device__ __forceinline__ bool with_parent_condition(const StructTree<T>& t, u32 node, const T* p, T tol)
+{
+  const T* nb = t.nodeBox + u64(node) * 6;
+  const T boxMax0 = nb[0] + nb[3];
+  if (p[0] > boxMax0)
+    return false;
+  T psize[3] = { T(p[3] - p[0]), T(p[4] - p[1]), T(p[5] - p[2]) };
+  return GeoD<T>::overlap_by_min_point(nb, nb + 3, p, psize, tol);
+}
+
+template<typename T>
+__global__ void __launch_bounds__(128) collide_filter_kernel(StructTree<T> A, StructTree<T> B, int selfMode, const u64* __restrict__ pairs, u64 m, T tol,
+                                                             u64* __restrict__ keys, unsigned long long* rejected)
+{
+  for (u64 idx = blockIdx.x * u64(blockDim.x) + threadIdx.x; idx < m; idx += u64(gridDim.x) * blockDim.x)
+  {
+    const u64 it = pairs[idx];
+    const u32 i = u32(it >> 32), j = u32(it);
+    const u32 xa = A.owner[i], xb = B.owner[j];
+    u32 ancA[21], ancB[21];
+    bool keep = true;
+    if (!(selfMode && xa == xb))
+    {
+      const int da = ancestors(A, xa, ancA);
+      const int db = ancestors(B, xb, ancB);
+      if (selfMode)
+      {
+        int dn = 0;
+        while (dn + 1 <= min(da, db) && ancA[dn + 1] == ancB[dn + 1])
+          ++dn;
+        if (dn == da)
+          keep = with_parent_condition(A, xb, A.geom + u64(i) * 6, tol);
+        else if (dn == db)
+          keep = with_parent_condition(A, xa, A.geom + u64(j) * 6, tol);
+        else
+          for (int k = dn + 2; k <= max(da, db) && keep; ++k)
+            keep = node_overlap(A, ancA[min(k, da)], A, ancB[min(k, db)], tol);
+      }
+      else
+      {
+        for (int k = 1; k <= max(da, db) && keep; ++k)
+          keep = node_overlap(A, ancA[min(k, da)], B, ancB[min(k, db)], tol);
+      }
+    }
+    u32 idA = A.ids[i], idB = B.ids[j];
+    if (selfMode && idA > idB)
+    {
+      u32 t = idA;
+      idA = idB;
+      idB = t;
+    }
+    keys[idx] = keep ? ((u64(idA) << 32) | idB) : ~0ull;
+    if (!keep)
+      atomicAdd(rejected, 1ull);
   }
 }
 
@@ -1190,6 +1291,13 @@ static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, do
 }
 
 template<typename T>
+static StructTree<T> struct_view(const TreeState& t)
+{
+  return StructTree<T>{ t.nodeBox.as<T>(), t.ownerNode.as<u32>(), t.nodeParent.as<u32>(), t.nodeDepth.as<unsigned char>(), t.sortedGeom.as<T>(),
+                        t.sortedIds.as<u32>() };
+}
+
+template<typename T>
 static int collide_impl(const TreeState& a, const TreeState& b, bool self, double tol, int algo, ResultState& r, cudaStream_t st)
 {
   if (a.n == 0 || b.n == 0)
@@ -1212,12 +1320,34 @@ static int collide_impl(const TreeState& a, const TreeState& b, bool self, doubl
     st);
   if (rc)
     return rc;
-  rc = finish_pairs(c, r, st);
+  const u64 m = c.m;
+  DevBuf keys, rej;
+  cudaError_t e;
+  if ((e = keys.ensure(sizeof(u64) * std::max<u64>(m, 1))) || (e = rej.ensure(sizeof(unsigned long long))))
+    return cuda_status(e, "allocating pair filter");
+  cudaMemsetAsync(rej.p, 0, sizeof(unsigned long long), st);
+  if (m)
+    collide_filter_kernel<T><<<blocks_for(m, 128), 128, 0, st>>>(struct_view<T>(a), struct_view<T>(b), self ? 1 : 0, c.items.as<u64>(), m, tl,
+                                                                  keys.as<u64>(), rej.as<unsigned long long>());
+  unsigned long long rejected = 0;
+  e = cudaMemcpyAsync(&rejected, rej.p, sizeof(rejected), cudaMemcpyDeviceToHost, st);
+  if (!e)
+    e = cudaStreamSynchronize(st);
+  if (e)
+    return cuda_status(e, "filtering pairs");
+  std::swap(c.items, keys);
+  rc = finish_pairs(c, r, st); // rejected pairs carry key ~0 and sort last
   if (rc)
     return rc;
-  if (c.m)
-    swap_pair_halves_kernel<<<blocks_for(c.m), 256, 0, st>>>(r.ids.as<u32>(), c.m);
-  return cuda_status(cudaStreamSynchronize(st), "finishing pairs");
+  const u64 kept = m - rejected;
+  r.nids = 2 * kept;
+  u64 offs[2] = { 0, 2 * kept };
+  e = cudaMemcpyAsync(r.offsets.p, offs, sizeof(offs), cudaMemcpyHostToDevice, st);
+  if (!e && kept)
+    swap_pair_halves_kernel<<<blocks_for(kept), 256, 0, st>>>(r.ids.as<u32>(), kept);
+  if (!e)
+    e = cudaStreamSynchronize(st);
+  return cuda_status(e, "finishing pairs");
 }
 
 int query_range(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
