@@ -4,9 +4,10 @@
 //   1. space box: given, or the entities' bounding box (IGM::GetBoundingBoxAD,
 //      detail/internal_geometry_module.h:342-370)                       -> bbox_kernel
 //   2. grid factors and MinPoint node sizes (detail/si_grid.h:65-103,
-//      core/ot_base.h:121-134)                                             -> space_setup_kernel
+//      core/ot_base.h:121-134), exact rasterisation thresholds and the
+//      MinPoint node table (otg_raster.cuh)                              -> space_setup / raster_tables / node_min_table
 //   3. one location key per entity (si_mortongrid.h:69-97) fused with the radix digit
-//      histograms of the sort                                              -> codegen_*_kernel
+//      histograms of the sort; integer compares against the thresholds   -> codegen_kernel
 //   4. stable radix sort of (key, id) (replaces std::sort(par), :791-796)  -> otg_sort.cuh
 //   5. entities gathered into tree order                                   -> gather_kernel
 //   6. node emission, one launch per depth (BuildSubtree/ProcessNode,
@@ -22,6 +23,7 @@
 //           reference stores in the root, si_mortongrid.h:57-62). 3*D + 1 bits.
 //   boxes : key = loc << 5 | depth. 3*D + 5 bits.
 #include "otg_internal.h"
+#include "otg_raster.cuh"
 #include "otg_sort.cuh"
 
 #include <algorithm>
@@ -31,41 +33,75 @@
 namespace otg
 {
 
-template<typename T>
-struct OrderedBits;
-template<>
-struct OrderedBits<double>
+// entities handled per thread step: 48 bytes = three 16-byte vector loads
+template<typename T, int W>
+struct Chunk
 {
-  using type = unsigned long long;
+  static constexpr int E = 48 / int(sizeof(T) * W);
+  static_assert(E >= 1 && E * int(sizeof(T)) * W == 48, "chunk must be 48 bytes");
 };
-template<>
-struct OrderedBits<float>
+
+// loads entities [first, first + E) (clipped at n) into v; vector loads when aligned and whole.
+// Every index is a compile-time constant after unrolling, so v stays in registers.
+template<typename T, int W>
+__device__ __forceinline__ int load_chunk(const T* __restrict__ ent, u64 n, u64 first, bool vec, T (&v)[Chunk<T, W>::E * W])
 {
-  using type = unsigned int;
-};
+  constexpr int E = Chunk<T, W>::E;
+  if (vec && first + E <= n)
+  {
+    const float4* src = reinterpret_cast<const float4*>(ent + first * W);
+    union
+    {
+      float4 f[3];
+      T t[E * W];
+    } u;
+    u.f[0] = __ldg(src);
+    u.f[1] = __ldg(src + 1);
+    u.f[2] = __ldg(src + 2);
+#pragma unroll
+    for (int k = 0; k < E * W; ++k)
+      v[k] = u.t[k];
+    return E;
+  }
+  const int cnt = int(min(u64(E), n - first));
+#pragma unroll
+  for (int k = 0; k < E * W; ++k)
+    v[k] = (k < cnt * W) ? ent[first * W + k] : T(0);
+  return cnt;
+}
 
 // ---------------------------------------------------------------- 1. bounding box
 template<typename T, int W>
-__global__ void __launch_bounds__(256) bbox_kernel(const T* __restrict__ ent, u64 n, typename OrderedBits<T>::type* acc)
+__global__ void __launch_bounds__(256) bbox_kernel(const T* __restrict__ ent, u64 n, bool vec, typename Ord<T>::U* acc)
 {
-  using B = typename OrderedBits<T>::type;
-  B mn[3], mx[3];
+  using O = Ord<T>;
+  using U = typename O::U;
+  constexpr int E = Chunk<T, W>::E;
+  U mn[3], mx[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d)
   {
-    mn[d] = B(~B(0));
-    mx[d] = B(0);
+    mn[d] = U(~U(0));
+    mx[d] = U(0);
   }
-  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < n; i += u64(gridDim.x) * blockDim.x)
+  const u64 chunks = (n + E - 1) / E;
+  for (u64 c = blockIdx.x * u64(blockDim.x) + threadIdx.x; c < chunks; c += u64(gridDim.x) * blockDim.x)
   {
-    const T* e = ent + i * W;
+    T v[E * W];
+    const int cnt = load_chunk<T, W>(ent, n, c * E, vec, v);
 #pragma unroll
-    for (int d = 0; d < 3; ++d)
+    for (int k = 0; k < E; ++k)
     {
-      B lo = ordered_bits(e[d]);
-      B hi = ordered_bits(e[W == 6 ? 3 + d : d]);
-      mn[d] = lo < mn[d] ? lo : mn[d];
-      mx[d] = hi > mx[d] ? hi : mx[d];
+      if (k >= cnt)
+        break;
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+      {
+        U lo = O::of(v[k * W + d]);
+        U hi = O::of(v[k * W + (W == 6 ? 3 + d : d)]);
+        mn[d] = lo < mn[d] ? lo : mn[d];
+        mx[d] = hi > mx[d] ? hi : mx[d];
+      }
     }
   }
 #pragma unroll
@@ -74,8 +110,8 @@ __global__ void __launch_bounds__(256) bbox_kernel(const T* __restrict__ ent, u6
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
     {
-      B a = __shfl_xor_sync(0xffffffffu, mn[d], o);
-      B b = __shfl_xor_sync(0xffffffffu, mx[d], o);
+      U a = __shfl_xor_sync(0xffffffffu, mn[d], o);
+      U b = __shfl_xor_sync(0xffffffffu, mx[d], o);
       mn[d] = a < mn[d] ? a : mn[d];
       mx[d] = b > mx[d] ? b : mx[d];
     }
@@ -91,22 +127,21 @@ __global__ void __launch_bounds__(256) bbox_kernel(const T* __restrict__ ent, u6
   }
 }
 
-template<typename T>
-__global__ void bbox_init_kernel(typename OrderedBits<T>::type* acc)
+template<typename U>
+__global__ void bbox_init_kernel(U* acc)
 {
-  using B = typename OrderedBits<T>::type;
   int d = threadIdx.x;
   if (d < 3)
   {
-    acc[d] = B(~B(0));
-    acc[3 + d] = B(0);
+    acc[d] = U(~U(0));
+    acc[3 + d] = U(0);
   }
 }
 
 // ---------------------------------------------------------------- 2. space
 // si_grid.h:65-103 (factors), ot_base.h:121-134 (MinPoint node size table)
 template<typename T>
-__global__ void space_setup_kernel(Space<T>* sp, const typename OrderedBits<T>::type* acc, const T* box, u32 D, int isPoints)
+__global__ void space_setup_kernel(Space<T>* sp, const typename Ord<T>::U* acc, const T* box, u32 D, int isPoints)
 {
   if (threadIdx.x != 0 || blockIdx.x != 0)
     return;
@@ -120,8 +155,8 @@ __global__ void space_setup_kernel(Space<T>* sp, const typename OrderedBits<T>::
     }
     else
     {
-      s.min[d] = from_ordered_bits(acc[d]);
-      s.max[d] = from_ordered_bits(acc[3 + d]);
+      s.min[d] = Ord<T>::val(acc[d]);
+      s.max[d] = Ord<T>::val(acc[3 + d]);
     }
     s.size[d] = s.max[d] - s.min[d];
   }
@@ -139,6 +174,9 @@ __global__ void space_setup_kernel(Space<T>* sp, const typename OrderedBits<T>::
     s.rastF[d] = s.rsizeF[d] == 0 ? 1.0f : (subF / s.rsizeF[d]);
   }
   s.rasterDouble = (sizeof(T) == 8 || D >= 16) ? 1u : 0u;
+  for (u32 d = 0; d < 22; ++d)
+    for (int c = 0; c < 3; ++c)
+      s.nodeSize[d][c] = T(0);
   if (isPoints)
   {
     T lf = T(1.0);
@@ -150,58 +188,29 @@ __global__ void space_setup_kernel(Space<T>* sp, const typename OrderedBits<T>::
 }
 
 // ---------------------------------------------------------------- 3. location keys
-template<typename R, typename T>
-struct Raster;
-template<typename T>
-struct Raster<double, T>
-{
-  static __device__ __forceinline__ double rsize(const Space<T>& s, int d) { return s.rsizeD[d]; }
-  static __device__ __forceinline__ double rast(const Space<T>& s, int d) { return s.rastD[d]; }
-  static __device__ __forceinline__ double derast(const Space<T>& s, int d) { return s.derastD[d]; }
-};
-template<typename T>
-struct Raster<float, T>
-{
-  static __device__ __forceinline__ float rsize(const Space<T>& s, int d) { return s.rsizeF[d]; }
-  static __device__ __forceinline__ float rast(const Space<T>& s, int d) { return s.rastF[d]; }
-  static __device__ __forceinline__ float derast(const Space<T>& s, int d) { return s.derastF[d]; }
-};
-
-__device__ __forceinline__ u32 to_grid(double v) { return u32(v); } // C++ truncation
-__device__ __forceinline__ u32 to_grid(float v) { return u32(v); }
-
+// Reference formulas, one entity (used for exports; the build uses the threshold tables).
 // si_grid.h:145-175 GetPointGridID + si_morton.h Encode -> key (loc + 1, or 0 when outside)
 template<typename T, typename R>
-__device__ __forceinline__ u64 point_key(const T* p, const Space<T>& s, u32 maxRasterID)
+__device__ __forceinline__ u64 point_key_ref(const T* p, const Space<T>& s, u32 maxRasterID)
 {
-  const T tol = base_tol<T>();
   u32 g[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d)
   {
-    T pc = T(p[d]) - s.min[d];
-    R rs = Raster<R, T>::rsize(s, d);
-    if (pc < -tol || pc > rs + R(tol))
+    if (point_below_ref<T, R>(p[d], s, d) || point_above_ref<T, R>(p[d], s, d))
       return 0;
-    if (pc <= 0)
-      g[d] = 0;
-    else
-    {
-      u32 rid = to_grid(R(pc) * Raster<R, T>::rast(s, d));
-      g[d] = rid < maxRasterID ? rid : maxRasterID;
-    }
+    g[d] = point_cell_ref<T, R>(p[d], s, d, maxRasterID);
   }
   return encode3(g[0], g[1], g[2]) + 1;
 }
 
 // si_grid.h:221-285 GetLooseBoxGridData<2.0> + si_mortongrid.h:78-88 -> loc << 5 | depth
 template<typename T, typename R>
-__device__ __forceinline__ u64 loose_box_key(const T* b, const Space<T>& s, u32 D)
+__device__ __forceinline__ u64 loose_box_key_ref(const T* b, const Space<T>& s, u32 D)
 {
   const T tol = base_tol<T>();
-  // DoesRangeContainBoxAD(space, box, tol), internal_geometry_module.h:214-225
 #pragma unroll
-  for (int d = 0; d < 3; ++d)
+  for (int d = 0; d < 3; ++d) // DoesRangeContainBoxAD(space, box, tol), internal_geometry_module.h:214-225
   {
     T rmin = s.min[d], rmax = s.max[d];
     if (rmin - tol > b[d] || b[d] > rmax + tol)
@@ -216,8 +225,8 @@ __device__ __forceinline__ u64 loose_box_key(const T* b, const Space<T>& s, u32 
   {
     T center = (b[d] + b[3 + d]) * T(0.5);
     T bsize = T(b[3 + d] - b[d]);
-    g[d] = to_grid(R(center - s.min[d]) * Raster<R, T>::rast(s, d));
-    maxRel = smax(maxRel, R(bsize) * Raster<R, T>::rast(s, d));
+    g[d] = center_cell_ref<T, R>(center, s, d);
+    maxRel = smax(maxRel, rel_size_ref<T, R>(bsize, s, d));
   }
   u32 maxRelGrid = to_grid(ceil(maxRel));
   u32 level = 0;
@@ -226,34 +235,121 @@ __device__ __forceinline__ u64 loose_box_key(const T* b, const Space<T>& s, u32 
   const u32 shift = level * 3u;
   u64 loc = encode3(g[0], g[1], g[2]);
   loc = shift < 64 ? ((loc >> shift) << shift) : 0;
-  const u64 depth = u64(u32(D - level));
-  return (loc << 5) | depth;
+  return (loc << 5) | u64(u32(D - level));
 }
 
-template<typename T, typename R, typename K, bool IS_BOX>
-__global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent, u64 n, const Space<T>* __restrict__ spg, K* __restrict__ keys,
-                                                      u32* __restrict__ hist, u32 passes)
+template<typename U>
+__device__ __forceinline__ u32 level_from_table(const U* __restrict__ thr, U o)
 {
+  u32 lo = 0, hi = kLevelThresholds; // thr[0] = 0 <= o
+  while (hi - lo > 1)
+  {
+    u32 m = (lo + hi) >> 1;
+    if (o < thr[m])
+      hi = m;
+    else
+      lo = m;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ float to_f(double v) { return __double2float_rn(v); }
+__device__ __forceinline__ float to_f(float v) { return v; }
+
+template<typename T, typename R, typename K, bool IS_BOX>
+__global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent, u64 n, bool vec, const Space<T>* __restrict__ spg,
+                                                      const typename Ord<T>::U* __restrict__ tabG, u32 cells, int tabInSmem,
+                                                      K* __restrict__ keys, u32* __restrict__ hist, u32 passes)
+{
+  using O = Ord<T>;
+  using U = typename O::U;
+  constexpr int W = IS_BOX ? 6 : 3;
+  constexpr int E = Chunk<T, W>::E;
+  extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ u32 sh[8][kRadix];
-  __shared__ Space<T> s;
+  __shared__ float minF[3], rastF[3];
+  __shared__ u32 sD;
+  const size_t perDim = RasterLayout<T>::per_dim(cells);
+  U* stab = reinterpret_cast<U*>(s_dyn);
   for (int i = threadIdx.x; i < 8 * kRadix; i += blockDim.x)
     (&sh[0][0])[i] = 0;
-  if (threadIdx.x == 0)
-    s = *spg;
-  __syncthreads();
-  const u32 D = s.D;
-  const u32 maxRasterID = (1u << D) - 1u;
-  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < n; i += u64(gridDim.x) * blockDim.x)
+  if (tabInSmem)
+    for (size_t i = threadIdx.x; i < 3 * perDim; i += blockDim.x)
+      stab[i] = tabG[i];
+  if (threadIdx.x < 3)
   {
-    u64 key;
-    if constexpr (IS_BOX)
-      key = loose_box_key<T, R>(ent + i * 6, s, D);
-    else
-      key = point_key<T, R>(ent + i * 3, s, maxRasterID);
-    K k = K(key);
-    keys[i] = k;
-    for (u32 p = 0; p < passes; ++p)
-      atomicAdd(&sh[p][(k >> (kRadixBits * p)) & (kRadix - 1)], 1u);
+    const Space<T>& s = *spg;
+    minF[threadIdx.x] = to_f(s.min[threadIdx.x]);
+    rastF[threadIdx.x] = float(Raster<R, T>::rast(s, threadIdx.x));
+    if (threadIdx.x == 0)
+      sD = s.D;
+  }
+  __syncthreads();
+  const U* tab = tabInSmem ? stab : tabG;
+  const u32 D = sD;
+  const u64 chunks = (n + E - 1) / E;
+  for (u64 c = blockIdx.x * u64(blockDim.x) + threadIdx.x; c < chunks; c += u64(gridDim.x) * blockDim.x)
+  {
+    T v[E * W];
+    const int cnt = load_chunk<T, W>(ent, n, c * E, vec, v);
+#pragma unroll
+    for (int k = 0; k < E; ++k)
+    {
+      if (k >= cnt)
+        break;
+      u64 key;
+      const T* e = v + k * W;
+      if constexpr (!IS_BOX)
+      {
+        bool valid = true;
+        u32 g[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+        {
+          const U* td = tab + d * perDim;
+          const U o = O::of(e[d]);
+          valid = valid && o >= td[0] && o <= td[1];
+          const float est = (to_f(e[d]) - minF[d]) * rastF[d];
+          g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, o, est > 2.0e9f ? 2000000000 : int(est));
+        }
+        key = valid ? encode3(g[0], g[1], g[2]) + 1 : 0;
+      }
+      else
+      {
+        bool valid = true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+        {
+          const U* td = tab + d * perDim;
+          const U lo = O::of(e[d]), hi = O::of(e[3 + d]);
+          valid = valid && lo >= td[0] && lo <= td[1] && hi >= td[0] && hi <= td[1];
+        }
+        if (!valid)
+          key = 0;
+        else
+        {
+          u32 g[3], level = 0;
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+          {
+            const U* td = tab + d * perDim;
+            const T center = (e[d] + e[3 + d]) * T(0.5); // internal_geometry_module.h:132-138
+            const T bsize = T(e[3 + d] - e[d]);           // internal_geometry_module.h:140-146
+            const float est = (to_f(center) - minF[d]) * rastF[d];
+            g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, O::of(center), est > 2.0e9f ? 2000000000 : int(est));
+            level = max(level, level_from_table(td + 2, O::of(bsize)));
+          }
+          const u32 shift = level * 3u;
+          u64 loc = encode3(g[0], g[1], g[2]);
+          loc = shift < 64 ? ((loc >> shift) << shift) : 0;
+          key = (loc << 5) | u64(u32(D - level));
+        }
+      }
+      const K kk = K(key);
+      keys[c * E + k] = kk;
+      for (u32 p = 0; p < passes; ++p)
+        atomicAdd(&sh[p][(kk >> (kRadixBits * p)) & (kRadix - 1)], 1u);
+    }
   }
   __syncthreads();
   for (u32 p = 0; p < passes; ++p)
@@ -262,20 +358,25 @@ __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent,
         atomicAdd(&hist[p * kRadix + d], sh[p][d]);
 }
 
-// per-entity location keys in input order, reference layout (loc << 5 | depth)
+// per-entity location keys in input order, reference layout (loc << 5 | depth), computed with the
+// reference formulas from the tree-ordered copy
 template<typename T, typename R, bool IS_BOX>
-__global__ void location_export_kernel(const T* __restrict__ ent, u64 n, const Space<T>* __restrict__ spg, u64* __restrict__ out)
+__global__ void location_export_kernel(const T* __restrict__ geom, const u32* __restrict__ ids, u64 n, const Space<T>* __restrict__ spg,
+                                       u64* __restrict__ out)
 {
   const Space<T> s = *spg;
   const u32 D = s.D;
   for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < n; i += u64(gridDim.x) * blockDim.x)
   {
+    const u32 id = ids[i];
+    if (id >= n)
+      continue;
     if constexpr (IS_BOX)
-      out[i] = loose_box_key<T, R>(ent + i * 6, s, D);
+      out[id] = loose_box_key_ref<T, R>(geom + i * 6, s, D);
     else
     {
-      u64 k = point_key<T, R>(ent + i * 3, s, (1u << D) - 1u);
-      out[i] = k == 0 ? 0 : (((k - 1) << 5) | D);
+      u64 k = point_key_ref<T, R>(geom + i * 3, s, (1u << D) - 1u);
+      out[id] = k == 0 ? 0 : (((k - 1) << 5) | D);
     }
   }
 }
@@ -337,26 +438,8 @@ __device__ __forceinline__ u32 compact1by2(u64 x)
   return u32(x);
 }
 
-// MinPoint of a node: CalculateGridCellCenter(Decode(key), D - depth) - nodeSize[depth + 1]
-// (si_grid.h:124-143, si_morton.h:576-622, ot_dynamic_hash_core.h:563-572)
-template<typename T, typename R>
-__device__ __forceinline__ void node_min_point(u64 key, u32 depth, const Space<T>& s, T out[3])
-{
-  const u32 D = s.D;
-  const u64 loc = key ^ (u64(1) << (3 * depth));
-  const u32 lvl = D - depth;
-  const R halfGrid = R(u64(1) << lvl) * R(0.5);
-#pragma unroll
-  for (int d = 0; d < 3; ++d)
-  {
-    u32 g = compact1by2(loc >> d) << lvl;
-    T c = T((R(g) + halfGrid) * Raster<R, T>::derast(s, d)) + s.min[d];
-    out[d] = c - s.nodeSize[depth + 1][d];
-  }
-}
-
 template<typename T>
-__global__ void root_init_kernel(uint4* link, u64* nodeKey, unsigned char* nodeDepth, u32* levelCount, u32 n)
+__global__ void root_init_kernel(uint4* link, u64* nodeKey, unsigned char* nodeDepth, u32* levelCount, u32 n, u32* nodeParent)
 {
   if (threadIdx.x == 0 && blockIdx.x == 0)
   {
@@ -364,6 +447,8 @@ __global__ void root_init_kernel(uint4* link, u64* nodeKey, unsigned char* nodeD
     nodeKey[0] = 1;
     nodeDepth[0] = 0;
     levelCount[0] = 1;
+    if (nodeParent)
+      nodeParent[0] = 0;
   }
 }
 
@@ -376,66 +461,78 @@ __device__ __forceinline__ void level_range(const u32* levelCount, u32 d, u32& b
   cnt = levelCount[d];
 }
 
+// Four nodes per warp, eight lanes per node: lane 0 finds the end of the node's stuck entities
+// (ProcessNode's partition_point, :658-671), lanes 1..7 find the start of child key ranges 1..7
+// (CreateProcessingData's partition_point, :695-711) at the same time, so the dependent-load
+// chain of a node is one binary search deep. Below the root every key of a node's range shares
+// its prefix, so the end of child 7 is the end of the range; at the root lane 0 also searches it
+// (locations outside the 3*D-bit grid sort after every child range and belong to no child).
 template<typename T, typename K, bool IS_BOX>
-__global__ void __launch_bounds__(256) emit_level_kernel(u32 d, u64 maxElem, const K* __restrict__ keys, uint4* __restrict__ link,
+__global__ void __launch_bounds__(256) emit_level_kernel(u32 d, u32 D, u64 maxElem, const K* __restrict__ keys, uint4* __restrict__ link,
                                                          u64* __restrict__ nodeKey, T* __restrict__ nodeBox, unsigned char* __restrict__ nodeDepth,
-                                                         u32* __restrict__ levelCount, const Space<T>* __restrict__ spg, u64 maxNodes,
-                                                         u32* __restrict__ err, u32* __restrict__ ownerNode, u32* __restrict__ nodeParent)
+                                                         u32* __restrict__ levelCount, const T* __restrict__ minTab, const Space<T>* __restrict__ spg,
+                                                         u64 maxNodes, u32* __restrict__ err, u32* __restrict__ ownerNode, u32* __restrict__ nodeParent)
 {
-  __shared__ Space<T> s;
-  if (threadIdx.x == 0)
-    s = *spg;
-  __syncthreads();
-  const u32 D = s.D;
   u32 begin, cnt;
   level_range(levelCount, d, begin, cnt);
   const u32 childBase = begin + cnt;
   const int lane = threadIdx.x & 31;
-  for (u32 i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < cnt; i0 += gridDim.x * blockDim.x)
+  const int grp = lane >> 3, gl = lane & 7;
+  const u32 groupMask = 0xffu << (grp * 8);
+  const u32 warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const u32 warpsTotal = (gridDim.x * blockDim.x) >> 5;
+  const u64 tabPerDim = (u64(2) << D) - 1;
+  for (u32 base = warpGlobal * 4; base < cnt; base += warpsTotal * 4)
   {
-    const u32 i = i0 + lane;
+    const u32 i = base + grp;
     const bool active = i < cnt;
     const u32 node = begin + i;
-    u32 bounds[9];
-    u32 nchild = 0;
-    u32 b = 0, e = 0, ownEnd = 0;
+    u32 b = 0, e = 0, bnd = 0, end8 = 0;
     u64 key = 1;
+    bool split = false;
     if (active)
     {
-      uint4 L = link[node];
+      const uint4 L = link[node];
       key = nodeKey[node];
       b = L.y;
       e = L.w;
-      const u64 count = u64(e - b);
-      const bool split = count > maxElem && d < D;
-      u32 sEnd = b;
-      const u64 lmin = (key ^ (u64(1) << (3 * d))) << (3 * (D - d));
+      end8 = e;
+      split = u64(e - b) > maxElem && d < D;
       if (split)
       {
-        if constexpr (IS_BOX)
-          sEnd = upper_bound_key(keys, b, e, (lmin << 5) | u64(d)); // ProcessNode partition_point, :658-671
-        else
-          sEnd = (d == 0) ? upper_bound_key(keys, b, e, 0) : b;
-      }
-      ownEnd = split ? sEnd : e;
-      if (split && sEnd < e)
-      {
+        const u64 lmin = (key ^ (u64(1) << (3 * d))) << (3 * (D - d));
         const u64 S = u64(1) << (3 * (D - d - 1));
-        bounds[0] = sEnd;
-#pragma unroll
-        for (int c = 1; c <= 8; ++c)
+        if (gl == 0)
         {
-          const u64 L0 = lmin + u64(c) * S;
-          const u64 target = IS_BOX ? (L0 << 5) : (L0 + 1);
-          bounds[c] = lower_bound_key(keys, bounds[c - 1], e, target);
+          if constexpr (IS_BOX)
+            bnd = upper_bound_key(keys, b, e, (lmin << 5) | u64(d));
+          else
+            bnd = (d == 0) ? upper_bound_key(keys, b, e, 0) : b;
+          if (d == 0)
+          {
+            const u64 L8 = lmin + 8 * S;
+            end8 = lower_bound_key(keys, bnd, e, IS_BOX ? (L8 << 5) : (L8 + 1));
+          }
         }
-#pragma unroll
-        for (int c = 0; c < 8; ++c)
-          nchild += bounds[c + 1] > bounds[c] ? 1u : 0u;
+        else
+        {
+          const u64 L0 = lmin + u64(gl) * S;
+          bnd = lower_bound_key(keys, b, e, IS_BOX ? (L0 << 5) : (L0 + 1));
+        }
       }
     }
+    const u32 end8g = __shfl_sync(0xffffffffu, end8, grp * 8);
+    const u32 myStart = bnd;                                            // lane c: start of child c (lane 0: stuck end)
+    const u32 nextLane = __shfl_sync(0xffffffffu, bnd, (lane + 1) & 31); // lane c: start of child c + 1
+    const u32 nextStart = gl < 7 ? nextLane : end8g;
+    const bool nonEmpty = active && split && nextStart > myStart;
+    const u32 ballot = __ballot_sync(0xffffffffu, nonEmpty) & groupMask;
+    const u32 nchild = __popc(ballot);
+    const u32 stuckEnd = __shfl_sync(0xffffffffu, bnd, grp * 8);
+    const u32 ownEnd = split ? stuckEnd : e;
     // warp-aggregated allocation of the children slots (children of one node are contiguous)
-    u32 incl = nchild;
+    const u32 mine = (gl == 0) ? nchild : 0u;
+    u32 incl = mine;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1)
     {
@@ -443,49 +540,44 @@ __global__ void __launch_bounds__(256) emit_level_kernel(u32 d, u64 maxElem, con
       if (lane >= o)
         incl += y;
     }
-    u32 warpTotal = __shfl_sync(0xffffffffu, incl, 31);
+    const u32 warpTotal = __shfl_sync(0xffffffffu, incl, 31);
     u32 warpBase = 0;
     if (lane == 31 && warpTotal)
       warpBase = atomicAdd(&levelCount[d + 1], warpTotal);
     warpBase = __shfl_sync(0xffffffffu, warpBase, 31);
-    const u32 firstChild = childBase + warpBase + incl - nchild;
+    const u32 firstChild = childBase + warpBase + __shfl_sync(0xffffffffu, incl - mine, grp * 8);
+    const bool overflow = u64(firstChild) + nchild > maxNodes;
     if (active)
     {
-      if (u64(firstChild) + nchild > maxNodes)
+      if (nonEmpty && !overflow)
       {
-        atomicOr(err, kErrCapacity);
-        nchild = 0;
+        const u32 ci = firstChild + __popc(ballot & lanemask_lt());
+        nodeKey[ci] = (key << 3) | u64(gl);
+        link[ci] = make_uint4(0, myStart, myStart, nextStart);
+        nodeDepth[ci] = (unsigned char)(d + 1);
+        if (nodeParent)
+          nodeParent[ci] = node;
       }
-      u32 j = 0;
-      for (int c = 0; c < 8 && nchild; ++c)
+      if (gl == 0)
       {
-        if (bounds[c + 1] > bounds[c])
-        {
-          const u32 ci = firstChild + j++;
-          nodeKey[ci] = (key << 3) | u64(c);
-          link[ci] = make_uint4(0, bounds[c], bounds[c], bounds[c + 1]);
-          nodeDepth[ci] = (unsigned char)(d + 1);
-          if (nodeParent)
-            nodeParent[ci] = node;
-        }
+        if (overflow)
+          atomicOr(err, kErrCapacity);
+        const u32 nc = overflow ? 0u : nchild;
+        link[node] = make_uint4((nc ? (firstChild & kFirstChildMask) : 0u) | (nc << kChildShift), b, ownEnd, e);
       }
-      link[node] = make_uint4((nchild ? (firstChild & kFirstChildMask) : 0u) | (nchild << kChildShift), b, ownEnd, e);
       if (ownerNode)
-        for (u32 q = b; q < ownEnd; ++q)
+        for (u32 q = b + gl; q < ownEnd; q += 8)
           ownerNode[q] = node;
       if constexpr (!IS_BOX)
       {
-        T mn[3];
-        if (s.rasterDouble)
-          node_min_point<T, double>(key, d, s, mn);
-        else
-          node_min_point<T, float>(key, d, s, mn);
-        T* nb = nodeBox + u64(node) * 6;
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
+        if (gl < 3)
         {
-          nb[c] = mn[c];
-          nb[3 + c] = s.nodeSize[d][c];
+          // MinPoint from the node table (identical arithmetic, computed once per cell)
+          const u64 loc = key ^ (u64(1) << (3 * d));
+          const u32 cell = compact1by2(loc >> gl);
+          T* nb = nodeBox + u64(node) * 6;
+          nb[gl] = minTab[u64(gl) * tabPerDim + ((u64(1) << d) - 1) + cell];
+          nb[3 + gl] = spg->nodeSize[d][gl];
         }
       }
     }
@@ -620,13 +712,16 @@ static u32 estimate_max_depth(u64 n, u64 maxElem)
 }
 
 template<typename T, typename K, bool IS_BOX>
-static int build_impl(TreeState& t, const void* box, u64 n, cudaStream_t st)
+static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaStream_t st)
 {
   constexpr int W = IS_BOX ? 6 : 3;
-  using B = typename OrderedBits<T>::type;
+  using U = typename Ord<T>::U;
   const u32 D = t.D;
   const u32 bits = IS_BOX ? 3 * D + 5 : 3 * D + 1;
   const u32 passes = (bits + kRadixBits - 1) / kRadixBits;
+  const u32 cells = IS_BOX ? (1u << D) + 2 : (1u << D);
+  const size_t tabBytes = RasterLayout<T>::bytes(cells);
+  const u64 minTabEntries = IS_BOX ? 1 : 3 * ((u64(2) << D) - 1);
   cudaError_t e;
 
   // buffers
@@ -636,7 +731,8 @@ static int build_impl(TreeState& t, const void* box, u64 n, cudaStream_t st)
       (e = t.valsB.ensure(sizeof(u32) * n)) || (e = t.sortedGeom.ensure(sizeof(T) * W * n)) || (e = t.nodeLink.ensure(sizeof(uint4) * maxNodes)) ||
       (e = t.nodeKey.ensure(sizeof(u64) * maxNodes)) || (e = t.nodeBox.ensure(sizeof(T) * 6 * maxNodes)) ||
       (e = t.nodeDepth.ensure(maxNodes)) || (e = t.levelCount.ensure(sizeof(u32) * 32)) || (e = t.space.ensure(sizeof(Space<T>))) ||
-      (e = t.sortScratch.ensure(SortScratch::bytes(n, passes))) || (e = t.bboxBits.ensure(sizeof(B) * 6)) ||
+      (e = t.sortScratch.ensure(SortScratch::bytes(n, passes))) || (e = t.bboxBits.ensure(sizeof(U) * 6)) ||
+      (e = t.rasterTab.ensure(tabBytes)) || (e = t.minTab.ensure(sizeof(T) * minTabEntries)) ||
       (IS_BOX && ((e = t.nodeMax.ensure(sizeof(T) * 3 * maxNodes)) || (e = t.ownerNode.ensure(sizeof(u32) * n)) ||
                   (e = t.nodeParent.ensure(sizeof(u32) * maxNodes)))))
     return cuda_status(e, "allocating tree buffers");
@@ -649,22 +745,47 @@ static int build_impl(TreeState& t, const void* box, u64 n, cudaStream_t st)
   cudaMemsetAsync(t.sortScratch.p, 0, SortScratch::bytes(n, passes), st);
   cudaMemsetAsync(t.levelCount.p, 0, sizeof(u32) * 32, st);
 
-  const T* ent = t.entities.as<T>();
+  const bool vec = (reinterpret_cast<uintptr_t>(ent) & 15) == 0;
   Space<T>* sp = t.space.as<Space<T>>();
   if (!box)
   {
     prof.mark("bbox", st);
-    bbox_init_kernel<T><<<1, 32, 0, st>>>(t.bboxBits.as<B>());
-    bbox_kernel<T, W><<<grid_blocks(n, 256, 152 * 8), 256, 0, st>>>(ent, n, t.bboxBits.as<B>());
+    bbox_init_kernel<U><<<1, 32, 0, st>>>(t.bboxBits.as<U>());
+    bbox_kernel<T, W><<<grid_blocks((n + Chunk<T, W>::E - 1) / Chunk<T, W>::E, 256, 152 * 8), 256, 0, st>>>(ent, n, vec, t.bboxBits.as<U>());
   }
-  space_setup_kernel<T><<<1, 1, 0, st>>>(sp, t.bboxBits.as<B>(), (const T*)box, D, IS_BOX ? 0 : 1);
-
+  prof.mark("tables", st);
+  space_setup_kernel<T><<<1, 1, 0, st>>>(sp, t.bboxBits.as<U>(), (const T*)box, D, IS_BOX ? 0 : 1);
   const bool rasterDouble = (sizeof(T) == 8) || D >= 16;
-  prof.mark("codegen", st);
+  U* tab = t.rasterTab.as<U>();
+  const u64 tabEntries = 3 * RasterLayout<T>::per_dim(cells);
   if (rasterDouble)
-    codegen_kernel<T, double, K, IS_BOX><<<grid_blocks(n, 256, 152 * 8), 256, 0, st>>>(ent, n, sp, t.keysA.as<K>(), ss.hist, passes);
+    raster_tables_kernel<T, double><<<grid_blocks(tabEntries, 128, 152 * 32), 128, 0, st>>>(sp, tab, cells, IS_BOX ? 1 : 0);
   else
-    codegen_kernel<T, float, K, IS_BOX><<<grid_blocks(n, 256, 152 * 8), 256, 0, st>>>(ent, n, sp, t.keysA.as<K>(), ss.hist, passes);
+    raster_tables_kernel<T, float><<<grid_blocks(tabEntries, 128, 152 * 32), 128, 0, st>>>(sp, tab, cells, IS_BOX ? 1 : 0);
+  if constexpr (!IS_BOX)
+  {
+    if (rasterDouble)
+      node_min_table_kernel<T, double><<<grid_blocks(minTabEntries), 256, 0, st>>>(sp, t.minTab.as<T>());
+    else
+      node_min_table_kernel<T, float><<<grid_blocks(minTabEntries), 256, 0, st>>>(sp, t.minTab.as<T>());
+  }
+
+  prof.mark("codegen", st);
+  const int tabInSmem = tabBytes <= 64 * 1024 ? 1 : 0;
+  const size_t cgSmem = tabInSmem ? tabBytes : 0;
+  const int cgBlocks = grid_blocks((n + Chunk<T, W>::E - 1) / Chunk<T, W>::E, 256, 152 * 4);
+  if (rasterDouble)
+  {
+    auto kfn = codegen_kernel<T, double, K, IS_BOX>;
+    cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
+    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes);
+  }
+  else
+  {
+    auto kfn = codegen_kernel<T, float, K, IS_BOX>;
+    cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
+    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes);
+  }
 
   prof.mark("sort", st);
   bool inB = onesweep_passes<K>(t.keysA.as<K>(), t.sortedIds.as<u32>(), t.keysB.as<K>(), t.valsB.as<u32>(), n, 0, passes, true, ss, t.err.as<u32>(), st);
@@ -681,12 +802,14 @@ static int build_impl(TreeState& t, const void* box, u64 n, cudaStream_t st)
   gather_kernel<T, W><<<grid_blocks(n, 256, 152 * 8), 256, 0, st>>>(ent, t.sortedIds.as<u32>(), n, t.sortedGeom.as<T>());
 
   prof.mark("emit", st);
-  root_init_kernel<T><<<1, 32, 0, st>>>(t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeDepth.as<unsigned char>(), t.levelCount.as<u32>(), u32(n));
-  const int emitBlocks = grid_blocks(n / std::max<u64>(1, t.maxElem / 2), 256, 152 * 4);
+  u32* parent = IS_BOX ? t.nodeParent.as<u32>() : nullptr;
+  root_init_kernel<T><<<1, 32, 0, st>>>(t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeDepth.as<unsigned char>(), t.levelCount.as<u32>(), u32(n),
+                                        parent);
+  const int emitBlocks = grid_blocks(maxNodes / 4, 256, 152 * 16);
   for (u32 d = 0; d <= D; ++d)
-    emit_level_kernel<T, K, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, t.maxElem, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
-                                                                t.nodeDepth.as<unsigned char>(), t.levelCount.as<u32>(), sp, maxNodes, t.err.as<u32>(),
-                                                                IS_BOX ? t.ownerNode.as<u32>() : nullptr, IS_BOX ? t.nodeParent.as<u32>() : nullptr);
+    emit_level_kernel<T, K, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, D, t.maxElem, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
+                                                                t.nodeDepth.as<unsigned char>(), t.levelCount.as<u32>(), t.minTab.as<T>(), sp, maxNodes,
+                                                                t.err.as<u32>(), IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent);
   prof.mark("geometry", st);
   if constexpr (IS_BOX)
   {
@@ -725,6 +848,12 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
     set_error("maxDepthID must be in [1, 19]");
     return OTG_ERR_INVALID_ARGUMENT;
   }
+  // node links pack the first-child index in 28 bits
+  if (n + u64(D) * (n / (maxElem + 1) + 1) + 2 >= (u64(1) << kChildShift))
+  {
+    set_error("entity count too large for the 28-bit node index of this build");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
   t.n = n;
   t.D = D;
   t.maxElem = maxElem;
@@ -732,25 +861,28 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
   t.countsKnown = false;
   t.boxGiven = box != nullptr;
   cudaError_t e;
-  if ((e = t.entities.ensure(esz * W * n)) || (e = t.err.ensure(sizeof(u32) * 4)))
-    return cuda_status(e, "allocating entity buffer");
+  if ((e = t.err.ensure(sizeof(u32) * 4)))
+    return cuda_status(e, "allocating status word");
   cudaMemsetAsync(t.err.p, 0, sizeof(u32) * 4, st);
-  if (n)
+  // Host entities are copied to the device; device entities are read in place during the build
+  // (the caller keeps them alive until the build completes on `st`, as for any stream-ordered call).
+  const void* ent = entities;
+  if (n && mem == OTG_MEM_HOST)
   {
-    e = cudaMemcpyAsync(t.entities.p, entities, esz * W * n, mem == OTG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st);
-    if (e)
+    if ((e = t.entities.ensure(esz * W * n)))
+      return cuda_status(e, "allocating entity buffer");
+    if ((e = cudaMemcpyAsync(t.entities.p, entities, esz * W * n, cudaMemcpyHostToDevice, st)))
       return cuda_status(e, "copying entities");
+    ent = t.entities.p;
   }
-  // the box is read by a kernel: stage it in device memory
-  DevBuf& boxBuf = t.boxDev;
   const void* dbox = nullptr;
   if (box)
   {
-    if ((e = boxBuf.ensure(esz * 6)))
+    if ((e = t.boxDev.ensure(esz * 6)))
       return cuda_status(e, "allocating box");
-    if ((e = cudaMemcpyAsync(boxBuf.p, box, esz * 6, mem == OTG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st)))
+    if ((e = cudaMemcpyAsync(t.boxDev.p, box, esz * 6, mem == OTG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st)))
       return cuda_status(e, "copying box");
-    dbox = boxBuf.p;
+    dbox = t.boxDev.p;
   }
   if (n == 0)
   {
@@ -764,26 +896,22 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
   }
   const u32 bits = isBox ? 3 * D + 5 : 3 * D + 1;
   t.keys32 = bits <= 32;
-  // node links pack the first-child index in 28 bits
-  if (n + u64(D) * (n / (maxElem + 1) + 1) + 2 >= (u64(1) << kChildShift))
-  {
-    set_error("entity count too large for the 28-bit node index of this build");
-    return OTG_ERR_NOT_SUPPORTED;
-  }
   int rc;
   if (t.scalar == OTG_SCALAR_F64)
   {
+    const double* p = static_cast<const double*>(ent);
     if (isBox)
-      rc = t.keys32 ? build_impl<double, u32, true>(t, dbox, n, st) : build_impl<double, u64, true>(t, dbox, n, st);
+      rc = t.keys32 ? build_impl<double, u32, true>(t, p, dbox, n, st) : build_impl<double, u64, true>(t, p, dbox, n, st);
     else
-      rc = t.keys32 ? build_impl<double, u32, false>(t, dbox, n, st) : build_impl<double, u64, false>(t, dbox, n, st);
+      rc = t.keys32 ? build_impl<double, u32, false>(t, p, dbox, n, st) : build_impl<double, u64, false>(t, p, dbox, n, st);
   }
   else
   {
+    const float* p = static_cast<const float*>(ent);
     if (isBox)
-      rc = t.keys32 ? build_impl<float, u32, true>(t, dbox, n, st) : build_impl<float, u64, true>(t, dbox, n, st);
+      rc = t.keys32 ? build_impl<float, u32, true>(t, p, dbox, n, st) : build_impl<float, u64, true>(t, p, dbox, n, st);
     else
-      rc = t.keys32 ? build_impl<float, u32, false>(t, dbox, n, st) : build_impl<float, u64, false>(t, dbox, n, st);
+      rc = t.keys32 ? build_impl<float, u32, false>(t, p, dbox, n, st) : build_impl<float, u64, false>(t, p, dbox, n, st);
   }
   if (rc)
     return rc;
@@ -843,30 +971,33 @@ int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st)
   const bool isBox = t.kind == OTG_KIND_BOXES;
   const bool rd = t.scalar == OTG_SCALAR_F64 || t.D >= 16;
   const int blocks = grid_blocks(t.n);
+  const u32* ids = t.sortedIds.as<u32>();
   if (t.scalar == OTG_SCALAR_F64)
   {
     auto sp = t.space.as<Space<double>>();
+    const double* g = t.sortedGeom.as<double>();
     if (isBox)
-      location_export_kernel<double, double, true><<<blocks, 256, 0, st>>>(t.entities.as<double>(), t.n, sp, out);
+      location_export_kernel<double, double, true><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
     else
-      location_export_kernel<double, double, false><<<blocks, 256, 0, st>>>(t.entities.as<double>(), t.n, sp, out);
+      location_export_kernel<double, double, false><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
   }
   else
   {
     auto sp = t.space.as<Space<float>>();
+    const float* g = t.sortedGeom.as<float>();
     if (isBox)
     {
       if (rd)
-        location_export_kernel<float, double, true><<<blocks, 256, 0, st>>>(t.entities.as<float>(), t.n, sp, out);
+        location_export_kernel<float, double, true><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
       else
-        location_export_kernel<float, float, true><<<blocks, 256, 0, st>>>(t.entities.as<float>(), t.n, sp, out);
+        location_export_kernel<float, float, true><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
     }
     else
     {
       if (rd)
-        location_export_kernel<float, double, false><<<blocks, 256, 0, st>>>(t.entities.as<float>(), t.n, sp, out);
+        location_export_kernel<float, double, false><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
       else
-        location_export_kernel<float, float, false><<<blocks, 256, 0, st>>>(t.entities.as<float>(), t.n, sp, out);
+        location_export_kernel<float, float, false><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
     }
   }
   cudaError_t e = cudaGetLastError();
@@ -876,16 +1007,12 @@ int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st)
     if (!e)
       e = cudaStreamSynchronize(st);
   }
-  tmp.release();
   return cuda_status(e, "exporting locations");
 }
 
 int export_nodes(const TreeState& t, u64* keys, double* minSize, u64* eoff, u32* eids, u32* childCount)
 {
   const u64 m = t.nodeCount;
-  std::vector<uint4> link(m);
-  std::vector<u32> ids(t.n);
-  cudaError_t e = cudaSuccess;
   if (t.n == 0)
   {
     keys[0] = 1;
@@ -896,7 +1023,9 @@ int export_nodes(const TreeState& t, u64* keys, double* minSize, u64* eoff, u32*
       childCount[0] = 0;
     return OTG_OK;
   }
-  e = cudaMemcpy(link.data(), t.nodeLink.p, sizeof(uint4) * m, cudaMemcpyDeviceToHost);
+  std::vector<uint4> link(m);
+  std::vector<u32> ids(t.n);
+  cudaError_t e = cudaMemcpy(link.data(), t.nodeLink.p, sizeof(uint4) * m, cudaMemcpyDeviceToHost);
   if (!e)
     e = cudaMemcpy(keys, t.nodeKey.p, sizeof(u64) * m, cudaMemcpyDeviceToHost);
   if (!e)

@@ -105,6 +105,8 @@ struct TreeState
   DevBuf bboxBits;   // ordered-bit min/max accumulators
   DevBuf locations;  // u64 per entity (input order), filled on export request
   DevBuf boxDev;     // the given space box (6 scalars)
+  DevBuf rasterTab;  // exact rasterisation thresholds (otg_raster.cuh)
+  DevBuf minTab;     // MinPoint node table per (dimension, depth, cell)
 
   // cached after the build (host copies, filled by sync)
   u64 nodeCount = 0;

@@ -666,10 +666,13 @@ __global__ void __launch_bounds__(128) collide_plain_kernel(TreeView<T> ta, Tree
     const u32 node = stack[--sp];
     const T* nmin = tb.nodeBox + u64(node) * 6;
     const T* nmax = tb.nodeMax + u64(node) * 3;
+    // GetBoxRelation can only answer "overlapped" when neither max + tol < other min (in the
+    // scalar's arithmetic); every box of the node lies inside its exact MBR, so this prune never
+    // drops a pair the predicate accepts
     bool disjoint = false;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
-      disjoint |= (a[3 + c] < nmin[c]) || (nmax[c] < a[c]);
+      disjoint |= (T(a[3 + c] + tol) < nmin[c]) || (T(nmax[c] + tol) < a[c]);
     if (disjoint)
       continue;
     const uint4 L = tb.link[node];
@@ -720,6 +723,7 @@ struct StructTree
   const unsigned char* depth;
   const T* geom;
   const u32* ids;
+  const uint4* link;
 };
 
 template<typename T>
@@ -753,6 +757,41 @@ __device__ __forceinline__ bool with_parent_condition(const StructTree<T>& t, u3
   return GeoD<T>::overlap_by_min_point(nb, nb + 3, p, psize, tol);
 }
 
+// The sweep-and-prune loops (ot_query.h:1367-1418, 1581-1650) visit, for an outer entity o, the
+// inner entities of a node sorted by min-x starting at the first one whose max-x >= o.minX. An
+// inner entity whose box ends before o starts is therefore tested only when an inner entity
+// sorted before it (min-x, then id) reaches o.minX. GetBoxRelation can call such a pair
+// overlapping when the gap is under one ulp but above the tolerance (the tolerance addition
+// rounds up to the other coordinate).
+template<typename T>
+__device__ __forceinline__ bool sweep_reaches(const StructTree<T>& t, u32 innerNode, u32 innerPos, T outerMinX)
+{
+  const uint4 L = t.link[innerNode];
+  const T* g = t.geom + u64(innerPos) * 6;
+  const T mx = g[0];
+  const u32 id = t.ids[innerPos];
+  for (u32 q = L.y; q < L.z; ++q)
+  {
+    const T* h = t.geom + u64(q) * 6;
+    const bool before = h[0] < mx || (h[0] == mx && t.ids[q] < id);
+    if (before && h[3] >= outerMinX)
+      return true;
+  }
+  return false;
+}
+
+// two-tree rules for outer (left) entity o and inner (right) entity at position ip in tree ti
+template<typename T>
+__device__ __forceinline__ bool sweep_pair(const T* o, const StructTree<T>& ti, u32 ip)
+{
+  const T* r = ti.geom + u64(ip) * 6;
+  if (o[3] < r[0]) // the inner loop breaks at the first inner min-x above o.maxX
+    return false;
+  if (r[3] < o[0])
+    return sweep_reaches(ti, ti.owner[ip], ip, o[0]);
+  return true;
+}
+
 template<typename T>
 __global__ void __launch_bounds__(128) collide_filter_kernel(StructTree<T> A, StructTree<T> B, int selfMode, const u64* __restrict__ pairs, u64 m, T tol,
                                                              u64* __restrict__ keys, unsigned long long* rejected)
@@ -762,29 +801,55 @@ __global__ void __launch_bounds__(128) collide_filter_kernel(StructTree<T> A, St
     const u64 it = pairs[idx];
     const u32 i = u32(it >> 32), j = u32(it);
     const u32 xa = A.owner[i], xb = B.owner[j];
+    const T* ga = A.geom + u64(i) * 6;
+    const T* gb = B.geom + u64(j) * 6;
     u32 ancA[21], ancB[21];
     bool keep = true;
-    if (!(selfMode && xa == xb))
+    if (!selfMode)
     {
+      // CollisionDetection(left = A, right = B): node-pair walk from the roots, then the sweep
+      keep = sweep_pair(ga, B, j);
       const int da = ancestors(A, xa, ancA);
       const int db = ancestors(B, xb, ancB);
-      if (selfMode)
+      for (int k = 1; k <= max(da, db) && keep; ++k)
+        keep = node_overlap(A, ancA[min(k, da)], B, ancB[min(k, db)], tol);
+    }
+    else if (xa == xb)
+    {
+      // InsertCollidedEntitiesInsideNode: ordered by (min-x, id), the later one must start
+      // before the earlier one ends
+      const bool aFirst = ga[0] < gb[0] || (ga[0] == gb[0] && A.ids[i] < A.ids[j]);
+      keep = aFirst ? !(ga[3] < gb[0]) : !(gb[3] < ga[0]);
+    }
+    else
+    {
+      const int da = ancestors(A, xa, ancA);
+      const int db = ancestors(A, xb, ancB);
+      int dn = 0;
+      while (dn + 1 <= min(da, db) && ancA[dn + 1] == ancB[dn + 1])
+        ++dn;
+      if (dn == da || dn == db)
       {
-        int dn = 0;
-        while (dn + 1 <= min(da, db) && ancA[dn + 1] == ancB[dn + 1])
-          ++dn;
-        if (dn == da)
-          keep = with_parent_condition(A, xb, A.geom + u64(i) * 6, tol);
-        else if (dn == db)
-          keep = with_parent_condition(A, xa, A.geom + u64(j) * 6, tol);
-        else
-          for (int k = dn + 2; k <= max(da, db) && keep; ++k)
-            keep = node_overlap(A, ancA[min(k, da)], A, ancB[min(k, db)], tol);
+        // InsertCollidedEntitiesWithParents: node entity e (deeper node x) against ancestor entity p
+        const bool aDeeper = dn == db ? true : false;
+        const u32 x = aDeeper ? xa : xb;
+        const u32 ep = aDeeper ? i : j;
+        const T* e = aDeeper ? ga : gb;
+        const T* p = aDeeper ? gb : ga;
+        keep = with_parent_condition(A, x, p, tol);
+        if (keep && p[3] < e[0])
+          keep = false;
+        if (keep && e[3] < p[0])
+          keep = sweep_reaches(A, x, ep, p[0]);
       }
       else
       {
-        for (int k = 1; k <= max(da, db) && keep; ++k)
-          keep = node_overlap(A, ancA[min(k, da)], B, ancB[min(k, db)], tol);
+        // sibling sub-trees (ot_query.h:1672-1684): two-tree walk from (c1, c2), the earlier
+        // child being the left tree; the first pair is not tested
+        const bool aLeft = ancA[dn + 1] < ancB[dn + 1];
+        keep = aLeft ? sweep_pair(ga, A, j) : sweep_pair(gb, A, i);
+        for (int k = dn + 2; k <= max(da, db) && keep; ++k)
+          keep = node_overlap(A, ancA[min(k, da)], A, ancB[min(k, db)], tol);
       }
     }
     u32 idA = A.ids[i], idB = B.ids[j];
@@ -1293,8 +1358,8 @@ static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, do
 template<typename T>
 static StructTree<T> struct_view(const TreeState& t)
 {
-  return StructTree<T>{ t.nodeBox.as<T>(), t.ownerNode.as<u32>(), t.nodeParent.as<u32>(), t.nodeDepth.as<unsigned char>(), t.sortedGeom.as<T>(),
-                        t.sortedIds.as<u32>() };
+  return StructTree<T>{ t.nodeBox.as<T>(),          t.ownerNode.as<u32>(), t.nodeParent.as<u32>(), t.nodeDepth.as<unsigned char>(),
+                        t.sortedGeom.as<T>(),        t.sortedIds.as<u32>(), t.nodeLink.as<uint4>() };
 }
 
 template<typename T>

@@ -15,8 +15,8 @@
 
 namespace otg
 {
-constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
+constexpr int kSortThreads = 512;
+constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems; // 4096
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kRadixBits = 8;
@@ -38,8 +38,8 @@ __device__ __forceinline__ u32 lanemask_lt()
   return m;
 }
 
-// exclusive scan of one value per thread over a 256-thread block; returns the block total
-__device__ __forceinline__ u32 block_exclusive_scan_256(u32 v, u32* s_warp, u32& total)
+// exclusive scan of one value per thread over the block (kSortWarps warps); returns the block total
+__device__ __forceinline__ u32 block_exclusive_scan(u32 v, u32* s_warp, u32& total)
 {
   int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   u32 x = v;
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256) radix_histogram_kernel(const K* __restric
 
 // One onesweep pass. vin == nullptr means values are the input positions (iota).
 template<typename K>
-__global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(const K* __restrict__ kin, const u32* __restrict__ vin, K* __restrict__ kout,
+__global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass_kernel(const K* __restrict__ kin, const u32* __restrict__ vin, K* __restrict__ kout,
                                                                      u32* __restrict__ vout, u32 n, u32 shift, const u32* __restrict__ hist,
                                                                      u32* __restrict__ status, u32* __restrict__ tileCounter, u32* __restrict__ err)
 {
@@ -150,57 +150,62 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(const K* __
   }
   __syncthreads();
 
-  // per digit (thread tid owns digit tid): warp offsets and the tile total
+  // per digit (thread tid < 256 owns digit tid): warp offsets and the tile total
   u32 total = 0;
-#pragma unroll
-  for (int w = 0; w < kSortWarps; ++w)
-  {
-    u32 c = s_warpHist[w][tid];
-    s_warpHist[w][tid] = total;
-    total += c;
-  }
-
-  // decoupled look-back over earlier tiles for digit tid
   u32 prefix = 0;
-  volatile u32* vstatus = status;
-  if (tile == 0)
+  if (tid < kRadix)
   {
-    vstatus[tid] = kStatusInclusive | total;
-  }
-  else
-  {
-    vstatus[u64(tile) * kRadix + tid] = kStatusAggregate | total;
-    long long j = (long long)tile - 1;
-    u32 spins = 0;
-    while (j >= 0)
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w)
     {
-      u32 s = vstatus[u64(j) * kRadix + tid];
-      u32 flag = s & ~kStatusValueMask;
-      if (flag == 0)
-      {
-        if (++spins > kLookbackSpinLimit)
-        {
-          atomicOr(err, kErrTimeout);
-          break;
-        }
-        __nanosleep(32);
-        continue;
-      }
-      prefix += s & kStatusValueMask;
-      if (flag == kStatusInclusive)
-        break;
-      --j;
+      u32 c = s_warpHist[w][tid];
+      s_warpHist[w][tid] = total;
+      total += c;
     }
-    vstatus[u64(tile) * kRadix + tid] = kStatusInclusive | ((prefix + total) & kStatusValueMask);
+    // decoupled look-back over earlier tiles for digit tid
+    volatile u32* vstatus = status;
+    if (tile == 0)
+    {
+      vstatus[tid] = kStatusInclusive | total;
+    }
+    else
+    {
+      vstatus[u64(tile) * kRadix + tid] = kStatusAggregate | total;
+      long long j = (long long)tile - 1;
+      u32 spins = 0;
+      while (j >= 0)
+      {
+        u32 sv = vstatus[u64(j) * kRadix + tid];
+        u32 flag = sv & ~kStatusValueMask;
+        if (flag == 0)
+        {
+          if (++spins > kLookbackSpinLimit)
+          {
+            atomicOr(err, kErrTimeout);
+            break;
+          }
+          __nanosleep(32);
+          continue;
+        }
+        prefix += sv & kStatusValueMask;
+        if (flag == kStatusInclusive)
+          break;
+        --j;
+      }
+      vstatus[u64(tile) * kRadix + tid] = kStatusInclusive | ((prefix + total) & kStatusValueMask);
+    }
   }
 
   u32 tileTotal;
-  u32 digitStart = block_exclusive_scan_256(total, s_scan, tileTotal);
-  u32 hcount = hist[tid];
+  u32 digitStart = block_exclusive_scan(total, s_scan, tileTotal);
+  u32 hcount = tid < kRadix ? hist[tid] : 0u;
   u32 hsum;
-  u32 histPrefix = block_exclusive_scan_256(hcount, s_scan, hsum);
-  s_digitStart[tid] = digitStart;
-  s_globalBase[tid] = histPrefix + prefix - digitStart;
+  u32 histPrefix = block_exclusive_scan(hcount, s_scan, hsum);
+  if (tid < kRadix)
+  {
+    s_digitStart[tid] = digitStart;
+    s_globalBase[tid] = histPrefix + prefix - digitStart;
+  }
   __syncthreads();
 
 #pragma unroll

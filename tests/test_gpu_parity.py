@@ -106,6 +106,37 @@ def test_boxes_random(dtype, max_depth, max_elem):
     assert np.array_equal(t.collision_pair(t2), o.collide_pair(o2))
 
 
+def _gap_boxes(dtype, seed):
+    """Boxes with coordinates in [140, 200], where the tolerance lies between half an ulp and an ulp,
+    half of them starting one ulp after other boxes end in x: exercises the rounding gap of
+    GetBoxRelation against the reference's sweep-and-prune."""
+    rng = np.random.default_rng(seed)
+    n = 3000
+    cen = rng.random((n, 3)) * 60 + 140
+    half = np.round(rng.random((n, 3)) * 4 + 0.5, 1)
+    ent = np.concatenate([cen - half, cen + half], 1).astype(dtype)
+    ent[n // 2 :, 0] = ent[: n - n // 2, 3]
+    ent[n // 2 :, 3] = ent[n // 2 :, 0] + dtype(2.0)
+    ent[n // 2 :, 0] = np.nextafter(ent[n // 2 :, 0], dtype(1e9))
+    ent[n // 2 :, 3] = np.maximum(ent[n // 2 :, 3], ent[n // 2 :, 0])
+    return ent
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("max_depth,max_elem", [(3, 4), (5, 8), (2, 2)])
+def test_collision_rounding_gap(dtype, max_depth, max_elem):
+    ent = _gap_boxes(dtype, 500 + max_depth)
+    t = _gpu_tree(ent, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    o = oracle().create(ent, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    assert np.array_equal(t.collision_self(), o.collide_self())
+    other = ent.copy()
+    other[:, [0, 3]] = other[:, [0, 3]] + (other[:, 3:4] - other[:, 0:1])
+    t2 = _gpu_tree(other, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    o2 = oracle().create(other, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    assert np.array_equal(t.collision_pair(t2), o.collide_pair(o2))
+    assert np.array_equal(t2.collision_pair(t), o2.collide_pair(o))
+
+
 EDGE_CASES = {
     "single": (np.array([[1.0, 2.0, 3.0]]), KIND_POINTS, None),
     "two_equal": (np.array([[1.0, 2.0, 3.0], [1.0, 2.0, 3.0]]), KIND_POINTS, None),

@@ -49,3 +49,24 @@ def test_random_boxes(seed, kind):
     assert _same_tree(a, b)
     assert np.array_equal(a.collide_self(), b.collide_self())
     assert np.array_equal(b.collide_self(), b.collide_self_par())
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_collision_rounding_gap(dtype):
+    """Boxes whose x faces are one ulp apart where the tolerance lies between half an ulp and an ulp
+    (coordinates in [140, 200]): the reference's sweep-and-prune decides these pairs."""
+    rng = np.random.default_rng(77)
+    n = 1500
+    cen = rng.random((n, 3)) * 60 + 140
+    half = np.round(rng.random((n, 3)) * 4 + 0.5, 1)
+    ent = np.concatenate([cen - half, cen + half], 1).astype(dtype)
+    ent[n // 2 :, 0] = ent[: n - n // 2, 3]
+    ent[n // 2 :, 3] = ent[n // 2 :, 0] + dtype(2.0)
+    ent[n // 2 :, 0] = np.nextafter(ent[n // 2 :, 0], dtype(1e9))
+    ent[n // 2 :, 3] = np.maximum(ent[n // 2 :, 3], ent[n // 2 :, 0])
+    a, b = oracle().create(ent, KIND_LOOSE_BOXES, 4, None, 4), reference().create(ent, KIND_LOOSE_BOXES, 4, None, 4)
+    assert np.array_equal(a.collide_self(), b.collide_self())
+    other = ent.copy()
+    other[:, [0, 3]] = other[:, [0, 3]] + (other[:, 3:4] - other[:, 0:1])
+    a2, b2 = oracle().create(other, KIND_LOOSE_BOXES, 4, None, 4), reference().create(other, KIND_LOOSE_BOXES, 4, None, 4)
+    assert np.array_equal(a.collide_pair(a2), b.collide_pair(b2))
