@@ -13,7 +13,7 @@
 //   6. node emission, one launch per depth (BuildSubtree/ProcessNode,
 //      :647-747): a node whose subtree holds more than maxElem entities and
 //      d < maxDepth keeps its "stuck" entities (location depth == d) and
-//      splits the rest into its <= 8 non-empty child key ranges            -> emit_level_kernel
+//      splits the rest into its <= 8 non-empty child key ranges            -> emit_classify / emit_split
 //   7. MBR node boxes bottom-up (:1425-1450) for box trees, or the root box
 //      widening of MinPoint trees built with a given box (:1573-1601)       -> mbr_level_kernel / root_box_kernel
 //
@@ -382,19 +382,37 @@ __global__ void location_export_kernel(const T* __restrict__ geom, const u32* __
 }
 
 // ---------------------------------------------------------------- 5. gather into tree order
+// Random reads of whole entities: every thread issues the loads of kGatherPerThread entities
+// before storing any of them, so many sectors are in flight per thread.
+constexpr int kGatherPerThread = 4;
 template<typename T, int W>
 __global__ void __launch_bounds__(256) gather_kernel(const T* __restrict__ ent, const u32* __restrict__ ids, u64 n, T* __restrict__ out)
 {
-  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < n; i += u64(gridDim.x) * blockDim.x)
+  const u64 stride = u64(gridDim.x) * blockDim.x;
+  for (u64 i0 = blockIdx.x * u64(blockDim.x) + threadIdx.x; i0 < n; i0 += stride * kGatherPerThread)
   {
-    const u32 id = ids[i];
-    if (id >= n)
-      continue; // only reachable after a reported sort failure
-    const T* src = ent + u64(id) * W;
-    T* dst = out + i * W;
+    T v[kGatherPerThread][W];
+    u32 id[kGatherPerThread];
 #pragma unroll
-    for (int c = 0; c < W; ++c)
-      dst[c] = src[c];
+    for (int k = 0; k < kGatherPerThread; ++k)
+    {
+      const u64 i = i0 + k * stride;
+      id[k] = i < n ? ids[i] : 0xffffffffu;
+    }
+#pragma unroll
+    for (int k = 0; k < kGatherPerThread; ++k)
+#pragma unroll
+      for (int c = 0; c < W; ++c)
+        v[k][c] = id[k] < n ? ent[u64(id[k]) * W + c] : T(0);
+#pragma unroll
+    for (int k = 0; k < kGatherPerThread; ++k)
+    {
+      const u64 i = i0 + k * stride;
+      if (i < n && id[k] < n)
+#pragma unroll
+        for (int c = 0; c < W; ++c)
+          out[i * W + c] = v[k][c];
+    }
   }
 }
 
@@ -461,35 +479,103 @@ __device__ __forceinline__ void level_range(const u32* levelCount, u32 d, u32& b
   cnt = levelCount[d];
 }
 
-// Four nodes per warp, eight lanes per node: lane 0 finds the end of the node's stuck entities
-// (ProcessNode's partition_point, :658-671), lanes 1..7 find the start of child key ranges 1..7
+// MinPoint of a node from the table (identical arithmetic, computed once per cell), dimension dim
+template<typename T>
+__device__ __forceinline__ void write_min_point(T* nodeBox, u32 node, u64 key, u32 d, int dim, const T* minTab, u64 tabPerDim, const Space<T>* spg)
+{
+  const u64 loc = key ^ (u64(1) << (3 * d));
+  const u32 cell = compact1by2(loc >> dim);
+  T* nb = nodeBox + u64(node) * 6;
+  nb[dim] = minTab[u64(dim) * tabPerDim + ((u64(1) << d) - 1) + cell];
+  nb[3 + dim] = spg->nodeSize[d][dim];
+}
+
+// Two launches per depth. emit_classify_kernel, one thread per node: a node that does not split
+// (at most maxElem entities in its subtree, or d == maxDepth) keeps all of them and is finished at
+// once (ProcessNode, :656-683); a node that splits goes to a queue. emit_split_kernel, eight lanes
+// per queued node: lane 0 finds the end of the node's stuck entities (ProcessNode's
+// partition_point, :658-671) and lanes 1..7 the start of child key ranges 1..7
 // (CreateProcessingData's partition_point, :695-711) at the same time, so the dependent-load
 // chain of a node is one binary search deep. Below the root every key of a node's range shares
-// its prefix, so the end of child 7 is the end of the range; at the root lane 0 also searches it
+// its prefix, so child 7 ends where the range ends; at the root lane 0 also searches that end
 // (locations outside the 3*D-bit grid sort after every child range and belong to no child).
+template<typename T, bool IS_BOX>
+__global__ void __launch_bounds__(256) emit_classify_kernel(u32 d, u32 D, u64 maxElem, uint4* __restrict__ link, const u64* __restrict__ nodeKey,
+                                                            T* __restrict__ nodeBox, const u32* __restrict__ levelCount, u32* __restrict__ splitCount,
+                                                            u32* __restrict__ splitQueue, u32 queueCap, const T* __restrict__ minTab,
+                                                            const Space<T>* __restrict__ spg, u32* __restrict__ ownerNode, u32* __restrict__ err)
+{
+  u32 begin, cnt;
+  level_range(levelCount, d, begin, cnt);
+  const int lane = threadIdx.x & 31;
+  const u64 tabPerDim = (u64(2) << D) - 1;
+  for (u32 i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < cnt; i0 += gridDim.x * blockDim.x)
+  {
+    const u32 i = i0 + lane;
+    bool split = false;
+    u32 node = 0;
+    if (i < cnt)
+    {
+      node = begin + i;
+      const uint4 L = link[node];
+      split = u64(L.w - L.y) > maxElem && d < D;
+      if (!split)
+      {
+        link[node] = make_uint4(0, L.y, L.w, L.w);
+        if (ownerNode)
+          for (u32 q = L.y; q < L.w; ++q)
+            ownerNode[q] = node;
+        if constexpr (!IS_BOX)
+        {
+          const u64 key = nodeKey[node];
+#pragma unroll
+          for (int dim = 0; dim < 3; ++dim)
+            write_min_point(nodeBox, node, key, d, dim, minTab, tabPerDim, spg);
+        }
+      }
+    }
+    const u32 m = __ballot_sync(0xffffffffu, split);
+    u32 qb = 0;
+    if (lane == 0 && m)
+      qb = atomicAdd(&splitCount[d], __popc(m));
+    qb = __shfl_sync(0xffffffffu, qb, 0);
+    if (split)
+    {
+      const u32 slot = qb + __popc(m & lanemask_lt());
+      if (slot < queueCap) // a node that splits holds more than maxElem entities: at most n / (maxElem + 1) per depth
+        splitQueue[slot] = node;
+      else
+        atomicOr(err, kErrCapacity);
+    }
+  }
+}
+
+constexpr u32 kEmitCountMax = 256;
+
 template<typename T, typename K, bool IS_BOX>
-__global__ void __launch_bounds__(256) emit_level_kernel(u32 d, u32 D, u64 maxElem, const K* __restrict__ keys, uint4* __restrict__ link,
-                                                         u64* __restrict__ nodeKey, T* __restrict__ nodeBox, unsigned char* __restrict__ nodeDepth,
-                                                         u32* __restrict__ levelCount, const T* __restrict__ minTab, const Space<T>* __restrict__ spg,
-                                                         u64 maxNodes, u32* __restrict__ err, u32* __restrict__ ownerNode, u32* __restrict__ nodeParent)
+__global__ void __launch_bounds__(256) emit_split_kernel(u32 d, u32 D, const K* __restrict__ keys, uint4* __restrict__ link, u64* __restrict__ nodeKey,
+                                                         T* __restrict__ nodeBox, unsigned char* __restrict__ nodeDepth, u32* __restrict__ levelCount,
+                                                         const u32* __restrict__ splitCount, const u32* __restrict__ splitQueue, u32 queueCap,
+                                                         const T* __restrict__ minTab, const Space<T>* __restrict__ spg, u64 maxNodes, u32* __restrict__ err,
+                                                         u32* __restrict__ ownerNode, u32* __restrict__ nodeParent)
 {
   u32 begin, cnt;
   level_range(levelCount, d, begin, cnt);
   const u32 childBase = begin + cnt;
+  const u32 qcount = min(splitCount[d], queueCap);
   const int lane = threadIdx.x & 31;
   const int grp = lane >> 3, gl = lane & 7;
   const u32 groupMask = 0xffu << (grp * 8);
   const u32 warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const u32 warpsTotal = (gridDim.x * blockDim.x) >> 5;
   const u64 tabPerDim = (u64(2) << D) - 1;
-  for (u32 base = warpGlobal * 4; base < cnt; base += warpsTotal * 4)
+  for (u32 qbase = warpGlobal * 4; qbase < qcount; qbase += warpsTotal * 4)
   {
-    const u32 i = base + grp;
-    const bool active = i < cnt;
-    const u32 node = begin + i;
+    const u32 qi = qbase + grp;
+    const bool active = qi < qcount;
+    const u32 node = active ? splitQueue[qi] : 0;
     u32 b = 0, e = 0, bnd = 0, end8 = 0;
     u64 key = 1;
-    bool split = false;
     if (active)
     {
       const uint4 L = link[node];
@@ -497,39 +583,85 @@ __global__ void __launch_bounds__(256) emit_level_kernel(u32 d, u32 D, u64 maxEl
       b = L.y;
       e = L.w;
       end8 = e;
-      split = u64(e - b) > maxElem && d < D;
-      if (split)
+    }
+    // small ranges: the group reads the range once and counts keys per child (coalesced, two
+    // round trips); large ranges (upper depths): one binary search per lane
+    const bool small = active && d > 0 && (e - b) <= kEmitCountMax; // uniform within a group
+    if (__any_sync(0xffffffffu, small))
+    {
+      // all lanes run the counting loop and the shuffles; groups that are not small count nothing
+      const u32 shiftChild = 3 * (D - d - 1);
+      u32 below[8]; // keys of this lane with child index < c (c = 1..7), and stuck keys in [0]
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        below[c] = 0;
+      const u64 lmin = (key ^ (u64(1) << (3 * d))) << (3 * (D - d));
+      for (u32 q = b + gl; small && q < e; q += 8)
       {
-        const u64 lmin = (key ^ (u64(1) << (3 * d))) << (3 * (D - d));
-        const u64 S = u64(1) << (3 * (D - d - 1));
-        if (gl == 0)
+        const u64 k = u64(keys[q]);
+        if constexpr (IS_BOX)
         {
-          if constexpr (IS_BOX)
-            bnd = upper_bound_key(keys, b, e, (lmin << 5) | u64(d));
-          else
-            bnd = (d == 0) ? upper_bound_key(keys, b, e, 0) : b;
-          if (d == 0)
-          {
-            const u64 L8 = lmin + 8 * S;
-            end8 = lower_bound_key(keys, bnd, e, IS_BOX ? (L8 << 5) : (L8 + 1));
-          }
+          const bool stuck = k <= ((lmin << 5) | u64(d));
+          below[0] += stuck ? 1u : 0u;
+          const u32 c = stuck ? 0u : u32(((k >> 5) >> shiftChild) & 7u);
+#pragma unroll
+          for (int cc = 1; cc < 8; ++cc)
+            below[cc] += (stuck || c < u32(cc)) ? 1u : 0u;
         }
         else
         {
-          const u64 L0 = lmin + u64(gl) * S;
-          bnd = lower_bound_key(keys, b, e, IS_BOX ? (L0 << 5) : (L0 + 1));
+          const u32 c = u32(((k - 1) >> shiftChild) & 7u);
+#pragma unroll
+          for (int cc = 1; cc < 8; ++cc)
+            below[cc] += c < u32(cc) ? 1u : 0u;
         }
+      }
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+      {
+        u32 v = below[c];
+        v += __shfl_xor_sync(0xffffffffu, v, 1);
+        v += __shfl_xor_sync(0xffffffffu, v, 2);
+        v += __shfl_xor_sync(0xffffffffu, v, 4);
+        below[c] = v;
+      }
+      u32 mine = below[0];
+#pragma unroll
+      for (int c = 1; c < 8; ++c)
+        mine = gl == c ? below[c] : mine;
+      if (small)
+        bnd = b + mine;
+    }
+    if (active && !small)
+    {
+      const u64 lmin = (key ^ (u64(1) << (3 * d))) << (3 * (D - d));
+      const u64 S = u64(1) << (3 * (D - d - 1));
+      if (gl == 0)
+      {
+        if constexpr (IS_BOX)
+          bnd = upper_bound_key(keys, b, e, (lmin << 5) | u64(d));
+        else
+          bnd = (d == 0) ? upper_bound_key(keys, b, e, 0) : b;
+        if (d == 0)
+        {
+          const u64 L8 = lmin + 8 * S;
+          end8 = lower_bound_key(keys, bnd, e, IS_BOX ? (L8 << 5) : (L8 + 1));
+        }
+      }
+      else
+      {
+        const u64 L0 = lmin + u64(gl) * S;
+        bnd = lower_bound_key(keys, b, e, IS_BOX ? (L0 << 5) : (L0 + 1));
       }
     }
     const u32 end8g = __shfl_sync(0xffffffffu, end8, grp * 8);
     const u32 myStart = bnd;                                            // lane c: start of child c (lane 0: stuck end)
     const u32 nextLane = __shfl_sync(0xffffffffu, bnd, (lane + 1) & 31); // lane c: start of child c + 1
     const u32 nextStart = gl < 7 ? nextLane : end8g;
-    const bool nonEmpty = active && split && nextStart > myStart;
+    const bool nonEmpty = active && nextStart > myStart;
     const u32 ballot = __ballot_sync(0xffffffffu, nonEmpty) & groupMask;
     const u32 nchild = __popc(ballot);
-    const u32 stuckEnd = __shfl_sync(0xffffffffu, bnd, grp * 8);
-    const u32 ownEnd = split ? stuckEnd : e;
+    const u32 ownEnd = __shfl_sync(0xffffffffu, bnd, grp * 8);
     // warp-aggregated allocation of the children slots (children of one node are contiguous)
     const u32 mine = (gl == 0) ? nchild : 0u;
     u32 incl = mine;
@@ -569,17 +701,8 @@ __global__ void __launch_bounds__(256) emit_level_kernel(u32 d, u32 D, u64 maxEl
         for (u32 q = b + gl; q < ownEnd; q += 8)
           ownerNode[q] = node;
       if constexpr (!IS_BOX)
-      {
         if (gl < 3)
-        {
-          // MinPoint from the node table (identical arithmetic, computed once per cell)
-          const u64 loc = key ^ (u64(1) << (3 * d));
-          const u32 cell = compact1by2(loc >> gl);
-          T* nb = nodeBox + u64(node) * 6;
-          nb[gl] = minTab[u64(gl) * tabPerDim + ((u64(1) << d) - 1) + cell];
-          nb[3 + gl] = spg->nodeSize[d][gl];
-        }
-      }
+          write_min_point(nodeBox, node, key, d, gl, minTab, tabPerDim, spg);
     }
   }
 }
@@ -730,7 +853,8 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   if ((e = t.keysA.ensure(sizeof(K) * n)) || (e = t.keysB.ensure(sizeof(K) * n)) || (e = t.sortedIds.ensure(sizeof(u32) * n)) ||
       (e = t.valsB.ensure(sizeof(u32) * n)) || (e = t.sortedGeom.ensure(sizeof(T) * W * n)) || (e = t.nodeLink.ensure(sizeof(uint4) * maxNodes)) ||
       (e = t.nodeKey.ensure(sizeof(u64) * maxNodes)) || (e = t.nodeBox.ensure(sizeof(T) * 6 * maxNodes)) ||
-      (e = t.nodeDepth.ensure(maxNodes)) || (e = t.levelCount.ensure(sizeof(u32) * 32)) || (e = t.space.ensure(sizeof(Space<T>))) ||
+      (e = t.nodeDepth.ensure(maxNodes)) || (e = t.levelCount.ensure(sizeof(u32) * 64)) ||
+      (e = t.splitQueue.ensure(sizeof(u32) * (n / (t.maxElem + 1) + 2))) || (e = t.space.ensure(sizeof(Space<T>))) ||
       (e = t.sortScratch.ensure(SortScratch::bytes(n, passes))) || (e = t.bboxBits.ensure(sizeof(U) * 6)) ||
       (e = t.rasterTab.ensure(tabBytes)) || (e = t.minTab.ensure(sizeof(T) * minTabEntries)) ||
       (IS_BOX && ((e = t.nodeMax.ensure(sizeof(T) * 3 * maxNodes)) || (e = t.ownerNode.ensure(sizeof(u32) * n)) ||
@@ -743,7 +867,7 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   SortScratch ss;
   ss.carve(t.sortScratch.p, n, passes);
   cudaMemsetAsync(t.sortScratch.p, 0, SortScratch::bytes(n, passes), st);
-  cudaMemsetAsync(t.levelCount.p, 0, sizeof(u32) * 32, st);
+  cudaMemsetAsync(t.levelCount.p, 0, sizeof(u32) * 64, st);
 
   const bool vec = (reinterpret_cast<uintptr_t>(ent) & 15) == 0;
   Space<T>* sp = t.space.as<Space<T>>();
@@ -799,17 +923,29 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   const K* keys = reinterpret_cast<const K*>(t.sortedKeys);
 
   prof.mark("gather", st);
-  gather_kernel<T, W><<<grid_blocks(n, 256, 152 * 8), 256, 0, st>>>(ent, t.sortedIds.as<u32>(), n, t.sortedGeom.as<T>());
+  gather_kernel<T, W><<<grid_blocks((n + kGatherPerThread - 1) / kGatherPerThread, 256, 152 * 16), 256, 0, st>>>(ent, t.sortedIds.as<u32>(), n,
+                                                                                                                  t.sortedGeom.as<T>());
+
 
   prof.mark("emit", st);
   u32* parent = IS_BOX ? t.nodeParent.as<u32>() : nullptr;
   root_init_kernel<T><<<1, 32, 0, st>>>(t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeDepth.as<unsigned char>(), t.levelCount.as<u32>(), u32(n),
                                         parent);
-  const int emitBlocks = grid_blocks(maxNodes / 4, 256, 152 * 16);
+  const int emitBlocks = grid_blocks(maxNodes, 256, 152 * 16);
+  u32* levelCount = t.levelCount.as<u32>();
+  u32* splitCount = levelCount + 32;
+  u32* splitQueue = t.splitQueue.as<u32>();
+  const u32 queueCap = u32(n / (t.maxElem + 1) + 2);
   for (u32 d = 0; d <= D; ++d)
-    emit_level_kernel<T, K, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, D, t.maxElem, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
-                                                                t.nodeDepth.as<unsigned char>(), t.levelCount.as<u32>(), t.minTab.as<T>(), sp, maxNodes,
-                                                                t.err.as<u32>(), IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent);
+  {
+    emit_classify_kernel<T, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, D, t.maxElem, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(), levelCount,
+                                                                splitCount, splitQueue, queueCap, t.minTab.as<T>(), sp,
+                                                                IS_BOX ? t.ownerNode.as<u32>() : nullptr, t.err.as<u32>());
+    if (d < D)
+      emit_split_kernel<T, K, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, D, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
+                                                                  t.nodeDepth.as<unsigned char>(), levelCount, splitCount, splitQueue, queueCap, t.minTab.as<T>(), sp,
+                                                                  maxNodes, t.err.as<u32>(), IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent);
+  }
   prof.mark("geometry", st);
   if constexpr (IS_BOX)
   {

@@ -98,7 +98,8 @@ struct TreeState
   DevBuf nodeLink, nodeKey, nodeBox, nodeMax, nodeDepth;
   DevBuf ownerNode; // u32 per sorted position: the node holding that entity (box trees)
   DevBuf nodeParent; // u32 per node (box trees)
-  DevBuf levelCount; // u32[32]: nodes per depth
+  DevBuf levelCount; // u32[64]: nodes per depth, then splitting nodes per depth
+  DevBuf splitQueue; // u32: nodes of the current depth that split
   DevBuf space;      // Space<T>
   DevBuf sortScratch;
   DevBuf err;        // u32 device error bits

@@ -25,6 +25,7 @@ constexpr u32 kStatusAggregate = 1u << 30;
 constexpr u32 kStatusInclusive = 2u << 30;
 constexpr u32 kStatusValueMask = (1u << 30) - 1;
 constexpr u32 kLookbackSpinLimit = 1u << 22;
+constexpr int kLookbackBatch = 8;
 
 // error bits reported by device code
 constexpr u32 kErrTimeout = 1u;
@@ -133,20 +134,21 @@ __global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass_kernel(const K*
     vals[i] = vin ? (valid ? vin[idx] : 0u) : u32(idx);
     dig[i] = valid ? u32((keys[i] >> shift) & (kRadix - 1)) : u32(kRadix);
   }
+  // rank within the warp: lanes with equal digits elect a leader whose shared atomic returns the
+  // count of that digit in earlier items (atomics of one warp to one address apply in issue order),
+  // so the items pipeline instead of forming a load/store chain
   const u32 ltmask = lanemask_lt();
 #pragma unroll
   for (int i = 0; i < kSortItems; ++i)
   {
-    u32 d = dig[i];
-    u32 peers = __match_any_sync(0xffffffffu, d);
-    u32 cnt = 0;
-    if (d < kRadix)
-      cnt = s_warpHist[warp][d];
-    rank[i] = cnt + __popc(peers & ltmask);
-    __syncwarp();
-    if (d < kRadix && lane == __ffs(peers) - 1)
-      s_warpHist[warp][d] = cnt + __popc(peers);
-    __syncwarp();
+    const u32 d = dig[i];
+    const u32 peers = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(peers) - 1;
+    u32 old = 0;
+    if (d < kRadix && lane == leader)
+      old = atomicAdd(&s_warpHist[warp][d], u32(__popc(peers)));
+    old = __shfl_sync(0xffffffffu, old, leader);
+    rank[i] = old + __popc(peers & ltmask);
   }
   __syncthreads();
 
@@ -162,7 +164,7 @@ __global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass_kernel(const K*
       s_warpHist[w][tid] = total;
       total += c;
     }
-    // decoupled look-back over earlier tiles for digit tid
+    // decoupled look-back over earlier tiles for digit tid, eight predecessors per round trip
     volatile u32* vstatus = status;
     if (tile == 0)
     {
@@ -175,9 +177,28 @@ __global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass_kernel(const K*
       u32 spins = 0;
       while (j >= 0)
       {
-        u32 sv = vstatus[u64(j) * kRadix + tid];
-        u32 flag = sv & ~kStatusValueMask;
-        if (flag == 0)
+        u32 sv[kLookbackBatch];
+#pragma unroll
+        for (int k = 0; k < kLookbackBatch; ++k)
+          sv[k] = (j - k >= 0) ? vstatus[u64(j - k) * kRadix + tid] : u32(kStatusInclusive);
+        int used = 0;
+        bool done = false;
+#pragma unroll
+        for (int k = 0; k < kLookbackBatch; ++k)
+        {
+          if (done || used < k)
+            continue;
+          const u32 flag = sv[k] & ~kStatusValueMask;
+          if (flag == 0)
+            continue; // not published yet: re-read from here
+          prefix += sv[k] & kStatusValueMask;
+          used = k + 1;
+          done = flag == kStatusInclusive;
+        }
+        if (done)
+          break;
+        j -= used;
+        if (used < kLookbackBatch)
         {
           if (++spins > kLookbackSpinLimit)
           {
@@ -185,12 +206,7 @@ __global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass_kernel(const K*
             break;
           }
           __nanosleep(32);
-          continue;
         }
-        prefix += sv & kStatusValueMask;
-        if (flag == kStatusInclusive)
-          break;
-        --j;
       }
       vstatus[u64(tile) * kRadix + tid] = kStatusInclusive | ((prefix + total) & kStatusValueMask);
     }
@@ -222,18 +238,47 @@ __global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass_kernel(const K*
   __syncthreads();
 
   const u32 tileCount = u32(min(u64(kSortTile), u64(n) - base));
-  for (u32 j = tid; j < tileCount; j += kSortThreads)
+  if (tileCount == kSortTile)
   {
-    K k = s_keys[j];
-    u32 d = u32((k >> shift) & (kRadix - 1));
-    u32 pos = s_globalBase[d] + j;
-    if (pos < n)
+    K kk[kSortItems];
+    u32 vv[kSortItems], pp[kSortItems];
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k)
     {
-      kout[pos] = k;
-      vout[pos] = s_vals[j];
+      const u32 j = tid + k * kSortThreads;
+      kk[k] = s_keys[j];
+      vv[k] = s_vals[j];
     }
-    else
-      atomicOr(err, kErrTimeout);
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k)
+      pp[k] = s_globalBase[u32((kk[k] >> shift) & (kRadix - 1))] + tid + k * kSortThreads;
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k)
+    {
+      if (pp[k] < n)
+      {
+        kout[pp[k]] = kk[k];
+        vout[pp[k]] = vv[k];
+      }
+      else
+        atomicOr(err, kErrTimeout);
+    }
+  }
+  else
+  {
+    for (u32 j = tid; j < tileCount; j += kSortThreads)
+    {
+      K k = s_keys[j];
+      u32 d = u32((k >> shift) & (kRadix - 1));
+      u32 pos = s_globalBase[d] + j;
+      if (pos < n)
+      {
+        kout[pos] = k;
+        vout[pos] = s_vals[j];
+      }
+      else
+        atomicOr(err, kErrTimeout);
+    }
   }
 }
 
