@@ -156,6 +156,27 @@ int otg_collision_self(const otg_tree* tree, double tol, int algo, otg_result** 
    Pairs (left id, right id), ascending. */
 int otg_collision_pair(const otg_tree* left, const otg_tree* right, double tol, int algo, otg_result** out, void* stream);
 
+/* kNN query that allocates no memory. No counterpart in the reference, whose
+   GetNearestNeighbors (core/ot_query.h:1208-1270) answers one query with a freshly allocated
+   std::vector. It exists for callers that cannot allocate device memory per call: frame loops
+   with a fixed memory budget, code that must avoid the device-wide synchronisation that
+   cudaMalloc/cudaFree imply, processes whose allocator is closed after start-up.
+   The result equals otg_knn(..., k = NULL, k_all = k, ...): counts[q] is the number of ids the
+   query has (ties within the tolerance can make it exceed k); the first min(counts[q],
+   slot_capacity) of them, by (distance, id), are written to ids[q * slot_capacity ...] and
+   distances[q * slot_capacity ...]. counts[q] > slot_capacity tells the caller the slot was too
+   small. points, counts, ids and distances must be device memory; the tree must have been
+   synchronised (otg_tree_sync or any earlier query). The call returns after its kernels finished.
+   Scratch: a fixed array in the library's static device memory (8 MiB + 256 bytes per device)
+   holds one threshold per query, so n_queries is at most 1048576 (larger values return
+   OTG_ERR_INVALID_ARGUMENT); k is at most 256. The first call on each device looks up the
+   array's device address (with that device current); make that first call, for instance with
+   n_queries = 0, which only does this set-up, before any stream capture begins. All calls on a
+   device share the one scratch array: calls that overlap on the GPU (from several host threads
+   or streams) race on it, so the caller must serialise them. */
+int otg_knn_noalloc(const otg_tree* tree, const void* points, uint64_t n_queries, uint32_t k, double max_distance, double tol,
+                    uint32_t slot_capacity, uint32_t* counts, uint32_t* ids, double* distances, void* stream);
+
 /* ---------------------------------------------------------------- results */
 int otg_result_info(const otg_result* r, uint64_t* n_queries, uint64_t* n_ids, int* has_distances);
 /* offsets[n_queries+1], ids[n_ids], distances[n_ids] (double; may be NULL). mem: destination space. */

@@ -51,6 +51,7 @@ EXPORTS = [
     ("otg_ray_first", _int, [_vp, _vp, _u64, _dbl, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_collision_self", _int, [_vp, _dbl, _int, C.POINTER(_vp), _vp]),
     ("otg_collision_pair", _int, [_vp, _vp, _dbl, _int, C.POINTER(_vp), _vp]),
+    ("otg_knn_noalloc", _int, [_vp, _vp, _u64, _u32, _dbl, _dbl, _u32, _vp, _vp, _vp, _vp]),
     ("otg_result_info", _int, [_vp, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_int)]),
     ("otg_result_copy", _int, [_vp, _vp, _vp, _vp, _int, _vp]),
     ("otg_result_device_ptrs", _int, [_vp, _vp, _vp, _vp]),

@@ -331,6 +331,21 @@ extern "C"
     return run_query(a, out, (cudaStream_t)stream, [&](ResultState& r) { return query_collide_pair(a->s, b->s, tol, algo, r, (cudaStream_t)stream); });
   }
 
+  int otg_knn_noalloc(const otg_tree* t, const void* points, uint64_t nq, uint32_t k, double max_distance, double tol, uint32_t slot_capacity,
+                      uint32_t* counts, uint32_t* ids, double* distances, void* stream)
+  {
+    if (int rc = require_device())
+      return rc;
+    if (int rc = require_tree(t))
+      return rc;
+    if (!t->s.countsKnown)
+    {
+      set_error("the tree's build has not been synchronised (call otg_tree_sync first)");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+    return query_knn_noalloc(t->s, points, nq, k, max_distance, tol, slot_capacity, counts, ids, distances, (cudaStream_t)stream);
+  }
+
   int otg_result_info(const otg_result* r, uint64_t* nq, uint64_t* nids, int* has_distances)
   {
     if (!r)

@@ -159,5 +159,8 @@ int query_ray(const TreeState& t, const void* rays, u64 nq, double tol, double t
               int mem, cudaStream_t st);
 int query_collide_self(const TreeState& t, double tol, int algo, ResultState& r, cudaStream_t st);
 int query_collide_pair(const TreeState& a, const TreeState& b, double tol, int algo, ResultState& r, cudaStream_t st);
+// kNN into caller-owned slots with static scratch: allocates no memory
+int query_knn_noalloc(const TreeState& t, const void* pts, u64 nq, u32 k, double maxDist, double tol, u32 cap, u32* counts, u32* ids, double* dist,
+                      cudaStream_t st);
 
 } // namespace otg

@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 namespace otg
@@ -1448,6 +1449,201 @@ int query_collide_self(const TreeState& t, double tol, int algo, ResultState& r,
 int query_collide_pair(const TreeState& a, const TreeState& b, double tol, int algo, ResultState& r, cudaStream_t st)
 {
   return a.scalar == OTG_SCALAR_F64 ? collide_impl<double>(a, b, false, tol, algo, r, st) : collide_impl<float>(a, b, false, tol, algo, r, st);
+}
+
+// ---------------------------------------------------------------- kNN without allocation
+// Some callers cannot allocate device memory per call: a frame loop with a fixed memory budget
+// (physics or game ticks that query neighbours every frame), code that must not trigger the
+// implicit device synchronisation of cudaMalloc/cudaFree, or a pool-managed process that forbids
+// allocations after start-up. For them the kNN query keeps its only scratch (the per-query
+// threshold of the first pass and a status word) in a fixed array in the module's static device
+// memory, and writes results straight into caller-owned per-query slots instead of a result
+// object. The scratch is shared by every call on a device, so calls that overlap on the GPU
+// (several host threads, or several streams) race on it and must be serialised by the caller.
+constexpr u64 kNoAllocMaxQueries = u64(1) << 20;            // queries per call
+constexpr u64 kNoAllocScratchBytes = 256 + 8 * kNoAllocMaxQueries; // status word, then one threshold per query
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noAllocScratch[kNoAllocScratchBytes];
+
+// Pass 2 of the kNN query writing into slots: every entity with (min) distance < F is counted,
+// and the smallest `cap` of them by (distance, id) are kept in the query's slot, in that order.
+template<typename T>
+__global__ void __launch_bounds__(128) knn_collect_slots_kernel(TreeView<T> tv, const T* __restrict__ pts, u32 nq, const T* __restrict__ Fin, T tol,
+                                                                u32 cap, u32* __restrict__ counts, u32* __restrict__ ids, double* __restrict__ dist,
+                                                                u32* err)
+{
+  using G = GeoD<T>;
+  const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq)
+    return;
+  const T F = Fin[q];
+  T p[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    p[c] = pts[u64(q) * 3 + c];
+  u32* sid = ids + u64(q) * cap;
+  double* sd = dist + u64(q) * cap;
+  u32 found = 0, kept = 0;
+  u32 stack[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp++] = 0;
+  while (sp > 0)
+  {
+    const u32 node = stack[--sp];
+    const T* nb = tv.nodeBox + u64(node) * 6;
+    if (G::wall_distance(p, nb, nb + 3) >= F)
+      continue;
+    const uint4 L = tv.link[node];
+    if (L.z > tv.n || L.w > tv.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      break;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      const T d = entity_distance(tv, e, p, tol);
+      if (!(d < F))
+        continue;
+      ++found;
+      const double dd = double(d);
+      const u32 id = tv.ids[e];
+      // insertion into the sorted slot; the largest entry falls off a full slot
+      u32 j = kept;
+      while (j > 0 && (dd < sd[j - 1] || (dd == sd[j - 1] && id < sid[j - 1])))
+      {
+        if (j < cap)
+        {
+          sd[j] = sd[j - 1];
+          sid[j] = sid[j - 1];
+        }
+        --j;
+      }
+      if (j < cap)
+      {
+        sd[j] = dd;
+        sid[j] = id;
+      }
+      if (kept < cap)
+        ++kept;
+    }
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      break;
+    }
+    for (u32 c = 0; c < cc; ++c)
+      stack[sp++] = fc + c;
+  }
+  counts[q] = found;
+}
+
+// Device address of the static scratch on the current device, looked up once per device.
+static int noalloc_scratch(unsigned char** out)
+{
+  static std::mutex lock;
+  static unsigned char* addr[kNoAllocMaxDevices] = {};
+  int dev = 0;
+  if (cudaError_t e = cudaGetDevice(&dev))
+    return cuda_status(e, "querying the current device");
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+  {
+    set_error("device ordinal above the supported maximum of 63");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
+  std::lock_guard<std::mutex> g(lock);
+  if (!addr[dev])
+  {
+    void* p = nullptr;
+    if (cudaError_t e = cudaGetSymbolAddress(&p, g_noAllocScratch))
+      return cuda_status(e, "looking up the no-allocation scratch");
+    addr[dev] = (unsigned char*)p;
+  }
+  *out = addr[dev];
+  return OTG_OK;
+}
+
+static bool device_accessible(const void* p)
+{
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+  {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+template<typename T>
+static int knn_noalloc_impl(const TreeState& t, const void* pts, u64 nq, u32 k, double maxDist, double tol, u32 cap, u32* counts, u32* ids,
+                            double* dist, unsigned char* scratch, cudaStream_t st)
+{
+  cudaError_t e;
+  if (t.n == 0)
+  {
+    e = cudaMemsetAsync(counts, 0, sizeof(u32) * nq, st);
+    if (!e)
+      e = cudaStreamSynchronize(st);
+    return cuda_status(e, "empty kNN result");
+  }
+  u32* err = (u32*)scratch;
+  T* F = (T*)(scratch + 256);
+  if ((e = cudaMemsetAsync(err, 0, sizeof(u32), st)))
+    return cuda_status(e, "clearing the kNN status");
+  auto tv = view<T>(t);
+  const T tl = tol_of<T>(tol);
+  const T F0 = maxDist < 0 ? Lim<T>::max() : upper_tol_host(T(maxDist), tl);
+  const u32 blocks = u32((nq + 127) / 128);
+  knn_threshold_kernel<T><<<blocks, 128, 0, st>>>(tv, (const T*)pts, u32(nq), nullptr, k, F0, tl, F, err);
+  knn_collect_slots_kernel<T><<<blocks, 128, 0, st>>>(tv, (const T*)pts, u32(nq), F, tl, cap, counts, ids, dist, err);
+  if ((e = cudaGetLastError()))
+    return cuda_status(e, "launching the kNN query");
+  u32 h = 0;
+  e = cudaMemcpyAsync(&h, err, sizeof(u32), cudaMemcpyDeviceToHost, st);
+  if (!e)
+    e = cudaStreamSynchronize(st);
+  if (e)
+    return cuda_status(e, "running the kNN query");
+  if (h & kErrStack)
+  {
+    set_error("traversal stack bound exceeded");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
+  return OTG_OK;
+}
+
+int query_knn_noalloc(const TreeState& t, const void* pts, u64 nq, u32 k, double maxDist, double tol, u32 cap, u32* counts, u32* ids, double* dist,
+                      cudaStream_t st)
+{
+  unsigned char* scratch = nullptr;
+  if (int rc = noalloc_scratch(&scratch)) // set-up happens even for n_queries == 0
+    return rc;
+  if (nq == 0)
+    return OTG_OK;
+  if (nq > kNoAllocMaxQueries)
+  {
+    set_error("n_queries above the no-allocation maximum of 1048576");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  if (k > u32(kKnnMaxK))
+  {
+    set_error("k above the supported maximum of 256");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
+  if (!pts || !counts || (cap && (!ids || !dist)))
+  {
+    set_error("points and counts (and ids and distances when slot_capacity > 0) must be given");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  if (!device_accessible(pts) || !device_accessible(counts) || (cap && (!device_accessible(ids) || !device_accessible(dist))))
+  {
+    set_error("points, counts, ids and distances must be device memory");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  return t.scalar == OTG_SCALAR_F64 ? knn_noalloc_impl<double>(t, pts, nq, k, maxDist, tol, cap, counts, ids, dist, scratch, st)
+                                    : knn_noalloc_impl<float>(t, pts, nq, k, maxDist, tol, cap, counts, ids, dist, scratch, st);
 }
 
 } // namespace otg
