@@ -357,12 +357,41 @@ def time_query(fn, reps=3):
     return statistics.median(t)
 
 
+def cluster_boxes(n, seed):
+    """Self-collision workload: centres 50% uniform in [0,1000)^3 and 50% from 64 isotropic Gaussian
+    clusters (sigma 10, centres uniform), half-extents lognormal(ln 0.5, 0.6) per axis."""
+    rng = np.random.default_rng(seed)
+    half = n // 2
+    centres = np.empty((n, 3))
+    centres[:half] = rng.random((half, 3)) * 1000
+    cc = np.random.default_rng(seed + 1).random((64, 3)) * 1000
+    pick = rng.integers(0, 64, n - half)
+    centres[half:] = cc[pick] + rng.normal(0, 10, (n - half, 3))
+    ext = rng.lognormal(np.log(0.5), 0.6, (n, 3))
+    return np.concatenate([centres - ext, centres + ext], 1)
+
+
+def mismatched_queries(a, b):
+    """Number of queries whose (id, distance) lists differ between two CSR results."""
+    oa, ob = a[0].astype(np.int64), b[0].astype(np.int64)
+    if np.array_equal(oa, ob) and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2]):
+        return 0
+    bad = 0
+    for qi in range(len(oa) - 1):
+        x = slice(oa[qi], oa[qi + 1])
+        y = slice(ob[qi], ob[qi + 1])
+        if not (np.array_equal(a[1][x], b[1][y]) and np.array_equal(a[2][x], b[2][y])):
+            bad += 1
+    return bad
+
+
 def run_queries(tree16, pts16_d, stream):
     import torch
 
     import octree_gb300 as otg
 
     out = {}
+    algos = ((otg.ALGO_PLAIN_FP64, "plain_fp64"), (otg.ALGO_FILTERED, "filtered_fp32"))
     rng = np.random.default_rng(103)
     # 1M uniform points in [0,100]^3, 10k range boxes (edges U[0.5,5]), 10k kNN k=8
     p1 = np.random.default_rng(101).random((1_000_000, 3)) * 100
@@ -371,17 +400,32 @@ def run_queries(tree16, pts16_d, stream):
     e = np.random.default_rng(102).uniform(0.5, 5, (10_000, 3))
     ranges = torch.as_tensor(np.concatenate([c - e / 2, c + e / 2], 1), device="cuda")
     q = torch.as_tensor(rng.random((10_000, 3)) * 100, device="cuda")
-    for algo, name in ((otg.ALGO_PLAIN_FP64, "plain_fp64"),):
-        s = time_query(lambda: t1.range_search(ranges, algo=algo, raw=True))
-        out[f"range_1M_10k_{name}_Mq_per_s"] = 10_000 / s / 1e6
+    s = time_query(lambda: t1.range_search(ranges, algo=otg.ALGO_PLAIN_FP64, raw=True))
+    out["range_1M_10k_plain_fp64_Mq_per_s"] = 10_000 / s / 1e6
+    for algo, name in algos:
         s = time_query(lambda: t1.knn(q, 8, algo=algo, raw=True))
         out[f"knn8_1M_10k_{name}_Mq_per_s"] = 10_000 / s / 1e6
     # batched uneven kNN on the 16M tree: 1M queries from the same mixture, k in 1..64
     qk = torch.as_tensor(shell_points(1_000_000, 302), device="cuda")
     ks = torch.as_tensor(np.random.default_rng(303).integers(1, 65, 1_000_000).astype(np.int32), device="cuda")
-    for algo, name in ((otg.ALGO_PLAIN_FP64, "plain_fp64"),):
-        s = time_query(lambda: tree16.knn(qk, ks, algo=algo, raw=True), reps=1)
+    res = {}
+    for algo, name in algos:
+        s = time_query(lambda: tree16.knn(qk, ks, algo=algo, raw=True), reps=1 if algo == otg.ALGO_PLAIN_FP64 else 3)
         out[f"knn_uneven_16M_1Mq_{name}_Mq_per_s"] = 1_000_000 / s / 1e6
+        res[name] = tree16.knn(qk, ks, algo=algo)
+    tests, rechecks = tree16.knn(qk, ks, algo=otg.ALGO_FILTERED, raw=True).stats()
+    out["knn_uneven_recheck_fraction"] = rechecks / max(tests, 1)
+    out["knn_uneven_mismatched_queries_filtered_vs_plain"] = mismatched_queries(res["plain_fp64"], res["filtered_fp32"])
+    out["knn_uneven_speedup_filtered_vs_plain"] = out["knn_uneven_16M_1Mq_filtered_fp32_Mq_per_s"] / out["knn_uneven_16M_1Mq_plain_fp64_Mq_per_s"]
+    # self-collision of 4M clustered FP64 boxes, depth 12, max 32 per node
+    boxes = torch.as_tensor(cluster_boxes(4_000_000, 201), device="cuda")
+    tb = otg.Tree("boxes").create(boxes, max_depth=12, max_elements=32)
+    tb.sync()
+    s = time_query(lambda: tb.collision_self(algo=otg.ALGO_PLAIN_FP64, raw=True), reps=1)
+    pairs = tb.collision_self(algo=otg.ALGO_PLAIN_FP64, raw=True).sizes()[1] // 2
+    out["collide_self_4M_plain_fp64_ms"] = s * 1e3
+    out["collide_self_4M_pairs"] = int(pairs)
+    out["collide_self_4M_plain_fp64_Mpairs_per_s"] = pairs / s / 1e6
     return out
 
 

@@ -995,6 +995,7 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
   t.maxElem = maxElem;
   t.built = false;
   t.countsKnown = false;
+  t.image32 = false;
   t.boxGiven = box != nullptr;
   cudaError_t e;
   if ((e = t.err.ensure(sizeof(u32) * 4)))

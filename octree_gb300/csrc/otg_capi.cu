@@ -112,7 +112,7 @@ static int new_result(otg_result** out)
 static void release_tree(TreeState& s)
 {
   DevBuf* bufs[] = { &s.entities, &s.sortedIds, &s.sortedGeom, &s.keysA, &s.keysB, &s.valsB, &s.nodeLink, &s.nodeKey, &s.nodeBox,
-                     &s.nodeMax, &s.nodeDepth, &s.levelCount, &s.space, &s.sortScratch, &s.err, &s.bboxBits, &s.locations, &s.boxDev, &s.ownerNode, &s.nodeParent, &s.rasterTab, &s.minTab, &s.splitQueue };
+                     &s.nodeMax, &s.nodeDepth, &s.levelCount, &s.space, &s.sortScratch, &s.err, &s.bboxBits, &s.locations, &s.boxDev, &s.ownerNode, &s.nodeParent, &s.rasterTab, &s.minTab, &s.splitQueue, &s.geom32, &s.nodeBox32 };
   for (DevBuf* b : bufs)
     b->release();
 }

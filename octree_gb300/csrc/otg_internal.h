@@ -108,6 +108,9 @@ struct TreeState
   DevBuf boxDev;     // the given space box (6 scalars)
   DevBuf rasterTab;  // exact rasterisation thresholds (otg_raster.cuh)
   DevBuf minTab;     // MinPoint node table per (dimension, depth, cell)
+  DevBuf geom32;     // FP32 image of sortedGeom for the query filters (built on first use)
+  DevBuf nodeBox32;  // FP32 outward-rounded node boxes for the query filters
+  bool image32 = false;
 
   // cached after the build (host copies, filled by sync)
   u64 nodeCount = 0;
@@ -159,6 +162,8 @@ int query_ray(const TreeState& t, const void* rays, u64 nq, double tol, double t
               int mem, cudaStream_t st);
 int query_collide_self(const TreeState& t, double tol, int algo, ResultState& r, cudaStream_t st);
 int query_collide_pair(const TreeState& a, const TreeState& b, double tol, int algo, ResultState& r, cudaStream_t st);
+// batched filtered kNN on point trees (otg_knn.cu); inputs in device memory
+int knn_filtered(TreeState& t, const void* dpts, const u32* dk, u64 nq, u32 kAll, double maxDist, double tol, ResultState& r, cudaStream_t st);
 // kNN into caller-owned slots with static scratch: allocates no memory
 int query_knn_noalloc(const TreeState& t, const void* pts, u64 nq, u32 k, double maxDist, double tol, u32 cap, u32* counts, u32* ids, double* dist,
                       cudaStream_t st);

@@ -14,8 +14,7 @@
 // Results are appended as (query << 32 | id) items (plus a distance where the query has one),
 // then ordered with stable radix sorts into CSR form: ids ascending per query, or by
 // (distance, id) for kNN and rays, or (i, j) pairs ascending for collisions.
-#include "otg_internal.h"
-#include "otg_sort.cuh"
+#include "otg_query.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -24,48 +23,6 @@
 
 namespace otg
 {
-
-constexpr int kStack = 168; // > 7 * 19 + 1 entries: depth-first stack bound for maxDepth <= 19
-
-template<typename T>
-struct TreeView
-{
-  const uint4* link;
-  const T* nodeBox; // {min xyz, size xyz}
-  const T* nodeMax; // box trees: exact max corner
-  const u32* ids;   // sortedIds
-  const T* geom;    // sortedGeom
-  u32 n;
-  int isBox;
-  u32 nNodes;
-};
-
-struct Appender
-{
-  u64* items;      // (query << 32) | id
-  double* dist;    // optional
-  unsigned long long* count;
-  u64 capacity;
-  __device__ __forceinline__ void put(u32 q, u32 id, double d = 0.0)
-  {
-    u64 pos = atomicAdd(count, 1ull);
-    if (pos < capacity)
-    {
-      items[pos] = (u64(q) << 32) | id;
-      if (dist)
-        dist[pos] = d;
-    }
-  }
-  __device__ __forceinline__ u64 reserve(u64 len) { return atomicAdd(count, (unsigned long long)len); }
-};
-
-template<typename T>
-__device__ __forceinline__ void load_box(const T* p, T b[6])
-{
-#pragma unroll
-  for (int c = 0; c < 6; ++c)
-    b[c] = p[c];
-}
 
 // ---------------------------------------------------------------- RangeSearch (plain)
 template<typename T>
@@ -293,26 +250,6 @@ __global__ void __launch_bounds__(128) frustum_plain_kernel(TreeView<T> tv, cons
 }
 
 // ---------------------------------------------------------------- kNN (plain)
-// ot_query.h:1033-1036 GetValueWithToleranceUpper
-template<typename T>
-__device__ __forceinline__ T upper_tol(T v, T tol)
-{
-  return fmax(tol, v * (T(1.0) + tol));
-}
-
-template<typename T>
-__device__ __forceinline__ T entity_distance(const TreeView<T>& tv, u32 e, const T* p, T tol)
-{
-  if (tv.isBox)
-  {
-    T mn, mm;
-    GeoD<T>::min_max_distance(p, tv.geom + u64(e) * 6, tol, mn, mm);
-    return mn;
-  }
-  return GeoD<T>::distance(p, tv.geom + u64(e) * 3);
-}
-
-constexpr int kKnnMaxK = 256;
 
 // Pass 1: the k-th smallest distance d_k (points) -> F = U(d_k), the reference's final
 // farthestEntityDistance. Box trees keep the reference's optimistic/pessimistic pair:
@@ -326,6 +263,11 @@ __global__ void __launch_bounds__(128) knn_threshold_kernel(TreeView<T> tv, cons
   if (q >= nq)
     return;
   u32 k = kArr ? kArr[q] : kAll;
+  if (k == 0) // ot_query.h:1217-1219: no neighbour requested -> empty result (no distance is below 0)
+  {
+    Fout[q] = T(0);
+    return;
+  }
   if (k > kKnnMaxK)
   {
     atomicOr(err, kErrCapacity);
@@ -931,75 +873,6 @@ __global__ void item_ids_kernel(const u64* __restrict__ items, u64 m, u32* __res
     dst[i] = u32(items[i]);
 }
 
-static int blocks_for(u64 n, int per = 256)
-{
-  return int(std::max<u64>(1, std::min<u64>((n + per - 1) / per, 152 * 16)));
-}
-
-static u32 bit_count(u64 v)
-{
-  u32 b = 0;
-  while (v)
-  {
-    ++b;
-    v >>= 1;
-  }
-  return b;
-}
-
-// Stable radix sort of (u64 key, u32 value) with temporary buffers; result in (keys, vals).
-static int sort_pairs_u64(u64* keys, u32* vals, u64 m, u32 bits, cudaStream_t st, u32* err)
-{
-  if (m <= 1 || bits == 0)
-    return OTG_OK;
-  const u32 passes = (bits + kRadixBits - 1) / kRadixBits;
-  DevBuf k1, v1, scratch;
-  cudaError_t e;
-  if ((e = k1.ensure(sizeof(u64) * m)) || (e = v1.ensure(sizeof(u32) * m)) || (e = scratch.ensure(SortScratch::bytes(m, passes))))
-    return cuda_status(e, "allocating sort buffers");
-  cudaMemsetAsync(scratch.p, 0, SortScratch::bytes(m, passes), st);
-  SortScratch ss;
-  ss.carve(scratch.p, m, passes);
-  radix_histogram_kernel<u64><<<blocks_for(m), 256, 0, st>>>(keys, m, 0, passes, ss.hist);
-  bool inB = onesweep_passes<u64>(keys, vals, k1.as<u64>(), v1.as<u32>(), m, 0, passes, false, ss, err, st);
-  if (inB)
-  {
-    cudaMemcpyAsync(keys, k1.p, sizeof(u64) * m, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(vals, v1.p, sizeof(u32) * m, cudaMemcpyDeviceToDevice, st);
-  }
-  cudaStreamSynchronize(st);
-  k1.release();
-  v1.release();
-  scratch.release();
-  return cuda_status(cudaGetLastError(), "sorting results");
-}
-
-static int sort_pairs_u32(u32* keys, u32* vals, u64 m, u32 bits, cudaStream_t st, u32* err)
-{
-  if (m <= 1 || bits == 0)
-    return OTG_OK;
-  const u32 passes = (bits + kRadixBits - 1) / kRadixBits;
-  DevBuf k1, v1, scratch;
-  cudaError_t e;
-  if ((e = k1.ensure(sizeof(u32) * m)) || (e = v1.ensure(sizeof(u32) * m)) || (e = scratch.ensure(SortScratch::bytes(m, passes))))
-    return cuda_status(e, "allocating sort buffers");
-  cudaMemsetAsync(scratch.p, 0, SortScratch::bytes(m, passes), st);
-  SortScratch ss;
-  ss.carve(scratch.p, m, passes);
-  radix_histogram_kernel<u32><<<blocks_for(m), 256, 0, st>>>(keys, m, 0, passes, ss.hist);
-  bool inB = onesweep_passes<u32>(keys, vals, k1.as<u32>(), v1.as<u32>(), m, 0, passes, false, ss, err, st);
-  if (inB)
-  {
-    cudaMemcpyAsync(keys, k1.p, sizeof(u32) * m, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(vals, v1.p, sizeof(u32) * m, cudaMemcpyDeviceToDevice, st);
-  }
-  cudaStreamSynchronize(st);
-  k1.release();
-  v1.release();
-  scratch.release();
-  return cuda_status(cudaGetLastError(), "sorting results");
-}
-
 struct Collected
 {
   DevBuf items, dist, count, err;
@@ -1164,25 +1037,6 @@ __global__ void swap_pair_halves_kernel(u32* ids, u64 m)
 }
 
 // ---------------------------------------------------------------- host entry points
-template<typename T>
-static TreeView<T> view(const TreeState& t)
-{
-  return TreeView<T>{ t.nodeLink.as<uint4>(), t.nodeBox.as<T>(), t.nodeMax.as<T>(), t.sortedIds.as<u32>(), t.sortedGeom.as<T>(), u32(t.n),
-                      t.kind == OTG_KIND_BOXES ? 1 : 0, u32(t.nodeCount) };
-}
-
-template<typename T>
-static T upper_tol_host(T v, T tol)
-{
-  return std::fmax(tol, v * (T(1.0) + tol));
-}
-
-template<typename T>
-static T tol_of(double tol)
-{
-  return tol < 0 ? base_tol<T>() : T(tol);
-}
-
 // stage a caller array in device memory
 static int stage_input(DevBuf& buf, const void* src, size_t bytes, int mem, cudaStream_t st, const void*& dptr)
 {
@@ -1296,6 +1150,8 @@ static int knn_impl(const TreeState& t, const void* pts, u64 nq, const u32* k, u
       return rc;
   if (t.n == 0 || nq == 0)
     return empty_result(nq, r, true, st);
+  if (algo != OTG_ALGO_PLAIN_FP64 && t.kind == OTG_KIND_POINTS)
+    return knn_filtered(const_cast<TreeState&>(t), d, (const u32*)dk, nq, kAll, maxDist, tol, r, st);
   if (cudaError_t e = F.ensure(sizeof(T) * nq))
     return cuda_status(e, "allocating kNN thresholds");
   auto tv = view<T>(t);
