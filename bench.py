@@ -421,11 +421,20 @@ def run_queries(tree16, pts16_d, stream):
     boxes = torch.as_tensor(cluster_boxes(4_000_000, 201), device="cuda")
     tb = otg.Tree("boxes").create(boxes, max_depth=12, max_elements=32)
     tb.sync()
-    s = time_query(lambda: tb.collision_self(algo=otg.ALGO_PLAIN_FP64, raw=True), reps=1)
-    pairs = tb.collision_self(algo=otg.ALGO_PLAIN_FP64, raw=True).sizes()[1] // 2
-    out["collide_self_4M_plain_fp64_ms"] = s * 1e3
+    pair_lists = {}
+    for algo, name in algos:
+        s = time_query(lambda: tb.collision_self(algo=algo, raw=True), reps=1 if algo == otg.ALGO_PLAIN_FP64 else 3)
+        r = tb.collision_self(algo=algo, raw=True)
+        pairs = r.sizes()[1] // 2
+        pair_lists[name] = r.to_host()[1]
+        out[f"collide_self_4M_{name}_ms"] = s * 1e3
+        out[f"collide_self_4M_{name}_Mpairs_per_s"] = pairs / s / 1e6
+        if algo == otg.ALGO_FILTERED:
+            tests, rechecks = r.stats()
+            out["collide_self_4M_recheck_fraction"] = rechecks / max(tests, 1)
     out["collide_self_4M_pairs"] = int(pairs)
-    out["collide_self_4M_plain_fp64_Mpairs_per_s"] = pairs / s / 1e6
+    out["collide_self_4M_pair_lists_equal"] = bool(np.array_equal(pair_lists["plain_fp64"], pair_lists["filtered_fp32"]))
+    out["collide_self_4M_speedup_filtered_vs_plain"] = out["collide_self_4M_plain_fp64_ms"] / out["collide_self_4M_filtered_fp32_ms"]
     return out
 
 

@@ -695,7 +695,7 @@ static void host_bounds(double v, float& lo, float& hi)
 }
 
 template<typename T>
-static int ensure_image32(TreeState& t, cudaStream_t st)
+static int ensure_image32_impl(TreeState& t, cudaStream_t st)
 {
   if (t.image32)
     return OTG_OK;
@@ -736,7 +736,7 @@ template<typename T>
 static int knn_filtered_impl(TreeState& t, const T* pts, const u32* dk, u64 nq, u32 kAll, double maxDist, double tol, ResultState& r, cudaStream_t st)
 {
   cudaError_t e;
-  if (int rc = ensure_image32<T>(t, st))
+  if (int rc = ensure_image32(t, st))
     return rc;
   const T tl = tol_of<T>(tol);
   const T F0 = maxDist < 0 ? Lim<T>::max() : upper_tol_host(T(maxDist), tl);
@@ -875,6 +875,11 @@ static int knn_filtered_impl(TreeState& t, const T* pts, const u32* dk, u64 nq, 
   r.filterTests = h.tests;
   r.rechecks = h.rechecks;
   return OTG_OK;
+}
+
+int ensure_image32(TreeState& t, cudaStream_t st)
+{
+  return t.scalar == OTG_SCALAR_F64 ? ensure_image32_impl<double>(t, st) : ensure_image32_impl<float>(t, st);
 }
 
 int knn_filtered(TreeState& t, const void* dpts, const u32* dk, u64 nq, u32 kAll, double maxDist, double tol, ResultState& r, cudaStream_t st)

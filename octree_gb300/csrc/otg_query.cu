@@ -1234,13 +1234,24 @@ static int collide_impl(const TreeState& a, const TreeState& b, bool self, doubl
   Collected c;
   auto ta = view<T>(a), tb = view<T>(b);
   T tl = tol_of<T>(tol);
+  const bool filtered = algo != OTG_ALGO_PLAIN_FP64;
+  CollideSearch search;
+  int searchRc = OTG_OK;
   int rc = collect(
     c, false, a.n * 4,
     [&](Appender ap, u32* err) {
-      collide_plain_kernel<T><<<u32((a.n + 127) / 128), 128, 0, st>>>(ta, tb, tl, self ? 1 : 0, ap, err);
+      if (filtered)
+        searchRc = collide_search_filtered(const_cast<TreeState&>(a), const_cast<TreeState&>(b), self, tol, ap, err, search, st);
+      else
+        collide_plain_kernel<T><<<u32((a.n + 127) / 128), 128, 0, st>>>(ta, tb, tl, self ? 1 : 0, ap, err);
     },
     st);
+  if (searchRc)
+    return searchRc;
   if (rc)
+    return rc;
+  u64 tests = 0, rechecks = 0;
+  if (filtered && (rc = collide_search_stats(search, tests, rechecks, st)))
     return rc;
   const u64 m = c.m;
   DevBuf keys, rej;
@@ -1269,6 +1280,8 @@ static int collide_impl(const TreeState& a, const TreeState& b, bool self, doubl
     swap_pair_halves_kernel<<<blocks_for(kept), 256, 0, st>>>(r.ids.as<u32>(), kept);
   if (!e)
     e = cudaStreamSynchronize(st);
+  r.filterTests = tests;
+  r.rechecks = rechecks;
   return cuda_status(e, "finishing pairs");
 }
 

@@ -161,4 +161,19 @@ static inline T tol_of(double tol)
   return tol < 0 ? base_tol<T>() : T(tol);
 }
 
+// FP32 images of a built tree for the query filters (otg_knn.cu): built on first use after a build
+int ensure_image32(TreeState& t, cudaStream_t st);
+
+// filtered candidate search of CollisionDetection (otg_collide.cu)
+struct CollideSearch
+{
+  DevBuf imgA, imgB, ctr; // tolerance-specific FP32 box images, counters
+  DevBuf order;           // processing order of the first tree's entities
+  float tolHi = 0.f;
+  bool ready = false;
+  bool orderReady = false;
+};
+int collide_search_filtered(TreeState& A, TreeState& B, bool self, double tol, Appender out, u32* err, CollideSearch& s, cudaStream_t st);
+int collide_search_stats(const CollideSearch& s, u64& tests, u64& rechecks, cudaStream_t st);
+
 } // namespace otg
