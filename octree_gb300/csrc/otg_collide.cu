@@ -52,6 +52,17 @@ __global__ void box_image_kernel(const T* __restrict__ geom, u64 n, float tolHi,
   }
 }
 
+// node MBRs for one call: {min rounded down, 0}, {max rounded up + tol rounded up, 0}
+__global__ void node_tol_image_kernel(const float4* __restrict__ nodes32, u64 m, float tolHi, float4* __restrict__ out)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+  {
+    const float4 mx = nodes32[2 * i + 1];
+    out[2 * i] = nodes32[2 * i];
+    out[2 * i + 1] = make_float4(__fadd_ru(mx.x, tolHi), __fadd_ru(mx.y, tolHi), __fadd_ru(mx.z, tolHi), 0.f);
+  }
+}
+
 struct BoxImg
 {
   float mnD[3], mxD[3], mnU[3], mxU[3];
@@ -99,7 +110,7 @@ struct CollideArgs
   const float4* imgB;
   const T* geomB;
   const uint4* linkB;
-  const float4* nodeB; // outward-rounded node MBRs of tree B (2 float4 per node)
+  const float4* nodeB; // node MBRs of tree B: min rounded down, max + tol rounded up (2 float4 per node)
   u32 nB, nNodesB;
   float tolHi;
   T tol;
@@ -203,7 +214,7 @@ __global__ void __launch_bounds__(kCollideWarps * 32) collide_box_kernel(Collide
           keep = true;
 #pragma unroll
           for (int c = 0; c < 3; ++c)
-            keep &= !((__fadd_ru(nmx[c], a.tolHi) < me.mnD[c]) | (me.mxU[c] < nmn[c]));
+            keep &= !((nmx[c] < me.mnD[c]) | (me.mxU[c] < nmn[c]));
           if (keep && a.selfMode)
             keep = a.linkB[ch].w > i + 1; // the subtree holds a position after this entity
         }
@@ -271,8 +282,9 @@ static int collide_search_impl(TreeState& A, TreeState& B, bool self, double tol
     const T tl = tol < 0 ? base_tol<T>() : T(tol);
     host_ru(double(tl), s.tolHi);
     if ((e = s.imgA.ensure(sizeof(float4) * 3 * std::max<u64>(A.n, 1))) || (!self && (e = s.imgB.ensure(sizeof(float4) * 3 * std::max<u64>(B.n, 1)))) ||
-        (e = s.ctr.ensure(sizeof(CollideCounters))))
+        (e = s.ctr.ensure(sizeof(CollideCounters))) || (e = s.nodesB.ensure(sizeof(float4) * 2 * std::max<u64>(B.nodeCount, 1))))
       return cuda_status(e, "allocating the collision images");
+    node_tol_image_kernel<<<blocks_for(B.nodeCount), 256, 0, st>>>(B.nodeBox32.as<float4>(), B.nodeCount, s.tolHi, s.nodesB.as<float4>());
     box_image_kernel<T><<<blocks_for(A.n), 256, 0, st>>>(A.sortedGeom.as<T>(), A.n, s.tolHi, s.imgA.as<float4>());
     if (!self)
       box_image_kernel<T><<<blocks_for(B.n), 256, 0, st>>>(B.sortedGeom.as<T>(), B.n, s.tolHi, s.imgB.as<float4>());
@@ -297,7 +309,7 @@ static int collide_search_impl(TreeState& A, TreeState& B, bool self, double tol
   a.imgB = self ? s.imgA.as<float4>() : s.imgB.as<float4>();
   a.geomB = B.sortedGeom.as<T>();
   a.linkB = B.nodeLink.as<uint4>();
-  a.nodeB = B.nodeBox32.as<float4>();
+  a.nodeB = s.nodesB.as<float4>();
   a.nB = u32(B.n);
   a.nNodesB = u32(B.nodeCount);
   a.tolHi = s.tolHi;

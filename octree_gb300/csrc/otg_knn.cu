@@ -80,6 +80,9 @@ struct KnnArgs
 };
 
 // ---------------------------------------------------------------- FP32 images
+// point: {x, y, z, e} with x = RN(x64) and e >= max |x64 - x| inflated by 2^-20 relative (the
+// per-entity bound arithmetic below relies on that margin); e = +inf and x = 0 for coordinates
+// outside the FP32 range (such entities always pass the filter).
 template<typename T>
 __global__ void point_image_kernel(const T* __restrict__ geom, u64 n, float4* __restrict__ out)
 {
@@ -97,7 +100,7 @@ __global__ void point_image_kernel(const T* __restrict__ geom, u64 n, float4* __
       v[c] = f;
       e = fmax(e, fabs(x - double(f)));
     }
-    out[i] = ok ? make_float4(v[0], v[1], v[2], __double2float_ru(e)) : make_float4(0.f, 0.f, 0.f, kInf);
+    out[i] = ok ? make_float4(v[0], v[1], v[2], __fmul_ru(__double2float_ru(e), 1.f + 0x1p-20f)) : make_float4(0.f, 0.f, 0.f, kInf);
   }
 }
 
@@ -122,32 +125,14 @@ __global__ void node_image_kernel(const T* __restrict__ nodeBox, const T* __rest
 }
 
 // ---------------------------------------------------------------- device helpers
-template<typename T>
-__device__ __forceinline__ float rd32(T v);
-template<>
-__device__ __forceinline__ float rd32<double>(double v)
-{
-  return __double2float_rd(v);
-}
-template<>
-__device__ __forceinline__ float rd32<float>(float v)
-{
-  return v;
-}
-template<typename T>
-__device__ __forceinline__ float ru32(T v);
-template<>
-__device__ __forceinline__ float ru32<double>(double v)
-{
-  return __double2float_ru(v);
-}
-template<>
-__device__ __forceinline__ float ru32<float>(float v)
-{
-  return v;
-}
+// The per-node and per-entity bounds use round-to-nearest FP32 only (directed-rounding FP32
+// instructions are much slower on this GPU); every rounding is covered by an explicit margin.
+// With u = 2^-24, a round-to-nearest result r of a normal operation is within u|r| of the exact
+// value, and sums and products of non-negative values gain at most a factor (1 + u) each.
 
-// lower bound of the squared distance from the query interval to an outward-rounded node box
+// lower bound of the squared distance from the query interval [plo, phi] to an outward-rounded
+// node box: each positive gap is shrunk by 2^-22 relative (covers its own rounding), the sum of
+// squares by 2^-20 (covers four roundings), then by the caller's margin.
 __device__ __forceinline__ float node_w2(const float4* __restrict__ nb, u32 node, const float* plo, const float* phi, float widenLo)
 {
   const float4 mn = nb[2 * size_t(node)], mx = nb[2 * size_t(node) + 1];
@@ -156,29 +141,35 @@ __device__ __forceinline__ float node_w2(const float4* __restrict__ nb, u32 node
 #pragma unroll
   for (int c = 0; c < 3; ++c)
   {
-    const float g = fmaxf(fmaxf(__fsub_rd(a[c], phi[c]), __fsub_rd(plo[c], b[c])), 0.f);
-    w2 = __fmaf_rd(g, g, w2);
+    const float g = fmaxf(fmaxf(a[c] - phi[c], plo[c] - b[c]), 0.f) * (1.f - 0x1p-22f);
+    w2 = fmaf(g, g, w2);
   }
-  return __fmul_rd(w2, widenLo);
+  return w2 * ((1.f - 0x1p-20f) * widenLo);
 }
 
-// bounds of the squared exact distance between the query and an entity image
-__device__ __forceinline__ void entity_bounds(float4 g, const float* plo, const float* phi, float widenLo, float widenHi, float& l2, float& h2)
+// Bounds lo2 <= d^2 <= hi2 of the squared distance between the query (p32 = RN(p), per-coordinate
+// error at most Sq, inflated by 2^-20) and an entity image {x32, e} (e inflated by 2^-20):
+//   t = RN(x32 - p32) is within u|t| + e + Sq of the exact difference;
+//   E = RN(|t| 2^-20 + RN(e + Sq)) >= 15u|t| + (e + Sq)_exact (1 + 12u) covers that error and the
+//   rounding of |t| + E and |t| - E; the sums of squares are then widened by the caller's
+//   margins, which also cover the rounding of the exact distance formula.
+__device__ __forceinline__ void entity_bounds(float4 g, const float* p32, float Sq, float widenLo, float widenHi, float& l2, float& h2)
 {
   const float x[3] = { g.x, g.y, g.z };
+  const float S = g.w + Sq;
   float L = 0.f, H = 0.f;
 #pragma unroll
   for (int c = 0; c < 3; ++c)
   {
-    const float lo = __fsub_rd(__fsub_rd(x[c], phi[c]), g.w);
-    const float hi = __fadd_ru(__fsub_ru(x[c], plo[c]), g.w);
-    const float al = lo > 0.f ? lo : (hi < 0.f ? -hi : 0.f);
-    const float ah = fmaxf(-lo, hi);
-    L = __fmaf_rd(al, al, L);
-    H = __fmaf_ru(ah, ah, H);
+    const float a = fabsf(x[c] - p32[c]);
+    const float E = fmaf(a, 0x1p-20f, S);
+    const float hi = a + E;
+    const float lo = fmaxf(a - E, 0.f);
+    L = fmaf(lo, lo, L);
+    H = fmaf(hi, hi, H);
   }
-  l2 = __fmul_rd(L, widenLo);
-  h2 = __fmul_ru(H, widenHi);
+  l2 = fmaxf(fmaf(L, widenLo, -0x1p-140f), 0.f);
+  h2 = fmaf(H, widenHi, 0x1p-140f);
 }
 
 __device__ __forceinline__ u32 pow2_at_least32(u32 v)
@@ -245,10 +236,11 @@ __device__ __forceinline__ void knn_flush(KnnWarpMem<CAP>& W, const KnnArgs<T>& 
     W.tmp[i] = (i < bufN && W.hi2[i] < a.F0lo2) ? W.hi2[i] : kInf;
   __syncwarp();
   warp_sort_f32(W.tmp, n2, lane);
+  // round-to-nearest with a 2^-20 margin per step keeps every value an upper bound
   const float R2 = k <= n2 ? W.tmp[k - 1] : kInf;
-  const float Rhi = R2 < kInf ? __fsqrt_ru(R2) : kInf;
-  const float Fc = fmaxf(a.tolHi, __fmul_ru(fminf(Rhi, a.F0hi), a.onePlusTolHi));
-  const float nFc2 = __fmul_ru(Fc, Fc);
+  const float Rhi = sqrtf(R2) * (1.f + 0x1p-20f);
+  const float Fc = fmaxf(a.tolHi, fminf(Rhi, a.F0hi) * a.onePlusTolHi);
+  const float nFc2 = (Fc * Fc) * (1.f + 0x1p-20f);
   Fc2 = fminf(Fc2, nFc2);
   const u32 lt = (1u << lane) - 1;
   u32 kept = 0;
@@ -313,20 +305,36 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_filtered_kernel(KnnArgs<T>
       }
       continue;
     }
+    // query: p32 = RN(p) with |p - p32| <= 2^-24 |p32| + 2^-150 <= Sq / 2 (doubled margin);
+    // [plo, phi] = p32 -/+ 2 Sq encloses p after its own rounding
     T p[3];
-    float plo[3], phi[3];
+    float plo[3], phi[3], p32[3];
+    float ap = 0.f;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
     {
       p[c] = a.pts[u64(q) * 3 + c];
-      plo[c] = rd32<T>(p[c]);
-      phi[c] = ru32<T>(p[c]);
+      p32[c] = float(p[c]);
+      ap = fmaxf(ap, fabsf(p32[c]));
+    }
+    float Sq = sizeof(T) == 4 ? 0.f : fmaf(ap, 0x1p-23f, 0x1p-140f);
+    if (!(ap < kInf))
+    {
+      // a query outside the FP32 range: every entity is a candidate
+      p32[0] = p32[1] = p32[2] = 0.f;
+      Sq = kInf;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+    {
+      plo[c] = p32[c] - 2.f * Sq;
+      phi[c] = p32[c] + 2.f * Sq;
     }
     u32 bufN = 0;
     float Fc2;
     {
-      const float Fc = fmaxf(a.tolHi, __fmul_ru(a.F0hi, a.onePlusTolHi));
-      Fc2 = __fmul_ru(Fc, Fc);
+      const float Fc = fmaxf(a.tolHi, a.F0hi * a.onePlusTolHi);
+      Fc2 = (Fc * Fc) * (1.f + 0x1p-20f);
     }
     u32 flushAt = min(u32(CAP), max(64u, 2 * k + 32));
     bool overflow = false;
@@ -377,7 +385,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_filtered_kernel(KnnArgs<T>
         bool keep = false;
         if (e < L.z)
         {
-          entity_bounds(a.geom32[e], plo, phi, a.widenLo, a.widenHi, l2, h2);
+          entity_bounds(a.geom32[e], p32, Sq, a.widenLo, a.widenHi, l2, h2);
           keep = l2 <= Fc2;
         }
         const u32 bal = __ballot_sync(~0u, keep);
@@ -454,20 +462,21 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_filtered_kernel(KnnArgs<T>
     __syncwarp();
     warp_sort_pairs(W.key, W.pos, n2, lane);
     rechecks += bufN;
+    // distances are non-negative: comparing bit patterns as integers orders them like values
+    const unsigned long long F0bits = (unsigned long long)__double_as_longlong(double(a.F0));
     u32 below0 = 0;
     for (u32 base = 0; base < bufN; base += 32)
     {
       const u32 i = base + lane;
-      const bool b = i < bufN && T(__longlong_as_double((long long)W.key[i])) < a.F0;
-      below0 += __popc(__ballot_sync(~0u, b));
+      below0 += __popc(__ballot_sync(~0u, i < bufN && W.key[i] < F0bits));
     }
     const T F = below0 >= k ? upper_tol(T(__longlong_as_double((long long)W.key[k - 1])), a.tol) : a.F0;
+    const unsigned long long Fbits = (unsigned long long)__double_as_longlong(double(F));
     u32 m = 0;
     for (u32 base = 0; base < bufN; base += 32)
     {
       const u32 i = base + lane;
-      const bool b = i < bufN && T(__longlong_as_double((long long)W.key[i])) < F;
-      m += __popc(__ballot_sync(~0u, b));
+      m += __popc(__ballot_sync(~0u, i < bufN && W.key[i] < Fbits));
     }
     unsigned long long s0 = 0;
     if (lane == 0)
@@ -799,10 +808,11 @@ static int knn_filtered_impl(TreeState& t, const T* pts, const u32* dk, u64 nq, 
   host_bounds(double(tl), lo, hi);
   a.tolHi = hi;
   host_bounds(double(T(T(1) + tl)), lo, hi);
+  host_bounds(double(hi) * (1.0 + 0x1p-20), lo, hi); // margin for the rounding of one product
   a.onePlusTolHi = hi;
   // relative margins that cover the rounding of the exact distance formula
-  a.widenLo = sizeof(T) == 8 ? 1.f - 0x1p-20f : 1.f - 0x1p-17f;
-  a.widenHi = sizeof(T) == 8 ? 1.f + 0x1p-20f : 1.f + 0x1p-17f;
+  a.widenLo = sizeof(T) == 8 ? 1.f - 0x1p-18f : 1.f - 0x1p-16f;
+  a.widenHi = sizeof(T) == 8 ? 1.f + 0x1p-18f : 1.f + 0x1p-16f;
   a.kLimit = big ? 240u : 112u;
   a.ctr = ctr.as<KnnCounters>();
   a.fallback = fb.as<u32>();

@@ -169,6 +169,7 @@ struct CollideSearch
 {
   DevBuf imgA, imgB, ctr; // tolerance-specific FP32 box images, counters
   DevBuf order;           // processing order of the first tree's entities
+  DevBuf nodesB;          // the second tree's node MBRs with the tolerance added
   float tolHi = 0.f;
   bool ready = false;
   bool orderReady = false;
