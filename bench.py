@@ -438,6 +438,41 @@ def run_queries(tree16, pts16_d, stream):
     return out
 
 
+PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m")
+
+
+def run_profile_case(name):
+    """Small cases for ncu captures (a few hundred MB on the device): each runs its kernels twice."""
+    import torch
+
+    import octree_gb300 as otg
+
+    if name == "knn_4m_200k":
+        pts = torch.as_tensor(shell_points(4_000_000, 301), device="cuda")
+        t = otg.Tree("points").create(pts, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
+        t.sync()
+        q = torch.as_tensor(shell_points(200_000, 302), device="cuda")
+        k = torch.as_tensor(np.random.default_rng(303).integers(1, 65, 200_000).astype(np.int32), device="cuda")
+        for _ in range(2):
+            r = t.knn(q, k, algo=otg.ALGO_FILTERED, raw=True)
+        print(json.dumps({"case": name, "results": r.sizes()[1], "stats": r.stats()}))
+    elif name == "collide_1m":
+        boxes = torch.as_tensor(cluster_boxes(1_000_000, 201), device="cuda")
+        t = otg.Tree("boxes").create(boxes, max_depth=12, max_elements=32)
+        t.sync()
+        for _ in range(2):
+            r = t.collision_self(algo=otg.ALGO_FILTERED, raw=True)
+        print(json.dumps({"case": name, "pairs": r.sizes()[1] // 2, "stats": r.stats()}))
+    elif name == "build_4m":
+        pts = torch.as_tensor(shell_points(4_000_000, 301), device="cuda")
+        t = otg.Tree("points")
+        for _ in range(2):
+            t.create(pts, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
+        t.sync()
+        print(json.dumps({"case": name, "nodes": int(t.node_count)}))
+    torch.cuda.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -446,7 +481,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-queries", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", choices=PROFILE_CASES, help="run one small case for an ncu capture and exit")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args.profile_case)
+        return
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":
         run_reference(args)

@@ -1,0 +1,398 @@
+// orthotree_gpu.hpp — C++20 drop-in types for OrthoTree's Managed octrees, backed by the GB300
+// library through its C-ABI (octree_gb300.h).
+//
+//   OrthoTreeGPU::OctreePointM   ~ OrthoTree::OctreePointM (core/ot_aliases.h:364)
+//   OrthoTreeGPU::OctreeBoxM     ~ OrthoTree::OctreeBoxM   (core/ot_aliases.h:369)
+//   (and the FP32 variants OctreePointMF / OctreeBoxMF)
+//
+// Construction and Create take the reference's arguments (core/ot_managed.h:169-228, 318-360):
+// entities, optional max depth, optional space box, max elements per node (default 16,
+// core/configuration.h:83). Queries have the reference's names, argument order and defaults
+// (core/ot_managed.h:584-893) and return the same id lists:
+//   PickSearch, RangeSearch, FrustumCulling, GetNearestNeighbors, RayIntersectedAll,
+//   RayIntersectedFirst, CollisionDetection (one tree and two trees).
+// Each query also has a batched form (…Batch) answering many query geometries in one GPU launch;
+// it returns a Csr (offsets + ids [+ distances]).
+//
+// Orders where the reference leaves ties unspecified are made canonical:
+//   * GetNearestNeighbors and RayIntersectedAll: by (distance, id);
+//   * RayIntersectedFirst: farthest first as the reference's max-heap pops them, ties by
+//     descending id;
+//   * CollisionDetection: pairs (i, j) ascending, i < j within one tree.
+//
+// Differences from the reference:
+//   * Errors throw OrthoTreeGPU::Error, where the reference terminates (ORTHOTREE_CRASH_IF,
+//     core/ot_base.h:104-108).
+//   * The tester / callback overloads (TTester, FCollisionDetector, entityDistanceFn) cannot run on
+//     the GPU and are not offered.
+//   * Execution tags are accepted and ignored: the work runs on the GPU.
+//   * There is no CPU fallback: without a CUDA device every call throws with status
+//     OTG_ERR_NO_DEVICE.
+#pragma once
+
+#include "octree_gb300.h"
+
+#include <array>
+#include <cstddef>
+#include <cstdint>
+#include <limits>
+#include <optional>
+#include <span>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace OrthoTreeGPU
+{
+using index_t = std::uint32_t;
+using EntityID = index_t;
+using depth_t = std::uint32_t;
+
+template<typename TScalar>
+using Vector3 = std::array<TScalar, 3>;
+
+// layouts of OrthoTree::BoundingBoxND / RayND / PlaneND (adapters/general.h:349-368)
+template<typename TScalar>
+struct BoundingBox3
+{
+  Vector3<TScalar> Min;
+  Vector3<TScalar> Max;
+};
+template<typename TScalar>
+struct Ray3
+{
+  Vector3<TScalar> Origin;
+  Vector3<TScalar> Direction;
+};
+template<typename TScalar>
+struct Plane3
+{
+  TScalar OrigoDistance;
+  Vector3<TScalar> Normal;
+};
+
+using Point3D = Vector3<double>;
+using BoundingBox3D = BoundingBox3<double>;
+using Ray3D = Ray3<double>;
+using Plane3D = Plane3<double>;
+
+// core/types.h:83-87
+enum class RangeSearchMode
+{
+  Inside = OTG_RANGE_INSIDE,
+  Overlap = OTG_RANGE_OVERLAP
+};
+
+// query kernels: the default is the batched FP32-filtered kernel where one exists
+enum class Algorithm
+{
+  Default = OTG_ALGO_DEFAULT,
+  PlainFP64 = OTG_ALGO_PLAIN_FP64,
+  Filtered = OTG_ALGO_FILTERED
+};
+
+class Error : public std::runtime_error
+{
+public:
+  Error(int status, const std::string& what)
+  : std::runtime_error(what)
+  , m_status(status)
+  {}
+  int status() const noexcept { return m_status; }
+
+private:
+  int m_status;
+};
+
+// CSR result of a batched query: ids of query q are ids[offsets[q] .. offsets[q+1])
+struct Csr
+{
+  std::vector<std::uint64_t> offsets;
+  std::vector<EntityID> ids;
+  std::vector<double> distances; // kNN and ray queries
+  std::uint64_t filterTests = 0;
+  std::uint64_t fp64Rechecks = 0;
+
+  std::span<const EntityID> operator[](std::size_t q) const { return { ids.data() + offsets[q], ids.data() + offsets[q + 1] }; }
+  std::size_t size() const { return offsets.empty() ? 0 : offsets.size() - 1; }
+};
+
+namespace detail
+{
+  inline void check(int rc)
+  {
+    if (rc != OTG_OK)
+      throw Error(rc, std::string("octree_gb300: ") + otg_last_error());
+  }
+
+  template<typename TScalar>
+  constexpr int scalar_code()
+  {
+    static_assert(std::is_same_v<TScalar, double> || std::is_same_v<TScalar, float>, "the GPU tree stores double or float");
+    return std::is_same_v<TScalar, double> ? OTG_SCALAR_F64 : OTG_SCALAR_F32;
+  }
+
+  // the reference's BASE_TOLERANCE default (adapters/general.h:57): a negative value selects it
+  template<typename TScalar>
+  constexpr double base_tolerance()
+  {
+    return double(std::numeric_limits<TScalar>::epsilon()) * 100.0;
+  }
+
+  // maxDistance = numeric_limits::max() (the reference's "unbounded") maps to the C-ABI's < 0
+  template<typename TScalar>
+  inline double max_distance_arg(TScalar d)
+  {
+    return d == std::numeric_limits<TScalar>::max() ? -1.0 : double(d);
+  }
+
+  inline Csr take(otg_result* r, void* stream)
+  {
+    struct Guard
+    {
+      otg_result* r;
+      ~Guard() { otg_result_free(r); }
+    } g{ r };
+    std::uint64_t nq = 0, n = 0;
+    int hasDist = 0;
+    check(otg_result_info(r, &nq, &n, &hasDist));
+    Csr out;
+    out.offsets.resize(nq + 1);
+    out.ids.resize(n);
+    if (hasDist)
+      out.distances.resize(n);
+    check(otg_result_copy(r, out.offsets.data(), out.ids.data(), hasDist ? out.distances.data() : nullptr, OTG_MEM_HOST, stream));
+    check(otg_result_stats(r, &out.filterTests, &out.fp64Rechecks));
+    return out;
+  }
+
+  inline std::vector<std::pair<EntityID, EntityID>> pairs_of(const Csr& c)
+  {
+    std::vector<std::pair<EntityID, EntityID>> p(c.ids.size() / 2);
+    for (std::size_t i = 0; i < p.size(); ++i)
+      p[i] = { c.ids[2 * i], c.ids[2 * i + 1] };
+    return p;
+  }
+} // namespace detail
+
+// Managed tree: owns a device copy of its entities (core/ot_managed.h:70-71).
+template<typename TEntity, typename TScalar, int KIND>
+class OrthoTreeManagedGPU
+{
+public:
+  using Entity = TEntity;
+  using TBox = BoundingBox3<TScalar>;
+  using TVector = Vector3<TScalar>;
+  using TRay = Ray3<TScalar>;
+  using TPlane = Plane3<TScalar>;
+  static constexpr std::size_t DEFAULT_TARGET_ELEMENT_NUM_IN_NODES = 16;
+
+  OrthoTreeManagedGPU() { detail::check(otg_tree_new(&m_tree, detail::scalar_code<TScalar>(), KIND)); }
+
+  // OrthoTreeManaged(geometryCollection, maxDepthID, boxSpace, maxElementNoInNode, execMode)
+  template<typename TExecMode = std::nullptr_t>
+  explicit OrthoTreeManagedGPU(std::span<const Entity> entities, std::optional<depth_t> maxDepthID = std::nullopt,
+                               std::optional<TBox> boxSpace = std::nullopt, std::size_t maxElementNoInNode = DEFAULT_TARGET_ELEMENT_NUM_IN_NODES,
+                               TExecMode = {})
+  : OrthoTreeManagedGPU()
+  {
+    Create(entities, maxDepthID, boxSpace, maxElementNoInNode);
+  }
+
+  OrthoTreeManagedGPU(const OrthoTreeManagedGPU&) = delete;
+  OrthoTreeManagedGPU& operator=(const OrthoTreeManagedGPU&) = delete;
+  OrthoTreeManagedGPU(OrthoTreeManagedGPU&& o) noexcept
+  : m_tree(std::exchange(o.m_tree, nullptr))
+  , m_stream(o.m_stream)
+  {}
+  OrthoTreeManagedGPU& operator=(OrthoTreeManagedGPU&& o) noexcept
+  {
+    if (this != &o)
+    {
+      otg_tree_free(m_tree);
+      m_tree = std::exchange(o.m_tree, nullptr);
+      m_stream = o.m_stream;
+    }
+    return *this;
+  }
+  ~OrthoTreeManagedGPU() { otg_tree_free(m_tree); }
+
+  // CUDA stream (cudaStream_t) the tree's work is ordered on; nullptr = legacy default stream
+  void SetStream(void* stream) noexcept { m_stream = stream; }
+  const otg_tree* Handle() const noexcept { return m_tree; }
+
+  // Create(entities, maxDepthID, boxSpace, maxElementNoInNode) — core/ot_dynamic_hash_core.h:751-822
+  void Create(std::span<const Entity> entities, std::optional<depth_t> maxDepthID = std::nullopt, std::optional<TBox> boxSpace = std::nullopt,
+              std::size_t maxElementNoInNode = DEFAULT_TARGET_ELEMENT_NUM_IN_NODES)
+  {
+    static_assert(sizeof(Entity) == sizeof(TScalar) * (KIND == OTG_KIND_POINTS ? 3 : 6), "entity layout");
+    detail::check(otg_tree_create(m_tree, entities.data(), entities.size(), maxDepthID.value_or(0), boxSpace ? &*boxSpace : nullptr,
+                                  maxElementNoInNode, OTG_MEM_HOST, m_stream));
+  }
+
+  otg_tree_info Info() const
+  {
+    otg_tree_info info{};
+    detail::check(otg_tree_info_get(m_tree, &info));
+    return info;
+  }
+  std::size_t GetNodeCount() const { return std::size_t(Info().node_count); }
+  depth_t GetMaxDepthID() const { return Info().max_depth; }
+
+  // ---------------------------------------------------------------- single queries (reference form)
+  std::vector<EntityID> PickSearch(const TVector& pickPoint, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return first(PickSearchBatch(std::span<const TVector>(&pickPoint, 1), tolerance));
+  }
+
+  std::vector<EntityID> RangeSearch(const TBox& range, RangeSearchMode mode = RangeSearchMode::Inside,
+                                    double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return first(RangeSearchBatch(std::span<const TBox>(&range, 1), mode, tolerance));
+  }
+
+  std::vector<EntityID> FrustumCulling(std::span<const TPlane> boundaryPlanes, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return first(FrustumCullingBatch(boundaryPlanes, boundaryPlanes.size(), tolerance));
+  }
+
+  std::vector<EntityID> GetNearestNeighbors(const TVector& searchPoint, std::size_t neighborCount, TScalar maxDistanceWithin,
+                                            double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return first(GetNearestNeighborsBatch(std::span<const TVector>(&searchPoint, 1), neighborCount, maxDistanceWithin, tolerance));
+  }
+  std::vector<EntityID> GetNearestNeighbors(const TVector& searchPoint, std::size_t neighborCount, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return GetNearestNeighbors(searchPoint, neighborCount, std::numeric_limits<TScalar>::max(), tolerance);
+  }
+
+  std::vector<EntityID> RayIntersectedAll(const TVector& rayBasePoint, const TVector& rayHeading, double tolerance = detail::base_tolerance<TScalar>(),
+                                          double toleranceIncrement = 0.0, TScalar maxExaminationDistance = std::numeric_limits<TScalar>::max()) const
+  {
+    const TRay ray{ rayBasePoint, rayHeading };
+    return first(RayIntersectedAllBatch(std::span<const TRay>(&ray, 1), tolerance, toleranceIncrement, maxExaminationDistance));
+  }
+  std::vector<EntityID> RayIntersectedAll(const TRay& ray, double tolerance = detail::base_tolerance<TScalar>(), double toleranceIncrement = 0.0,
+                                          TScalar maxExaminationDistance = std::numeric_limits<TScalar>::max()) const
+  {
+    return RayIntersectedAll(ray.Origin, ray.Direction, tolerance, toleranceIncrement, maxExaminationDistance);
+  }
+
+  std::vector<EntityID> RayIntersectedFirst(const TVector& rayBasePoint, const TVector& rayHeading, double tolerance = detail::base_tolerance<TScalar>(),
+                                            double toleranceIncrement = 0.0, TScalar maxDistance = std::numeric_limits<TScalar>::max()) const
+  {
+    const TRay ray{ rayBasePoint, rayHeading };
+    auto ids = first(RayIntersectedFirstBatch(std::span<const TRay>(&ray, 1), tolerance, toleranceIncrement, maxDistance));
+    return { ids.rbegin(), ids.rend() }; // the reference's max-heap pops the farthest first
+  }
+  std::vector<EntityID> RayIntersectedFirst(const TRay& ray, double tolerance = detail::base_tolerance<TScalar>(), double toleranceIncrement = 0.0,
+                                            TScalar maxDistance = std::numeric_limits<TScalar>::max()) const
+  {
+    return RayIntersectedFirst(ray.Origin, ray.Direction, tolerance, toleranceIncrement, maxDistance);
+  }
+
+  // ---------------------------------------------------------------- batched queries (one launch)
+  Csr PickSearchBatch(std::span<const TVector> points, double tolerance = detail::base_tolerance<TScalar>(), Algorithm algo = Algorithm::Default) const
+  {
+    otg_result* r = nullptr;
+    detail::check(otg_pick_search(m_tree, points.data(), points.size(), tolerance, int(algo), &r, OTG_MEM_HOST, m_stream));
+    return detail::take(r, m_stream);
+  }
+  Csr RangeSearchBatch(std::span<const TBox> ranges, RangeSearchMode mode = RangeSearchMode::Inside, double tolerance = detail::base_tolerance<TScalar>(),
+                       Algorithm algo = Algorithm::Default) const
+  {
+    otg_result* r = nullptr;
+    detail::check(otg_range_search(m_tree, ranges.data(), ranges.size(), int(mode), tolerance, int(algo), &r, OTG_MEM_HOST, m_stream));
+    return detail::take(r, m_stream);
+  }
+  // planes: n_queries consecutive groups of planesPerQuery planes
+  Csr FrustumCullingBatch(std::span<const TPlane> planes, std::size_t planesPerQuery, double tolerance = detail::base_tolerance<TScalar>(),
+                          Algorithm algo = Algorithm::Default) const
+  {
+    if (planesPerQuery == 0 || planes.size() % planesPerQuery)
+      throw Error(OTG_ERR_INVALID_ARGUMENT, "planes must hold whole groups of planesPerQuery");
+    otg_result* r = nullptr;
+    detail::check(otg_frustum_culling(m_tree, planes.data(), planesPerQuery, planes.size() / planesPerQuery, tolerance, int(algo), &r, OTG_MEM_HOST,
+                                      m_stream));
+    return detail::take(r, m_stream);
+  }
+  Csr GetNearestNeighborsBatch(std::span<const TVector> points, std::size_t neighborCount,
+                               TScalar maxDistanceWithin = std::numeric_limits<TScalar>::max(), double tolerance = detail::base_tolerance<TScalar>(),
+                               Algorithm algo = Algorithm::Default) const
+  {
+    otg_result* r = nullptr;
+    detail::check(otg_knn(m_tree, points.data(), points.size(), nullptr, std::uint32_t(neighborCount), detail::max_distance_arg(maxDistanceWithin),
+                          tolerance, int(algo), &r, OTG_MEM_HOST, m_stream));
+    return detail::take(r, m_stream);
+  }
+  // per-query neighbour counts
+  Csr GetNearestNeighborsBatch(std::span<const TVector> points, std::span<const std::uint32_t> neighborCounts,
+                               TScalar maxDistanceWithin = std::numeric_limits<TScalar>::max(), double tolerance = detail::base_tolerance<TScalar>(),
+                               Algorithm algo = Algorithm::Default) const
+  {
+    if (neighborCounts.size() != points.size())
+      throw Error(OTG_ERR_INVALID_ARGUMENT, "one neighbour count per query point");
+    otg_result* r = nullptr;
+    detail::check(otg_knn(m_tree, points.data(), points.size(), neighborCounts.data(), 0, detail::max_distance_arg(maxDistanceWithin), tolerance,
+                          int(algo), &r, OTG_MEM_HOST, m_stream));
+    return detail::take(r, m_stream);
+  }
+  Csr RayIntersectedAllBatch(std::span<const TRay> rays, double tolerance = detail::base_tolerance<TScalar>(), double toleranceIncrement = 0.0,
+                             TScalar maxExaminationDistance = std::numeric_limits<TScalar>::max(), Algorithm algo = Algorithm::Default) const
+  {
+    otg_result* r = nullptr;
+    detail::check(otg_ray_all(m_tree, rays.data(), rays.size(), tolerance, toleranceIncrement, detail::max_distance_arg(maxExaminationDistance),
+                              int(algo), &r, OTG_MEM_HOST, m_stream));
+    return detail::take(r, m_stream);
+  }
+  // ids per ray by (enter distance, id); RayIntersectedFirst() returns them farthest first
+  Csr RayIntersectedFirstBatch(std::span<const TRay> rays, double tolerance = detail::base_tolerance<TScalar>(), double toleranceIncrement = 0.0,
+                               TScalar maxDistance = std::numeric_limits<TScalar>::max(), Algorithm algo = Algorithm::Default) const
+  {
+    otg_result* r = nullptr;
+    detail::check(otg_ray_first(m_tree, rays.data(), rays.size(), tolerance, toleranceIncrement, detail::max_distance_arg(maxDistance), int(algo), &r,
+                                OTG_MEM_HOST, m_stream));
+    return detail::take(r, m_stream);
+  }
+
+  // ---------------------------------------------------------------- collision (box trees)
+  // CollisionDetection(tolerance, execMode) — core/ot_managed.h:700-709, core/ot_query.h:1902-1906
+  template<typename TExecMode = std::nullptr_t>
+  std::vector<std::pair<EntityID, EntityID>> CollisionDetection(double tolerance = detail::base_tolerance<TScalar>(), TExecMode = {},
+                                                                Algorithm algo = Algorithm::Default) const
+    requires(KIND == OTG_KIND_BOXES)
+  {
+    otg_result* r = nullptr;
+    detail::check(otg_collision_self(m_tree, tolerance, int(algo), &r, m_stream));
+    return detail::pairs_of(detail::take(r, m_stream));
+  }
+  // CollisionDetection(otherTree, tolerance) — core/ot_managed.h:712-718, core/ot_query.h:1462-1497
+  std::vector<std::pair<EntityID, EntityID>> CollisionDetection(const OrthoTreeManagedGPU& otherTree, double tolerance = detail::base_tolerance<TScalar>(),
+                                                                Algorithm algo = Algorithm::Default) const
+    requires(KIND == OTG_KIND_BOXES)
+  {
+    otg_result* r = nullptr;
+    detail::check(otg_collision_pair(m_tree, otherTree.m_tree, tolerance, int(algo), &r, m_stream));
+    return detail::pairs_of(detail::take(r, m_stream));
+  }
+  static std::vector<std::pair<EntityID, EntityID>> CollisionDetection(const OrthoTreeManagedGPU& leftTree, const OrthoTreeManagedGPU& rightTree,
+                                                                       double tolerance = detail::base_tolerance<TScalar>())
+    requires(KIND == OTG_KIND_BOXES)
+  {
+    return leftTree.CollisionDetection(rightTree, tolerance);
+  }
+
+private:
+  static std::vector<EntityID> first(const Csr& c) { return c.size() ? std::vector<EntityID>(c[0].begin(), c[0].end()) : std::vector<EntityID>{}; }
+
+  otg_tree* m_tree = nullptr;
+  void* m_stream = nullptr;
+};
+
+using OctreePointM = OrthoTreeManagedGPU<Vector3<double>, double, OTG_KIND_POINTS>;
+using OctreeBoxM = OrthoTreeManagedGPU<BoundingBox3<double>, double, OTG_KIND_BOXES>;
+using OctreePointMF = OrthoTreeManagedGPU<Vector3<float>, float, OTG_KIND_POINTS>;
+using OctreeBoxMF = OrthoTreeManagedGPU<BoundingBox3<float>, float, OTG_KIND_BOXES>;
+
+} // namespace OrthoTreeGPU

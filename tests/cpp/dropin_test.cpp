@@ -1,0 +1,183 @@
+// Drop-in test of include/orthotree_gpu.hpp: builds point and box trees through the C++ types and
+// compares every query with the CPU oracle (oracle/otg_oracle_capi.cpp, linked as test
+// infrastructure). Without a CUDA device it checks that the types fail loudly instead.
+//   exit 0 and "OK" on success; any mismatch prints the query and exits 1.
+#include "orthotree_gpu.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+#include <vector>
+
+extern "C"
+{
+  void* oro_create(int scalar, int kind, const void* ent, uint64_t n, uint32_t maxDepth, const void* box, uint64_t maxElem);
+  void oro_destroy(void* h);
+  void* oro_range(void* h, const void* ranges, uint64_t nq, int mode, double tol);
+  void* oro_pick(void* h, const void* pts, uint64_t nq, double tol);
+  void* oro_knn(void* h, const void* pts, uint64_t nq, const uint32_t* k, double maxDist, double tol);
+  void* oro_ray(void* h, const void* rays, uint64_t nq, double tol, double tolInc, double maxDist, int first);
+  void* oro_frustum(void* h, const void* planes, uint64_t np, uint64_t nq, double tol);
+  void* oro_collide_self(void* h, double tol);
+  void* oro_collide_pair(void* h1, void* h2, double tol);
+  uint64_t oro_res_nq(void* r);
+  uint64_t oro_res_total(void* r);
+  void oro_res_copy(void* r, uint64_t* offsets, uint32_t* ids, double* dist);
+  void oro_res_free(void* r);
+}
+
+using namespace OrthoTreeGPU;
+
+static int g_fail = 0;
+
+static std::vector<uint32_t> oracle_ids(void* r, uint64_t q)
+{
+  std::vector<uint64_t> off(oro_res_nq(r) + 1);
+  std::vector<uint32_t> ids(oro_res_total(r));
+  std::vector<double> dist(ids.size());
+  oro_res_copy(r, off.data(), ids.data(), dist.data());
+  return { ids.begin() + off[q], ids.begin() + off[q + 1] };
+}
+
+static void expect(const std::vector<uint32_t>& got, void* oracleResult, uint64_t q, const char* what)
+{
+  auto want = oracle_ids(oracleResult, q);
+  if (got != want)
+  {
+    std::printf("MISMATCH %s query %llu: %zu vs %zu ids\n", what, (unsigned long long)q, got.size(), want.size());
+    ++g_fail;
+  }
+}
+
+int main()
+{
+  if (otg_device_count() == 0)
+  {
+    try
+    {
+      std::vector<Point3D> pts(16, Point3D{ 0, 0, 0 });
+      OctreePointM t(pts, 4);
+      std::printf("no exception without a device\n");
+      return 1;
+    }
+    catch (const Error& e)
+    {
+      if (e.status() != OTG_ERR_NO_DEVICE)
+        return 1;
+      std::printf("OK (no device: %s)\n", e.what());
+      return 0;
+    }
+  }
+
+  std::mt19937_64 rng(7);
+  std::uniform_real_distribution<double> U(0.0, 100.0), E(0.05, 3.0);
+  // ---- points
+  std::vector<Point3D> pts(50000);
+  for (auto& p : pts)
+    p = { U(rng), U(rng), U(rng) };
+  OctreePointM tp(pts, 8, std::nullopt, 20);
+  void* op = oro_create(0, 0, pts.data(), pts.size(), 8, nullptr, 20);
+  const int nq = 64;
+  std::vector<BoundingBox3D> ranges(nq);
+  std::vector<Point3D> qp(nq);
+  std::vector<Ray3D> rays(nq);
+  std::normal_distribution<double> N(0.0, 1.0);
+  for (int i = 0; i < nq; ++i)
+  {
+    const Point3D c{ U(rng), U(rng), U(rng) };
+    const double e = E(rng);
+    ranges[i] = { { c[0] - e, c[1] - e, c[2] - e }, { c[0] + e, c[1] + e, c[2] + e } };
+    qp[i] = { U(rng), U(rng), U(rng) };
+    Point3D d{ N(rng), N(rng), N(rng) };
+    const double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    rays[i] = { qp[i], { d[0] / l, d[1] / l, d[2] / l } };
+  }
+  {
+    void* r = oro_range(op, ranges.data(), nq, 0, -1.0);
+    for (int i = 0; i < nq; ++i)
+      expect(tp.RangeSearch(ranges[i]), r, i, "RangeSearch");
+    oro_res_free(r);
+    std::vector<uint32_t> k(nq, 9);
+    r = oro_knn(op, qp.data(), nq, k.data(), -1.0, -1.0);
+    for (int i = 0; i < nq; ++i)
+      expect(tp.GetNearestNeighbors(qp[i], 9), r, i, "GetNearestNeighbors");
+    oro_res_free(r);
+    const Csr batch = tp.GetNearestNeighborsBatch(std::span<const Point3D>(qp), 9);
+    r = oro_knn(op, qp.data(), nq, k.data(), -1.0, -1.0);
+    for (int i = 0; i < nq; ++i)
+      expect({ batch[i].begin(), batch[i].end() }, r, i, "GetNearestNeighborsBatch");
+    oro_res_free(r);
+  }
+  oro_destroy(op);
+
+  // ---- boxes
+  std::vector<BoundingBox3D> boxes(20000);
+  for (auto& b : boxes)
+  {
+    const Point3D c{ U(rng), U(rng), U(rng) };
+    const double e = E(rng) * 0.3;
+    b = { { c[0] - e, c[1] - e, c[2] - e }, { c[0] + e, c[1] + e, c[2] + e } };
+  }
+  OctreeBoxM tb(boxes, 7, std::nullopt, 16);
+  void* ob = oro_create(0, 1, boxes.data(), boxes.size(), 7, nullptr, 16);
+  {
+    void* r = oro_pick(ob, qp.data(), nq, -1.0);
+    for (int i = 0; i < nq; ++i)
+      expect(tb.PickSearch(qp[i]), r, i, "PickSearch");
+    oro_res_free(r);
+    r = oro_range(ob, ranges.data(), nq, 1, -1.0);
+    for (int i = 0; i < nq; ++i)
+      expect(tb.RangeSearch(ranges[i], RangeSearchMode::Overlap), r, i, "RangeSearch overlap");
+    oro_res_free(r);
+    r = oro_ray(ob, rays.data(), nq, -1.0, 0.0, -1.0, 0);
+    for (int i = 0; i < nq; ++i)
+      expect(tb.RayIntersectedAll(rays[i]), r, i, "RayIntersectedAll");
+    oro_res_free(r);
+    r = oro_ray(ob, rays.data(), nq, -1.0, 0.0, -1.0, 1);
+    for (int i = 0; i < nq; ++i)
+    {
+      auto got = tb.RayIntersectedFirst(rays[i]);
+      std::reverse(got.begin(), got.end()); // farthest first -> the oracle's (distance, id) order
+      expect(got, r, i, "RayIntersectedFirst");
+    }
+    oro_res_free(r);
+    std::vector<Plane3D> planes = { { 20.0, { 1, 0, 0 } }, { -80.0, { -1, 0, 0 } }, { 30.0, { 0, 1, 0 } },
+                                    { -70.0, { 0, -1, 0 } }, { 10.0, { 0, 0, 1 } }, { -60.0, { 0, 0, -1 } } };
+    r = oro_frustum(ob, planes.data(), planes.size(), 1, -1.0);
+    expect(tb.FrustumCulling(planes), r, 0, "FrustumCulling");
+    oro_res_free(r);
+    // collisions: pairs flattened to ids
+    auto flat = [](const std::vector<std::pair<EntityID, EntityID>>& p) {
+      std::vector<uint32_t> v;
+      for (auto [a, b] : p)
+      {
+        v.push_back(a);
+        v.push_back(b);
+      }
+      return v;
+    };
+    r = oro_collide_self(ob, -1.0);
+    expect(flat(tb.CollisionDetection()), r, 0, "CollisionDetection");
+    oro_res_free(r);
+    std::vector<BoundingBox3D> other(boxes.begin(), boxes.begin() + 5000);
+    for (auto& b : other)
+      for (int c = 0; c < 3; ++c)
+      {
+        b.Min[c] += 0.2;
+        b.Max[c] += 0.2;
+      }
+    OctreeBoxM to(other, 6, std::nullopt, 12);
+    void* oo = oro_create(0, 1, other.data(), other.size(), 6, nullptr, 12);
+    r = oro_collide_pair(ob, oo, -1.0);
+    expect(flat(OctreeBoxM::CollisionDetection(tb, to)), r, 0, "CollisionDetection(two trees)");
+    oro_res_free(r);
+    oro_destroy(oo);
+  }
+  oro_destroy(ob);
+  if (g_fail)
+    return 1;
+  std::printf("OK\n");
+  return 0;
+}
