@@ -71,7 +71,7 @@ typedef struct otg_tree_info
   uint32_t max_depth;   /* maxDepthID after EstimateMaxDepth (detail/utils.h:613-622) */
   uint32_t scalar;      /* OTG_SCALAR_* */
   uint32_t kind;        /* OTG_KIND_* */
-  uint32_t reserved;
+  uint32_t n_trees;     /* trees of a forest (otg_forest_create), 0 for a single tree */
   uint64_t max_elements;
   double space_min[3];  /* the tree's space (given box or the entities' bounding box) */
   double space_max[3];
@@ -176,6 +176,33 @@ int otg_collision_pair(const otg_tree* left, const otg_tree* right, double tol, 
    or streams) race on it, so the caller must serialise them. */
 int otg_knn_noalloc(const otg_tree* tree, const void* points, uint64_t n_queries, uint32_t k, double max_distance, double tol,
                     uint32_t slot_capacity, uint32_t* counts, uint32_t* ids, double* distances, void* stream);
+
+/* ---------------------------------------------------------------- forests: many independent trees
+   Builds n_trees independent trees in one launch sequence; no counterpart as one call in the
+   reference, where each tree is its own Create (core/ot_dynamic_hash_core.h:751-822). Tree t is
+   the Create of entities [tree_offsets[t], tree_offsets[t+1]) of `entities`, with max_depth
+   (0: EstimateMaxDepth of that tree's size), its box boxes[t] (boxes NULL: its entities'
+   bounding box) and max_elements. tree_offsets: n_trees + 1 host values starting at 0.
+   Queries of forest t return the ids that tree t's own Create would give (0 .. size - 1). */
+int otg_forest_create(otg_tree* tree, const void* entities, const uint64_t* tree_offsets, uint32_t n_trees, uint32_t max_depth, const void* boxes,
+                      uint64_t max_elements, int mem, void* stream);
+/* tree of every node (node_count uint32, host), e.g. to split otg_tree_export_nodes per tree */
+int otg_forest_node_trees(const otg_tree* tree, uint32_t* node_tree);
+/* The single-tree queries above, answered for many trees in one call: queries
+   [query_offsets[t], query_offsets[t+1]) ask tree t (n_trees + 1 host values starting at 0);
+   results are per query in that order. */
+int otg_forest_range_search(const otg_tree* tree, const void* ranges, const uint64_t* query_offsets, int mode, double tol, int algo, otg_result** out,
+                            int mem, void* stream);
+int otg_forest_pick_search(const otg_tree* tree, const void* points, const uint64_t* query_offsets, double tol, int algo, otg_result** out, int mem,
+                           void* stream);
+int otg_forest_knn(const otg_tree* tree, const void* points, const uint64_t* query_offsets, const uint32_t* k, uint32_t k_all, double max_distance,
+                   double tol, int algo, otg_result** out, int mem, void* stream);
+int otg_forest_frustum_culling(const otg_tree* tree, const void* planes, uint64_t planes_per_query, const uint64_t* query_offsets, double tol, int algo,
+                               otg_result** out, int mem, void* stream);
+int otg_forest_ray_all(const otg_tree* tree, const void* rays, const uint64_t* query_offsets, double tol, double tol_increment, double max_distance,
+                       int algo, otg_result** out, int mem, void* stream);
+int otg_forest_ray_first(const otg_tree* tree, const void* rays, const uint64_t* query_offsets, double tol, double tol_increment, double max_distance,
+                         int algo, otg_result** out, int mem, void* stream);
 
 /* ---------------------------------------------------------------- results */
 int otg_result_info(const otg_result* r, uint64_t* n_queries, uint64_t* n_ids, int* has_distances);

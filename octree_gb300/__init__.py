@@ -52,6 +52,14 @@ EXPORTS = [
     ("otg_collision_self", _int, [_vp, _dbl, _int, C.POINTER(_vp), _vp]),
     ("otg_collision_pair", _int, [_vp, _vp, _dbl, _int, C.POINTER(_vp), _vp]),
     ("otg_knn_noalloc", _int, [_vp, _vp, _u64, _u32, _dbl, _dbl, _u32, _vp, _vp, _vp, _vp]),
+    ("otg_forest_create", _int, [_vp, _vp, _vp, _u32, _u32, _vp, _u64, _int, _vp]),
+    ("otg_forest_node_trees", _int, [_vp, _vp]),
+    ("otg_forest_range_search", _int, [_vp, _vp, _vp, _int, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_forest_pick_search", _int, [_vp, _vp, _vp, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_forest_knn", _int, [_vp, _vp, _vp, _vp, _u32, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_forest_frustum_culling", _int, [_vp, _vp, _u64, _vp, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_forest_ray_all", _int, [_vp, _vp, _vp, _dbl, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_forest_ray_first", _int, [_vp, _vp, _vp, _dbl, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_result_info", _int, [_vp, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_int)]),
     ("otg_result_copy", _int, [_vp, _vp, _vp, _vp, _int, _vp]),
     ("otg_result_device_ptrs", _int, [_vp, _vp, _vp, _vp]),
@@ -74,7 +82,7 @@ class _TreeInfo(C.Structure):
         ("max_depth", _u32),
         ("scalar", _u32),
         ("kind", _u32),
-        ("reserved", _u32),
+        ("n_trees", _u32),
         ("max_elements", _u64),
         ("space_min", _dbl * 3),
         ("space_max", _dbl * 3),
@@ -317,3 +325,77 @@ class Tree:
         _check(library().otg_collision_pair(self.h, other.h, tol, algo, C.byref(out), _stream_ptr(stream)))
         r = Result(out)
         return r if raw else r.to_host(stream)[1].reshape(-1, 2)
+
+
+def _offsets(off):
+    off = np.ascontiguousarray(off, dtype=np.uint64)
+    return off.ctypes.data_as(_vp), off
+
+
+class Forest(Tree):
+    """Many independent trees built by one launch sequence (otg_forest_create): tree t holds the
+    entities [tree_offsets[t], tree_offsets[t+1]) of one array. Queries name their tree through
+    query_offsets (queries [query_offsets[t], query_offsets[t+1]) ask tree t) and return the ids
+    tree t's own Create would give."""
+
+    def create(self, entities, tree_offsets, max_depth=0, boxes=None, max_elements=16, stream=None):
+        p, mem, keep = _arg(entities, self.dtype)
+        op, okeep = _offsets(tree_offsets)
+        bp, bmem, bkeep = _arg(boxes, self.dtype)
+        if boxes is not None and bmem != mem:
+            raise OtgError("entities and boxes must be in the same memory space")
+        _check(library().otg_forest_create(self.h, p, op, len(okeep) - 1, max_depth, bp, max_elements, mem, _stream_ptr(stream)))
+        self._keep = (keep, bkeep, okeep)
+        return self
+
+    @property
+    def tree_count(self):
+        return self.info().n_trees
+
+    def node_trees(self):
+        out = np.zeros(self.node_count, np.uint32)
+        _check(library().otg_forest_node_trees(self.h, out.ctypes.data_as(_vp)))
+        return out
+
+    def _fquery(self, name, data, qoff, args, mem, stream, raw):
+        op, okeep = _offsets(qoff)
+        out = _vp()
+        fn = getattr(library(), name)
+        _check(fn(self.h, data, op, *args, C.byref(out), mem, _stream_ptr(stream)))
+        r = Result(out)
+        return r if raw else r.to_host(stream)
+
+    def range_search(self, ranges, query_offsets, mode=RANGE_INSIDE, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        p, mem, keep = _arg(ranges, self.dtype)
+        return self._fquery("otg_forest_range_search", p, query_offsets, [mode, tol, algo], mem, stream, raw)
+
+    def pick_search(self, points, query_offsets, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        p, mem, keep = _arg(points, self.dtype)
+        return self._fquery("otg_forest_pick_search", p, query_offsets, [tol, algo], mem, stream, raw)
+
+    def knn(self, points, query_offsets, k, max_distance=-1.0, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        p, mem, keep = _arg(points, self.dtype)
+        kp, kall, kkeep = None, 0, None
+        if np.isscalar(k):
+            kall = int(k)
+        else:
+            kkeep = np.ascontiguousarray(k, dtype=np.uint32) if not _is_torch(k) else k.to(__import__("torch").int32).contiguous()
+            kp = kkeep.ctypes.data_as(_vp) if not _is_torch(k) else C.c_void_p(kkeep.data_ptr())
+        return self._fquery("otg_forest_knn", p, query_offsets, [kp, kall, max_distance, tol, algo], mem, stream, raw)
+
+    def frustum_culling(self, planes, query_offsets, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        """planes: (n_queries, planes_per_query, 4) as {origo distance, nx, ny, nz}."""
+        p, mem, keep = _arg(planes, self.dtype)
+        op, okeep = _offsets(query_offsets)
+        out = _vp()
+        _check(library().otg_forest_frustum_culling(self.h, p, int(planes.shape[1]), op, tol, algo, C.byref(out), mem, _stream_ptr(stream)))
+        r = Result(out)
+        return r if raw else r.to_host(stream)
+
+    def ray_all(self, rays, query_offsets, tol=-1.0, tol_increment=0.0, max_distance=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        p, mem, keep = _arg(rays, self.dtype)
+        return self._fquery("otg_forest_ray_all", p, query_offsets, [tol, tol_increment, max_distance, algo], mem, stream, raw)
+
+    def ray_first(self, rays, query_offsets, tol=-1.0, tol_increment=0.0, max_distance=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        p, mem, keep = _arg(rays, self.dtype)
+        return self._fquery("otg_forest_ray_first", p, query_offsets, [tol, tol_increment, max_distance, algo], mem, stream, raw)

@@ -141,11 +141,8 @@ __global__ void bbox_init_kernel(U* acc)
 // ---------------------------------------------------------------- 2. space
 // si_grid.h:65-103 (factors), ot_base.h:121-134 (MinPoint node size table)
 template<typename T>
-__global__ void space_setup_kernel(Space<T>* sp, const typename Ord<T>::U* acc, const T* box, u32 D, int isPoints)
+__device__ void make_space(Space<T>& s, const typename Ord<T>::U* acc, const T* box, u32 D, int isPoints)
 {
-  if (threadIdx.x != 0 || blockIdx.x != 0)
-    return;
-  Space<T> s;
   for (int d = 0; d < 3; ++d)
   {
     if (box)
@@ -184,6 +181,15 @@ __global__ void space_setup_kernel(Space<T>* sp, const typename Ord<T>::U* acc, 
       for (int c = 0; c < 3; ++c)
         s.nodeSize[d][c] = s.size[c] * lf;
   }
+}
+
+template<typename T>
+__global__ void space_setup_kernel(Space<T>* sp, const typename Ord<T>::U* acc, const T* box, u32 D, int isPoints)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0)
+    return;
+  Space<T> s;
+  make_space(s, acc, box, D, isPoints);
   *sp = s;
 }
 
@@ -256,6 +262,59 @@ __device__ __forceinline__ u32 level_from_table(const U* __restrict__ thr, U o)
 __device__ __forceinline__ float to_f(double v) { return __double2float_rn(v); }
 __device__ __forceinline__ float to_f(float v) { return v; }
 
+// Location key of one entity from the threshold tables (layout in otg_raster.cuh): integer
+// compares only, around an FP32 estimate of the cell.
+template<typename T, bool IS_BOX>
+__device__ __forceinline__ u64 entity_key(const T* e, const typename Ord<T>::U* __restrict__ tab, size_t perDim, u32 cells, const float* minF,
+                                          const float* rastF, u32 D)
+{
+  using O = Ord<T>;
+  using U = typename O::U;
+  if constexpr (!IS_BOX)
+  {
+    bool valid = true;
+    u32 g[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+      const U* td = tab + d * perDim;
+      const U o = O::of(e[d]);
+      valid = valid && o >= td[0] && o <= td[1];
+      const float est = (to_f(e[d]) - minF[d]) * rastF[d];
+      g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, o, est > 2.0e9f ? 2000000000 : int(est));
+    }
+    return valid ? encode3(g[0], g[1], g[2]) + 1 : 0;
+  }
+  else
+  {
+    bool valid = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+      const U* td = tab + d * perDim;
+      const U lo = O::of(e[d]), hi = O::of(e[3 + d]);
+      valid = valid && lo >= td[0] && lo <= td[1] && hi >= td[0] && hi <= td[1];
+    }
+    if (!valid)
+      return 0;
+    u32 g[3], level = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+      const U* td = tab + d * perDim;
+      const T center = (e[d] + e[3 + d]) * T(0.5); // internal_geometry_module.h:132-138
+      const T bsize = T(e[3 + d] - e[d]);           // internal_geometry_module.h:140-146
+      const float est = (to_f(center) - minF[d]) * rastF[d];
+      g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, O::of(center), est > 2.0e9f ? 2000000000 : int(est));
+      level = max(level, level_from_table(td + 2, O::of(bsize)));
+    }
+    const u32 shift = level * 3u;
+    u64 loc = encode3(g[0], g[1], g[2]);
+    loc = shift < 64 ? ((loc >> shift) << shift) : 0;
+    return (loc << 5) | u64(u32(D - level));
+  }
+}
+
 template<typename T, typename R, typename K, bool IS_BOX>
 __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent, u64 n, bool vec, const Space<T>* __restrict__ spg,
                                                       const typename Ord<T>::U* __restrict__ tabG, u32 cells, int tabInSmem,
@@ -297,55 +356,7 @@ __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent,
     {
       if (k >= cnt)
         break;
-      u64 key;
-      const T* e = v + k * W;
-      if constexpr (!IS_BOX)
-      {
-        bool valid = true;
-        u32 g[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-        {
-          const U* td = tab + d * perDim;
-          const U o = O::of(e[d]);
-          valid = valid && o >= td[0] && o <= td[1];
-          const float est = (to_f(e[d]) - minF[d]) * rastF[d];
-          g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, o, est > 2.0e9f ? 2000000000 : int(est));
-        }
-        key = valid ? encode3(g[0], g[1], g[2]) + 1 : 0;
-      }
-      else
-      {
-        bool valid = true;
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-        {
-          const U* td = tab + d * perDim;
-          const U lo = O::of(e[d]), hi = O::of(e[3 + d]);
-          valid = valid && lo >= td[0] && lo <= td[1] && hi >= td[0] && hi <= td[1];
-        }
-        if (!valid)
-          key = 0;
-        else
-        {
-          u32 g[3], level = 0;
-#pragma unroll
-          for (int d = 0; d < 3; ++d)
-          {
-            const U* td = tab + d * perDim;
-            const T center = (e[d] + e[3 + d]) * T(0.5); // internal_geometry_module.h:132-138
-            const T bsize = T(e[3 + d] - e[d]);           // internal_geometry_module.h:140-146
-            const float est = (to_f(center) - minF[d]) * rastF[d];
-            g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, O::of(center), est > 2.0e9f ? 2000000000 : int(est));
-            level = max(level, level_from_table(td + 2, O::of(bsize)));
-          }
-          const u32 shift = level * 3u;
-          u64 loc = encode3(g[0], g[1], g[2]);
-          loc = shift < 64 ? ((loc >> shift) << shift) : 0;
-          key = (loc << 5) | u64(u32(D - level));
-        }
-      }
-      const K kk = K(key);
+      const K kk = K(entity_key<T, IS_BOX>(v + k * W, tab, perDim, cells, minF, rastF, D));
       keys[c * E + k] = kk;
       for (u32 p = 0; p < passes; ++p)
         atomicAdd(&sh[p][(kk >> (kRadixBits * p)) & (kRadix - 1)], 1u);
@@ -499,16 +510,39 @@ __device__ __forceinline__ void write_min_point(T* nodeBox, u32 node, u64 key, u
 // chain of a node is one binary search deep. Below the root every key of a node's range shares
 // its prefix, so child 7 ends where the range ends; at the root lane 0 also searches that end
 // (locations outside the 3*D-bit grid sort after every child range and belong to no child).
+// Per-tree parameters of a forest build (several independent trees emitted together: node t is
+// the root of tree t). All null for a single tree.
+struct ForestNodes
+{
+  u32* nodeTree;     // tree of each node
+  const u32* treeD;  // max depth of each tree
+  const u64* minOff; // offset of each tree's MinPoint table (point trees)
+};
+
+// the depth, space and MinPoint table of the tree that holds `node`
+template<typename T>
+__device__ __forceinline__ void node_tree_params(const ForestNodes& fn, u32 node, u32& D, const Space<T>*& sp, const T*& minTab)
+{
+  if (fn.nodeTree)
+  {
+    const u32 tr = fn.nodeTree[node];
+    D = fn.treeD[tr];
+    sp += tr;
+    if (fn.minOff)
+      minTab += fn.minOff[tr];
+  }
+}
+
 template<typename T, bool IS_BOX>
 __global__ void __launch_bounds__(256) emit_classify_kernel(u32 d, u32 D, u64 maxElem, uint4* __restrict__ link, const u64* __restrict__ nodeKey,
                                                             T* __restrict__ nodeBox, const u32* __restrict__ levelCount, u32* __restrict__ splitCount,
                                                             u32* __restrict__ splitQueue, u32 queueCap, const T* __restrict__ minTab,
-                                                            const Space<T>* __restrict__ spg, u32* __restrict__ ownerNode, u32* __restrict__ err)
+                                                            const Space<T>* __restrict__ spg, u32* __restrict__ ownerNode, u32* __restrict__ err,
+                                                            ForestNodes fn)
 {
   u32 begin, cnt;
   level_range(levelCount, d, begin, cnt);
   const int lane = threadIdx.x & 31;
-  const u64 tabPerDim = (u64(2) << D) - 1;
   for (u32 i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < cnt; i0 += gridDim.x * blockDim.x)
   {
     const u32 i = i0 + lane;
@@ -517,8 +551,12 @@ __global__ void __launch_bounds__(256) emit_classify_kernel(u32 d, u32 D, u64 ma
     if (i < cnt)
     {
       node = begin + i;
+      u32 Dn = D;
+      const Space<T>* spn = spg;
+      const T* mt = minTab;
+      node_tree_params(fn, node, Dn, spn, mt);
       const uint4 L = link[node];
-      split = u64(L.w - L.y) > maxElem && d < D;
+      split = u64(L.w - L.y) > maxElem && d < Dn;
       if (!split)
       {
         link[node] = make_uint4(0, L.y, L.w, L.w);
@@ -528,9 +566,10 @@ __global__ void __launch_bounds__(256) emit_classify_kernel(u32 d, u32 D, u64 ma
         if constexpr (!IS_BOX)
         {
           const u64 key = nodeKey[node];
+          const u64 tabPerDim = (u64(2) << Dn) - 1;
 #pragma unroll
           for (int dim = 0; dim < 3; ++dim)
-            write_min_point(nodeBox, node, key, d, dim, minTab, tabPerDim, spg);
+            write_min_point(nodeBox, node, key, d, dim, mt, tabPerDim, spn);
         }
       }
     }
@@ -557,7 +596,7 @@ __global__ void __launch_bounds__(256) emit_split_kernel(u32 d, u32 D, const K* 
                                                          T* __restrict__ nodeBox, unsigned char* __restrict__ nodeDepth, u32* __restrict__ levelCount,
                                                          const u32* __restrict__ splitCount, const u32* __restrict__ splitQueue, u32 queueCap,
                                                          const T* __restrict__ minTab, const Space<T>* __restrict__ spg, u64 maxNodes, u32* __restrict__ err,
-                                                         u32* __restrict__ ownerNode, u32* __restrict__ nodeParent)
+                                                         u32* __restrict__ ownerNode, u32* __restrict__ nodeParent, ForestNodes fn)
 {
   u32 begin, cnt;
   level_range(levelCount, d, begin, cnt);
@@ -568,7 +607,7 @@ __global__ void __launch_bounds__(256) emit_split_kernel(u32 d, u32 D, const K* 
   const u32 groupMask = 0xffu << (grp * 8);
   const u32 warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const u32 warpsTotal = (gridDim.x * blockDim.x) >> 5;
-  const u64 tabPerDim = (u64(2) << D) - 1;
+  const u32 D0 = D;
   for (u32 qbase = warpGlobal * 4; qbase < qcount; qbase += warpsTotal * 4)
   {
     const u32 qi = qbase + grp;
@@ -576,6 +615,18 @@ __global__ void __launch_bounds__(256) emit_split_kernel(u32 d, u32 D, const K* 
     const u32 node = active ? splitQueue[qi] : 0;
     u32 b = 0, e = 0, bnd = 0, end8 = 0;
     u64 key = 1;
+    // the tree of this group's node: its depth, space and MinPoint table
+    u32 D = D0;
+    const Space<T>* spn = spg;
+    const T* mt = minTab;
+    u32 tree = 0;
+    if (active)
+    {
+      node_tree_params(fn, node, D, spn, mt);
+      if (fn.nodeTree)
+        tree = fn.nodeTree[node];
+    }
+    const u64 tabPerDim = (u64(2) << D) - 1;
     if (active)
     {
       const uint4 L = link[node];
@@ -689,6 +740,8 @@ __global__ void __launch_bounds__(256) emit_split_kernel(u32 d, u32 D, const K* 
         nodeDepth[ci] = (unsigned char)(d + 1);
         if (nodeParent)
           nodeParent[ci] = node;
+        if (fn.nodeTree)
+          fn.nodeTree[ci] = tree;
       }
       if (gl == 0)
       {
@@ -702,7 +755,7 @@ __global__ void __launch_bounds__(256) emit_split_kernel(u32 d, u32 D, const K* 
           ownerNode[q] = node;
       if constexpr (!IS_BOX)
         if (gl < 3)
-          write_min_point(nodeBox, node, key, d, gl, minTab, tabPerDim, spg);
+          write_min_point(nodeBox, node, key, d, gl, mt, tabPerDim, spn);
     }
   }
 }
@@ -764,12 +817,16 @@ __global__ void __launch_bounds__(256) mbr_level_kernel(u32 d, const u32* __rest
 
 // ot_dynamic_hash_core.h:1573-1601 InitializeRootNodeBox (MinPoint, out-of-space insertion allowed):
 // the root box becomes the union of its nominal box and its own entities.
+// One block per root (node r is the root of tree r in a forest; a single tree has root 0).
 template<typename T>
 __global__ void __launch_bounds__(256) root_box_kernel(const uint4* __restrict__ link, const T* __restrict__ sortedGeom, T* __restrict__ nodeBox,
-                                                       Space<T>* sp)
+                                                       Space<T>* spAll)
 {
   __shared__ T smn[3][256], smx[3][256];
-  const uint4 L = link[0];
+  const u32 root = blockIdx.x;
+  Space<T>* sp = spAll + root;
+  nodeBox += u64(root) * 6;
+  const uint4 L = link[root];
   T mn[3], mx[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
@@ -940,11 +997,11 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   {
     emit_classify_kernel<T, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, D, t.maxElem, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(), levelCount,
                                                                 splitCount, splitQueue, queueCap, t.minTab.as<T>(), sp,
-                                                                IS_BOX ? t.ownerNode.as<u32>() : nullptr, t.err.as<u32>());
+                                                                IS_BOX ? t.ownerNode.as<u32>() : nullptr, t.err.as<u32>(), ForestNodes{});
     if (d < D)
       emit_split_kernel<T, K, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, D, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
                                                                   t.nodeDepth.as<unsigned char>(), levelCount, splitCount, splitQueue, queueCap, t.minTab.as<T>(), sp,
-                                                                  maxNodes, t.err.as<u32>(), IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent);
+                                                                  maxNodes, t.err.as<u32>(), IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent, ForestNodes{});
   }
   prof.mark("geometry", st);
   if constexpr (IS_BOX)
@@ -996,6 +1053,7 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
   t.built = false;
   t.countsKnown = false;
   t.image32 = false;
+  t.trees = 0;
   t.boxGiven = box != nullptr;
   cudaError_t e;
   if ((e = t.err.ensure(sizeof(u32) * 4)))
@@ -1058,6 +1116,435 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
   return OTG_OK;
 }
 
+
+// ---------------------------------------------------------------- forest: many independent trees
+// Several trees are built by one launch sequence. Tree t holds the entities [off[t], off[t+1]) of
+// one input array, has its own space box (given, or its entities' bounding box), its own max
+// depth (given, or EstimateMaxDepth of its size) and therefore its own threshold tables. Per-tree
+// work is expressed through the sort's tile table: tile i is tile segTiles[i].y of tree
+// segTiles[i].x, and bounding box, key generation and the segmented radix sort run one block per
+// tile. Emission is the single-tree emission with per-node trees: node t is the root of tree t.
+
+template<typename T, int W>
+__global__ void __launch_bounds__(256) forest_bbox_kernel(const T* __restrict__ ent, const uint2* __restrict__ segTiles, const u64* __restrict__ off,
+                                                          typename Ord<T>::U* __restrict__ acc)
+{
+  using O = Ord<T>;
+  using U = typename O::U;
+  const uint2 st = segTiles[blockIdx.x];
+  const u64 b = off[st.x] + u64(st.y) * kSortTile;
+  const u64 e = min(off[st.x + 1], b + kSortTile);
+  U mn[3], mx[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    mn[d] = U(~U(0));
+    mx[d] = U(0);
+  }
+  for (u64 i = b + threadIdx.x; i < e; i += blockDim.x)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+      const U lo = O::of(ent[i * W + d]);
+      const U hi = O::of(ent[i * W + (W == 6 ? 3 + d : d)]);
+      mn[d] = lo < mn[d] ? lo : mn[d];
+      mx[d] = hi > mx[d] ? hi : mx[d];
+    }
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+      const U a = __shfl_xor_sync(0xffffffffu, mn[d], o);
+      const U c = __shfl_xor_sync(0xffffffffu, mx[d], o);
+      mn[d] = a < mn[d] ? a : mn[d];
+      mx[d] = c > mx[d] ? c : mx[d];
+    }
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+      atomicMin(&acc[u64(st.x) * 6 + d], mn[d]);
+      atomicMax(&acc[u64(st.x) * 6 + 3 + d], mx[d]);
+    }
+}
+
+template<typename U>
+__global__ void forest_bbox_init_kernel(U* acc, u32 trees)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < u64(trees) * 6; i += u64(gridDim.x) * blockDim.x)
+    acc[i] = (i % 6) < 3 ? U(~U(0)) : U(0);
+}
+
+template<typename T>
+__global__ void forest_space_kernel(Space<T>* __restrict__ sp, const typename Ord<T>::U* __restrict__ acc, const T* __restrict__ boxes,
+                                    const u32* __restrict__ treeD, u32 trees, int isPoints)
+{
+  for (u32 t = blockIdx.x * blockDim.x + threadIdx.x; t < trees; t += gridDim.x * blockDim.x)
+  {
+    Space<T> s;
+    make_space(s, acc + u64(t) * 6, boxes ? boxes + u64(t) * 6 : nullptr, treeD[t], isPoints);
+    sp[t] = s;
+  }
+}
+
+// tree holding entry i of a concatenation with offsets off[0..trees]
+__device__ __forceinline__ u32 tree_of(const u64* __restrict__ off, u32 trees, u64 i)
+{
+  u32 lo = 0, hi = trees; // off[lo] <= i < off[hi]
+  while (hi - lo > 1)
+  {
+    const u32 m = (lo + hi) >> 1;
+    if (off[m] <= i)
+      lo = m;
+    else
+      hi = m;
+  }
+  return lo;
+}
+
+template<typename T>
+__global__ void forest_tables_kernel(const Space<T>* __restrict__ sp, typename Ord<T>::U* __restrict__ tab, const u64* __restrict__ tabOff, u32 trees,
+                                     int isBox)
+{
+  const u64 total = tabOff[trees];
+  for (u64 idx = blockIdx.x * u64(blockDim.x) + threadIdx.x; idx < total; idx += u64(gridDim.x) * blockDim.x)
+  {
+    const u32 t = tree_of(tabOff, trees, idx);
+    const Space<T>& s = sp[t];
+    const u32 cells = isBox ? (1u << s.D) + 2 : (1u << s.D);
+    const u64 perDim = RasterLayout<T>::per_dim(cells);
+    const u64 local = idx - tabOff[t];
+    const int d = int(local / perDim);
+    const u32 j = u32(local % perDim);
+    tab[idx] = s.rasterDouble ? raster_threshold<T, double>(s, d, j, cells, isBox) : raster_threshold<T, float>(s, d, j, cells, isBox);
+  }
+}
+
+template<typename T>
+__global__ void forest_min_table_kernel(const Space<T>* __restrict__ sp, T* __restrict__ tab, const u64* __restrict__ minOff, u32 trees)
+{
+  const u64 total = minOff[trees];
+  for (u64 idx = blockIdx.x * u64(blockDim.x) + threadIdx.x; idx < total; idx += u64(gridDim.x) * blockDim.x)
+  {
+    const u32 t = tree_of(minOff, trees, idx);
+    const Space<T>& s = sp[t];
+    const u64 perDim = (u64(2) << s.D) - 1;
+    const u64 local = idx - minOff[t];
+    tab[idx] = s.rasterDouble ? node_min_entry<T, double>(s, int(local / perDim), local % perDim)
+                              : node_min_entry<T, float>(s, int(local / perDim), local % perDim);
+  }
+}
+
+// One block per sort tile: keys of the tile's entities with its tree's tables (in shared memory
+// when they fit), and the tree's radix digit counts ([pass][tree][256]).
+template<typename T, typename K, bool IS_BOX>
+__global__ void __launch_bounds__(256) forest_codegen_kernel(const T* __restrict__ ent, const uint2* __restrict__ segTiles, const u64* __restrict__ off,
+                                                             const Space<T>* __restrict__ sp, const typename Ord<T>::U* __restrict__ tabG,
+                                                             const u64* __restrict__ tabOff, int tabInSmem, K* __restrict__ keys, u32* __restrict__ hist,
+                                                             u32 trees, u32 passes)
+{
+  using U = typename Ord<T>::U;
+  constexpr int W = IS_BOX ? 6 : 3;
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  __shared__ u32 sh[8][kRadix];
+  __shared__ float minF[3], rastF[3];
+  const uint2 st = segTiles[blockIdx.x];
+  const u32 tr = st.x;
+  const Space<T>& s = sp[tr];
+  const u32 D = s.D;
+  const u32 cells = IS_BOX ? (1u << D) + 2 : (1u << D);
+  const size_t perDim = RasterLayout<T>::per_dim(cells);
+  const U* tab = tabG + tabOff[tr];
+  U* stab = reinterpret_cast<U*>(s_dyn);
+  for (int i = threadIdx.x; i < 8 * kRadix; i += blockDim.x)
+    (&sh[0][0])[i] = 0;
+  if (tabInSmem)
+    for (size_t i = threadIdx.x; i < 3 * perDim; i += blockDim.x)
+      stab[i] = tab[i];
+  if (threadIdx.x < 3)
+  {
+    minF[threadIdx.x] = to_f(s.min[threadIdx.x]);
+    rastF[threadIdx.x] = s.rasterDouble ? float(s.rastD[threadIdx.x]) : s.rastF[threadIdx.x];
+  }
+  __syncthreads();
+  if (tabInSmem)
+    tab = stab;
+  const u64 b = off[tr] + u64(st.y) * kSortTile;
+  const u64 e = min(off[tr + 1], b + kSortTile);
+  for (u64 i = b + threadIdx.x; i < e; i += blockDim.x)
+  {
+    T v[W];
+#pragma unroll
+    for (int c = 0; c < W; ++c)
+      v[c] = ent[i * W + c];
+    const K kk = K(entity_key<T, IS_BOX>(v, tab, perDim, cells, minF, rastF, D));
+    keys[i] = kk;
+    for (u32 p = 0; p < passes; ++p)
+      atomicAdd(&sh[p][(kk >> (kRadixBits * p)) & (kRadix - 1)], 1u);
+  }
+  __syncthreads();
+  for (u32 p = 0; p < passes; ++p)
+    for (int d = threadIdx.x; d < kRadix; d += blockDim.x)
+      if (sh[p][d])
+        atomicAdd(&hist[(u64(p) * trees + tr) * kRadix + d], sh[p][d]);
+}
+
+__global__ void forest_root_init_kernel(uint4* link, u64* nodeKey, unsigned char* nodeDepth, u32* levelCount, const u64* __restrict__ off, u32 trees,
+                                        u32* nodeParent, u32* nodeTree)
+{
+  for (u32 t = blockIdx.x * blockDim.x + threadIdx.x; t < trees; t += gridDim.x * blockDim.x)
+  {
+    link[t] = make_uint4(0, u32(off[t]), u32(off[t]), u32(off[t + 1]));
+    nodeKey[t] = 1;
+    nodeDepth[t] = 0;
+    nodeTree[t] = t;
+    if (nodeParent)
+      nodeParent[t] = t;
+    if (t == 0)
+      levelCount[0] = trees;
+  }
+}
+
+template<typename T, typename K, bool IS_BOX>
+static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStream_t st)
+{
+  constexpr int W = IS_BOX ? 6 : 3;
+  using U = typename Ord<T>::U;
+  const u32 trees = t.trees;
+  const u64 n = t.n;
+  const u32 Dmax = t.D;
+  const u32 bits = IS_BOX ? 3 * Dmax + 5 : 3 * Dmax + 1;
+  const u32 passes = (bits + kRadixBits - 1) / kRadixBits;
+  const u32 tiles = u32(t.segTilesHost.size());
+  const u64 tabEntries = t.tabOffHost.back();
+  const u64 minEntries = IS_BOX ? 1 : t.minOffHost.back();
+  u64 maxTab = 0;
+  for (u32 i = 0; i < trees; ++i)
+    maxTab = std::max(maxTab, t.tabOffHost[i + 1] - t.tabOffHost[i]);
+  const size_t maxTabBytes = sizeof(U) * maxTab;
+  const u64 maxNodes = n + trees + u64(Dmax) * (n / (t.maxElem + 1) + 1) + 2;
+  t.maxNodes = maxNodes;
+  const size_t histWords = size_t(passes) * trees * kRadix;
+  const size_t scratchWords = histWords + size_t(passes) * std::max<u32>(tiles, 1) * kRadix + passes + 8;
+  cudaError_t e;
+  if ((e = t.keysA.ensure(sizeof(K) * std::max<u64>(n, 1))) || (e = t.keysB.ensure(sizeof(K) * std::max<u64>(n, 1))) ||
+      (e = t.sortedIds.ensure(sizeof(u32) * std::max<u64>(n, 1))) || (e = t.valsB.ensure(sizeof(u32) * std::max<u64>(n, 1))) ||
+      (e = t.sortedGeom.ensure(sizeof(T) * W * std::max<u64>(n, 1))) || (e = t.nodeLink.ensure(sizeof(uint4) * maxNodes)) ||
+      (e = t.nodeKey.ensure(sizeof(u64) * maxNodes)) || (e = t.nodeBox.ensure(sizeof(T) * 6 * maxNodes)) || (e = t.nodeDepth.ensure(maxNodes)) ||
+      (e = t.nodeTree.ensure(sizeof(u32) * maxNodes)) || (e = t.levelCount.ensure(sizeof(u32) * 64)) ||
+      (e = t.splitQueue.ensure(sizeof(u32) * (n / (t.maxElem + 1) + 2))) || (e = t.space.ensure(sizeof(Space<T>) * trees)) ||
+      (e = t.sortScratch.ensure(sizeof(u32) * scratchWords)) || (e = t.bboxBits.ensure(sizeof(U) * 6 * trees)) ||
+      (e = t.rasterTab.ensure(sizeof(U) * std::max<u64>(tabEntries, 1))) || (e = t.minTab.ensure(sizeof(T) * minEntries)) ||
+      (e = t.treeOff.ensure(sizeof(u64) * (trees + 1))) || (e = t.treeD.ensure(sizeof(u32) * trees)) ||
+      (e = t.tabOff.ensure(sizeof(u64) * (trees + 1))) || (e = t.minOff.ensure(sizeof(u64) * (trees + 1))) ||
+      (e = t.segTiles.ensure(sizeof(uint2) * std::max<u32>(tiles, 1))) ||
+      (IS_BOX && ((e = t.nodeMax.ensure(sizeof(T) * 3 * maxNodes)) || (e = t.ownerNode.ensure(sizeof(u32) * std::max<u64>(n, 1))) ||
+                  (e = t.nodeParent.ensure(sizeof(u32) * maxNodes)))))
+    return cuda_status(e, "allocating forest buffers");
+
+  // host-computed layout: tree offsets, depths, table offsets, tile table
+  cudaMemcpyAsync(t.treeOff.p, t.treeOffHost.data(), sizeof(u64) * (trees + 1), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(t.treeD.p, t.treeDHost.data(), sizeof(u32) * trees, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(t.tabOff.p, t.tabOffHost.data(), sizeof(u64) * (trees + 1), cudaMemcpyHostToDevice, st);
+  if (!IS_BOX)
+    cudaMemcpyAsync(t.minOff.p, t.minOffHost.data(), sizeof(u64) * (trees + 1), cudaMemcpyHostToDevice, st);
+  if (tiles)
+    cudaMemcpyAsync(t.segTiles.p, t.segTilesHost.data(), sizeof(uint2) * tiles, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(t.sortScratch.p, 0, sizeof(u32) * scratchWords, st);
+  cudaMemsetAsync(t.levelCount.p, 0, sizeof(u32) * 64, st);
+
+  Profiler& prof = profiler();
+  prof.reset();
+  const u64* off = t.treeOff.as<u64>();
+  const uint2* segTiles = t.segTiles.as<uint2>();
+  Space<T>* sp = t.space.as<Space<T>>();
+  prof.mark("bbox", st);
+  if (!boxes)
+  {
+    forest_bbox_init_kernel<U><<<grid_blocks(u64(trees) * 6), 256, 0, st>>>(t.bboxBits.as<U>(), trees);
+    if (tiles)
+      forest_bbox_kernel<T, W><<<tiles, 256, 0, st>>>(ent, segTiles, off, t.bboxBits.as<U>());
+  }
+  prof.mark("tables", st);
+  forest_space_kernel<T><<<grid_blocks(trees, 128), 128, 0, st>>>(sp, t.bboxBits.as<U>(), boxes, t.treeD.as<u32>(), trees, IS_BOX ? 0 : 1);
+  forest_tables_kernel<T><<<grid_blocks(tabEntries, 128, 152 * 32), 128, 0, st>>>(sp, t.rasterTab.as<U>(), t.tabOff.as<u64>(), trees, IS_BOX ? 1 : 0);
+  if (!IS_BOX)
+    forest_min_table_kernel<T><<<grid_blocks(minEntries), 256, 0, st>>>(sp, t.minTab.as<T>(), t.minOff.as<u64>(), trees);
+
+  prof.mark("codegen", st);
+  u32* scratch = t.sortScratch.as<u32>();
+  u32* hist = scratch;
+  u32* status = scratch + histWords;
+  u32* counters = status + size_t(passes) * std::max<u32>(tiles, 1) * kRadix;
+  const int tabInSmem = maxTabBytes <= 64 * 1024 ? 1 : 0;
+  const size_t cgSmem = tabInSmem ? maxTabBytes : 0;
+  if (tiles)
+  {
+    auto kfn = forest_codegen_kernel<T, K, IS_BOX>;
+    cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
+    kfn<<<tiles, 256, cgSmem, st>>>(ent, segTiles, off, sp, t.rasterTab.as<U>(), t.tabOff.as<u64>(), tabInSmem, t.keysA.as<K>(), hist, trees, passes);
+  }
+
+  prof.mark("sort", st);
+  const bool inB = onesweep_passes_segmented<K>(t.keysA.as<K>(), t.sortedIds.as<u32>(), t.keysB.as<K>(), t.valsB.as<u32>(), n, passes, true, segTiles,
+                                                tiles, off, trees, hist, status, counters, t.err.as<u32>(), st);
+  if (inB)
+  {
+    std::swap(t.sortedIds, t.valsB);
+    t.sortedKeys = t.keysB.p;
+  }
+  else
+    t.sortedKeys = t.keysA.p;
+  const K* keys = reinterpret_cast<const K*>(t.sortedKeys);
+
+  prof.mark("gather", st);
+  if (n)
+    gather_kernel<T, W><<<grid_blocks((n + kGatherPerThread - 1) / kGatherPerThread, 256, 152 * 16), 256, 0, st>>>(ent, t.sortedIds.as<u32>(), n,
+                                                                                                                    t.sortedGeom.as<T>());
+  prof.mark("emit", st);
+  u32* parent = IS_BOX ? t.nodeParent.as<u32>() : nullptr;
+  forest_root_init_kernel<<<grid_blocks(trees, 128), 128, 0, st>>>(t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeDepth.as<unsigned char>(),
+                                                                   t.levelCount.as<u32>(), off, trees, parent, t.nodeTree.as<u32>());
+  const int emitBlocks = grid_blocks(maxNodes, 256, 152 * 16);
+  u32* levelCount = t.levelCount.as<u32>();
+  u32* splitCount = levelCount + 32;
+  const u32 queueCap = u32(n / (t.maxElem + 1) + 2);
+  const ForestNodes fn{ t.nodeTree.as<u32>(), t.treeD.as<u32>(), IS_BOX ? nullptr : t.minOff.as<u64>() };
+  for (u32 d = 0; d <= Dmax; ++d)
+  {
+    emit_classify_kernel<T, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, Dmax, t.maxElem, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
+                                                                levelCount, splitCount, t.splitQueue.as<u32>(), queueCap, t.minTab.as<T>(), sp,
+                                                                IS_BOX ? t.ownerNode.as<u32>() : nullptr, t.err.as<u32>(), fn);
+    if (d < Dmax)
+      emit_split_kernel<T, K, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, Dmax, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
+                                                                  t.nodeDepth.as<unsigned char>(), levelCount, splitCount, t.splitQueue.as<u32>(), queueCap,
+                                                                  t.minTab.as<T>(), sp, maxNodes, t.err.as<u32>(),
+                                                                  IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent, fn);
+  }
+  prof.mark("geometry", st);
+  if constexpr (IS_BOX)
+  {
+    for (int d = int(Dmax); d >= 0; --d)
+      mbr_level_kernel<T><<<emitBlocks, 256, 0, st>>>(u32(d), levelCount, t.nodeLink.as<uint4>(), t.sortedGeom.as<T>(), t.nodeBox.as<T>(),
+                                                      t.nodeMax.as<T>());
+  }
+  else if (boxes)
+    root_box_kernel<T><<<trees, 256, 0, st>>>(t.nodeLink.as<uint4>(), t.sortedGeom.as<T>(), t.nodeBox.as<T>(), sp);
+  prof.mark("end", st);
+  return cuda_status(cudaGetLastError(), "launching forest build kernels");
+}
+
+int build_forest(TreeState& t, const void* entities, const u64* treeOffsets, u32 trees, u32 maxDepth, const void* boxes, u64 maxElem, int mem,
+                 cudaStream_t st)
+{
+  const bool isBox = t.kind == OTG_KIND_BOXES;
+  const int W = isBox ? 6 : 3;
+  const size_t esz = t.scalar == OTG_SCALAR_F64 ? 8 : 4;
+  if (maxElem == 0 || trees == 0 || !treeOffsets || treeOffsets[0] != 0)
+  {
+    set_error("a forest needs at least one tree, offsets starting at 0 and maxElementNo > 0");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  const u64 n = treeOffsets[trees];
+  if (n >= (u64(1) << 30))
+  {
+    set_error("entity count must be below 2^30");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  if (maxDepth > 19)
+  {
+    set_error("maxDepthID must be in [1, 19]");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  t.treeOffHost.assign(treeOffsets, treeOffsets + trees + 1);
+  t.treeDHost.resize(trees);
+  t.tabOffHost.assign(trees + 1, 0);
+  t.minOffHost.assign(trees + 1, 0);
+  t.segTilesHost.clear();
+  u32 Dmax = 1;
+  for (u32 i = 0; i < trees; ++i)
+  {
+    if (treeOffsets[i + 1] < treeOffsets[i])
+    {
+      set_error("tree offsets must not decrease");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+    const u64 ni = treeOffsets[i + 1] - treeOffsets[i];
+    const u32 D = maxDepth ? maxDepth : estimate_max_depth(ni, maxElem);
+    t.treeDHost[i] = D;
+    Dmax = std::max(Dmax, D);
+    const u32 cells = isBox ? (1u << D) + 2 : (1u << D);
+    t.tabOffHost[i + 1] = t.tabOffHost[i] + 3 * (2 + kLevelThresholds + cells);
+    t.minOffHost[i + 1] = t.minOffHost[i] + 3 * ((u64(2) << D) - 1);
+    const u64 nt = (ni + kSortTile - 1) / kSortTile;
+    for (u64 k = 0; k < nt; ++k)
+      t.segTilesHost.push_back(make_uint2(i, u32(k)));
+  }
+  if (n + trees + u64(Dmax) * (n / (maxElem + 1) + 1) + 2 >= (u64(1) << kChildShift))
+  {
+    set_error("entity count too large for the 28-bit node index of this build");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
+  t.n = n;
+  t.D = Dmax;
+  t.maxElem = maxElem;
+  t.built = false;
+  t.countsKnown = false;
+  t.image32 = false;
+  t.trees = trees;
+  t.boxGiven = boxes != nullptr;
+  cudaError_t e;
+  if ((e = t.err.ensure(sizeof(u32) * 4)))
+    return cuda_status(e, "allocating status word");
+  cudaMemsetAsync(t.err.p, 0, sizeof(u32) * 4, st);
+  const void* ent = entities;
+  if (n && mem == OTG_MEM_HOST)
+  {
+    if ((e = t.entities.ensure(esz * W * n)))
+      return cuda_status(e, "allocating entity buffer");
+    if ((e = cudaMemcpyAsync(t.entities.p, entities, esz * W * n, cudaMemcpyHostToDevice, st)))
+      return cuda_status(e, "copying entities");
+    ent = t.entities.p;
+  }
+  const void* dboxes = nullptr;
+  if (boxes)
+  {
+    if ((e = t.boxDev.ensure(esz * 6 * trees)))
+      return cuda_status(e, "allocating boxes");
+    if ((e = cudaMemcpyAsync(t.boxDev.p, boxes, esz * 6 * trees, mem == OTG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st)))
+      return cuda_status(e, "copying boxes");
+    dboxes = t.boxDev.p;
+  }
+  const u32 bits = isBox ? 3 * Dmax + 5 : 3 * Dmax + 1;
+  t.keys32 = bits <= 32;
+  int rc;
+  if (t.scalar == OTG_SCALAR_F64)
+  {
+    const double* p = static_cast<const double*>(ent);
+    const double* b = static_cast<const double*>(dboxes);
+    if (isBox)
+      rc = t.keys32 ? forest_build_impl<double, u32, true>(t, p, b, st) : forest_build_impl<double, u64, true>(t, p, b, st);
+    else
+      rc = t.keys32 ? forest_build_impl<double, u32, false>(t, p, b, st) : forest_build_impl<double, u64, false>(t, p, b, st);
+  }
+  else
+  {
+    const float* p = static_cast<const float*>(ent);
+    const float* b = static_cast<const float*>(dboxes);
+    if (isBox)
+      rc = t.keys32 ? forest_build_impl<float, u32, true>(t, p, b, st) : forest_build_impl<float, u64, true>(t, p, b, st);
+    else
+      rc = t.keys32 ? forest_build_impl<float, u32, false>(t, p, b, st) : forest_build_impl<float, u64, false>(t, p, b, st);
+  }
+  if (rc)
+    return rc;
+  t.built = true;
+  if (mem == OTG_MEM_HOST)
+    return finish_build(t, st);
+  return OTG_OK;
+}
+
 int finish_build(TreeState& t, cudaStream_t st)
 {
   if (t.countsKnown)
@@ -1065,7 +1552,7 @@ int finish_build(TreeState& t, cudaStream_t st)
   u32 hostErr = 0;
   std::vector<u32> lc(32, 0);
   cudaError_t e = cudaMemcpyAsync(&hostErr, t.err.p, sizeof(u32), cudaMemcpyDeviceToHost, st);
-  if (!e && t.n)
+  if (!e && (t.n || t.trees))
     e = cudaMemcpyAsync(lc.data(), t.levelCount.p, sizeof(u32) * 32, cudaMemcpyDeviceToHost, st);
   if (!e)
     e = cudaStreamSynchronize(st);
@@ -1081,7 +1568,7 @@ int finish_build(TreeState& t, cudaStream_t st)
     set_error("node capacity exceeded during emission");
     return OTG_ERR_OUT_OF_MEMORY;
   }
-  if (t.n)
+  if (t.n || t.trees)
   {
     t.levelCountsHost.assign(lc.begin(), lc.begin() + t.D + 1);
     u64 s = 0;
@@ -1095,6 +1582,11 @@ int finish_build(TreeState& t, cudaStream_t st)
 
 int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st)
 {
+  if (t.trees)
+  {
+    set_error("location export is defined for a single tree, not a forest");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
   if (t.n == 0)
     return OTG_OK;
   DevBuf tmp;

@@ -112,18 +112,24 @@ static int new_result(otg_result** out)
 static void release_tree(TreeState& s)
 {
   DevBuf* bufs[] = { &s.entities, &s.sortedIds, &s.sortedGeom, &s.keysA, &s.keysB, &s.valsB, &s.nodeLink, &s.nodeKey, &s.nodeBox,
-                     &s.nodeMax, &s.nodeDepth, &s.levelCount, &s.space, &s.sortScratch, &s.err, &s.bboxBits, &s.locations, &s.boxDev, &s.ownerNode, &s.nodeParent, &s.rasterTab, &s.minTab, &s.splitQueue, &s.geom32, &s.nodeBox32 };
+                     &s.nodeMax, &s.nodeDepth, &s.levelCount, &s.space, &s.sortScratch, &s.err, &s.bboxBits, &s.locations, &s.boxDev, &s.ownerNode, &s.nodeParent, &s.rasterTab, &s.minTab, &s.splitQueue, &s.geom32, &s.nodeBox32, &s.treeOff, &s.treeD, &s.nodeTree, &s.tabOff, &s.minOff, &s.segTiles };
   for (DevBuf* b : bufs)
     b->release();
 }
 
+// forest: the query addresses the trees of a forest (per-query trees) rather than a single tree
 template<typename F>
-static int run_query(const otg_tree* t, otg_result** out, cudaStream_t st, F&& f)
+static int run_query(const otg_tree* t, otg_result** out, cudaStream_t st, F&& f, bool forest = false)
 {
   if (int rc = require_device())
     return rc;
   if (int rc = ready(t, st))
     return rc;
+  if ((t->s.trees != 0) != forest)
+  {
+    set_error(forest ? "otg_forest_* queries need a tree built by otg_forest_create" : "a forest is queried with the otg_forest_* calls");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
   if (int rc = new_result(out))
     return rc;
   int rc = f((*out)->s);
@@ -137,6 +143,23 @@ static int run_query(const otg_tree* t, otg_result** out, cudaStream_t st, F&& f
 } // namespace otg
 
 using namespace otg;
+
+// forest queries: queries [query_offsets[t], query_offsets[t+1]) ask tree t (host offsets)
+template<typename F>
+static int forest_query(const otg_tree* t, const uint64_t* qoff, otg_result** out, void* stream, F&& f)
+{
+  return run_query(
+    t, out, (cudaStream_t)stream,
+    [&](ResultState& r) {
+      DevBuf qoffDev, qTree;
+      u64 nq = 0;
+      if (int rc = forest_query_trees(t->s, qoff, qoffDev, qTree, nq, (cudaStream_t)stream))
+        return rc;
+      return f(r, nq, qTree.as<u32>());
+    },
+    true);
+}
+
 
 extern "C"
 {
@@ -211,6 +234,7 @@ extern "C"
     info->max_depth = t->s.D;
     info->scalar = uint32_t(t->s.scalar);
     info->kind = uint32_t(t->s.kind);
+    info->n_trees = t->s.trees;
     info->max_elements = t->s.maxElem;
     if (t->s.n)
     {
@@ -323,6 +347,11 @@ extern "C"
   {
     if (int rc = ready(b, (cudaStream_t)stream))
       return rc;
+    if (b->s.trees)
+    {
+      set_error("collision detection is defined for single trees, not forests");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
     if ((a && a->s.kind != OTG_KIND_BOXES) || b->s.kind != OTG_KIND_BOXES || (a && a->s.scalar != b->s.scalar))
     {
       set_error("collision detection needs two box trees of the same scalar type");
@@ -343,7 +372,88 @@ extern "C"
       set_error("the tree's build has not been synchronised (call otg_tree_sync first)");
       return OTG_ERR_INVALID_ARGUMENT;
     }
+    if (t->s.trees)
+    {
+      set_error("otg_knn_noalloc answers queries on a single tree, not a forest");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
     return query_knn_noalloc(t->s, points, nq, k, max_distance, tol, slot_capacity, counts, ids, distances, (cudaStream_t)stream);
+  }
+
+  int otg_forest_create(otg_tree* t, const void* entities, const uint64_t* tree_offsets, uint32_t n_trees, uint32_t max_depth, const void* boxes,
+                        uint64_t max_elements, int mem, void* stream)
+  {
+    if (int rc = require_tree(t, false))
+      return rc;
+    if ((!entities && tree_offsets && n_trees && tree_offsets[n_trees]) || (mem != OTG_MEM_HOST && mem != OTG_MEM_DEVICE))
+    {
+      set_error("otg_forest_create: invalid argument");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+    if (int rc = require_device())
+      return rc;
+    return build_forest(t->s, entities, tree_offsets, n_trees, max_depth, boxes, max_elements, mem, (cudaStream_t)stream);
+  }
+
+  int otg_forest_node_trees(const otg_tree* t, uint32_t* node_tree)
+  {
+    if (int rc = ready(t, nullptr))
+      return rc;
+    if (!t->s.trees || !node_tree)
+    {
+      set_error("otg_forest_node_trees needs a forest and an output array");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+    return cuda_status(cudaMemcpy(node_tree, t->s.nodeTree.p, sizeof(uint32_t) * t->s.nodeCount, cudaMemcpyDeviceToHost), "exporting node trees");
+  }
+
+  int otg_forest_range_search(const otg_tree* t, const void* ranges, const uint64_t* query_offsets, int mode, double tol, int algo, otg_result** out, int mem,
+                              void* stream)
+  {
+    if (mode != OTG_RANGE_INSIDE && mode != OTG_RANGE_OVERLAP)
+      return OTG_ERR_INVALID_ARGUMENT;
+    return forest_query(t, query_offsets, out, stream, [&](ResultState& r, u64 nq, const u32* qt) {
+      return query_range(t->s, ranges, nq, mode, tol, algo, r, mem, (cudaStream_t)stream, qt);
+    });
+  }
+
+  int otg_forest_pick_search(const otg_tree* t, const void* points, const uint64_t* query_offsets, double tol, int algo, otg_result** out, int mem,
+                             void* stream)
+  {
+    return forest_query(t, query_offsets, out, stream,
+                        [&](ResultState& r, u64 nq, const u32* qt) { return query_pick(t->s, points, nq, tol, algo, r, mem, (cudaStream_t)stream, qt); });
+  }
+
+  int otg_forest_knn(const otg_tree* t, const void* points, const uint64_t* query_offsets, const uint32_t* k, uint32_t k_all, double max_distance,
+                     double tol, int algo, otg_result** out, int mem, void* stream)
+  {
+    return forest_query(t, query_offsets, out, stream, [&](ResultState& r, u64 nq, const u32* qt) {
+      return query_knn(t->s, points, nq, k, k_all, max_distance, tol, algo, r, mem, (cudaStream_t)stream, qt);
+    });
+  }
+
+  int otg_forest_frustum_culling(const otg_tree* t, const void* planes, uint64_t planes_per_query, const uint64_t* query_offsets, double tol, int algo,
+                                 otg_result** out, int mem, void* stream)
+  {
+    return forest_query(t, query_offsets, out, stream, [&](ResultState& r, u64 nq, const u32* qt) {
+      return query_frustum(t->s, planes, planes_per_query, nq, tol, algo, r, mem, (cudaStream_t)stream, qt);
+    });
+  }
+
+  int otg_forest_ray_all(const otg_tree* t, const void* rays, const uint64_t* query_offsets, double tol, double tol_increment, double max_distance, int algo,
+                         otg_result** out, int mem, void* stream)
+  {
+    return forest_query(t, query_offsets, out, stream, [&](ResultState& r, u64 nq, const u32* qt) {
+      return query_ray(t->s, rays, nq, tol, tol_increment, max_distance, false, algo, r, mem, (cudaStream_t)stream, qt);
+    });
+  }
+
+  int otg_forest_ray_first(const otg_tree* t, const void* rays, const uint64_t* query_offsets, double tol, double tol_increment, double max_distance,
+                           int algo, otg_result** out, int mem, void* stream)
+  {
+    return forest_query(t, query_offsets, out, stream, [&](ResultState& r, u64 nq, const u32* qt) {
+      return query_ray(t->s, rays, nq, tol, tol_increment, max_distance, true, algo, r, mem, (cudaStream_t)stream, qt);
+    });
   }
 
   int otg_result_info(const otg_result* r, uint64_t* nq, uint64_t* nids, int* has_distances)

@@ -108,6 +108,19 @@ struct TreeState
   DevBuf boxDev;     // the given space box (6 scalars)
   DevBuf rasterTab;  // exact rasterisation thresholds (otg_raster.cuh)
   DevBuf minTab;     // MinPoint node table per (dimension, depth, cell)
+  // forest: `trees` independent trees built and queried together (0 = a single tree). Node t is
+  // the root of tree t; tree t holds the entities [treeOff[t], treeOff[t+1]) of the input.
+  u32 trees = 0;
+  std::vector<u64> treeOffHost;
+  std::vector<u32> treeDHost;
+  DevBuf treeOff;    // u64[trees + 1]
+  DevBuf treeD;      // u32[trees]: max depth of each tree
+  DevBuf nodeTree;   // u32 per node: its tree
+  DevBuf tabOff;     // u64[trees + 1]: offset of each tree's threshold tables (entries)
+  DevBuf minOff;     // u64[trees + 1]: offset of each tree's MinPoint table (point trees)
+  DevBuf segTiles;   // uint2 per sort tile: {tree, tile within the tree}
+  std::vector<u64> tabOffHost, minOffHost;
+  std::vector<uint2> segTilesHost;
   DevBuf geom32;     // FP32 image of sortedGeom for the query filters (built on first use)
   DevBuf nodeBox32;  // FP32 outward-rounded node boxes for the query filters
   bool image32 = false;
@@ -148,18 +161,24 @@ int cuda_status(cudaError_t e, const char* what);
 
 // build entry (otg_build.cu)
 int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const void* box, u64 maxElem, int mem, cudaStream_t st);
+int build_forest(TreeState& t, const void* entities, const u64* treeOffsets, u32 trees, u32 maxDepth, const void* boxes, u64 maxElem, int mem,
+                 cudaStream_t st);
 int finish_build(TreeState& t, cudaStream_t st);
 int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st);
 int export_nodes(const TreeState& t, u64* keys, double* minSize, u64* eoff, u32* eids, u32* childCount);
 
-// queries (otg_query.cu)
-int query_range(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st);
-int query_pick(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st);
+// queries (otg_query.cu). qTree: the tree of each query when t is a forest (null otherwise).
+int query_range(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
+                const u32* qTree = nullptr);
+int query_pick(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st, const u32* qTree = nullptr);
 int query_knn(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAll, double maxDist, double tol, int algo, ResultState& r, int mem,
-              cudaStream_t st);
-int query_frustum(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st);
+              cudaStream_t st, const u32* qTree = nullptr);
+int query_frustum(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
+                  const u32* qTree = nullptr);
 int query_ray(const TreeState& t, const void* rays, u64 nq, double tol, double tolInc, double maxDist, bool first, int algo, ResultState& r,
-              int mem, cudaStream_t st);
+              int mem, cudaStream_t st, const u32* qTree = nullptr);
+// per-query trees of a forest from host query offsets (queries [qoff[t], qoff[t+1]) ask tree t)
+int forest_query_trees(const TreeState& t, const u64* qoffHost, DevBuf& qoffDev, DevBuf& qTree, u64& nq, cudaStream_t st);
 int query_collide_self(const TreeState& t, double tol, int algo, ResultState& r, cudaStream_t st);
 int query_collide_pair(const TreeState& a, const TreeState& b, double tol, int algo, ResultState& r, cudaStream_t st);
 // batched filtered kNN on point trees (otg_knn.cu); inputs in device memory

@@ -33,6 +33,8 @@ __global__ void __launch_bounds__(128) range_plain_kernel(TreeView<T> tv, const 
   const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq)
     return;
+  const u32 root = query_root(tv, q);
+  const u32 idBase = id_base(tv, root);
   T r[6];
   load_box(ranges + u64(q) * 6, r);
   // root shortcut (:488-511): the whole root box inside the range -> every entity id
@@ -41,13 +43,14 @@ __global__ void __launch_bounds__(128) range_plain_kernel(TreeView<T> tv, const 
 #pragma unroll
     for (int c = 0; c < 3; ++c)
     {
-      rb[c] = tv.nodeBox[c];
-      rb[3 + c] = tv.nodeBox[c] + tv.nodeBox[3 + c];
+      rb[c] = tv.nodeBox[u64(root) * 6 + c];
+      rb[3 + c] = tv.nodeBox[u64(root) * 6 + c] + tv.nodeBox[u64(root) * 6 + 3 + c];
     }
     if (G::range_contains_box(r, rb, tol))
     {
-      u64 pos = out.reserve(tv.n);
-      for (u32 i = 0; i < tv.n; ++i)
+      const u32 nt = tv.qTree ? u32(tv.treeOff[root + 1] - tv.treeOff[root]) : tv.n;
+      u64 pos = out.reserve(nt);
+      for (u32 i = 0; i < nt; ++i)
         if (pos + i < out.capacity)
           out.items[pos + i] = (u64(q) << 32) | i;
       return;
@@ -70,7 +73,7 @@ __global__ void __launch_bounds__(128) range_plain_kernel(TreeView<T> tv, const 
   u32 stack[kStack];
   int sp = 0;
   u32 visits = 0;
-  stack[sp++] = 0;
+  stack[sp++] = root;
   while (sp > 0)
   {
     const u32 node = stack[--sp];
@@ -97,7 +100,7 @@ __global__ void __launch_bounds__(128) range_plain_kernel(TreeView<T> tv, const 
       u64 pos = out.reserve(len);
       for (u32 i = 0; i < len; ++i)
         if (pos + i < out.capacity)
-          out.items[pos + i] = (u64(q) << 32) | tv.ids[L.y + i];
+          out.items[pos + i] = (u64(q) << 32) | (tv.ids[L.y + i] - idBase);
       continue;
     }
     for (u32 e = L.y; e < L.z; ++e)
@@ -112,7 +115,7 @@ __global__ void __launch_bounds__(128) range_plain_kernel(TreeView<T> tv, const 
         ok = (mode == OTG_RANGE_OVERLAP) ? (G::box_relation(r, b, tol) == -1) : G::contains_box_no_tol(r, b);
       }
       if (ok)
-        out.put(q, tv.ids[e]);
+        out.put(q, (tv.ids[e] - idBase));
     }
     const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
     if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
@@ -133,6 +136,8 @@ __global__ void __launch_bounds__(128) pick_plain_kernel(TreeView<T> tv, const T
   const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq)
     return;
+  const u32 root = query_root(tv, q);
+  const u32 idBase = id_base(tv, root);
   T p[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
@@ -142,8 +147,8 @@ __global__ void __launch_bounds__(128) pick_plain_kernel(TreeView<T> tv, const T
 #pragma unroll
     for (int c = 0; c < 3; ++c)
     {
-      rb[c] = tv.nodeBox[c];
-      rb[3 + c] = tv.nodeBox[c] + tv.nodeBox[3 + c];
+      rb[c] = tv.nodeBox[u64(root) * 6 + c];
+      rb[3 + c] = tv.nodeBox[u64(root) * 6 + c] + tv.nodeBox[u64(root) * 6 + 3 + c];
     }
     if (!G::box_contains_point(rb, p, tol)) // :430-431 (DoesBoxContainPointAD box form)
       return;
@@ -151,7 +156,7 @@ __global__ void __launch_bounds__(128) pick_plain_kernel(TreeView<T> tv, const T
   u32 stack[kStack];
   int sp = 0;
   u32 visits = 0;
-  stack[sp++] = 0;
+  stack[sp++] = root;
   while (sp > 0)
   {
     const u32 node = stack[--sp];
@@ -168,7 +173,7 @@ __global__ void __launch_bounds__(128) pick_plain_kernel(TreeView<T> tv, const T
     {
       bool ok = tv.isBox ? G::box_contains_point(tv.geom + u64(e) * 6, p, tol) : G::points_equal(tv.geom + u64(e) * 3, p, tol);
       if (ok)
-        out.put(q, tv.ids[e]);
+        out.put(q, (tv.ids[e] - idBase));
     }
     const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
     if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
@@ -190,11 +195,13 @@ __global__ void __launch_bounds__(128) frustum_plain_kernel(TreeView<T> tv, cons
   const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq || np == 0)
     return;
+  const u32 root = query_root(tv, q);
+  const u32 idBase = id_base(tv, root);
   const T* pl = planes + u64(q) * np * 4;
   u32 stack[kStack];
   int sp = 0;
   u32 visits = 0;
-  stack[sp++] = 0;
+  stack[sp++] = root;
   while (sp > 0)
   {
     const u32 node = stack[--sp];
@@ -236,7 +243,7 @@ __global__ void __launch_bounds__(128) frustum_plain_kernel(TreeView<T> tv, cons
         neg = rel == 0;
       }
       if (!neg)
-        out.put(q, tv.ids[e]);
+        out.put(q, (tv.ids[e] - idBase));
     }
     const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
     if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
@@ -262,6 +269,8 @@ __global__ void __launch_bounds__(128) knn_threshold_kernel(TreeView<T> tv, cons
   const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq)
     return;
+  const u32 root = query_root(tv, q);
+  const u32 idBase = id_base(tv, root);
   u32 k = kArr ? kArr[q] : kAll;
   if (k == 0) // ot_query.h:1217-1219: no neighbour requested -> empty result (no distance is below 0)
   {
@@ -284,8 +293,8 @@ __global__ void __launch_bounds__(128) knn_threshold_kernel(TreeView<T> tv, cons
   T sdist[kStack];
   int sp = 0;
   u32 visits = 0;
-  stack[sp] = 0;
-  sdist[sp++] = G::wall_distance(p, tv.nodeBox, tv.nodeBox + 3);
+  stack[sp] = root;
+  sdist[sp++] = G::wall_distance(p, tv.nodeBox + u64(root) * 6, tv.nodeBox + u64(root) * 6 + 3);
   while (sp > 0 && k > 0)
   {
     --sp;
@@ -390,6 +399,8 @@ __global__ void __launch_bounds__(128) knn_collect_kernel(TreeView<T> tv, const 
   const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq)
     return;
+  const u32 root = query_root(tv, q);
+  const u32 idBase = id_base(tv, root);
   const T F = Fin[q];
   T p[3];
 #pragma unroll
@@ -398,7 +409,7 @@ __global__ void __launch_bounds__(128) knn_collect_kernel(TreeView<T> tv, const 
   u32 stack[kStack];
   int sp = 0;
   u32 visits = 0;
-  stack[sp++] = 0;
+  stack[sp++] = root;
   while (sp > 0)
   {
     const u32 node = stack[--sp];
@@ -415,7 +426,7 @@ __global__ void __launch_bounds__(128) knn_collect_kernel(TreeView<T> tv, const 
     {
       T d = entity_distance(tv, e, p, tol);
       if (d < F)
-        out.put(q, tv.ids[e], double(d));
+        out.put(q, (tv.ids[e] - idBase), double(d));
     }
     const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
     if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
@@ -443,6 +454,8 @@ __global__ void __launch_bounds__(128) ray_all_plain_kernel(TreeView<T> tv, cons
   const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq)
     return;
+  const u32 root = query_root(tv, q);
+  const u32 idBase = id_base(tv, root);
   RayD<T> ray;
   ray.make(rays + u64(q) * 6, rays + u64(q) * 6 + 3, tol, tolInc);
   if (!ray.valid)
@@ -450,7 +463,7 @@ __global__ void __launch_bounds__(128) ray_all_plain_kernel(TreeView<T> tv, cons
   u32 stack[kStack];
   int sp = 0;
   u32 visits = 0;
-  stack[sp++] = 0;
+  stack[sp++] = root;
   while (sp > 0)
   {
     const u32 node = stack[--sp];
@@ -470,7 +483,7 @@ __global__ void __launch_bounds__(128) ray_all_plain_kernel(TreeView<T> tv, cons
         continue;
       if (!(maxDist == T(0) || en <= maxDist))
         continue;
-      out.put(q, tv.ids[e], double(en));
+      out.put(q, (tv.ids[e] - idBase), double(en));
     }
     const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
     if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
@@ -492,6 +505,8 @@ __global__ void __launch_bounds__(128) ray_first_threshold_kernel(TreeView<T> tv
   const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq)
     return;
+  const u32 root = query_root(tv, q);
+  const u32 idBase = id_base(tv, root);
   RayD<T> ray;
   ray.make(rays + u64(q) * 6, rays + u64(q) * 6 + 3, tol, tolInc);
   T M = maxDist;
@@ -504,7 +519,7 @@ __global__ void __launch_bounds__(128) ray_first_threshold_kernel(TreeView<T> tv
   u32 stack[kStack];
   int sp = 0;
   u32 visits = 0;
-  stack[sp++] = 0;
+  stack[sp++] = root;
   while (sp > 0)
   {
     const u32 node = stack[--sp];
@@ -545,6 +560,8 @@ __global__ void __launch_bounds__(128) ray_first_collect_kernel(TreeView<T> tv, 
   const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq)
     return;
+  const u32 root = query_root(tv, q);
+  const u32 idBase = id_base(tv, root);
   RayD<T> ray;
   ray.make(rays + u64(q) * 6, rays + u64(q) * 6 + 3, tol, tolInc);
   if (!ray.valid)
@@ -553,7 +570,7 @@ __global__ void __launch_bounds__(128) ray_first_collect_kernel(TreeView<T> tv, 
   u32 stack[kStack];
   int sp = 0;
   u32 visits = 0;
-  stack[sp++] = 0;
+  stack[sp++] = root;
   while (sp > 0)
   {
     const u32 node = stack[--sp];
@@ -573,7 +590,7 @@ __global__ void __launch_bounds__(128) ray_first_collect_kernel(TreeView<T> tv, 
         continue;
       if (en > M)
         continue;
-      out.put(q, tv.ids[e], double(en));
+      out.put(q, (tv.ids[e] - idBase), double(en));
     }
     const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
     if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
@@ -1071,7 +1088,8 @@ static int empty_result(u64 nq, ResultState& r, bool dist, cudaStream_t st)
 }
 
 template<typename T>
-static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
+                      const u32* qTree)
 {
   DevBuf in;
   const void* d;
@@ -1080,7 +1098,7 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
   if (t.n == 0 || nq == 0)
     return empty_result(nq, r, false, st);
   Collected c;
-  auto tv = view<T>(t);
+  auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
   int rc = collect(
     c, false, nq * 32,
@@ -1094,7 +1112,7 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
 }
 
 template<typename T>
-static int pick_impl(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+static int pick_impl(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st, const u32* qTree)
 {
   DevBuf in;
   const void* d;
@@ -1103,7 +1121,7 @@ static int pick_impl(const TreeState& t, const void* pts, u64 nq, double tol, in
   if (t.n == 0 || nq == 0)
     return empty_result(nq, r, false, st);
   Collected c;
-  auto tv = view<T>(t);
+  auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
   int rc = collect(
     c, false, nq * 8,
@@ -1114,7 +1132,8 @@ static int pick_impl(const TreeState& t, const void* pts, u64 nq, double tol, in
 }
 
 template<typename T>
-static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
+                        const u32* qTree)
 {
   DevBuf in;
   const void* d;
@@ -1123,7 +1142,7 @@ static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, 
   if (t.n == 0 || nq == 0 || np == 0)
     return empty_result(nq, r, false, st);
   Collected c;
-  auto tv = view<T>(t);
+  auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
   int rc = collect(
     c, false, std::max<u64>(nq * 64, t.n / 4),
@@ -1138,7 +1157,7 @@ static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, 
 
 template<typename T>
 static int knn_impl(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAll, double maxDist, double tol, int algo, ResultState& r, int mem,
-                    cudaStream_t st)
+                    cudaStream_t st, const u32* qTree)
 {
   DevBuf in, kin, F;
   const void* d;
@@ -1150,11 +1169,11 @@ static int knn_impl(const TreeState& t, const void* pts, u64 nq, const u32* k, u
       return rc;
   if (t.n == 0 || nq == 0)
     return empty_result(nq, r, true, st);
-  if (algo != OTG_ALGO_PLAIN_FP64 && t.kind == OTG_KIND_POINTS)
+  if (algo != OTG_ALGO_PLAIN_FP64 && t.kind == OTG_KIND_POINTS && !qTree)
     return knn_filtered(const_cast<TreeState&>(t), d, (const u32*)dk, nq, kAll, maxDist, tol, r, st);
   if (cudaError_t e = F.ensure(sizeof(T) * nq))
     return cuda_status(e, "allocating kNN thresholds");
-  auto tv = view<T>(t);
+  auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
   T F0 = maxDist < 0 ? Lim<T>::max() : upper_tol_host(T(maxDist), tl);
   Collected c;
@@ -1172,7 +1191,7 @@ static int knn_impl(const TreeState& t, const void* pts, u64 nq, const u32* k, u
 
 template<typename T>
 static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, double tolInc, double maxDist, bool first, int algo, ResultState& r,
-                    int mem, cudaStream_t st)
+                    int mem, cudaStream_t st, const u32* qTree)
 {
   DevBuf in, M;
   const void* d;
@@ -1180,7 +1199,7 @@ static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, do
     return rc;
   if (t.n == 0 || nq == 0)
     return empty_result(nq, r, true, st);
-  auto tv = view<T>(t);
+  auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
   T ti = T(tolInc);
   T md = maxDist < 0 ? Lim<T>::max() : T(maxDist);
@@ -1285,32 +1304,81 @@ static int collide_impl(const TreeState& a, const TreeState& b, bool self, doubl
   return cuda_status(e, "finishing pairs");
 }
 
-int query_range(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+int query_range(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st, const u32* qTree)
 {
-  return t.scalar == OTG_SCALAR_F64 ? range_impl<double>(t, ranges, nq, mode, tol, algo, r, mem, st)
-                                    : range_impl<float>(t, ranges, nq, mode, tol, algo, r, mem, st);
+  return t.scalar == OTG_SCALAR_F64 ? range_impl<double>(t, ranges, nq, mode, tol, algo, r, mem, st, qTree)
+                                    : range_impl<float>(t, ranges, nq, mode, tol, algo, r, mem, st, qTree);
 }
-int query_pick(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+int query_pick(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st, const u32* qTree)
 {
-  return t.scalar == OTG_SCALAR_F64 ? pick_impl<double>(t, pts, nq, tol, algo, r, mem, st) : pick_impl<float>(t, pts, nq, tol, algo, r, mem, st);
+  return t.scalar == OTG_SCALAR_F64 ? pick_impl<double>(t, pts, nq, tol, algo, r, mem, st, qTree)
+                                    : pick_impl<float>(t, pts, nq, tol, algo, r, mem, st, qTree);
 }
 int query_knn(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAll, double maxDist, double tol, int algo, ResultState& r, int mem,
-              cudaStream_t st)
+              cudaStream_t st, const u32* qTree)
 {
-  return t.scalar == OTG_SCALAR_F64 ? knn_impl<double>(t, pts, nq, k, kAll, maxDist, tol, algo, r, mem, st)
-                                    : knn_impl<float>(t, pts, nq, k, kAll, maxDist, tol, algo, r, mem, st);
+  return t.scalar == OTG_SCALAR_F64 ? knn_impl<double>(t, pts, nq, k, kAll, maxDist, tol, algo, r, mem, st, qTree)
+                                    : knn_impl<float>(t, pts, nq, k, kAll, maxDist, tol, algo, r, mem, st, qTree);
 }
-int query_frustum(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+int query_frustum(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
+                  const u32* qTree)
 {
-  return t.scalar == OTG_SCALAR_F64 ? frustum_impl<double>(t, planes, np, nq, tol, algo, r, mem, st)
-                                    : frustum_impl<float>(t, planes, np, nq, tol, algo, r, mem, st);
+  return t.scalar == OTG_SCALAR_F64 ? frustum_impl<double>(t, planes, np, nq, tol, algo, r, mem, st, qTree)
+                                    : frustum_impl<float>(t, planes, np, nq, tol, algo, r, mem, st, qTree);
 }
 int query_ray(const TreeState& t, const void* rays, u64 nq, double tol, double tolInc, double maxDist, bool first, int algo, ResultState& r, int mem,
-              cudaStream_t st)
+              cudaStream_t st, const u32* qTree)
 {
-  return t.scalar == OTG_SCALAR_F64 ? ray_impl<double>(t, rays, nq, tol, tolInc, maxDist, first, algo, r, mem, st)
-                                    : ray_impl<float>(t, rays, nq, tol, tolInc, maxDist, first, algo, r, mem, st);
+  return t.scalar == OTG_SCALAR_F64 ? ray_impl<double>(t, rays, nq, tol, tolInc, maxDist, first, algo, r, mem, st, qTree)
+                                    : ray_impl<float>(t, rays, nq, tol, tolInc, maxDist, first, algo, r, mem, st, qTree);
 }
+
+// tree of each query of a forest: queries [qoff[t], qoff[t+1]) belong to tree t
+__global__ void query_tree_kernel(const u64* __restrict__ qoff, u32 trees, u64 nq, u32* __restrict__ qTree)
+{
+  for (u64 q = blockIdx.x * u64(blockDim.x) + threadIdx.x; q < nq; q += u64(gridDim.x) * blockDim.x)
+  {
+    u32 lo = 0, hi = trees;
+    while (hi - lo > 1)
+    {
+      const u32 m = (lo + hi) >> 1;
+      if (qoff[m] <= q)
+        lo = m;
+      else
+        hi = m;
+    }
+    qTree[q] = lo;
+  }
+}
+
+int forest_query_trees(const TreeState& t, const u64* qoffHost, DevBuf& qoffDev, DevBuf& qTree, u64& nq, cudaStream_t st)
+{
+  const u32 trees = t.trees;
+  if (!qoffHost || qoffHost[0] != 0)
+  {
+    set_error("query offsets must start at 0");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  for (u32 i = 0; i < trees; ++i)
+    if (qoffHost[i + 1] < qoffHost[i])
+    {
+      set_error("query offsets must not decrease");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+  nq = qoffHost[trees];
+  cudaError_t e;
+  if ((e = qoffDev.ensure(sizeof(u64) * (trees + 1))) || (e = qTree.ensure(sizeof(u32) * std::max<u64>(nq, 1))))
+    return cuda_status(e, "allocating query trees");
+  if ((e = cudaMemcpyAsync(qoffDev.p, qoffHost, sizeof(u64) * (trees + 1), cudaMemcpyHostToDevice, st)))
+    return cuda_status(e, "copying query offsets");
+  if (nq)
+    query_tree_kernel<<<blocks_for(nq), 256, 0, st>>>(qoffDev.as<u64>(), trees, nq, qTree.as<u32>());
+  // the host offsets may be released by the caller once the copy has run
+  if ((e = cudaStreamSynchronize(st)))
+    return cuda_status(e, "mapping queries to trees");
+  return OTG_OK;
+}
+
 int query_collide_self(const TreeState& t, double tol, int algo, ResultState& r, cudaStream_t st)
 {
   return t.scalar == OTG_SCALAR_F64 ? collide_impl<double>(t, t, true, tol, algo, r, st) : collide_impl<float>(t, t, true, tol, algo, r, st);

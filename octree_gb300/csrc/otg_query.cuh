@@ -24,7 +24,21 @@ struct TreeView
   u32 n;
   int isBox;
   u32 nNodes;
+  const u32* qTree;   // forest: tree (= root node) of each query; null for a single tree
+  const u64* treeOff; // forest: first entity of each tree (ids are returned relative to it)
 };
+
+// root node and id base of query q (node t is the root of tree t in a forest)
+template<typename T>
+__device__ __forceinline__ u32 query_root(const TreeView<T>& tv, u32 q)
+{
+  return tv.qTree ? tv.qTree[q] : 0u;
+}
+template<typename T>
+__device__ __forceinline__ u32 id_base(const TreeView<T>& tv, u32 root)
+{
+  return tv.qTree ? u32(tv.treeOff[root]) : 0u;
+}
 
 struct Appender
 {
@@ -142,11 +156,12 @@ static inline int sort_pairs_u32(u32* keys, u32* vals, u64 m, u32 bits, cudaStre
   return cuda_status(cudaGetLastError(), "sorting results");
 }
 
+// qTree: the tree of each query when t is a forest (null for a single tree)
 template<typename T>
-static inline TreeView<T> view(const TreeState& t)
+static inline TreeView<T> view(const TreeState& t, const u32* qTree = nullptr)
 {
   return TreeView<T>{ t.nodeLink.as<uint4>(), t.nodeBox.as<T>(), t.nodeMax.as<T>(), t.sortedIds.as<u32>(), t.sortedGeom.as<T>(), u32(t.n),
-                      t.kind == OTG_KIND_BOXES ? 1 : 0, u32(t.nodeCount) };
+                      t.kind == OTG_KIND_BOXES ? 1 : 0, u32(t.nodeCount), qTree, qTree ? t.treeOff.as<u64>() : nullptr };
 }
 
 template<typename T>

@@ -199,66 +199,55 @@ struct RasterLayout
   static __host__ __device__ size_t bytes(u32 cells) { return sizeof(U) * 3 * per_dim(cells); }
 };
 
-// One thread per (dimension, threshold index). isBox selects the box variants.
+// Threshold j of dimension d (layout above) for the space s. isBox selects the box variants.
+template<typename T, typename R>
+__device__ typename Ord<T>::U raster_threshold(const Space<T>& s, int d, u32 j, u32 cells, int isBox)
+{
+  using O = Ord<T>;
+  const u32 D = s.D;
+  const u32 maxRasterID = (1u << D) - 1u;
+  const T dr = T(Raster<R, T>::derast(s, d));
+  if (j == 0)
+  {
+    if (isBox) // DoesRangeContainBox lower bound: !(rmin - tol > b)  <=>  b >= rmin - tol
+      return O::of(T(s.min[d] - base_tol<T>()));
+    return first_true<T>([&](T x) { return !point_below_ref<T, R>(x, s, d); }, s.min[d]);
+  }
+  if (j == 1)
+  {
+    if (isBox) // !(b > rmax + tol)
+      return O::of(T(s.max[d] + base_tol<T>()));
+    typename O::U a = first_true<T>([&](T x) { return point_above_ref<T, R>(x, s, d); }, s.max[d]);
+    return a == O::kNever ? O::of(Lim<T>::max()) + 1 : a - 1;
+  }
+  if (j < 2 + kLevelThresholds)
+  {
+    // level >= L  <=>  R(size) * factor > 2^(L - 1)
+    const u32 L = j - 2;
+    if (L == 0)
+      return 0;
+    const R lim = R(u64(1) << (L - 1));
+    return first_true<T>([&](T size) { return rel_size_ref<T, R>(size, s, d) > lim; }, T(lim) * dr);
+  }
+  const u32 g = j - 2 - kLevelThresholds;
+  if (g == 0)
+    return 0;
+  if (isBox)
+    return first_true<T>([&](T c) { return center_cell_ref<T, R>(c, s, d) >= g; }, T(s.min[d] + T(g) * dr));
+  if (g > maxRasterID)
+    return O::kNever;
+  return first_true<T>([&](T x) { return point_cell_ref<T, R>(x, s, d, maxRasterID) >= g; }, T(s.min[d] + T(g) * dr));
+}
+
+// One thread per (dimension, threshold index).
 template<typename T, typename R>
 __global__ void raster_tables_kernel(const Space<T>* __restrict__ spg, typename Ord<T>::U* __restrict__ tab, u32 cells, int isBox)
 {
-  using O = Ord<T>;
-  using U = typename O::U;
   const Space<T>& s = *spg;
-  const u32 D = s.D;
-  const u32 maxRasterID = (1u << D) - 1u;
   const size_t perDim = RasterLayout<T>::per_dim(cells);
   const u64 total = 3 * perDim;
   for (u64 idx = blockIdx.x * u64(blockDim.x) + threadIdx.x; idx < total; idx += u64(gridDim.x) * blockDim.x)
-  {
-    const int d = int(idx / perDim);
-    const u32 j = u32(idx % perDim);
-    U out;
-    const T dr = T(Raster<R, T>::derast(s, d));
-    if (j == 0)
-    {
-      if (isBox) // DoesRangeContainBox lower bound: !(rmin - tol > b)  <=>  b >= rmin - tol
-        out = O::of(T(s.min[d] - base_tol<T>()));
-      else
-        out = first_true<T>([&](T x) { return !point_below_ref<T, R>(x, s, d); }, s.min[d]);
-    }
-    else if (j == 1)
-    {
-      if (isBox) // !(b > rmax + tol)
-        out = O::of(T(s.max[d] + base_tol<T>()));
-      else
-      {
-        U a = first_true<T>([&](T x) { return point_above_ref<T, R>(x, s, d); }, s.max[d]);
-        out = a == O::kNever ? O::of(Lim<T>::max()) + 1 : a - 1;
-      }
-    }
-    else if (j < 2 + kLevelThresholds)
-    {
-      // level >= L  <=>  R(size) * factor > 2^(L - 1)
-      const u32 L = j - 2;
-      if (L == 0)
-        out = 0;
-      else
-      {
-        const R lim = R(u64(1) << (L - 1));
-        out = first_true<T>([&](T size) { return rel_size_ref<T, R>(size, s, d) > lim; }, T(lim) * dr);
-      }
-    }
-    else
-    {
-      const u32 g = j - 2 - kLevelThresholds;
-      if (g == 0)
-        out = 0;
-      else if (isBox)
-        out = first_true<T>([&](T c) { return center_cell_ref<T, R>(c, s, d) >= g; }, T(s.min[d] + T(g) * dr));
-      else if (g > maxRasterID)
-        out = O::kNever;
-      else
-        out = first_true<T>([&](T x) { return point_cell_ref<T, R>(x, s, d, maxRasterID) >= g; }, T(s.min[d] + T(g) * dr));
-    }
-    tab[idx] = out;
-  }
+    tab[idx] = raster_threshold<T, R>(s, int(idx / perDim), u32(idx % perDim), cells, isBox);
 }
 
 // number of thresholds <= o, minus one (the cell), searching around an estimate
@@ -298,22 +287,23 @@ __device__ __forceinline__ u32 cell_from_table(const U* __restrict__ thr, u32 ce
 // MinPoint node table: minTab[d][(2^depth - 1) + cell] for depth 0..D (si_grid.h:124-143 and
 // ot_dynamic_hash_core.h:563-572): T((R(cell << (D - depth)) + halfGrid) * derast) + min - nodeSize[depth + 1]
 template<typename T, typename R>
+__device__ __forceinline__ T node_min_entry(const Space<T>& s, int d, u64 j)
+{
+  const u32 depth = u32(63 - __clzll((long long)(j + 1)));
+  const u64 cell = (j + 1) - (u64(1) << depth);
+  const u32 lvl = s.D - depth;
+  const R halfGrid = R(u64(1) << lvl) * R(0.5);
+  const T c = T((R(u32(cell << lvl)) + halfGrid) * Raster<R, T>::derast(s, d)) + s.min[d];
+  return c - s.nodeSize[depth + 1][d];
+}
+
+template<typename T, typename R>
 __global__ void node_min_table_kernel(const Space<T>* __restrict__ spg, T* __restrict__ tab)
 {
   const Space<T>& s = *spg;
-  const u32 D = s.D;
-  const u64 perDim = (u64(2) << D) - 1;
+  const u64 perDim = (u64(2) << s.D) - 1;
   for (u64 idx = blockIdx.x * u64(blockDim.x) + threadIdx.x; idx < 3 * perDim; idx += u64(gridDim.x) * blockDim.x)
-  {
-    const int d = int(idx / perDim);
-    const u64 j = idx % perDim;
-    const u32 depth = u32(63 - __clzll((long long)(j + 1)));
-    const u64 cell = (j + 1) - (u64(1) << depth);
-    const u32 lvl = D - depth;
-    const R halfGrid = R(u64(1) << lvl) * R(0.5);
-    const T c = T((R(u32(cell << lvl)) + halfGrid) * Raster<R, T>::derast(s, d)) + s.min[d];
-    tab[idx] = c - s.nodeSize[depth + 1][d];
-  }
+    tab[idx] = node_min_entry<T, R>(s, int(idx / perDim), idx % perDim);
 }
 
 } // namespace otg

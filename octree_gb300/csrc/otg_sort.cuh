@@ -5,9 +5,9 @@
 // sort is unstable, this one is stable, so equal keys keep ascending entity id).
 //
 // Per pass, every CTA takes the next tile id from a counter (so tiles start in launch order),
-// ranks its 4096 keys by digit with warp match-any, publishes its per-digit counts and looks back
-// over earlier tiles' published counts (decoupled look-back) to get its global offsets, stages the
-// tile in shared memory in digit order and writes it out in runs. Look-back spins are bounded:
+// counts its 4096 keys per digit and publishes the counts, ranks the keys stably with warp
+// ballots, looks back over earlier tiles' published counts (decoupled look-back) to get its global
+// offsets, stages the tile in shared memory in digit order and writes it out in runs. Look-back spins are bounded:
 // on timeout the CTA sets an error bit and finishes, so a broken invariant can never hang the GPU.
 #pragma once
 
@@ -97,16 +97,26 @@ __global__ void __launch_bounds__(256) radix_histogram_kernel(const K* __restric
 }
 
 // One onesweep pass. vin == nullptr means values are the input positions (iota).
-template<typename K>
+// Order of work in a tile: per-warp digit counts (shared-memory atomics without return values),
+// publication of the tile's counts as an aggregate right away, then the ranking, and only then
+// the look-back: predecessors have had the ranking's duration to publish their inclusive prefixes.
+// Ranking is stable: a warp finds the lanes sharing its digit with eight ballots (one per digit
+// bit), the group leader advances the warp's position cursor for that digit with one shared
+// atomic, and each lane adds its rank among lower lanes.
+// Segmented form (segTiles != null): independent sorts of the segments [segOff[s], segOff[s+1])
+// in one launch. Tile i covers tile segTiles[i].y of segment segTiles[i].x (the tiles of a segment
+// are consecutive, in order), the look-back stops at the segment's first tile, and hist holds
+// 256 digit counts per segment. Positions are below 2^30, so they are kept in 32 bits.
+template<typename K, bool SEG = false>
 __global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass_kernel(const K* __restrict__ kin, const u32* __restrict__ vin, K* __restrict__ kout,
                                                                      u32* __restrict__ vout, u32 n, u32 shift, const u32* __restrict__ hist,
-                                                                     u32* __restrict__ status, u32* __restrict__ tileCounter, u32* __restrict__ err)
+                                                                     u32* __restrict__ status, u32* __restrict__ tileCounter, u32* __restrict__ err,
+                                                                     const uint2* __restrict__ segTiles = nullptr, const u64* __restrict__ segOff = nullptr)
 {
   extern __shared__ __align__(16) unsigned char s_dyn[];
   K* s_keys = reinterpret_cast<K*>(s_dyn);
   u32* s_vals = reinterpret_cast<u32*>(s_dyn + sizeof(K) * kSortTile);
-  __shared__ u32 s_warpHist[kSortWarps][kRadix];
-  __shared__ u32 s_digitStart[kRadix];
+  __shared__ u32 s_cnt[kSortWarps][kRadix]; // warp digit counts, then tile-local position cursors
   __shared__ u32 s_globalBase[kRadix];
   __shared__ u32 s_scan[kSortWarps];
   __shared__ u32 s_tile;
@@ -115,170 +125,156 @@ __global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass_kernel(const K*
   if (tid == 0)
     s_tile = atomicAdd(tileCounter, 1u);
   for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads)
-    (&s_warpHist[0][0])[i] = 0;
+    (&s_cnt[0][0])[i] = 0;
   __syncthreads();
   const u32 tile = s_tile;
-  const u64 base = u64(tile) * kSortTile;
+  // segment of this tile: [segBase, segEnd), its digit counts, its first tile
+  u32 segBase = 0, segEnd = n, tileInSeg = tile;
+  if constexpr (SEG)
+  {
+    const uint2 st = segTiles[tile];
+    segBase = u32(segOff[st.x]);
+    segEnd = u32(segOff[st.x + 1]);
+    tileInSeg = st.y;
+    hist += u64(st.x) * kRadix;
+  }
+  const u32 base = segBase + tileInSeg * u32(kSortTile);
+  const u32 firstTile = tile - tileInSeg;
 
   K keys[kSortItems];
   u32 vals[kSortItems];
-  u32 rank[kSortItems];
   u32 dig[kSortItems];
-  const u64 wbase = base + u64(warp) * (32 * kSortItems);
+  const u32 wbase = base + u32(warp) * (32 * kSortItems);
 #pragma unroll
   for (int i = 0; i < kSortItems; ++i)
   {
-    u64 idx = wbase + i * 32 + lane;
-    bool valid = idx < n;
+    const u32 idx = wbase + i * 32 + lane;
+    const bool valid = idx < segEnd;
     keys[i] = valid ? kin[idx] : K(0);
-    vals[i] = vin ? (valid ? vin[idx] : 0u) : u32(idx);
+    vals[i] = vin ? (valid ? vin[idx] : 0u) : idx;
     dig[i] = valid ? u32((keys[i] >> shift) & (kRadix - 1)) : u32(kRadix);
   }
-  // rank within the warp: lanes with equal digits elect a leader whose shared atomic returns the
-  // count of that digit in earlier items (atomics of one warp to one address apply in issue order),
-  // so the items pipeline instead of forming a load/store chain
-  const u32 ltmask = lanemask_lt();
 #pragma unroll
   for (int i = 0; i < kSortItems; ++i)
-  {
-    const u32 d = dig[i];
-    const u32 peers = __match_any_sync(0xffffffffu, d);
-    const int leader = __ffs(peers) - 1;
-    u32 old = 0;
-    if (d < kRadix && lane == leader)
-      old = atomicAdd(&s_warpHist[warp][d], u32(__popc(peers)));
-    old = __shfl_sync(0xffffffffu, old, leader);
-    rank[i] = old + __popc(peers & ltmask);
-  }
+    if (dig[i] < kRadix)
+      atomicAdd(&s_cnt[warp][dig[i]], 1u);
   __syncthreads();
 
-  // per digit (thread tid < 256 owns digit tid): warp offsets and the tile total
+  // per digit (thread tid < 256 owns digit tid): warp offsets, the tile total, early publication
   u32 total = 0;
-  u32 prefix = 0;
+  volatile u32* vstatus = status;
   if (tid < kRadix)
   {
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w)
     {
-      u32 c = s_warpHist[w][tid];
-      s_warpHist[w][tid] = total;
+      u32 c = s_cnt[w][tid];
+      s_cnt[w][tid] = total;
       total += c;
     }
-    // decoupled look-back over earlier tiles for digit tid, eight predecessors per round trip
-    volatile u32* vstatus = status;
-    if (tile == 0)
-    {
-      vstatus[tid] = kStatusInclusive | total;
-    }
-    else
-    {
-      vstatus[u64(tile) * kRadix + tid] = kStatusAggregate | total;
-      long long j = (long long)tile - 1;
-      u32 spins = 0;
-      while (j >= 0)
-      {
-        u32 sv[kLookbackBatch];
-#pragma unroll
-        for (int k = 0; k < kLookbackBatch; ++k)
-          sv[k] = (j - k >= 0) ? vstatus[u64(j - k) * kRadix + tid] : u32(kStatusInclusive);
-        int used = 0;
-        bool done = false;
-#pragma unroll
-        for (int k = 0; k < kLookbackBatch; ++k)
-        {
-          if (done || used < k)
-            continue;
-          const u32 flag = sv[k] & ~kStatusValueMask;
-          if (flag == 0)
-            continue; // not published yet: re-read from here
-          prefix += sv[k] & kStatusValueMask;
-          used = k + 1;
-          done = flag == kStatusInclusive;
-        }
-        if (done)
-          break;
-        j -= used;
-        if (used < kLookbackBatch)
-        {
-          if (++spins > kLookbackSpinLimit)
-          {
-            atomicOr(err, kErrTimeout);
-            break;
-          }
-          __nanosleep(32);
-        }
-      }
-      vstatus[u64(tile) * kRadix + tid] = kStatusInclusive | ((prefix + total) & kStatusValueMask);
-    }
+    vstatus[u64(tile) * kRadix + tid] = (tileInSeg == 0 ? kStatusInclusive : kStatusAggregate) | total;
   }
-
   u32 tileTotal;
-  u32 digitStart = block_exclusive_scan(total, s_scan, tileTotal);
-  u32 hcount = tid < kRadix ? hist[tid] : 0u;
-  u32 hsum;
-  u32 histPrefix = block_exclusive_scan(hcount, s_scan, hsum);
+  const u32 digitStart = block_exclusive_scan(total, s_scan, tileTotal);
   if (tid < kRadix)
   {
-    s_digitStart[tid] = digitStart;
-    s_globalBase[tid] = histPrefix + prefix - digitStart;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w)
+      s_cnt[w][tid] += digitStart;
   }
   __syncthreads();
 
+  const u32 ltmask = lanemask_lt();
+  u32 pos[kSortItems];
 #pragma unroll
   for (int i = 0; i < kSortItems; ++i)
   {
-    u32 d = dig[i];
-    if (d < kRadix)
+    const u32 d = dig[i];
+    u32 peers = __ballot_sync(0xffffffffu, d < kRadix);
+#pragma unroll
+    for (int b = 0; b < kRadixBits; ++b)
     {
-      u32 pos = s_digitStart[d] + s_warpHist[warp][d] + rank[i];
-      s_keys[pos] = keys[i];
-      s_vals[pos] = vals[i];
+      const u32 bal = __ballot_sync(0xffffffffu, (d >> b) & 1u);
+      peers &= ((d >> b) & 1u) ? bal : ~bal;
     }
+    if (d >= kRadix)
+      peers = 1u << lane;
+    const int leader = __ffs(peers) - 1;
+    u32 old = 0;
+    if (d < kRadix && lane == leader)
+      old = atomicAdd(&s_cnt[warp][d], u32(__popc(peers)));
+    old = __shfl_sync(0xffffffffu, old, leader);
+    pos[i] = old + __popc(peers & ltmask);
   }
+
+  // decoupled look-back over earlier tiles of the segment for digit tid, eight predecessors per round trip
+  u32 prefix = 0;
+  if (tid < kRadix && tileInSeg > 0)
+  {
+    long long j = (long long)tile - 1;
+    u32 spins = 0;
+    while (j >= (long long)firstTile)
+    {
+      u32 sv[kLookbackBatch];
+#pragma unroll
+      for (int k = 0; k < kLookbackBatch; ++k)
+        sv[k] = (j - k >= (long long)firstTile) ? vstatus[u64(j - k) * kRadix + tid] : u32(kStatusInclusive);
+      int used = 0;
+      bool done = false;
+#pragma unroll
+      for (int k = 0; k < kLookbackBatch; ++k)
+      {
+        if (done || used < k)
+          continue;
+        const u32 flag = sv[k] & ~kStatusValueMask;
+        if (flag == 0)
+          continue; // not published yet: re-read from here
+        prefix += sv[k] & kStatusValueMask;
+        used = k + 1;
+        done = flag == kStatusInclusive;
+      }
+      if (done)
+        break;
+      j -= used;
+      if (used < kLookbackBatch)
+      {
+        if (++spins > kLookbackSpinLimit)
+        {
+          atomicOr(err, kErrTimeout);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    vstatus[u64(tile) * kRadix + tid] = kStatusInclusive | ((prefix + total) & kStatusValueMask);
+  }
+  u32 hcount = tid < kRadix ? hist[tid] : 0u;
+  u32 hsum;
+  const u32 histPrefix = block_exclusive_scan(hcount, s_scan, hsum); // its barriers also end the ranking
+  if (tid < kRadix)
+    s_globalBase[tid] = segBase + histPrefix + prefix - digitStart;
+#pragma unroll
+  for (int i = 0; i < kSortItems; ++i)
+    if (dig[i] < kRadix)
+    {
+      const u32 p = pos[i] & (kSortTile - 1); // ranks of a tile are below kSortTile by construction
+      s_keys[p] = keys[i];
+      s_vals[p] = vals[i];
+    }
   __syncthreads();
 
-  const u32 tileCount = u32(min(u64(kSortTile), u64(n) - base));
-  if (tileCount == kSortTile)
+  const u32 tileCount = min(u32(kSortTile), segEnd - base);
+  for (u32 j = tid; j < tileCount; j += kSortThreads)
   {
-    K kk[kSortItems];
-    u32 vv[kSortItems], pp[kSortItems];
-#pragma unroll
-    for (int k = 0; k < kSortItems; ++k)
+    const K k = s_keys[j];
+    const u32 p = s_globalBase[u32((k >> shift) & (kRadix - 1))] + j;
+    if (p - segBase < segEnd - segBase)
     {
-      const u32 j = tid + k * kSortThreads;
-      kk[k] = s_keys[j];
-      vv[k] = s_vals[j];
+      kout[p] = k;
+      vout[p] = s_vals[j];
     }
-#pragma unroll
-    for (int k = 0; k < kSortItems; ++k)
-      pp[k] = s_globalBase[u32((kk[k] >> shift) & (kRadix - 1))] + tid + k * kSortThreads;
-#pragma unroll
-    for (int k = 0; k < kSortItems; ++k)
-    {
-      if (pp[k] < n)
-      {
-        kout[pp[k]] = kk[k];
-        vout[pp[k]] = vv[k];
-      }
-      else
-        atomicOr(err, kErrTimeout);
-    }
-  }
-  else
-  {
-    for (u32 j = tid; j < tileCount; j += kSortThreads)
-    {
-      K k = s_keys[j];
-      u32 d = u32((k >> shift) & (kRadix - 1));
-      u32 pos = s_globalBase[d] + j;
-      if (pos < n)
-      {
-        kout[pos] = k;
-        vout[pos] = s_vals[j];
-      }
-      else
-        atomicOr(err, kErrTimeout);
-    }
+    else
+      atomicOr(err, kErrTimeout);
   }
 }
 
@@ -324,6 +320,27 @@ inline bool onesweep_passes(K* k0, u32* v0, K* k1, u32* v1, u64 n, u32 shift0, u
     u32* vo = even ? v1 : v0;
     onesweep_pass_kernel<K><<<tiles, kSortThreads, onesweep_smem_bytes<K>(), st>>>(ki, vi, ko, vo, u32(n), shift0 + kRadixBits * p, s.hist + p * kRadix,
                                                                                s.status + size_t(p) * tiles * kRadix, s.tileCounters + p, err);
+  }
+  return (passes % 2) == 1;
+}
+
+// Segmented passes: `tiles` tiles listed in segTiles; hist holds [pass][segment][256] counts.
+template<typename K>
+inline bool onesweep_passes_segmented(K* k0, u32* v0, K* k1, u32* v1, u64 n, u32 passes, bool iotaValues, const uint2* segTiles, u32 tiles,
+                                      const u64* segOff, u32 segments, const u32* hist, u32* status, u32* counters, u32* err, cudaStream_t st)
+{
+  cudaFuncSetAttribute(onesweep_pass_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(onesweep_smem_bytes<K>()));
+  for (u32 p = 0; p < passes; ++p)
+  {
+    const bool even = (p % 2) == 0;
+    const K* ki = even ? k0 : k1;
+    const u32* vi = (p == 0 && iotaValues) ? nullptr : (even ? v0 : v1);
+    K* ko = even ? k1 : k0;
+    u32* vo = even ? v1 : v0;
+    if (tiles)
+      onesweep_pass_kernel<K, true><<<tiles, kSortThreads, onesweep_smem_bytes<K>(), st>>>(ki, vi, ko, vo, u32(n), kRadixBits * p,
+                                                                                   hist + u64(p) * segments * kRadix, status + size_t(p) * tiles * kRadix,
+                                                                                   counters + p, err, segTiles, segOff);
   }
   return (passes % 2) == 1;
 }
