@@ -334,6 +334,7 @@ def run_gpu(args):
         }
     if not args.no_queries:
         line["queries"] = run_queries(tree, pts_d, stream)
+        line["many_trees"] = run_many_trees()
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -436,6 +437,121 @@ def run_queries(tree16, pts16_d, stream):
     out["collide_self_4M_pair_lists_equal"] = bool(np.array_equal(pair_lists["plain_fp64"], pair_lists["filtered_fp32"]))
     out["collide_self_4M_speedup_filtered_vs_plain"] = out["collide_self_4M_plain_fp64_ms"] / out["collide_self_4M_filtered_fp32_ms"]
     return out
+
+
+def many_trees(trees, seed):
+    """Many small box trees: sizes lognormal(ln 8000, 1.2) clipped to [1000, 200000]; boxes with
+    centres uniform in [0,100)^3 and half-extents uniform in [0.05, 1], drawn in FP64 and stored as
+    FP32. Per tree 256 range boxes (centres uniform, edges uniform in [0.5, 5]), 256 rays (origins
+    uniform, directions uniform on the sphere, unbounded) and one frustum of 6 axis-aligned planes."""
+    rng = np.random.default_rng(seed)
+    sizes = np.clip(rng.lognormal(np.log(8000), 1.2, trees), 1000, 200000).astype(np.int64)
+    n = int(sizes.sum())
+    c = rng.random((n, 3)) * 100
+    e = rng.uniform(0.05, 1.0, (n, 3))
+    boxes = np.empty((n, 6), np.float32)
+    boxes[:, :3] = c - e
+    boxes[:, 3:] = c + e
+    del c, e
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    qrng = np.random.default_rng(seed + 1)
+    nq = trees * 256
+    qc = qrng.random((nq, 3)) * 100
+    qe = qrng.uniform(0.5, 5, (nq, 3))
+    ranges = np.concatenate([qc - qe / 2, qc + qe / 2], 1).astype(np.float32)
+    d = qrng.normal(size=(nq, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([qrng.random((nq, 3)) * 100, d], 1).astype(np.float32)
+    planes = np.zeros((trees, 6, 4), np.float32)
+    lo, hi = qrng.random((trees, 3)) * 40, 60 + qrng.random((trees, 3)) * 40
+    for a in range(3):
+        planes[:, 2 * a, 0], planes[:, 2 * a, 1 + a] = lo[:, a], 1.0
+        planes[:, 2 * a + 1, 0], planes[:, 2 * a + 1, 1 + a] = -hi[:, a], -1.0
+    return boxes, off, ranges, rays, planes
+
+
+def run_many_trees(trees=4096, sample=48):
+    """The many-small-trees workload: one forest (one build + three batched query launches for all
+    trees) against per-tree Create + queries with the one-query-per-thread kernels, on a sample."""
+    import torch
+
+    import octree_gb300 as otg
+
+    boxes, off, ranges, rays, planes = many_trees(trees, 401)
+    qoff = np.arange(trees + 1, dtype=np.uint64) * 256
+    foff = np.arange(trees + 1, dtype=np.uint64)
+    d_boxes = torch.as_tensor(boxes, device="cuda")
+    d_ranges = torch.as_tensor(ranges, device="cuda")
+    d_rays = torch.as_tensor(rays, device="cuda")
+    d_planes = torch.as_tensor(planes, device="cuda")
+    f = otg.Forest("boxes", np.float32)
+
+    def forest_step():
+        f.create(d_boxes, off, max_elements=16)
+        a = f.range_search(d_ranges, qoff, raw=True)
+        b = f.ray_all(d_rays, qoff, raw=True)
+        c = f.frustum_culling(d_planes, foff, raw=True)
+        return a, b, c
+
+    forest_step()
+    torch.cuda.synchronize()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        res = forest_step()
+    torch.cuda.synchronize()
+    step_s = (time.perf_counter() - t0) / reps
+    # phases of one step
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    f.create(d_boxes, off, max_elements=16)
+    f.sync()
+    t1 = time.perf_counter()
+    f.range_search(d_ranges, qoff, raw=True)
+    t2 = time.perf_counter()
+    f.ray_all(d_rays, qoff, raw=True)
+    t3 = time.perf_counter()
+    f.frustum_culling(d_planes, foff, raw=True)
+    t4 = time.perf_counter()
+    n_ids = [r.sizes()[1] for r in res]
+    # per-tree plain launches on a sample of trees
+    host = [r.to_host() for r in res]
+    idx = np.random.default_rng(7).choice(trees, sample, replace=False)
+    mism = 0
+    t_plain = 0.0
+    for t in idx:
+        a, b = int(off[t]), int(off[t + 1])
+        q = slice(t * 256, (t + 1) * 256)
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        tr = otg.Tree("boxes", np.float32).create(d_boxes[a:b], max_elements=16)
+        ra = tr.range_search(d_ranges[q], algo=otg.ALGO_PLAIN_FP64)
+        rb = tr.ray_all(d_rays[q], algo=otg.ALGO_PLAIN_FP64)
+        rc = tr.frustum_culling(d_planes[t : t + 1], algo=otg.ALGO_PLAIN_FP64)
+        torch.cuda.synchronize()
+        t_plain += time.perf_counter() - s0
+        for got, (fo, fi, fd), nper, qi in ((ra, host[0], 256, t * 256), (rb, host[1], 256, t * 256), (rc, host[2], 1, t)):
+            o0, o1 = int(fo[qi]), int(fo[qi + nper])
+            same = np.array_equal(got[1], fi[o0:o1]) and np.array_equal(np.diff(got[0].astype(np.int64)), np.diff(fo[qi : qi + nper + 1].astype(np.int64)))
+            mism += 0 if same else 1
+    per_tree_s = t_plain / sample
+    return {
+        "trees": trees,
+        "entities": int(off[-1]),
+        "queries_per_step": int(2 * trees * 256 + trees),
+        "forest_step_ms": step_s * 1e3,
+        "forest_trees_per_s": trees / step_s,
+        "forest_queries_per_s_M": (2 * trees * 256 + trees) / step_s / 1e6,
+        "forest_build_ms": (t1 - t0) * 1e3,
+        "forest_range_ms": (t2 - t1) * 1e3,
+        "forest_ray_all_ms": (t3 - t2) * 1e3,
+        "forest_frustum_ms": (t4 - t3) * 1e3,
+        "result_ids": {"range": int(n_ids[0]), "ray_all": int(n_ids[1]), "frustum": int(n_ids[2])},
+        "per_tree_plain_trees_per_s": 1.0 / per_tree_s,
+        "per_tree_plain_sample_trees": int(sample),
+        "speedup_forest_vs_per_tree": (1.0 / per_tree_s) and (trees / step_s) / (1.0 / per_tree_s),
+        "mismatched_query_groups_in_sample": int(mism),
+    }
 
 
 PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m")

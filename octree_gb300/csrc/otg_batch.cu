@@ -1,0 +1,340 @@
+// otg_batch.cu — batched RangeSearch, FrustumCulling and RayIntersectedAll: persistent kernels in
+// which each warp takes the next query from a shared counter (queries of uneven cost balance out,
+// in one tree or across the trees of a forest) and answers it cooperatively:
+//   * the node's own entities are tested by the 32 lanes in parallel (coalesced reads of the
+//     tree-ordered geometry), hits compacted with a ballot into a per-warp shared buffer that is
+//     flushed to the result with one atomic per flush;
+//   * the node's children are tested by one lane each before they are pushed, so the depth-first
+//     stack (in shared memory) only ever holds nodes the query enters.
+// Every node and entity test is the reference predicate in the tree's scalar type, applied to the
+// same nodes as the one-query-per-thread kernels of otg_query.cu, so the id sets are identical:
+//   RangeSearch         core/ot_query.h:476-583
+//   FrustumCulling      core/ot_query.h:767-833
+//   RayIntersectedAll   core/ot_query.h:1928-2022
+#include "otg_query.cuh"
+
+namespace otg
+{
+
+constexpr int kBatchWarps = 4;
+constexpr u32 kItemBuf = 128;
+constexpr u32 kContained = 1u << 31; // stack entry flag: the range contains the node (emit its subtree)
+
+struct WarpSink
+{
+  u64* items;
+  double* dist;
+  u32 n;
+};
+
+// flushes the warp's buffered results to the appender (all lanes)
+__device__ __forceinline__ void sink_flush(WarpSink& s, Appender& out, u32 lane)
+{
+  if (s.n == 0)
+    return;
+  unsigned long long base = 0;
+  if (lane == 0)
+    base = out.reserve(s.n);
+  base = __shfl_sync(~0u, base, 0);
+  for (u32 t = lane; t < s.n; t += 32)
+    if (base + t < out.capacity)
+    {
+      out.items[base + t] = s.items[t];
+      if (out.dist)
+        out.dist[base + t] = s.dist[t];
+    }
+  __syncwarp();
+  s.n = 0;
+}
+
+// appends the lanes with hit set (all lanes call)
+__device__ __forceinline__ void sink_put(WarpSink& s, Appender& out, u32 lane, bool hit, u32 q, u32 id, double d)
+{
+  const u32 bal = __ballot_sync(~0u, hit);
+  if (!bal)
+    return;
+  if (s.n + 32 > kItemBuf)
+    sink_flush(s, out, lane);
+  if (hit)
+  {
+    const u32 slot = s.n + __popc(bal & ((1u << lane) - 1));
+    s.items[slot] = (u64(q) << 32) | id;
+    if (out.dist)
+      s.dist[slot] = d;
+  }
+  s.n += __popc(bal);
+  __syncwarp();
+}
+
+// query kinds
+constexpr int kRange = 0, kFrustum = 1, kRayAll = 2;
+
+template<typename T, int KIND>
+struct BatchArgs
+{
+  TreeView<T> tv;
+  const T* q;   // ranges (6 per query), planes (4 * np per query) or rays (6 per query)
+  u32 np;       // planes per query
+  u32 nq;
+  int mode;     // RangeSearchMode
+  T tol, tolInc, maxDist;
+  Appender out;
+  u32* work;
+  u32* err;
+};
+
+template<typename T, int KIND>
+__global__ void __launch_bounds__(kBatchWarps * 32) batch_query_kernel(BatchArgs<T, KIND> a)
+{
+  using G = GeoD<T>;
+  __shared__ u32 stackMem[kBatchWarps][kStack];
+  __shared__ u64 itemMem[kBatchWarps][kItemBuf];
+  __shared__ double distMem[KIND == kRayAll ? kBatchWarps : 1][KIND == kRayAll ? kItemBuf : 1];
+  const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  u32* stack = stackMem[w];
+  WarpSink sink{ itemMem[w], KIND == kRayAll ? distMem[w] : nullptr, 0 };
+  const TreeView<T>& tv = a.tv;
+  for (;;)
+  {
+    u32 q = 0;
+    if (lane == 0)
+      q = atomicAdd(a.work, 1u);
+    q = __shfl_sync(~0u, q, 0);
+    if (q >= a.nq)
+      break;
+    const u32 root = query_root(tv, q);
+    const u32 idBase = id_base(tv, root);
+    // ---- query setup (identical on all lanes)
+    T r[6], rsize[3];
+    const T* pl = nullptr;
+    RayD<T> ray;
+    bool skip = false;
+    if constexpr (KIND == kRange)
+    {
+      load_box(a.q + u64(q) * 6, r);
+      T rb[6];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+      {
+        rb[c] = tv.nodeBox[u64(root) * 6 + c];
+        rb[3 + c] = tv.nodeBox[u64(root) * 6 + c] + tv.nodeBox[u64(root) * 6 + 3 + c];
+      }
+      if (G::range_contains_box(r, rb, a.tol)) // root shortcut (:488-511): every id of the tree
+      {
+        const u32 nt = tv.qTree ? u32(tv.treeOff[root + 1] - tv.treeOff[root]) : tv.n;
+        unsigned long long base = 0;
+        if (lane == 0)
+          base = a.out.reserve(nt);
+        base = __shfl_sync(~0u, base, 0);
+        for (u32 i = lane; i < nt; i += 32)
+          if (base + i < a.out.capacity)
+            a.out.items[base + i] = (u64(q) << 32) | i;
+        continue;
+      }
+      T vol = T(1); // zero-volume range -> empty (:514-519)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+      {
+        rsize[c] = T(r[3 + c] - r[c]);
+        vol *= rsize[c];
+      }
+      skip = vol <= T(0);
+    }
+    else if constexpr (KIND == kFrustum)
+    {
+      pl = a.q + u64(q) * a.np * 4;
+      skip = a.np == 0;
+    }
+    else
+    {
+      ray.make(a.q + u64(q) * 6, a.q + u64(q) * 6 + 3, a.tol, a.tolInc);
+      skip = !ray.valid;
+    }
+    if (skip)
+      continue;
+    // ---- node test of one node (run by one lane per child)
+    auto enters = [&](u32 node, bool& contained) -> bool {
+      const T* nb = tv.nodeBox + u64(node) * 6;
+      contained = false;
+      if constexpr (KIND == kRange)
+      {
+        T nmin[3] = { nb[0], nb[1], nb[2] }, nsize[3] = { nb[3], nb[4], nb[5] };
+        if (!G::overlap_by_min_point(r, rsize, nmin, nsize, a.tol))
+          return false;
+        contained = G::range_contains_min_size(r, nmin, nsize, a.tol);
+        return true;
+      }
+      else if constexpr (KIND == kFrustum)
+      {
+        for (u32 i = 0; i < a.np; ++i) // :779-795 first Hit selects, first Negative prunes
+        {
+          const int rel = G::box_plane(nb, nb + 3, pl[4 * i], pl + 4 * i + 1, a.tol);
+          if (rel == 1)
+            return true;
+          if (rel == 0)
+            return false;
+        }
+        return true;
+      }
+      else
+      {
+        T en, ex;
+        return ray.hit_node(nb, nb + 3, en, ex);
+      }
+    };
+    u32 sp = 0;
+    if (lane == 0)
+    {
+      bool contained;
+      if (enters(root, contained))
+      {
+        stack[0] = root | (contained ? kContained : 0u);
+        sp = 1;
+      }
+    }
+    sp = __shfl_sync(~0u, sp, 0);
+    __syncwarp();
+    u32 visits = 0;
+    bool bad = false;
+    while (sp > 0)
+    {
+      const u32 entry = stack[--sp];
+      __syncwarp();
+      const u32 node = entry & ~kContained;
+      const uint4 L = tv.link[node];
+      if (L.z > tv.n || L.w > tv.n || L.y > L.z || ++visits > tv.nNodes)
+      {
+        bad = true;
+        break;
+      }
+      if constexpr (KIND == kRange)
+      {
+        if (entry & kContained)
+        {
+          // whole subtree without entity tests (:549-567); the subtree is one run of sortedIds
+          sink_flush(sink, a.out, lane);
+          const u32 len = L.w - L.y;
+          unsigned long long base = 0;
+          if (lane == 0)
+            base = a.out.reserve(len);
+          base = __shfl_sync(~0u, base, 0);
+          for (u32 i = lane; i < len; i += 32)
+            if (base + i < a.out.capacity)
+              a.out.items[base + i] = (u64(q) << 32) | (tv.ids[L.y + i] - idBase);
+          continue;
+        }
+      }
+      for (u32 b = L.y; b < L.z; b += 32)
+      {
+        const u32 e = b + lane;
+        bool hit = false;
+        double d = 0.0;
+        if (e < L.z)
+        {
+          if constexpr (KIND == kRange)
+          {
+            if (!tv.isBox)
+              hit = G::box_contains_point(r, tv.geom + u64(e) * 3, a.tol);
+            else
+            {
+              T bx[6];
+              load_box(tv.geom + u64(e) * 6, bx);
+              hit = (a.mode == OTG_RANGE_OVERLAP) ? (G::box_relation(r, bx, a.tol) == -1) : G::contains_box_no_tol(r, bx);
+            }
+          }
+          else if constexpr (KIND == kFrustum)
+          {
+            bool neg = false;
+            for (u32 i = 0; i < a.np && !neg; ++i)
+            {
+              int rel;
+              if (tv.isBox)
+              {
+                const T* bx = tv.geom + u64(e) * 6;
+                T bsize[3] = { T(bx[3] - bx[0]), T(bx[4] - bx[1]), T(bx[5] - bx[2]) };
+                rel = G::box_plane(bx, bsize, pl[4 * i], pl + 4 * i + 1, a.tol);
+              }
+              else
+                rel = G::point_plane(tv.geom + u64(e) * 3, pl[4 * i], pl + 4 * i + 1, a.tol);
+              neg = rel == 0;
+            }
+            hit = !neg;
+          }
+          else
+          {
+            T en, ex;
+            hit = (tv.isBox ? ray.hit_box(tv.geom + u64(e) * 6, en, ex) : ray.hit_point(tv.geom + u64(e) * 3, en, ex)) &&
+                  (a.maxDist == T(0) || en <= a.maxDist);
+            d = double(en);
+          }
+        }
+        sink_put(sink, a.out, lane, hit, q, hit ? tv.ids[e] - idBase : 0u, d);
+      }
+      const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+      if (cc)
+      {
+        if (u64(fc) + cc > tv.nNodes || sp + cc > u32(kStack))
+        {
+          bad = true;
+          break;
+        }
+        bool keep = false, contained = false;
+        if (lane < cc)
+          keep = enters(fc + lane, contained);
+        const u32 bal = __ballot_sync(~0u, keep);
+        if (keep)
+          stack[sp + __popc(bal & ((1u << lane) - 1))] = (fc + lane) | (contained ? kContained : 0u);
+        sp += __popc(bal);
+        __syncwarp();
+      }
+    }
+    if (bad && lane == 0)
+      atomicOr(a.err, kErrStack);
+    sink_flush(sink, a.out, lane);
+  }
+}
+
+template<typename T, int KIND>
+static int launch_batch(const BatchArgs<T, KIND>& a0, cudaStream_t st)
+{
+  BatchArgs<T, KIND> a = a0;
+  int dev = 0, sms = 0, per = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (!e)
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (!e)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_query_kernel<T, KIND>, kBatchWarps * 32, 0);
+  if (!e)
+    e = cudaMemsetAsync(a.work, 0, sizeof(u32), st);
+  if (e)
+    return cuda_status(e, "configuring the batched query kernel");
+  const u64 want = (u64(a.nq) + kBatchWarps - 1) / kBatchWarps;
+  const u32 grid = u32(std::max<u64>(1, std::min<u64>(u64(sms) * std::max(per, 1), want)));
+  batch_query_kernel<T, KIND><<<grid, kBatchWarps * 32, 0, st>>>(a);
+  return cuda_status(cudaGetLastError(), "launching the batched query kernel");
+}
+
+template<typename T>
+int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st)
+{
+  return launch_batch<T, kRange>(BatchArgs<T, kRange>{ tv, ranges, 0, nq, mode, tol, T(0), T(0), out, work, err }, st);
+}
+template<typename T>
+int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st)
+{
+  return launch_batch<T, kFrustum>(BatchArgs<T, kFrustum>{ tv, planes, np, nq, 0, tol, T(0), T(0), out, work, err }, st);
+}
+template<typename T>
+int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st)
+{
+  return launch_batch<T, kRayAll>(BatchArgs<T, kRayAll>{ tv, rays, 0, nq, 0, tol, tolInc, maxDist, out, work, err }, st);
+}
+
+template int batch_range<double>(const TreeView<double>&, const double*, u32, int, double, Appender, u32*, u32*, cudaStream_t);
+template int batch_range<float>(const TreeView<float>&, const float*, u32, int, float, Appender, u32*, u32*, cudaStream_t);
+template int batch_frustum<double>(const TreeView<double>&, const double*, u32, u32, double, Appender, u32*, u32*, cudaStream_t);
+template int batch_frustum<float>(const TreeView<float>&, const float*, u32, u32, float, Appender, u32*, u32*, cudaStream_t);
+template int batch_ray_all<double>(const TreeView<double>&, const double*, u32, double, double, double, Appender, u32*, u32*, cudaStream_t);
+template int batch_ray_all<float>(const TreeView<float>&, const float*, u32, float, float, float, Appender, u32*, u32*, cudaStream_t);
+
+} // namespace otg

@@ -1100,12 +1100,21 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
   Collected c;
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
+  DevBuf work;
+  if (cudaError_t e = work.ensure(sizeof(u32)))
+    return cuda_status(e, "allocating the work counter");
+  int launchRc = OTG_OK;
   int rc = collect(
     c, false, nq * 32,
     [&](Appender a, u32* err) {
-      range_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), mode, tl, a, err);
+      if (algo == OTG_ALGO_PLAIN_FP64)
+        range_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), mode, tl, a, err);
+      else
+        launchRc = batch_range<T>(tv, (const T*)d, u32(nq), mode, tl, a, work.as<u32>(), err, st);
     },
     st);
+  if (launchRc)
+    return launchRc;
   if (rc)
     return rc;
   return finish_sorted_ids(c, nq, r, st);
@@ -1144,12 +1153,21 @@ static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, 
   Collected c;
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
+  DevBuf work;
+  if (cudaError_t e = work.ensure(sizeof(u32)))
+    return cuda_status(e, "allocating the work counter");
+  int launchRc = OTG_OK;
   int rc = collect(
     c, false, std::max<u64>(nq * 64, t.n / 4),
     [&](Appender a, u32* err) {
-      frustum_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(np), u32(nq), tl, a, err);
+      if (algo == OTG_ALGO_PLAIN_FP64)
+        frustum_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(np), u32(nq), tl, a, err);
+      else
+        launchRc = batch_frustum<T>(tv, (const T*)d, u32(np), u32(nq), tl, a, work.as<u32>(), err, st);
     },
     st);
+  if (launchRc)
+    return launchRc;
   if (rc)
     return rc;
   return finish_sorted_ids(c, nq, r, st);
@@ -1207,12 +1225,21 @@ static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, do
   int rc;
   if (!first)
   {
+    DevBuf work;
+    if (cudaError_t e = work.ensure(sizeof(u32)))
+      return cuda_status(e, "allocating the work counter");
+    int launchRc = OTG_OK;
     rc = collect(
       c, true, nq * 16,
       [&](Appender a, u32* err) {
-        ray_all_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, ti, md, a, err);
+        if (algo == OTG_ALGO_PLAIN_FP64)
+          ray_all_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, ti, md, a, err);
+        else
+          launchRc = batch_ray_all<T>(tv, (const T*)d, u32(nq), tl, ti, md, a, work.as<u32>(), err, st);
       },
       st);
+    if (launchRc)
+      return launchRc;
   }
   else
   {

@@ -176,6 +176,14 @@ static inline T tol_of(double tol)
   return tol < 0 ? base_tol<T>() : T(tol);
 }
 
+// batched warp-per-query kernels (otg_batch.cu); `work` is a device counter the launch resets
+template<typename T>
+int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st);
+template<typename T>
+int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st);
+template<typename T>
+int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st);
+
 // FP32 images of a built tree for the query filters (otg_knn.cu): built on first use after a build
 int ensure_image32(TreeState& t, cudaStream_t st);
 
