@@ -117,14 +117,21 @@ def dist_setup():
 
 
 def reduce_max(values, world):
+    """Element-wise maximum over the ranks (replicas: the slowest rank sets the time)."""
     if world == 1:
         return values
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor(values, dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor(values, dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return t.tolist()
+
+
+def replica_throughput(units_per_rank, ms_max, world):
+    """Whole-job throughput of independent replicas: all ranks' units over the slowest rank's time."""
+    return world * units_per_rank / (ms_max / 1e3)
 
 
 def barrier(world):
@@ -253,7 +260,7 @@ def run_gpu(args):
     tree.sync(stream)
     info = tree.info()
     ms = reduce_max([statistics.mean(step_ms)], world)[0]
-    value = world * N_POINTS / (ms / 1e3) / 1e6
+    value = replica_throughput(N_POINTS, ms, world) / 1e6
 
     # e2e through the C-ABI: pinned host input, copies inside the timed region
     pinned = torch.from_numpy(pts_h).pin_memory()
@@ -267,7 +274,7 @@ def run_gpu(args):
         if i >= args.warmup:
             e2e_ms.append((t1 - t0) * 1e3)
     e2e_ms_v = reduce_max([statistics.mean(e2e_ms)], world)[0]
-    e2e_value = world * N_POINTS / (e2e_ms_v / 1e3) / 1e6
+    e2e_value = replica_throughput(N_POINTS, e2e_ms_v, world) / 1e6
     otg.profile_enable(False)
 
     # roofline of the dominant phase
@@ -335,6 +342,7 @@ def run_gpu(args):
     if not args.no_queries:
         line["queries"] = run_queries(tree, pts_d, stream)
         line["many_trees"] = run_many_trees()
+        line["two_trees"] = run_two_trees()
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -514,6 +522,19 @@ def run_many_trees(trees=4096, sample=48):
     f.frustum_culling(d_planes, foff, raw=True)
     t4 = time.perf_counter()
     n_ids = [r.sizes()[1] for r in res]
+    # the same step recorded as a CUDA graph and replayed
+    plan = otg.ForestPlan(otg.Forest("boxes", np.float32), d_boxes, off, max_elements=16, ranges=d_ranges, range_offsets=qoff, rays=d_rays,
+                          ray_offsets=qoff, planes=d_planes, frustum_offsets=foff, capacity_factor=1.25)
+    plan.run()
+    torch.cuda.synchronize()
+    g0 = time.perf_counter()
+    for _ in range(reps):
+        plan.run()
+    torch.cuda.synchronize()
+    graph_step_s = (time.perf_counter() - g0) / reps
+    graph_same = all(
+        np.array_equal(plan.result(k)[0], r.to_host()[0]) and np.array_equal(plan.result(k)[1], r.to_host()[1]) for k, r in enumerate(res)
+    )
     # per-tree plain launches on a sample of trees
     host = [r.to_host() for r in res]
     idx = np.random.default_rng(7).choice(trees, sample, replace=False)
@@ -542,6 +563,9 @@ def run_many_trees(trees=4096, sample=48):
         "forest_step_ms": step_s * 1e3,
         "forest_trees_per_s": trees / step_s,
         "forest_queries_per_s_M": (2 * trees * 256 + trees) / step_s / 1e6,
+        "graph_step_ms": graph_step_s * 1e3,
+        "graph_trees_per_s": trees / graph_step_s,
+        "graph_results_equal_to_calls": bool(graph_same),
         "forest_build_ms": (t1 - t0) * 1e3,
         "forest_range_ms": (t2 - t1) * 1e3,
         "forest_ray_all_ms": (t3 - t2) * 1e3,
@@ -551,6 +575,75 @@ def run_many_trees(trees=4096, sample=48):
         "per_tree_plain_sample_trees": int(sample),
         "speedup_forest_vs_per_tree": (1.0 / per_tree_s) and (trees / step_s) / (1.0 / per_tree_s),
         "mismatched_query_groups_in_sample": int(mism),
+    }
+
+
+def two_tree_boxes(n, seed, span=4096.0):
+    """Boxes with centres uniform in [0, span)^3 and half-extents lognormal(ln 1, 0.8) per axis."""
+    rng = np.random.default_rng(seed)
+    c = rng.random((n, 3)) * span
+    e = rng.lognormal(0.0, 0.8, (n, 3))
+    return np.concatenate([c - e, c + e], 1)
+
+
+def run_two_trees(steps=10):
+    """Two-tree collision at scale: a static tree A of 16M boxes against a tree B of 8M boxes that
+    moves by a per-box velocity N(0, 0.5) per axis and per step and is rebuilt every step."""
+    import torch
+
+    import octree_gb300 as otg
+
+    a = torch.as_tensor(two_tree_boxes(16_000_000, 501), device="cuda")
+    b0 = torch.as_tensor(two_tree_boxes(8_000_000, 502), device="cuda")
+    v = torch.as_tensor(np.random.default_rng(503).normal(0.0, 0.5, (8_000_000, 3)), device="cuda")
+    shift = torch.cat([v, v], 1)
+    ta = otg.Tree("boxes")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ta.create(a)
+    ta.sync()
+    build_a_ms = (time.perf_counter() - t0) * 1e3
+    tb = otg.Tree("boxes")
+    rebuild, collide, pairs = [], [], []
+    plain_ms = None
+    equal_step0 = None
+    for s in range(steps + 1):
+        b = b0 + shift * float(s)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tb.create(b)
+        tb.sync()
+        t1 = time.perf_counter()
+        r = ta.collision_pair(tb, raw=True)
+        t2 = time.perf_counter()
+        if s == 0:
+            # warm-up step; also the plain kernel for comparison
+            t3 = time.perf_counter()
+            rp = ta.collision_pair(tb, algo=otg.ALGO_PLAIN_FP64, raw=True)
+            plain_ms = (time.perf_counter() - t3) * 1e3
+            equal_step0 = bool(np.array_equal(r.to_host()[1], rp.to_host()[1]))
+            continue
+        rebuild.append((t1 - t0) * 1e3)
+        collide.append((t2 - t1) * 1e3)
+        pairs.append(r.sizes()[1] // 2)
+    info = tb.info()
+    passes = (3 * info.max_depth + 5 + 7) // 8
+    rebuild_bytes = 8_000_000 * (48 + 12 + 8 + 24 * passes + 12)
+    tests, rechecks = r.stats()
+    return {
+        "tree_a_boxes": 16_000_000,
+        "tree_b_boxes": 8_000_000,
+        "steps": steps,
+        "tree_a_build_ms": build_a_ms,
+        "rebuild_b_ms_mean": statistics.mean(rebuild),
+        "rebuild_b_GBps_algorithmic": rebuild_bytes / (statistics.mean(rebuild) / 1e3) / 1e9,
+        "collide_ms_mean": statistics.mean(collide),
+        "pairs_per_step_mean": statistics.mean(pairs),
+        "pairs_per_s_M": statistics.mean(pairs) / (statistics.mean(collide) / 1e3) / 1e6,
+        "step_ms_mean": statistics.mean(rebuild) + statistics.mean(collide),
+        "collide_plain_fp64_ms_step0": plain_ms,
+        "pair_lists_equal_step0": equal_step0,
+        "recheck_fraction": rechecks / max(tests, 1),
     }
 
 

@@ -204,6 +204,30 @@ int otg_forest_ray_all(const otg_tree* tree, const void* rays, const uint64_t* q
 int otg_forest_ray_first(const otg_tree* tree, const void* rays, const uint64_t* query_offsets, double tol, double tol_increment, double max_distance,
                          int algo, otg_result** out, int mem, void* stream);
 
+/* ---------------------------------------------------------------- recorded forest steps (CUDA graph)
+   No counterpart in the reference. A plan records one step of a forest workload as a CUDA graph:
+   the forest Create of `entities` (device memory, tree sizes given by tree_offsets) followed by
+   the batched range search, ray-all (unbounded) and frustum queries of the given device inputs
+   (any of the three may be NULL with its offsets NULL). otg_forest_plan_new runs the step once
+   through the ordinary calls, sizes every result buffer at capacity_factor times that run's
+   result count, and records the step. otg_forest_plan_run replays it on `stream`: the inputs are
+   re-read from the same device buffers, so a caller updates them in place between runs.
+   otg_forest_plan_result waits for the run and returns device pointers to the CSR result
+   (which: 0 range, 1 ray-all, 2 frustum), valid until the next run; OTG_ERR_OUT_OF_MEMORY if the
+   results outgrew the capacity. The plan uses `tree` until it is freed. */
+typedef struct otg_plan otg_plan;
+int otg_forest_plan_new(otg_plan** plan, otg_tree* tree, const void* entities, const uint64_t* tree_offsets, uint32_t n_trees, uint32_t max_depth,
+                        uint64_t max_elements, const void* ranges, const uint64_t* range_offsets, int mode, const void* rays,
+                        const uint64_t* ray_offsets, const void* planes, uint64_t planes_per_query, const uint64_t* frustum_offsets, double tol,
+                        double capacity_factor, void* stream);
+int otg_forest_plan_run(otg_plan* plan, void* stream);
+int otg_forest_plan_result(otg_plan* plan, int which, uint64_t* n_queries, uint64_t* n_ids, const uint64_t** offsets, const uint32_t** ids,
+                           const double** distances, void* stream);
+/* copies the last run's result `which` into caller arrays (offsets[n_queries+1], ids[n_ids],
+   distances[n_ids] or NULL; mem: destination space) */
+int otg_forest_plan_copy(otg_plan* plan, int which, uint64_t* offsets, uint32_t* ids, double* distances, int mem, void* stream);
+void otg_forest_plan_free(otg_plan* plan);
+
 /* ---------------------------------------------------------------- results */
 int otg_result_info(const otg_result* r, uint64_t* n_queries, uint64_t* n_ids, int* has_distances);
 /* offsets[n_queries+1], ids[n_ids], distances[n_ids] (double; may be NULL). mem: destination space. */

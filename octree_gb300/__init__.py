@@ -60,6 +60,11 @@ EXPORTS = [
     ("otg_forest_frustum_culling", _int, [_vp, _vp, _u64, _vp, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_forest_ray_all", _int, [_vp, _vp, _vp, _dbl, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_forest_ray_first", _int, [_vp, _vp, _vp, _dbl, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_forest_plan_new", _int, [C.POINTER(_vp), _vp, _vp, _vp, _u32, _u32, _u64, _vp, _vp, _int, _vp, _vp, _vp, _u64, _vp, _dbl, _dbl, _vp]),
+    ("otg_forest_plan_run", _int, [_vp, _vp]),
+    ("otg_forest_plan_result", _int, [_vp, _int, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), _vp]),
+    ("otg_forest_plan_copy", _int, [_vp, _int, _vp, _vp, _vp, _int, _vp]),
+    ("otg_forest_plan_free", None, [_vp]),
     ("otg_result_info", _int, [_vp, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_int)]),
     ("otg_result_copy", _int, [_vp, _vp, _vp, _vp, _int, _vp]),
     ("otg_result_device_ptrs", _int, [_vp, _vp, _vp, _vp]),
@@ -399,3 +404,47 @@ class Forest(Tree):
     def ray_first(self, rays, query_offsets, tol=-1.0, tol_increment=0.0, max_distance=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
         p, mem, keep = _arg(rays, self.dtype)
         return self._fquery("otg_forest_ray_first", p, query_offsets, [tol, tol_increment, max_distance, algo], mem, stream, raw)
+
+
+class ForestPlan:
+    """One step of a forest workload recorded as a CUDA graph (otg_forest_plan_new): the forest
+    Create of `entities` plus batched range search, ray-all and frustum queries, replayed by run().
+    Inputs are torch CUDA tensors that run() re-reads; update them in place between runs."""
+
+    RANGE, RAY_ALL, FRUSTUM = 0, 1, 2
+
+    def __init__(self, forest, entities, tree_offsets, max_depth=0, max_elements=16, ranges=None, range_offsets=None, mode=RANGE_INSIDE,
+                 rays=None, ray_offsets=None, planes=None, frustum_offsets=None, tol=-1.0, capacity_factor=1.5, stream=None):
+        self.forest = forest
+        self._keep = [entities, ranges, rays, planes]
+        ptr = lambda t: None if t is None else C.c_void_p(t.data_ptr())
+        offs = []
+        for o in (tree_offsets, range_offsets, ray_offsets, frustum_offsets):
+            offs.append((None, None) if o is None else _offsets(o))
+        self._offs = offs
+        self._nq = [None if o is None else len(o) - 1 for o in (range_offsets, ray_offsets, frustum_offsets)]
+        h = _vp()
+        _check(library().otg_forest_plan_new(
+            C.byref(h), forest.h, ptr(entities), offs[0][0], len(offs[0][1]) - 1, max_depth, max_elements, ptr(ranges), offs[1][0], mode,
+            ptr(rays), offs[2][0], ptr(planes), 0 if planes is None else int(planes.shape[1]), offs[3][0], tol, capacity_factor, _stream_ptr(stream)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            library().otg_forest_plan_free(self.h)
+            self.h = None
+
+    def run(self, stream=None):
+        _check(library().otg_forest_plan_run(self.h, _stream_ptr(stream)))
+
+    def result(self, which, stream=None):
+        """(offsets, ids, distances or None) of the last run, on the host."""
+        nq, n = _u64(), _u64()
+        o, i, d = _vp(), _vp(), _vp()
+        _check(library().otg_forest_plan_result(self.h, which, C.byref(nq), C.byref(n), C.byref(o), C.byref(i), C.byref(d), _stream_ptr(stream)))
+        off = np.zeros(nq.value + 1, np.uint64)
+        ids = np.zeros(max(n.value, 1), np.uint32)
+        dist = np.zeros(max(n.value, 1), np.float64) if which == self.RAY_ALL else None
+        _check(library().otg_forest_plan_copy(self.h, which, off.ctypes.data_as(_vp), ids.ctypes.data_as(_vp),
+                                              None if dist is None else dist.ctypes.data_as(_vp), MEM_HOST, _stream_ptr(stream)))
+        return off, ids[: n.value], (dist[: n.value] if dist is not None else None)

@@ -1306,8 +1306,10 @@ __global__ void forest_root_init_kernel(uint4* link, u64* nodeKey, unsigned char
   }
 }
 
+// launchOnly: the buffers and the host-computed layout of this forest are in place from an earlier
+// build with the same tree sizes; only device work is issued (stream-capturable).
 template<typename T, typename K, bool IS_BOX>
-static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStream_t st)
+static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStream_t st, bool launchOnly = false)
 {
   constexpr int W = IS_BOX ? 6 : 3;
   using U = typename Ord<T>::U;
@@ -1328,6 +1330,8 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
   const size_t histWords = size_t(passes) * trees * kRadix;
   const size_t scratchWords = histWords + size_t(passes) * std::max<u32>(tiles, 1) * kRadix + passes + 8;
   cudaError_t e;
+  if (!launchOnly)
+  {
   if ((e = t.keysA.ensure(sizeof(K) * std::max<u64>(n, 1))) || (e = t.keysB.ensure(sizeof(K) * std::max<u64>(n, 1))) ||
       (e = t.sortedIds.ensure(sizeof(u32) * std::max<u64>(n, 1))) || (e = t.valsB.ensure(sizeof(u32) * std::max<u64>(n, 1))) ||
       (e = t.sortedGeom.ensure(sizeof(T) * W * std::max<u64>(n, 1))) || (e = t.nodeLink.ensure(sizeof(uint4) * maxNodes)) ||
@@ -1351,10 +1355,13 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
     cudaMemcpyAsync(t.minOff.p, t.minOffHost.data(), sizeof(u64) * (trees + 1), cudaMemcpyHostToDevice, st);
   if (tiles)
     cudaMemcpyAsync(t.segTiles.p, t.segTilesHost.data(), sizeof(uint2) * tiles, cudaMemcpyHostToDevice, st);
+  }
   cudaMemsetAsync(t.sortScratch.p, 0, sizeof(u32) * scratchWords, st);
   cudaMemsetAsync(t.levelCount.p, 0, sizeof(u32) * 64, st);
+  cudaMemsetAsync(t.err.p, 0, sizeof(u32) * 4, st);
 
-  Profiler& prof = profiler();
+  Profiler idle;
+  Profiler& prof = launchOnly ? idle : profiler();
   prof.reset();
   const u64* off = t.treeOff.as<u64>();
   const uint2* segTiles = t.segTiles.as<uint2>();
@@ -1543,6 +1550,38 @@ int build_forest(TreeState& t, const void* entities, const u64* treeOffsets, u32
   if (mem == OTG_MEM_HOST)
     return finish_build(t, st);
   return OTG_OK;
+}
+
+// Re-issues the device work of the forest's last build on new entity values (same tree sizes,
+// depths and boxes); allocates and copies nothing from the host, so it can be stream-captured.
+int forest_relaunch(TreeState& t, const void* entities, const void* boxes, cudaStream_t st)
+{
+  if (!t.trees || !t.built)
+  {
+    set_error("forest_relaunch needs a forest that was built before");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  const bool isBox = t.kind == OTG_KIND_BOXES;
+  int rc;
+  if (t.scalar == OTG_SCALAR_F64)
+  {
+    const double* p = static_cast<const double*>(entities);
+    const double* b = static_cast<const double*>(boxes);
+    if (isBox)
+      rc = t.keys32 ? forest_build_impl<double, u32, true>(t, p, b, st, true) : forest_build_impl<double, u64, true>(t, p, b, st, true);
+    else
+      rc = t.keys32 ? forest_build_impl<double, u32, false>(t, p, b, st, true) : forest_build_impl<double, u64, false>(t, p, b, st, true);
+  }
+  else
+  {
+    const float* p = static_cast<const float*>(entities);
+    const float* b = static_cast<const float*>(boxes);
+    if (isBox)
+      rc = t.keys32 ? forest_build_impl<float, u32, true>(t, p, b, st, true) : forest_build_impl<float, u64, true>(t, p, b, st, true);
+    else
+      rc = t.keys32 ? forest_build_impl<float, u32, false>(t, p, b, st, true) : forest_build_impl<float, u64, false>(t, p, b, st, true);
+  }
+  return rc;
 }
 
 int finish_build(TreeState& t, cudaStream_t st)

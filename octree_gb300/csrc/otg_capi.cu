@@ -8,14 +8,6 @@
 #include <new>
 #include <string>
 
-struct otg_tree
-{
-  otg::TreeState s;
-};
-struct otg_result
-{
-  otg::ResultState s;
-};
 
 namespace otg
 {

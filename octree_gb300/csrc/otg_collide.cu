@@ -115,6 +115,7 @@ struct CollideArgs
   float tolHi;
   T tol;
   int selfMode;
+  int swapOut; // two trees searched from the second tree's entities: emit (walked position, entity position)
   Appender out;
   CollideCounters* ctr;
   u32* err;
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(kCollideWarps * 32) collide_box_kernel(Collide
             nbuf = 0;
           }
           if (hit)
-            pbuf[nbuf + __popc(bal & lt)] = (u64(i) << 32) | j;
+            pbuf[nbuf + __popc(bal & lt)] = a.swapOut ? ((u64(j) << 32) | i) : ((u64(i) << 32) | j);
           nbuf += __popc(bal);
           __syncwarp();
         }
@@ -272,7 +273,8 @@ static void host_ru(double v, float& hi)
 
 // Per-call state of the filtered search: the tolerance-specific FP32 images of both trees.
 template<typename T>
-static int collide_search_impl(TreeState& A, TreeState& B, bool self, double tol, Appender out, u32* err, CollideSearch& s, cudaStream_t st)
+static int collide_search_impl(TreeState& A, TreeState& B, bool self, bool swapOut, double tol, Appender out, u32* err, CollideSearch& s,
+                               cudaStream_t st)
 {
   cudaError_t e;
   if (!s.ready)
@@ -315,6 +317,7 @@ static int collide_search_impl(TreeState& A, TreeState& B, bool self, double tol
   a.tolHi = s.tolHi;
   a.tol = tol < 0 ? base_tol<T>() : T(tol);
   a.selfMode = self ? 1 : 0;
+  a.swapOut = swapOut ? 1 : 0;
   a.out = out;
   a.ctr = s.ctr.as<CollideCounters>();
   a.err = err;
@@ -331,10 +334,15 @@ static int collide_search_impl(TreeState& A, TreeState& B, bool self, double tol
   return cuda_status(cudaGetLastError(), "launching the collision kernel");
 }
 
+// Two trees are searched from the smaller tree's entities (a warp per entity walking the larger
+// tree); the candidate pairs keep the (left, right) roles either way.
 int collide_search_filtered(TreeState& A, TreeState& B, bool self, double tol, Appender out, u32* err, CollideSearch& s, cudaStream_t st)
 {
-  return A.scalar == OTG_SCALAR_F64 ? collide_search_impl<double>(A, B, self, tol, out, err, s, st)
-                                    : collide_search_impl<float>(A, B, self, tol, out, err, s, st);
+  const bool swap = !self && B.n < A.n;
+  TreeState& Q = swap ? B : A;
+  TreeState& W = swap ? A : B;
+  return A.scalar == OTG_SCALAR_F64 ? collide_search_impl<double>(Q, W, self, swap, tol, out, err, s, st)
+                                    : collide_search_impl<float>(Q, W, self, swap, tol, out, err, s, st);
 }
 
 int collide_search_stats(const CollideSearch& s, u64& tests, u64& rechecks, cudaStream_t st)

@@ -164,6 +164,7 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
 int build_forest(TreeState& t, const void* entities, const u64* treeOffsets, u32 trees, u32 maxDepth, const void* boxes, u64 maxElem, int mem,
                  cudaStream_t st);
 int finish_build(TreeState& t, cudaStream_t st);
+int forest_relaunch(TreeState& t, const void* entities, const void* boxes, cudaStream_t st);
 int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st);
 int export_nodes(const TreeState& t, u64* keys, double* minSize, u64* eoff, u32* eids, u32* childCount);
 
@@ -188,3 +189,13 @@ int query_knn_noalloc(const TreeState& t, const void* pts, u64 nq, u32 k, double
                       cudaStream_t st);
 
 } // namespace otg
+
+// the opaque handles of the C-ABI
+struct otg_tree
+{
+  otg::TreeState s;
+};
+struct otg_result
+{
+  otg::ResultState s;
+};

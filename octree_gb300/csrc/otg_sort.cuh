@@ -76,9 +76,14 @@ __device__ __forceinline__ u32 block_exclusive_scan(u32 v, u32* s_warp, u32& tot
 }
 
 // All-pass digit histograms of `keys` (shift0 + 8p for p < passes) accumulated into hist[p][256].
+// nDev (optional): the element count in device memory (at most n), for launches recorded before
+// the count is known (graph replay)
 template<typename K>
-__global__ void __launch_bounds__(256) radix_histogram_kernel(const K* __restrict__ keys, u64 n, u32 shift0, u32 passes, u32* __restrict__ hist)
+__global__ void __launch_bounds__(256) radix_histogram_kernel(const K* __restrict__ keys, u64 n, u32 shift0, u32 passes, u32* __restrict__ hist,
+                                                             const unsigned long long* __restrict__ nDev = nullptr)
 {
+  if (nDev)
+    n = min(n, u64(*nDev));
   __shared__ u32 sh[8][kRadix];
   for (int i = threadIdx.x; i < 8 * kRadix; i += blockDim.x)
     (&sh[0][0])[i] = 0;
@@ -107,7 +112,9 @@ __global__ void __launch_bounds__(256) radix_histogram_kernel(const K* __restric
 // in one launch. Tile i covers tile segTiles[i].y of segment segTiles[i].x (the tiles of a segment
 // are consecutive, in order), the look-back stops at the segment's first tile, and hist holds
 // 256 digit counts per segment. Positions are below 2^30, so they are kept in 32 bits.
-template<typename K, bool SEG = false>
+// DEVN: the element count is read from device memory (segOff[0] as unsigned long long, at most n);
+// tiles that start past it end at once (no later tile looks back at them).
+template<typename K, bool SEG = false, bool DEVN = false>
 __global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass_kernel(const K* __restrict__ kin, const u32* __restrict__ vin, K* __restrict__ kout,
                                                                      u32* __restrict__ vout, u32 n, u32 shift, const u32* __restrict__ hist,
                                                                      u32* __restrict__ status, u32* __restrict__ tileCounter, u32* __restrict__ err,
@@ -130,6 +137,12 @@ __global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass_kernel(const K*
   const u32 tile = s_tile;
   // segment of this tile: [segBase, segEnd), its digit counts, its first tile
   u32 segBase = 0, segEnd = n, tileInSeg = tile;
+  if constexpr (DEVN)
+  {
+    segEnd = u32(min(u64(n), u64(*reinterpret_cast<const unsigned long long*>(segOff))));
+    if (u64(tile) * kSortTile >= segEnd)
+      return;
+  }
   if constexpr (SEG)
   {
     const uint2 st = segTiles[tile];
@@ -320,6 +333,27 @@ inline bool onesweep_passes(K* k0, u32* v0, K* k1, u32* v1, u64 n, u32 shift0, u
     u32* vo = even ? v1 : v0;
     onesweep_pass_kernel<K><<<tiles, kSortThreads, onesweep_smem_bytes<K>(), st>>>(ki, vi, ko, vo, u32(n), shift0 + kRadixBits * p, s.hist + p * kRadix,
                                                                                s.status + size_t(p) * tiles * kRadix, s.tileCounters + p, err);
+  }
+  return (passes % 2) == 1;
+}
+
+// Passes over a count known only on the device (*nDev <= n): launched for n elements.
+template<typename K>
+inline bool onesweep_passes_devn(K* k0, u32* v0, K* k1, u32* v1, u64 n, const unsigned long long* nDev, u32 shift0, u32 passes, bool iotaValues,
+                                 SortScratch& s, u32* err, cudaStream_t st)
+{
+  cudaFuncSetAttribute(onesweep_pass_kernel<K, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(onesweep_smem_bytes<K>()));
+  const u32 tiles = u32(SortScratch::tiles(n));
+  for (u32 p = 0; p < passes; ++p)
+  {
+    const bool even = (p % 2) == 0;
+    const K* ki = even ? k0 : k1;
+    const u32* vi = (p == 0 && iotaValues) ? nullptr : (even ? v0 : v1);
+    K* ko = even ? k1 : k0;
+    u32* vo = even ? v1 : v0;
+    onesweep_pass_kernel<K, false, true><<<tiles, kSortThreads, onesweep_smem_bytes<K>(), st>>>(
+      ki, vi, ko, vo, u32(n), shift0 + kRadixBits * p, s.hist + p * kRadix, s.status + size_t(p) * tiles * kRadix, s.tileCounters + p, err, nullptr,
+      reinterpret_cast<const u64*>(nDev));
   }
   return (passes % 2) == 1;
 }
