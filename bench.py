@@ -343,6 +343,7 @@ def run_gpu(args):
         line["queries"] = run_queries(tree, pts_d, stream)
         line["many_trees"] = run_many_trees()
         line["two_trees"] = run_two_trees()
+        line["autotune"] = otg.autotune_entries()
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -238,6 +238,16 @@ int otg_result_device_ptrs(const otg_result* r, const uint64_t** offsets, const 
 int otg_result_stats(const otg_result* r, uint64_t* filter_tests, uint64_t* fp64_rechecks);
 void otg_result_free(otg_result* r);
 
+/* ---------------------------------------------------------------- kernel-shape autotuning
+   No counterpart in the reference. Query kernels exist in shapes that return identical results
+   (one query per thread or per warp; 2, 4 or 8 warps per block). With autotuning on (the default)
+   the first call of a query kind on a size class (kind, scalar, log2 entity count, log2 query
+   count) times every shape on that call's own work and keeps the fastest for the class.
+   otg_autotune_entry describes entry `index`: the class, each shape's time and the choice. */
+int otg_autotune_enable(int on);
+int otg_autotune_count(void);
+int otg_autotune_entry(int index, char* text, int capacity);
+
 /* ---------------------------------------------------------------- instrumentation
    No counterpart in the reference. When enabled, each otg_tree_create records a CUDA event on
    its stream before every build phase; after the stream has completed, otg_profile_phase()

@@ -70,6 +70,9 @@ EXPORTS = [
     ("otg_result_device_ptrs", _int, [_vp, _vp, _vp, _vp]),
     ("otg_result_stats", _int, [_vp, C.POINTER(_u64), C.POINTER(_u64)]),
     ("otg_result_free", None, [_vp]),
+    ("otg_autotune_enable", _int, [_int]),
+    ("otg_autotune_count", _int, []),
+    ("otg_autotune_entry", _int, [_int, C.c_char_p, _int]),
     ("otg_profile_enable", _int, [_int]),
     ("otg_profile_phase_count", _int, []),
     ("otg_profile_phase", _int, [_int, C.c_char_p, _int, C.POINTER(C.c_float)]),
@@ -120,6 +123,21 @@ def _check(rc):
 
 def device_count():
     return library().otg_device_count()
+
+
+def autotune_enable(on=True):
+    _check(library().otg_autotune_enable(1 if on else 0))
+
+
+def autotune_entries():
+    """[text] of the autotuner's choices so far: size class, time of each shape, chosen shape."""
+    lib = library()
+    out = []
+    for i in range(lib.otg_autotune_count()):
+        buf = C.create_string_buffer(512)
+        _check(lib.otg_autotune_entry(i, buf, 512))
+        out.append(buf.value.decode())
+    return out
 
 
 def profile_enable(on=True):

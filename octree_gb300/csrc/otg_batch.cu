@@ -16,7 +16,6 @@
 namespace otg
 {
 
-constexpr int kBatchWarps = 4;
 constexpr u32 kItemBuf = 128;
 constexpr u32 kContained = 1u << 31; // stack entry flag: the range contains the node (emit its subtree)
 
@@ -83,13 +82,13 @@ struct BatchArgs
   u32* err;
 };
 
-template<typename T, int KIND>
-__global__ void __launch_bounds__(kBatchWarps * 32) batch_query_kernel(BatchArgs<T, KIND> a)
+template<typename T, int KIND, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KIND> a)
 {
   using G = GeoD<T>;
-  __shared__ u32 stackMem[kBatchWarps][kStack];
-  __shared__ u64 itemMem[kBatchWarps][kItemBuf];
-  __shared__ double distMem[KIND == kRayAll ? kBatchWarps : 1][KIND == kRayAll ? kItemBuf : 1];
+  __shared__ u32 stackMem[WARPS][kStack];
+  __shared__ u64 itemMem[WARPS][kItemBuf];
+  __shared__ double distMem[KIND == kRayAll ? WARPS : 1][KIND == kRayAll ? kItemBuf : 1];
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   u32* stack = stackMem[w];
   WarpSink sink{ itemMem[w], KIND == kRayAll ? distMem[w] : nullptr, 0 };
@@ -294,47 +293,58 @@ __global__ void __launch_bounds__(kBatchWarps * 32) batch_query_kernel(BatchArgs
   }
 }
 
-template<typename T, int KIND>
-static int launch_batch(const BatchArgs<T, KIND>& a0, cudaStream_t st)
+template<typename T, int KIND, int WARPS>
+static int launch_batch_w(const BatchArgs<T, KIND>& a, cudaStream_t st)
 {
-  BatchArgs<T, KIND> a = a0;
   int dev = 0, sms = 0, per = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (!e)
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (!e)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_query_kernel<T, KIND>, kBatchWarps * 32, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_query_kernel<T, KIND, WARPS>, WARPS * 32, 0);
   if (!e)
     e = cudaMemsetAsync(a.work, 0, sizeof(u32), st);
   if (e)
     return cuda_status(e, "configuring the batched query kernel");
-  const u64 want = (u64(a.nq) + kBatchWarps - 1) / kBatchWarps;
+  const u64 want = (u64(a.nq) + WARPS - 1) / WARPS;
   const u32 grid = u32(std::max<u64>(1, std::min<u64>(u64(sms) * std::max(per, 1), want)));
-  batch_query_kernel<T, KIND><<<grid, kBatchWarps * 32, 0, st>>>(a);
+  batch_query_kernel<T, KIND, WARPS><<<grid, WARPS * 32, 0, st>>>(a);
   return cuda_status(cudaGetLastError(), "launching the batched query kernel");
 }
 
-template<typename T>
-int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st)
+// shape: warps per block, 2, 4 or 8 (autotuned)
+template<typename T, int KIND>
+static int launch_batch(const BatchArgs<T, KIND>& a, int shape, cudaStream_t st)
 {
-  return launch_batch<T, kRange>(BatchArgs<T, kRange>{ tv, ranges, 0, nq, mode, tol, T(0), T(0), out, work, err }, st);
-}
-template<typename T>
-int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st)
-{
-  return launch_batch<T, kFrustum>(BatchArgs<T, kFrustum>{ tv, planes, np, nq, 0, tol, T(0), T(0), out, work, err }, st);
-}
-template<typename T>
-int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st)
-{
-  return launch_batch<T, kRayAll>(BatchArgs<T, kRayAll>{ tv, rays, 0, nq, 0, tol, tolInc, maxDist, out, work, err }, st);
+  if (shape == 2)
+    return launch_batch_w<T, KIND, 2>(a, st);
+  if (shape == 8)
+    return launch_batch_w<T, KIND, 8>(a, st);
+  return launch_batch_w<T, KIND, 4>(a, st);
 }
 
-template int batch_range<double>(const TreeView<double>&, const double*, u32, int, double, Appender, u32*, u32*, cudaStream_t);
-template int batch_range<float>(const TreeView<float>&, const float*, u32, int, float, Appender, u32*, u32*, cudaStream_t);
-template int batch_frustum<double>(const TreeView<double>&, const double*, u32, u32, double, Appender, u32*, u32*, cudaStream_t);
-template int batch_frustum<float>(const TreeView<float>&, const float*, u32, u32, float, Appender, u32*, u32*, cudaStream_t);
-template int batch_ray_all<double>(const TreeView<double>&, const double*, u32, double, double, double, Appender, u32*, u32*, cudaStream_t);
-template int batch_ray_all<float>(const TreeView<float>&, const float*, u32, float, float, float, Appender, u32*, u32*, cudaStream_t);
+template<typename T>
+int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape)
+{
+  return launch_batch<T, kRange>(BatchArgs<T, kRange>{ tv, ranges, 0, nq, mode, tol, T(0), T(0), out, work, err }, shape, st);
+}
+template<typename T>
+int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape)
+{
+  return launch_batch<T, kFrustum>(BatchArgs<T, kFrustum>{ tv, planes, np, nq, 0, tol, T(0), T(0), out, work, err }, shape, st);
+}
+template<typename T>
+int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st,
+                  int shape)
+{
+  return launch_batch<T, kRayAll>(BatchArgs<T, kRayAll>{ tv, rays, 0, nq, 0, tol, tolInc, maxDist, out, work, err }, shape, st);
+}
+
+template int batch_range<double>(const TreeView<double>&, const double*, u32, int, double, Appender, u32*, u32*, cudaStream_t, int);
+template int batch_range<float>(const TreeView<float>&, const float*, u32, int, float, Appender, u32*, u32*, cudaStream_t, int);
+template int batch_frustum<double>(const TreeView<double>&, const double*, u32, u32, double, Appender, u32*, u32*, cudaStream_t, int);
+template int batch_frustum<float>(const TreeView<float>&, const float*, u32, u32, float, Appender, u32*, u32*, cudaStream_t, int);
+template int batch_ray_all<double>(const TreeView<double>&, const double*, u32, double, double, double, Appender, u32*, u32*, cudaStream_t, int);
+template int batch_ray_all<float>(const TreeView<float>&, const float*, u32, float, float, float, Appender, u32*, u32*, cudaStream_t, int);
 
 } // namespace otg

@@ -448,6 +448,24 @@ extern "C"
     });
   }
 
+  int otg_autotune_enable(int on)
+  {
+    tune_enable(on != 0);
+    return OTG_OK;
+  }
+
+  int otg_autotune_count(void) { return tune_count(); }
+
+  int otg_autotune_entry(int index, char* text, int capacity)
+  {
+    if (!text || capacity <= 0 || index < 0 || index >= tune_count())
+      return OTG_ERR_INVALID_ARGUMENT;
+    const std::string s = tune_entry(index);
+    std::strncpy(text, s.c_str(), size_t(capacity) - 1);
+    text[capacity - 1] = 0;
+    return OTG_OK;
+  }
+
   int otg_result_info(const otg_result* r, uint64_t* nq, uint64_t* nids, int* has_distances)
   {
     if (!r)

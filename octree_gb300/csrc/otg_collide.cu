@@ -19,7 +19,6 @@
 namespace otg
 {
 
-constexpr int kCollideWarps = 4;
 constexpr int kPairBuf = 256;
 
 struct CollideCounters
@@ -121,11 +120,11 @@ struct CollideArgs
   u32* err;
 };
 
-template<typename T>
-__global__ void __launch_bounds__(kCollideWarps * 32) collide_box_kernel(CollideArgs<T> a)
+template<typename T, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) collide_box_kernel(CollideArgs<T> a)
 {
-  __shared__ u32 stackMem[kCollideWarps][kStack];
-  __shared__ u64 pairMem[kCollideWarps][kPairBuf];
+  __shared__ u32 stackMem[WARPS][kStack];
+  __shared__ u64 pairMem[WARPS][kPairBuf];
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   u32* stack = stackMem[w];
   u64* pbuf = pairMem[w];
@@ -271,6 +270,22 @@ static void host_ru(double v, float& hi)
   hi = f;
 }
 
+template<typename T, int WARPS>
+static int launch_collide(const CollideArgs<T>& a, cudaStream_t st)
+{
+  int dev = 0, sms = 0, per = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (!e)
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (!e)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, collide_box_kernel<T, WARPS>, WARPS * 32, 0);
+  if (e)
+    return cuda_status(e, "configuring the collision kernel");
+  const u32 grid = u32(std::max<u64>(1, std::min<u64>(u64(sms) * std::max(per, 1), (u64(a.nA) + WARPS - 1) / WARPS)));
+  collide_box_kernel<T, WARPS><<<grid, WARPS * 32, 0, st>>>(a);
+  return cuda_status(cudaGetLastError(), "launching the collision kernel");
+}
+
 // Per-call state of the filtered search: the tolerance-specific FP32 images of both trees.
 template<typename T>
 static int collide_search_impl(TreeState& A, TreeState& B, bool self, bool swapOut, double tol, Appender out, u32* err, CollideSearch& s,
@@ -302,7 +317,6 @@ static int collide_search_impl(TreeState& A, TreeState& B, bool self, bool swapO
       return rc;
     s.orderReady = true;
   }
-  cudaMemsetAsync(s.ctr.p, 0, sizeof(CollideCounters), st);
   CollideArgs<T> a{};
   a.order = s.order.as<u32>();
   a.imgA = s.imgA.as<float4>();
@@ -321,21 +335,18 @@ static int collide_search_impl(TreeState& A, TreeState& B, bool self, bool swapO
   a.out = out;
   a.ctr = s.ctr.as<CollideCounters>();
   a.err = err;
-  int dev = 0, sms = 0, per = 0;
-  e = cudaGetDevice(&dev);
-  if (!e)
-    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (!e)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, collide_box_kernel<T>, kCollideWarps * 32, 0);
-  if (e)
-    return cuda_status(e, "configuring the collision kernel");
-  const u32 grid = u32(std::max<u64>(1, std::min<u64>(u64(sms) * std::max(per, 1), (A.n + kCollideWarps - 1) / kCollideWarps)));
-  collide_box_kernel<T><<<grid, kCollideWarps * 32, 0, st>>>(a);
-  return cuda_status(cudaGetLastError(), "launching the collision kernel");
+  return tune_run(tune_key(self ? "collide self" : "collide pair", sizeof(T) == 8, 1, B.n, A.n), { { 2, "warp x2" }, { 4, "warp x4" }, { 8, "warp x8" } }, 4,
+                  st, [&](int shape) {
+                    cudaMemsetAsync(s.ctr.p, 0, sizeof(CollideCounters), st);
+                    cudaMemsetAsync(out.count, 0, sizeof(unsigned long long), st);
+                    if (shape == 2)
+                      return launch_collide<T, 2>(a, st);
+                    if (shape == 8)
+                      return launch_collide<T, 8>(a, st);
+                    return launch_collide<T, 4>(a, st);
+                  });
 }
 
-// Two trees are searched from the smaller tree's entities (a warp per entity walking the larger
-// tree); the candidate pairs keep the (left, right) roles either way.
 int collide_search_filtered(TreeState& A, TreeState& B, bool self, double tol, Appender out, u32* err, CollideSearch& s, cudaStream_t st)
 {
   const bool swap = !self && B.n < A.n;

@@ -20,7 +20,9 @@
 #include "otg_device.cuh"
 
 #include <cuda_runtime.h>
+#include <functional>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace otg
@@ -158,6 +160,16 @@ struct Profiler
 };
 Profiler& profiler();
 int cuda_status(cudaError_t e, const char* what);
+
+// kernel-shape autotuner (otg_tune.cu): runs launch(shape) with the fastest candidate shape of the
+// key's size class, timing every candidate on the first call of the class
+std::string tune_key(const char* op, bool f64, int kind, u64 entities, u64 queries);
+int tune_run(const std::string& key, const std::vector<std::pair<int, const char*>>& cands, int fallback, cudaStream_t st,
+             const std::function<int(int)>& launch);
+int tune_lookup(const std::string& key, int fallback);
+void tune_enable(bool on);
+int tune_count();
+std::string tune_entry(int i);
 
 // build entry (otg_build.cu)
 int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const void* box, u64 maxElem, int mem, cudaStream_t st);

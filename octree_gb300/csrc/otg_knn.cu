@@ -27,7 +27,6 @@
 namespace otg
 {
 
-constexpr int kKnnWarps = 4; // warps per block of the filtered kernel
 constexpr float kInf = __builtin_huge_valf();
 
 template<int CAP>
@@ -272,8 +271,8 @@ __device__ __forceinline__ void knn_flush(KnnWarpMem<CAP>& W, const KnnArgs<T>& 
   bufN = kept;
 }
 
-template<typename T, int CAP>
-__global__ void __launch_bounds__(kKnnWarps * 32) knn_filtered_kernel(KnnArgs<T> a)
+template<typename T, int CAP, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) knn_filtered_kernel(KnnArgs<T> a)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   const u32 lane = threadIdx.x & 31;
@@ -721,24 +720,35 @@ static int ensure_image32_impl(TreeState& t, cudaStream_t st)
   return OTG_OK;
 }
 
-template<typename T, int CAP>
-static int launch_filtered(const KnnArgs<T>& a, cudaStream_t st)
+template<typename T, int CAP, int WARPS>
+static int launch_filtered_w(const KnnArgs<T>& a, cudaStream_t st)
 {
-  const size_t smem = sizeof(KnnWarpMem<CAP>) * kKnnWarps;
-  cudaError_t e = cudaFuncSetAttribute(knn_filtered_kernel<T, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  const size_t smem = sizeof(KnnWarpMem<CAP>) * WARPS;
+  cudaError_t e = cudaFuncSetAttribute(knn_filtered_kernel<T, CAP, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   int dev = 0, sms = 0, per = 0;
   if (!e)
     e = cudaGetDevice(&dev);
   if (!e)
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (!e)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, knn_filtered_kernel<T, CAP>, kKnnWarps * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, knn_filtered_kernel<T, CAP, WARPS>, WARPS * 32, smem);
   if (e)
     return cuda_status(e, "configuring the kNN kernel");
-  const u64 want = (u64(a.nq) + kKnnWarps - 1) / kKnnWarps;
+  const u64 want = (u64(a.nq) + WARPS - 1) / WARPS;
   const u32 grid = u32(std::max<u64>(1, std::min<u64>(u64(sms) * std::max(per, 1), want)));
-  knn_filtered_kernel<T, CAP><<<grid, kKnnWarps * 32, smem, st>>>(a);
+  knn_filtered_kernel<T, CAP, WARPS><<<grid, WARPS * 32, smem, st>>>(a);
   return cuda_status(cudaGetLastError(), "launching the kNN kernel");
+}
+
+// shape: warps per block (2, 4 or 8)
+template<typename T, int CAP>
+static int launch_filtered(const KnnArgs<T>& a, int shape, cudaStream_t st)
+{
+  if (shape == 2)
+    return launch_filtered_w<T, CAP, 2>(a, st);
+  if (shape == 8)
+    return launch_filtered_w<T, CAP, 8>(a, st);
+  return launch_filtered_w<T, CAP, 4>(a, st);
 }
 
 template<typename T>
@@ -827,8 +837,11 @@ static int knn_filtered_impl(TreeState& t, const T* pts, const u32* dk, u64 nq, 
     a.outIds = oIds.as<u32>();
     a.outDist = oDist.as<double>();
     a.outCap = cap;
-    cudaMemsetAsync(ctr.p, 0, offsetof(KnnCounters, err), st); // keeps the sort's error bits
-    int rc = big ? launch_filtered<T, 512>(a, st) : launch_filtered<T, 256>(a, st);
+    int rc = tune_run(tune_key("knn", sizeof(T) == 8, int(t.kind), t.n, nq), { { 2, "warp x2" }, { 4, "warp x4" }, { 8, "warp x8" } }, 4, st,
+                      [&](int shape) {
+                        cudaMemsetAsync(ctr.p, 0, offsetof(KnnCounters, err), st); // keeps the sort's error bits
+                        return big ? launch_filtered<T, 512>(a, shape, st) : launch_filtered<T, 256>(a, shape, st);
+                      });
     if (rc)
       return rc;
     e = cudaMemcpyAsync(&h, ctr.p, sizeof(h), cudaMemcpyDeviceToHost, st);

@@ -180,13 +180,16 @@ static int plan_record_query(Plan& p, PlanQuery& q, cudaStream_t st)
   cudaMemsetAsync(q.err.p, 0, sizeof(u32), st);
   const bool withDist = q.kind == kPlanRayAll;
   Appender a{ q.items.as<u64>(), withDist ? q.dist.as<double>() : nullptr, q.count.as<unsigned long long>(), q.cap };
+  // the warp shape the first (ordinary) run chose
+  static const char* ops[3] = { "range", "ray all", "frustum" };
+  const int shape = tune_lookup(query_key(ops[q.kind], OTG_ALGO_FILTERED, true, sizeof(T) == 8, t.kind, t.n, q.nq), 4);
   int rc;
   if (q.kind == kPlanRange)
-    rc = batch_range<T>(tv, (const T*)q.input, u32(q.nq), q.mode, tl, a, q.work.as<u32>(), q.err.as<u32>(), st);
+    rc = batch_range<T>(tv, (const T*)q.input, u32(q.nq), q.mode, tl, a, q.work.as<u32>(), q.err.as<u32>(), st, shape);
   else if (q.kind == kPlanFrustum)
-    rc = batch_frustum<T>(tv, (const T*)q.input, q.np, u32(q.nq), tl, a, q.work.as<u32>(), q.err.as<u32>(), st);
+    rc = batch_frustum<T>(tv, (const T*)q.input, q.np, u32(q.nq), tl, a, q.work.as<u32>(), q.err.as<u32>(), st, shape);
   else
-    rc = batch_ray_all<T>(tv, (const T*)q.input, u32(q.nq), tl, T(0), Lim<T>::max(), a, q.work.as<u32>(), q.err.as<u32>(), st);
+    rc = batch_ray_all<T>(tv, (const T*)q.input, u32(q.nq), tl, T(0), Lim<T>::max(), a, q.work.as<u32>(), q.err.as<u32>(), st, shape);
   if (rc)
     return rc;
   const unsigned long long* m = q.count.as<unsigned long long>();
@@ -273,11 +276,11 @@ int plan_create(Plan& p, TreeState& t, const void* ent, const u64* treeOff, u32 
     ResultState r;
     int rc;
     if (k == kPlanRange)
-      rc = query_range(t, q.input, q.nq, mode, tol, OTG_ALGO_DEFAULT, r, OTG_MEM_DEVICE, st, q.qTree.as<u32>());
+      rc = query_range(t, q.input, q.nq, mode, tol, OTG_ALGO_FILTERED, r, OTG_MEM_DEVICE, st, q.qTree.as<u32>());
     else if (k == kPlanRayAll)
-      rc = query_ray(t, q.input, q.nq, tol, 0.0, -1.0, false, OTG_ALGO_DEFAULT, r, OTG_MEM_DEVICE, st, q.qTree.as<u32>());
+      rc = query_ray(t, q.input, q.nq, tol, 0.0, -1.0, false, OTG_ALGO_FILTERED, r, OTG_MEM_DEVICE, st, q.qTree.as<u32>());
     else
-      rc = query_frustum(t, q.input, np, q.nq, tol, OTG_ALGO_DEFAULT, r, OTG_MEM_DEVICE, st, q.qTree.as<u32>());
+      rc = query_frustum(t, q.input, np, q.nq, tol, OTG_ALGO_FILTERED, r, OTG_MEM_DEVICE, st, q.qTree.as<u32>());
     if (rc)
       return rc;
     q.cap = std::max<u64>(4096, u64(std::ceil(double(r.nids) * std::max(1.0, capScale))));

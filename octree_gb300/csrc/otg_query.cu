@@ -1087,6 +1087,17 @@ static int empty_result(u64 nq, ResultState& r, bool dist, cudaStream_t st)
   return cuda_status(e, "empty result");
 }
 
+// shapes of the batched query kernels: 0 = one query per thread, 2/4/8 = warps per block of the
+// warp-per-query kernel. OTG_ALGO_DEFAULT lets the autotuner choose among all of them,
+// OTG_ALGO_FILTERED among the warp shapes.
+static std::vector<std::pair<int, const char*>> query_shapes(int algo)
+{
+  if (algo == OTG_ALGO_DEFAULT)
+    return { { 0, "thread" }, { 2, "warp x2" }, { 4, "warp x4" }, { 8, "warp x8" } };
+  return { { 2, "warp x2" }, { 4, "warp x4" }, { 8, "warp x8" } };
+}
+
+
 template<typename T>
 static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
                       const u32* qTree)
@@ -1110,7 +1121,16 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
       if (algo == OTG_ALGO_PLAIN_FP64)
         range_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), mode, tl, a, err);
       else
-        launchRc = batch_range<T>(tv, (const T*)d, u32(nq), mode, tl, a, work.as<u32>(), err, st);
+        launchRc = tune_run(query_key("range", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st, [&](int shape) {
+          cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
+          cudaMemsetAsync(err, 0, sizeof(u32), st);
+          if (shape == 0)
+          {
+            range_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), mode, tl, a, err);
+            return cuda_status(cudaGetLastError(), "launching the range search");
+          }
+          return batch_range<T>(tv, (const T*)d, u32(nq), mode, tl, a, work.as<u32>(), err, st, shape);
+        });
     },
     st);
   if (launchRc)
@@ -1163,7 +1183,16 @@ static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, 
       if (algo == OTG_ALGO_PLAIN_FP64)
         frustum_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(np), u32(nq), tl, a, err);
       else
-        launchRc = batch_frustum<T>(tv, (const T*)d, u32(np), u32(nq), tl, a, work.as<u32>(), err, st);
+        launchRc = tune_run(query_key("frustum", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st, [&](int shape) {
+          cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
+          cudaMemsetAsync(err, 0, sizeof(u32), st);
+          if (shape == 0)
+          {
+            frustum_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(np), u32(nq), tl, a, err);
+            return cuda_status(cudaGetLastError(), "launching the frustum culling");
+          }
+          return batch_frustum<T>(tv, (const T*)d, u32(np), u32(nq), tl, a, work.as<u32>(), err, st, shape);
+        });
     },
     st);
   if (launchRc)
@@ -1235,7 +1264,16 @@ static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, do
         if (algo == OTG_ALGO_PLAIN_FP64)
           ray_all_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, ti, md, a, err);
         else
-          launchRc = batch_ray_all<T>(tv, (const T*)d, u32(nq), tl, ti, md, a, work.as<u32>(), err, st);
+          launchRc = tune_run(query_key("ray all", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st, [&](int shape) {
+            cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
+            cudaMemsetAsync(err, 0, sizeof(u32), st);
+            if (shape == 0)
+            {
+              ray_all_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, ti, md, a, err);
+              return cuda_status(cudaGetLastError(), "launching the ray query");
+            }
+            return batch_ray_all<T>(tv, (const T*)d, u32(nq), tl, ti, md, a, work.as<u32>(), err, st, shape);
+          });
       },
       st);
     if (launchRc)

@@ -176,13 +176,22 @@ static inline T tol_of(double tol)
   return tol < 0 ? base_tol<T>() : T(tol);
 }
 
-// batched warp-per-query kernels (otg_batch.cu); `work` is a device counter the launch resets
+// batched warp-per-query kernels (otg_batch.cu); `work` is a device counter the launch resets;
+// shape: warps per block (2, 4 or 8)
 template<typename T>
-int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st);
+int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4);
 template<typename T>
-int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st);
+int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4);
 template<typename T>
-int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st);
+int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st,
+                  int shape = 4);
+
+// autotuner size class of a batched query
+inline std::string query_key(const char* op, int algo, bool forest, bool f64, int kind, u64 n, u64 nq)
+{
+  std::string name = std::string(op) + (forest ? " forest" : "") + (algo == OTG_ALGO_FILTERED ? " warp" : "");
+  return tune_key(name.c_str(), f64, kind, n, nq);
+}
 
 // FP32 images of a built tree for the query filters (otg_knn.cu): built on first use after a build
 int ensure_image32(TreeState& t, cudaStream_t st);
