@@ -97,10 +97,10 @@ __global__ void __launch_bounds__(256) bbox_kernel(const T* __restrict__ ent, u6
 #pragma unroll
       for (int d = 0; d < 3; ++d)
       {
-        U lo = O::of(v[k * W + d]);
-        U hi = O::of(v[k * W + (W == 6 ? 3 + d : d)]);
-        mn[d] = lo < mn[d] ? lo : mn[d];
-        mx[d] = hi > mx[d] ? hi : mx[d];
+        const U lo = ord_bits(v[k * W + d]);
+        const U hi = W == 6 ? ord_bits(v[k * W + 3 + d]) : lo;
+        mn[d] = lt_ord(lo, mn[d]) ? lo : mn[d];
+        mx[d] = lt_ord(mx[d], hi) ? hi : mx[d];
       }
     }
   }
@@ -112,18 +112,32 @@ __global__ void __launch_bounds__(256) bbox_kernel(const T* __restrict__ ent, u6
     {
       U a = __shfl_xor_sync(0xffffffffu, mn[d], o);
       U b = __shfl_xor_sync(0xffffffffu, mx[d], o);
-      mn[d] = a < mn[d] ? a : mn[d];
-      mx[d] = b > mx[d] ? b : mx[d];
+      mn[d] = lt_ord(a, mn[d]) ? a : mn[d];
+      mx[d] = lt_ord(mx[d], b) ? b : mx[d];
     }
   }
-  if ((threadIdx.x & 31) == 0)
-  {
+  // block reduction, then one atomic per block and coordinate (same-address atomics serialise)
+  __shared__ U smn[3][8], smx[3][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
 #pragma unroll
     for (int d = 0; d < 3; ++d)
     {
-      atomicMin(&acc[d], mn[d]);
-      atomicMax(&acc[3 + d], mx[d]);
+      smn[d][warp] = mn[d];
+      smx[d][warp] = mx[d];
     }
+  __syncthreads();
+  if (threadIdx.x < 3)
+  {
+    const int d = threadIdx.x;
+    U a = smn[d][0], b = smx[d][0];
+    for (int w = 1; w < int(blockDim.x >> 5); ++w)
+    {
+      a = smn[d][w] < a ? smn[d][w] : a;
+      b = smx[d][w] > b ? smx[d][w] : b;
+    }
+    atomicMin(&acc[d], a);
+    atomicMax(&acc[3 + d], b);
   }
 }
 
@@ -278,9 +292,9 @@ __device__ __forceinline__ u64 entity_key(const T* e, const typename Ord<T>::U* 
     for (int d = 0; d < 3; ++d)
     {
       const U* td = tab + d * perDim;
-      const U o = O::of(e[d]);
+      const U o = ord_bits(e[d]);
       valid = valid && o >= td[0] && o <= td[1];
-      const float est = (to_f(e[d]) - minF[d]) * rastF[d];
+      const float est = (approx_f(e[d]) - minF[d]) * rastF[d];
       g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, o, est > 2.0e9f ? 2000000000 : int(est));
     }
     return valid ? encode3(g[0], g[1], g[2]) + 1 : 0;
@@ -292,7 +306,7 @@ __device__ __forceinline__ u64 entity_key(const T* e, const typename Ord<T>::U* 
     for (int d = 0; d < 3; ++d)
     {
       const U* td = tab + d * perDim;
-      const U lo = O::of(e[d]), hi = O::of(e[3 + d]);
+      const U lo = ord_bits(e[d]), hi = ord_bits(e[3 + d]);
       valid = valid && lo >= td[0] && lo <= td[1] && hi >= td[0] && hi <= td[1];
     }
     if (!valid)
@@ -304,9 +318,9 @@ __device__ __forceinline__ u64 entity_key(const T* e, const typename Ord<T>::U* 
       const U* td = tab + d * perDim;
       const T center = (e[d] + e[3 + d]) * T(0.5); // internal_geometry_module.h:132-138
       const T bsize = T(e[3 + d] - e[d]);           // internal_geometry_module.h:140-146
-      const float est = (to_f(center) - minF[d]) * rastF[d];
-      g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, O::of(center), est > 2.0e9f ? 2000000000 : int(est));
-      level = max(level, level_from_table(td + 2, O::of(bsize)));
+      const float est = (approx_f(center) - minF[d]) * rastF[d];
+      g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, ord_bits(center), est > 2.0e9f ? 2000000000 : int(est));
+      level = max(level, level_from_table(td + 2, ord_bits(bsize)));
     }
     const u32 shift = level * 3u;
     u64 loc = encode3(g[0], g[1], g[2]);
@@ -396,6 +410,7 @@ __global__ void location_export_kernel(const T* __restrict__ geom, const u32* __
 // Random reads of whole entities: every thread issues the loads of kGatherPerThread entities
 // before storing any of them, so many sectors are in flight per thread.
 constexpr int kGatherPerThread = 4;
+
 template<typename T, int W>
 __global__ void __launch_bounds__(256) gather_kernel(const T* __restrict__ ent, const u32* __restrict__ ids, u64 n, T* __restrict__ out)
 {
@@ -412,9 +427,10 @@ __global__ void __launch_bounds__(256) gather_kernel(const T* __restrict__ ent, 
     }
 #pragma unroll
     for (int k = 0; k < kGatherPerThread; ++k)
+      if (id[k] < n)
 #pragma unroll
-      for (int c = 0; c < W; ++c)
-        v[k][c] = id[k] < n ? ent[u64(id[k]) * W + c] : T(0);
+        for (int c = 0; c < W; ++c)
+          v[k][c] = ent[u64(id[k]) * W + c];
 #pragma unroll
     for (int k = 0; k < kGatherPerThread; ++k)
     {
@@ -980,8 +996,8 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   const K* keys = reinterpret_cast<const K*>(t.sortedKeys);
 
   prof.mark("gather", st);
-  gather_kernel<T, W><<<grid_blocks((n + kGatherPerThread - 1) / kGatherPerThread, 256, 152 * 16), 256, 0, st>>>(ent, t.sortedIds.as<u32>(), n,
-                                                                                                                  t.sortedGeom.as<T>());
+  gather_kernel<T, W><<<grid_blocks((n + kGatherPerThread - 1) / kGatherPerThread, 256, 152 * 16), 256, 0, st>>>(
+    ent, t.sortedIds.as<u32>(), n, t.sortedGeom.as<T>());
 
 
   prof.mark("emit", st);
@@ -1407,8 +1423,8 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
 
   prof.mark("gather", st);
   if (n)
-    gather_kernel<T, W><<<grid_blocks((n + kGatherPerThread - 1) / kGatherPerThread, 256, 152 * 16), 256, 0, st>>>(ent, t.sortedIds.as<u32>(), n,
-                                                                                                                    t.sortedGeom.as<T>());
+    gather_kernel<T, W><<<grid_blocks((n + kGatherPerThread - 1) / kGatherPerThread, 256, 152 * 16), 256, 0, st>>>(
+      ent, t.sortedIds.as<u32>(), n, t.sortedGeom.as<T>());
   prof.mark("emit", st);
   u32* parent = IS_BOX ? t.nodeParent.as<u32>() : nullptr;
   forest_root_init_kernel<<<grid_blocks(trees, 128), 128, 0, st>>>(t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeDepth.as<unsigned char>(),

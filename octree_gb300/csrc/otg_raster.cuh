@@ -250,6 +250,44 @@ __global__ void raster_tables_kernel(const Space<T>* __restrict__ spg, typename 
     tab[idx] = raster_threshold<T, R>(s, int(idx / perDim), u32(idx % perDim), cells, isBox);
 }
 
+// Unsigned 64-bit order with 32-bit operations only. 64-bit integer compares and selects appear to
+// issue on the FP64 pipe of this GPU: in min/max reductions over every entity (bounding box) the
+// 32-bit form is faster; where the compares are few and other work dominates, native compares
+// overlap better.
+__device__ __forceinline__ bool lt_u64(unsigned long long a, unsigned long long b)
+{
+  const u32 ah = u32(a >> 32), bh = u32(b >> 32);
+  return ah < bh || (ah == bh && u32(a) < u32(b));
+}
+__device__ __forceinline__ bool lt_ord(unsigned long long a, unsigned long long b) { return lt_u64(a, b); }
+__device__ __forceinline__ bool lt_ord(unsigned int a, unsigned int b) { return a < b; }
+
+// ordered bits of a double from its two 32-bit halves (same map as Ord<double>::of)
+__device__ __forceinline__ unsigned long long ord_bits(double v)
+{
+  const u32 hi = u32(__double2hiint(v)), lo = u32(__double2loint(v));
+  const u32 s = u32(int(hi) >> 31);
+  return (u64(hi ^ (s | 0x80000000u)) << 32) | u64(lo ^ s);
+}
+__device__ __forceinline__ unsigned int ord_bits(float v)
+{
+  const u32 b = __float_as_uint(v);
+  return b ^ (u32(int(b) >> 31) | 0x80000000u);
+}
+
+// an FP32 value close to v (truncated from the bit pattern, no conversion instruction): estimates only
+__device__ __forceinline__ float approx_f(double v)
+{
+  const u32 hi = u32(__double2hiint(v)), lo = u32(__double2loint(v));
+  const int ex = int((hi >> 20) & 0x7ffu) - 1023 + 127;
+  if (ex <= 0)
+    return 0.f;
+  if (ex >= 255)
+    return (hi >> 31) ? -3.0e38f : 3.0e38f;
+  return __uint_as_float((hi & 0x80000000u) | (u32(ex) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
+__device__ __forceinline__ float approx_f(float v) { return v; }
+
 // number of thresholds <= o, minus one (the cell), searching around an estimate
 template<typename U>
 __device__ __forceinline__ u32 cell_from_table(const U* __restrict__ thr, u32 cells, U o, int estimate)

@@ -225,3 +225,26 @@ def test_device_inputs_match_host_inputs():
     a = th.range_search(ranges)
     b = td.range_search(torch.as_tensor(ranges, device="cuda"))
     assert_csr_equal(a[:2], b[:2], "device input")
+
+
+def test_device_inputs_at_unaligned_offsets():
+    """Entities handed over as device views that start 8 bytes past a 16-byte boundary (a slice of a
+    larger tensor) take the scalar loads of the gather; the trees must equal host-built ones."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(14)
+    pts = rng.random((50_001, 3)) * 100
+    d = torch.as_tensor(pts, device="cuda")[1:]  # 24-byte offset
+    a = otg.Tree("points").create(pts[1:], max_depth=8, max_elements=16)
+    b = otg.Tree("points").create(d, max_depth=8, max_elements=16)
+    b.sync()
+    assert np.array_equal(a.location_keys(), b.location_keys())
+    q = rng.random((200, 3)) * 100
+    assert_csr_equal(a.knn(q, 5), b.knn(q, 5), "unaligned points")
+    c = rng.random((30_001, 3)) * 100
+    e = rng.uniform(0.05, 1.0, (30_001, 3))
+    boxes = np.concatenate([c - e, c + e], 1).astype(np.float32)
+    db = torch.as_tensor(boxes, device="cuda")[1:]
+    ta = otg.Tree("boxes", np.float32).create(boxes[1:], max_depth=7, max_elements=16)
+    tb = otg.Tree("boxes", np.float32).create(db, max_depth=7, max_elements=16)
+    tb.sync()
+    assert np.array_equal(ta.collision_self(), tb.collision_self())
