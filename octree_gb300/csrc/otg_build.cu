@@ -897,6 +897,14 @@ static int grid_blocks(u64 n, int perBlock = 256, int maxBlocks = 152 * 16)
   return int(std::max<u64>(1, std::min<u64>(b, u64(maxBlocks))));
 }
 
+// Grid of one emission launch at depth d: `roots` trees hold at most roots * 8^d nodes there, and
+// splitting ones are also bounded by the queue; `perBlock` nodes per 256-thread block.
+static int emit_blocks(u32 d, u64 roots, int maxBlocks, u64 queueCap, u64 perBlock)
+{
+  const u64 cap = std::min<u64>(d < 20 ? roots << (3 * d) : ~u64(0), queueCap);
+  return int(std::max<u64>(1, std::min<u64>(u64(maxBlocks), (cap + perBlock - 1) / perBlock)));
+}
+
 // detail/utils.h:613-622 EstimateMaxDepth (3-D)
 static u32 estimate_max_depth(u64 n, u64 maxElem)
 {
@@ -995,35 +1003,54 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
     t.sortedKeys = t.keysA.p;
   const K* keys = reinterpret_cast<const K*>(t.sortedKeys);
 
-  prof.mark("gather", st);
+  // Node emission reads only the sorted keys, so it runs on a second stream beside the gather: the
+  // gather is bound by DRAM, the emission by the latency of its short dependent launches.
+  cudaStream_t es = st;
+  {
+    if (!t.side)
+    {
+      // the emission's launches are short and dependent: they go first when both streams have work
+      int lowest = 0, highest = 0;
+      cudaDeviceGetStreamPriorityRange(&lowest, &highest);
+      if ((e = cudaStreamCreateWithPriority(&t.side, cudaStreamNonBlocking, highest)) || (e = cudaEventCreateWithFlags(&t.fork, cudaEventDisableTiming)) ||
+          (e = cudaEventCreateWithFlags(&t.join, cudaEventDisableTiming)))
+        return cuda_status(e, "creating the emission stream");
+    }
+    if ((e = cudaEventRecord(t.fork, st)) || (e = cudaStreamWaitEvent(t.side, t.fork, 0)))
+      return cuda_status(e, "ordering the emission stream");
+    es = t.side;
+  }
+  prof.mark("gather+emit", st);
   gather_kernel<T, W><<<grid_blocks((n + kGatherPerThread - 1) / kGatherPerThread, 256, 152 * 16), 256, 0, st>>>(
     ent, t.sortedIds.as<u32>(), n, t.sortedGeom.as<T>());
 
-
-  prof.mark("emit", st);
   u32* parent = IS_BOX ? t.nodeParent.as<u32>() : nullptr;
-  root_init_kernel<T><<<1, 32, 0, st>>>(t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeDepth.as<unsigned char>(), t.levelCount.as<u32>(), u32(n),
-                                        parent);
   const int emitBlocks = grid_blocks(maxNodes, 256, 152 * 16);
   u32* levelCount = t.levelCount.as<u32>();
   u32* splitCount = levelCount + 32;
   u32* splitQueue = t.splitQueue.as<u32>();
   const u32 queueCap = u32(n / (t.maxElem + 1) + 2);
+  root_init_kernel<T><<<1, 32, 0, es>>>(t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeDepth.as<unsigned char>(), levelCount, u32(n), parent);
   for (u32 d = 0; d <= D; ++d)
   {
-    emit_classify_kernel<T, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, D, t.maxElem, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(), levelCount,
-                                                                splitCount, splitQueue, queueCap, t.minTab.as<T>(), sp,
-                                                                IS_BOX ? t.ownerNode.as<u32>() : nullptr, t.err.as<u32>(), ForestNodes{});
+    const int classifyBlocks = emit_blocks(d, 1, emitBlocks, ~u64(0), 256);
+    const int splitBlocks = emit_blocks(d, 1, emitBlocks, queueCap, 32);
+    emit_classify_kernel<T, IS_BOX><<<classifyBlocks, 256, 0, es>>>(d, D, t.maxElem, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
+                                                                    levelCount, splitCount, splitQueue, queueCap, t.minTab.as<T>(), sp,
+                                                                    IS_BOX ? t.ownerNode.as<u32>() : nullptr, t.err.as<u32>(), ForestNodes{});
     if (d < D)
-      emit_split_kernel<T, K, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, D, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
-                                                                  t.nodeDepth.as<unsigned char>(), levelCount, splitCount, splitQueue, queueCap, t.minTab.as<T>(), sp,
-                                                                  maxNodes, t.err.as<u32>(), IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent, ForestNodes{});
+      emit_split_kernel<T, K, IS_BOX><<<splitBlocks, 256, 0, es>>>(d, D, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
+                                                                  t.nodeDepth.as<unsigned char>(), levelCount, splitCount, splitQueue, queueCap,
+                                                                  t.minTab.as<T>(), sp, maxNodes, t.err.as<u32>(),
+                                                                  IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent, ForestNodes{});
   }
+  if ((e = cudaEventRecord(t.join, es)) || (e = cudaStreamWaitEvent(st, t.join, 0)))
+    return cuda_status(e, "joining the emission stream");
   prof.mark("geometry", st);
   if constexpr (IS_BOX)
   {
     for (int d = int(D); d >= 0; --d)
-      mbr_level_kernel<T><<<emitBlocks, 256, 0, st>>>(u32(d), t.levelCount.as<u32>(), t.nodeLink.as<uint4>(), t.sortedGeom.as<T>(), t.nodeBox.as<T>(),
+      mbr_level_kernel<T><<<emit_blocks(u32(d), 1, emitBlocks, ~u64(0), 256), 256, 0, st>>>(u32(d), t.levelCount.as<u32>(), t.nodeLink.as<uint4>(), t.sortedGeom.as<T>(), t.nodeBox.as<T>(),
                                                       t.nodeMax.as<T>());
   }
   else
@@ -1436,11 +1463,11 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
   const ForestNodes fn{ t.nodeTree.as<u32>(), t.treeD.as<u32>(), IS_BOX ? nullptr : t.minOff.as<u64>() };
   for (u32 d = 0; d <= Dmax; ++d)
   {
-    emit_classify_kernel<T, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, Dmax, t.maxElem, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
+    emit_classify_kernel<T, IS_BOX><<<emit_blocks(d, trees, emitBlocks, ~u64(0), 256), 256, 0, st>>>(d, Dmax, t.maxElem, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
                                                                 levelCount, splitCount, t.splitQueue.as<u32>(), queueCap, t.minTab.as<T>(), sp,
                                                                 IS_BOX ? t.ownerNode.as<u32>() : nullptr, t.err.as<u32>(), fn);
     if (d < Dmax)
-      emit_split_kernel<T, K, IS_BOX><<<emitBlocks, 256, 0, st>>>(d, Dmax, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
+      emit_split_kernel<T, K, IS_BOX><<<emit_blocks(d, trees, emitBlocks, queueCap, 32), 256, 0, st>>>(d, Dmax, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
                                                                   t.nodeDepth.as<unsigned char>(), levelCount, splitCount, t.splitQueue.as<u32>(), queueCap,
                                                                   t.minTab.as<T>(), sp, maxNodes, t.err.as<u32>(),
                                                                   IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent, fn);
@@ -1449,7 +1476,7 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
   if constexpr (IS_BOX)
   {
     for (int d = int(Dmax); d >= 0; --d)
-      mbr_level_kernel<T><<<emitBlocks, 256, 0, st>>>(u32(d), levelCount, t.nodeLink.as<uint4>(), t.sortedGeom.as<T>(), t.nodeBox.as<T>(),
+      mbr_level_kernel<T><<<emit_blocks(u32(d), trees, emitBlocks, ~u64(0), 256), 256, 0, st>>>(u32(d), levelCount, t.nodeLink.as<uint4>(), t.sortedGeom.as<T>(), t.nodeBox.as<T>(),
                                                       t.nodeMax.as<T>());
   }
   else if (boxes)

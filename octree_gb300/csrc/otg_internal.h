@@ -86,6 +86,19 @@ constexpr u32 kFirstChildMask = (1u << kChildShift) - 1;
 
 struct TreeState
 {
+  TreeState() = default;
+  TreeState(const TreeState&) = delete;
+  TreeState& operator=(const TreeState&) = delete;
+  ~TreeState()
+  {
+    if (side)
+      cudaStreamDestroy(side);
+    if (fork)
+      cudaEventDestroy(fork);
+    if (join)
+      cudaEventDestroy(join);
+  }
+
   int scalar = OTG_SCALAR_F64;
   int kind = OTG_KIND_POINTS;
   u64 n = 0;
@@ -102,6 +115,9 @@ struct TreeState
   DevBuf nodeParent; // u32 per node (box trees)
   DevBuf levelCount; // u32[64]: nodes per depth, then splitting nodes per depth
   DevBuf splitQueue; // u32: nodes of the current depth that split
+  // point builds emit nodes on a second stream beside the gather (created on first use)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   DevBuf space;      // Space<T>
   DevBuf sortScratch;
   DevBuf err;        // u32 device error bits

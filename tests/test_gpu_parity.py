@@ -85,6 +85,57 @@ def test_points_random(dtype, max_depth, max_elem):
     _check_queries(t, o, _queries(rng, dtype, 100), KIND_POINTS, 0.05, "points")
 
 
+def _emission_case(name):
+    rng = np.random.default_rng(77)
+    if name == "all_outside":
+        return rng.random((5000, 3)) * 50 + 100, np.array([0.0, 0, 0, 50, 50, 50]), 10, 8
+    if name == "partly_outside":
+        return rng.random((40_000, 3)) * 100, np.array([20.0, 20, 20, 70, 70, 70]), 9, 12
+    if name in ("n_eq_max", "n_above_max"):
+        n = 64 if name == "n_eq_max" else 65
+        return rng.random((n, 3)), None, 6, 64
+    if name in ("dup_run_d10", "dup_run_d19"):
+        # identical points spanning several tiles of sorted keys: a chain down to the deepest depth
+        pts = np.concatenate([np.repeat([[0.3, 0.6, 0.2]], 5000, 0), rng.random((3000, 3)), np.repeat([[0.9, 0.1, 0.5]], 2100, 0)])
+        return pts, None, 10 if name == "dup_run_d10" else 19, 8
+    if name in ("max_elem_1024", "max_elem_1025"):
+        return rng.random((60_000, 3)) * 10, None, 8, 1024 if name == "max_elem_1024" else 1025
+    if name == "shell":
+        n = 300_000
+        u = rng.random((n * 7 // 10, 3))
+        d = rng.normal(size=(n - len(u), 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        return np.concatenate([u, 0.5 + d * rng.normal(0.4, 0.005, (len(d), 1))]), None, 12, 20
+    raise KeyError(name)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize(
+    "name", ["all_outside", "partly_outside", "n_eq_max", "n_above_max", "dup_run_d10", "dup_run_d19", "max_elem_1024", "max_elem_1025", "shell"]
+)
+def test_point_emission_layouts(dtype, name):
+    """Point-tree node emission on layouts that stress it: outside points held by the root, a root
+    at the split threshold, runs of identical points crossing sorted-key tiles down to the deepest
+    depth, the largest and smallest maxElementNo of each emission method, and a dense shell."""
+    pts, box, max_depth, max_elem = _emission_case(name)
+    pts = pts.astype(dtype)
+    box = None if box is None else box.astype(dtype)
+    t = _gpu_tree(pts, KIND_POINTS, max_depth, box, max_elem)
+    o = oracle().create(pts, KIND_POINTS, max_depth, box, max_elem)
+    assert t.max_depth == o.max_depth
+    assert np.array_equal(t.location_keys(), o.location_keys())
+    assert_nodes_equal(t.nodes(), o.nodes(), name)
+    rng = np.random.default_rng(5)
+    lo, hi = pts.min(0), pts.max(0)
+    c = lo + rng.random((200, 3)) * (hi - lo)
+    e = rng.random((200, 3)) * (hi - lo) * 0.05
+    ranges = np.concatenate([c - e, c + e], 1).astype(dtype)
+    for mode in (0, 1):
+        assert_csr_equal(t.range_search(ranges, mode)[:2], o.range_search(ranges, mode), f"{name} range{mode}")
+    q = c.astype(dtype)
+    assert_csr_equal(t.knn(q, 9), o.knn(q, 9), f"{name} knn")
+
+
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("max_depth,max_elem", [(8, 32), (0, 16), (4, 2)])
 def test_boxes_random(dtype, max_depth, max_elem):
