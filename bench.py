@@ -54,16 +54,64 @@ def shell_points(n, seed):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    """SM clock and clock-event reasons of this process's GPU, polled every millisecond through NVML
+    (the driver's libnvidia-ml, read-only queries) while running; nvidia-smi every 200 ms if NVML
+    cannot be loaded."""
 
     FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, index):
         self.index = index
         self.proc = None
         self.lines = []
+        self.samples = []  # (sm MHz, max sm MHz, reason bits)
+        self.stop = threading.Event()
+        self.nvml = None
+
+    def _nvml_handle(self):
+        import ctypes
+
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        uuid = None
+        try:
+            import torch
+
+            u = getattr(torch.cuda.get_device_properties(self.index), "uuid", None)
+            uuid = ("GPU-" + str(u)) if u is not None else None
+        except Exception:
+            uuid = None
+        if not (uuid and lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(h)) == 0):
+            if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(h)) != 0:
+                return None
+        self.nvml = lib
+        return h
+
+    def _poll(self, h):
+        import ctypes
+
+        lib = self.nvml
+        reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))
+        sm, bits = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(sm)) == 0 and reasons_fn(h, ctypes.byref(bits)) == 0:
+                self.samples.append((sm.value, mx.value, bits.value))
+            self.stop.wait(0.001)
 
     def __enter__(self):
+        try:
+            h = self._nvml_handle()
+        except Exception:
+            h = None
+        if h is not None:
+            self.t = threading.Thread(target=self._poll, args=(h,), daemon=True)
+            self.t.start()
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
@@ -82,6 +130,9 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        self.stop.set()
+        if self.nvml is not None:
+            self.t.join(timeout=5)
         if self.proc:
             self.proc.terminate()
             try:
@@ -90,6 +141,15 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.samples:
+            reasons = sorted({nm for _, _, b in self.samples for bit, nm in self.REASONS.items() if b & bit})
+            return {
+                "sm_mhz": statistics.median(s for s, _, _ in self.samples),
+                "sm_max_mhz": max(m for _, m, _ in self.samples),
+                "reasons": reasons,
+                "samples": len(self.samples),
+                "source": "nvml 1 ms",
+            }
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
@@ -106,7 +166,7 @@ class ClockSampler:
                     reasons.add(nm)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi 200 ms"}
 
 
 def dist_setup():
