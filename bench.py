@@ -708,7 +708,7 @@ def run_two_trees(steps=10):
     }
 
 
-PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m")
+PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m", "forest_frustum_1024")
 
 
 def run_profile_case(name):
@@ -733,6 +733,17 @@ def run_profile_case(name):
         for _ in range(2):
             r = t.collision_self(algo=otg.ALGO_FILTERED, raw=True)
         print(json.dumps({"case": name, "pairs": r.sizes()[1] // 2, "stats": r.stats()}))
+    elif name == "forest_frustum_1024":
+        boxes, off, _, _, planes = many_trees(1024, 401)
+        d_boxes = torch.as_tensor(boxes, device="cuda")
+        d_planes = torch.as_tensor(planes, device="cuda")
+        foff = np.arange(1025, dtype=np.uint64)
+        f = otg.Forest("boxes", np.float32)
+        f.create(d_boxes, off, max_elements=16)
+        for _ in range(2):
+            r = f.frustum_culling(d_planes, foff, raw=True)
+        f.sync()
+        print(json.dumps({"case": name, "boxes": int(off[-1]), "frustum_ids": int(r.sizes()[1])}))
     elif name == "build_4m":
         pts = torch.as_tensor(shell_points(4_000_000, 301), device="cuda")
         t = otg.Tree("points")

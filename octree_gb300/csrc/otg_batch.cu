@@ -18,6 +18,11 @@ namespace otg
 
 constexpr u32 kItemBuf = 128;
 constexpr u32 kContained = 1u << 31; // stack entry flag: the range contains the node (emit its subtree)
+// Per-warp node stack. A step pops up to 32 nodes and pushes at most 8 children each, so it runs
+// only while that cannot pass kWideStack - kWideReserve; beyond, one node per step (depth first)
+// adds at most 7 entries per level over at most 19 levels.
+constexpr int kWideStack = 768;
+constexpr int kWideReserve = 160;
 
 struct WarpSink
 {
@@ -86,7 +91,7 @@ template<typename T, int KIND, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KIND> a)
 {
   using G = GeoD<T>;
-  __shared__ u32 stackMem[WARPS][kStack];
+  __shared__ u32 stackMem[WARPS][kWideStack];
   __shared__ u64 itemMem[WARPS][kItemBuf];
   __shared__ double distMem[KIND == kRayAll ? WARPS : 1][KIND == kRayAll ? kItemBuf : 1];
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -195,97 +200,158 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
     __syncwarp();
     u32 visits = 0;
     bool bad = false;
+    // the lane holding flat item f of a run of per-lane counts with inclusive prefix `incl`
+    auto owner = [&](u32 incl, u32 f) -> u32 {
+      u32 o = 0;
+#pragma unroll
+      for (u32 s = 16; s >= 1; s >>= 1)
+        if (__shfl_sync(~0u, incl, o + s - 1) <= f)
+          o += s;
+      return o;
+    };
     while (sp > 0)
     {
-      const u32 entry = stack[--sp];
+      // up to 32 nodes per step, one per lane; one at a time (depth first) near the stack's end. The
+      // entities and children of the popped nodes are spread over the lanes as one flat run, so
+      // consecutive lanes read consecutive entities of a node.
+      const u32 take = (sp + 7u * 32u <= u32(kWideStack - kWideReserve)) ? min(sp, 32u) : 1u;
+      sp -= take;
+      const bool act = lane < take;
+      const u32 entry = act ? stack[sp + lane] : 0u;
       __syncwarp();
       const u32 node = entry & ~kContained;
-      const uint4 L = tv.link[node];
-      if (L.z > tv.n || L.w > tv.n || L.y > L.z || ++visits > tv.nNodes)
+      uint4 L = make_uint4(0u, 0u, 0u, 0u);
+      if (act)
+        L = tv.link[node];
+      visits += take;
+      const bool badLane = act && (L.z > tv.n || L.w > tv.n || L.y > L.z || (L.x >> kChildShift) > 8u ||
+                                   u64(L.x & kFirstChildMask) + (L.x >> kChildShift) > tv.nNodes);
+      if (__any_sync(~0u, badLane) || visits > tv.nNodes)
       {
         bad = true;
         break;
       }
+      bool whole = false;
       if constexpr (KIND == kRange)
       {
-        if (entry & kContained)
-        {
-          // whole subtree without entity tests (:549-567); the subtree is one run of sortedIds
+        whole = act && (entry & kContained);
+        // whole subtrees without entity tests (:549-567); a subtree is one run of sortedIds
+        u32 cm = __ballot_sync(~0u, whole);
+        if (cm)
           sink_flush(sink, a.out, lane);
-          const u32 len = L.w - L.y;
+        while (cm)
+        {
+          const int src = __ffs(int(cm)) - 1;
+          cm &= cm - 1;
+          const u32 y = __shfl_sync(~0u, L.y, src), len = __shfl_sync(~0u, L.w, src) - y;
           unsigned long long base = 0;
           if (lane == 0)
             base = a.out.reserve(len);
           base = __shfl_sync(~0u, base, 0);
           for (u32 i = lane; i < len; i += 32)
             if (base + i < a.out.capacity)
-              a.out.items[base + i] = (u64(q) << 32) | (tv.ids[L.y + i] - idBase);
-          continue;
+              a.out.items[base + i] = (u64(q) << 32) | (tv.ids[y + i] - idBase);
         }
       }
-      for (u32 b = L.y; b < L.z; b += 32)
+      const bool tests = act && !whole;
+      // entities of the popped nodes
       {
-        const u32 e = b + lane;
-        bool hit = false;
-        double d = 0.0;
-        if (e < L.z)
+        const u32 cnt = tests ? L.z - L.y : 0u;
+        u32 incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
         {
-          if constexpr (KIND == kRange)
+          const u32 y = __shfl_up_sync(~0u, incl, o);
+          if (lane >= u32(o))
+            incl += y;
+        }
+        const u32 total = __shfl_sync(~0u, incl, 31);
+        for (u32 f0 = 0; f0 < total; f0 += 32)
+        {
+          const u32 f = f0 + lane;
+          const u32 o = owner(incl, min(f, total - 1));
+          const u32 oy = __shfl_sync(~0u, L.y, o), oex = __shfl_sync(~0u, incl - cnt, o);
+          const bool v = f < total;
+          const u32 e = oy + (f - oex);
+          bool hit = false;
+          double d = 0.0;
+          if (v)
           {
-            if (!tv.isBox)
-              hit = G::box_contains_point(r, tv.geom + u64(e) * 3, a.tol);
+            if constexpr (KIND == kRange)
+            {
+              if (!tv.isBox)
+                hit = G::box_contains_point(r, tv.geom + u64(e) * 3, a.tol);
+              else
+              {
+                T bx[6];
+                load_box(tv.geom + u64(e) * 6, bx);
+                hit = (a.mode == OTG_RANGE_OVERLAP) ? (G::box_relation(r, bx, a.tol) == -1) : G::contains_box_no_tol(r, bx);
+              }
+            }
+            else if constexpr (KIND == kFrustum)
+            {
+              bool neg = false;
+              for (u32 i = 0; i < a.np && !neg; ++i)
+              {
+                int rel;
+                if (tv.isBox)
+                {
+                  const T* bx = tv.geom + u64(e) * 6;
+                  T bsize[3] = { T(bx[3] - bx[0]), T(bx[4] - bx[1]), T(bx[5] - bx[2]) };
+                  rel = G::box_plane(bx, bsize, pl[4 * i], pl + 4 * i + 1, a.tol);
+                }
+                else
+                  rel = G::point_plane(tv.geom + u64(e) * 3, pl[4 * i], pl + 4 * i + 1, a.tol);
+                neg = rel == 0;
+              }
+              hit = !neg;
+            }
             else
             {
-              T bx[6];
-              load_box(tv.geom + u64(e) * 6, bx);
-              hit = (a.mode == OTG_RANGE_OVERLAP) ? (G::box_relation(r, bx, a.tol) == -1) : G::contains_box_no_tol(r, bx);
+              T en, ex;
+              hit = (tv.isBox ? ray.hit_box(tv.geom + u64(e) * 6, en, ex) : ray.hit_point(tv.geom + u64(e) * 3, en, ex)) &&
+                    (a.maxDist == T(0) || en <= a.maxDist);
+              d = double(en);
             }
           }
-          else if constexpr (KIND == kFrustum)
-          {
-            bool neg = false;
-            for (u32 i = 0; i < a.np && !neg; ++i)
-            {
-              int rel;
-              if (tv.isBox)
-              {
-                const T* bx = tv.geom + u64(e) * 6;
-                T bsize[3] = { T(bx[3] - bx[0]), T(bx[4] - bx[1]), T(bx[5] - bx[2]) };
-                rel = G::box_plane(bx, bsize, pl[4 * i], pl + 4 * i + 1, a.tol);
-              }
-              else
-                rel = G::point_plane(tv.geom + u64(e) * 3, pl[4 * i], pl + 4 * i + 1, a.tol);
-              neg = rel == 0;
-            }
-            hit = !neg;
-          }
-          else
-          {
-            T en, ex;
-            hit = (tv.isBox ? ray.hit_box(tv.geom + u64(e) * 6, en, ex) : ray.hit_point(tv.geom + u64(e) * 3, en, ex)) &&
-                  (a.maxDist == T(0) || en <= a.maxDist);
-            d = double(en);
-          }
+          sink_put(sink, a.out, lane, hit, q, hit ? tv.ids[e] - idBase : 0u, d);
         }
-        sink_put(sink, a.out, lane, hit, q, hit ? tv.ids[e] - idBase : 0u, d);
       }
-      const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
-      if (cc)
+      // children of the popped nodes, tested before they are pushed
       {
-        if (u64(fc) + cc > tv.nNodes || sp + cc > u32(kStack))
+        const u32 cnt = tests ? (L.x >> kChildShift) : 0u;
+        u32 incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
         {
-          bad = true;
-          break;
+          const u32 y = __shfl_up_sync(~0u, incl, o);
+          if (lane >= u32(o))
+            incl += y;
         }
-        bool keep = false, contained = false;
-        if (lane < cc)
-          keep = enters(fc + lane, contained);
-        const u32 bal = __ballot_sync(~0u, keep);
-        if (keep)
-          stack[sp + __popc(bal & ((1u << lane) - 1))] = (fc + lane) | (contained ? kContained : 0u);
-        sp += __popc(bal);
-        __syncwarp();
+        const u32 total = __shfl_sync(~0u, incl, 31);
+        for (u32 f0 = 0; f0 < total; f0 += 32)
+        {
+          const u32 f = f0 + lane;
+          const u32 o = owner(incl, min(f, total - 1));
+          const u32 ofc = __shfl_sync(~0u, L.x & kFirstChildMask, o), oex = __shfl_sync(~0u, incl - cnt, o);
+          bool keep = false, contained = false;
+          const u32 child = ofc + (f - oex);
+          if (f < total)
+            keep = enters(child, contained);
+          const u32 bal = __ballot_sync(~0u, keep);
+          if (sp + __popc(bal) > u32(kWideStack))
+          {
+            bad = true;
+            break;
+          }
+          if (keep)
+            stack[sp + __popc(bal & ((1u << lane) - 1))] = child | (contained ? kContained : 0u);
+          sp += __popc(bal);
+        }
       }
+      __syncwarp();
+      if (bad)
+        break;
     }
     if (bad && lane == 0)
       atomicOr(a.err, kErrStack);
