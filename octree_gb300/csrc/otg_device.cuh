@@ -237,6 +237,28 @@ struct GeoD
     for (int d = 0; d < 3; ++d)
       dot += n[d] * center[d];
     T cproj = dot - dist;
+    if constexpr (sizeof(T) == 4)
+    {
+      // FP32 decision with the double-accumulated radius bracketed: with tol >= 0 the four addends
+      // are non-negative, so the float sum rf is within 3 * 2^-24 (plus 3 * 2^-53) of the double one.
+      // rf +- rf * 2^-19 brackets it after its own rounding; only positions inside the bracket take
+      // the double path below. The double instructions run on the slow FP64 pipe of this GPU.
+      if (tol >= T(0))
+      {
+        float rf = tol;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          rf += half[d] * fabsf(n[d]);
+        const float e = rf * 0x1p-19f + 0x1p-126f;
+        const float hi = rf + e, lo = rf - e;
+        if (cproj < -hi)
+          return 0;
+        if (cproj > hi)
+          return 2;
+        if (cproj > -lo && cproj < lo)
+          return 1;
+      }
+    }
     if (double(cproj) + radius < 0.0)
       return 0;
     if (double(cproj) - radius > 0.0)

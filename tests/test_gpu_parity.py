@@ -299,3 +299,27 @@ def test_device_inputs_at_unaligned_offsets():
     tb = otg.Tree("boxes", np.float32).create(db, max_depth=7, max_elements=16)
     tb.sync()
     assert np.array_equal(ta.collision_self(), tb.collision_self())
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("tol", [0.0, 0.25, -1.0])
+def test_frustum_on_plane_boundaries(dtype, tol):
+    """Boxes with corners on a grid and axis-aligned or diagonal planes through grid values: many
+    box-plane relations are exact ties (projected centre at exactly +-radius), where the FP32 plane
+    decision must hand over to the reference's double-accumulated radius."""
+    rng = np.random.default_rng(31)
+    lo = rng.integers(0, 64, (20000, 3)).astype(np.float64)
+    ext = rng.integers(0, 4, (20000, 3)).astype(np.float64)
+    boxes = np.concatenate([lo, lo + ext], 1).astype(dtype)
+    t = _gpu_tree(boxes, KIND_LOOSE_BOXES, 6, None, 8)
+    o = oracle().create(boxes, KIND_LOOSE_BOXES, 6, None, 8)
+    planes = np.zeros((48, 6, 4), np.float64)
+    for q in range(48):
+        a, b = rng.integers(4, 30, 3), rng.integers(34, 60, 3)
+        for ax in range(3):
+            planes[q, 2 * ax, 0], planes[q, 2 * ax, 1 + ax] = a[ax], 1.0
+            planes[q, 2 * ax + 1, 0], planes[q, 2 * ax + 1, 1 + ax] = -b[ax], -1.0
+        if q % 3 == 0:  # a diagonal plane through grid points
+            planes[q, 0] = [rng.integers(20, 60) / np.sqrt(2.0), 1 / np.sqrt(2.0), 1 / np.sqrt(2.0), 0.0]
+    planes = planes.astype(dtype)
+    assert_csr_equal(t.frustum_culling(planes, tol=tol)[:2], o.frustum(planes, tol=tol), f"frustum tol={tol}")
