@@ -708,7 +708,7 @@ def run_two_trees(steps=10):
     }
 
 
-PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m", "forest_frustum_1024")
+PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m", "build_4m_clustered", "forest_frustum_1024")
 
 
 def run_profile_case(name):
@@ -744,6 +744,18 @@ def run_profile_case(name):
             r = f.frustum_culling(d_planes, foff, raw=True)
         f.sync()
         print(json.dumps({"case": name, "boxes": int(off[-1]), "frustum_ids": int(r.sizes()[1])}))
+    elif name == "build_4m_clustered":
+        # half the points in 64 tight clusters: buckets above the shared-memory capacity of one block
+        rng = np.random.default_rng(311)
+        pts = rng.random((4_000_000, 3))
+        centres = rng.random((64, 3))
+        pts[:2_000_000] = centres[rng.integers(0, 64, 2_000_000)] + rng.normal(0.0, 0.01, (2_000_000, 3))
+        pts = torch.as_tensor(pts, device="cuda")
+        t = otg.Tree("points")
+        for _ in range(2):
+            t.create(pts, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
+        t.sync()
+        print(json.dumps({"case": name, "nodes": int(t.node_count)}))
     elif name == "build_4m":
         pts = torch.as_tensor(shell_points(4_000_000, 301), device="cuda")
         t = otg.Tree("points")

@@ -100,6 +100,19 @@ def _emission_case(name):
         return pts, None, 10 if name == "dup_run_d10" else 19, 8
     if name in ("max_elem_1024", "max_elem_1025"):
         return rng.random((60_000, 3)) * 10, None, 8, 1024 if name == "max_elem_1024" else 1025
+    if name == "clusters_big":
+        # tight clusters: depth-B cells of tens of thousands of points, split cell by cell
+        c = rng.random((4, 3))
+        pts = np.concatenate([c[rng.integers(0, 4, 100_000)] + rng.normal(0, 0.002, (100_000, 3)), rng.random((100_000, 3))])
+        return pts, None, 10, 20
+    if name == "dup_big":
+        # one depth-D cell holding more points than a block handles in shared memory
+        return np.concatenate([np.repeat([[0.41, 0.52, 0.63]], 20_000, 0), rng.random((5000, 3))]), None, 10, 8
+    if name == "pairs_max_elem_1":
+        # near-identical pairs with maxElementNo 1: node chains down to where each pair separates
+        # (more nodes than positions in a work item)
+        p0 = rng.random((30_000, 3))
+        return np.concatenate([p0, p0 + rng.normal(0, 2e-4, p0.shape)]), None, 10, 1
     if name == "shell":
         n = 300_000
         u = rng.random((n * 7 // 10, 3))
@@ -111,12 +124,16 @@ def _emission_case(name):
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize(
-    "name", ["all_outside", "partly_outside", "n_eq_max", "n_above_max", "dup_run_d10", "dup_run_d19", "max_elem_1024", "max_elem_1025", "shell"]
+    "name",
+    ["all_outside", "partly_outside", "n_eq_max", "n_above_max", "dup_run_d10", "dup_run_d19", "max_elem_1024", "max_elem_1025", "shell",
+     "clusters_big", "dup_big", "pairs_max_elem_1"],
 )
 def test_point_emission_layouts(dtype, name):
     """Point-tree node emission on layouts that stress it: outside points held by the root, a root
     at the split threshold, runs of identical points crossing sorted-key tiles down to the deepest
-    depth, the largest and smallest maxElementNo of each emission method, and a dense shell."""
+    depth, the largest and smallest maxElementNo of each emission method, a dense shell, buckets
+    above one block's shared-memory capacity (tight clusters, one cell of identical points), and
+    more nodes than positions (near-identical pairs, maxElementNo 1)."""
     pts, box, max_depth, max_elem = _emission_case(name)
     pts = pts.astype(dtype)
     box = None if box is None else box.astype(dtype)
