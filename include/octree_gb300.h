@@ -137,6 +137,17 @@ int otg_knn(const otg_tree* tree, const void* points, uint64_t n_queries, const 
 int otg_frustum_culling(const otg_tree* tree, const void* planes, uint64_t planes_per_query, uint64_t n_queries, double tol, int algo,
                         otg_result** out, int mem, void* stream);
 
+/* PlaneSearch(distanceOfOrigo, planeNormal, entities, tol) (core/ot_query.h:612-636; the same as
+   PlaneIntersection, :656-664): one plane {origoDistance, nx, ny, nz} (normalized) per query; the
+   ids of the entities the plane hits, ascending per query. */
+int otg_plane_search(const otg_tree* tree, const void* planes, uint64_t n_queries, double tol, int algo, otg_result** out, int mem, void* stream);
+
+/* PlanePositiveSegmentation(distanceOfOrigo, planeNormal, entities, tol) (core/ot_query.h:687-744):
+   one plane per query; the ids of the entities not on its negative side, ascending per query (a
+   node wholly on the positive side contributes its subtree untested, as in the reference). */
+int otg_plane_positive_segmentation(const otg_tree* tree, const void* planes, uint64_t n_queries, double tol, int algo, otg_result** out, int mem,
+                                    void* stream);
+
 /* RayIntersectedAll(origin, direction, entities, tol, toleranceIncrement, maxExaminationDistance)
    (core/ot_query.h:1928-2022). max_distance < 0: unbounded; 0: no limit (reference semantics).
    Results by (enter distance, id). */

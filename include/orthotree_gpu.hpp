@@ -9,8 +9,9 @@
 // entities, optional max depth, optional space box, max elements per node (default 16,
 // core/configuration.h:83). Queries have the reference's names, argument order and defaults
 // (core/ot_managed.h:584-893) and return the same id lists:
-//   PickSearch, RangeSearch, FrustumCulling, GetNearestNeighbors, RayIntersectedAll,
-//   RayIntersectedFirst, CollisionDetection (one tree and two trees).
+//   PickSearch, RangeSearch, FrustumCulling, PlaneSearch / PlaneIntersection,
+//   PlanePositiveSegmentation, GetNearestNeighbors, RayIntersectedAll, RayIntersectedFirst,
+//   CollisionDetection (one tree and two trees).
 // Each query also has a batched form (…Batch) answering many query geometries in one GPU launch;
 // it returns a Csr (offsets + ids [+ distances]).
 //
@@ -257,6 +258,32 @@ public:
     return first(FrustumCullingBatch(boundaryPlanes, boundaryPlanes.size(), tolerance));
   }
 
+  // core/ot_query.h:612-664 (PlaneSearch; PlaneIntersection is the same query)
+  std::vector<EntityID> PlaneSearch(TScalar distanceOfOrigo, const TVector& planeNormal, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    const TPlane plane{ distanceOfOrigo, planeNormal };
+    return first(PlaneSearchBatch(std::span<const TPlane>(&plane, 1), tolerance));
+  }
+  std::vector<EntityID> PlaneSearch(const TPlane& plane, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return first(PlaneSearchBatch(std::span<const TPlane>(&plane, 1), tolerance));
+  }
+  std::vector<EntityID> PlaneIntersection(const TPlane& plane, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return PlaneSearch(plane, tolerance);
+  }
+  // core/ot_query.h:687-758
+  std::vector<EntityID> PlanePositiveSegmentation(TScalar distanceOfOrigo, const TVector& planeNormal,
+                                                  double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    const TPlane plane{ distanceOfOrigo, planeNormal };
+    return first(PlanePositiveSegmentationBatch(std::span<const TPlane>(&plane, 1), tolerance));
+  }
+  std::vector<EntityID> PlanePositiveSegmentation(const TPlane& plane, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return first(PlanePositiveSegmentationBatch(std::span<const TPlane>(&plane, 1), tolerance));
+  }
+
   std::vector<EntityID> GetNearestNeighbors(const TVector& searchPoint, std::size_t neighborCount, TScalar maxDistanceWithin,
                                             double tolerance = detail::base_tolerance<TScalar>()) const
   {
@@ -315,6 +342,20 @@ public:
     otg_result* r = nullptr;
     detail::check(otg_frustum_culling(m_tree, planes.data(), planesPerQuery, planes.size() / planesPerQuery, tolerance, int(algo), &r, OTG_MEM_HOST,
                                       m_stream));
+    return detail::take(r, m_stream);
+  }
+  // one plane per query
+  Csr PlaneSearchBatch(std::span<const TPlane> planes, double tolerance = detail::base_tolerance<TScalar>(), Algorithm algo = Algorithm::Default) const
+  {
+    otg_result* r = nullptr;
+    detail::check(otg_plane_search(m_tree, planes.data(), planes.size(), tolerance, int(algo), &r, OTG_MEM_HOST, m_stream));
+    return detail::take(r, m_stream);
+  }
+  Csr PlanePositiveSegmentationBatch(std::span<const TPlane> planes, double tolerance = detail::base_tolerance<TScalar>(),
+                                     Algorithm algo = Algorithm::Default) const
+  {
+    otg_result* r = nullptr;
+    detail::check(otg_plane_positive_segmentation(m_tree, planes.data(), planes.size(), tolerance, int(algo), &r, OTG_MEM_HOST, m_stream));
     return detail::take(r, m_stream);
   }
   Csr GetNearestNeighborsBatch(std::span<const TVector> points, std::size_t neighborCount,

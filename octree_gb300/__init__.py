@@ -47,6 +47,8 @@ EXPORTS = [
     ("otg_pick_search", _int, [_vp, _vp, _u64, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_knn", _int, [_vp, _vp, _u64, _vp, _u32, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_frustum_culling", _int, [_vp, _vp, _u64, _u64, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_plane_search", _int, [_vp, _vp, _u64, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_plane_positive_segmentation", _int, [_vp, _vp, _u64, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_ray_all", _int, [_vp, _vp, _u64, _dbl, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_ray_first", _int, [_vp, _vp, _u64, _dbl, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_collision_self", _int, [_vp, _dbl, _int, C.POINTER(_vp), _vp]),
@@ -328,6 +330,16 @@ class Tree:
         """planes: (n_queries, planes_per_query, 4) as {origo distance, nx, ny, nz}."""
         p, mem, keep = _arg(planes, self.dtype)
         return self._query("otg_frustum_culling", [p, int(planes.shape[1]), int(planes.shape[0]), tol, algo], mem, stream, raw)
+
+    def plane_search(self, planes, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        """PlaneSearch: planes (n_queries, 4) as {origo distance, nx, ny, nz}, one per query."""
+        p, mem, keep = _arg(planes, self.dtype)
+        return self._query("otg_plane_search", [p, int(planes.shape[0]), tol, algo], mem, stream, raw)
+
+    def plane_positive_segmentation(self, planes, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        """PlanePositiveSegmentation: planes (n_queries, 4), one per query."""
+        p, mem, keep = _arg(planes, self.dtype)
+        return self._query("otg_plane_positive_segmentation", [p, int(planes.shape[0]), tol, algo], mem, stream, raw)
 
     def ray_all(self, rays, tol=-1.0, tol_increment=0.0, max_distance=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
         p, mem, keep = _arg(rays, self.dtype)

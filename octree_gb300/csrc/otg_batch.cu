@@ -1,4 +1,5 @@
-// otg_batch.cu — batched RangeSearch, FrustumCulling and RayIntersectedAll: persistent kernels in
+// otg_batch.cu — batched RangeSearch, FrustumCulling, RayIntersectedAll, PlaneSearch and
+// PlanePositiveSegmentation: persistent kernels in
 // which each warp takes the next query from a shared counter (queries of uneven cost balance out,
 // in one tree or across the trees of a forest) and answers it cooperatively:
 //   * the node's own entities are tested by the 32 lanes in parallel (coalesced reads of the
@@ -11,6 +12,8 @@
 //   RangeSearch         core/ot_query.h:476-583
 //   FrustumCulling      core/ot_query.h:767-833
 //   RayIntersectedAll   core/ot_query.h:1928-2022
+//   PlaneSearch         core/ot_query.h:612-636
+//   PlanePositiveSegmentation core/ot_query.h:687-744
 #include "otg_query.cuh"
 
 namespace otg
@@ -71,13 +74,13 @@ __device__ __forceinline__ void sink_put(WarpSink& s, Appender& out, u32 lane, b
 }
 
 // query kinds
-constexpr int kRange = 0, kFrustum = 1, kRayAll = 2;
+constexpr int kRange = 0, kFrustum = 1, kRayAll = 2, kPlane = 3, kPlanePositive = 4;
 
 template<typename T, int KIND>
 struct BatchArgs
 {
   TreeView<T> tv;
-  const T* q;   // ranges (6 per query), planes (4 * np per query) or rays (6 per query)
+  const T* q;   // ranges (6 per query), planes (4 * np per query, 4 for the plane kinds) or rays (6 per query)
   u32 np;       // planes per query
   u32 nq;
   int mode;     // RangeSearchMode
@@ -149,6 +152,8 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
       pl = a.q + u64(q) * a.np * 4;
       skip = a.np == 0;
     }
+    else if constexpr (KIND == kPlane || KIND == kPlanePositive)
+      pl = a.q + u64(q) * 4;
     else
     {
       ray.make(a.q + u64(q) * 6, a.q + u64(q) * 6 + 3, a.tol, a.tolInc);
@@ -179,6 +184,14 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
             return false;
         }
         return true;
+      }
+      else if constexpr (KIND == kPlane)
+        return G::box_plane(nb, nb + 3, pl[0], pl + 1, a.tol) == 1; // :620-621 only nodes the plane hits
+      else if constexpr (KIND == kPlanePositive)
+      {
+        const int rel = G::box_plane(nb, nb + 3, pl[0], pl + 1, a.tol); // :702-710 negative prunes, positive takes the subtree
+        contained = rel == 2;
+        return rel != 0;
       }
       else
       {
@@ -232,10 +245,11 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
         break;
       }
       bool whole = false;
-      if constexpr (KIND == kRange)
+      if constexpr (KIND == kRange || KIND == kPlanePositive)
       {
         whole = act && (entry & kContained);
-        // whole subtrees without entity tests (:549-567); a subtree is one run of sortedIds
+        // whole subtrees without entity tests (range :549-567, positive side :711-726); a subtree is
+        // one run of sortedIds
         u32 cm = __ballot_sync(~0u, whole);
         if (cm)
           sink_flush(sink, a.out, lane);
@@ -305,6 +319,19 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
                 neg = rel == 0;
               }
               hit = !neg;
+            }
+            else if constexpr (KIND == kPlane || KIND == kPlanePositive)
+            {
+              int rel; // ot_query.h:586-602 GetEntityPlaneRelation
+              if (tv.isBox)
+              {
+                const T* bx = tv.geom + u64(e) * 6;
+                T bsize[3] = { T(bx[3] - bx[0]), T(bx[4] - bx[1]), T(bx[5] - bx[2]) };
+                rel = G::box_plane(bx, bsize, pl[0], pl + 1, a.tol);
+              }
+              else
+                rel = G::point_plane(tv.geom + u64(e) * 3, pl[0], pl + 1, a.tol);
+              hit = KIND == kPlane ? rel == 1 : rel != 0;
             }
             else
             {
@@ -400,6 +427,13 @@ int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol,
   return launch_batch<T, kFrustum>(BatchArgs<T, kFrustum>{ tv, planes, np, nq, 0, tol, T(0), T(0), out, work, err }, shape, st);
 }
 template<typename T>
+int batch_plane(const TreeView<T>& tv, const T* planes, u32 nq, bool positive, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape)
+{
+  if (positive)
+    return launch_batch<T, kPlanePositive>(BatchArgs<T, kPlanePositive>{ tv, planes, 1, nq, 0, tol, T(0), T(0), out, work, err }, shape, st);
+  return launch_batch<T, kPlane>(BatchArgs<T, kPlane>{ tv, planes, 1, nq, 0, tol, T(0), T(0), out, work, err }, shape, st);
+}
+template<typename T>
 int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st,
                   int shape)
 {
@@ -410,6 +444,8 @@ template int batch_range<double>(const TreeView<double>&, const double*, u32, in
 template int batch_range<float>(const TreeView<float>&, const float*, u32, int, float, Appender, u32*, u32*, cudaStream_t, int);
 template int batch_frustum<double>(const TreeView<double>&, const double*, u32, u32, double, Appender, u32*, u32*, cudaStream_t, int);
 template int batch_frustum<float>(const TreeView<float>&, const float*, u32, u32, float, Appender, u32*, u32*, cudaStream_t, int);
+template int batch_plane<double>(const TreeView<double>&, const double*, u32, bool, double, Appender, u32*, u32*, cudaStream_t, int);
+template int batch_plane<float>(const TreeView<float>&, const float*, u32, bool, float, Appender, u32*, u32*, cudaStream_t, int);
 template int batch_ray_all<double>(const TreeView<double>&, const double*, u32, double, double, double, Appender, u32*, u32*, cudaStream_t, int);
 template int batch_ray_all<float>(const TreeView<float>&, const float*, u32, float, float, float, Appender, u32*, u32*, cudaStream_t, int);
 

@@ -305,6 +305,20 @@ extern "C"
                      [&](ResultState& r) { return query_frustum(t->s, planes, planes_per_query, nq, tol, algo, r, mem, (cudaStream_t)stream); });
   }
 
+  int otg_plane_search(const otg_tree* t, const void* planes, uint64_t nq, double tol, int algo, otg_result** out, int mem, void* stream)
+  {
+    if (nq && !planes)
+      return OTG_ERR_INVALID_ARGUMENT;
+    return run_query(t, out, (cudaStream_t)stream, [&](ResultState& r) { return query_plane(t->s, planes, nq, false, tol, algo, r, mem, (cudaStream_t)stream); });
+  }
+
+  int otg_plane_positive_segmentation(const otg_tree* t, const void* planes, uint64_t nq, double tol, int algo, otg_result** out, int mem, void* stream)
+  {
+    if (nq && !planes)
+      return OTG_ERR_INVALID_ARGUMENT;
+    return run_query(t, out, (cudaStream_t)stream, [&](ResultState& r) { return query_plane(t->s, planes, nq, true, tol, algo, r, mem, (cudaStream_t)stream); });
+  }
+
   int otg_ray_all(const otg_tree* t, const void* rays, uint64_t nq, double tol, double tol_increment, double max_distance, int algo, otg_result** out,
                   int mem, void* stream)
   {

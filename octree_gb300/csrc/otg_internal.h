@@ -202,6 +202,9 @@ int query_range(const TreeState& t, const void* ranges, u64 nq, int mode, double
 int query_pick(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st, const u32* qTree = nullptr);
 int query_knn(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAll, double maxDist, double tol, int algo, ResultState& r, int mem,
               cudaStream_t st, const u32* qTree = nullptr);
+// one plane {origoDistance, nx, ny, nz} per query: PlaneSearch, or PlanePositiveSegmentation (positive)
+int query_plane(const TreeState& t, const void* planes, u64 nq, bool positive, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
+                const u32* qTree = nullptr);
 int query_frustum(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
                   const u32* qTree = nullptr);
 int query_ray(const TreeState& t, const void* rays, u64 nq, double tol, double tolInc, double maxDist, bool first, int algo, ResultState& r,

@@ -6,6 +6,8 @@
 //   RangeSearch         core/ot_query.h:476-583
 //   PickSearch          core/ot_query.h:425-466
 //   FrustumCulling      core/ot_query.h:767-833
+//   PlaneSearch         core/ot_query.h:612-636
+//   PlanePositiveSegmentation core/ot_query.h:687-744
 //   GetNearestNeighbors core/ot_query.h:1208-1270
 //   RayIntersectedAll   core/ot_query.h:1928-2022
 //   RayIntersectedFirst core/ot_query.h:2035-2146
@@ -243,6 +245,73 @@ __global__ void __launch_bounds__(128) frustum_plain_kernel(TreeView<T> tv, cons
         neg = rel == 0;
       }
       if (!neg)
+        out.put(q, (tv.ids[e] - idBase));
+    }
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 c = 0; c < cc; ++c)
+      stack[sp++] = fc + c;
+  }
+}
+
+// ---------------------------------------------------------------- PlaneSearch / PlanePositiveSegmentation (plain)
+// One plane {origoDistance, nx, ny, nz} per query. PlaneSearch enters the nodes the plane hits and
+// keeps the entities it hits; PlanePositiveSegmentation prunes negative nodes, takes a positive
+// node's whole subtree untested and keeps the entities of hit nodes that are not negative.
+template<typename T>
+__global__ void __launch_bounds__(128) plane_plain_kernel(TreeView<T> tv, const T* __restrict__ planes, u32 nq, int positive, T tol, Appender out,
+                                                          u32* err)
+{
+  using G = GeoD<T>;
+  const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq)
+    return;
+  const u32 root = query_root(tv, q);
+  const u32 idBase = id_base(tv, root);
+  const T* pl = planes + u64(q) * 4;
+  u32 stack[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp++] = root;
+  while (sp > 0)
+  {
+    const u32 node = stack[--sp];
+    const T* nb = tv.nodeBox + u64(node) * 6;
+    const int rel = G::box_plane(nb, nb + 3, pl[0], pl + 1, tol);
+    if (positive ? rel == 0 : rel != 1)
+      continue;
+    const uint4 L = tv.link[node];
+    if (L.z > tv.n || L.w > tv.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    if (positive && rel == 2)
+    {
+      // the whole subtree, untested (:711-726); a subtree is one run of sortedIds
+      const u32 len = L.w - L.y;
+      u64 pos = out.reserve(len);
+      for (u32 i = 0; i < len; ++i)
+        if (pos + i < out.capacity)
+          out.items[pos + i] = (u64(q) << 32) | (tv.ids[L.y + i] - idBase);
+      continue;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      int er; // :586-602 GetEntityPlaneRelation
+      if (tv.isBox)
+      {
+        const T* b = tv.geom + u64(e) * 6;
+        T bsize[3] = { T(b[3] - b[0]), T(b[4] - b[1]), T(b[5] - b[2]) };
+        er = G::box_plane(b, bsize, pl[0], pl + 1, tol);
+      }
+      else
+        er = G::point_plane(tv.geom + u64(e) * 3, pl[0], pl + 1, tol);
+      if (positive ? er != 0 : er == 1)
         out.put(q, (tv.ids[e] - idBase));
     }
     const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
@@ -1203,6 +1272,49 @@ static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, 
 }
 
 template<typename T>
+static int plane_impl(const TreeState& t, const void* planes, u64 nq, bool positive, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
+                      const u32* qTree)
+{
+  DevBuf in;
+  const void* d;
+  if (int rc = stage_input(in, planes, sizeof(T) * 4 * nq, mem, st, d))
+    return rc;
+  if (t.n == 0 || nq == 0)
+    return empty_result(nq, r, false, st);
+  Collected c;
+  auto tv = view<T>(t, qTree);
+  T tl = tol_of<T>(tol);
+  DevBuf work;
+  if (cudaError_t e = work.ensure(sizeof(u32)))
+    return cuda_status(e, "allocating the work counter");
+  int launchRc = OTG_OK;
+  int rc = collect(
+    c, false, std::max<u64>(nq * 64, positive ? t.n : t.n / 16),
+    [&](Appender a, u32* err) {
+      if (algo == OTG_ALGO_PLAIN_FP64)
+        plane_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), positive ? 1 : 0, tl, a, err);
+      else
+        launchRc = tune_run(query_key(positive ? "plane positive" : "plane", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st,
+                            [&](int shape) {
+                              cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
+                              cudaMemsetAsync(err, 0, sizeof(u32), st);
+                              if (shape == 0)
+                              {
+                                plane_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), positive ? 1 : 0, tl, a, err);
+                                return cuda_status(cudaGetLastError(), "launching the plane search");
+                              }
+                              return batch_plane<T>(tv, (const T*)d, u32(nq), positive, tl, a, work.as<u32>(), err, st, shape);
+                            });
+    },
+    st);
+  if (launchRc)
+    return launchRc;
+  if (rc)
+    return rc;
+  return finish_sorted_ids(c, nq, r, st);
+}
+
+template<typename T>
 static int knn_impl(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAll, double maxDist, double tol, int algo, ResultState& r, int mem,
                     cudaStream_t st, const u32* qTree)
 {
@@ -1384,6 +1496,12 @@ int query_knn(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAl
 {
   return t.scalar == OTG_SCALAR_F64 ? knn_impl<double>(t, pts, nq, k, kAll, maxDist, tol, algo, r, mem, st, qTree)
                                     : knn_impl<float>(t, pts, nq, k, kAll, maxDist, tol, algo, r, mem, st, qTree);
+}
+int query_plane(const TreeState& t, const void* planes, u64 nq, bool positive, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
+                const u32* qTree)
+{
+  return t.scalar == OTG_SCALAR_F64 ? plane_impl<double>(t, planes, nq, positive, tol, algo, r, mem, st, qTree)
+                                    : plane_impl<float>(t, planes, nq, positive, tol, algo, r, mem, st, qTree);
 }
 int query_frustum(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
                   const u32* qTree)

@@ -183,6 +183,8 @@ int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol,
 template<typename T>
 int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4);
 template<typename T>
+int batch_plane(const TreeView<T>& tv, const T* planes, u32 nq, bool positive, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4);
+template<typename T>
 int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st,
                   int shape = 4);
 

@@ -948,6 +948,60 @@ public:
     return found;
   }
 
+  // relation of one entity to a plane: ot_query.h:586-602 GetEntityPlaneRelation
+  PlaneRel entity_plane(u32 id, const T* pl, T tol) const
+  {
+    if (isBox)
+    {
+      const T* b = ent(id);
+      T bsize[3] = { T(b[3] - b[0]), T(b[4] - b[1]), T(b[5] - b[2]) };
+      return G::box_plane(b, bsize, pl[0], pl + 1, tol);
+    }
+    return G::point_plane(ent(id), pl[0], pl + 1, tol);
+  }
+
+  // ot_query.h:612-636 PlaneSearch (plane: {origoDistance, nx, ny, nz}): nodes the plane hits, their
+  // entities the plane hits
+  std::vector<u32> plane_search(const T* pl, T tol) const
+  {
+    std::vector<u32> found;
+    dfs(
+      [&](const Node& n) {
+        if (G::box_plane(node_min(n), node_size(n), pl[0], pl + 1, tol) != PlaneRel::Hit)
+          return false;
+        for (u32 id : n.entities)
+          if (entity_plane(id, pl, tol) == PlaneRel::Hit)
+            found.push_back(id);
+        return true;
+      },
+      root());
+    return found;
+  }
+
+  // ot_query.h:687-744 PlanePositiveSegmentation: a node on the positive side gives its whole subtree
+  // untested, a node the plane hits gives its entities that are not on the negative side
+  std::vector<u32> plane_positive(const T* pl, T tol) const
+  {
+    std::vector<u32> found;
+    dfs(
+      [&](const Node& n) {
+        const PlaneRel r = G::box_plane(node_min(n), node_size(n), pl[0], pl + 1, tol);
+        if (r == PlaneRel::Negative)
+          return false;
+        if (r == PlaneRel::Positive)
+        {
+          collect_subtree(n, found);
+          return false;
+        }
+        for (u32 id : n.entities)
+          if (entity_plane(id, pl, tol) != PlaneRel::Negative)
+            found.push_back(id);
+        return true;
+      },
+      root());
+    return found;
+  }
+
   // ot_query.h:767-833 FrustumCulling (planes: np x {origoDistance, nx, ny, nz})
   std::vector<u32> frustum(const T* planes, size_t np, T tol) const
   {

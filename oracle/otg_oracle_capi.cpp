@@ -86,6 +86,15 @@ Result* frustum_impl(Tree<T>& t, const T* planes, uint64_t np, uint64_t nq, doub
   });
 }
 template<typename T>
+Result* plane_impl(Tree<T>& t, const T* planes, uint64_t nq, double tol, int positive)
+{
+  return run_queries<T>(nq, [&](uint64_t q, Result& r) {
+    auto v = positive ? t.plane_positive(planes + 4 * q, tol_or_default<T>(tol)) : t.plane_search(planes + 4 * q, tol_or_default<T>(tol));
+    std::sort(v.begin(), v.end());
+    r.ids.insert(r.ids.end(), v.begin(), v.end());
+  });
+}
+template<typename T>
 Result* knn_impl(Tree<T>& t, const T* pts, uint64_t nq, const uint32_t* k, double maxDist, double tol)
 {
   T md = maxDist < 0 ? std::numeric_limits<T>::max() : T(maxDist);
@@ -230,6 +239,12 @@ extern "C"
   {
     auto* a = (AnyTree*)h;
     return a->scalar == 0 ? pick_impl(*a->d, (const double*)pts, nq, tol) : pick_impl(*a->f, (const float*)pts, nq, tol);
+  }
+  // one plane per query; positive = 0: PlaneSearch, 1: PlanePositiveSegmentation
+  void* oro_plane(void* h, const void* planes, uint64_t nq, double tol, int positive)
+  {
+    auto* a = (AnyTree*)h;
+    return a->scalar == 0 ? plane_impl(*a->d, (const double*)planes, nq, tol, positive) : plane_impl(*a->f, (const float*)planes, nq, tol, positive);
   }
   void* oro_frustum(void* h, const void* planes, uint64_t np, uint64_t nq, double tol)
   {

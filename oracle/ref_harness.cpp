@@ -159,6 +159,19 @@ Result* frustum_impl(Tree const& t, Span ents, const T* planes, uint64_t np, uin
     r.ids.insert(r.ids.end(), v.begin(), v.end());
   });
 }
+template<typename T, typename Tree, typename Span>
+Result* plane_impl(Tree const& t, Span ents, const T* planes, uint64_t nq, double tol, int positive)
+{
+  return run_queries(nq, [&](uint64_t q, Result& r) {
+    const T* s = planes + 4 * q;
+    PlaneND<3, T> pl;
+    pl.OrigoDistance = s[0];
+    pl.Normal = { s[1], s[2], s[3] };
+    auto v = positive ? t.PlanePositiveSegmentation(pl, ents, tol_or_default<T>(tol)) : t.PlaneSearch(pl, ents, tol_or_default<T>(tol));
+    std::sort(v.begin(), v.end());
+    r.ids.insert(r.ids.end(), v.begin(), v.end());
+  });
+}
 template<typename T, bool IS_BOX, typename Tree, typename Span>
 Result* knn_impl(Tree const& t, Span ents, const T* pts, uint64_t nq, const uint32_t* k, double maxDist, double tol)
 {
@@ -327,6 +340,13 @@ extern "C"
     return with_tree((AnyRef*)h, [&](auto& t, auto ents, auto s, auto) -> Result* {
       using T = decltype(s);
       return pick_impl<T>(t, ents, (const T*)pts, nq, tol);
+    });
+  }
+  void* oro_plane(void* h, const void* planes, uint64_t nq, double tol, int positive)
+  {
+    return with_tree((AnyRef*)h, [&](auto& t, auto ents, auto s, auto) -> Result* {
+      using T = decltype(s);
+      return plane_impl<T>(t, ents, (const T*)planes, nq, tol, positive);
     });
   }
   void* oro_frustum(void* h, const void* planes, uint64_t np, uint64_t nq, double tol)

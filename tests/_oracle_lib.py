@@ -37,6 +37,7 @@ class OracleLib:
             "oro_range": (_vp, [_vp, _vp, _u64, _int, _dbl]),
             "oro_pick": (_vp, [_vp, _vp, _u64, _dbl]),
             "oro_frustum": (_vp, [_vp, _vp, _u64, _u64, _dbl]),
+            "oro_plane": (_vp, [_vp, _vp, _u64, _dbl, _int]),
             "oro_knn": (_vp, [_vp, _vp, _u64, _vp, _dbl, _dbl]),
             "oro_ray": (_vp, [_vp, _vp, _u64, _dbl, _dbl, _dbl, _int]),
             "oro_collide_self": (_vp, [_vp, _dbl]),
@@ -142,6 +143,15 @@ class OracleTree:
         planes = self._q(planes)
         nq, np_ = planes.shape[0], planes.shape[1]
         return self.o._result(self.lib.oro_frustum(self.h, _ptr(planes), np_, nq, tol))[:2]
+
+    def plane_search(self, planes, tol=-1.0):
+        """planes: (nq, 4) as {origoDistance, nx, ny, nz}, one per query."""
+        planes = self._q(planes)
+        return self.o._result(self.lib.oro_plane(self.h, _ptr(planes), planes.shape[0], tol, 0))[:2]
+
+    def plane_positive(self, planes, tol=-1.0):
+        planes = self._q(planes)
+        return self.o._result(self.lib.oro_plane(self.h, _ptr(planes), planes.shape[0], tol, 1))[:2]
 
     def knn(self, pts, k, max_dist=-1.0, tol=-1.0):
         pts = self._q(pts)

@@ -50,6 +50,27 @@ def run_case(name, ent, kind, max_depth, box, max_elem, q, ray_tol):
     out["knn_off"], out["knn_ids"], out["knn_dist"] = o, i, d
     o, i = t.frustum(q["planes"])
     out["frustum_off"], out["frustum_ids"] = o, i
+    # single planes for PlaneSearch / PlanePositiveSegmentation, from their own seed so that the
+    # earlier queries of every case stay as they were
+    prng = np.random.default_rng(sum(map(ord, name)))
+    scale = float(np.max(np.abs(ent))) if ent.size else 1.0
+    nrm = prng.normal(size=(48, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    dist = prng.random((48, 1)) * scale * 1.2 - 0.1 * scale
+    ax = np.arange(48) % 4 == 0
+    nrm[ax] = np.eye(3)[np.arange(ax.sum()) % 3]
+    dist[ax] = np.round(dist[ax] / (scale / 8)) * (scale / 8)
+    out["single_planes"] = np.concatenate([dist, nrm], 1).astype(ent.dtype)
+    o, i = t.plane_search(out["single_planes"])
+    out["plane_off"], out["plane_ids"] = o, i
+    o, i = t.plane_positive(out["single_planes"])
+    out["planepos_off"], out["planepos_ids"] = o, i
+    # a wide tolerance (1% of the extent), where points near the plane count as hit
+    out["plane_tol"] = np.float64(0.01 * scale)
+    o, i = t.plane_search(out["single_planes"], float(out["plane_tol"]))
+    out["planetol_off"], out["planetol_ids"] = o, i
+    o, i = t.plane_positive(out["single_planes"], float(out["plane_tol"]))
+    out["planepostol_off"], out["planepostol_ids"] = o, i
     for first in (0, 1):
         o, i, d = t.ray(q["rays"], first=bool(first), tol=ray_tol)
         out[f"ray{first}_off"], out[f"ray{first}_ids"], out[f"ray{first}_dist"] = o, i, d

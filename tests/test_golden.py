@@ -31,3 +31,16 @@ def test_oracle_matches_reference_fixture(name):
         assert np.array_equal(t.collide_self(), g["collide"])
         t2 = oracle().create(g["other"], kind, int(g["max_depth"]), None, int(g["max_elem"]))
         assert np.array_equal(t.collide_pair(t2), g["collide_pair"])
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_oracle_plane_queries_match_reference_fixture(name):
+    """PlaneSearch and PlanePositiveSegmentation (default and 1% tolerance) against the reference."""
+    g = load_golden(name)
+    t = oracle().create(g["entities"], int(g["kind"]), int(g["max_depth"]), g.get("box"), int(g["max_elem"]))
+    pl = g["single_planes"]
+    assert_csr_equal(t.plane_search(pl), (g["plane_off"], g["plane_ids"]), "plane search")
+    assert_csr_equal(t.plane_positive(pl), (g["planepos_off"], g["planepos_ids"]), "plane positive")
+    tol = float(g["plane_tol"])
+    assert_csr_equal(t.plane_search(pl, tol), (g["planetol_off"], g["planetol_ids"]), "plane search, wide tolerance")
+    assert_csr_equal(t.plane_positive(pl, tol), (g["planepostol_off"], g["planepostol_ids"]), "plane positive, wide tolerance")

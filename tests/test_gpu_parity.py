@@ -340,3 +340,51 @@ def test_frustum_on_plane_boundaries(dtype, tol):
             planes[q, 0] = [rng.integers(20, 60) / np.sqrt(2.0), 1 / np.sqrt(2.0), 1 / np.sqrt(2.0), 0.0]
     planes = planes.astype(dtype)
     assert_csr_equal(t.frustum_culling(planes, tol=tol)[:2], o.frustum(planes, tol=tol), f"frustum tol={tol}")
+
+
+@pytest.mark.parametrize("name", golden_cases())
+@pytest.mark.parametrize("algo", [otg.ALGO_DEFAULT, otg.ALGO_PLAIN_FP64])
+def test_gpu_plane_queries_match_reference_fixture(name, algo):
+    """PlaneSearch and PlanePositiveSegmentation (default and 1% tolerance) against the reference."""
+    g = load_golden(name)
+    t = _gpu_tree(g["entities"], int(g["kind"]), int(g["max_depth"]), g.get("box"), int(g["max_elem"]))
+    pl = g["single_planes"]
+    tol = float(g["plane_tol"])
+    assert_csr_equal(t.plane_search(pl, algo=algo)[:2], (g["plane_off"], g["plane_ids"]), "plane search")
+    assert_csr_equal(t.plane_positive_segmentation(pl, algo=algo)[:2], (g["planepos_off"], g["planepos_ids"]), "plane positive")
+    assert_csr_equal(t.plane_search(pl, tol, algo=algo)[:2], (g["planetol_off"], g["planetol_ids"]), "plane search, wide tolerance")
+    assert_csr_equal(t.plane_positive_segmentation(pl, tol, algo=algo)[:2], (g["planepostol_off"], g["planepostol_ids"]), "plane positive, wide tol")
+
+
+def _single_planes(rng, n, scale):
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    d = rng.random((n, 1)) * scale * 1.4 - 0.2 * scale
+    ax = np.arange(n) % 3 == 0  # axis-aligned planes on node faces
+    nrm[ax] = np.eye(3)[np.arange(ax.sum()) % 3]
+    d[ax] = np.round(d[ax] / (scale / 32)) * (scale / 32)
+    return np.concatenate([d, nrm], 1)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("kind", [KIND_POINTS, KIND_LOOSE_BOXES])
+def test_plane_queries_random(dtype, kind):
+    rng = np.random.default_rng(4242 + kind)
+    n = 150_000
+    if kind == KIND_POINTS:
+        ent = rng.random((n, 3)) * 100
+        D, me = 9, 16
+    else:
+        cen = rng.random((n, 3)) * 100
+        half = rng.lognormal(np.log(0.3), 0.6, (n, 3))
+        ent = np.concatenate([cen - half, cen + half], 1)
+        D, me = 7, 24
+    ent = ent.astype(dtype)
+    t = _gpu_tree(ent, kind, D, None, me)
+    o = oracle().create(ent, kind, D, None, me)
+    planes = _single_planes(rng, 300, 100).astype(dtype)
+    for tol in (-1.0, 0.25):
+        ref_s, ref_p = o.plane_search(planes, tol), o.plane_positive(planes, tol)
+        for algo in (otg.ALGO_DEFAULT, otg.ALGO_PLAIN_FP64):
+            assert_csr_equal(t.plane_search(planes, tol, algo=algo)[:2], ref_s, f"plane search tol={tol} algo={algo}")
+            assert_csr_equal(t.plane_positive_segmentation(planes, tol, algo=algo)[:2], ref_p, f"plane positive tol={tol} algo={algo}")

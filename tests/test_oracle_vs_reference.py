@@ -70,3 +70,39 @@ def test_collision_rounding_gap(dtype):
     other[:, [0, 3]] = other[:, [0, 3]] + (other[:, 3:4] - other[:, 0:1])
     a2, b2 = oracle().create(other, KIND_LOOSE_BOXES, 4, None, 4), reference().create(other, KIND_LOOSE_BOXES, 4, None, 4)
     assert np.array_equal(a.collide_pair(a2), b.collide_pair(b2))
+
+
+def _planes(rng, n, scale):
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    # offsets through the data, a share of axis-aligned planes (node faces lie on them exactly)
+    d = rng.random((n, 1)) * scale * 1.4 - 0.2 * scale
+    ax = rng.random(n) < 0.3
+    nrm[ax] = np.eye(3)[rng.integers(0, 3, ax.sum())]
+    d[ax] = np.round(d[ax] / (scale / 16)) * (scale / 16)
+    return np.concatenate([d, nrm], 1)
+
+
+@pytest.mark.parametrize("seed", range(3))
+@pytest.mark.parametrize("kind", [KIND_POINTS, KIND_LOOSE_BOXES])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_plane_search_and_segmentation(seed, kind, dtype):
+    """PlaneSearch and PlanePositiveSegmentation of the oracle against the reference's."""
+    rng = np.random.default_rng(200 + seed)
+    n = int(rng.integers(100, 3000))
+    if kind == KIND_POINTS:
+        ent = rng.random((n, 3)) * 100
+    else:
+        cen = rng.random((n, 3)) * 100
+        half = rng.random((n, 3)) * 2
+        ent = np.concatenate([cen - half, cen + half], 1)
+    ent = ent.astype(dtype)
+    D = int(rng.integers(2, 8))
+    me = int(rng.integers(1, 20))
+    a, b = oracle().create(ent, kind, D, None, me), reference().create(ent, kind, D, None, me)
+    planes = _planes(rng, 120, 100).astype(dtype)
+    for tol in (-1.0, 0.5):
+        for x, y in zip(a.plane_search(planes, tol), b.plane_search(planes, tol)):
+            assert np.array_equal(x, y)
+        for x, y in zip(a.plane_positive(planes, tol), b.plane_positive(planes, tol)):
+            assert np.array_equal(x, y)
