@@ -475,6 +475,24 @@ def run_queries(tree16, pts16_d, stream):
     for algo, name in algos:
         s = time_query(lambda: t1.knn(q, 8, algo=algo, raw=True))
         out[f"knn8_1M_10k_{name}_Mq_per_s"] = 10_000 / s / 1e6
+    # plane queries on the same tree: 10k PlaneSearch at a 0.1 tolerance (about 2k ids each) and 256
+    # PlanePositiveSegmentation (about half the points each); planes with uniform normals through the data
+    nrm = rng.normal(size=(10_000, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    through = rng.random((10_000, 3)) * 100
+    planes = torch.as_tensor(np.concatenate([(nrm * through).sum(1, keepdims=True), nrm], 1), device="cuda")
+    plane_sets = {}
+    for algo, name in ((otg.ALGO_PLAIN_FP64, "plain_fp64"), (otg.ALGO_DEFAULT, "batched")):
+        s = time_query(lambda: t1.plane_search(planes, 0.1, algo=algo, raw=True))
+        out[f"plane_search_1M_10k_{name}_Mq_per_s"] = 10_000 / s / 1e6
+        s = time_query(lambda: t1.plane_positive_segmentation(planes[:256], algo=algo, raw=True))
+        r = t1.plane_positive_segmentation(planes[:256], algo=algo, raw=True)
+        out[f"plane_positive_1M_256_{name}_ms"] = s * 1e3
+        out[f"plane_positive_1M_256_{name}_Mids_per_s"] = r.sizes()[1] / s / 1e6
+        plane_sets[name] = (t1.plane_search(planes, 0.1, algo=algo)[:2], r.to_host()[:2])
+    out["plane_results_equal_batched_vs_plain"] = bool(
+        all(np.array_equal(a, b) for x, y in zip(plane_sets["plain_fp64"], plane_sets["batched"]) for a, b in zip(x, y))
+    )
     # batched uneven kNN on the 16M tree: 1M queries from the same mixture, k in 1..64
     qk = torch.as_tensor(shell_points(1_000_000, 302), device="cuda")
     ks = torch.as_tensor(np.random.default_rng(303).integers(1, 65, 1_000_000).astype(np.int32), device="cuda")

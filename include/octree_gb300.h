@@ -148,6 +148,35 @@ int otg_plane_search(const otg_tree* tree, const void* planes, uint64_t n_querie
 int otg_plane_positive_segmentation(const otg_tree* tree, const void* planes, uint64_t n_queries, double tol, int algo, otg_result** out, int mem,
                                     void* stream);
 
+/* One condition of a combined query, the QueryCondition variant of core/ot_query.h:835-861 without
+   its callback alternatives (EntityIDCondition / EntityCondition cannot run on the GPU):
+     OTG_COND_FRUSTUM       ByInFrustum: planes [first, first + count) of `planes`, each with its
+                            isCrossingAllowed flag in `crossing_allowed`
+     OTG_COND_RANGE_INSIDE  ByWithin: box `first` of `boxes`
+     OTG_COND_RANGE_OVERLAP ByOverlaps: box `first` of `boxes`
+     OTG_COND_PLANE         ByIntersecting: plane `first`, with its own tolerance `tol` (< 0: default) */
+#define OTG_COND_FRUSTUM 0
+#define OTG_COND_RANGE_INSIDE 1
+#define OTG_COND_RANGE_OVERLAP 2
+#define OTG_COND_PLANE 3
+typedef struct otg_condition
+{
+  int32_t kind;
+  uint32_t first;
+  uint32_t count;
+  uint32_t reserved; /* 0 */
+  double tol;
+} otg_condition;
+
+/* Query<LogicalOperator::And / Or>(conditions, entities, tol) (core/ot_query.h:864-1026), batched:
+   query q combines conditions[query_offsets[q] .. query_offsets[q + 1]) with AND (logical_or = 0)
+   or OR (1). planes: n_planes planes, crossing_allowed: n_planes bytes, boxes: n_boxes boxes; all
+   arrays, conditions and offsets included, in memory space `mem`. tol applies to the frustum and
+   range conditions. Ids ascending per query. */
+int otg_query(const otg_tree* tree, const otg_condition* conditions, const uint64_t* query_offsets, uint64_t n_queries, const void* planes,
+              const uint8_t* crossing_allowed, uint64_t n_planes, const void* boxes, uint64_t n_boxes, int logical_or, double tol, int algo,
+              otg_result** out, int mem, void* stream);
+
 /* RayIntersectedAll(origin, direction, entities, tol, toleranceIncrement, maxExaminationDistance)
    (core/ot_query.h:1928-2022). max_distance < 0: unbounded; 0: no limit (reference semantics).
    Results by (enter distance, id). */

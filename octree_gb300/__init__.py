@@ -20,6 +20,9 @@ SCALAR_F64, SCALAR_F32 = 0, 1
 KIND_POINTS, KIND_BOXES = 0, 1
 RANGE_INSIDE, RANGE_OVERLAP = 0, 1
 ALGO_DEFAULT, ALGO_PLAIN_FP64, ALGO_FILTERED = 0, 1, 2
+# one condition of a combined query: the otg_condition record (include/octree_gb300.h)
+COND_DTYPE = np.dtype([("kind", "<i4"), ("first", "<u4"), ("count", "<u4"), ("reserved", "<u4"), ("tol", "<f8")])
+COND_FRUSTUM, COND_RANGE_INSIDE, COND_RANGE_OVERLAP, COND_PLANE = 0, 1, 2, 3
 
 _STATUS = {
     1: "invalid argument",
@@ -49,6 +52,7 @@ EXPORTS = [
     ("otg_frustum_culling", _int, [_vp, _vp, _u64, _u64, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_plane_search", _int, [_vp, _vp, _u64, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_plane_positive_segmentation", _int, [_vp, _vp, _u64, _dbl, _int, C.POINTER(_vp), _int, _vp]),
+    ("otg_query", _int, [_vp, _vp, _vp, _u64, _vp, _vp, _u64, _vp, _u64, _int, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_ray_all", _int, [_vp, _vp, _u64, _dbl, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_ray_first", _int, [_vp, _vp, _u64, _dbl, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_collision_self", _int, [_vp, _dbl, _int, C.POINTER(_vp), _vp]),
@@ -340,6 +344,18 @@ class Tree:
         """PlanePositiveSegmentation: planes (n_queries, 4), one per query."""
         p, mem, keep = _arg(planes, self.dtype)
         return self._query("otg_plane_positive_segmentation", [p, int(planes.shape[0]), tol, algo], mem, stream, raw)
+
+    def query(self, conds, offsets, planes=None, crossing=None, boxes=None, logical_or=False, tol=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
+        """Query<And / Or>, batched: query q combines conds[offsets[q]:offsets[q+1]] (COND_DTYPE
+        records); planes (n, 4) with crossing (n,) flags, boxes (m, 6). Host (numpy) inputs."""
+        conds = np.ascontiguousarray(conds, COND_DTYPE)
+        off = np.ascontiguousarray(offsets, np.uint64)
+        pl = np.ascontiguousarray(np.zeros((0, 4)) if planes is None else planes, self.dtype).reshape(-1, 4)
+        cr = np.ascontiguousarray(np.zeros(len(pl)) if crossing is None else crossing, np.uint8)
+        bx = np.ascontiguousarray(np.zeros((0, 6)) if boxes is None else boxes, self.dtype).reshape(-1, 6)
+        args = [conds.ctypes.data_as(_vp), off.ctypes.data_as(_vp), len(off) - 1, pl.ctypes.data_as(_vp), cr.ctypes.data_as(_vp), len(pl),
+                bx.ctypes.data_as(_vp), len(bx), int(bool(logical_or)), tol, algo]
+        return self._query("otg_query", args, MEM_HOST, stream, raw)
 
     def ray_all(self, rays, tol=-1.0, tol_increment=0.0, max_distance=-1.0, algo=ALGO_DEFAULT, stream=None, raw=False):
         p, mem, keep = _arg(rays, self.dtype)

@@ -14,6 +14,7 @@
 //   RayIntersectedAll   core/ot_query.h:1928-2022
 //   PlaneSearch         core/ot_query.h:612-636
 //   PlanePositiveSegmentation core/ot_query.h:687-744
+//   Query<And / Or>     core/ot_query.h:864-1026
 #include "otg_query.cuh"
 
 namespace otg
@@ -74,7 +75,7 @@ __device__ __forceinline__ void sink_put(WarpSink& s, Appender& out, u32 lane, b
 }
 
 // query kinds
-constexpr int kRange = 0, kFrustum = 1, kRayAll = 2, kPlane = 3, kPlanePositive = 4;
+constexpr int kRange = 0, kFrustum = 1, kRayAll = 2, kPlane = 3, kPlanePositive = 4, kQuery = 5;
 
 template<typename T, int KIND>
 struct BatchArgs
@@ -88,11 +89,13 @@ struct BatchArgs
   Appender out;
   u32* work;
   u32* err;
+  QueryProgram<T> qp; // combined queries
 };
 
 template<typename T, int KIND, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KIND> a)
 {
+  static_assert(KIND >= kRange && KIND <= kQuery, "every query kind has its own setup, node test and entity test below");
   using G = GeoD<T>;
   __shared__ u32 stackMem[WARPS][kWideStack];
   __shared__ u64 itemMem[WARPS][kItemBuf];
@@ -154,7 +157,7 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
     }
     else if constexpr (KIND == kPlane || KIND == kPlanePositive)
       pl = a.q + u64(q) * 4;
-    else
+    else if constexpr (KIND == kRayAll)
     {
       ray.make(a.q + u64(q) * 6, a.q + u64(q) * 6 + 3, a.tol, a.tolInc);
       skip = !ray.valid;
@@ -193,7 +196,9 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
         contained = rel == 2;
         return rel != 0;
       }
-      else
+      else if constexpr (KIND == kQuery)
+        return cond_combine(a.qp, q, a.err, [&](const QueryCond& c) { return cond_node(a.qp, c, nb, a.tol); });
+      else if constexpr (KIND == kRayAll)
       {
         T en, ex;
         return ray.hit_node(nb, nb + 3, en, ex);
@@ -333,7 +338,12 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
                 rel = G::point_plane(tv.geom + u64(e) * 3, pl[0], pl + 1, a.tol);
               hit = KIND == kPlane ? rel == 1 : rel != 0;
             }
-            else
+            else if constexpr (KIND == kQuery)
+            {
+              const T* g = tv.geom + u64(e) * (tv.isBox ? 6 : 3);
+              hit = cond_combine(a.qp, q, a.err, [&](const QueryCond& c) { return cond_entity(a.qp, c, g, tv.isBox != 0, a.tol); });
+            }
+            else if constexpr (KIND == kRayAll)
             {
               T en, ex;
               hit = (tv.isBox ? ray.hit_box(tv.geom + u64(e) * 6, en, ex) : ray.hit_point(tv.geom + u64(e) * 3, en, ex)) &&
@@ -434,6 +444,13 @@ int batch_plane(const TreeView<T>& tv, const T* planes, u32 nq, bool positive, T
   return launch_batch<T, kPlane>(BatchArgs<T, kPlane>{ tv, planes, 1, nq, 0, tol, T(0), T(0), out, work, err }, shape, st);
 }
 template<typename T>
+int batch_query_program(const TreeView<T>& tv, const QueryProgram<T>& qp, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape)
+{
+  BatchArgs<T, kQuery> a{ tv, nullptr, 0, nq, 0, tol, T(0), T(0), out, work, err };
+  a.qp = qp;
+  return launch_batch<T, kQuery>(a, shape, st);
+}
+template<typename T>
 int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st,
                   int shape)
 {
@@ -446,6 +463,8 @@ template int batch_frustum<double>(const TreeView<double>&, const double*, u32, 
 template int batch_frustum<float>(const TreeView<float>&, const float*, u32, u32, float, Appender, u32*, u32*, cudaStream_t, int);
 template int batch_plane<double>(const TreeView<double>&, const double*, u32, bool, double, Appender, u32*, u32*, cudaStream_t, int);
 template int batch_plane<float>(const TreeView<float>&, const float*, u32, bool, float, Appender, u32*, u32*, cudaStream_t, int);
+template int batch_query_program<double>(const TreeView<double>&, const QueryProgram<double>&, u32, double, Appender, u32*, u32*, cudaStream_t, int);
+template int batch_query_program<float>(const TreeView<float>&, const QueryProgram<float>&, u32, float, Appender, u32*, u32*, cudaStream_t, int);
 template int batch_ray_all<double>(const TreeView<double>&, const double*, u32, double, double, double, Appender, u32*, u32*, cudaStream_t, int);
 template int batch_ray_all<float>(const TreeView<float>&, const float*, u32, float, float, float, Appender, u32*, u32*, cudaStream_t, int);
 

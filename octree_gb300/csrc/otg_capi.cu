@@ -319,6 +319,21 @@ extern "C"
     return run_query(t, out, (cudaStream_t)stream, [&](ResultState& r) { return query_plane(t->s, planes, nq, true, tol, algo, r, mem, (cudaStream_t)stream); });
   }
 
+  int otg_query(const otg_tree* t, const otg_condition* conditions, const uint64_t* query_offsets, uint64_t nq, const void* planes,
+                const uint8_t* crossing_allowed, uint64_t n_planes, const void* boxes, uint64_t n_boxes, int logical_or, double tol, int algo,
+                otg_result** out, int mem, void* stream)
+  {
+    static_assert(sizeof(otg_condition) == 24, "otg_condition is the 24-byte record the kernels read");
+    if (nq && !query_offsets)
+      return OTG_ERR_INVALID_ARGUMENT;
+    if ((n_planes && (!planes || !crossing_allowed)) || (n_boxes && !boxes))
+      return OTG_ERR_INVALID_ARGUMENT;
+    return run_query(t, out, (cudaStream_t)stream, [&](ResultState& r) {
+      return query_combined(t->s, conditions, query_offsets, nq, planes, crossing_allowed, n_planes, boxes, n_boxes, logical_or, tol, algo, r, mem,
+                            (cudaStream_t)stream);
+    });
+  }
+
   int otg_ray_all(const otg_tree* t, const void* rays, uint64_t nq, double tol, double tol_increment, double max_distance, int algo, otg_result** out,
                   int mem, void* stream)
   {

@@ -202,6 +202,9 @@ int query_range(const TreeState& t, const void* ranges, u64 nq, int mode, double
 int query_pick(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st, const u32* qTree = nullptr);
 int query_knn(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAll, double maxDist, double tol, int algo, ResultState& r, int mem,
               cudaStream_t st, const u32* qTree = nullptr);
+// combined queries (otg_query): conds in the otg_condition layout, query q holds [off[q], off[q + 1])
+int query_combined(const TreeState& t, const void* conds, const u64* off, u64 nq, const void* planes, const unsigned char* cross, u64 nPlanes,
+                   const void* boxes, u64 nBoxes, int orOp, double tol, int algo, ResultState& r, int mem, cudaStream_t st);
 // one plane {origoDistance, nx, ny, nz} per query: PlaneSearch, or PlanePositiveSegmentation (positive)
 int query_plane(const TreeState& t, const void* planes, u64 nq, bool positive, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
                 const u32* qTree = nullptr);

@@ -8,6 +8,7 @@
 //   FrustumCulling      core/ot_query.h:767-833
 //   PlaneSearch         core/ot_query.h:612-636
 //   PlanePositiveSegmentation core/ot_query.h:687-744
+//   Query<And / Or>     core/ot_query.h:864-1026
 //   GetNearestNeighbors core/ot_query.h:1208-1270
 //   RayIntersectedAll   core/ot_query.h:1928-2022
 //   RayIntersectedFirst core/ot_query.h:2035-2146
@@ -312,6 +313,51 @@ __global__ void __launch_bounds__(128) plane_plain_kernel(TreeView<T> tv, const 
       else
         er = G::point_plane(tv.geom + u64(e) * 3, pl[0], pl + 1, tol);
       if (positive ? er != 0 : er == 1)
+        out.put(q, (tv.ids[e] - idBase));
+    }
+    const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
+    if (sp + int(cc) > kStack || (cc && u64(fc) + cc > tv.nNodes) || ++visits > tv.nNodes)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 c = 0; c < cc; ++c)
+      stack[sp++] = fc + c;
+  }
+}
+
+// ---------------------------------------------------------------- Query<And / Or> (plain)
+// A node is entered when its conditions pass (all under And, any under Or), and its own entities are
+// kept when theirs pass; there is no whole-subtree shortcut, as in the reference.
+template<typename T>
+__global__ void __launch_bounds__(128) query_plain_kernel(TreeView<T> tv, QueryProgram<T> qp, u32 nq, T tol, Appender out, u32* err)
+{
+  const u32 q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq)
+    return;
+  const u32 root = query_root(tv, q);
+  const u32 idBase = id_base(tv, root);
+  const u32 W = tv.isBox ? 6 : 3;
+  u32 stack[kStack];
+  int sp = 0;
+  u32 visits = 0;
+  stack[sp++] = root;
+  while (sp > 0)
+  {
+    const u32 node = stack[--sp];
+    const T* nb = tv.nodeBox + u64(node) * 6;
+    if (!cond_combine(qp, q, err, [&](const QueryCond& c) { return cond_node(qp, c, nb, tol); }))
+      continue;
+    const uint4 L = tv.link[node];
+    if (L.z > tv.n || L.w > tv.n || L.y > L.z)
+    {
+      atomicOr(err, kErrStack);
+      return;
+    }
+    for (u32 e = L.y; e < L.z; ++e)
+    {
+      const T* g = tv.geom + u64(e) * W;
+      if (cond_combine(qp, q, err, [&](const QueryCond& c) { return cond_entity(qp, c, g, tv.isBox != 0, tol); }))
         out.put(q, (tv.ids[e] - idBase));
     }
     const u32 fc = L.x & kFirstChildMask, cc = L.x >> kChildShift;
@@ -988,6 +1034,11 @@ static int check_err(const DevBuf& err, cudaStream_t st)
     set_error("k above the supported maximum of 256");
     return OTG_ERR_NOT_SUPPORTED;
   }
+  if (h & kErrArgument)
+  {
+    set_error("a query condition names a plane or box outside the given arrays, or an unknown kind");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
   return OTG_OK;
 }
 
@@ -1314,6 +1365,101 @@ static int plane_impl(const TreeState& t, const void* planes, u64 nq, bool posit
   return finish_sorted_ids(c, nq, r, st);
 }
 
+// conditions given in host memory are checked here; device conditions are checked by the kernels
+static int check_program_host(const QueryCond* conds, const u64* off, u64 nq, u64 nPlanes, u64 nBoxes)
+{
+  for (u64 q = 0; q < nq; ++q)
+    if (off[q + 1] < off[q])
+    {
+      set_error("query offsets must not decrease");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+  for (u64 i = off[0]; i < off[nq]; ++i)
+  {
+    const QueryCond& c = conds[i];
+    const bool ok = c.kind == kCondFrustum ? u64(c.first) + c.count <= nPlanes
+                    : c.kind == kCondPlane ? c.first < nPlanes
+                    : (c.kind == kCondRangeInside || c.kind == kCondRangeOverlap) ? c.first < nBoxes
+                                                                                   : false;
+    if (!ok)
+    {
+      set_error("query condition " + std::to_string(i) + ": unknown kind, or planes / box outside the given arrays");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+  }
+  return OTG_OK;
+}
+
+template<typename T>
+static int query_impl(const TreeState& t, const QueryCond* conds, const u64* off, u64 nq, const void* planes, const unsigned char* cross, u64 nPlanes,
+                      const void* boxes, u64 nBoxes, int orOp, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+{
+  u64 nConds = 0;
+  if (nq)
+  {
+    if (mem == OTG_MEM_HOST)
+    {
+      nConds = off[nq];
+      if (int rc = check_program_host(conds, off, nq, nPlanes, nBoxes))
+        return rc;
+    }
+    else
+    {
+      cudaError_t e = cudaMemcpyAsync(&nConds, off + nq, sizeof(u64), cudaMemcpyDeviceToHost, st);
+      if (!e)
+        e = cudaStreamSynchronize(st);
+      if (e)
+        return cuda_status(e, "reading the condition count");
+    }
+  }
+  DevBuf inC, inO, inP, inX, inB;
+  const void *dC, *dO, *dP, *dX, *dB;
+  if (int rc = stage_input(inC, conds, sizeof(QueryCond) * nConds, mem, st, dC))
+    return rc;
+  if (int rc = stage_input(inO, off, sizeof(u64) * (nq + 1), mem, st, dO))
+    return rc;
+  if (int rc = stage_input(inP, planes, sizeof(T) * 4 * nPlanes, mem, st, dP))
+    return rc;
+  if (int rc = stage_input(inX, cross, nPlanes, mem, st, dX))
+    return rc;
+  if (int rc = stage_input(inB, boxes, sizeof(T) * 6 * nBoxes, mem, st, dB))
+    return rc;
+  if (t.n == 0 || nq == 0)
+    return empty_result(nq, r, false, st);
+  QueryProgram<T> qp{ (const QueryCond*)dC, (const u64*)dO, (const T*)dP, (const unsigned char*)dX, (const T*)dB, nConds, nPlanes, nBoxes, orOp ? 1 : 0 };
+  Collected c;
+  auto tv = view<T>(t, nullptr);
+  T tl = tol_of<T>(tol);
+  DevBuf work;
+  if (cudaError_t e = work.ensure(sizeof(u32)))
+    return cuda_status(e, "allocating the work counter");
+  int launchRc = OTG_OK;
+  int rc = collect(
+    c, false, std::max<u64>(nq * 64, t.n / 4),
+    [&](Appender a, u32* err) {
+      if (algo == OTG_ALGO_PLAIN_FP64)
+        query_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, qp, u32(nq), tl, a, err);
+      else
+        launchRc = tune_run(query_key(orOp ? "query or" : "query and", algo, false, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st,
+                            [&](int shape) {
+                              cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
+                              cudaMemsetAsync(err, 0, sizeof(u32), st);
+                              if (shape == 0)
+                              {
+                                query_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, qp, u32(nq), tl, a, err);
+                                return cuda_status(cudaGetLastError(), "launching the combined query");
+                              }
+                              return batch_query_program<T>(tv, qp, u32(nq), tl, a, work.as<u32>(), err, st, shape);
+                            });
+    },
+    st);
+  if (launchRc)
+    return launchRc;
+  if (rc)
+    return rc;
+  return finish_sorted_ids(c, nq, r, st);
+}
+
 template<typename T>
 static int knn_impl(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAll, double maxDist, double tol, int algo, ResultState& r, int mem,
                     cudaStream_t st, const u32* qTree)
@@ -1496,6 +1642,13 @@ int query_knn(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAl
 {
   return t.scalar == OTG_SCALAR_F64 ? knn_impl<double>(t, pts, nq, k, kAll, maxDist, tol, algo, r, mem, st, qTree)
                                     : knn_impl<float>(t, pts, nq, k, kAll, maxDist, tol, algo, r, mem, st, qTree);
+}
+int query_combined(const TreeState& t, const void* conds, const u64* off, u64 nq, const void* planes, const unsigned char* cross, u64 nPlanes,
+                   const void* boxes, u64 nBoxes, int orOp, double tol, int algo, ResultState& r, int mem, cudaStream_t st)
+{
+  const QueryCond* c = static_cast<const QueryCond*>(conds);
+  return t.scalar == OTG_SCALAR_F64 ? query_impl<double>(t, c, off, nq, planes, cross, nPlanes, boxes, nBoxes, orOp, tol, algo, r, mem, st)
+                                    : query_impl<float>(t, c, off, nq, planes, cross, nPlanes, boxes, nBoxes, orOp, tol, algo, r, mem, st);
 }
 int query_plane(const TreeState& t, const void* planes, u64 nq, bool positive, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
                 const u32* qTree)

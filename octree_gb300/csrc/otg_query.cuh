@@ -59,6 +59,133 @@ struct Appender
   __device__ __forceinline__ u64 reserve(u64 len) { return atomicAdd(count, (unsigned long long)len); }
 };
 
+// ---- combined queries (core/ot_query.h:835-1026): conditions of the otg_condition layout
+struct QueryCond
+{
+  int kind;
+  u32 first;
+  u32 count;
+  u32 reserved;
+  double tol;
+};
+constexpr int kCondFrustum = OTG_COND_FRUSTUM, kCondRangeInside = OTG_COND_RANGE_INSIDE, kCondRangeOverlap = OTG_COND_RANGE_OVERLAP,
+              kCondPlane = OTG_COND_PLANE;
+
+template<typename T>
+struct QueryProgram
+{
+  const QueryCond* conds;
+  const u64* off;    // conditions of query q: [off[q], off[q + 1])
+  const T* planes;   // {origo distance, normal} per plane
+  const unsigned char* cross; // isCrossingAllowed per plane
+  const T* boxes;
+  u64 nConds, nPlanes, nBoxes;
+  int orOp;
+};
+
+// whether condition c names planes / a box inside the arrays (a bad one reads nothing)
+template<typename T>
+__device__ __forceinline__ bool cond_valid(const QueryProgram<T>& qp, const QueryCond& c)
+{
+  if (c.kind == kCondFrustum)
+    return u64(c.first) + c.count <= qp.nPlanes;
+  if (c.kind == kCondPlane)
+    return c.first < qp.nPlanes;
+  if (c.kind == kCondRangeInside || c.kind == kCondRangeOverlap)
+    return c.first < qp.nBoxes;
+  return false;
+}
+
+// ot_query.h:893-916: node selection of one condition (node {min xyz, size xyz})
+template<typename T>
+__device__ __forceinline__ bool cond_node(const QueryProgram<T>& qp, const QueryCond& c, const T* nb, T tol)
+{
+  using G = GeoD<T>;
+  if (c.kind == kCondFrustum)
+  {
+    for (u32 i = c.first; i < c.first + c.count; ++i)
+    {
+      const int rel = G::box_plane(nb, nb + 3, qp.planes[4 * u64(i)], qp.planes + 4 * u64(i) + 1, tol);
+      if (rel == 1)
+        return true;
+      if (rel == 0)
+        return false;
+    }
+    return true;
+  }
+  if (c.kind == kCondPlane)
+  {
+    const T ptol = c.tol < 0 ? base_tol<T>() : T(c.tol);
+    return G::box_plane(nb, nb + 3, qp.planes[4 * u64(c.first)], qp.planes + 4 * u64(c.first) + 1, ptol) == 1;
+  }
+  const T* r = qp.boxes + 6 * u64(c.first);
+  T rsize[3] = { T(r[3] - r[0]), T(r[4] - r[1]), T(r[5] - r[2]) };
+  T nmin[3] = { nb[0], nb[1], nb[2] }, nsize[3] = { nb[3], nb[4], nb[5] };
+  return G::overlap_by_min_point(r, rsize, nmin, nsize, tol);
+}
+
+// ot_query.h:949-998: entity selection of one condition (g: the entity's point or box)
+template<typename T>
+__device__ __forceinline__ bool cond_entity(const QueryProgram<T>& qp, const QueryCond& c, const T* g, bool isBox, T tol)
+{
+  using G = GeoD<T>;
+  auto rel = [&](const T* pl, T t) {
+    if (isBox)
+    {
+      T bsize[3] = { T(g[3] - g[0]), T(g[4] - g[1]), T(g[5] - g[2]) };
+      return G::box_plane(g, bsize, pl[0], pl + 1, t);
+    }
+    return G::point_plane(g, pl[0], pl + 1, t);
+  };
+  if (c.kind == kCondFrustum)
+  {
+    for (u32 i = c.first; i < c.first + c.count; ++i)
+    {
+      const int r = rel(qp.planes + 4 * u64(i), tol);
+      if (r == 0 || (r == 1 && !qp.cross[i]))
+        return false;
+    }
+    return true;
+  }
+  if (c.kind == kCondPlane)
+    return rel(qp.planes + 4 * u64(c.first), c.tol < 0 ? base_tol<T>() : T(c.tol)) == 1;
+  T r[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+    r[k] = qp.boxes[6 * u64(c.first) + k];
+  if (!isBox)
+    return G::box_contains_point(r, g, tol);
+  return c.kind == kCondRangeInside ? G::contains_box_no_tol(r, g) : G::box_relation(r, g, tol) == -1;
+}
+
+// the conditions of query q over a node (node) or an entity (entity): all of them (And) or any (Or);
+// no condition passes every node and entity under And and none under Or
+template<typename T, typename F>
+__device__ __forceinline__ bool cond_combine(const QueryProgram<T>& qp, u32 q, u32* err, F&& test)
+{
+  const u64 c0 = qp.off[q], c1 = qp.off[q + 1];
+  if (c1 < c0 || c1 > qp.nConds)
+  {
+    atomicOr(err, kErrArgument);
+    return false;
+  }
+  for (u64 i = c0; i < c1; ++i)
+  {
+    const QueryCond c = qp.conds[i];
+    if (!cond_valid(qp, c))
+    {
+      atomicOr(err, kErrArgument);
+      return false;
+    }
+    const bool ok = test(c);
+    if (qp.orOp && ok)
+      return true;
+    if (!qp.orOp && !ok)
+      return false;
+  }
+  return !qp.orOp;
+}
+
 template<typename T>
 __device__ __forceinline__ void load_box(const T* p, T b[6])
 {
@@ -184,6 +311,9 @@ template<typename T>
 int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4);
 template<typename T>
 int batch_plane(const TreeView<T>& tv, const T* planes, u32 nq, bool positive, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4);
+template<typename T>
+int batch_query_program(const TreeView<T>& tv, const QueryProgram<T>& qp, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st,
+                        int shape = 4);
 template<typename T>
 int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st,
                   int shape = 4);

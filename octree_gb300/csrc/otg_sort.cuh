@@ -31,6 +31,7 @@ constexpr int kLookbackBatch = 8;
 constexpr u32 kErrTimeout = 1u;
 constexpr u32 kErrCapacity = 2u;
 constexpr u32 kErrStack = 4u;
+constexpr u32 kErrArgument = 8u; // an input index out of range (reported, never followed)
 
 __device__ __forceinline__ u32 lanemask_lt()
 {

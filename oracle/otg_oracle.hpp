@@ -1002,6 +1002,117 @@ public:
     return found;
   }
 
+  // one condition of Query (ot_query.h:835-861): kind 0 frustum (planes [first, first + count),
+  // each with its crossing flag), 1 range Inside, 2 range Overlap (box `first`), 3 plane intersection
+  // (plane `first`, own tolerance tol, < 0: the default)
+  struct Cond
+  {
+    int kind;
+    u32 first;
+    u32 count;
+    double tol;
+  };
+  static constexpr int kCondFrustum = 0, kCondRangeInside = 1, kCondRangeOverlap = 2, kCondPlane = 3;
+
+  // ot_query.h:893-916 node selection of one condition
+  bool cond_node(const Cond& c, const Node& n, const T* planes, const T* boxes, T tol) const
+  {
+    if (c.kind == kCondFrustum)
+    {
+      for (u32 i = c.first; i < c.first + c.count; ++i)
+      {
+        const PlaneRel r = G::box_plane(node_min(n), node_size(n), planes[4 * i], planes + 4 * i + 1, tol);
+        if (r == PlaneRel::Hit)
+          return true;
+        if (r == PlaneRel::Negative)
+          return false;
+      }
+      return true;
+    }
+    if (c.kind == kCondPlane)
+    {
+      const T ptol = c.tol < 0 ? base_tolerance<T>() : T(c.tol);
+      return G::box_plane(node_min(n), node_size(n), planes[4 * c.first], planes + 4 * c.first + 1, ptol) == PlaneRel::Hit;
+    }
+    const T* r = boxes + 6 * u64(c.first);
+    T rsize[3] = { T(r[3] - r[0]), T(r[4] - r[1]), T(r[5] - r[2]) };
+    return G::overlap_by_min_point(r, rsize, node_min(n), node_size(n), tol);
+  }
+
+  // ot_query.h:949-998 entity selection of one condition
+  bool cond_entity(const Cond& c, u32 id, const T* planes, const unsigned char* cross, const T* boxes, T tol) const
+  {
+    if (c.kind == kCondFrustum)
+    {
+      for (u32 i = c.first; i < c.first + c.count; ++i)
+      {
+        const PlaneRel r = entity_plane(id, planes + 4 * i, tol);
+        if (r == PlaneRel::Negative || (r == PlaneRel::Hit && !cross[i]))
+          return false;
+      }
+      return true;
+    }
+    if (c.kind == kCondPlane)
+    {
+      const T ptol = c.tol < 0 ? base_tolerance<T>() : T(c.tol);
+      return entity_plane(id, planes + 4 * c.first, ptol) == PlaneRel::Hit;
+    }
+    const T* r = boxes + 6 * u64(c.first);
+    if (!isBox)
+      return G::box_contains_point(r, ent(id), tol);
+    return c.kind == kCondRangeInside ? G::contains_box_no_tol(r, ent(id)) : G::overlapped_strict(r, ent(id), tol);
+  }
+
+  // ot_query.h:864-1026 Query<And / Or>: a node is entered when its conditions pass (all, or any),
+  // its entities are kept when theirs pass
+  std::vector<u32> query(const Cond* conds, size_t nc, const T* planes, const unsigned char* cross, const T* boxes, bool orOp, T tol) const
+  {
+    std::vector<u32> found;
+    dfs(
+      [&](const Node& n) {
+        bool pass = !orOp;
+        for (size_t i = 0; i < nc; ++i)
+        {
+          const bool c = cond_node(conds[i], n, planes, boxes, tol);
+          if (orOp && c)
+          {
+            pass = true;
+            break;
+          }
+          if (!orOp && !c)
+          {
+            pass = false;
+            break;
+          }
+        }
+        if (!pass)
+          return false;
+        for (u32 id : n.entities)
+        {
+          bool ok = !orOp;
+          for (size_t i = 0; i < nc; ++i)
+          {
+            const bool c = cond_entity(conds[i], id, planes, cross, boxes, tol);
+            if (orOp && c)
+            {
+              ok = true;
+              break;
+            }
+            if (!orOp && !c)
+            {
+              ok = false;
+              break;
+            }
+          }
+          if (ok)
+            found.push_back(id);
+        }
+        return true;
+      },
+      root());
+    return found;
+  }
+
   // ot_query.h:767-833 FrustumCulling (planes: np x {origoDistance, nx, ny, nz})
   std::vector<u32> frustum(const T* planes, size_t np, T tol) const
   {

@@ -94,6 +94,28 @@ Result* plane_impl(Tree<T>& t, const T* planes, uint64_t nq, double tol, int pos
     r.ids.insert(r.ids.end(), v.begin(), v.end());
   });
 }
+// one condition of a combined query, laid out as otg_condition in include/octree_gb300.h
+struct CondC
+{
+  int32_t kind;
+  uint32_t first;
+  uint32_t count;
+  uint32_t pad;
+  double tol;
+};
+template<typename T>
+Result* query_impl(Tree<T>& t, const CondC* conds, const uint64_t* off, uint64_t nq, const T* planes, const unsigned char* cross, const T* boxes,
+                   int orOp, double tol)
+{
+  return run_queries<T>(nq, [&](uint64_t q, Result& r) {
+    std::vector<typename Tree<T>::Cond> c;
+    for (uint64_t i = off[q]; i < off[q + 1]; ++i)
+      c.push_back({ conds[i].kind, conds[i].first, conds[i].count, conds[i].tol });
+    auto v = t.query(c.data(), c.size(), planes, cross, boxes, orOp != 0, tol_or_default<T>(tol));
+    std::sort(v.begin(), v.end());
+    r.ids.insert(r.ids.end(), v.begin(), v.end());
+  });
+}
 template<typename T>
 Result* knn_impl(Tree<T>& t, const T* pts, uint64_t nq, const uint32_t* k, double maxDist, double tol)
 {
@@ -245,6 +267,15 @@ extern "C"
   {
     auto* a = (AnyTree*)h;
     return a->scalar == 0 ? plane_impl(*a->d, (const double*)planes, nq, tol, positive) : plane_impl(*a->f, (const float*)planes, nq, tol, positive);
+  }
+  // combined queries: query q holds conditions [off[q], off[q + 1]); or_op 0: And, 1: Or
+  void* oro_query(void* h, const void* conds, const uint64_t* off, uint64_t nq, const void* planes, const unsigned char* cross, const void* boxes,
+                  int or_op, double tol)
+  {
+    auto* a = (AnyTree*)h;
+    const CondC* c = (const CondC*)conds;
+    return a->scalar == 0 ? query_impl(*a->d, c, off, nq, (const double*)planes, cross, (const double*)boxes, or_op, tol)
+                          : query_impl(*a->f, c, off, nq, (const float*)planes, cross, (const float*)boxes, or_op, tol);
   }
   void* oro_frustum(void* h, const void* planes, uint64_t np, uint64_t nq, double tol)
   {

@@ -172,6 +172,52 @@ Result* plane_impl(Tree const& t, Span ents, const T* planes, uint64_t nq, doubl
     r.ids.insert(r.ids.end(), v.begin(), v.end());
   });
 }
+// one condition of a combined query, laid out as otg_condition in include/octree_gb300.h
+struct CondC
+{
+  int32_t kind;
+  uint32_t first;
+  uint32_t count;
+  uint32_t pad;
+  double tol;
+};
+template<typename T, typename Tree, typename Span>
+Result* query_impl(Tree const& t, Span ents, const CondC* conds, const uint64_t* off, uint64_t nq, const T* planes, const unsigned char* cross,
+                   const T* boxes, int orOp, double tol)
+{
+  using Plane = PlaneND<3, T>;
+  auto plane = [&](uint32_t j) {
+    Plane p;
+    p.OrigoDistance = planes[4 * j];
+    p.Normal = { planes[4 * j + 1], planes[4 * j + 2], planes[4 * j + 3] };
+    return p;
+  };
+  return run_queries(nq, [&](uint64_t q, Result& r) {
+    std::vector<typename Tree::QueryCondition> c;
+    for (uint64_t i = off[q]; i < off[q + 1]; ++i)
+    {
+      const CondC& k = conds[i];
+      if (k.kind == 0)
+      {
+        std::vector<std::pair<Plane, bool>> ps;
+        for (uint32_t j = k.first; j < k.first + k.count; ++j)
+          ps.emplace_back(plane(j), cross[j] != 0);
+        c.push_back(Tree::ByInFrustum(std::move(ps)));
+      }
+      else if (k.kind == 3)
+        c.push_back(Tree::ByIntersecting(plane(k.first), k.tol < 0 ? tol_or_default<T>(-1.0) : T(k.tol)));
+      else
+      {
+        const auto& b = *reinterpret_cast<const typename Tree::TBox*>(boxes + 6 * uint64_t(k.first));
+        c.push_back(k.kind == 1 ? Tree::ByWithin(b) : Tree::ByOverlaps(b));
+      }
+    }
+    auto v = orOp ? t.template Query<LogicalOperator::Or>(c, ents, tol_or_default<T>(tol))
+                  : t.template Query<LogicalOperator::And>(c, ents, tol_or_default<T>(tol));
+    std::sort(v.begin(), v.end());
+    r.ids.insert(r.ids.end(), v.begin(), v.end());
+  });
+}
 template<typename T, bool IS_BOX, typename Tree, typename Span>
 Result* knn_impl(Tree const& t, Span ents, const T* pts, uint64_t nq, const uint32_t* k, double maxDist, double tol)
 {
@@ -347,6 +393,14 @@ extern "C"
     return with_tree((AnyRef*)h, [&](auto& t, auto ents, auto s, auto) -> Result* {
       using T = decltype(s);
       return plane_impl<T>(t, ents, (const T*)planes, nq, tol, positive);
+    });
+  }
+  void* oro_query(void* h, const void* conds, const uint64_t* off, uint64_t nq, const void* planes, const unsigned char* cross, const void* boxes,
+                  int or_op, double tol)
+  {
+    return with_tree((AnyRef*)h, [&](auto& t, auto ents, auto s, auto) -> Result* {
+      using T = decltype(s);
+      return query_impl<T>(t, ents, (const CondC*)conds, off, nq, (const T*)planes, cross, (const T*)boxes, or_op, tol);
     });
   }
   void* oro_frustum(void* h, const void* planes, uint64_t np, uint64_t nq, double tol)

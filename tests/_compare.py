@@ -57,3 +57,48 @@ def assert_nodes_equal(gpu, ref, what):
 
 def node_dict(prefix, g):
     return {k: g[prefix + k] for k in ("keys", "min", "size", "eoff", "eids")}
+
+
+def random_query_program(rng, nq, scale, dtype):
+    """Combined-query inputs: per query 0-4 conditions (frustum of 1-6 planes with random crossing
+    flags, range Inside / Overlap, plane intersection with the default or a 1% tolerance). Returns
+    (conds, offsets, planes, crossing, boxes) in the layout of otg_query."""
+    from _oracle_lib import COND_DTYPE, COND_FRUSTUM, COND_PLANE, COND_RANGE_INSIDE, COND_RANGE_OVERLAP
+
+    conds, offsets, planes, crossing, boxes = [], [0], [], [], []
+
+    def plane():
+        n = rng.normal(size=3)
+        n /= np.linalg.norm(n)
+        if rng.random() < 0.3:  # axis-aligned, on a node face
+            n = np.eye(3)[rng.integers(0, 3)]
+            return [np.round(rng.random() * 16) * scale / 16, *n]
+        return [float(n @ (rng.random(3) * scale)), *n]
+
+    for q in range(nq):
+        k = 0 if q % 17 == 0 else int(rng.integers(1, 5))
+        for _ in range(k):
+            kind = int(rng.integers(0, 4))
+            if kind == COND_FRUSTUM:
+                m = int(rng.integers(1, 7))
+                conds.append((COND_FRUSTUM, len(planes), m, 0, -1.0))
+                for _ in range(m):
+                    planes.append(plane())
+                    crossing.append(int(rng.random() < 0.5))
+            elif kind == COND_PLANE:
+                conds.append((COND_PLANE, len(planes), 1, 0, -1.0 if rng.random() < 0.5 else 0.01 * scale))
+                planes.append(plane())
+                crossing.append(0)
+            else:
+                c = rng.random(3) * scale
+                e = rng.uniform(0.05, 0.4, 3) * scale
+                conds.append((COND_RANGE_INSIDE if kind == 1 else COND_RANGE_OVERLAP, len(boxes), 1, 0, -1.0))
+                boxes.append([*(c - e / 2), *(c + e / 2)])
+        offsets.append(len(conds))
+    return (
+        np.array(conds, COND_DTYPE),
+        np.array(offsets, np.uint64),
+        np.array(planes, dtype).reshape(-1, 4),
+        np.array(crossing, np.uint8),
+        np.array(boxes, dtype).reshape(-1, 6),
+    )

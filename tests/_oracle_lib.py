@@ -11,6 +11,9 @@ ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "libotg_oracle.so")
 REF_SO = os.path.join(ROOT, "oracle", "_ref", "libref_orthotree.so")
 
 KIND_POINTS, KIND_LOOSE_BOXES, KIND_BOXES = 0, 1, 2
+# one condition of a combined query (the otg_condition record of include/octree_gb300.h)
+COND_DTYPE = np.dtype([("kind", "<i4"), ("first", "<u4"), ("count", "<u4"), ("reserved", "<u4"), ("tol", "<f8")])
+COND_FRUSTUM, COND_RANGE_INSIDE, COND_RANGE_OVERLAP, COND_PLANE = 0, 1, 2, 3
 
 _vp = C.c_void_p
 _u64 = C.c_uint64
@@ -38,6 +41,7 @@ class OracleLib:
             "oro_pick": (_vp, [_vp, _vp, _u64, _dbl]),
             "oro_frustum": (_vp, [_vp, _vp, _u64, _u64, _dbl]),
             "oro_plane": (_vp, [_vp, _vp, _u64, _dbl, _int]),
+            "oro_query": (_vp, [_vp, _vp, _vp, _u64, _vp, _vp, _vp, _int, _dbl]),
             "oro_knn": (_vp, [_vp, _vp, _u64, _vp, _dbl, _dbl]),
             "oro_ray": (_vp, [_vp, _vp, _u64, _dbl, _dbl, _dbl, _int]),
             "oro_collide_self": (_vp, [_vp, _dbl]),
@@ -152,6 +156,18 @@ class OracleTree:
     def plane_positive(self, planes, tol=-1.0):
         planes = self._q(planes)
         return self.o._result(self.lib.oro_plane(self.h, _ptr(planes), planes.shape[0], tol, 1))[:2]
+
+    def query(self, conds, offsets, planes, crossing, boxes, or_op=False, tol=-1.0):
+        """Combined queries: query q holds conds[offsets[q]:offsets[q+1]] (COND_DTYPE records);
+        planes (n, 4), crossing (n,) uint8 per plane, boxes (m, 6)."""
+        conds = np.ascontiguousarray(conds, COND_DTYPE)
+        off = np.ascontiguousarray(offsets, np.uint64)
+        planes = self._q(np.asarray(planes).reshape(-1, 4))
+        cross = np.ascontiguousarray(crossing, np.uint8)
+        boxes = self._q(np.asarray(boxes).reshape(-1, 6))
+        return self.o._result(
+            self.lib.oro_query(self.h, _ptr(conds), _ptr(off), len(off) - 1, _ptr(planes), _ptr(cross), _ptr(boxes), int(or_op), tol)
+        )[:2]
 
     def knn(self, pts, k, max_dist=-1.0, tol=-1.0):
         pts = self._q(pts)

@@ -388,3 +388,45 @@ def test_plane_queries_random(dtype, kind):
         for algo in (otg.ALGO_DEFAULT, otg.ALGO_PLAIN_FP64):
             assert_csr_equal(t.plane_search(planes, tol, algo=algo)[:2], ref_s, f"plane search tol={tol} algo={algo}")
             assert_csr_equal(t.plane_positive_segmentation(planes, tol, algo=algo)[:2], ref_p, f"plane positive tol={tol} algo={algo}")
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("kind", [KIND_POINTS, KIND_LOOSE_BOXES])
+def test_combined_query_random(dtype, kind):
+    """Query<And> / Query<Or> with frustum (crossing flags), range Inside / Overlap and plane
+    conditions, batched and plain, against the oracle."""
+    from _compare import random_query_program
+
+    rng = np.random.default_rng(777 + kind)
+    n = 120_000
+    if kind == KIND_POINTS:
+        ent = rng.random((n, 3)) * 100
+        D, me = 8, 16
+    else:
+        cen = rng.random((n, 3)) * 100
+        half = rng.lognormal(np.log(0.3), 0.6, (n, 3))
+        ent = np.concatenate([cen - half, cen + half], 1)
+        D, me = 7, 24
+    ent = ent.astype(dtype)
+    t = _gpu_tree(ent, kind, D, None, me)
+    o = oracle().create(ent, kind, D, None, me)
+    conds, off, planes, cross, boxes = random_query_program(rng, 200, 100.0, dtype)
+    for logical_or in (False, True):
+        ref = o.query(conds, off, planes, cross, boxes, or_op=logical_or)
+        assert len(ref[1]) > 0
+        for algo in (otg.ALGO_DEFAULT, otg.ALGO_PLAIN_FP64):
+            got = t.query(conds, off, planes, cross, boxes, logical_or=logical_or, algo=algo)
+            assert_csr_equal(got[:2], ref, f"query or={logical_or} algo={algo}")
+
+
+def test_combined_query_rejects_bad_conditions():
+    t = _gpu_tree(np.random.default_rng(1).random((1000, 3)), KIND_POINTS, 4, None, 8)
+    bad = np.zeros(1, otg.COND_DTYPE)
+    bad["kind"] = otg.COND_PLANE
+    bad["first"] = 3  # one plane given
+    with pytest.raises(otg.OtgError):
+        t.query(bad, [0, 1], np.array([[0.5, 1.0, 0, 0]]), np.zeros(1, np.uint8))
+    bad["kind"] = 9
+    bad["first"] = 0
+    with pytest.raises(otg.OtgError):
+        t.query(bad, [0, 1], np.array([[0.5, 1.0, 0, 0]]), np.zeros(1, np.uint8))

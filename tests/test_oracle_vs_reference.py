@@ -106,3 +106,28 @@ def test_plane_search_and_segmentation(seed, kind, dtype):
             assert np.array_equal(x, y)
         for x, y in zip(a.plane_positive(planes, tol), b.plane_positive(planes, tol)):
             assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("seed", range(3))
+@pytest.mark.parametrize("kind", [KIND_POINTS, KIND_LOOSE_BOXES, KIND_BOXES])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_combined_query(seed, kind, dtype):
+    """Query<And> and Query<Or> with frustum, range and plane conditions: oracle against reference."""
+    from _compare import random_query_program
+
+    rng = np.random.default_rng(300 + seed)
+    n = int(rng.integers(200, 3000))
+    if kind == KIND_POINTS:
+        ent = rng.random((n, 3)) * 100
+    else:
+        cen = rng.random((n, 3)) * 100
+        half = rng.random((n, 3)) * 2
+        ent = np.concatenate([cen - half, cen + half], 1)
+    ent = ent.astype(dtype)
+    D = int(rng.integers(2, 7))
+    me = int(rng.integers(1, 20))
+    a, b = oracle().create(ent, kind, D, None, me), reference().create(ent, kind, D, None, me)
+    prog = random_query_program(rng, 80, 100.0, dtype)
+    for or_op in (False, True):
+        for x, y in zip(a.query(*prog, or_op=or_op), b.query(*prog, or_op=or_op)):
+            assert np.array_equal(x, y)
