@@ -10,8 +10,9 @@
 // core/configuration.h:83). Queries have the reference's names, argument order and defaults
 // (core/ot_managed.h:584-893) and return the same id lists:
 //   PickSearch, RangeSearch, FrustumCulling, PlaneSearch / PlaneIntersection,
-//   PlanePositiveSegmentation, GetNearestNeighbors, RayIntersectedAll, RayIntersectedFirst,
-//   CollisionDetection (one tree and two trees).
+//   PlanePositiveSegmentation, Query<And / Or> (ByWithin, ByOverlaps, ByInFrustum, ByIntersecting),
+//   GetNearestNeighbors, RayIntersectedAll, RayIntersectedFirst, CollisionDetection (one tree and
+//   two trees).
 // Each query also has a batched form (…Batch) answering many query geometries in one GPU launch;
 // it returns a Csr (offsets + ids [+ distances]).
 //
@@ -24,8 +25,8 @@
 // Differences from the reference:
 //   * Errors throw OrthoTreeGPU::Error, where the reference terminates (ORTHOTREE_CRASH_IF,
 //     core/ot_base.h:104-108).
-//   * The tester / callback overloads (TTester, FCollisionDetector, entityDistanceFn) cannot run on
-//     the GPU and are not offered.
+//   * The tester / callback overloads (TTester, FCollisionDetector, entityDistanceFn) and the
+//     callback conditions of Query (BySatisfies) cannot run on the GPU and are not offered.
 //   * Execution tags are accepted and ignored: the work runs on the GPU.
 //   * There is no CPU fallback: without a CUDA device every call throws with status
 //     OTG_ERR_NO_DEVICE.
@@ -83,6 +84,13 @@ enum class RangeSearchMode
 {
   Inside = OTG_RANGE_INSIDE,
   Overlap = OTG_RANGE_OVERLAP
+};
+
+// core/types.h:69-73
+enum class LogicalOperator
+{
+  And,
+  Or
 };
 
 // query kernels: the default is the batched FP32-filtered kernel where one exists
@@ -284,6 +292,33 @@ public:
     return first(PlanePositiveSegmentationBatch(std::span<const TPlane>(&plane, 1), tolerance));
   }
 
+  // core/ot_query.h:835-861: one condition of Query (the callback conditions are not offered)
+  struct QueryCondition
+  {
+    int kind = OTG_COND_RANGE_INSIDE;
+    std::vector<std::pair<TPlane, bool>> planes; // frustum: planes with isCrossingAllowed; plane condition: its plane
+    TBox range{};
+    double tolerance = -1.0;                     // plane condition: its own tolerance
+  };
+  static QueryCondition ByWithin(const TBox& range) { return { OTG_COND_RANGE_INSIDE, {}, range, -1.0 }; }
+  static QueryCondition ByOverlaps(const TBox& range) { return { OTG_COND_RANGE_OVERLAP, {}, range, -1.0 }; }
+  static QueryCondition ByInFrustum(std::vector<std::pair<TPlane, bool>> boundaryPlanes)
+  {
+    return { OTG_COND_FRUSTUM, std::move(boundaryPlanes), {}, -1.0 };
+  }
+  static QueryCondition ByIntersecting(const TPlane& plane, double tolerance = detail::base_tolerance<TScalar>())
+  {
+    return { OTG_COND_PLANE, { { plane, false } }, {}, tolerance };
+  }
+
+  // core/ot_query.h:864-1026 Query<And / Or>(conditions, entities, tolerance)
+  template<LogicalOperator OP = LogicalOperator::And, typename TConditions>
+  std::vector<EntityID> Query(const TConditions& conditions, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    const std::vector<std::vector<QueryCondition>> one(1, std::vector<QueryCondition>(std::begin(conditions), std::end(conditions)));
+    return first(QueryBatch<OP>(one, tolerance));
+  }
+
   std::vector<EntityID> GetNearestNeighbors(const TVector& searchPoint, std::size_t neighborCount, TScalar maxDistanceWithin,
                                             double tolerance = detail::base_tolerance<TScalar>()) const
   {
@@ -356,6 +391,47 @@ public:
   {
     otg_result* r = nullptr;
     detail::check(otg_plane_positive_segmentation(m_tree, planes.data(), planes.size(), tolerance, int(algo), &r, OTG_MEM_HOST, m_stream));
+    return detail::take(r, m_stream);
+  }
+  // one condition list per query
+  template<LogicalOperator OP = LogicalOperator::And>
+  Csr QueryBatch(std::span<const std::vector<QueryCondition>> queries, double tolerance = detail::base_tolerance<TScalar>(),
+                 Algorithm algo = Algorithm::Default) const
+  {
+    std::vector<otg_condition> conds;
+    std::vector<std::uint64_t> offsets{ 0 };
+    std::vector<TPlane> planes;
+    std::vector<std::uint8_t> crossing;
+    std::vector<TBox> boxes;
+    for (const auto& q : queries)
+    {
+      for (const auto& c : q)
+      {
+        otg_condition oc{ c.kind, 0, 1, 0, c.tolerance };
+        if (c.kind == OTG_COND_FRUSTUM || c.kind == OTG_COND_PLANE)
+        {
+          if (c.kind == OTG_COND_PLANE && c.planes.size() != 1)
+            throw Error(OTG_ERR_INVALID_ARGUMENT, "a plane condition holds one plane");
+          oc.first = std::uint32_t(planes.size());
+          oc.count = std::uint32_t(c.planes.size());
+          for (const auto& [plane, crossingAllowed] : c.planes)
+          {
+            planes.push_back(plane);
+            crossing.push_back(crossingAllowed ? 1 : 0);
+          }
+        }
+        else
+        {
+          oc.first = std::uint32_t(boxes.size());
+          boxes.push_back(c.range);
+        }
+        conds.push_back(oc);
+      }
+      offsets.push_back(conds.size());
+    }
+    otg_result* r = nullptr;
+    detail::check(otg_query(m_tree, conds.data(), offsets.data(), queries.size(), planes.data(), crossing.data(), planes.size(), boxes.data(),
+                            boxes.size(), OP == LogicalOperator::Or ? 1 : 0, tolerance, int(algo), &r, OTG_MEM_HOST, m_stream));
     return detail::take(r, m_stream);
   }
   Csr GetNearestNeighborsBatch(std::span<const TVector> points, std::size_t neighborCount,

@@ -20,6 +20,9 @@ extern "C"
   void* oro_knn(void* h, const void* pts, uint64_t nq, const uint32_t* k, double maxDist, double tol);
   void* oro_ray(void* h, const void* rays, uint64_t nq, double tol, double tolInc, double maxDist, int first);
   void* oro_frustum(void* h, const void* planes, uint64_t np, uint64_t nq, double tol);
+  void* oro_plane(void* h, const void* planes, uint64_t nq, double tol, int positive);
+  void* oro_query(void* h, const void* conds, const uint64_t* off, uint64_t nq, const void* planes, const unsigned char* cross, const void* boxes,
+                  int or_op, double tol);
   void* oro_collide_self(void* h, double tol);
   void* oro_collide_pair(void* h1, void* h2, double tol);
   uint64_t oro_res_nq(void* r);
@@ -148,6 +151,36 @@ int main()
     r = oro_frustum(ob, planes.data(), planes.size(), 1, -1.0);
     expect(tb.FrustumCulling(planes), r, 0, "FrustumCulling");
     oro_res_free(r);
+    const Plane3D cut{ 45.0, { 0.6, 0.8, 0.0 } };
+    r = oro_plane(ob, &cut, 1, 0.5, 0);
+    expect(tb.PlaneSearch(cut, 0.5), r, 0, "PlaneSearch");
+    oro_res_free(r);
+    r = oro_plane(ob, &cut, 1, -1.0, 1);
+    expect(tb.PlanePositiveSegmentation(cut), r, 0, "PlanePositiveSegmentation");
+    oro_res_free(r);
+    // Query: a frustum (one plane may be crossed) and an overlap range, And and Or
+    {
+      const BoundingBox3D range{ { 30, 30, 30 }, { 70, 70, 70 } };
+      std::vector<std::pair<Plane3D, bool>> fr;
+      for (std::size_t i = 0; i < planes.size(); ++i)
+        fr.emplace_back(planes[i], i == 0);
+      const std::vector<OctreeBoxM::QueryCondition> conds = { OctreeBoxM::ByInFrustum(fr), OctreeBoxM::ByOverlaps(range) };
+      struct
+      {
+        int32_t kind;
+        uint32_t first, count, reserved;
+        double tol;
+      } oc[2] = { { OTG_COND_FRUSTUM, 0, uint32_t(planes.size()), 0, -1.0 }, { OTG_COND_RANGE_OVERLAP, 0, 1, 0, -1.0 } };
+      const uint64_t off[2] = { 0, 2 };
+      std::vector<unsigned char> cross(planes.size(), 0);
+      cross[0] = 1;
+      for (int orOp = 0; orOp < 2; ++orOp)
+      {
+        r = oro_query(ob, oc, off, 1, planes.data(), cross.data(), &range, orOp, -1.0);
+        expect(orOp ? tb.Query<LogicalOperator::Or>(conds) : tb.Query<LogicalOperator::And>(conds), r, 0, orOp ? "Query<Or>" : "Query<And>");
+        oro_res_free(r);
+      }
+    }
     // collisions: pairs flattened to ids
     auto flat = [](const std::vector<std::pair<EntityID, EntityID>>& p) {
       std::vector<uint32_t> v;
