@@ -87,9 +87,11 @@ struct BatchArgs
   int mode;     // RangeSearchMode
   T tol, tolInc, maxDist;
   Appender out;
-  u32* work;
+  u32* work;          // counters (see batch_work_bytes), then the split items
   u32* err;
   QueryProgram<T> qp; // combined queries
+  int phase;          // 0: whole queries; 1: top levels, deeper subtrees become items; 2: the items
+  u32 splitCap;       // item capacity of the work buffer
 };
 
 template<typename T, int KIND, int WARPS>
@@ -104,14 +106,33 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
   u32* stack = stackMem[w];
   WarpSink sink{ itemMem[w], KIND == kRayAll ? distMem[w] : nullptr, 0 };
   const TreeView<T>& tv = a.tv;
+  u64* items = reinterpret_cast<u64*>(a.work + 4);
   for (;;)
   {
-    u32 q = 0;
-    if (lane == 0)
-      q = atomicAdd(a.work, 1u);
-    q = __shfl_sync(~0u, q, 0);
-    if (q >= a.nq)
-      break;
+    u32 q = 0, start = 0;
+    if (a.phase == 2)
+    {
+      // the next (query, subtree) item left by the first phase
+      u32 idx = 0;
+      if (lane == 0)
+        idx = atomicAdd(a.work + 1, 1u);
+      idx = __shfl_sync(~0u, idx, 0);
+      if (idx >= min(a.work[2], a.splitCap))
+        break;
+      const u64 item = items[idx];
+      q = u32(item >> 32);
+      start = u32(item);
+      if (q >= a.nq)
+        break;
+    }
+    else
+    {
+      if (lane == 0)
+        q = atomicAdd(a.work, 1u);
+      q = __shfl_sync(~0u, q, 0);
+      if (q >= a.nq)
+        break;
+    }
     const u32 root = query_root(tv, q);
     const u32 idBase = id_base(tv, root);
     // ---- query setup (identical on all lanes)
@@ -122,24 +143,27 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
     if constexpr (KIND == kRange)
     {
       load_box(a.q + u64(q) * 6, r);
-      T rb[6];
+      if (a.phase != 2) // items continue queries that passed this setup in the first phase
+      {
+        T rb[6];
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-      {
-        rb[c] = tv.nodeBox[u64(root) * 6 + c];
-        rb[3 + c] = tv.nodeBox[u64(root) * 6 + c] + tv.nodeBox[u64(root) * 6 + 3 + c];
-      }
-      if (G::range_contains_box(r, rb, a.tol)) // root shortcut (:488-511): every id of the tree
-      {
-        const u32 nt = tv.qTree ? u32(tv.treeOff[root + 1] - tv.treeOff[root]) : tv.n;
-        unsigned long long base = 0;
-        if (lane == 0)
-          base = a.out.reserve(nt);
-        base = __shfl_sync(~0u, base, 0);
-        for (u32 i = lane; i < nt; i += 32)
-          if (base + i < a.out.capacity)
-            a.out.items[base + i] = (u64(q) << 32) | i;
-        continue;
+        for (int c = 0; c < 3; ++c)
+        {
+          rb[c] = tv.nodeBox[u64(root) * 6 + c];
+          rb[3 + c] = tv.nodeBox[u64(root) * 6 + c] + tv.nodeBox[u64(root) * 6 + 3 + c];
+        }
+        if (G::range_contains_box(r, rb, a.tol)) // root shortcut (:488-511): every id of the tree
+        {
+          const u32 nt = tv.qTree ? u32(tv.treeOff[root + 1] - tv.treeOff[root]) : tv.n;
+          unsigned long long base = 0;
+          if (lane == 0)
+            base = a.out.reserve(nt);
+          base = __shfl_sync(~0u, base, 0);
+          for (u32 i = lane; i < nt; i += 32)
+            if (base + i < a.out.capacity)
+              a.out.items[base + i] = (u64(q) << 32) | i;
+          continue;
+        }
       }
       T vol = T(1); // zero-volume range -> empty (:514-519)
 #pragma unroll
@@ -208,7 +232,12 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
     if (lane == 0)
     {
       bool contained;
-      if (enters(root, contained))
+      if (a.phase == 2)
+      {
+        stack[0] = start; // entered (its node test passed) in the first phase
+        sp = 1;
+      }
+      else if (enters(root, contained))
       {
         stack[0] = root | (contained ? kContained : 0u);
         sp = 1;
@@ -375,6 +404,28 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
           const u32 child = ofc + (f - oex);
           if (f < total)
             keep = enters(child, contained);
+          if (a.phase == 1)
+          {
+            // subtrees at the split depth become items for any warp
+            const bool defer = keep && tv.nodeDepth[child] >= kSplitDepth;
+            const u32 dbal = __ballot_sync(~0u, defer);
+            if (dbal)
+            {
+              u32 ibase = 0;
+              if (lane == 0)
+                ibase = atomicAdd(a.work + 2, u32(__popc(dbal)));
+              ibase = __shfl_sync(~0u, ibase, 0);
+              if (defer)
+              {
+                const u32 slot = ibase + __popc(dbal & ((1u << lane) - 1));
+                if (slot < a.splitCap)
+                  items[slot] = (u64(q) << 32) | child | (contained ? kContained : 0u);
+                else
+                  atomicOr(a.err, kErrStack);
+              }
+            }
+            keep = keep && !defer;
+          }
           const u32 bal = __ballot_sync(~0u, keep);
           if (sp + __popc(bal) > u32(kWideStack))
           {
@@ -406,19 +457,40 @@ static int launch_batch_w(const BatchArgs<T, KIND>& a, cudaStream_t st)
   if (!e)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_query_kernel<T, KIND, WARPS>, WARPS * 32, 0);
   if (!e)
-    e = cudaMemsetAsync(a.work, 0, sizeof(u32), st);
+    e = cudaMemsetAsync(a.work, 0, 16, st);
   if (e)
     return cuda_status(e, "configuring the batched query kernel");
+  const u64 resident = u64(sms) * std::max(per, 1);
   const u64 want = (u64(a.nq) + WARPS - 1) / WARPS;
-  const u32 grid = u32(std::max<u64>(1, std::min<u64>(u64(sms) * std::max(per, 1), want)));
-  batch_query_kernel<T, KIND, WARPS><<<grid, WARPS * 32, 0, st>>>(a);
+  const u32 grid = u32(std::max<u64>(1, std::min<u64>(resident, want)));
+  if (a.splitCap == 0)
+  {
+    batch_query_kernel<T, KIND, WARPS><<<grid, WARPS * 32, 0, st>>>(a);
+    return cuda_status(cudaGetLastError(), "launching the batched query kernel");
+  }
+  // a small batch: the top levels of every query, then its subtrees spread over every resident warp
+  BatchArgs<T, KIND> b = a;
+  b.phase = 1;
+  batch_query_kernel<T, KIND, WARPS><<<grid, WARPS * 32, 0, st>>>(b);
+  b.phase = 2;
+  batch_query_kernel<T, KIND, WARPS><<<u32(resident), WARPS * 32, 0, st>>>(b);
   return cuda_status(cudaGetLastError(), "launching the batched query kernel");
 }
 
 // shape: warps per block, 2, 4 or 8 (autotuned)
+// workBytes: size of the work buffer; a batch of at most kSplitQueries queries is split when the
+// buffer holds its items (batch_work_bytes)
 template<typename T, int KIND>
-static int launch_batch(const BatchArgs<T, KIND>& a, int shape, cudaStream_t st)
+static int launch_batch(const BatchArgs<T, KIND>& a0, int shape, cudaStream_t st, size_t workBytes)
 {
+  if (workBytes < 16)
+  {
+    set_error("batched query work buffer below its 16 bytes of counters");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  BatchArgs<T, KIND> a = a0;
+  a.phase = 0;
+  a.splitCap = (a.nq <= kSplitQueries && a.tv.nodeDepth && workBytes >= batch_work_bytes(a.nq)) ? a.nq * kSplitItemsPerQuery : 0u;
   if (shape == 2)
     return launch_batch_w<T, KIND, 2>(a, st);
   if (shape == 8)
@@ -427,45 +499,45 @@ static int launch_batch(const BatchArgs<T, KIND>& a, int shape, cudaStream_t st)
 }
 
 template<typename T>
-int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape)
+int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape, size_t workBytes)
 {
-  return launch_batch<T, kRange>(BatchArgs<T, kRange>{ tv, ranges, 0, nq, mode, tol, T(0), T(0), out, work, err }, shape, st);
+  return launch_batch<T, kRange>(BatchArgs<T, kRange>{ tv, ranges, 0, nq, mode, tol, T(0), T(0), out, work, err }, shape, st, workBytes);
 }
 template<typename T>
-int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape)
+int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape, size_t workBytes)
 {
-  return launch_batch<T, kFrustum>(BatchArgs<T, kFrustum>{ tv, planes, np, nq, 0, tol, T(0), T(0), out, work, err }, shape, st);
+  return launch_batch<T, kFrustum>(BatchArgs<T, kFrustum>{ tv, planes, np, nq, 0, tol, T(0), T(0), out, work, err }, shape, st, workBytes);
 }
 template<typename T>
-int batch_plane(const TreeView<T>& tv, const T* planes, u32 nq, bool positive, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape)
+int batch_plane(const TreeView<T>& tv, const T* planes, u32 nq, bool positive, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape, size_t workBytes)
 {
   if (positive)
-    return launch_batch<T, kPlanePositive>(BatchArgs<T, kPlanePositive>{ tv, planes, 1, nq, 0, tol, T(0), T(0), out, work, err }, shape, st);
-  return launch_batch<T, kPlane>(BatchArgs<T, kPlane>{ tv, planes, 1, nq, 0, tol, T(0), T(0), out, work, err }, shape, st);
+    return launch_batch<T, kPlanePositive>(BatchArgs<T, kPlanePositive>{ tv, planes, 1, nq, 0, tol, T(0), T(0), out, work, err }, shape, st, workBytes);
+  return launch_batch<T, kPlane>(BatchArgs<T, kPlane>{ tv, planes, 1, nq, 0, tol, T(0), T(0), out, work, err }, shape, st, workBytes);
 }
 template<typename T>
-int batch_query_program(const TreeView<T>& tv, const QueryProgram<T>& qp, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape)
+int batch_query_program(const TreeView<T>& tv, const QueryProgram<T>& qp, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape, size_t workBytes)
 {
   BatchArgs<T, kQuery> a{ tv, nullptr, 0, nq, 0, tol, T(0), T(0), out, work, err };
   a.qp = qp;
-  return launch_batch<T, kQuery>(a, shape, st);
+  return launch_batch<T, kQuery>(a, shape, st, workBytes);
 }
 template<typename T>
 int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st,
-                  int shape)
+                  int shape, size_t workBytes)
 {
-  return launch_batch<T, kRayAll>(BatchArgs<T, kRayAll>{ tv, rays, 0, nq, 0, tol, tolInc, maxDist, out, work, err }, shape, st);
+  return launch_batch<T, kRayAll>(BatchArgs<T, kRayAll>{ tv, rays, 0, nq, 0, tol, tolInc, maxDist, out, work, err }, shape, st, workBytes);
 }
 
-template int batch_range<double>(const TreeView<double>&, const double*, u32, int, double, Appender, u32*, u32*, cudaStream_t, int);
-template int batch_range<float>(const TreeView<float>&, const float*, u32, int, float, Appender, u32*, u32*, cudaStream_t, int);
-template int batch_frustum<double>(const TreeView<double>&, const double*, u32, u32, double, Appender, u32*, u32*, cudaStream_t, int);
-template int batch_frustum<float>(const TreeView<float>&, const float*, u32, u32, float, Appender, u32*, u32*, cudaStream_t, int);
-template int batch_plane<double>(const TreeView<double>&, const double*, u32, bool, double, Appender, u32*, u32*, cudaStream_t, int);
-template int batch_plane<float>(const TreeView<float>&, const float*, u32, bool, float, Appender, u32*, u32*, cudaStream_t, int);
-template int batch_query_program<double>(const TreeView<double>&, const QueryProgram<double>&, u32, double, Appender, u32*, u32*, cudaStream_t, int);
-template int batch_query_program<float>(const TreeView<float>&, const QueryProgram<float>&, u32, float, Appender, u32*, u32*, cudaStream_t, int);
-template int batch_ray_all<double>(const TreeView<double>&, const double*, u32, double, double, double, Appender, u32*, u32*, cudaStream_t, int);
-template int batch_ray_all<float>(const TreeView<float>&, const float*, u32, float, float, float, Appender, u32*, u32*, cudaStream_t, int);
+template int batch_range<double>(const TreeView<double>&, const double*, u32, int, double, Appender, u32*, u32*, cudaStream_t, int, size_t);
+template int batch_range<float>(const TreeView<float>&, const float*, u32, int, float, Appender, u32*, u32*, cudaStream_t, int, size_t);
+template int batch_frustum<double>(const TreeView<double>&, const double*, u32, u32, double, Appender, u32*, u32*, cudaStream_t, int, size_t);
+template int batch_frustum<float>(const TreeView<float>&, const float*, u32, u32, float, Appender, u32*, u32*, cudaStream_t, int, size_t);
+template int batch_plane<double>(const TreeView<double>&, const double*, u32, bool, double, Appender, u32*, u32*, cudaStream_t, int, size_t);
+template int batch_plane<float>(const TreeView<float>&, const float*, u32, bool, float, Appender, u32*, u32*, cudaStream_t, int, size_t);
+template int batch_query_program<double>(const TreeView<double>&, const QueryProgram<double>&, u32, double, Appender, u32*, u32*, cudaStream_t, int, size_t);
+template int batch_query_program<float>(const TreeView<float>&, const QueryProgram<float>&, u32, float, Appender, u32*, u32*, cudaStream_t, int, size_t);
+template int batch_ray_all<double>(const TreeView<double>&, const double*, u32, double, double, double, Appender, u32*, u32*, cudaStream_t, int, size_t);
+template int batch_ray_all<float>(const TreeView<float>&, const float*, u32, float, float, float, Appender, u32*, u32*, cudaStream_t, int, size_t);
 
 } // namespace otg

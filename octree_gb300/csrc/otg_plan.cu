@@ -185,11 +185,11 @@ static int plan_record_query(Plan& p, PlanQuery& q, cudaStream_t st)
   const int shape = tune_lookup(query_key(ops[q.kind], OTG_ALGO_FILTERED, true, sizeof(T) == 8, t.kind, t.n, q.nq), 4);
   int rc;
   if (q.kind == kPlanRange)
-    rc = batch_range<T>(tv, (const T*)q.input, u32(q.nq), q.mode, tl, a, q.work.as<u32>(), q.err.as<u32>(), st, shape);
+    rc = batch_range<T>(tv, (const T*)q.input, u32(q.nq), q.mode, tl, a, q.work.as<u32>(), q.err.as<u32>(), st, shape, q.work.bytes);
   else if (q.kind == kPlanFrustum)
-    rc = batch_frustum<T>(tv, (const T*)q.input, q.np, u32(q.nq), tl, a, q.work.as<u32>(), q.err.as<u32>(), st, shape);
+    rc = batch_frustum<T>(tv, (const T*)q.input, q.np, u32(q.nq), tl, a, q.work.as<u32>(), q.err.as<u32>(), st, shape, q.work.bytes);
   else
-    rc = batch_ray_all<T>(tv, (const T*)q.input, u32(q.nq), tl, T(0), Lim<T>::max(), a, q.work.as<u32>(), q.err.as<u32>(), st, shape);
+    rc = batch_ray_all<T>(tv, (const T*)q.input, u32(q.nq), tl, T(0), Lim<T>::max(), a, q.work.as<u32>(), q.err.as<u32>(), st, shape, q.work.bytes);
   if (rc)
     return rc;
   const unsigned long long* m = q.count.as<unsigned long long>();
@@ -236,7 +236,7 @@ static int plan_alloc(PlanQuery& q, u64 nEntities)
   const u32 passes = (bitsMax + kRadixBits - 1) / kRadixBits;
   cudaError_t e;
   if ((e = q.items.ensure(sizeof(u64) * cap)) || (e = q.count.ensure(sizeof(unsigned long long))) || (e = q.err.ensure(sizeof(u32))) ||
-      (e = q.work.ensure(sizeof(u32))) || (e = q.keysB.ensure(sizeof(u64) * cap)) || (e = q.vals.ensure(sizeof(u32) * cap)) ||
+      (e = q.work.ensure(batch_work_bytes(q.nq))) || (e = q.keysB.ensure(sizeof(u64) * cap)) || (e = q.vals.ensure(sizeof(u32) * cap)) ||
       (e = q.valsB.ensure(sizeof(u32) * cap)) || (e = q.k32.ensure(sizeof(u32) * cap)) || (e = q.scratch.ensure(SortScratch::bytes(cap, passes))) ||
       (e = q.offsets.ensure(sizeof(u64) * (q.nq + 1))) || (e = q.ids.ensure(sizeof(u32) * cap)))
     return cuda_status(e, "allocating plan buffers");

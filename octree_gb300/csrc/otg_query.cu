@@ -1232,7 +1232,7 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
   DevBuf work;
-  if (cudaError_t e = work.ensure(sizeof(u32)))
+  if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
     return cuda_status(e, "allocating the work counter");
   int launchRc = OTG_OK;
   int rc = collect(
@@ -1249,7 +1249,7 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
             range_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), mode, tl, a, err);
             return cuda_status(cudaGetLastError(), "launching the range search");
           }
-          return batch_range<T>(tv, (const T*)d, u32(nq), mode, tl, a, work.as<u32>(), err, st, shape);
+          return batch_range<T>(tv, (const T*)d, u32(nq), mode, tl, a, work.as<u32>(), err, st, shape, work.bytes);
         });
     },
     st);
@@ -1294,7 +1294,7 @@ static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, 
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
   DevBuf work;
-  if (cudaError_t e = work.ensure(sizeof(u32)))
+  if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
     return cuda_status(e, "allocating the work counter");
   int launchRc = OTG_OK;
   int rc = collect(
@@ -1311,7 +1311,7 @@ static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, 
             frustum_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(np), u32(nq), tl, a, err);
             return cuda_status(cudaGetLastError(), "launching the frustum culling");
           }
-          return batch_frustum<T>(tv, (const T*)d, u32(np), u32(nq), tl, a, work.as<u32>(), err, st, shape);
+          return batch_frustum<T>(tv, (const T*)d, u32(np), u32(nq), tl, a, work.as<u32>(), err, st, shape, work.bytes);
         });
     },
     st);
@@ -1336,7 +1336,7 @@ static int plane_impl(const TreeState& t, const void* planes, u64 nq, bool posit
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
   DevBuf work;
-  if (cudaError_t e = work.ensure(sizeof(u32)))
+  if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
     return cuda_status(e, "allocating the work counter");
   int launchRc = OTG_OK;
   int rc = collect(
@@ -1354,7 +1354,7 @@ static int plane_impl(const TreeState& t, const void* planes, u64 nq, bool posit
                                 plane_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), positive ? 1 : 0, tl, a, err);
                                 return cuda_status(cudaGetLastError(), "launching the plane search");
                               }
-                              return batch_plane<T>(tv, (const T*)d, u32(nq), positive, tl, a, work.as<u32>(), err, st, shape);
+                              return batch_plane<T>(tv, (const T*)d, u32(nq), positive, tl, a, work.as<u32>(), err, st, shape, work.bytes);
                             });
     },
     st);
@@ -1431,7 +1431,7 @@ static int query_impl(const TreeState& t, const QueryCond* conds, const u64* off
   auto tv = view<T>(t, nullptr);
   T tl = tol_of<T>(tol);
   DevBuf work;
-  if (cudaError_t e = work.ensure(sizeof(u32)))
+  if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
     return cuda_status(e, "allocating the work counter");
   int launchRc = OTG_OK;
   int rc = collect(
@@ -1449,7 +1449,7 @@ static int query_impl(const TreeState& t, const QueryCond* conds, const u64* off
                                 query_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, qp, u32(nq), tl, a, err);
                                 return cuda_status(cudaGetLastError(), "launching the combined query");
                               }
-                              return batch_query_program<T>(tv, qp, u32(nq), tl, a, work.as<u32>(), err, st, shape);
+                              return batch_query_program<T>(tv, qp, u32(nq), tl, a, work.as<u32>(), err, st, shape, work.bytes);
                             });
     },
     st);
@@ -1513,7 +1513,7 @@ static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, do
   if (!first)
   {
     DevBuf work;
-    if (cudaError_t e = work.ensure(sizeof(u32)))
+    if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
       return cuda_status(e, "allocating the work counter");
     int launchRc = OTG_OK;
     rc = collect(
@@ -1530,7 +1530,7 @@ static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, do
               ray_all_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, ti, md, a, err);
               return cuda_status(cudaGetLastError(), "launching the ray query");
             }
-            return batch_ray_all<T>(tv, (const T*)d, u32(nq), tl, ti, md, a, work.as<u32>(), err, st, shape);
+            return batch_ray_all<T>(tv, (const T*)d, u32(nq), tl, ti, md, a, work.as<u32>(), err, st, shape, work.bytes);
           });
       },
       st);

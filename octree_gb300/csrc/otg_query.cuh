@@ -26,6 +26,7 @@ struct TreeView
   u32 nNodes;
   const u32* qTree;   // forest: tree (= root node) of each query; null for a single tree
   const u64* treeOff; // forest: first entity of each tree (ids are returned relative to it)
+  const unsigned char* nodeDepth; // depth of each node below its tree's root
 };
 
 // root node and id base of query q (node t is the root of tree t in a forest)
@@ -288,7 +289,8 @@ template<typename T>
 static inline TreeView<T> view(const TreeState& t, const u32* qTree = nullptr)
 {
   return TreeView<T>{ t.nodeLink.as<uint4>(), t.nodeBox.as<T>(), t.nodeMax.as<T>(), t.sortedIds.as<u32>(), t.sortedGeom.as<T>(), u32(t.n),
-                      t.kind == OTG_KIND_BOXES ? 1 : 0, u32(t.nodeCount), qTree, qTree ? t.treeOff.as<u64>() : nullptr };
+                      t.kind == OTG_KIND_BOXES ? 1 : 0, u32(t.nodeCount), qTree, qTree ? t.treeOff.as<u64>() : nullptr,
+                      t.nodeDepth.as<unsigned char>() };
 }
 
 template<typename T>
@@ -306,17 +308,28 @@ static inline T tol_of(double tol)
 // batched warp-per-query kernels (otg_batch.cu); `work` is a device counter the launch resets;
 // shape: warps per block (2, 4 or 8)
 template<typename T>
-int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4);
+int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4, size_t workBytes = 0);
+// Work buffer of the batched kernels: four counters, then the (query, subtree) items of a split
+// batch. A batch of at most kSplitQueries queries is split: each query runs its top levels, and the
+// subtrees at depth kSplitDepth it enters become items that any warp takes, so that a few costly
+// queries (large trees of a forest, wide frusta) spread over the whole GPU.
+constexpr u32 kSplitQueries = 8192;
+constexpr u32 kSplitDepth = 2;
+constexpr u32 kSplitItemsPerQuery = 1u << (3 * kSplitDepth);
+inline size_t batch_work_bytes(u64 nq)
+{
+  return 16 + (nq <= kSplitQueries ? sizeof(u64) * kSplitItemsPerQuery * nq : 0);
+}
 template<typename T>
-int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4);
+int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4, size_t workBytes = 0);
 template<typename T>
-int batch_plane(const TreeView<T>& tv, const T* planes, u32 nq, bool positive, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4);
+int batch_plane(const TreeView<T>& tv, const T* planes, u32 nq, bool positive, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4, size_t workBytes = 0);
 template<typename T>
 int batch_query_program(const TreeView<T>& tv, const QueryProgram<T>& qp, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st,
-                        int shape = 4);
+                        int shape = 4, size_t workBytes = 0);
 template<typename T>
 int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st,
-                  int shape = 4);
+                  int shape = 4, size_t workBytes = 0);
 
 // autotuner size class of a batched query
 inline std::string query_key(const char* op, int algo, bool forest, bool f64, int kind, u64 n, u64 nq)

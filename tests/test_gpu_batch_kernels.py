@@ -1,7 +1,9 @@
 """The batched warp-per-query kernels (default algorithm) against the one-query-per-thread kernels
 (OTG_ALGO_PLAIN_FP64) for RangeSearch, FrustumCulling and RayIntersectedAll: identical id lists and
-ray distances, on point and box trees of both scalar types and on a forest. (Both are checked
-against the oracle by the parity tests; this pins them to each other on larger inputs.)"""
+ray distances, on point and box trees of both scalar types and on a forest. Batches of at most
+8192 queries run split (top levels per query, then their depth-2 subtrees as separate work items);
+larger ones run whole, and both sizes are covered. (Both kernels are checked against the oracle by
+the parity tests; this pins them to each other on larger inputs.)"""
 import numpy as np
 import pytest
 
@@ -28,8 +30,9 @@ def _inputs(rng, n_q, dtype, span=100.0):
     return ranges, rays, planes.astype(dtype)
 
 
+@pytest.mark.parametrize("nq", [3000, 12000])
 @pytest.mark.parametrize("kind,dtype", [("points", np.float64), ("boxes", np.float64), ("boxes", np.float32), ("points", np.float32)])
-def test_batch_kernels_match_plain(kind, dtype):
+def test_batch_kernels_match_plain(kind, dtype, nq):
     rng = np.random.default_rng(111)
     n = 150_000
     if kind == "points":
@@ -39,7 +42,7 @@ def test_batch_kernels_match_plain(kind, dtype):
         e = rng.uniform(0.05, 1.0, (n, 3))
         ent = np.concatenate([c - e, c + e], 1).astype(dtype)
     t = otg.Tree(kind, dtype).create(ent, max_depth=8, max_elements=20)
-    ranges, rays, planes = _inputs(rng, 3000, dtype)
+    ranges, rays, planes = _inputs(rng, nq, dtype)
     for mode in (otg.RANGE_INSIDE, otg.RANGE_OVERLAP):
         assert_csr_equal(t.range_search(ranges, mode), t.range_search(ranges, mode, algo=otg.ALGO_PLAIN_FP64), f"range {mode}")
     assert_csr_equal(t.frustum_culling(planes)[:2], t.frustum_culling(planes, algo=otg.ALGO_PLAIN_FP64)[:2], "frustum")
