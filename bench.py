@@ -211,13 +211,33 @@ def oracle_lib():
     return OracleLib(ORACLE_SO), "port"
 
 
-def cpu_build_rate(pts, reps, threads):
-    """M entities/s of the CPU Create on `pts` (oracle port, or the reference where it was built)."""
-    lib, kind = oracle_lib()
+def cpu_threads(lib):
+    """Host threads of the timed CPU Create: every core for the oracle port, whose location transform
+    and sort run on workers as the reference's ParExec steps do; 1 for the reference harness built
+    here (its std::execution::par runs sequentially without a parallel backend)."""
+    if not hasattr(lib.lib, "oro_time_create_points_par"):
+        return 1
+    return os.cpu_count() or 1
+
+
+def time_cpu_create(lib, pts, reps, threads):
+    """Seconds of `reps` CPU Creates of `pts` on `threads` workers."""
+    import ctypes
+
     p = np.ascontiguousarray(pts)
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    secs = lib.lib.oro_time_create_points(p.ctypes.data_as(__import__("ctypes").c_void_p), p.shape[0], MAX_DEPTH, MAX_ELEM, reps)
-    return p.shape[0] * reps / secs / 1e6, kind
+    ptr = p.ctypes.data_as(ctypes.c_void_p)
+    if threads > 1:
+        return lib.lib.oro_time_create_points_par(ptr, p.shape[0], MAX_DEPTH, MAX_ELEM, reps, threads)
+    return lib.lib.oro_time_create_points(ptr, p.shape[0], MAX_DEPTH, MAX_ELEM, reps)
+
+
+def cpu_build_rate(pts, reps):
+    """(M entities/s, kind, threads) of the CPU Create on `pts` (oracle port, or the reference where it
+    was built), on every host thread it can use."""
+    lib, kind = oracle_lib()
+    threads = cpu_threads(lib)
+    secs = time_cpu_create(lib, pts, reps, threads)
+    return len(pts) * reps / secs / 1e6, kind, threads
 
 
 def run_reference(args):
@@ -226,16 +246,14 @@ def run_reference(args):
         return
     pts = shell_points(N_POINTS, 301)
     lib, kind = oracle_lib()
-    threads = 1
+    threads = cpu_threads(lib)
     sample_n = 2_000_000
     sample = np.ascontiguousarray(pts[:sample_n])
-    import ctypes
-
     for _ in range(max(0, args.warmup)):
-        lib.lib.oro_time_create_points(sample.ctypes.data_as(ctypes.c_void_p), sample_n, MAX_DEPTH, MAX_ELEM, 1)
+        time_cpu_create(lib, sample, 1, threads)
     times = []
     for _ in range(args.steps):
-        times.append(lib.lib.oro_time_create_points(sample.ctypes.data_as(ctypes.c_void_p), sample_n, MAX_DEPTH, MAX_ELEM, 1))
+        times.append(time_cpu_create(lib, sample, 1, threads))
     ms = statistics.mean(times) * 1e3
     value = sample_n / (ms / 1e3) / 1e6
     line = {
@@ -258,7 +276,8 @@ def run_reference(args):
             "unit": "M entities/s",
             "cores": threads,
             "kind": kind,
-            "sample": f"{sample_n} points per step (bounded sample of the 16M workload), single-threaded Create",
+            "sample": f"{sample_n} points per step (bounded sample of the 16M workload), Create with the location transform and sort "
+            f"on {threads} threads, BuildSubtree sequential as in the reference",
         },
         "e2e": {"value": value, "unit": "M entities/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -391,13 +410,13 @@ def run_gpu(args):
     line["gpu_launches"] = args.steps * (2 + 1 + 1 + passes + 1 + 1 + MAX_DEPTH + 1)
     if rank == 0 and not args.no_cpu_baseline:
         sample = pts_h[:1_000_000]
-        rate, kind = cpu_build_rate(sample, 3, 1)
+        rate, kind, threads = cpu_build_rate(sample, 3)
         line["cpu_baseline"] = {
             "value": rate,
             "unit": "M entities/s",
-            "cores": 1,
+            "cores": threads,
             "kind": kind,
-            "sample": "1M of the 16M points, 3 single-threaded Creates",
+            "sample": f"1M of the 16M points, 3 Creates, location transform and sort on {threads} threads",
         }
     if not args.no_queries:
         line["queries"] = run_queries(tree, pts_d, stream)

@@ -30,6 +30,8 @@
 #include <unordered_map>
 #include <utility>
 #include <vector>
+#include <thread>
+#include <atomic>
 
 namespace otg_oracle
 {
@@ -694,16 +696,33 @@ public:
       return;
     }
 
-    // :774-783 locations
+    // :774-783 locations (std::transform with the execution policy: `threads` workers)
     locationKeys.resize(n);
-    for (size_t i = 0; i < n; ++i)
-      locationKeys[i] = rasterDouble ? location_key<double>(ent(u32(i)), rsizeD, rastD) : location_key<float>(ent(u32(i)), rsizeF, rastF);
+    parallel_ranges(n, [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i)
+        locationKeys[i] = rasterDouble ? location_key<double>(ent(u32(i)), rsizeD, rastD) : location_key<float>(ent(u32(i)), rsizeF, rastF);
+    });
 
     // :791-796 sort by location (ParExec path). Ties are ordered by id here; the reference's
     // std::sort leaves them unspecified, so every comparison is made on canonical (sorted) id sets.
+    // With several workers: sorted chunks merged pairwise, each round's merges in parallel.
     std::vector<u32> order(n);
     std::iota(order.begin(), order.end(), 0u);
-    std::stable_sort(order.begin(), order.end(), [&](u32 a, u32 b) { return locationKeys[a] < locationKeys[b]; });
+    auto less = [&](u32 a, u32 b) { return locationKeys[a] < locationKeys[b] || (locationKeys[a] == locationKeys[b] && a < b); };
+    const size_t chunks = std::min<size_t>(threads, std::max<size_t>(1, n / 4096));
+    std::vector<size_t> cut(chunks + 1);
+    for (size_t c = 0; c <= chunks; ++c)
+      cut[c] = n * c / chunks;
+    run_workers(chunks, [&](size_t c) { std::sort(order.begin() + cut[c], order.begin() + cut[c + 1], less); });
+    std::vector<u32> tmp(chunks > 1 ? n : 0);
+    for (size_t width = 1; width < chunks; width *= 2)
+    {
+      run_workers((chunks + 2 * width - 1) / (2 * width), [&](size_t m) {
+        const size_t lo = cut[2 * width * m], mid = cut[std::min(chunks, 2 * width * m + width)], hi = cut[std::min(chunks, 2 * width * (m + 1))];
+        std::merge(order.begin() + lo, order.begin() + mid, order.begin() + mid, order.begin() + hi, tmp.begin() + lo, less);
+        std::copy(tmp.begin() + lo, tmp.begin() + hi, order.begin() + lo);
+      });
+    }
 
     // :717-747 BuildSubtree (depth-first emission)
     build_subtree(root, 0, order, 0, n);
@@ -713,6 +732,35 @@ public:
       init_mbr(nodes.at(1));
     else if (box)
       init_root_box_min_point();
+  }
+
+  // Workers for the steps the reference runs with its execution policy (location transform, sort);
+  // 1 = the sequential path. BuildSubtree stays sequential, as in the reference.
+  unsigned threads = 1;
+  template<typename F>
+  void run_workers(size_t count, F&& f) const
+  {
+    if (count <= 1 || threads <= 1)
+    {
+      for (size_t i = 0; i < count; ++i)
+        f(i);
+      return;
+    }
+    std::vector<std::thread> pool;
+    std::atomic<size_t> next{ 0 };
+    for (unsigned w = 0; w < std::min<size_t>(threads, count); ++w)
+      pool.emplace_back([&] {
+        for (size_t i; (i = next.fetch_add(1)) < count;)
+          f(i);
+      });
+    for (auto& t : pool)
+      t.join();
+  }
+  template<typename F>
+  void parallel_ranges(size_t n, F&& f) const
+  {
+    const size_t parts = std::min<size_t>(threads, std::max<size_t>(1, n / 4096));
+    run_workers(parts, [&](size_t p) { f(n * p / parts, n * (p + 1) / parts); });
   }
 
   // ot_dynamic_hash_core.h:647-747 (ProcessNode / CreateProcessingData / BuildSubtree)

@@ -198,21 +198,28 @@ extern "C"
 {
   // kind: 0 points, 1 loose boxes (OctreeBox), 2 non-loose boxes. scalar: 0 double, 1 float.
   // box: 6 scalars (min xyz, max xyz) or NULL; maxDepth 0 = EstimateMaxDepth.
-  void* oro_create(int scalar, int kind, const void* ent, uint64_t n, uint32_t maxDepth, const void* box, uint64_t maxElem)
+  // threads: workers of the location transform and the sort (the reference's ParExec steps)
+  void* oro_create_threads(int scalar, int kind, const void* ent, uint64_t n, uint32_t maxDepth, const void* box, uint64_t maxElem, unsigned threads)
   {
     auto* a = new AnyTree();
     a->scalar = scalar;
     if (scalar == 0)
     {
       a->d = std::make_unique<Tree<double>>();
+      a->d->threads = std::max(1u, threads);
       a->d->create((const double*)ent, n, maxDepth, (const double*)box, maxElem, kind != 0, kind == 1);
     }
     else
     {
       a->f = std::make_unique<Tree<float>>();
+      a->f->threads = std::max(1u, threads);
       a->f->create((const float*)ent, n, maxDepth, (const float*)box, maxElem, kind != 0, kind == 1);
     }
     return a;
+  }
+  void* oro_create(int scalar, int kind, const void* ent, uint64_t n, uint32_t maxDepth, const void* box, uint64_t maxElem)
+  {
+    return oro_create_threads(scalar, kind, ent, n, maxDepth, box, maxElem, 1);
   }
   void oro_destroy(void* h) { delete (AnyTree*)h; }
   uint32_t oro_max_depth(void* h)
@@ -374,15 +381,21 @@ extern "C"
   }
 
   // Timed CPU baseline helper: builds and destroys `reps` trees (points, double), returns seconds.
-  double oro_time_create_points(const double* pts, uint64_t n, uint32_t maxDepth, uint64_t maxElem, int reps)
+  // threads: workers of the location transform and the sort (the reference's ParExec steps)
+  double oro_time_create_points_par(const double* pts, uint64_t n, uint32_t maxDepth, uint64_t maxElem, int reps, unsigned threads)
   {
     auto t0 = std::chrono::steady_clock::now();
     for (int r = 0; r < reps; ++r)
     {
       Tree<double> t;
+      t.threads = std::max(1u, threads);
       t.create(pts, n, maxDepth, nullptr, maxElem, false, false);
     }
     auto t1 = std::chrono::steady_clock::now();
     return std::chrono::duration<double>(t1 - t0).count();
+  }
+  double oro_time_create_points(const double* pts, uint64_t n, uint32_t maxDepth, uint64_t maxElem, int reps)
+  {
+    return oro_time_create_points_par(pts, n, maxDepth, maxElem, reps, 1);
   }
 }

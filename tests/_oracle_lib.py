@@ -60,19 +60,29 @@ class OracleLib:
         if hasattr(lib, "oro_brute_collide"):
             lib.oro_brute_collide.restype = _vp
             lib.oro_brute_collide.argtypes = [_int, _vp, _u64, _dbl]
+        if hasattr(lib, "oro_create_threads"):
+            lib.oro_create_threads.restype = _vp
+            lib.oro_create_threads.argtypes = [_int, _int, _vp, _u64, _u32, _vp, _u64, _u32]
+        if hasattr(lib, "oro_time_create_points_par"):
+            lib.oro_time_create_points_par.restype = _dbl
+            lib.oro_time_create_points_par.argtypes = [_vp, _u64, _u32, _u64, _int, _u32]
         if hasattr(lib, "oro_collide_self_par"):
             lib.oro_collide_self_par.restype = _vp
             lib.oro_collide_self_par.argtypes = [_vp, _dbl]
         self.lib = lib
 
     # -------------------------------------------------------------- trees
-    def create(self, ent, kind, max_depth=0, box=None, max_elem=16):
+    def create(self, ent, kind, max_depth=0, box=None, max_elem=16, threads=1):
+        """threads > 1: the location transform and sort on that many workers (the oracle only)."""
         ent = np.ascontiguousarray(ent)
         scalar = 0 if ent.dtype == np.float64 else 1
         if box is not None:
             box = np.ascontiguousarray(box, dtype=ent.dtype)
         n = ent.shape[0] if ent.size else 0
-        h = self.lib.oro_create(scalar, kind, _ptr(ent), n, max_depth, _ptr(box), max_elem)
+        if threads > 1:
+            h = self.lib.oro_create_threads(scalar, kind, _ptr(ent), n, max_depth, _ptr(box), max_elem, threads)
+        else:
+            h = self.lib.oro_create(scalar, kind, _ptr(ent), n, max_depth, _ptr(box), max_elem)
         return OracleTree(self, h, ent, kind)
 
     def brute_collide(self, boxes, tol=-1.0):

@@ -44,3 +44,23 @@ def test_oracle_plane_queries_match_reference_fixture(name):
     tol = float(g["plane_tol"])
     assert_csr_equal(t.plane_search(pl, tol), (g["planetol_off"], g["planetol_ids"]), "plane search, wide tolerance")
     assert_csr_equal(t.plane_positive(pl, tol), (g["planepostol_off"], g["planepostol_ids"]), "plane positive, wide tolerance")
+
+
+@pytest.mark.parametrize("kind", [KIND_POINTS, 1])
+def test_threaded_oracle_create_matches_sequential(kind):
+    """The oracle's threaded location transform and sort (the reference's ParExec steps, used for
+    the timed CPU baseline) build the same tree as its sequential path."""
+    rng = np.random.default_rng(12)
+    n = 60_000
+    if kind == KIND_POINTS:
+        ent = rng.random((n, 3)) * 100
+    else:
+        c = rng.random((n, 3)) * 100
+        h = rng.random((n, 3))
+        ent = np.concatenate([c - h, c + h], 1)
+    a = oracle().create(ent, kind, 8, None, 12)
+    b = oracle().create(ent, kind, 8, None, 12, threads=7)
+    assert np.array_equal(a.location_keys(), b.location_keys())
+    na, nb = a.nodes(), b.nodes()
+    for k in na:
+        assert np.array_equal(na[k], nb[k]), k
