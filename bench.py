@@ -29,6 +29,8 @@ N_POINTS = 16_000_000
 MAX_DEPTH = 10
 MAX_ELEM = 20
 METRIC = "M entities/s build (OctreePoint Create, 16M FP64 points, depth 10, max 20 per node)"
+# mean dram__bytes_read.sum + dram__bytes_write.sum of the four radix passes of this build (one ncu capture)
+SORT_PASS_DRAM_BYTES = 191.7e6
 
 
 def peaks():
@@ -375,7 +377,10 @@ def run_gpu(args):
         "peak_kind": peak_kind,
         "unit": "GB/s",
         "frac": achieved / hbm,
-        "traffic": None,
+        # DRAM bytes per sort pass of this workload from one ncu capture
+        # (profiles/onesweep_pass_kernel_16m_traffic.md); not measurable inside a timed run
+        "traffic": SORT_PASS_DRAM_BYTES if dom == "sort" else None,
+        "traffic_source": "profiles/onesweep_pass_kernel_16m_traffic.md" if dom == "sort" else None,
         "algorithmic_bytes_per_launch": per_launch_bytes,
         "launches_per_step": launches,
     }
