@@ -499,6 +499,13 @@ def run_queries(tree16, pts16_d, stream):
     q = torch.as_tensor(rng.random((10_000, 3)) * 100, device="cuda")
     s = time_query(lambda: t1.range_search(ranges, algo=otg.ALGO_PLAIN_FP64, raw=True))
     out["range_1M_10k_plain_fp64_Mq_per_s"] = 10_000 / s / 1e6
+    s = time_query(lambda: t1.range_search(ranges, raw=True))
+    out["range_1M_10k_batched_Mq_per_s"] = 10_000 / s / 1e6
+    # 10k PickSearch at points of the tree (each finds its point)
+    picks = torch.as_tensor(p1[np.random.default_rng(104).integers(0, len(p1), 10_000)], device="cuda")
+    for algo, name in ((otg.ALGO_PLAIN_FP64, "plain_fp64"), (otg.ALGO_DEFAULT, "batched")):
+        s = time_query(lambda: t1.pick_search(picks, algo=algo, raw=True))
+        out[f"pick_1M_10k_{name}_Mq_per_s"] = 10_000 / s / 1e6
     for algo, name in algos:
         s = time_query(lambda: t1.knn(q, 8, algo=algo, raw=True))
         out[f"knn8_1M_10k_{name}_Mq_per_s"] = 10_000 / s / 1e6

@@ -15,6 +15,7 @@
 //   PlaneSearch         core/ot_query.h:612-636
 //   PlanePositiveSegmentation core/ot_query.h:687-744
 //   Query<And / Or>     core/ot_query.h:864-1026
+//   PickSearch          core/ot_query.h:425-466
 #include "otg_query.cuh"
 
 namespace otg
@@ -75,13 +76,13 @@ __device__ __forceinline__ void sink_put(WarpSink& s, Appender& out, u32 lane, b
 }
 
 // query kinds
-constexpr int kRange = 0, kFrustum = 1, kRayAll = 2, kPlane = 3, kPlanePositive = 4, kQuery = 5;
+constexpr int kRange = 0, kFrustum = 1, kRayAll = 2, kPlane = 3, kPlanePositive = 4, kQuery = 5, kPick = 6;
 
 template<typename T, int KIND>
 struct BatchArgs
 {
   TreeView<T> tv;
-  const T* q;   // ranges (6 per query), planes (4 * np per query, 4 for the plane kinds) or rays (6 per query)
+  const T* q;   // ranges (6 per query), planes (4 * np per query, 4 for the plane kinds), rays (6 per query) or points (3 per query)
   u32 np;       // planes per query
   u32 nq;
   int mode;     // RangeSearchMode
@@ -97,7 +98,7 @@ struct BatchArgs
 template<typename T, int KIND, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KIND> a)
 {
-  static_assert(KIND >= kRange && KIND <= kQuery, "every query kind has its own setup, node test and entity test below");
+  static_assert(KIND >= kRange && KIND <= kPick, "every query kind has its own setup, node test and entity test below");
   using G = GeoD<T>;
   __shared__ u32 stackMem[WARPS][kWideStack];
   __shared__ u64 itemMem[WARPS][kItemBuf];
@@ -181,6 +182,21 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
     }
     else if constexpr (KIND == kPlane || KIND == kPlanePositive)
       pl = a.q + u64(q) * 4;
+    else if constexpr (KIND == kPick)
+    {
+      pl = a.q + u64(q) * 3; // the point
+      if (a.phase != 2)
+      {
+        T rb[6];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+        {
+          rb[c] = tv.nodeBox[u64(root) * 6 + c];
+          rb[3 + c] = tv.nodeBox[u64(root) * 6 + c] + tv.nodeBox[u64(root) * 6 + 3 + c];
+        }
+        skip = !G::box_contains_point(rb, pl, a.tol); // :430-431 the point outside the tree's box
+      }
+    }
     else if constexpr (KIND == kRayAll)
     {
       ray.make(a.q + u64(q) * 6, a.q + u64(q) * 6 + 3, a.tol, a.tolInc);
@@ -222,6 +238,8 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
       }
       else if constexpr (KIND == kQuery)
         return cond_combine(a.qp, q, a.err, [&](const QueryCond& c) { return cond_node(a.qp, c, nb, a.tol); });
+      else if constexpr (KIND == kPick)
+        return G::node_contains_point(nb, nb + 3, pl, a.tol);
       else if constexpr (KIND == kRayAll)
       {
         T en, ex;
@@ -372,6 +390,8 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
               const T* g = tv.geom + u64(e) * (tv.isBox ? 6 : 3);
               hit = cond_combine(a.qp, q, a.err, [&](const QueryCond& c) { return cond_entity(a.qp, c, g, tv.isBox != 0, a.tol); });
             }
+            else if constexpr (KIND == kPick)
+              hit = tv.isBox ? G::box_contains_point(tv.geom + u64(e) * 6, pl, a.tol) : G::points_equal(tv.geom + u64(e) * 3, pl, a.tol);
             else if constexpr (KIND == kRayAll)
             {
               T en, ex;
@@ -523,6 +543,11 @@ int batch_query_program(const TreeView<T>& tv, const QueryProgram<T>& qp, u32 nq
   return launch_batch<T, kQuery>(a, shape, st, workBytes);
 }
 template<typename T>
+int batch_pick(const TreeView<T>& tv, const T* pts, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape, size_t workBytes)
+{
+  return launch_batch<T, kPick>(BatchArgs<T, kPick>{ tv, pts, 0, nq, 0, tol, T(0), T(0), out, work, err }, shape, st, workBytes);
+}
+template<typename T>
 int batch_ray_all(const TreeView<T>& tv, const T* rays, u32 nq, T tol, T tolInc, T maxDist, Appender out, u32* work, u32* err, cudaStream_t st,
                   int shape, size_t workBytes)
 {
@@ -537,6 +562,8 @@ template int batch_plane<double>(const TreeView<double>&, const double*, u32, bo
 template int batch_plane<float>(const TreeView<float>&, const float*, u32, bool, float, Appender, u32*, u32*, cudaStream_t, int, size_t);
 template int batch_query_program<double>(const TreeView<double>&, const QueryProgram<double>&, u32, double, Appender, u32*, u32*, cudaStream_t, int, size_t);
 template int batch_query_program<float>(const TreeView<float>&, const QueryProgram<float>&, u32, float, Appender, u32*, u32*, cudaStream_t, int, size_t);
+template int batch_pick<double>(const TreeView<double>&, const double*, u32, double, Appender, u32*, u32*, cudaStream_t, int, size_t);
+template int batch_pick<float>(const TreeView<float>&, const float*, u32, float, Appender, u32*, u32*, cudaStream_t, int, size_t);
 template int batch_ray_all<double>(const TreeView<double>&, const double*, u32, double, double, double, Appender, u32*, u32*, cudaStream_t, int, size_t);
 template int batch_ray_all<float>(const TreeView<float>&, const float*, u32, float, float, float, Appender, u32*, u32*, cudaStream_t, int, size_t);
 

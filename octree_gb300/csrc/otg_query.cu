@@ -1272,9 +1272,30 @@ static int pick_impl(const TreeState& t, const void* pts, u64 nq, double tol, in
   Collected c;
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
+  DevBuf work;
+  if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
+    return cuda_status(e, "allocating the work counter");
+  int launchRc = OTG_OK;
   int rc = collect(
     c, false, nq * 8,
-    [&](Appender a, u32* err) { pick_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, a, err); }, st);
+    [&](Appender a, u32* err) {
+      if (algo == OTG_ALGO_PLAIN_FP64)
+        pick_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, a, err);
+      else
+        launchRc = tune_run(query_key("pick", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st, [&](int shape) {
+          cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
+          cudaMemsetAsync(err, 0, sizeof(u32), st);
+          if (shape == 0)
+          {
+            pick_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, a, err);
+            return cuda_status(cudaGetLastError(), "launching the pick search");
+          }
+          return batch_pick<T>(tv, (const T*)d, u32(nq), tl, a, work.as<u32>(), err, st, shape, work.bytes);
+        });
+    },
+    st);
+  if (launchRc)
+    return launchRc;
   if (rc)
     return rc;
   return finish_sorted_ids(c, nq, r, st);

@@ -325,6 +325,8 @@ int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol,
 template<typename T>
 int batch_plane(const TreeView<T>& tv, const T* planes, u32 nq, bool positive, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4, size_t workBytes = 0);
 template<typename T>
+int batch_pick(const TreeView<T>& tv, const T* pts, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4, size_t workBytes = 0);
+template<typename T>
 int batch_query_program(const TreeView<T>& tv, const QueryProgram<T>& qp, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st,
                         int shape = 4, size_t workBytes = 0);
 template<typename T>

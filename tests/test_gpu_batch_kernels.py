@@ -1,5 +1,5 @@
 """The batched warp-per-query kernels (default algorithm) against the one-query-per-thread kernels
-(OTG_ALGO_PLAIN_FP64) for RangeSearch, FrustumCulling and RayIntersectedAll: identical id lists and
+(OTG_ALGO_PLAIN_FP64) for RangeSearch, FrustumCulling, RayIntersectedAll and PickSearch: identical id lists and
 ray distances, on point and box trees of both scalar types and on a forest. Batches of at most
 8192 queries run split (top levels per query, then their depth-2 subtrees as separate work items);
 larger ones run whole, and both sizes are covered. (Both kernels are checked against the oracle by
@@ -47,6 +47,9 @@ def test_batch_kernels_match_plain(kind, dtype, nq):
         assert_csr_equal(t.range_search(ranges, mode), t.range_search(ranges, mode, algo=otg.ALGO_PLAIN_FP64), f"range {mode}")
     assert_csr_equal(t.frustum_culling(planes)[:2], t.frustum_culling(planes, algo=otg.ALGO_PLAIN_FP64)[:2], "frustum")
     assert_csr_equal(t.ray_all(rays), t.ray_all(rays, algo=otg.ALGO_PLAIN_FP64), "ray_all")
+    pts = (ent[:nq, :3] if kind == "points" else rng.random((nq, 3)) * 100).astype(dtype)  # entity points: exact hits
+    assert_csr_equal(t.pick_search(pts)[:2], t.pick_search(pts, algo=otg.ALGO_PLAIN_FP64)[:2], "pick")
+    assert len(t.pick_search(pts)[1]) > 0
     assert_csr_equal(t.ray_all(rays, max_distance=20.0), t.ray_all(rays, max_distance=20.0, algo=otg.ALGO_PLAIN_FP64), "ray_all bounded")
 
 
