@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(256) radix_histogram_kernel(const K* __restric
 // DEVN: the element count is read from device memory (segOff[0] as unsigned long long, at most n);
 // tiles that start past it end at once (no later tile looks back at them).
 template<typename K, bool SEG = false, bool DEVN = false>
-__global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass_kernel(const K* __restrict__ kin, const u32* __restrict__ vin, K* __restrict__ kout,
+__global__ void __launch_bounds__(kSortThreads, 3) onesweep_pass_kernel(const K* __restrict__ kin, const u32* __restrict__ vin, K* __restrict__ kout,
                                                                      u32* __restrict__ vout, u32 n, u32 shift, const u32* __restrict__ hist,
                                                                      u32* __restrict__ status, u32* __restrict__ tileCounter, u32* __restrict__ err,
                                                                      const uint2* __restrict__ segTiles = nullptr, const u64* __restrict__ segOff = nullptr)
