@@ -411,11 +411,11 @@ def run_gpu(args):
         "gpu_launches": None,
         "clocks": clk.summary(),
     }
-    # kernel launches per build of this workload (33 in the ncu launch list of
+    # kernel launches per build of this workload (as in the ncu launch list of
     # profiles/build16m_launch_list.md): bbox init, bbox, space setup, raster tables, MinPoint table,
-    # codegen, the radix passes, gather, root init, a classify launch per depth 0..D and a split
-    # launch per depth 0..D-1
-    line["gpu_launches"] = args.steps * (6 + passes + 1 + 1 + (MAX_DEPTH + 1) + MAX_DEPTH)
+    # codegen, the radix passes, gather, root init, the root's classify launch and a split launch per
+    # depth 0..D-1
+    line["gpu_launches"] = args.steps * (6 + passes + 1 + 1 + 1 + MAX_DEPTH)
     if rank == 0 and not args.no_cpu_baseline:
         sample = pts_h[:1_000_000]
         rate, kind, threads = cpu_build_rate(sample, 3)

@@ -537,10 +537,11 @@ __device__ __forceinline__ void write_node_min(T* nodeBox, u32 node, u64 key, u3
   p[2] = V2{v[4], v[5]};
 }
 
-// Two launches per depth. emit_classify_kernel, one thread per node: a node that does not split
-// (at most maxElem entities in its subtree, or d == maxDepth) keeps all of them and is finished at
-// once (ProcessNode, :656-683); a node that splits goes to a queue. emit_split_kernel, eight lanes
-// per queued node: lane 0 finds the end of the node's stuck entities (ProcessNode's
+// emit_classify_kernel, one thread per node, decides the roots: a node that does not split (at most
+// maxElem entities in its subtree, or d == maxDepth) keeps all of them and is finished at once
+// (ProcessNode, :656-683); a node that splits goes to a queue. Then one emit_split_kernel launch per
+// depth, eight lanes per queued node, which also decides each child it creates (leaf now, or the
+// next depth's queue, of two alternating queue buffers): lane 0 finds the end of the node's stuck entities (ProcessNode's
 // partition_point, :658-671) and lanes 1..7 the start of child key ranges 1..7
 // (CreateProcessingData's partition_point, :695-711) at the same time, so the dependent-load
 // chain of a node is one binary search deep. Below the root every key of a node's range shares
@@ -624,9 +625,10 @@ constexpr u32 kEmitCountMax = 256;
 template<typename T, typename K, bool IS_BOX>
 __global__ void __launch_bounds__(256) emit_split_kernel(u32 d, u32 D, const K* __restrict__ keys, uint4* __restrict__ link, u64* __restrict__ nodeKey,
                                                          T* __restrict__ nodeBox, unsigned char* __restrict__ nodeDepth, u32* __restrict__ levelCount,
-                                                         const u32* __restrict__ splitCount, const u32* __restrict__ splitQueue, u32 queueCap,
+                                                         u32* __restrict__ splitCount, const u32* __restrict__ splitQueue, u32 queueCap,
                                                          const T* __restrict__ minTab, const Space<T>* __restrict__ spg, u64 maxNodes, u32* __restrict__ err,
-                                                         u32* __restrict__ ownerNode, u32* __restrict__ nodeParent, ForestNodes fn)
+                                                         u32* __restrict__ ownerNode, u32* __restrict__ nodeParent, ForestNodes fn, u64 maxElem,
+                                                         u32* __restrict__ queueOut)
 {
   u32 begin, cnt;
   level_range(levelCount, d, begin, cnt);
@@ -771,18 +773,35 @@ __global__ void __launch_bounds__(256) emit_split_kernel(u32 d, u32 D, const K* 
     warpBase = __shfl_sync(0xffffffffu, warpBase, 31);
     const u32 firstChild = childBase + warpBase + __shfl_sync(0xffffffffu, incl - mine, grp * 8);
     const bool overflow = u64(firstChild) + nchild > maxNodes;
+    u32 ci = 0;
+    bool enq = false;
     if (active)
     {
       if (nonEmpty && !overflow)
       {
-        const u32 ci = firstChild + __popc(ballot & lanemask_lt());
-        nodeKey[ci] = (key << 3) | u64(gl);
-        link[ci] = make_uint4(0, myStart, myStart, nextStart);
+        ci = firstChild + __popc(ballot & lanemask_lt());
+        const u64 ckey = (key << 3) | u64(gl);
+        nodeKey[ci] = ckey;
         nodeDepth[ci] = (unsigned char)(d + 1);
         if (nodeParent)
           nodeParent[ci] = node;
         if (fn.nodeTree)
           fn.nodeTree[ci] = tree;
+        // the child's own split decision (ProcessNode, :656-683), made here instead of by a
+        // classify launch at the next depth: a child that splits goes to the next depth's queue
+        // and gets its children there; one that does not keeps all its entities now
+        enq = u64(nextStart - myStart) > maxElem && d + 1 < D;
+        if (enq)
+          link[ci] = make_uint4(0, myStart, myStart, nextStart);
+        else
+        {
+          link[ci] = make_uint4(0, myStart, nextStart, nextStart);
+          if (ownerNode)
+            for (u32 q = myStart; q < nextStart; ++q)
+              ownerNode[q] = ci;
+          if constexpr (!IS_BOX)
+            write_node_min(nodeBox, ci, ckey, d + 1, mt, tabPerDim, spn->nodeSize);
+        }
       }
       if (gl == 0)
       {
@@ -797,6 +816,23 @@ __global__ void __launch_bounds__(256) emit_split_kernel(u32 d, u32 D, const K* 
       if constexpr (!IS_BOX)
         if (gl < 3)
           write_min_point(nodeBox, node, key, d, gl, mt, tabPerDim, spn);
+    }
+    // warp-aggregated append of the children that split
+    const u32 qm = __ballot_sync(0xffffffffu, enq);
+    if (qm)
+    {
+      u32 qb0 = 0;
+      if (lane == 0)
+        qb0 = atomicAdd(&splitCount[d + 1], u32(__popc(qm)));
+      qb0 = __shfl_sync(0xffffffffu, qb0, 0);
+      if (enq)
+      {
+        const u32 slot = qb0 + __popc(qm & lanemask_lt());
+        if (slot < queueCap)
+          queueOut[slot] = ci;
+        else
+          atomicOr(err, kErrCapacity);
+      }
     }
   }
 }
@@ -960,7 +996,7 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
       (e = t.valsB.ensure(sizeof(u32) * n)) || (e = t.sortedGeom.ensure(sizeof(T) * W * n)) || (e = t.nodeLink.ensure(sizeof(uint4) * maxNodes)) ||
       (e = t.nodeKey.ensure(sizeof(u64) * maxNodes)) || (e = t.nodeBox.ensure(sizeof(T) * 6 * maxNodes)) ||
       (e = t.nodeDepth.ensure(maxNodes)) || (e = t.levelCount.ensure(sizeof(u32) * 64)) ||
-      (e = t.splitQueue.ensure(sizeof(u32) * (n / (t.maxElem + 1) + 2))) || (e = t.space.ensure(sizeof(Space<T>))) ||
+      (e = t.splitQueue.ensure(2 * sizeof(u32) * (n / (t.maxElem + 1) + 2))) || (e = t.space.ensure(sizeof(Space<T>))) ||
       (e = t.sortScratch.ensure(SortScratch::bytes(n, passes))) || (e = t.bboxBits.ensure(sizeof(U) * 6)) ||
       (e = t.rasterTab.ensure(tabBytes)) || (e = t.minTab.ensure(sizeof(T) * minTabEntries)) ||
       (IS_BOX && ((e = t.nodeMax.ensure(sizeof(T) * 3 * maxNodes)) || (e = t.ownerNode.ensure(sizeof(u32) * n)) ||
@@ -1059,18 +1095,18 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   u32* splitQueue = t.splitQueue.as<u32>();
   const u32 queueCap = u32(n / (t.maxElem + 1) + 2);
   root_init_kernel<T><<<1, 32, 0, es>>>(t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeDepth.as<unsigned char>(), levelCount, u32(n), parent);
-  for (u32 d = 0; d <= D; ++d)
+  // the root's decision, then one launch per depth (queues of depths d and d + 1 alternate halves)
+  emit_classify_kernel<T, IS_BOX><<<1, 256, 0, es>>>(0, D, t.maxElem, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(), levelCount,
+                                                     splitCount, splitQueue, queueCap, t.minTab.as<T>(), sp, IS_BOX ? t.ownerNode.as<u32>() : nullptr,
+                                                     t.err.as<u32>(), ForestNodes{});
+  for (u32 d = 0; d < D; ++d)
   {
-    const int classifyBlocks = emit_blocks(d, 1, emitBlocks, ~u64(0), 256);
     const int splitBlocks = emit_blocks(d, 1, emitBlocks, queueCap, 32);
-    emit_classify_kernel<T, IS_BOX><<<classifyBlocks, 256, 0, es>>>(d, D, t.maxElem, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
-                                                                    levelCount, splitCount, splitQueue, queueCap, t.minTab.as<T>(), sp,
-                                                                    IS_BOX ? t.ownerNode.as<u32>() : nullptr, t.err.as<u32>(), ForestNodes{});
-    if (d < D)
-      emit_split_kernel<T, K, IS_BOX><<<splitBlocks, 256, 0, es>>>(d, D, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
-                                                                  t.nodeDepth.as<unsigned char>(), levelCount, splitCount, splitQueue, queueCap,
-                                                                  t.minTab.as<T>(), sp, maxNodes, t.err.as<u32>(),
-                                                                  IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent, ForestNodes{});
+    emit_split_kernel<T, K, IS_BOX><<<splitBlocks, 256, 0, es>>>(d, D, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
+                                                                t.nodeDepth.as<unsigned char>(), levelCount, splitCount, splitQueue + (d & 1) * queueCap,
+                                                                queueCap, t.minTab.as<T>(), sp, maxNodes, t.err.as<u32>(),
+                                                                IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent, ForestNodes{}, t.maxElem,
+                                                                splitQueue + ((d + 1) & 1) * queueCap);
   }
   if ((e = cudaEventRecord(t.join, es)) || (e = cudaStreamWaitEvent(st, t.join, 0)))
     return cuda_status(e, "joining the emission stream");
@@ -1408,7 +1444,7 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
       (e = t.sortedGeom.ensure(sizeof(T) * W * std::max<u64>(n, 1))) || (e = t.nodeLink.ensure(sizeof(uint4) * maxNodes)) ||
       (e = t.nodeKey.ensure(sizeof(u64) * maxNodes)) || (e = t.nodeBox.ensure(sizeof(T) * 6 * maxNodes)) || (e = t.nodeDepth.ensure(maxNodes)) ||
       (e = t.nodeTree.ensure(sizeof(u32) * maxNodes)) || (e = t.levelCount.ensure(sizeof(u32) * 64)) ||
-      (e = t.splitQueue.ensure(sizeof(u32) * (n / (t.maxElem + 1) + 2))) || (e = t.space.ensure(sizeof(Space<T>) * trees)) ||
+      (e = t.splitQueue.ensure(2 * sizeof(u32) * (n / (t.maxElem + 1) + 2))) || (e = t.space.ensure(sizeof(Space<T>) * trees)) ||
       (e = t.sortScratch.ensure(sizeof(u32) * scratchWords)) || (e = t.bboxBits.ensure(sizeof(U) * 6 * trees)) ||
       (e = t.rasterTab.ensure(sizeof(U) * std::max<u64>(tabEntries, 1))) || (e = t.minTab.ensure(sizeof(T) * minEntries)) ||
       (e = t.treeOff.ensure(sizeof(u64) * (trees + 1))) || (e = t.treeD.ensure(sizeof(u32) * trees)) ||
@@ -1489,17 +1525,18 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
   u32* splitCount = levelCount + 32;
   const u32 queueCap = u32(n / (t.maxElem + 1) + 2);
   const ForestNodes fn{ t.nodeTree.as<u32>(), t.treeD.as<u32>(), IS_BOX ? nullptr : t.minOff.as<u64>() };
-  for (u32 d = 0; d <= Dmax; ++d)
-  {
-    emit_classify_kernel<T, IS_BOX><<<emit_blocks(d, trees, emitBlocks, ~u64(0), 256), 256, 0, st>>>(d, Dmax, t.maxElem, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
-                                                                levelCount, splitCount, t.splitQueue.as<u32>(), queueCap, t.minTab.as<T>(), sp,
-                                                                IS_BOX ? t.ownerNode.as<u32>() : nullptr, t.err.as<u32>(), fn);
-    if (d < Dmax)
-      emit_split_kernel<T, K, IS_BOX><<<emit_blocks(d, trees, emitBlocks, queueCap, 32), 256, 0, st>>>(d, Dmax, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(),
-                                                                  t.nodeDepth.as<unsigned char>(), levelCount, splitCount, t.splitQueue.as<u32>(), queueCap,
-                                                                  t.minTab.as<T>(), sp, maxNodes, t.err.as<u32>(),
-                                                                  IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent, fn);
-  }
+  u32* splitQueue = t.splitQueue.as<u32>();
+  // the roots' decisions, then one launch per depth (queues of depths d and d + 1 alternate halves)
+  emit_classify_kernel<T, IS_BOX><<<emit_blocks(0, trees, emitBlocks, ~u64(0), 256), 256, 0, st>>>(0, Dmax, t.maxElem, t.nodeLink.as<uint4>(),
+                                                                                                t.nodeKey.as<u64>(), t.nodeBox.as<T>(), levelCount,
+                                                                                                splitCount, splitQueue, queueCap, t.minTab.as<T>(), sp,
+                                                                                                IS_BOX ? t.ownerNode.as<u32>() : nullptr,
+                                                                                                t.err.as<u32>(), fn);
+  for (u32 d = 0; d < Dmax; ++d)
+    emit_split_kernel<T, K, IS_BOX><<<emit_blocks(d, trees, emitBlocks, queueCap, 32), 256, 0, st>>>(
+      d, Dmax, keys, t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeBox.as<T>(), t.nodeDepth.as<unsigned char>(), levelCount, splitCount,
+      splitQueue + (d & 1) * queueCap, queueCap, t.minTab.as<T>(), sp, maxNodes, t.err.as<u32>(), IS_BOX ? t.ownerNode.as<u32>() : nullptr, parent, fn,
+      t.maxElem, splitQueue + ((d + 1) & 1) * queueCap);
   prof.mark("geometry", st);
   if constexpr (IS_BOX)
   {
