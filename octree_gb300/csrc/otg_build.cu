@@ -49,18 +49,31 @@ __device__ __forceinline__ int load_chunk(const T* __restrict__ ent, u64 n, u64 
   constexpr int E = Chunk<T, W>::E;
   if (vec && first + E <= n)
   {
-    const float4* src = reinterpret_cast<const float4*>(ent + first * W);
-    union
+    // typed vector loads (no union: a union of vectors and scalars is kept in local memory)
+    if constexpr (sizeof(T) == 8)
     {
-      float4 f[3];
-      T t[E * W];
-    } u;
-    u.f[0] = __ldg(src);
-    u.f[1] = __ldg(src + 1);
-    u.f[2] = __ldg(src + 2);
+      const double2* src = reinterpret_cast<const double2*>(ent + first * W);
 #pragma unroll
-    for (int k = 0; k < E * W; ++k)
-      v[k] = u.t[k];
+      for (int j = 0; j < 3; ++j)
+      {
+        const double2 x = __ldg(src + j);
+        v[2 * j] = x.x;
+        v[2 * j + 1] = x.y;
+      }
+    }
+    else
+    {
+      const float4* src = reinterpret_cast<const float4*>(ent + first * W);
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+      {
+        const float4 x = __ldg(src + j);
+        v[4 * j] = x.x;
+        v[4 * j + 1] = x.y;
+        v[4 * j + 2] = x.z;
+        v[4 * j + 3] = x.w;
+      }
+    }
     return E;
   }
   const int cnt = int(min(u64(E), n - first));
