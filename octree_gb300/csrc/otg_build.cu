@@ -1049,7 +1049,8 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   {
     prof.mark("bbox", st);
     bbox_init_kernel<U><<<1, 32, 0, st>>>(t.bboxBits.as<U>());
-    bbox_kernel<T, W><<<grid_blocks((n + Chunk<T, W>::E - 1) / Chunk<T, W>::E, 256, 152 * 8), 256, 0, st>>>(ent, n, vec, t.bboxBits.as<U>());
+    // up to 16 blocks per SM (16M points: 0.0925 ms at 8 per SM, 0.088 ms at 16)
+    bbox_kernel<T, W><<<grid_blocks((n + Chunk<T, W>::E - 1) / Chunk<T, W>::E, 256, 152 * 16), 256, 0, st>>>(ent, n, vec, t.bboxBits.as<U>());
   }
   prof.mark("tables", st);
   space_setup_kernel<T><<<1, 1, 0, st>>>(sp, t.bboxBits.as<U>(), (const T*)box, D, IS_BOX ? 0 : 1);
@@ -1071,7 +1072,9 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   prof.mark("codegen", st);
   const int tabInSmem = tabBytes <= 64 * 1024 ? 1 : 0;
   const size_t cgSmem = tabInSmem ? tabBytes : 0;
-  const int cgBlocks = grid_blocks((n + Chunk<T, W>::E - 1) / Chunk<T, W>::E, 256, 152 * 4);
+  // up to 16 blocks per SM: more blocks in flight than fit at once balance the grid-stride loop
+  // (16M points: 0.184 ms at 4 per SM, 0.168 ms at 16, 0.186 ms at 64)
+  const int cgBlocks = grid_blocks((n + Chunk<T, W>::E - 1) / Chunk<T, W>::E, 256, 152 * 16);
   if (rasterDouble)
   {
     auto kfn = codegen_kernel<T, double, K, IS_BOX>;
