@@ -154,6 +154,108 @@ __global__ void __launch_bounds__(256) bbox_kernel(const T* __restrict__ ent, u6
   }
 }
 
+// Upload and bounding box in one pass over host-mapped entities (16-byte aligned): consecutive
+// threads read consecutive 16-byte units, so the reads over the host link are whole lines; every
+// unit is written to the device copy, and each scalar updates the min or max of its dimension
+// (point coordinates both; box minima the min, box maxima the max).
+template<typename T, int W>
+__global__ void __launch_bounds__(256) pull_bbox_kernel(const T* __restrict__ src, u64 n, T* __restrict__ dst, typename Ord<T>::U* acc)
+{
+  using U = typename Ord<T>::U;
+  using V = typename std::conditional<sizeof(T) == 8, double2, float4>::type;
+  constexpr int PER = int(16 / sizeof(T));
+  U mn[3], mx[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    mn[d] = U(~U(0));
+    mx[d] = U(0);
+  }
+  auto take = [&](T val, u32 c) {
+    const U o = ord_bits(val);
+    const u32 d = c < 3 ? c : c - 3;
+    const bool lo = W == 3 || c < 3, hi = W == 3 || c >= 3;
+    if (d == 0)
+    {
+      mn[0] = lo && lt_ord(o, mn[0]) ? o : mn[0];
+      mx[0] = hi && lt_ord(mx[0], o) ? o : mx[0];
+    }
+    else if (d == 1)
+    {
+      mn[1] = lo && lt_ord(o, mn[1]) ? o : mn[1];
+      mx[1] = hi && lt_ord(mx[1], o) ? o : mx[1];
+    }
+    else
+    {
+      mn[2] = lo && lt_ord(o, mn[2]) ? o : mn[2];
+      mx[2] = hi && lt_ord(mx[2], o) ? o : mx[2];
+    }
+  };
+  const u64 total = n * W, units = total / PER;
+  const u64 stride = u64(gridDim.x) * blockDim.x;
+  for (u64 u = blockIdx.x * u64(blockDim.x) + threadIdx.x; u < units; u += stride)
+  {
+    const V x = reinterpret_cast<const V*>(src)[u];
+    reinterpret_cast<V*>(dst)[u] = x;
+    u32 c = u32((u * PER) % W);
+    if constexpr (sizeof(T) == 8)
+    {
+      take(x.x, c);
+      take(x.y, c + 1 == W ? 0 : c + 1);
+    }
+    else
+    {
+      take(x.x, c);
+      c = c + 1 == W ? 0 : c + 1;
+      take(x.y, c);
+      c = c + 1 == W ? 0 : c + 1;
+      take(x.z, c);
+      c = c + 1 == W ? 0 : c + 1;
+      take(x.w, c);
+    }
+  }
+  for (u64 j = units * PER + blockIdx.x * u64(blockDim.x) + threadIdx.x; j < total; j += stride)
+  {
+    const T val = src[j];
+    dst[j] = val;
+    take(val, u32(j % W));
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+      U a = __shfl_xor_sync(0xffffffffu, mn[d], o);
+      U b = __shfl_xor_sync(0xffffffffu, mx[d], o);
+      mn[d] = lt_ord(a, mn[d]) ? a : mn[d];
+      mx[d] = lt_ord(mx[d], b) ? b : mx[d];
+    }
+  }
+  __shared__ U smn[3][8], smx[3][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+      smn[d][warp] = mn[d];
+      smx[d][warp] = mx[d];
+    }
+  __syncthreads();
+  if (threadIdx.x < 3)
+  {
+    const int d = threadIdx.x;
+    U a = smn[d][0], b = smx[d][0];
+    for (int w = 1; w < int(blockDim.x >> 5); ++w)
+    {
+      a = smn[d][w] < a ? smn[d][w] : a;
+      b = smx[d][w] > b ? smx[d][w] : b;
+    }
+    atomicMin(&acc[d], a);
+    atomicMax(&acc[3 + d], b);
+  }
+}
+
 template<typename U>
 __global__ void bbox_init_kernel(U* acc)
 {
@@ -1009,7 +1111,9 @@ static int emission_stream(TreeState& t, cudaStream_t& es)
 }
 
 template<typename T, typename K, bool IS_BOX>
-static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaStream_t st)
+// pull (optional): the entities in pinned host memory, mapped for the device; the bounding-box pass
+// reads them there and writes the device copy `ent` on the way
+static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaStream_t st, const T* pull = nullptr)
 {
   constexpr int W = IS_BOX ? 6 : 3;
   using U = typename Ord<T>::U;
@@ -1050,7 +1154,11 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
     prof.mark("bbox", st);
     bbox_init_kernel<U><<<1, 32, 0, st>>>(t.bboxBits.as<U>());
     // up to 16 blocks per SM (16M points: 0.0925 ms at 8 per SM, 0.088 ms at 16)
-    bbox_kernel<T, W><<<grid_blocks((n + Chunk<T, W>::E - 1) / Chunk<T, W>::E, 256, 152 * 16), 256, 0, st>>>(ent, n, vec, t.bboxBits.as<U>());
+    if (pull)
+      pull_bbox_kernel<T, W><<<grid_blocks(n * W * sizeof(T) / 16 + 1, 256, 152 * 16), 256, 0, st>>>(pull, n, const_cast<T*>(ent),
+                                                                                                      t.bboxBits.as<U>());
+    else
+      bbox_kernel<T, W><<<grid_blocks((n + Chunk<T, W>::E - 1) / Chunk<T, W>::E, 256, 152 * 16), 256, 0, st>>>(ent, n, vec, t.bboxBits.as<U>());
   }
   prof.mark("tables", st);
   space_setup_kernel<T><<<1, 1, 0, st>>>(sp, t.bboxBits.as<U>(), (const T*)box, D, IS_BOX ? 0 : 1);
@@ -1198,11 +1306,21 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
   // Host entities are copied to the device; device entities are read in place during the build
   // (the caller keeps them alive until the build completes on `st`, as for any stream-ordered call).
   const void* ent = entities;
+  const void* pull = nullptr;
   if (n && mem == OTG_MEM_HOST)
   {
     if ((e = t.entities.ensure(esz * W * n)))
       return cuda_status(e, "allocating entity buffer");
-    if ((e = cudaMemcpyAsync(t.entities.p, entities, esz * W * n, cudaMemcpyHostToDevice, st)))
+    // Pinned host memory that the device can map is read by the bounding-box pass itself, which
+    // writes the device copy as it goes (the upload is bound by the host link either way). Other
+    // host memory, or a given space box (no bounding-box pass), is copied first.
+    cudaPointerAttributes at{};
+    const bool mapped = !box && cudaPointerGetAttributes(&at, entities) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer &&
+                        (reinterpret_cast<uintptr_t>(at.devicePointer) & 15) == 0;
+    cudaGetLastError(); // a pointer unknown to CUDA leaves no error behind
+    if (mapped)
+      pull = at.devicePointer;
+    else if ((e = cudaMemcpyAsync(t.entities.p, entities, esz * W * n, cudaMemcpyHostToDevice, st)))
       return cuda_status(e, "copying entities");
     ent = t.entities.p;
   }
@@ -1231,18 +1349,20 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
   if (t.scalar == OTG_SCALAR_F64)
   {
     const double* p = static_cast<const double*>(ent);
+    const double* q = static_cast<const double*>(pull);
     if (isBox)
-      rc = t.keys32 ? build_impl<double, u32, true>(t, p, dbox, n, st) : build_impl<double, u64, true>(t, p, dbox, n, st);
+      rc = t.keys32 ? build_impl<double, u32, true>(t, p, dbox, n, st, q) : build_impl<double, u64, true>(t, p, dbox, n, st, q);
     else
-      rc = t.keys32 ? build_impl<double, u32, false>(t, p, dbox, n, st) : build_impl<double, u64, false>(t, p, dbox, n, st);
+      rc = t.keys32 ? build_impl<double, u32, false>(t, p, dbox, n, st, q) : build_impl<double, u64, false>(t, p, dbox, n, st, q);
   }
   else
   {
     const float* p = static_cast<const float*>(ent);
+    const float* q = static_cast<const float*>(pull);
     if (isBox)
-      rc = t.keys32 ? build_impl<float, u32, true>(t, p, dbox, n, st) : build_impl<float, u64, true>(t, p, dbox, n, st);
+      rc = t.keys32 ? build_impl<float, u32, true>(t, p, dbox, n, st, q) : build_impl<float, u64, true>(t, p, dbox, n, st, q);
     else
-      rc = t.keys32 ? build_impl<float, u32, false>(t, p, dbox, n, st) : build_impl<float, u64, false>(t, p, dbox, n, st);
+      rc = t.keys32 ? build_impl<float, u32, false>(t, p, dbox, n, st, q) : build_impl<float, u64, false>(t, p, dbox, n, st, q);
   }
   if (rc)
     return rc;
