@@ -427,6 +427,7 @@ def run_gpu(args):
             "sample": f"1M of the 16M points, 3 Creates, location transform and sort on {threads} threads",
         }
     if not args.no_queries:
+        line["static_layout"] = run_static_export(tree, pts_h)
         line["queries"] = run_queries(tree, pts_d, stream)
         line["many_trees"] = run_many_trees()
         line["two_trees"] = run_two_trees()
@@ -437,6 +438,51 @@ def run_gpu(args):
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def run_static_export(tree16, pts16_h, reps=5):
+    """Export of the 16M-point tree to the static linear layout (StaticLinearOrthoTreeCore's
+    arrays): device time of the export, then with the copy of every array to host memory; for
+    scale, the CPU side (the oracle port, or the reference where it was built) building the
+    dynamic tree and then the static layout of a 1M sample on one thread. The GPU export of that
+    sample is checked against the CPU layout."""
+    import ctypes
+
+    import torch
+
+    import octree_gb300 as otg
+
+    lib = otg.library()
+    lay = otg.StaticLayout()
+
+    def export():
+        otg._check(lib.otg_tree_export_static(tree16.h, ctypes.byref(lay), None))
+
+    s_dev = time_query(export, reps)
+    s_host = time_query(lambda: tree16.export_static(), reps)
+    out = {
+        "tree": "the 16M-point Create above (depth 10, max 20)",
+        "dynamic_nodes": int(tree16.node_count),
+        "static_nodes": int(lay.node_count),
+        "export_ms": s_dev * 1e3,
+        "export_plus_host_copy_ms": s_host * 1e3,
+        "launches_per_export": 3 * (MAX_DEPTH + 1) + 2,
+        "bound": "launch latency: three launches per static level and one readback",
+    }
+    sample = np.ascontiguousarray(pts16_h[:1_000_000])
+    lib_o, kind = oracle_lib()
+    t0 = time.perf_counter()
+    ref = lib_o.create(sample, 0, MAX_DEPTH, None, MAX_ELEM).static_layout()
+    out["cpu_dynamic_then_static_1M_s"] = time.perf_counter() - t0
+    out["cpu_kind"] = kind
+    ts = otg.Tree("points").create(sample, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
+    got = ts.export_static()
+    same = all(np.array_equal(got[k], ref[k]) for k in ("child_begins", "segments", "depth", "geometry"))
+    if kind == "port":
+        same = same and np.array_equal(got["entity_storage"], ref["entity_storage"])
+    out["sample_layout_equal_to_cpu"] = bool(same)
+    torch.cuda.synchronize()
+    return out
 
 
 def time_query(fn, reps=3):

@@ -117,6 +117,37 @@ int otg_tree_export_locations(const otg_tree* tree, uint64_t* keys, int mem, voi
 int otg_tree_export_nodes(const otg_tree* tree, uint64_t* keys, double* min_size, uint64_t* entity_offsets, uint32_t* entity_ids,
                           uint32_t* child_count);
 
+/* The tree in the array layout of StaticLinearOrthoTreeCore (core/ot_static_linear_core.h:81-89),
+   node for node as its parallel Create (:524-600) lays out the same entities: nodes breadth first,
+   children in Morton order, each node below the root at the lowest common ancestor of its
+   entities' locations, MinPoint (points) or MBR (boxes) node geometry. The arrays are those of
+   GetNodes() (NodeStorageGeneral: 32-bit segment begins and lengths), GetNodeDepthIDs(),
+   GetEntityStorage() and GetNodeGeometries(). entity_storage lists ids in location order; entities
+   with equal locations are in id order, which the reference's unstable sort leaves unspecified. */
+typedef struct otg_static_layout
+{
+  uint64_t node_count;
+  uint64_t child_begin_count;      /* entries the reference stores: last node with children + 2; 1 without one; 0 when empty */
+  uint64_t entity_count;
+  uint32_t geometry_per_node;      /* scalars: 3 (points: min point) or 6 (boxes: min point, size) */
+  uint32_t scalar_bytes;           /* 8 (double) or 4 (float): the tree's scalar type */
+  const uint32_t* child_begins;    /* device: node_count + 1 entries; node i's children are [b[i], b[i+1]) */
+  const uint32_t* entity_segments; /* device: {begin, length} per node, into entity_storage */
+  const uint8_t* depth_ids;        /* device: node_count */
+  const uint32_t* entity_storage;  /* device: entity_count */
+  const void* geometry;            /* device: node_count * geometry_per_node scalars of the tree's type */
+} otg_static_layout;
+
+/* Computes the static layout of a single built tree on `stream` (synchronises it) and fills `out`
+   with device pointers owned by the tree, valid until its next build, export or destruction.
+   OTG_ERR_INVALID_ARGUMENT for a forest, and where the reference has no such tree: points outside
+   the space of a point tree (its static Build does not end on them) or locations outside the grid. */
+int otg_tree_export_static(otg_tree* tree, otg_static_layout* out, void* stream);
+
+/* Copies an exported static layout into host arrays (sizes as above; a null pointer skips an array). */
+int otg_static_layout_copy(const otg_static_layout* layout, uint32_t* child_begins, uint32_t* entity_segments, uint8_t* depth_ids,
+                           uint32_t* entity_storage, void* geometry);
+
 /* ---------------------------------------------------------------- queries (batched) */
 
 /* RangeSearch(range, entities, mode, tol) per query box (core/ot_query.h:476-583). */

@@ -46,6 +46,8 @@ EXPORTS = [
     ("otg_tree_info_get", _int, [_vp, _vp]),
     ("otg_tree_export_locations", _int, [_vp, _vp, _int, _vp]),
     ("otg_tree_export_nodes", _int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    ("otg_tree_export_static", _int, [_vp, _vp, _vp]),
+    ("otg_static_layout_copy", _int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("otg_range_search", _int, [_vp, _vp, _u64, _int, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_pick_search", _int, [_vp, _vp, _u64, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_knn", _int, [_vp, _vp, _u64, _vp, _u32, _dbl, _dbl, _int, C.POINTER(_vp), _int, _vp]),
@@ -100,6 +102,23 @@ class _TreeInfo(C.Structure):
         ("max_elements", _u64),
         ("space_min", _dbl * 3),
         ("space_max", _dbl * 3),
+    ]
+
+
+class StaticLayout(C.Structure):
+    """otg_static_layout: the device arrays of the static linear layout (include/octree_gb300.h)."""
+
+    _fields_ = [
+        ("node_count", _u64),
+        ("child_begin_count", _u64),
+        ("entity_count", _u64),
+        ("geometry_per_node", _u32),
+        ("scalar_bytes", _u32),
+        ("child_begins", _vp),
+        ("entity_segments", _vp),
+        ("depth_ids", _vp),
+        ("entity_storage", _vp),
+        ("geometry", _vp),
     ]
 
 
@@ -296,6 +315,24 @@ class Tree:
             )
         )
         return dict(keys=keys, min=ms[:, :3], size=ms[:, 3:], eoff=eoff, eids=eids[: int(eoff[-1])], child_count=cc)
+
+    def export_static(self, stream=None):
+        """The tree in StaticLinearOrthoTreeCore's array layout (core/ot_static_linear_core.h),
+        copied to the host: child_begins as the reference stores them, entity segments
+        (begin, length), depth ids, entity storage and node geometry (MinPoint per node for points,
+        MBR min and size for boxes), in the tree's scalar type."""
+        lay = StaticLayout()
+        _check(library().otg_tree_export_static(self.h, C.byref(lay), _stream_ptr(stream)))
+        m, ne, w = lay.node_count, lay.entity_count, lay.geometry_per_node
+        cb = np.zeros(m + 1, np.uint32)
+        seg = np.zeros((m, 2), np.uint32)
+        dep = np.zeros(m, np.uint8)
+        es = np.zeros(ne, np.uint32)
+        geo = np.zeros((m, w), self.dtype)
+        ptr = lambda a: a.ctypes.data_as(_vp) if a.size else None
+        _check(library().otg_static_layout_copy(C.byref(lay), ptr(cb), ptr(seg), ptr(dep), ptr(es), ptr(geo)))
+        return dict(child_begins=cb[: lay.child_begin_count], child_begins_full=cb if m else cb[:0], segments=seg, depth=dep,
+                    entity_storage=es, geometry=geo)
 
     # ------------------------------------------------------------------ queries
     def _query(self, name, args, mem, stream, raw):

@@ -588,17 +588,6 @@ __device__ __forceinline__ u32 upper_bound_key(const K* keys, u32 lo, u32 hi, u6
   return lo;
 }
 
-// every third bit (inverse of part1by2)
-__device__ __forceinline__ u32 compact1by2(u64 x)
-{
-  x &= 0x9249249249249249ULL;
-  x = (x ^ (x >> 2)) & 0x30c30c30c30c30c3ULL;
-  x = (x ^ (x >> 4)) & 0xf00f00f00f00f00fULL;
-  x = (x ^ (x >> 8)) & 0x00ff0000ff0000ffULL;
-  x = (x ^ (x >> 16)) & 0xffff00000000ffffULL;
-  x = (x ^ (x >> 32)) & 0x00000000001fffffULL;
-  return u32(x);
-}
 
 template<typename T>
 __global__ void root_init_kernel(uint4* link, u64* nodeKey, unsigned char* nodeDepth, u32* levelCount, u32 n, u32* nodeParent)

@@ -104,7 +104,8 @@ static int new_result(otg_result** out)
 static void release_tree(TreeState& s)
 {
   DevBuf* bufs[] = { &s.entities, &s.sortedIds, &s.sortedGeom, &s.keysA, &s.keysB, &s.valsB, &s.nodeLink, &s.nodeKey, &s.nodeBox,
-                     &s.nodeMax, &s.nodeDepth, &s.levelCount, &s.space, &s.sortScratch, &s.err, &s.bboxBits, &s.locations, &s.boxDev, &s.ownerNode, &s.nodeParent, &s.rasterTab, &s.minTab, &s.splitQueue, &s.geom32, &s.nodeBox32, &s.treeOff, &s.treeD, &s.nodeTree, &s.tabOff, &s.minOff, &s.segTiles };
+                     &s.nodeMax, &s.nodeDepth, &s.levelCount, &s.space, &s.sortScratch, &s.err, &s.bboxBits, &s.locations, &s.boxDev, &s.ownerNode, &s.nodeParent, &s.rasterTab, &s.minTab, &s.splitQueue, &s.geom32, &s.nodeBox32, &s.treeOff, &s.treeD, &s.nodeTree, &s.tabOff, &s.minOff, &s.segTiles,
+                     &s.stOrder, &s.stChildBegin, &s.stSeg, &s.stDepth, &s.stGeom, &s.stCtl };
   for (DevBuf* b : bufs)
     b->release();
 }
@@ -270,6 +271,49 @@ extern "C"
     if (!keys || !min_size || !entity_offsets || (!entity_ids && t->s.n))
       return OTG_ERR_INVALID_ARGUMENT;
     return export_nodes(t->s, keys, min_size, entity_offsets, entity_ids, child_count);
+  }
+
+  int otg_tree_export_static(otg_tree* t, otg_static_layout* out, void* stream)
+  {
+    if (int rc = require_device())
+      return rc;
+    if (int rc = ready(t, (cudaStream_t)stream))
+      return rc;
+    return export_static(t->s, out, (cudaStream_t)stream);
+  }
+
+  int otg_static_layout_copy(const otg_static_layout* l, uint32_t* child_begins, uint32_t* entity_segments, uint8_t* depth_ids, uint32_t* entity_storage,
+                             void* geometry)
+  {
+    if (!l)
+    {
+      set_error("otg_static_layout_copy: null layout");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+    const uint64_t m = l->node_count;
+    const size_t scalar = l->scalar_bytes;
+    struct Part
+    {
+      void* dst;
+      const void* src;
+      size_t bytes;
+    } parts[] = { { child_begins, l->child_begins, m ? sizeof(uint32_t) * (m + 1) : 0 },
+                  { entity_segments, l->entity_segments, sizeof(uint32_t) * 2 * m },
+                  { depth_ids, l->depth_ids, m },
+                  { entity_storage, l->entity_storage, sizeof(uint32_t) * l->entity_count },
+                  { geometry, l->geometry, scalar * l->geometry_per_node * m } };
+    for (const Part& p : parts)
+      if (p.dst && p.bytes)
+      {
+        if (!p.src)
+        {
+          set_error("otg_static_layout_copy: the layout holds no such array");
+          return OTG_ERR_INVALID_ARGUMENT;
+        }
+        if (cudaError_t e = cudaMemcpy(p.dst, p.src, p.bytes, cudaMemcpyDeviceToHost))
+          return cuda_status(e, "copying the static layout");
+      }
+    return OTG_OK;
   }
 
   int otg_range_search(const otg_tree* t, const void* ranges, uint64_t nq, int mode, double tol, int algo, otg_result** out, int mem, void* stream)

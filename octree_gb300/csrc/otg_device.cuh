@@ -63,6 +63,19 @@ __host__ __device__ __forceinline__ u64 part1by2(u32 g)
   x = (x ^ (x << 2)) & 0x9249249249249249ULL;
   return x;
 }
+
+// every third bit (inverse of part1by2)
+__device__ __forceinline__ u32 compact1by2(u64 x)
+{
+  x &= 0x9249249249249249ULL;
+  x = (x ^ (x >> 2)) & 0x30c30c30c30c30c3ULL;
+  x = (x ^ (x >> 4)) & 0xf00f00f00f00f00fULL;
+  x = (x ^ (x >> 8)) & 0x00ff0000ff0000ffULL;
+  x = (x ^ (x >> 16)) & 0xffff00000000ffffULL;
+  x = (x ^ (x >> 32)) & 0x00000000001fffffULL;
+  return u32(x);
+}
+
 // detail/si_morton.h:519-535 3-D Encode (x -> bit 0, y -> bit 1, z -> bit 2)
 __host__ __device__ __forceinline__ u64 encode3(u32 x, u32 y, u32 z) { return (part1by2(z) << 2) + (part1by2(y) << 1) + part1by2(x); }
 

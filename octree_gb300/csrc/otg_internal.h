@@ -139,6 +139,9 @@ struct TreeState
   DevBuf segTiles;   // uint2 per sort tile: {tree, tile within the tree}
   std::vector<u64> tabOffHost, minOffHost;
   std::vector<uint2> segTilesHost;
+  // static linear layout (otg_static.cu), filled by export_static: the dynamic node of each static
+  // node, then the reference's arrays, and the per-level control block
+  DevBuf stOrder, stChildBegin, stSeg, stDepth, stGeom, stCtl;
   DevBuf geom32;     // FP32 image of sortedGeom for the query filters (built on first use)
   DevBuf nodeBox32;  // FP32 outward-rounded node boxes for the query filters
   bool image32 = false;
@@ -195,6 +198,8 @@ int finish_build(TreeState& t, cudaStream_t st);
 int forest_relaunch(TreeState& t, const void* entities, const void* boxes, cudaStream_t st);
 int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st);
 int export_nodes(const TreeState& t, u64* keys, double* minSize, u64* eoff, u32* eids, u32* childCount);
+// the static linear layout of a single tree (otg_static.cu)
+int export_static(TreeState& t, otg_static_layout* out, cudaStream_t st);
 
 // queries (otg_query.cu). qTree: the tree of each query when t is a forest (null otherwise).
 int query_range(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st,

@@ -22,6 +22,7 @@
 #include <bit>
 #include <cmath>
 #include <cstdint>
+#include <deque>
 #include <functional>
 #include <limits>
 #include <numeric>
@@ -481,6 +482,7 @@ public:
   std::vector<std::array<T, 3>> nodeSize; // MinPoint per-depth sizes (core/ot_base.h:121-134)
   std::unordered_map<u64, Node> nodes;
   std::vector<u64> locationKeys; // per entity, input order
+  std::vector<u32> sortedOrder;  // entity ids in sorted-location order (ties by id)
 
   const T* ent(u32 id) const { return &geom[size_t(id) * (isBox ? 6 : 3)]; }
 
@@ -635,6 +637,7 @@ public:
     geom.assign(entities, entities + n * (isBox ? 6 : 3));
     nodes.clear();
     locationKeys.clear();
+    sortedOrder.clear();
 
     // :759 box space: given, else IGM::GetBoundingBoxAD (internal_geometry_module.h:342-370)
     if (box)
@@ -726,6 +729,7 @@ public:
 
     // :717-747 BuildSubtree (depth-first emission)
     build_subtree(root, 0, order, 0, n);
+    sortedOrder = std::move(order);
 
     // :803-806 node geometry
     if (isBox)
@@ -876,6 +880,153 @@ public:
       root.minPoint[d] = bmin[d];
       nodeSize[0][d] = bmax[d] - bmin[d];
     }
+  }
+
+  // ------------------------------------------------------------------ static linear layout
+  // StaticLinearOrthoTreeCore (core/ot_static_linear_core.h) over the same sorted locations: the
+  // parallel Create (:524-600: locations sorted, so every child group is one run), Build (:419-521:
+  // breadth first; a node with more than maxElem entities below max depth keeps its entities of
+  // its own depth and splits the rest by the digit of the next level; each group becomes a node at
+  // the lowest common ancestor of its locations, detail/si_morton.h:347-387), CreateNode
+  // (:383-414: child segment begins only up to the last node with children) and the node geometry
+  // (:346-366 MinPoint; :281-325 MBR, a node's entities and then its children's min + size).
+  struct StaticLayout
+  {
+    std::vector<u32> childBegins;         // nodeChildSegmentBegins as stored
+    std::vector<u32> segBegin, segLength; // nodeEntitySegment
+    std::vector<unsigned char> depth;     // m_nodeDepthIDs
+    std::vector<u32> entityStorage;       // m_entityStorage
+    std::vector<T> geometry;              // per node: MinPoint (3) or MBR min and size (6)
+  };
+
+  // False where the layout is undefined: a point tree holding points outside its space. Their
+  // location is the root's (depth 0, si_mortongrid.h:57-62), they lead the group of child 0, and a
+  // group placed at its first location's depth would be placed at depth 0 again and again.
+  bool static_layout(StaticLayout& s) const
+  {
+    s = StaticLayout{};
+    if (N == 0)
+      return true; // :539-540: no node at all
+    if (!isBox)
+      for (size_t i = 0; i < N; ++i)
+        if (key_loc_depth(locationKeys[i]) != D)
+          return false;
+    auto keyAt = [&](size_t pos) { return locationKeys[sortedOrder[pos]]; };
+    struct Item
+    {
+      u64 loc;
+      u32 depth;
+      u32 begin, count;
+    };
+    std::deque<Item> queue;
+    queue.push_back({ 0, 0, 0, u32(N) });
+    s.childBegins.push_back(1);
+    auto createNode = [&](const Item& it, u32 ownCount, u32 childCount) {
+      const u32 id = u32(s.depth.size());
+      s.depth.push_back((unsigned char)it.depth);
+      s.segBegin.push_back(it.begin);
+      s.segLength.push_back(ownCount);
+      if (childCount > 0)
+      {
+        s.childBegins.resize(id + 2, s.childBegins.back());
+        s.childBegins.back() += childCount;
+      }
+      if (!isBox)
+      {
+        Node tmp;
+        tmp.key = (u64(1) << (3 * it.depth)) | (it.loc >> (3 * (D - it.depth)));
+        init_min_point(tmp);
+        s.geometry.insert(s.geometry.end(), tmp.minPoint, tmp.minPoint + 3);
+      }
+    };
+    while (!queue.empty())
+    {
+      const Item it = queue.front();
+      queue.pop_front();
+      if (it.count <= maxElem || it.depth >= D)
+      {
+        createNode(it, it.count, 0);
+        continue;
+      }
+      u32 pos = it.begin;
+      const u32 end = it.begin + it.count;
+      u32 stuck = 0;
+      if (isBox)
+      {
+        while (pos < end && key_loc_depth(keyAt(pos)) == it.depth)
+          ++pos;
+        stuck = pos - it.begin;
+        if (stuck == it.count)
+        {
+          createNode(it, it.count, 0);
+          continue;
+        }
+      }
+      const u32 examined = D - (it.depth + 1);
+      const u64 mask = u64(7) << (3 * examined);
+      u32 children = 0;
+      while (pos < end)
+      {
+        const u64 pivot = keyAt(pos);
+        const u64 flag = key_loc(pivot) & mask;
+        u32 minDepth = key_loc_depth(pivot);
+        u64 diff = 0;
+        u32 e = pos;
+        while (e < end && (key_loc(keyAt(e)) & mask) == flag)
+        {
+          if (isBox)
+            minDepth = std::min(minDepth, key_loc_depth(keyAt(e)));
+          diff |= key_loc(pivot) ^ key_loc(keyAt(e));
+          ++e;
+        }
+        const u32 levelDiff = (u32(std::bit_width(diff)) + 2) / 3;
+        queue.push_back({ key_loc(pivot), std::min(minDepth, D - levelDiff), pos, e - pos });
+        ++children;
+        pos = e;
+      }
+      createNode(it, stuck, children);
+    }
+    s.entityStorage = sortedOrder;
+    if (isBox)
+    {
+      // children have larger ids than their parent, so one pass from the last node up suffices
+      const size_t M = s.depth.size();
+      s.geometry.assign(M * 6, T(0));
+      for (size_t id = M; id-- > 0;)
+      {
+        T bmin[3], bmax[3];
+        for (int d = 0; d < 3; ++d)
+        {
+          bmin[d] = std::numeric_limits<T>::max();
+          bmax[d] = -std::numeric_limits<T>::max();
+        }
+        for (u32 j = s.segBegin[id]; j < s.segBegin[id] + s.segLength[id]; ++j)
+        {
+          const T* e = ent(s.entityStorage[j]);
+          for (int d = 0; d < 3; ++d)
+          {
+            bmin[d] = std::min(bmin[d], e[d]);
+            bmax[d] = std::max(bmax[d], e[3 + d]);
+          }
+        }
+        if (id + 1 < s.childBegins.size())
+          for (u32 c = s.childBegins[id]; c < s.childBegins[id + 1]; ++c)
+          {
+            const T* g = &s.geometry[size_t(c) * 6];
+            for (int d = 0; d < 3; ++d)
+            {
+              bmin[d] = std::min(bmin[d], g[d]);
+              bmax[d] = std::max(bmax[d], T(g[d] + g[3 + d]));
+            }
+          }
+        for (int d = 0; d < 3; ++d)
+        {
+          s.geometry[id * 6 + d] = bmin[d];
+          s.geometry[id * 6 + 3 + d] = bmax[d] - bmin[d];
+        }
+      }
+    }
+    return true;
   }
 
   // ------------------------------------------------------------------ node accessors

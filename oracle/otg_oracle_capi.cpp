@@ -33,6 +33,35 @@ struct Result
   std::vector<double> dist;
 };
 
+// static layout flattened for the C-ABI: segments as {begin, length} pairs, geometry widened to double
+struct StaticOut
+{
+  std::vector<uint32_t> childBegins, segments, entityStorage;
+  std::vector<uint8_t> depth;
+  std::vector<double> geometry;
+  uint64_t geomPerNode = 3;
+};
+
+template<typename T>
+bool fill_static(const Tree<T>& t, StaticOut& o)
+{
+  typename Tree<T>::StaticLayout s;
+  if (!t.static_layout(s))
+    return false;
+  o.childBegins = s.childBegins;
+  o.segments.resize(2 * s.segBegin.size());
+  for (size_t i = 0; i < s.segBegin.size(); ++i)
+  {
+    o.segments[2 * i] = s.segBegin[i];
+    o.segments[2 * i + 1] = s.segLength[i];
+  }
+  o.depth.assign(s.depth.begin(), s.depth.end());
+  o.entityStorage = s.entityStorage;
+  o.geometry.assign(s.geometry.begin(), s.geometry.end());
+  o.geomPerNode = t.isBox ? 6 : 3;
+  return true;
+}
+
 template<typename T>
 T tol_or_default(double tol)
 {
@@ -233,6 +262,39 @@ extern "C"
     return a->scalar == 0 ? a->d->nodes.size() : a->f->nodes.size();
   }
   // per-entity compact location key (loc << 5 | depth), input order
+  // Static linear layout (Tree::static_layout): a handle, or null where the layout is undefined.
+  // Sizes: {nodes, stored child segment begins, entities, scalars of geometry per node}.
+  void* oro_static(void* h)
+  {
+    auto* a = (AnyTree*)h;
+    auto* out = new StaticOut();
+    bool ok = a->scalar == 0 ? fill_static(*a->d, *out) : fill_static(*a->f, *out);
+    if (!ok)
+    {
+      delete out;
+      return nullptr;
+    }
+    return out;
+  }
+  void oro_static_sizes(void* s, uint64_t* sizes4)
+  {
+    auto* o = (StaticOut*)s;
+    sizes4[0] = o->depth.size();
+    sizes4[1] = o->childBegins.size();
+    sizes4[2] = o->entityStorage.size();
+    sizes4[3] = o->geomPerNode;
+  }
+  void oro_static_copy(void* s, uint32_t* childBegins, uint32_t* segments, uint8_t* depth, uint32_t* entityStorage, double* geometry)
+  {
+    auto* o = (StaticOut*)s;
+    std::memcpy(childBegins, o->childBegins.data(), o->childBegins.size() * sizeof(uint32_t));
+    std::memcpy(segments, o->segments.data(), o->segments.size() * sizeof(uint32_t));
+    std::memcpy(depth, o->depth.data(), o->depth.size());
+    std::memcpy(entityStorage, o->entityStorage.data(), o->entityStorage.size() * sizeof(uint32_t));
+    std::memcpy(geometry, o->geometry.data(), o->geometry.size() * sizeof(double));
+  }
+  void oro_static_free(void* s) { delete (StaticOut*)s; }
+
   void oro_location_keys(void* h, uint64_t* out)
   {
     auto* a = (AnyTree*)h;

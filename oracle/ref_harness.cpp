@@ -23,6 +23,12 @@ template<typename T>
 using LooseBoxTree = OrthoTreeBoxND<3, true, T>;
 template<typename T>
 using BoxTree = OrthoTreeBoxND<3, false, T>;
+template<typename T>
+using StaticPointTree = StaticOrthoTreePointND<3, T>;
+template<typename T>
+using StaticLooseBoxTree = StaticOrthoTreeBoxND<3, true, T>;
+template<typename T>
+using StaticBoxTree = StaticOrthoTreeBoxND<3, false, T>;
 
 struct Result
 {
@@ -45,7 +51,63 @@ struct AnyRef
   std::unique_ptr<LooseBoxTree<float>> lbf;
   std::unique_ptr<BoxTree<float>> bf;
   std::vector<uint64_t> locKeys;
+  // the Create arguments, for the static tree of the same entities
+  uint32_t maxDepthArg = 0;
+  uint64_t maxElem = 16;
+  bool hasBox = false;
+  std::vector<double> boxd;
+  std::vector<float> boxf;
 };
+
+// StaticLinearOrthoTreeCore's arrays (ORTHOTREE__PUBLIC_LINEARDATA_INTERFACE), widened to 32 bits
+struct StaticOut
+{
+  std::vector<uint32_t> childBegins, segments, entityStorage;
+  std::vector<uint8_t> depth;
+  std::vector<double> geometry;
+  uint64_t geomPerNode = 3;
+};
+
+template<typename StaticTree, typename T, typename Span>
+StaticOut* static_dump(Span ents, const AnyRef* a, const std::vector<T>& box, bool isBox)
+{
+  std::optional<typename StaticTree::TBox> ob;
+  if (a->hasBox)
+    ob = *reinterpret_cast<const typename StaticTree::TBox*>(box.data());
+  std::optional<depth_t> od;
+  if (a->maxDepthArg)
+    od = a->maxDepthArg;
+  StaticTree t(PAR_EXEC, ents, od, ob, a->maxElem);
+  auto* o = new StaticOut();
+  std::visit(
+    [&](auto const& nodes) {
+      for (auto v : nodes.nodeChildSegmentBegins)
+        o->childBegins.push_back(uint32_t(v));
+      for (auto const& sg : nodes.nodeEntitySegment)
+      {
+        o->segments.push_back(uint32_t(sg.begin));
+        o->segments.push_back(uint32_t(sg.length));
+      }
+    },
+    t.GetNodes());
+  o->depth.assign(t.GetNodeDepthIDs().begin(), t.GetNodeDepthIDs().end());
+  o->entityStorage.assign(t.GetEntityStorage().begin(), t.GetEntityStorage().end());
+  o->geomPerNode = isBox ? 6 : 3;
+  for (auto const& g : t.GetNodeGeometries())
+  {
+    if constexpr (requires { g.minPoint; })
+    {
+      for (int d = 0; d < 3; ++d)
+        o->geometry.push_back(double(g.minPoint[d]));
+      for (int d = 0; d < 3; ++d)
+        o->geometry.push_back(double(g.size[d]));
+    }
+    else
+      for (int d = 0; d < 3; ++d)
+        o->geometry.push_back(double(g[d]));
+  }
+  return o;
+}
 
 template<typename T>
 std::span<const PointND<3, T>> pts_span(const std::vector<T>& v)
@@ -330,6 +392,13 @@ extern "C"
     auto* a = new AnyRef();
     a->scalar = scalar;
     a->kind = kind;
+    a->maxDepthArg = maxDepth;
+    a->maxElem = maxElem;
+    a->hasBox = box != nullptr;
+    if (box && scalar == 0)
+      a->boxd.assign((const double*)box, (const double*)box + 6);
+    if (box && scalar == 1)
+      a->boxf.assign((const float*)box, (const float*)box + 6);
     size_t w = kind == 0 ? 3 : 6;
     if (scalar == 0)
     {
@@ -361,6 +430,49 @@ extern "C"
   {
     return with_tree((AnyRef*)h, [](auto& t, auto, auto, auto) { return uint64_t(t.GetNodeCount()); });
   }
+  // The reference's static tree of the same entities (PAR_EXEC Create), or null for a point tree
+  // holding points outside its space: the reference's static Build does not end on those when the
+  // group of child 0 holds more than maxElem entities, so it is not called for them.
+  void* oro_static(void* h)
+  {
+    auto* a = (AnyRef*)h;
+    if (a->kind == 0)
+      for (auto k : a->locKeys)
+        if ((k & 31u) != a->D)
+          return nullptr;
+    if (a->scalar == 0)
+    {
+      if (a->kind == 0)
+        return static_dump<StaticPointTree<double>>(pts_span(a->ed), a, a->boxd, false);
+      if (a->kind == 1)
+        return static_dump<StaticLooseBoxTree<double>>(box_span(a->ed), a, a->boxd, true);
+      return static_dump<StaticBoxTree<double>>(box_span(a->ed), a, a->boxd, true);
+    }
+    if (a->kind == 0)
+      return static_dump<StaticPointTree<float>>(pts_span(a->ef), a, a->boxf, false);
+    if (a->kind == 1)
+      return static_dump<StaticLooseBoxTree<float>>(box_span(a->ef), a, a->boxf, true);
+    return static_dump<StaticBoxTree<float>>(box_span(a->ef), a, a->boxf, true);
+  }
+  void oro_static_sizes(void* s, uint64_t* sizes4)
+  {
+    auto* o = (StaticOut*)s;
+    sizes4[0] = o->depth.size();
+    sizes4[1] = o->childBegins.size();
+    sizes4[2] = o->entityStorage.size();
+    sizes4[3] = o->geomPerNode;
+  }
+  void oro_static_copy(void* s, uint32_t* childBegins, uint32_t* segments, uint8_t* depth, uint32_t* entityStorage, double* geometry)
+  {
+    auto* o = (StaticOut*)s;
+    std::memcpy(childBegins, o->childBegins.data(), o->childBegins.size() * sizeof(uint32_t));
+    std::memcpy(segments, o->segments.data(), o->segments.size() * sizeof(uint32_t));
+    std::memcpy(depth, o->depth.data(), o->depth.size());
+    std::memcpy(entityStorage, o->entityStorage.data(), o->entityStorage.size() * sizeof(uint32_t));
+    std::memcpy(geometry, o->geometry.data(), o->geometry.size() * sizeof(double));
+  }
+  void oro_static_free(void* s) { delete (StaticOut*)s; }
+
   void oro_location_keys(void* h, uint64_t* out)
   {
     auto* a = (AnyRef*)h;

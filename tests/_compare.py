@@ -102,3 +102,35 @@ def random_query_program(rng, nq, scale, dtype):
         np.array(crossing, np.uint8),
         np.array(boxes, dtype).reshape(-1, 6),
     )
+
+
+STATIC_KEYS = ("child_begins", "segments", "depth", "entity_storage", "geometry")
+
+
+def static_from_golden(g):
+    """The reference's static layout stored in a fixture, or None where it is undefined."""
+    if not int(g["static_defined"]):
+        return None
+    return {k: g["static_" + k] for k in STATIC_KEYS}
+
+
+def assert_static_equal(a, b, what, exact_storage=False):
+    """Static linear layouts (StaticLinearOrthoTreeCore's arrays) equal array for array: child
+    segment begins as stored, entity segments, depth ids and node geometry bit for bit (geometry
+    compared in double; float values widen exactly). Entity storage holds the same ids in every
+    node's segment; exact_storage also asks for the same order inside segments (entities with
+    equal locations are in id order on both sides unless one side is the reference, whose
+    unstable sort leaves them unspecified)."""
+    for k in ("child_begins", "segments", "depth"):
+        assert a[k].shape == b[k].shape and np.array_equal(a[k], b[k]), f"{what}: static {k}"
+    ga, gb = np.asarray(a["geometry"], np.float64), np.asarray(b["geometry"], np.float64)
+    assert ga.shape == gb.shape and np.array_equal(ga, gb), f"{what}: static geometry"
+    ea, eb = a["entity_storage"], b["entity_storage"]
+    assert ea.shape == eb.shape, f"{what}: static entity storage size"
+    if exact_storage:
+        assert np.array_equal(ea, eb), f"{what}: static entity storage"
+        return
+    for bg, ln in a["segments"]:
+        sa, sb = np.sort(ea[bg : bg + ln]), np.sort(eb[bg : bg + ln])
+        assert np.array_equal(sa, sb), f"{what}: static entities of the segment at {bg}"
+    assert np.array_equal(np.sort(ea), np.sort(eb)), f"{what}: static entity storage as a set"

@@ -52,6 +52,10 @@ class OracleLib:
             "oro_res_copy": (None, [_vp, _vp, _vp, _vp]),
             "oro_res_free": (None, [_vp]),
             "oro_time_create_points": (_dbl, [_vp, _u64, _u32, _u64, _int]),
+            "oro_static": (_vp, [_vp]),
+            "oro_static_sizes": (None, [_vp, _vp]),
+            "oro_static_copy": (None, [_vp, _vp, _vp, _vp, _vp, _vp]),
+            "oro_static_free": (None, [_vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -124,6 +128,26 @@ class OracleTree:
     @property
     def node_count(self):
         return self.lib.oro_node_count(self.h)
+
+    def static_layout(self):
+        """The static linear layout of the same entities (StaticLinearOrthoTreeCore's arrays), or
+        None where it is undefined (a point tree holding points outside its space)."""
+        h = self.lib.oro_static(self.h)
+        if not h:
+            return None
+        try:
+            sz = np.zeros(4, np.uint64)
+            self.lib.oro_static_sizes(h, _ptr(sz))
+            m, nb, ne, w = (int(v) for v in sz)
+            cb = np.zeros(max(nb, 1), np.uint32)
+            seg = np.zeros((max(m, 1), 2), np.uint32)
+            dep = np.zeros(max(m, 1), np.uint8)
+            es = np.zeros(max(ne, 1), np.uint32)
+            geo = np.zeros((max(m, 1), w), np.float64)
+            self.lib.oro_static_copy(h, _ptr(cb), _ptr(seg), _ptr(dep), _ptr(es), _ptr(geo))
+        finally:
+            self.lib.oro_static_free(h)
+        return dict(child_begins=cb[:nb], segments=seg[:m], depth=dep[:m], entity_storage=es[:ne], geometry=geo[:m])
 
     def location_keys(self):
         out = np.zeros(self.n, np.uint64)

@@ -82,6 +82,13 @@ def run_case(name, ent, kind, max_depth, box, max_elem, q, ray_tol):
         t2 = R.create(other, kind, max_depth, None, max_elem)
         out["other"] = other
         out["collide_pair"] = t.collide_pair(t2)
+    # the reference's static linear tree of the same entities (StaticOctreePoint / StaticOctreeBox,
+    # parallel Create); undefined for point trees holding points outside their space
+    st = t.static_layout()
+    out["static_defined"] = np.int32(st is not None)
+    if st is not None:
+        for k, v in st.items():
+            out["static_" + k] = v
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(name, "nodes", len(nd["keys"]), "depth", t.max_depth)
 

@@ -3,7 +3,7 @@ itself (tests/golden/make_golden.py). This pins the restatement to the reference
 import numpy as np
 import pytest
 
-from _compare import assert_csr_equal, golden_cases, load_golden, node_dict
+from _compare import assert_csr_equal, assert_static_equal, golden_cases, load_golden, node_dict, static_from_golden
 from _oracle_lib import KIND_POINTS, oracle
 
 
@@ -64,3 +64,16 @@ def test_threaded_oracle_create_matches_sequential(kind):
     na, nb = a.nodes(), b.nodes()
     for k in na:
         assert np.array_equal(na[k], nb[k]), k
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_oracle_static_layout_matches_reference_fixture(name):
+    """The static linear layout (StaticLinearOrthoTreeCore's arrays) of the same entities."""
+    g = load_golden(name)
+    t = oracle().create(g["entities"], int(g["kind"]), int(g["max_depth"]), g.get("box"), int(g["max_elem"]))
+    ref = static_from_golden(g)
+    got = t.static_layout()
+    if ref is None:
+        assert got is None
+        return
+    assert_static_equal(got, ref, name)

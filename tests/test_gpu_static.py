@@ -1,0 +1,127 @@
+"""Export to the static linear layout (otg_tree_export_static): the GPU-built tree in the arrays of
+the reference's StaticLinearOrthoTreeCore, against the reference's own static trees (golden
+fixtures) and the CPU oracle's restatement on seeded inputs, with the refusals where the reference
+has no such tree. Child segment begins, entity segments, depth ids and node geometry are compared
+bit for bit; entity storage exactly against the oracle (both keep equal locations in id order) and
+per node as sets against the reference (its unstable sort leaves that order unspecified)."""
+import numpy as np
+import pytest
+
+import octree_gb300 as otg
+from _compare import assert_static_equal, golden_cases, load_golden, static_from_golden
+from _oracle_lib import KIND_LOOSE_BOXES, KIND_POINTS, oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_tree(ent, kind, max_depth, box, max_elem):
+    t = otg.Tree("points" if kind == KIND_POINTS else "boxes", ent.dtype)
+    return t.create(ent, max_depth=max_depth, box=box, max_elements=max_elem)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_static_layout_matches_reference_fixture(name):
+    g = load_golden(name)
+    kind = int(g["kind"])
+    t = _gpu_tree(g["entities"], kind, int(g["max_depth"]), g.get("box"), int(g["max_elem"]))
+    ref = static_from_golden(g)
+    if ref is None:
+        with pytest.raises(otg.OtgError):
+            t.export_static()
+        return
+    assert_static_equal(t.export_static(), ref, name)
+
+
+def _cases():
+    rng = np.random.default_rng(2026)
+    pts = rng.random((20000, 3)) * 100
+    clustered = np.concatenate(
+        [rng.normal(50, 0.01, (12000, 3)), rng.random((8000, 3)) * 100, np.repeat(rng.random((20, 3)) * 100, 60, 0)]
+    )
+    c = rng.random((15000, 3)) * 100
+    h = rng.lognormal(np.log(0.8), 0.7, (15000, 3))
+    boxes = np.concatenate([c - h, c + h], 1)
+    big = np.array([[-50.0, -50, -50, 200, 200, 200], [1.0, 1, 1, 99, 99, 99]])
+    space = np.array([0.0, 0, 0, 100, 100, 100])
+    return {
+        "points": (pts, KIND_POINTS, 8, None, 16),
+        "points_f32": (pts.astype(np.float32), KIND_POINTS, 8, None, 16),
+        "points_keys64": (clustered, KIND_POINTS, 19, None, 4),
+        "clustered_estimated_depth": (clustered, KIND_POINTS, 0, None, 20),
+        "max_elem_1": (pts[:3000], KIND_POINTS, 10, None, 1),
+        "root_leaf": (pts[:7], KIND_POINTS, 6, None, 16),
+        "depth_0": (pts[:300], KIND_POINTS, 1, None, 16),
+        "duplicates": (np.repeat(pts[:40], 30, 0), KIND_POINTS, 10, None, 8),
+        "boxes": (boxes, KIND_LOOSE_BOXES, 8, None, 8),
+        "boxes_f32": (boxes.astype(np.float32), KIND_LOOSE_BOXES, 8, None, 8),
+        "boxes_deep": (boxes, KIND_LOOSE_BOXES, 17, None, 2),
+        "boxes_outside_space": (np.concatenate([boxes, big]), KIND_LOOSE_BOXES, 6, space, 4),
+        "duplicate_boxes": (np.repeat(boxes[:30], 40, 0), KIND_LOOSE_BOXES, 12, None, 6),
+    }
+
+
+@pytest.mark.parametrize("case", list(_cases()))
+def test_static_layout_matches_oracle(case):
+    ent, kind, depth, box, max_elem = _cases()[case]
+    t = _gpu_tree(ent, kind, depth, box, max_elem)
+    ref = oracle().create(ent, kind, depth, box, max_elem).static_layout()
+    assert ref is not None
+    got = t.export_static()
+    assert_static_equal(got, ref, case, exact_storage=True)
+    # the exported geometry is in the tree's own scalar type
+    assert got["geometry"].dtype == ent.dtype
+
+
+def test_static_layout_empty_tree():
+    t = _gpu_tree(np.zeros((0, 3)), KIND_POINTS, 4, None, 16)
+    s = t.export_static()
+    assert s["child_begins"].size == 0 and s["segments"].shape == (0, 2) and s["depth"].size == 0 and s["entity_storage"].size == 0
+
+
+def test_static_layout_refusals():
+    rng = np.random.default_rng(3)
+    pts = rng.random((2000, 3))
+    # points outside the given space: the reference's static Build does not end on them
+    t = _gpu_tree(pts, KIND_POINTS, 5, np.array([0.2, 0.2, 0.2, 0.8, 0.8, 0.8]), 4)
+    with pytest.raises(otg.OtgError):
+        t.export_static()
+    # a forest has no single static layout
+    f = otg.Forest("points").create(pts, np.array([0, 1000, 2000], np.uint64))
+    with pytest.raises(otg.OtgError):
+        f.export_static()
+    # the tree stays usable after a refusal
+    assert t.range_search(np.array([[0.0, 0, 0, 1, 1, 1]]))[1].size == 2000
+
+
+def test_static_layout_full_size_properties():
+    """16M clustered points (depth 10, max 20): the layout is a tree over all entities, numbered
+    breadth first with children in location order, and equals the oracle on a 2M-point sample."""
+    rng = np.random.default_rng(301)
+    n = 16_000_000
+    pts = np.concatenate([rng.random((int(n * 0.7), 3)), rng.normal(0.5, 0.05, (n - int(n * 0.7), 3))])
+    t = _gpu_tree(pts, KIND_POINTS, 10, None, 20)
+    s = t.export_static()
+    m = s["depth"].size
+    cb = s["child_begins_full"]
+    seg = s["segments"].astype(np.int64)
+    # every entity in exactly one segment
+    assert seg[:, 1].sum() == n
+    assert np.array_equal(np.sort(s["entity_storage"]), np.arange(n, dtype=np.uint32))
+    # child segments: contiguous, in id order, covering nodes 1..m-1 once
+    assert cb[0] == 1 and cb[-1] == m and np.all(np.diff(cb.astype(np.int64)) >= 0)
+    cnt = np.diff(cb.astype(np.int64))
+    parent = np.repeat(np.arange(m), cnt)
+    assert parent.size == m - 1
+    child = np.arange(1, m)
+    # children are deeper than their parent, and their ranges follow the parent's own entities
+    assert np.all(s["depth"][child] > s["depth"][parent])
+    assert np.all(seg[child, 0] >= seg[parent, 0] + seg[parent, 1])
+    # siblings in location order: entity segment begins increase along each child segment
+    same = parent[1:] == parent[:-1]
+    assert np.all(seg[child[1:], 0][same] > seg[child[:-1], 0][same])
+    # a node with children is not a pass-through: two or more children, or entities of its own
+    has = cnt > 0
+    assert np.all((cnt[has] >= 2) | (seg[has, 1] > 0) | (np.arange(m)[has] == 0))
+    sample = pts[:2_000_000]
+    ts = _gpu_tree(sample, KIND_POINTS, 10, None, 20)
+    assert_static_equal(ts.export_static(), oracle().create(sample, KIND_POINTS, 10, None, 20).static_layout(), "2M sample", exact_storage=True)

@@ -4,6 +4,7 @@ the committed golden fixtures carry the pin."""
 import numpy as np
 import pytest
 
+from _compare import assert_static_equal
 from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, oracle, reference
 
 pytestmark = pytest.mark.skipif(reference() is None, reason="reference harness not built here")
@@ -131,3 +132,47 @@ def test_combined_query(seed, kind, dtype):
     for or_op in (False, True):
         for x, y in zip(a.query(*prog, or_op=or_op), b.query(*prog, or_op=or_op)):
             assert np.array_equal(x, y)
+
+
+def _static_cases():
+    rng = np.random.default_rng(77)
+    pts = rng.random((4000, 3))
+    clustered = np.concatenate([rng.normal(0.5, 0.001, (2500, 3)), rng.random((1500, 3)), np.repeat(rng.random((5, 3)), 40, 0)])
+    c = rng.random((3000, 3)) * 100
+    h = rng.random((3000, 3)) * 2
+    boxes = np.concatenate([c - h, c + h], 1)
+    outside = np.concatenate([boxes, [[-50.0, -50, -50, 200, 200, 200], [-5.0, -5, -5, -1, -1, -1]]])
+    space = np.array([0.0, 0, 0, 100, 100, 100])
+    return {
+        "points": (pts, KIND_POINTS, 6, None, 8),
+        "points_f32": (pts.astype(np.float32), KIND_POINTS, 6, None, 8),
+        "clustered_deep": (clustered, KIND_POINTS, 19, None, 2),
+        "clustered_estimated_depth": (clustered, KIND_POINTS, 0, None, 16),
+        "max_elem_1": (pts[:900], KIND_POINTS, 8, None, 1),
+        "single_leaf": (pts[:10], KIND_POINTS, 6, None, 16),
+        "empty": (np.zeros((0, 3)), KIND_POINTS, 4, None, 16),
+        "loose_boxes": (boxes, KIND_LOOSE_BOXES, 7, None, 4),
+        "loose_boxes_f32": (boxes.astype(np.float32), KIND_LOOSE_BOXES, 7, None, 4),
+        "loose_boxes_outside_space": (outside, KIND_LOOSE_BOXES, 6, space, 3),
+        "boxes_outside_space": (outside, KIND_BOXES, 6, space, 3),
+        "duplicate_boxes": (np.repeat(boxes[:5], 50, 0), KIND_LOOSE_BOXES, 9, None, 4),
+        "loose_boxes_deep": (boxes, KIND_LOOSE_BOXES, 17, None, 2),
+    }
+
+
+@pytest.mark.parametrize("case", list(_static_cases()))
+def test_static_layout(case):
+    """The oracle's static linear layout against the reference's StaticOctreePoint / StaticOctreeBox
+    (parallel Create) of the same entities."""
+    ent, kind, depth, box, max_elem = _static_cases()[case]
+    got = oracle().create(ent, kind, depth, box, max_elem).static_layout()
+    ref = reference().create(ent, kind, depth, box, max_elem).static_layout()
+    assert got is not None and ref is not None
+    assert_static_equal(got, ref, case)
+
+
+def test_static_layout_undefined_for_points_outside_space():
+    pts = np.random.default_rng(5).random((500, 3))
+    box = np.array([0.2, 0.2, 0.2, 0.8, 0.8, 0.8])
+    assert oracle().create(pts, KIND_POINTS, 5, box, 4).static_layout() is None
+    assert reference().create(pts, KIND_POINTS, 5, box, 4).static_layout() is None
