@@ -144,6 +144,26 @@ typedef struct otg_static_layout
    the space of a point tree (its static Build does not end on them) or locations outside the grid. */
 int otg_tree_export_static(otg_tree* tree, otg_static_layout* out, void* stream);
 
+/* The tree as the reference's BinaryOutputArchive writes its static tree (`ar & tree`,
+   serialization.h:359-385 with serialization/binary_archive.h and serialization/stl/*.h):
+   StaticOctreePoint / StaticOctreeBox, or with with_entities != 0 the Managed
+   StaticOctreePointM / StaticOctreeBoxM, which also holds the entities (serialization.h:433-438).
+   The reference's BinaryInputArchive loads the bytes into that type. Little-endian scalars and
+   32-bit size tags (serialized_size_t without ORTHOTREE__LARGE_DATASET, core/types.h:51-55); the
+   node storage is the variant its Create picks. buffer NULL: only *size is set. A buffer shorter
+   than the archive: OTG_ERR_INVALID_ARGUMENT with *size set. Host memory; synchronises `stream`.
+   The same trees as otg_tree_export_static are refused. */
+int otg_tree_save_static(otg_tree* tree, int with_entities, void* buffer, uint64_t capacity, uint64_t* size, void* stream);
+
+/* Resumes a tree from a Managed archive (StaticOctreePointM / StaticOctreeBoxM, as written by the
+   reference or by otg_tree_save_static with entities): its entities are rebuilt with the archived
+   max depth and max elements per node, in `box` (NULL: the entities' bounding box, as Create
+   without a box), and the rebuild is checked against every archived array (entity order within a
+   node aside). OTG_ERR_INVALID_ARGUMENT for another tree type, a malformed archive, an archive
+   without entities, or one whose tree is not the rebuild of its entities. `tree` gives the scalar
+   type and kind (otg_tree_new); host memory. */
+int otg_tree_load_static(otg_tree* tree, const void* buffer, uint64_t size, const void* box, void* stream);
+
 /* Copies an exported static layout into host arrays (sizes as above; a null pointer skips an array). */
 int otg_static_layout_copy(const otg_static_layout* layout, uint32_t* child_begins, uint32_t* entity_segments, uint8_t* depth_ids,
                            uint32_t* entity_storage, void* geometry);

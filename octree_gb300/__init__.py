@@ -47,6 +47,8 @@ EXPORTS = [
     ("otg_tree_export_locations", _int, [_vp, _vp, _int, _vp]),
     ("otg_tree_export_nodes", _int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("otg_tree_export_static", _int, [_vp, _vp, _vp]),
+    ("otg_tree_save_static", _int, [_vp, _int, _vp, _u64, C.POINTER(_u64), _vp]),
+    ("otg_tree_load_static", _int, [_vp, _vp, _u64, _vp, _vp]),
     ("otg_static_layout_copy", _int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("otg_range_search", _int, [_vp, _vp, _u64, _int, _dbl, _int, C.POINTER(_vp), _int, _vp]),
     ("otg_pick_search", _int, [_vp, _vp, _u64, _dbl, _int, C.POINTER(_vp), _int, _vp]),
@@ -333,6 +335,27 @@ class Tree:
         _check(library().otg_static_layout_copy(C.byref(lay), ptr(cb), ptr(seg), ptr(dep), ptr(es), ptr(geo)))
         return dict(child_begins=cb[: lay.child_begin_count], child_begins_full=cb if m else cb[:0], segments=seg, depth=dep,
                     entity_storage=es, geometry=geo)
+
+    def save_static(self, with_entities=True, stream=None):
+        """The reference's binary archive of this tree's static form (bytes): StaticOctreePointM /
+        StaticOctreeBoxM with the entities, or the core StaticOctreePoint / StaticOctreeBox."""
+        size = _u64()
+        _check(library().otg_tree_save_static(self.h, int(bool(with_entities)), None, 0, C.byref(size), _stream_ptr(stream)))
+        buf = np.zeros(size.value, np.uint8)
+        _check(library().otg_tree_save_static(self.h, int(bool(with_entities)), buf.ctypes.data_as(_vp), size.value, C.byref(size), _stream_ptr(stream)))
+        return buf.tobytes()
+
+    def load_static(self, archive, box=None, stream=None):
+        """Resumes this tree from a Managed archive (see save_static): rebuilds the archived
+        entities and checks the rebuild against the archive."""
+        buf = np.frombuffer(archive, np.uint8)
+        b = None if box is None else np.ascontiguousarray(box, dtype=self.dtype)
+        _check(
+            library().otg_tree_load_static(
+                self.h, buf.ctypes.data_as(_vp) if buf.size else None, buf.size, None if b is None else b.ctypes.data_as(_vp), _stream_ptr(stream)
+            )
+        )
+        return self
 
     # ------------------------------------------------------------------ queries
     def _query(self, name, args, mem, stream, raw):

@@ -282,6 +282,34 @@ extern "C"
     return export_static(t->s, out, (cudaStream_t)stream);
   }
 
+  int otg_tree_save_static(otg_tree* t, int with_entities, void* buffer, uint64_t capacity, uint64_t* size, void* stream)
+  {
+    if (int rc = require_device())
+      return rc;
+    if (int rc = ready(t, (cudaStream_t)stream))
+      return rc;
+    if (!size)
+    {
+      set_error("otg_tree_save_static: null size");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+    return save_static_archive(t->s, with_entities != 0, buffer, capacity, size, (cudaStream_t)stream);
+  }
+
+  int otg_tree_load_static(otg_tree* t, const void* buffer, uint64_t size, const void* box, void* stream)
+  {
+    if (int rc = require_tree(t, false))
+      return rc;
+    if (!buffer && size)
+    {
+      set_error("otg_tree_load_static: null buffer");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+    if (int rc = require_device())
+      return rc;
+    return load_static_archive(t->s, buffer, size, box, (cudaStream_t)stream);
+  }
+
   int otg_static_layout_copy(const otg_static_layout* l, uint32_t* child_begins, uint32_t* entity_segments, uint8_t* depth_ids, uint32_t* entity_storage,
                              void* geometry)
   {

@@ -200,6 +200,9 @@ int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st);
 int export_nodes(const TreeState& t, u64* keys, double* minSize, u64* eoff, u32* eids, u32* childCount);
 // the static linear layout of a single tree (otg_static.cu)
 int export_static(TreeState& t, otg_static_layout* out, cudaStream_t st);
+// the reference's binary archive of that static tree, and a tree resumed from one (otg_archive.cu)
+int save_static_archive(TreeState& t, bool managed, void* buffer, u64 capacity, u64* size, cudaStream_t st);
+int load_static_archive(TreeState& t, const void* buffer, u64 size, const void* box, cudaStream_t st);
 
 // queries (otg_query.cu). qTree: the tree of each query when t is a forest (null otherwise).
 int query_range(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st,

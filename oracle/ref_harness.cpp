@@ -5,12 +5,16 @@
 // TEST INFRASTRUCTURE ONLY. Built by oracle/Makefile into oracle/_ref/ (git-ignored), and only
 // where the reference sources are present. Results are canonicalised exactly like the restatement's.
 #include "orthotree/octree.h"
+#include "orthotree/serialization.h"
+#include "orthotree/serialization/binary_archive.h"
 
 #include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <memory>
 #include <span>
+#include <sstream>
+#include <string>
 #include <vector>
 
 using namespace OrthoTree;
@@ -59,25 +63,40 @@ struct AnyRef
   std::vector<float> boxf;
 };
 
-// StaticLinearOrthoTreeCore's arrays (ORTHOTREE__PUBLIC_LINEARDATA_INTERFACE), widened to 32 bits
+template<typename T>
+std::span<const PointND<3, T>> pts_span(const std::vector<T>& v)
+{
+  return { reinterpret_cast<const PointND<3, T>*>(v.data()), v.size() / 3 };
+}
+template<typename T>
+std::span<const BoundingBoxND<3, T>> box_span(const std::vector<T>& v)
+{
+  return { reinterpret_cast<const BoundingBoxND<3, T>*>(v.data()), v.size() / 6 };
+}
+
+// StaticLinearOrthoTreeCore's arrays (ORTHOTREE__PUBLIC_LINEARDATA_INTERFACE), widened to 32 bits;
+// `equal`: a loaded archive's tree IsEqualTo the reference's own tree of the same entities
 struct StaticOut
 {
   std::vector<uint32_t> childBegins, segments, entityStorage;
   std::vector<uint8_t> depth;
   std::vector<double> geometry;
   uint64_t geomPerNode = 3;
+  int equal = 0;
 };
 
-template<typename StaticTree, typename T, typename Span>
-StaticOut* static_dump(Span ents, const AnyRef* a, const std::vector<T>& box, bool isBox)
+template<typename StaticTree, typename T>
+void static_args(const AnyRef* a, const std::vector<T>& box, std::optional<typename StaticTree::TBox>& ob, std::optional<depth_t>& od)
 {
-  std::optional<typename StaticTree::TBox> ob;
   if (a->hasBox)
     ob = *reinterpret_cast<const typename StaticTree::TBox*>(box.data());
-  std::optional<depth_t> od;
   if (a->maxDepthArg)
     od = a->maxDepthArg;
-  StaticTree t(PAR_EXEC, ents, od, ob, a->maxElem);
+}
+
+template<typename StaticTree>
+StaticOut* static_arrays(StaticTree const& t, bool isBox)
+{
   auto* o = new StaticOut();
   std::visit(
     [&](auto const& nodes) {
@@ -109,16 +128,92 @@ StaticOut* static_dump(Span ents, const AnyRef* a, const std::vector<T>& box, bo
   return o;
 }
 
-template<typename T>
-std::span<const PointND<3, T>> pts_span(const std::vector<T>& v)
+template<typename StaticTree, typename T, typename Span>
+StaticOut* static_dump(Span ents, const AnyRef* a, const std::vector<T>& box, bool isBox)
 {
-  return { reinterpret_cast<const PointND<3, T>*>(v.data()), v.size() / 3 };
+  std::optional<typename StaticTree::TBox> ob;
+  std::optional<depth_t> od;
+  static_args<StaticTree>(a, box, ob, od);
+  StaticTree t(PAR_EXEC, ents, od, ob, a->maxElem);
+  return static_arrays(t, isBox);
 }
-template<typename T>
-std::span<const BoundingBoxND<3, T>> box_span(const std::vector<T>& v)
+
+// The reference's binary archive (serialization/binary_archive.h) of its static tree of the same
+// entities: the core (`ar & tree`) or the Managed form with the entities.
+template<typename StaticTree, typename T, typename Span>
+std::string static_archive(Span ents, const AnyRef* a, const std::vector<T>& box, bool managed)
 {
-  return { reinterpret_cast<const BoundingBoxND<3, T>*>(v.data()), v.size() / 6 };
+  std::optional<typename StaticTree::TBox> ob;
+  std::optional<depth_t> od;
+  static_args<StaticTree>(a, box, ob, od);
+  std::stringstream ss(std::ios::in | std::ios::out | std::ios::binary);
+  BinaryOutputArchive ar(ss);
+  if (managed)
+  {
+    OrthoTreeManaged<StaticTree> m(ents, od, ob, a->maxElem, PAR_EXEC);
+    ar & m;
+  }
+  else
+  {
+    StaticTree t(PAR_EXEC, ents, od, ob, a->maxElem);
+    ar & t;
+  }
+  return ss.str();
 }
+
+// Loads archive bytes with the reference's BinaryInputArchive into its static tree type (null when
+// the stream runs short or bytes are left over) and compares the loaded tree with the reference's
+// own tree of the same entities: IsEqualTo both ways and, for the Managed form, equal entities.
+template<typename StaticTree, typename T, typename Span>
+StaticOut* static_load(Span ents, const AnyRef* a, const std::vector<T>& box, const std::string& bytes, bool managed, bool isBox)
+{
+  std::optional<typename StaticTree::TBox> ob;
+  std::optional<depth_t> od;
+  static_args<StaticTree>(a, box, ob, od);
+  StaticTree own(PAR_EXEC, ents, od, ob, a->maxElem);
+  std::stringstream ss(bytes, std::ios::in | std::ios::out | std::ios::binary);
+  BinaryInputArchive ar(ss);
+  auto finish = [&](StaticTree const& core, bool entitiesEqual) -> StaticOut* {
+    if (!ss || ss.peek() != std::char_traits<char>::eof())
+      return nullptr;
+    auto* o = static_arrays(core, isBox);
+    // IsEqualTo reads the root even when there is no node (empty trees): compare counts there
+    const bool empty = core.GetNodeCount() == 0 || own.GetNodeCount() == 0;
+    const bool same = empty ? core.GetNodeCount() == own.GetNodeCount() : core.IsEqualTo(own) && own.IsEqualTo(core);
+    o->equal = entitiesEqual && same ? 1 : 0;
+    return o;
+  };
+  if (managed)
+  {
+    OrthoTreeManaged<StaticTree> m;
+    ar & m;
+    auto const& data = m.GetData();
+    bool same = data.size() == ents.size() && std::memcmp(data.data(), ents.data(), ents.size_bytes()) == 0;
+    return finish(m.GetCore(), same);
+  }
+  StaticTree t;
+  ar & t;
+  return finish(t, true);
+}
+
+template<typename F>
+auto with_static(AnyRef* a, F&& f)
+{
+  if (a->scalar == 0)
+  {
+    if (a->kind == 0)
+      return f.template operator()<StaticPointTree<double>>(pts_span(a->ed), a->boxd, false);
+    if (a->kind == 1)
+      return f.template operator()<StaticLooseBoxTree<double>>(box_span(a->ed), a->boxd, true);
+    return f.template operator()<StaticBoxTree<double>>(box_span(a->ed), a->boxd, true);
+  }
+  if (a->kind == 0)
+    return f.template operator()<StaticPointTree<float>>(pts_span(a->ef), a->boxf, false);
+  if (a->kind == 1)
+    return f.template operator()<StaticLooseBoxTree<float>>(box_span(a->ef), a->boxf, true);
+  return f.template operator()<StaticBoxTree<float>>(box_span(a->ef), a->boxf, true);
+}
+
 
 template<typename T>
 T tol_or_default(double tol)
@@ -472,6 +567,28 @@ extern "C"
     std::memcpy(geometry, o->geometry.data(), o->geometry.size() * sizeof(double));
   }
   void oro_static_free(void* s) { delete (StaticOut*)s; }
+  int oro_static_equal(void* s) { return ((StaticOut*)s)->equal; }
+
+  // The reference's archive of its static tree (managed: with the entities); returns its size and
+  // copies it when `cap` allows. Not for point trees with points outside their space (see oro_static).
+  uint64_t oro_static_archive(void* h, int managed, uint8_t* buf, uint64_t cap)
+  {
+    auto* a = (AnyRef*)h;
+    std::string bytes = with_static(a, [&]<typename ST>(auto ents, auto const& box, bool) { return static_archive<ST>(ents, a, box, managed != 0); });
+    if (buf && cap >= bytes.size())
+      std::memcpy(buf, bytes.data(), bytes.size());
+    return bytes.size();
+  }
+
+  // Archive bytes loaded by the reference (see static_load); null when they do not load.
+  void* oro_static_load(void* h, const uint8_t* buf, uint64_t size, int managed)
+  {
+    auto* a = (AnyRef*)h;
+    std::string bytes(reinterpret_cast<const char*>(buf), size);
+    return with_static(a, [&]<typename ST>(auto ents, auto const& box, bool isBox) -> StaticOut* {
+      return static_load<ST>(ents, a, box, bytes, managed != 0, isBox);
+    });
+  }
 
   void oro_location_keys(void* h, uint64_t* out)
   {

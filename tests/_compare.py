@@ -134,3 +134,97 @@ def assert_static_equal(a, b, what, exact_storage=False):
         sa, sb = np.sort(ea[bg : bg + ln]), np.sort(eb[bg : bg + ln])
         assert np.array_equal(sa, sb), f"{what}: static entities of the segment at {bg}"
     assert np.array_equal(np.sort(ea), np.sort(eb)), f"{what}: static entity storage as a set"
+
+
+def static_storage_index(n, depth):
+    """The node storage variant the reference's static Create picks: IsFit over
+    GetMaxPossibleNodeCount (core/ot_static_linear_core.h:326-344, :370-376, :574-580)."""
+    if n == 0:
+        return 0
+    node_num = lambda d: ((1 << (3 * d)) - 1) // 7
+    full = min(depth, (n - 1).bit_length() // 3)
+    m = min(node_num(full) + (depth - full) * n, node_num(depth))
+    if m < 0xFF and n < 0xFF:
+        return 0
+    if m < 0xFFFF and n < 0xFFFF:
+        return 1
+    return 2
+
+
+def static_archive_bytes(layout, is_box, dtype, n, depth, max_elem, space_min, space_size, entities=None):
+    """The bytes of the reference's BinaryOutputArchive for a static tree with this layout
+    (serialization.h:359-385, :433-438; serialization/binary_archive.h; serialization/stl/*.h):
+    little-endian scalars, u32 size tags before every vector and std::array, std::monostate empty.
+    entities: the Managed form's entity array, or None for the core alone."""
+    T = np.dtype(dtype).newbyteorder("<")
+    out = bytearray()
+    u32 = lambda v: out.extend(np.uint32(v).astype("<u4").tobytes())
+
+    def vec3_rows(rows, groups):
+        # each row: `groups` std::arrays of 3 scalars, each after its size tag 3
+        rows = np.asarray(rows, T).reshape(len(rows), groups, 3)
+        rec = np.zeros((len(rows), groups), np.dtype([("tag", "<u4"), ("v", T, 3)]))
+        rec["tag"] = 3
+        rec["v"] = rows
+        out.extend(rec.tobytes())
+
+    u32(0)  # StaticLinearOrthoTreeCore version
+    u32(0)  # OrthoTreeCoreBase version
+    out.extend(np.uint64(max_elem).astype("<u8").tobytes())
+    u32(depth)
+    space_min = np.asarray(space_min, T)
+    space_size = np.asarray(space_size, T)
+    if is_box:
+        vec3_rows(np.concatenate([space_min, space_size])[None], 2)  # m_nominalTreeBox {minPoint, size}
+    else:
+        u32(depth + 2)  # m_nodeSize (core/ot_base.h:121-134)
+        lf = T.type(1)
+        sizes = []
+        for _ in range(depth + 2):
+            sizes.append(space_size * lf)
+            lf = T.type(lf * T.type(0.5))
+        vec3_rows(sizes, 1)
+    idx = static_storage_index(n, depth)
+    u32(idx)
+    w = ("<u1", "<u2", "<u4")[idx]
+    cb = np.asarray(layout["child_begins"])
+    u32(cb.size)
+    out.extend(cb.astype(w).tobytes())
+    seg = np.asarray(layout["segments"]).reshape(-1, 2)
+    u32(seg.shape[0])
+    out.extend(seg.astype(w).tobytes())
+    dep = np.asarray(layout["depth"], np.uint8)
+    u32(dep.size)
+    out.extend(dep.tobytes())
+    es = np.asarray(layout["entity_storage"])
+    u32(es.size)
+    out.extend(es.astype("<u4").tobytes())
+    geo = np.asarray(layout["geometry"], T)
+    u32(geo.shape[0])
+    if geo.shape[0]:
+        vec3_rows(geo, 2 if is_box else 1)
+    if entities is not None:
+        ent = np.asarray(entities, T)
+        u32(ent.shape[0])
+        if ent.shape[0]:
+            vec3_rows(ent, 2 if is_box else 1)
+    return bytes(out)
+
+
+def space_of(ent, is_box, box=None):
+    """The tree's space as Create finds it (given box, or the entities' bounding box) and its size
+    Max - Min in the tree's scalar type (detail/si_grid.h:65-100)."""
+    T = ent.dtype.type
+    if box is not None:
+        b = np.asarray(box, ent.dtype)
+        mn, mx = b[:3], b[3:]
+    elif ent.shape[0] == 0:
+        # the bounding box of nothing is the inverted box (IGM::BoxInvertedInit): its size overflows
+        big = np.finfo(ent.dtype).max
+        mn, mx = np.full(3, big, ent.dtype), np.full(3, -big, ent.dtype)
+        with np.errstate(over="ignore"):
+            return mn, (mx - mn).astype(T)
+    else:
+        mn = ent[:, :3].min(axis=0)
+        mx = (ent[:, 3:] if is_box else ent).max(axis=0)
+    return mn, (mx - mn).astype(T)

@@ -70,6 +70,13 @@ class OracleLib:
         if hasattr(lib, "oro_time_create_points_par"):
             lib.oro_time_create_points_par.restype = _dbl
             lib.oro_time_create_points_par.argtypes = [_vp, _u64, _u32, _u64, _int, _u32]
+        if hasattr(lib, "oro_static_archive"):  # the reference harness only
+            lib.oro_static_archive.restype = _u64
+            lib.oro_static_archive.argtypes = [_vp, _int, _vp, _u64]
+            lib.oro_static_load.restype = _vp
+            lib.oro_static_load.argtypes = [_vp, _vp, _u64, _int]
+            lib.oro_static_equal.restype = _int
+            lib.oro_static_equal.argtypes = [_vp]
         if hasattr(lib, "oro_collide_self_par"):
             lib.oro_collide_self_par.restype = _vp
             lib.oro_collide_self_par.argtypes = [_vp, _dbl]
@@ -148,6 +155,36 @@ class OracleTree:
         finally:
             self.lib.oro_static_free(h)
         return dict(child_begins=cb[:nb], segments=seg[:m], depth=dep[:m], entity_storage=es[:ne], geometry=geo[:m])
+
+    def static_archive(self, managed=True):
+        """The reference's own binary archive of its static tree of these entities (harness only)."""
+        size = self.lib.oro_static_archive(self.h, int(managed), None, 0)
+        buf = np.zeros(size, np.uint8)
+        self.lib.oro_static_archive(self.h, int(managed), _ptr(buf), size)
+        return buf.tobytes()
+
+    def static_load(self, data, managed=True):
+        """Loads archive bytes with the reference's BinaryInputArchive (harness only): None when
+        they do not load, else (layout of the loaded tree, whether it IsEqualTo the reference's own
+        tree of these entities and holds the same entities)."""
+        buf = np.frombuffer(data, np.uint8).copy()
+        h = self.lib.oro_static_load(self.h, _ptr(buf), buf.size, int(managed))
+        if not h:
+            return None
+        equal = bool(self.lib.oro_static_equal(h))
+        try:
+            sz = np.zeros(4, np.uint64)
+            self.lib.oro_static_sizes(h, _ptr(sz))
+            m, nb, ne, w = (int(v) for v in sz)
+            cb = np.zeros(max(nb, 1), np.uint32)
+            seg = np.zeros((max(m, 1), 2), np.uint32)
+            dep = np.zeros(max(m, 1), np.uint8)
+            es = np.zeros(max(ne, 1), np.uint32)
+            geo = np.zeros((max(m, 1), w), np.float64)
+            self.lib.oro_static_copy(h, _ptr(cb), _ptr(seg), _ptr(dep), _ptr(es), _ptr(geo))
+        finally:
+            self.lib.oro_static_free(h)
+        return dict(child_begins=cb[:nb], segments=seg[:m], depth=dep[:m], entity_storage=es[:ne], geometry=geo[:m]), equal
 
     def location_keys(self):
         out = np.zeros(self.n, np.uint64)

@@ -89,6 +89,8 @@ def run_case(name, ent, kind, max_depth, box, max_elem, q, ray_tol):
     if st is not None:
         for k, v in st.items():
             out["static_" + k] = v
+        # the reference's binary archive of its Managed static tree (StaticOctreePointM / BoxM)
+        out["static_archive"] = np.frombuffer(t.static_archive(True), np.uint8)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(name, "nodes", len(nd["keys"]), "depth", t.max_depth)
 

@@ -3,7 +3,16 @@ itself (tests/golden/make_golden.py). This pins the restatement to the reference
 import numpy as np
 import pytest
 
-from _compare import assert_csr_equal, assert_static_equal, golden_cases, load_golden, node_dict, static_from_golden
+from _compare import (
+    assert_csr_equal,
+    assert_static_equal,
+    golden_cases,
+    load_golden,
+    node_dict,
+    space_of,
+    static_archive_bytes,
+    static_from_golden,
+)
 from _oracle_lib import KIND_POINTS, oracle
 
 
@@ -77,3 +86,17 @@ def test_oracle_static_layout_matches_reference_fixture(name):
         assert got is None
         return
     assert_static_equal(got, ref, name)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_archive_writer_matches_reference_fixture(name):
+    """The archive writer restated in tests/_compare.py, fed with the reference's static layout,
+    gives the bytes the reference's BinaryOutputArchive wrote for its StaticOctreePointM / BoxM."""
+    g = load_golden(name)
+    if not int(g["static_defined"]):
+        pytest.skip("no static tree for points outside the space")
+    ent = g["entities"]
+    is_box = int(g["kind"]) != KIND_POINTS
+    mn, size = space_of(ent, is_box, g.get("box"))
+    data = static_archive_bytes(static_from_golden(g), is_box, ent.dtype, len(ent), int(g["depth"]), int(g["max_elem"]), mn, size, ent)
+    assert data == g["static_archive"].tobytes()

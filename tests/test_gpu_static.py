@@ -1,5 +1,6 @@
-"""Export to the static linear layout (otg_tree_export_static): the GPU-built tree in the arrays of
-the reference's StaticLinearOrthoTreeCore, against the reference's own static trees (golden
+"""Export to the static linear layout (otg_tree_export_static) and the binary archive of that static
+tree (otg_tree_save_static / otg_tree_load_static): the GPU-built tree in the arrays of the
+reference's StaticLinearOrthoTreeCore, against the reference's own static trees (golden
 fixtures) and the CPU oracle's restatement on seeded inputs, with the refusals where the reference
 has no such tree. Child segment begins, entity segments, depth ids and node geometry are compared
 bit for bit; entity storage exactly against the oracle (both keep equal locations in id order) and
@@ -8,7 +9,15 @@ import numpy as np
 import pytest
 
 import octree_gb300 as otg
-from _compare import assert_static_equal, golden_cases, load_golden, static_from_golden
+from _compare import (
+    assert_csr_equal,
+    assert_static_equal,
+    golden_cases,
+    load_golden,
+    space_of,
+    static_archive_bytes,
+    static_from_golden,
+)
 from _oracle_lib import KIND_LOOSE_BOXES, KIND_POINTS, oracle
 
 pytestmark = pytest.mark.gpu
@@ -125,3 +134,82 @@ def test_static_layout_full_size_properties():
     sample = pts[:2_000_000]
     ts = _gpu_tree(sample, KIND_POINTS, 10, None, 20)
     assert_static_equal(ts.export_static(), oracle().create(sample, KIND_POINTS, 10, None, 20).static_layout(), "2M sample", exact_storage=True)
+
+
+# ---------------------------------------------------------------- binary archive (save / resume)
+
+
+def _writer_bytes(t, lay, ent, kind, box, max_elem, with_entities):
+    is_box = kind != KIND_POINTS
+    mn, size = space_of(ent, is_box, box)
+    return static_archive_bytes(lay, is_box, ent.dtype, len(ent), t.max_depth, max_elem, mn, size, ent if with_entities else None)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_archive_matches_reference_fixture(name):
+    """otg_tree_save_static writes the bytes of the reference's BinaryOutputArchive: equal to the
+    reference's own archive where both order the entities of every node alike, and always equal to
+    the writer restated in tests/_compare.py over the exported layout."""
+    g = load_golden(name)
+    if not int(g["static_defined"]):
+        pytest.skip("no static tree for points outside the space")
+    ent, kind, box, me = g["entities"], int(g["kind"]), g.get("box"), int(g["max_elem"])
+    t = _gpu_tree(ent, kind, int(g["max_depth"]), box, me)
+    lay = t.export_static()
+    managed = t.save_static(True)
+    assert managed == _writer_bytes(t, lay, ent, kind, box, me, True)
+    assert t.save_static(False) == _writer_bytes(t, lay, ent, kind, box, me, False)
+    if np.array_equal(lay["entity_storage"], g["static_entity_storage"]):
+        assert managed == g["static_archive"].tobytes()
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_resume_from_reference_archive(name):
+    """A tree resumed from the reference's own archive is the reference's tree: its static layout
+    equals the archived one and it answers the fixture's queries as the reference did."""
+    g = load_golden(name)
+    if not int(g["static_defined"]):
+        pytest.skip("no static tree for points outside the space")
+    ent, kind = g["entities"], int(g["kind"])
+    t = otg.Tree("points" if kind == KIND_POINTS else "boxes", ent.dtype).load_static(g["static_archive"].tobytes(), box=g.get("box"))
+    assert_static_equal(t.export_static(), static_from_golden(g), name)
+    for mode in (0, 1):
+        assert_csr_equal(t.range_search(g["ranges"], mode)[:2], (g[f"range{mode}_off"], g[f"range{mode}_ids"]), f"{name} range{mode}")
+    assert_csr_equal(t.knn(g["qpts"], g["k"]), (g["knn_off"], g["knn_ids"], g["knn_dist"]), f"{name} knn")
+
+
+@pytest.mark.parametrize("case", ["clustered_estimated_depth", "boxes_f32", "duplicate_boxes", "points_keys64"])
+def test_archive_round_trip(case):
+    """save -> resume into a new tree -> save gives the same bytes; the resumed tree is the tree."""
+    ent, kind, depth, box, me = _cases()[case]
+    t = _gpu_tree(ent, kind, depth, box, me)
+    data = t.save_static(True)
+    t2 = otg.Tree("points" if kind == KIND_POINTS else "boxes", ent.dtype).load_static(data, box=box)
+    assert t2.save_static(True) == data
+    assert t2.node_count == t.node_count
+
+
+def test_resume_refusals():
+    rng = np.random.default_rng(9)
+    pts = rng.random((5000, 3)) * 10
+    t = _gpu_tree(pts, KIND_POINTS, 6, None, 8)
+    data = t.save_static(True)
+    fresh = lambda dtype=np.float64: otg.Tree("points", dtype)
+    with pytest.raises(otg.OtgError):  # the core form holds no entities to rebuild
+        fresh().load_static(t.save_static(False))
+    with pytest.raises(otg.OtgError):  # cut short
+        fresh().load_static(data[:-3])
+    with pytest.raises(otg.OtgError):  # trailing bytes
+        fresh().load_static(data + b"\0")
+    with pytest.raises(otg.OtgError):  # another scalar type
+        fresh(np.float32).load_static(data)
+    with pytest.raises(otg.OtgError):  # another kind
+        otg.Tree("boxes").load_static(data)
+    with pytest.raises(otg.OtgError):  # not an archive
+        fresh().load_static(bytes(range(256)) * 4)
+    # a tree created in a given box does not resume without it (the rebuild differs)
+    box = np.array([-1.0, -1, -1, 12, 12, 12])
+    tb = _gpu_tree(pts, KIND_POINTS, 6, box, 8)
+    with pytest.raises(otg.OtgError):
+        fresh().load_static(tb.save_static(True))
+    assert fresh().load_static(tb.save_static(True), box=box).save_static(True) == tb.save_static(True)

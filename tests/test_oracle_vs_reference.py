@@ -4,7 +4,7 @@ the committed golden fixtures carry the pin."""
 import numpy as np
 import pytest
 
-from _compare import assert_static_equal
+from _compare import assert_static_equal, space_of, static_archive_bytes
 from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, oracle, reference
 
 pytestmark = pytest.mark.skipif(reference() is None, reason="reference harness not built here")
@@ -176,3 +176,35 @@ def test_static_layout_undefined_for_points_outside_space():
     box = np.array([0.2, 0.2, 0.2, 0.8, 0.8, 0.8])
     assert oracle().create(pts, KIND_POINTS, 5, box, 4).static_layout() is None
     assert reference().create(pts, KIND_POINTS, 5, box, 4).static_layout() is None
+
+
+@pytest.mark.parametrize("managed", [False, True])
+@pytest.mark.parametrize("case", list(_static_cases()))
+def test_static_archive_format(case, managed):
+    """The archive writer restated in tests/_compare.py gives the reference's own BinaryOutputArchive
+    bytes of its static tree (core, or Managed with the entities), fed with the reference's layout."""
+    ent, kind, depth, box, max_elem = _static_cases()[case]
+    t = reference().create(ent, kind, depth, box, max_elem)
+    is_box = kind != KIND_POINTS
+    mn, size = space_of(ent, is_box, box)
+    mine = static_archive_bytes(t.static_layout(), is_box, ent.dtype, len(ent), t.max_depth, max_elem, mn, size, ent if managed else None)
+    assert mine == t.static_archive(managed)
+
+
+@pytest.mark.parametrize("case", list(_static_cases()))
+def test_reference_loads_oracle_archive(case):
+    """Archive bytes of the oracle's layout load into the reference's static tree type, which then
+    IsEqualTo the reference's own tree and holds exactly the archived arrays."""
+    ent, kind, depth, box, max_elem = _static_cases()[case]
+    o = oracle().create(ent, kind, depth, box, max_elem)
+    is_box = kind != KIND_POINTS
+    mn, size = space_of(ent, is_box, box)
+    lay = o.static_layout()
+    data = static_archive_bytes(lay, is_box, ent.dtype, len(ent), o.max_depth, max_elem, mn, size, ent)
+    loaded = reference().create(ent, kind, depth, box, max_elem).static_load(data)
+    assert loaded is not None
+    arrays, equal = loaded
+    assert equal
+    assert_static_equal(arrays, lay, case, exact_storage=True)
+    # a cut archive does not load
+    assert reference().create(ent, kind, depth, box, max_elem).static_load(data[:-1]) is None
