@@ -481,6 +481,15 @@ def run_static_export(tree16, pts16_h, reps=5):
     if kind == "port":
         same = same and np.array_equal(got["entity_storage"], ref["entity_storage"])
     out["sample_layout_equal_to_cpu"] = bool(same)
+    # the reference's binary archive of the sample's Managed static tree, and a tree resumed from it
+    t0 = time.perf_counter()
+    data = ts.save_static(True)
+    out["archive_1M_managed_bytes"] = len(data)
+    out["archive_1M_save_ms"] = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    resumed = otg.Tree("points").load_static(data)
+    out["archive_1M_resume_ms"] = (time.perf_counter() - t0) * 1e3
+    out["archive_1M_round_trip_equal"] = resumed.save_static(True) == data
     torch.cuda.synchronize()
     return out
 

@@ -173,6 +173,8 @@ template<typename T>
 void write_archive(const TreeState& t, const StaticHost<T>& h, bool managed, ArchiveOut& a, u64& esBegin, u64& esEnd)
 {
   const bool box = t.kind != OTG_KIND_POINTS;
+  const size_t vec = 4 + 3 * sizeof(T), groups = box ? 2 : 1;
+  a.bytes.reserve(64 + (t.D + 2) * vec + h.depth.size() * (9 + groups * vec) + t.n * (4 + (managed ? groups * vec : 0)));
   a.put(u32(0)); // StaticLinearOrthoTreeCore SERIALIZED_VERSION_ID
   a.put(u32(0)); // OrthoTreeCoreBase SERIALIZED_VERSION_ID
   a.put(u64(t.maxElem));
