@@ -249,6 +249,54 @@ public:
   std::size_t GetNodeCount() const { return std::size_t(Info().node_count); }
   depth_t GetMaxDepthID() const { return Info().max_depth; }
 
+  // ---------------------------------------------------------------- static form and archives
+  // The arrays of StaticLinearOrthoTreeCore (core/ot_static_linear_core.h:81-89, GetNodes(),
+  // GetNodeDepthIDs(), GetEntityStorage(), GetNodeGeometries()) for these entities, computed on
+  // the device: NodeStorageGeneral widths; geometry per node is the MinPoint (points) or
+  // {minPoint, size} (boxes).
+  struct StaticLayout
+  {
+    std::vector<std::uint32_t> nodeChildSegmentBegins; // as stored: up to the last node with children + 1
+    std::vector<std::pair<std::uint32_t, std::uint32_t>> nodeEntitySegment; // {begin, length}
+    std::vector<std::uint8_t> nodeDepthIDs;
+    std::vector<EntityID> entityStorage;
+    std::vector<TScalar> nodeGeometry; // 3 (points) or 6 (boxes) scalars per node
+  };
+  StaticLayout ExportStatic() const
+  {
+    otg_static_layout l{};
+    detail::check(otg_tree_export_static(m_tree, &l, m_stream));
+    StaticLayout s;
+    std::vector<std::uint32_t> begins(l.node_count + 1), seg(2 * l.node_count);
+    s.nodeDepthIDs.resize(l.node_count);
+    s.entityStorage.resize(l.entity_count);
+    s.nodeGeometry.resize(l.node_count * l.geometry_per_node);
+    detail::check(otg_static_layout_copy(&l, l.node_count ? begins.data() : nullptr, seg.data(), s.nodeDepthIDs.data(), s.entityStorage.data(),
+                                         s.nodeGeometry.data()));
+    s.nodeChildSegmentBegins.assign(begins.begin(), begins.begin() + l.child_begin_count);
+    for (std::size_t i = 0; i < l.node_count; ++i)
+      s.nodeEntitySegment.emplace_back(seg[2 * i], seg[2 * i + 1]);
+    return s;
+  }
+
+  // `ar & tree` of the reference's BinaryOutputArchive for StaticOctreePointM / StaticOctreeBoxM
+  // (withEntities) or StaticOctreePoint / StaticOctreeBox (serialization.h:359-385, 433-438)
+  std::vector<std::uint8_t> SaveStatic(bool withEntities = true) const
+  {
+    std::uint64_t size = 0;
+    detail::check(otg_tree_save_static(m_tree, withEntities ? 1 : 0, nullptr, 0, &size, m_stream));
+    std::vector<std::uint8_t> bytes(size);
+    detail::check(otg_tree_save_static(m_tree, withEntities ? 1 : 0, bytes.data(), size, &size, m_stream));
+    return bytes;
+  }
+
+  // Resumes from a Managed archive (the reference's or SaveStatic's): rebuilds its entities in
+  // boxSpace (default: their bounding box) and checks the rebuild against the archive
+  void LoadStatic(std::span<const std::uint8_t> archive, std::optional<TBox> boxSpace = std::nullopt)
+  {
+    detail::check(otg_tree_load_static(m_tree, archive.data(), archive.size(), boxSpace ? &*boxSpace : nullptr, m_stream));
+  }
+
   // ---------------------------------------------------------------- single queries (reference form)
   std::vector<EntityID> PickSearch(const TVector& pickPoint, double tolerance = detail::base_tolerance<TScalar>()) const
   {

@@ -29,6 +29,10 @@ extern "C"
   uint64_t oro_res_total(void* r);
   void oro_res_copy(void* r, uint64_t* offsets, uint32_t* ids, double* dist);
   void oro_res_free(void* r);
+  void* oro_static(void* h);
+  void oro_static_sizes(void* s, uint64_t* sizes4);
+  void oro_static_copy(void* s, uint32_t* childBegins, uint32_t* segments, uint8_t* depth, uint32_t* entityStorage, double* geometry);
+  void oro_static_free(void* s);
 }
 
 using namespace OrthoTreeGPU;
@@ -112,6 +116,36 @@ int main()
     for (int i = 0; i < nq; ++i)
       expect({ batch[i].begin(), batch[i].end() }, r, i, "GetNearestNeighborsBatch");
     oro_res_free(r);
+  }
+  // the static form: ExportStatic against the oracle's restatement, and an archive round trip
+  {
+    const auto sl = tp.ExportStatic();
+    void* os = oro_static(op);
+    uint64_t sz[4];
+    oro_static_sizes(os, sz);
+    std::vector<uint32_t> cb(sz[1]), seg(2 * sz[0]), es(sz[2]);
+    std::vector<uint8_t> dep(sz[0]);
+    std::vector<double> geo(sz[0] * sz[3]);
+    oro_static_copy(os, cb.data(), seg.data(), dep.data(), es.data(), geo.data());
+    oro_static_free(os);
+    bool same = sl.nodeChildSegmentBegins == cb && sl.nodeDepthIDs == dep && sl.entityStorage == es && sl.nodeGeometry.size() == geo.size();
+    for (std::size_t i = 0; same && i < sl.nodeEntitySegment.size(); ++i)
+      same = sl.nodeEntitySegment[i].first == seg[2 * i] && sl.nodeEntitySegment[i].second == seg[2 * i + 1];
+    for (std::size_t i = 0; same && i < geo.size(); ++i)
+      same = sl.nodeGeometry[i] == geo[i];
+    if (!same)
+    {
+      std::printf("MISMATCH ExportStatic\n");
+      ++g_fail;
+    }
+    const auto archive = tp.SaveStatic();
+    OctreePointM resumed;
+    resumed.LoadStatic(archive);
+    if (resumed.SaveStatic() != archive || resumed.RangeSearch(ranges[0]) != tp.RangeSearch(ranges[0]))
+    {
+      std::printf("MISMATCH SaveStatic / LoadStatic\n");
+      ++g_fail;
+    }
   }
   oro_destroy(op);
 
