@@ -428,6 +428,8 @@ def run_gpu(args):
         }
     if not args.no_queries:
         line["static_layout"] = run_static_export(tree, pts_h)
+        if rank == 0 and not args.no_cpu_baseline:
+            line["cpu_configs"] = run_cpu_configs()
         line["queries"] = run_queries(tree, pts_d, stream)
         line["many_trees"] = run_many_trees()
         line["two_trees"] = run_two_trees()
@@ -491,6 +493,80 @@ def run_static_export(tree16, pts16_h, reps=5):
     out["archive_1M_resume_ms"] = (time.perf_counter() - t0) * 1e3
     out["archive_1M_round_trip_equal"] = resumed.save_static(True) == data
     torch.cuda.synchronize()
+    return out
+
+
+def run_cpu_configs():
+    """The CPU side of each query config, beside the GPU figures: the oracle port (or the reference
+    where it was built here) on bounded samples of the same inputs. Trees are built with the
+    port's threaded location transform and sort where it has them; queries are split over every
+    host core (the ctypes calls run in parallel), as the reference's std::for_each(par) would run
+    them. Each entry names its sample."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    lib, kind = oracle_lib()
+    threads = os.cpu_count() or 1
+    build_threads = threads if hasattr(lib.lib, "oro_create_threads") else 1
+    pool = ThreadPoolExecutor(threads)
+
+    def par_queries(fn, arrays):
+        # fn(slice arrays...) for `threads` contiguous slices, concurrently; returns seconds
+        n = len(arrays[0])
+        cuts = [n * i // threads for i in range(threads + 1)]
+        t0 = time.perf_counter()
+        list(pool.map(lambda i: fn(*[a[cuts[i] : cuts[i + 1]] for a in arrays]), range(threads)))
+        return time.perf_counter() - t0
+
+    out = {"kind": kind, "query_threads": threads, "build_threads": build_threads}
+    # C1: 1M uniform points (depth 10, max 20); 2000 of the 10k range boxes and 2000 kNN(k=8) queries
+    p1 = np.random.default_rng(101).random((1_000_000, 3)) * 100
+    t0 = time.perf_counter()
+    t1 = lib.create(p1, 0, 10, None, 20, threads=build_threads)
+    out["c1_create_1M_s"] = time.perf_counter() - t0
+    c = np.random.default_rng(102).random((10_000, 3)) * 100
+    e = np.random.default_rng(102).uniform(0.5, 5, (10_000, 3))
+    ranges = np.concatenate([c - e / 2, c + e / 2], 1)[:2000]
+    s = par_queries(lambda r: t1.range_search(r), [ranges])
+    out["c1_range_Mq_per_s"] = 2000 / s / 1e6
+    q = np.random.default_rng(103).random((2000, 3)) * 100
+    s = par_queries(lambda x: t1.knn(x, 8), [q])
+    out["c1_knn8_Mq_per_s"] = 2000 / s / 1e6
+    out["c1_sample"] = "2000 of the 10k range boxes, 2000 kNN(k=8) queries"
+    del t1
+    # C3: the 16M shell points; 2000 of the 1M uneven kNN queries (k in 1..64)
+    pts = shell_points(N_POINTS, 301)
+    t0 = time.perf_counter()
+    t3 = lib.create(pts, 0, MAX_DEPTH, None, MAX_ELEM, threads=build_threads)
+    out["c3_create_16M_s"] = time.perf_counter() - t0
+    qk = shell_points(1_000_000, 302)[:2000]
+    ks = np.random.default_rng(303).integers(1, 65, 1_000_000).astype(np.uint32)[:2000]
+    s = par_queries(lambda x, k: t3.knn(x, k), [qk, ks])
+    out["c3_knn_uneven_Mq_per_s"] = 2000 / s / 1e6
+    out["c3_sample"] = "2000 of the 1M queries, k in 1..64"
+    del t3, pts
+    # C2: self-collision of every 8th of the 4M clustered boxes (one sequential call: the
+    # reference's parallel CollisionDetection is a different traversal order, same pairs)
+    boxes = np.ascontiguousarray(cluster_boxes(4_000_000, 201)[::8])
+    tb = lib.create(boxes, 1, 12, None, 32, threads=build_threads)
+    t0 = time.perf_counter()
+    pairs = tb.collide_self()
+    s = time.perf_counter() - t0
+    out["c2_collide_self_500k_ms"] = s * 1e3
+    out["c2_collide_self_500k_Mpairs_per_s"] = len(pairs) / s / 1e6
+    out["c2_sample"] = "every 8th of the 4M boxes (500k, one eighth of the density), one thread"
+    del tb
+    # C4: 16 FP32 box trees drawn as the 4096 are: Create, 256 ranges, 256 rays and one frustum each
+    ent, off, qr, rays, planes = many_trees(16, 401)
+    t0 = time.perf_counter()
+    for t in range(16):
+        tt = lib.create(ent[off[t] : off[t + 1]], 1, 0, None, 16, threads=build_threads)
+        tt.range_search(qr[256 * t : 256 * (t + 1)], 1)
+        tt.ray(rays[256 * t : 256 * (t + 1)])
+        tt.frustum(planes[t : t + 1])
+    s = time.perf_counter() - t0
+    out["c4_trees_per_s"] = 16 / s
+    out["c4_sample"] = "16 trees of the same distribution, one after another"
+    pool.shutdown()
     return out
 
 
