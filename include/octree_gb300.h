@@ -160,8 +160,8 @@ int otg_tree_save_static(otg_tree* tree, int with_entities, void* buffer, uint64
    max depth and max elements per node, in `box` (NULL: the entities' bounding box, as Create
    without a box), and the rebuild is checked against every archived array (entity order within a
    node aside). OTG_ERR_INVALID_ARGUMENT for another tree type, a malformed archive, an archive
-   without entities, or one whose tree is not the rebuild of its entities. `tree` gives the scalar
-   type and kind (otg_tree_new); host memory. */
+   without entities, or one whose tree is not the rebuild of its entities (the tree then holds
+   that rebuild). `tree` gives the scalar type and kind (otg_tree_new); host memory. */
 int otg_tree_load_static(otg_tree* tree, const void* buffer, uint64_t size, const void* box, void* stream);
 
 /* Copies an exported static layout into host arrays (sizes as above; a null pointer skips an array). */
