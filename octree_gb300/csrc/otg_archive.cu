@@ -147,7 +147,9 @@ int gather_static(TreeState& t, bool managed, StaticHost<T>& h, cudaStream_t st)
   h.depth.resize(m);
   h.storage.resize(n);
   h.geometry.resize(m * L.geometry_per_node);
-  h.entities.resize(managed ? n * W : 0);
+  // the entities in input order come from the tree's own sorted copy (entity storage[i] is the
+  // id of sortedGeom[i]): a tree built from device memory holds no input-order copy of them
+  std::vector<T> sorted(managed ? n * W : 0);
   struct Part
   {
     void* dst;
@@ -158,12 +160,26 @@ int gather_static(TreeState& t, bool managed, StaticHost<T>& h, cudaStream_t st)
                 { h.depth.data(), L.depth_ids, h.depth.size() },
                 { h.storage.data(), L.entity_storage, sizeof(u32) * h.storage.size() },
                 { h.geometry.data(), L.geometry, sizeof(T) * h.geometry.size() },
-                { h.entities.data(), t.entities.p, sizeof(T) * h.entities.size() },
+                { sorted.data(), t.sortedGeom.p, sizeof(T) * sorted.size() },
                 { &h.sp, t.space.p, t.space.p ? sizeof(Space<T>) : 0 } };
   for (const Part& p : parts)
     if (p.bytes)
       if (cudaError_t e = cudaMemcpy(p.dst, p.src, p.bytes, cudaMemcpyDeviceToHost))
         return cuda_status(e, "copying the tree for its archive");
+  if (managed)
+  {
+    h.entities.resize(n * W);
+    for (u64 i = 0; i < n; ++i)
+    {
+      const u32 id = h.storage[i];
+      if (id >= n)
+      {
+        set_error("archive: entity storage holds an id out of range");
+        return OTG_ERR_CUDA;
+      }
+      std::memcpy(&h.entities[size_t(id) * W], &sorted[i * W], sizeof(T) * W);
+    }
+  }
   return OTG_OK;
 }
 

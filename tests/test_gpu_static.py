@@ -213,3 +213,20 @@ def test_resume_refusals():
     with pytest.raises(otg.OtgError):
         fresh().load_static(tb.save_static(True))
     assert fresh().load_static(tb.save_static(True), box=box).save_static(True) == tb.save_static(True)
+
+
+def test_archive_of_a_tree_built_from_device_memory():
+    """A tree built from device memory (read in place, no input-order copy kept) archives the same
+    entities and bytes as one built from host memory."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(44)
+    c = rng.random((30000, 3)) * 50
+    h = rng.random((30000, 3))
+    boxes = np.concatenate([c - h, c + h], 1)
+    th = _gpu_tree(boxes, KIND_LOOSE_BOXES, 7, None, 8)
+    dev = torch.as_tensor(boxes, device="cuda")
+    td = otg.Tree("boxes").create(dev, max_depth=7, max_elements=8)
+    torch.cuda.synchronize()
+    dev.fill_(0.0)  # the archive must not read the caller's array
+    torch.cuda.synchronize()
+    assert td.save_static(True) == th.save_static(True)
