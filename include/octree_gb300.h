@@ -50,6 +50,8 @@ extern "C" {
 /* tree kinds: core/ot_aliases.h:119 (OctreePoint) and :122 (OctreeBox) */
 #define OTG_KIND_POINTS 0 /* loose factor 1.0, MinPoint node geometry (core/configuration.h:104-105) */
 #define OTG_KIND_BOXES 1  /* loose factor 2.0, MBR node geometry      (core/configuration.h:107-108) */
+#define OTG_KIND_BOXES_REGULAR 2 /* OrthoTreeBoxND<3, false> (core/ot_aliases.h:62-66): loose factor 1.0,
+                                    MBR node geometry, box locations by GetBoxGridID (detail/si_grid.h:177-219) */
 
 /* RangeSearchMode, core/types.h:83-87 */
 #define OTG_RANGE_INSIDE 0

@@ -3,7 +3,8 @@
 //
 //   OrthoTreeGPU::OctreePointM   ~ OrthoTree::OctreePointM (core/ot_aliases.h:364)
 //   OrthoTreeGPU::OctreeBoxM     ~ OrthoTree::OctreeBoxM   (core/ot_aliases.h:369)
-//   (and the FP32 variants OctreePointMF / OctreeBoxMF)
+//   OrthoTreeGPU::OctreeBoxMs<L> ~ OrthoTree::OctreeBoxMs<L> (core/ot_aliases.h:367-368; false: regular boxes)
+//   (and the FP32 variants OctreePointMF / OctreeBoxMF / OctreeBoxMsF)
 //
 // Construction and Create take the reference's arguments (core/ot_managed.h:169-228, 318-360):
 // entities, optional max depth, optional space box, max elements per node (default 16,
@@ -14,7 +15,9 @@
 //   GetNearestNeighbors, RayIntersectedAll, RayIntersectedFirst, CollisionDetection (one tree and
 //   two trees).
 // Each query also has a batched form (…Batch) answering many query geometries in one GPU launch;
-// it returns a Csr (offsets + ids [+ distances]).
+// it returns a Csr (offsets + ids [+ distances]). ExportStatic gives the arrays of the reference's
+// static linear tree of the same entities; SaveStatic / LoadStatic write and resume its binary
+// archive (serialization/binary_archive.h).
 //
 // Orders where the reference leaves ties unspecified are made canonical:
 //   * GetNearestNeighbors and RayIntersectedAll: by (distance, id);
@@ -526,7 +529,7 @@ public:
   template<typename TExecMode = std::nullptr_t>
   std::vector<std::pair<EntityID, EntityID>> CollisionDetection(double tolerance = detail::base_tolerance<TScalar>(), TExecMode = {},
                                                                 Algorithm algo = Algorithm::Default) const
-    requires(KIND == OTG_KIND_BOXES)
+    requires(KIND != OTG_KIND_POINTS)
   {
     otg_result* r = nullptr;
     detail::check(otg_collision_self(m_tree, tolerance, int(algo), &r, m_stream));
@@ -535,7 +538,7 @@ public:
   // CollisionDetection(otherTree, tolerance) — core/ot_managed.h:712-718, core/ot_query.h:1462-1497
   std::vector<std::pair<EntityID, EntityID>> CollisionDetection(const OrthoTreeManagedGPU& otherTree, double tolerance = detail::base_tolerance<TScalar>(),
                                                                 Algorithm algo = Algorithm::Default) const
-    requires(KIND == OTG_KIND_BOXES)
+    requires(KIND != OTG_KIND_POINTS)
   {
     otg_result* r = nullptr;
     detail::check(otg_collision_pair(m_tree, otherTree.m_tree, tolerance, int(algo), &r, m_stream));
@@ -543,7 +546,7 @@ public:
   }
   static std::vector<std::pair<EntityID, EntityID>> CollisionDetection(const OrthoTreeManagedGPU& leftTree, const OrthoTreeManagedGPU& rightTree,
                                                                        double tolerance = detail::base_tolerance<TScalar>())
-    requires(KIND == OTG_KIND_BOXES)
+    requires(KIND != OTG_KIND_POINTS)
   {
     return leftTree.CollisionDetection(rightTree, tolerance);
   }
@@ -559,5 +562,10 @@ using OctreePointM = OrthoTreeManagedGPU<Vector3<double>, double, OTG_KIND_POINT
 using OctreeBoxM = OrthoTreeManagedGPU<BoundingBox3<double>, double, OTG_KIND_BOXES>;
 using OctreePointMF = OrthoTreeManagedGPU<Vector3<float>, float, OTG_KIND_POINTS>;
 using OctreeBoxMF = OrthoTreeManagedGPU<BoundingBox3<float>, float, OTG_KIND_BOXES>;
+// OctreeBoxMs<IS_LOOSE_TREE> (core/ot_aliases.h:367-368): false = the regular box tree (loose factor 1.0)
+template<bool IS_LOOSE_TREE>
+using OctreeBoxMs = OrthoTreeManagedGPU<BoundingBox3<double>, double, IS_LOOSE_TREE ? OTG_KIND_BOXES : OTG_KIND_BOXES_REGULAR>;
+template<bool IS_LOOSE_TREE>
+using OctreeBoxMsF = OrthoTreeManagedGPU<BoundingBox3<float>, float, IS_LOOSE_TREE ? OTG_KIND_BOXES : OTG_KIND_BOXES_REGULAR>;
 
 } // namespace OrthoTreeGPU

@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(_HERE, "_build", "liboctree_gb300.so")
 OTG_OK = 0
 MEM_HOST, MEM_DEVICE = 0, 1
 SCALAR_F64, SCALAR_F32 = 0, 1
-KIND_POINTS, KIND_BOXES = 0, 1
+KIND_POINTS, KIND_BOXES, KIND_BOXES_REGULAR = 0, 1, 2
 RANGE_INSIDE, RANGE_OVERLAP = 0, 1
 ALGO_DEFAULT, ALGO_PLAIN_FP64, ALGO_FILTERED = 0, 1, 2
 # one condition of a combined query: the otg_condition record (include/octree_gb300.h)
@@ -246,10 +246,15 @@ class Result:
 
 
 class Tree:
-    """A GPU OctreePoint (kind='points') or OctreeBox (kind='boxes', loose factor 2.0)."""
+    """A GPU OctreePoint (kind='points'), OctreeBox (kind='boxes', loose factor 2.0) or a regular
+    box tree OrthoTreeBoxND<3, false> (kind='regular_boxes', loose factor 1.0)."""
+
+    _KINDS = {"points": KIND_POINTS, "boxes": KIND_BOXES, "regular_boxes": KIND_BOXES_REGULAR}
 
     def __init__(self, kind="points", dtype=np.float64):
-        self.kind = KIND_POINTS if kind == "points" else KIND_BOXES
+        if kind not in self._KINDS:
+            raise ValueError(f"kind must be one of {sorted(self._KINDS)}")
+        self.kind = self._KINDS[kind]
         self.dtype = np.dtype(dtype).type
         self.scalar = SCALAR_F64 if self.dtype == np.float64 else SCALAR_F32
         h = _vp()

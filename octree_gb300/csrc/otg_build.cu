@@ -339,6 +339,46 @@ __device__ __forceinline__ u64 point_key_ref(const T* p, const Space<T>& s, u32 
   return encode3(g[0], g[1], g[2]) + 1;
 }
 
+// si_grid.h:177-219 GetBoxGridID + si_morton.h:698-722 GetRangeLocation (regular box trees, loose
+// factor 1.0) -> loc << 5 | depth: the cells of the min and max corner (the max cell stepped back
+// when it falls on a cell boundary or past the grid) and their lowest common ancestor. Outside
+// the space: the root's location (key 0). The arithmetic is the reference's, operation by operation.
+template<typename T, typename R>
+__device__ __forceinline__ u64 regular_box_key_ref(const T* b, const Space<T>& s, u32 D)
+{
+  const T tol = base_tol<T>();
+  const u32 res = 1u << D;
+  const R zero = R(0), maxR = R(res);
+  u32 g0[3], g1[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    const T bmin = T(b[d] - s.min[d]);
+    const T bmax = T(b[3 + d] - s.min[d]);
+    if (bmin < -tol || bmax > s.size[d] + tol)
+      return 0;
+    const R r = Raster<R, T>::rast(s, d);
+    const R mn = R(bmin) * r, mx = R(bmax) * r;
+    g0[d] = to_grid(mn < zero ? zero : (maxR < mn ? maxR : mn)); // std::clamp
+    g1[d] = to_grid(mx < zero ? zero : (maxR < mx ? maxR : mx));
+    if ((g0[d] != g1[d] && floor(mx) == mx) || g1[d] >= res)
+      --g1[d];
+  }
+  const u64 l0 = encode3(g0[0], g0[1], g0[2]), l1 = encode3(g1[0], g1[1], g1[2]);
+  if (l0 == l1)
+    return (l0 << 5) | u64(D);
+  const u64 diff = l0 ^ l1;
+  const u32 levelID = (64u - u32(__clzll((long long)diff)) + 2u) / 3u;
+  const u32 shift = 3u * levelID;
+  return (((l0 >> shift) << shift) << 5) | u64(D - levelID);
+}
+
+template<typename T>
+__device__ __forceinline__ u64 regular_box_key(const T* b, const Space<T>& s, u32 D)
+{
+  return s.rasterDouble ? regular_box_key_ref<T, double>(b, s, D) : regular_box_key_ref<T, float>(b, s, D);
+}
+
 // si_grid.h:221-285 GetLooseBoxGridData<2.0> + si_mortongrid.h:78-88 -> loc << 5 | depth
 template<typename T, typename R>
 __device__ __forceinline__ u64 loose_box_key_ref(const T* b, const Space<T>& s, u32 D)
@@ -447,7 +487,7 @@ __device__ __forceinline__ u64 entity_key(const T* e, const typename Ord<T>::U* 
 template<typename T, typename R, typename K, bool IS_BOX>
 __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent, u64 n, bool vec, const Space<T>* __restrict__ spg,
                                                       const typename Ord<T>::U* __restrict__ tabG, u32 cells, int tabInSmem,
-                                                      K* __restrict__ keys, u32* __restrict__ hist, u32 passes)
+                                                      K* __restrict__ keys, u32* __restrict__ hist, u32 passes, bool regular)
 {
   using O = Ord<T>;
   using U = typename O::U;
@@ -485,7 +525,11 @@ __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent,
     {
       if (k >= cnt)
         break;
-      const K kk = K(entity_key<T, IS_BOX>(v + k * W, tab, perDim, cells, minF, rastF, D));
+      K kk;
+      if constexpr (IS_BOX)
+        kk = K(regular ? regular_box_key<T>(v + k * W, *spg, D) : entity_key<T, IS_BOX>(v + k * W, tab, perDim, cells, minF, rastF, D));
+      else
+        kk = K(entity_key<T, IS_BOX>(v + k * W, tab, perDim, cells, minF, rastF, D));
       keys[c * E + k] = kk;
       for (u32 p = 0; p < passes; ++p)
         atomicAdd(&sh[p][(kk >> (kRadixBits * p)) & (kRadix - 1)], 1u);
@@ -502,7 +546,7 @@ __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent,
 // reference formulas from the tree-ordered copy
 template<typename T, typename R, bool IS_BOX>
 __global__ void location_export_kernel(const T* __restrict__ geom, const u32* __restrict__ ids, u64 n, const Space<T>* __restrict__ spg,
-                                       u64* __restrict__ out)
+                                       u64* __restrict__ out, bool regular)
 {
   const Space<T> s = *spg;
   const u32 D = s.D;
@@ -512,7 +556,7 @@ __global__ void location_export_kernel(const T* __restrict__ geom, const u32* __
     if (id >= n)
       continue;
     if constexpr (IS_BOX)
-      out[id] = loose_box_key_ref<T, R>(geom + i * 6, s, D);
+      out[id] = regular ? regular_box_key_ref<T, R>(geom + i * 6, s, D) : loose_box_key_ref<T, R>(geom + i * 6, s, D);
     else
     {
       u64 k = point_key_ref<T, R>(geom + i * 3, s, (1u << D) - 1u);
@@ -1106,6 +1150,7 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
 {
   constexpr int W = IS_BOX ? 6 : 3;
   using U = typename Ord<T>::U;
+  const bool regular = t.kind == OTG_KIND_BOXES_REGULAR; // GetBoxGridID instead of the loose grid data
   const u32 D = t.D;
   const u32 bits = IS_BOX ? 3 * D + 5 : 3 * D + 1;
   const u32 passes = (bits + kRadixBits - 1) / kRadixBits;
@@ -1176,13 +1221,13 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   {
     auto kfn = codegen_kernel<T, double, K, IS_BOX>;
     cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
-    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes);
+    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes, regular);
   }
   else
   {
     auto kfn = codegen_kernel<T, float, K, IS_BOX>;
     cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
-    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes);
+    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes, regular);
   }
 
   prof.mark("sort", st);
@@ -1254,7 +1299,7 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
 
 int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const void* box, u64 maxElem, int mem, cudaStream_t st)
 {
-  const bool isBox = t.kind == OTG_KIND_BOXES;
+  const bool isBox = t.kind != OTG_KIND_POINTS;
   const int W = isBox ? 6 : 3;
   const size_t esz = t.scalar == OTG_SCALAR_F64 ? 8 : 4;
   if (maxElem == 0)
@@ -1487,7 +1532,7 @@ template<typename T, typename K, bool IS_BOX>
 __global__ void __launch_bounds__(256) forest_codegen_kernel(const T* __restrict__ ent, const uint2* __restrict__ segTiles, const u64* __restrict__ off,
                                                              const Space<T>* __restrict__ sp, const typename Ord<T>::U* __restrict__ tabG,
                                                              const u64* __restrict__ tabOff, int tabInSmem, K* __restrict__ keys, u32* __restrict__ hist,
-                                                             u32 trees, u32 passes)
+                                                             u32 trees, u32 passes, bool regular)
 {
   using U = typename Ord<T>::U;
   constexpr int W = IS_BOX ? 6 : 3;
@@ -1523,7 +1568,11 @@ __global__ void __launch_bounds__(256) forest_codegen_kernel(const T* __restrict
 #pragma unroll
     for (int c = 0; c < W; ++c)
       v[c] = ent[i * W + c];
-    const K kk = K(entity_key<T, IS_BOX>(v, tab, perDim, cells, minF, rastF, D));
+    K kk;
+    if constexpr (IS_BOX)
+      kk = K(regular ? regular_box_key<T>(v, s, D) : entity_key<T, IS_BOX>(v, tab, perDim, cells, minF, rastF, D));
+    else
+      kk = K(entity_key<T, IS_BOX>(v, tab, perDim, cells, minF, rastF, D));
     keys[i] = kk;
     for (u32 p = 0; p < passes; ++p)
       atomicAdd(&sh[p][(kk >> (kRadixBits * p)) & (kRadix - 1)], 1u);
@@ -1558,6 +1607,7 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
 {
   constexpr int W = IS_BOX ? 6 : 3;
   using U = typename Ord<T>::U;
+  const bool regular = t.kind == OTG_KIND_BOXES_REGULAR;
   const u32 trees = t.trees;
   const u64 n = t.n;
   const u32 Dmax = t.D;
@@ -1635,7 +1685,8 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
   {
     auto kfn = forest_codegen_kernel<T, K, IS_BOX>;
     cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
-    kfn<<<tiles, 256, cgSmem, st>>>(ent, segTiles, off, sp, t.rasterTab.as<U>(), t.tabOff.as<u64>(), tabInSmem, t.keysA.as<K>(), hist, trees, passes);
+    kfn<<<tiles, 256, cgSmem, st>>>(ent, segTiles, off, sp, t.rasterTab.as<U>(), t.tabOff.as<u64>(), tabInSmem, t.keysA.as<K>(), hist, trees, passes,
+                                    regular);
   }
 
   prof.mark("sort", st);
@@ -1695,7 +1746,7 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
 int build_forest(TreeState& t, const void* entities, const u64* treeOffsets, u32 trees, u32 maxDepth, const void* boxes, u64 maxElem, int mem,
                  cudaStream_t st)
 {
-  const bool isBox = t.kind == OTG_KIND_BOXES;
+  const bool isBox = t.kind != OTG_KIND_POINTS;
   const int W = isBox ? 6 : 3;
   const size_t esz = t.scalar == OTG_SCALAR_F64 ? 8 : 4;
   if (maxElem == 0 || trees == 0 || !treeOffsets || treeOffsets[0] != 0)
@@ -1811,7 +1862,7 @@ int forest_relaunch(TreeState& t, const void* entities, const void* boxes, cudaS
     set_error("forest_relaunch needs a forest that was built before");
     return OTG_ERR_INVALID_ARGUMENT;
   }
-  const bool isBox = t.kind == OTG_KIND_BOXES;
+  const bool isBox = t.kind != OTG_KIND_POINTS;
   int rc;
   if (t.scalar == OTG_SCALAR_F64)
   {
@@ -1886,7 +1937,7 @@ int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st)
       return cuda_status(e, "allocating export buffer");
     out = tmp.as<u64>();
   }
-  const bool isBox = t.kind == OTG_KIND_BOXES;
+  const bool isBox = t.kind != OTG_KIND_POINTS;
   const bool rd = t.scalar == OTG_SCALAR_F64 || t.D >= 16;
   const int blocks = grid_blocks(t.n);
   const u32* ids = t.sortedIds.as<u32>();
@@ -1895,9 +1946,9 @@ int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st)
     auto sp = t.space.as<Space<double>>();
     const double* g = t.sortedGeom.as<double>();
     if (isBox)
-      location_export_kernel<double, double, true><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
+      location_export_kernel<double, double, true><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out, t.kind == OTG_KIND_BOXES_REGULAR);
     else
-      location_export_kernel<double, double, false><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
+      location_export_kernel<double, double, false><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out, t.kind == OTG_KIND_BOXES_REGULAR);
   }
   else
   {
@@ -1906,16 +1957,16 @@ int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st)
     if (isBox)
     {
       if (rd)
-        location_export_kernel<float, double, true><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
+        location_export_kernel<float, double, true><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out, t.kind == OTG_KIND_BOXES_REGULAR);
       else
-        location_export_kernel<float, float, true><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
+        location_export_kernel<float, float, true><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out, t.kind == OTG_KIND_BOXES_REGULAR);
     }
     else
     {
       if (rd)
-        location_export_kernel<float, double, false><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
+        location_export_kernel<float, double, false><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out, t.kind == OTG_KIND_BOXES_REGULAR);
       else
-        location_export_kernel<float, float, false><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out);
+        location_export_kernel<float, float, false><<<blocks, 256, 0, st>>>(g, ids, t.n, sp, out, t.kind == OTG_KIND_BOXES_REGULAR);
     }
   }
   cudaError_t e = cudaGetLastError();

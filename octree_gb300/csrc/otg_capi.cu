@@ -171,7 +171,7 @@ extern "C"
 
   int otg_tree_new(otg_tree** out, int scalar, int kind)
   {
-    if (!out || (scalar != OTG_SCALAR_F64 && scalar != OTG_SCALAR_F32) || (kind != OTG_KIND_POINTS && kind != OTG_KIND_BOXES))
+    if (!out || (scalar != OTG_SCALAR_F64 && scalar != OTG_SCALAR_F32) || (kind != OTG_KIND_POINTS && kind != OTG_KIND_BOXES && kind != OTG_KIND_BOXES_REGULAR))
     {
       set_error("otg_tree_new: invalid argument");
       return OTG_ERR_INVALID_ARGUMENT;
@@ -428,7 +428,7 @@ extern "C"
 
   int otg_collision_self(const otg_tree* t, double tol, int algo, otg_result** out, void* stream)
   {
-    if (t && t->s.kind != OTG_KIND_BOXES)
+    if (t && t->s.kind == OTG_KIND_POINTS)
     {
       set_error("collision detection needs a box tree");
       return OTG_ERR_INVALID_ARGUMENT;
@@ -445,7 +445,7 @@ extern "C"
       set_error("collision detection is defined for single trees, not forests");
       return OTG_ERR_INVALID_ARGUMENT;
     }
-    if ((a && a->s.kind != OTG_KIND_BOXES) || b->s.kind != OTG_KIND_BOXES || (a && a->s.scalar != b->s.scalar))
+    if ((a && a->s.kind == OTG_KIND_POINTS) || b->s.kind == OTG_KIND_POINTS || (a && a->s.kind != b->s.kind) || (a && a->s.scalar != b->s.scalar))
     {
       set_error("collision detection needs two box trees of the same scalar type");
       return OTG_ERR_INVALID_ARGUMENT;

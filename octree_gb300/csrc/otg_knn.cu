@@ -712,7 +712,7 @@ static int ensure_image32_impl(TreeState& t, cudaStream_t st)
     return cuda_status(e, "allocating the FP32 tree image");
   if (t.kind == OTG_KIND_POINTS && t.n)
     point_image_kernel<T><<<blocks_for(t.n), 256, 0, st>>>(t.sortedGeom.as<T>(), t.n, t.geom32.as<float4>());
-  node_image_kernel<T><<<blocks_for(t.nodeCount), 256, 0, st>>>(t.nodeBox.as<T>(), t.kind == OTG_KIND_BOXES ? t.nodeMax.as<T>() : nullptr, t.nodeCount,
+  node_image_kernel<T><<<blocks_for(t.nodeCount), 256, 0, st>>>(t.nodeBox.as<T>(), t.kind != OTG_KIND_POINTS ? t.nodeMax.as<T>() : nullptr, t.nodeCount,
                                                                  t.nodeBox32.as<float4>());
   if ((e = cudaGetLastError()))
     return cuda_status(e, "building the FP32 tree image");

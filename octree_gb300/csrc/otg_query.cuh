@@ -289,7 +289,7 @@ template<typename T>
 static inline TreeView<T> view(const TreeState& t, const u32* qTree = nullptr)
 {
   return TreeView<T>{ t.nodeLink.as<uint4>(), t.nodeBox.as<T>(), t.nodeMax.as<T>(), t.sortedIds.as<u32>(), t.sortedGeom.as<T>(), u32(t.n),
-                      t.kind == OTG_KIND_BOXES ? 1 : 0, u32(t.nodeCount), qTree, qTree ? t.treeOff.as<u64>() : nullptr,
+                      t.kind != OTG_KIND_POINTS ? 1 : 0, u32(t.nodeCount), qTree, qTree ? t.treeOff.as<u64>() : nullptr,
                       t.nodeDepth.as<unsigned char>() };
 }
 

@@ -51,7 +51,7 @@ static u32 log2_bucket(u64 v)
 std::string tune_key(const char* op, bool f64, int kind, u64 entities, u64 queries)
 {
   char buf[128];
-  std::snprintf(buf, sizeof(buf), "%s %s %s n=2^%u q=2^%u", op, f64 ? "f64" : "f32", kind == OTG_KIND_BOXES ? "boxes" : "points", log2_bucket(entities),
+  std::snprintf(buf, sizeof(buf), "%s %s %s n=2^%u q=2^%u", op, f64 ? "f64" : "f32", kind != OTG_KIND_POINTS ? "boxes" : "points", log2_bucket(entities),
                 log2_bucket(queries));
   return buf;
 }

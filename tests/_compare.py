@@ -6,6 +6,9 @@ import numpy as np
 
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
+# the GPU tree kind of each oracle kind (0 points, 1 loose boxes, 2 regular boxes)
+GPU_KIND = {0: "points", 1: "boxes", 2: "regular_boxes"}
+
 
 def golden_cases():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))

@@ -11,7 +11,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
-from _oracle_lib import KIND_LOOSE_BOXES, KIND_POINTS, reference  # noqa: E402
+from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, reference  # noqa: E402
 
 
 def queries(rng, dtype, scale, nq=48):
@@ -121,6 +121,18 @@ def main():
     # degenerate boxes (points as boxes), given box
     deg = np.concatenate([cen[:600], cen[:600]], 1)
     run_case("boxes_f64_degenerate", deg, KIND_LOOSE_BOXES, 6, np.array([0.0, 0, 0, 100, 100, 100]), 8, queries(rng, np.float64, 100), 0.0)
+    # regular (non-loose) box trees, OctreeBoxs<false>: FP64 with the data's bounding box, and FP32
+    # in a given box with corners on cell boundaries and boxes outside it (drawn from their own seed,
+    # so the earlier cases stay as they were). Every box has extent: the reference asserts on a
+    # degenerate box on the max face of its space (si_grid.h:213), where the second tree of the
+    # fixture, in its data's bounding box, would have one.
+    rrng = np.random.default_rng(20261204)
+    run_case("boxes_regular_f64", boxes, KIND_BOXES, 5, None, 16, queries(rrng, np.float64, 100), 0.0)
+    grid = np.floor(rrng.random((1200, 3)) * 32) * (100 / 32)
+    on_grid = np.concatenate([grid, grid + rrng.integers(1, 3, (1200, 3)) * (100 / 32)], 1)
+    on_grid[:20] += 150.0
+    run_case("boxes_regular_f32_box", on_grid.astype(np.float32), KIND_BOXES, 6, np.array([0.0, 0, 0, 100, 100, 100], np.float32), 8,
+             queries(rrng, np.float32, 100), 0.0)
 
 
 if __name__ == "__main__":

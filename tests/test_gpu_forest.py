@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import octree_gb300 as otg
-from _compare import assert_csr_equal, assert_dist_close, assert_nodes_equal, node_dict
+from _compare import GPU_KIND, assert_csr_equal, assert_dist_close, assert_nodes_equal, node_dict
 from _oracle_lib import KIND_LOOSE_BOXES, KIND_POINTS, oracle
 
 pytestmark = pytest.mark.gpu
@@ -80,7 +80,7 @@ def test_forest_matches_oracle_trees(kind, dtype, max_depth, given_box):
     boxes = None
     if given_box:
         boxes = np.tile(np.array([[-5.0, -5.0, -5.0, 105.0, 105.0, 105.0]]), (trees, 1)).astype(dtype)
-    f = otg.Forest("points" if kind == KIND_POINTS else "boxes", dtype).create(ent, off, max_depth=max_depth, boxes=boxes, max_elements=16)
+    f = otg.Forest(GPU_KIND[kind], dtype).create(ent, off, max_depth=max_depth, boxes=boxes, max_elements=16)
     assert f.tree_count == trees
     ranges, pts, rays, planes, qoff = _queries(rng, trees, 40, dtype)
     res = {

@@ -5,8 +5,8 @@ import numpy as np
 import pytest
 
 import octree_gb300 as otg
-from _compare import assert_csr_equal, assert_dist_close, assert_nodes_equal, golden_cases, load_golden, node_dict
-from _oracle_lib import KIND_LOOSE_BOXES, KIND_POINTS, oracle
+from _compare import GPU_KIND, assert_csr_equal, assert_dist_close, assert_nodes_equal, golden_cases, load_golden, node_dict
+from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -14,7 +14,7 @@ RAY_REL = 1e-12
 
 
 def _gpu_tree(ent, kind, max_depth, box, max_elem):
-    t = otg.Tree("points" if kind == KIND_POINTS else "boxes", ent.dtype)
+    t = otg.Tree(GPU_KIND[kind], ent.dtype)
     return t.create(ent, max_depth=max_depth, box=box, max_elements=max_elem)
 
 
@@ -153,24 +153,26 @@ def test_point_emission_layouts(dtype, name):
     assert_csr_equal(t.knn(q, 9), o.knn(q, 9), f"{name} knn")
 
 
+@pytest.mark.parametrize("kind", [KIND_LOOSE_BOXES, KIND_BOXES])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("max_depth,max_elem", [(8, 32), (0, 16), (4, 2)])
-def test_boxes_random(dtype, max_depth, max_elem):
+def test_boxes_random(dtype, max_depth, max_elem, kind):
+    """Loose (OctreeBox) and regular (OctreeBoxs<false>) box trees against the oracle."""
     rng = np.random.default_rng(7 + max_depth + max_elem)
     n = 60_000
     cen = np.where(rng.random((n, 1)) < 0.5, rng.random((n, 3)) * 1000, rng.normal(500, 10, (n, 3)))
     half = rng.lognormal(np.log(0.5), 0.6, (n, 3))
     boxes = np.concatenate([cen - half, cen + half], 1).astype(dtype)
-    t = _gpu_tree(boxes, KIND_LOOSE_BOXES, max_depth, None, max_elem)
-    o = oracle().create(boxes, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    t = _gpu_tree(boxes, kind, max_depth, None, max_elem)
+    o = oracle().create(boxes, kind, max_depth, None, max_elem)
     assert np.array_equal(t.location_keys(), o.location_keys())
     assert_nodes_equal(t.nodes(), o.nodes(), "boxes")
-    _check_queries(t, o, _queries(rng, dtype, 1000), KIND_LOOSE_BOXES, 0.0, "boxes")
+    _check_queries(t, o, _queries(rng, dtype, 1000), kind, 0.0, "boxes")
     assert np.array_equal(t.collision_self(), o.collide_self())
     other = boxes.copy()
     other += dtype(0.4)
-    t2 = _gpu_tree(other, KIND_LOOSE_BOXES, max_depth, None, max_elem)
-    o2 = oracle().create(other, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    t2 = _gpu_tree(other, kind, max_depth, None, max_elem)
+    o2 = oracle().create(other, kind, max_depth, None, max_elem)
     assert np.array_equal(t.collision_pair(t2), o.collide_pair(o2))
 
 
@@ -190,17 +192,18 @@ def _gap_boxes(dtype, seed):
     return ent
 
 
+@pytest.mark.parametrize("kind", [KIND_LOOSE_BOXES, KIND_BOXES])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 @pytest.mark.parametrize("max_depth,max_elem", [(3, 4), (5, 8), (2, 2)])
-def test_collision_rounding_gap(dtype, max_depth, max_elem):
+def test_collision_rounding_gap(dtype, max_depth, max_elem, kind):
     ent = _gap_boxes(dtype, 500 + max_depth)
-    t = _gpu_tree(ent, KIND_LOOSE_BOXES, max_depth, None, max_elem)
-    o = oracle().create(ent, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    t = _gpu_tree(ent, kind, max_depth, None, max_elem)
+    o = oracle().create(ent, kind, max_depth, None, max_elem)
     assert np.array_equal(t.collision_self(), o.collide_self())
     other = ent.copy()
     other[:, [0, 3]] = other[:, [0, 3]] + (other[:, 3:4] - other[:, 0:1])
-    t2 = _gpu_tree(other, KIND_LOOSE_BOXES, max_depth, None, max_elem)
-    o2 = oracle().create(other, KIND_LOOSE_BOXES, max_depth, None, max_elem)
+    t2 = _gpu_tree(other, kind, max_depth, None, max_elem)
+    o2 = oracle().create(other, kind, max_depth, None, max_elem)
     assert np.array_equal(t.collision_pair(t2), o.collide_pair(o2))
     assert np.array_equal(t2.collision_pair(t), o2.collide_pair(o))
 
@@ -226,12 +229,22 @@ def _edge_boxes():
     corner = b.copy()
     corner[1] = [50, 50, 50, 50, 50, 50]
     corner[2] = [0, 0, 0, 0, 0, 0]
-    return {
+    # regular trees: boxes whose max corner falls exactly on a cell boundary (the reference steps the
+    # max cell back there, si_grid.h:207-211), at the space's max face, and spanning several cells
+    grid = np.floor(rng.random((1500, 3)) * 64) * (50 / 64)
+    steps = rng.integers(0, 4, (1500, 3)) * (50 / 64)
+    on_grid = np.concatenate([grid, np.minimum(grid + steps, 50.0)], 1)
+    cases = {
         "boxes_degenerate": (np.concatenate([cen, cen], 1), KIND_LOOSE_BOXES, None),
         "box_spans_space": (span, KIND_LOOSE_BOXES, None),
         "boxes_on_max_corner": (corner, KIND_LOOSE_BOXES, np.array([0.0, 0, 0, 50, 50, 50])),
         "boxes_outside_box": (b, KIND_LOOSE_BOXES, np.array([10.0, 10, 10, 40, 40, 40])),
+        "regular_boxes_on_cell_boundaries": (on_grid, KIND_BOXES, np.array([0.0, 0, 0, 50, 50, 50])),
     }
+    for name in ("boxes_degenerate", "box_spans_space", "boxes_on_max_corner", "boxes_outside_box"):
+        ent, _, box = cases[name]
+        cases["regular_" + name] = (ent, KIND_BOXES, box)
+    return cases
 
 
 @pytest.mark.parametrize("name", list(EDGE_CASES) + list(_edge_boxes()))
@@ -367,7 +380,7 @@ def _single_planes(rng, n, scale):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-@pytest.mark.parametrize("kind", [KIND_POINTS, KIND_LOOSE_BOXES])
+@pytest.mark.parametrize("kind", [KIND_POINTS, KIND_LOOSE_BOXES, KIND_BOXES])
 def test_plane_queries_random(dtype, kind):
     rng = np.random.default_rng(4242 + kind)
     n = 150_000
@@ -391,7 +404,7 @@ def test_plane_queries_random(dtype, kind):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-@pytest.mark.parametrize("kind", [KIND_POINTS, KIND_LOOSE_BOXES])
+@pytest.mark.parametrize("kind", [KIND_POINTS, KIND_LOOSE_BOXES, KIND_BOXES])
 def test_combined_query_random(dtype, kind):
     """Query<And> / Query<Or> with frustum (crossing flags), range Inside / Overlap and plane
     conditions, batched and plain, against the oracle."""
@@ -450,7 +463,7 @@ def test_build_from_pinned_host_memory(kind, dtype, offset):
         ent = np.concatenate([c - h, c + h], 1)
     pinned = torch.from_numpy(ent.astype(dtype)).pin_memory()[offset:]
     host = pinned.numpy()
-    t = otg.Tree("points" if kind == KIND_POINTS else "boxes", dtype).create(pinned, max_depth=8, max_elements=16)
+    t = otg.Tree(GPU_KIND[kind], dtype).create(pinned, max_depth=8, max_elements=16)
     o = oracle().create(host, kind, 8, None, 16)
     assert np.array_equal(t.location_keys(), o.location_keys())
     assert_nodes_equal(t.nodes(), o.nodes(), "pinned")

@@ -10,6 +10,7 @@ import pytest
 
 import octree_gb300 as otg
 from _compare import (
+    GPU_KIND,
     assert_csr_equal,
     assert_static_equal,
     golden_cases,
@@ -18,13 +19,13 @@ from _compare import (
     static_archive_bytes,
     static_from_golden,
 )
-from _oracle_lib import KIND_LOOSE_BOXES, KIND_POINTS, oracle
+from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, oracle
 
 pytestmark = pytest.mark.gpu
 
 
 def _gpu_tree(ent, kind, max_depth, box, max_elem):
-    t = otg.Tree("points" if kind == KIND_POINTS else "boxes", ent.dtype)
+    t = otg.Tree(GPU_KIND[kind], ent.dtype)
     return t.create(ent, max_depth=max_depth, box=box, max_elements=max_elem)
 
 
@@ -66,6 +67,8 @@ def _cases():
         "boxes_deep": (boxes, KIND_LOOSE_BOXES, 17, None, 2),
         "boxes_outside_space": (np.concatenate([boxes, big]), KIND_LOOSE_BOXES, 6, space, 4),
         "duplicate_boxes": (np.repeat(boxes[:30], 40, 0), KIND_LOOSE_BOXES, 12, None, 6),
+        "regular_boxes": (boxes, KIND_BOXES, 8, None, 8),
+        "regular_boxes_f32_outside_space": (np.concatenate([boxes, big]).astype(np.float32), KIND_BOXES, 6, space, 4),
     }
 
 
@@ -171,20 +174,20 @@ def test_resume_from_reference_archive(name):
     if not int(g["static_defined"]):
         pytest.skip("no static tree for points outside the space")
     ent, kind = g["entities"], int(g["kind"])
-    t = otg.Tree("points" if kind == KIND_POINTS else "boxes", ent.dtype).load_static(g["static_archive"].tobytes(), box=g.get("box"))
+    t = otg.Tree(GPU_KIND[kind], ent.dtype).load_static(g["static_archive"].tobytes(), box=g.get("box"))
     assert_static_equal(t.export_static(), static_from_golden(g), name)
     for mode in (0, 1):
         assert_csr_equal(t.range_search(g["ranges"], mode)[:2], (g[f"range{mode}_off"], g[f"range{mode}_ids"]), f"{name} range{mode}")
     assert_csr_equal(t.knn(g["qpts"], g["k"]), (g["knn_off"], g["knn_ids"], g["knn_dist"]), f"{name} knn")
 
 
-@pytest.mark.parametrize("case", ["clustered_estimated_depth", "boxes_f32", "duplicate_boxes", "points_keys64"])
+@pytest.mark.parametrize("case", ["clustered_estimated_depth", "boxes_f32", "duplicate_boxes", "points_keys64", "regular_boxes"])
 def test_archive_round_trip(case):
     """save -> resume into a new tree -> save gives the same bytes; the resumed tree is the tree."""
     ent, kind, depth, box, me = _cases()[case]
     t = _gpu_tree(ent, kind, depth, box, me)
     data = t.save_static(True)
-    t2 = otg.Tree("points" if kind == KIND_POINTS else "boxes", ent.dtype).load_static(data, box=box)
+    t2 = otg.Tree(GPU_KIND[kind], ent.dtype).load_static(data, box=box)
     assert t2.save_static(True) == data
     assert t2.node_count == t.node_count
 
