@@ -343,6 +343,9 @@ __device__ __forceinline__ u64 point_key_ref(const T* p, const Space<T>& s, u32 
 // factor 1.0) -> loc << 5 | depth: the cells of the min and max corner (the max cell stepped back
 // when it falls on a cell boundary or past the grid) and their lowest common ancestor. Outside
 // the space: the root's location (key 0). The arithmetic is the reference's, operation by operation.
+// A min corner in cell 2^D (a box on the max face of the space, within the tolerance) is where the
+// reference asserts (si_grid.h:213); it returns kBadRegularBox, which the build reports.
+constexpr u64 kBadRegularBox = ~u64(0);
 template<typename T, typename R>
 __device__ __forceinline__ u64 regular_box_key_ref(const T* b, const Space<T>& s, u32 D)
 {
@@ -361,6 +364,8 @@ __device__ __forceinline__ u64 regular_box_key_ref(const T* b, const Space<T>& s
     const R mn = R(bmin) * r, mx = R(bmax) * r;
     g0[d] = to_grid(mn < zero ? zero : (maxR < mn ? maxR : mn)); // std::clamp
     g1[d] = to_grid(mx < zero ? zero : (maxR < mx ? maxR : mx));
+    if (g0[d] >= res)
+      return kBadRegularBox;
     if ((g0[d] != g1[d] && floor(mx) == mx) || g1[d] >= res)
       --g1[d];
   }
@@ -487,7 +492,7 @@ __device__ __forceinline__ u64 entity_key(const T* e, const typename Ord<T>::U* 
 template<typename T, typename R, typename K, bool IS_BOX>
 __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent, u64 n, bool vec, const Space<T>* __restrict__ spg,
                                                       const typename Ord<T>::U* __restrict__ tabG, u32 cells, int tabInSmem,
-                                                      K* __restrict__ keys, u32* __restrict__ hist, u32 passes, bool regular)
+                                                      K* __restrict__ keys, u32* __restrict__ hist, u32 passes, bool regular, u32* __restrict__ err)
 {
   using O = Ord<T>;
   using U = typename O::U;
@@ -527,7 +532,15 @@ __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent,
         break;
       K kk;
       if constexpr (IS_BOX)
-        kk = K(regular ? regular_box_key<T>(v + k * W, *spg, D) : entity_key<T, IS_BOX>(v + k * W, tab, perDim, cells, minF, rastF, D));
+      {
+        u64 k64 = regular ? regular_box_key<T>(v + k * W, *spg, D) : entity_key<T, IS_BOX>(v + k * W, tab, perDim, cells, minF, rastF, D);
+        if (k64 == kBadRegularBox)
+        {
+          atomicOr(err, kErrArgument);
+          k64 = 0;
+        }
+        kk = K(k64);
+      }
       else
         kk = K(entity_key<T, IS_BOX>(v + k * W, tab, perDim, cells, minF, rastF, D));
       keys[c * E + k] = kk;
@@ -1221,13 +1234,13 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   {
     auto kfn = codegen_kernel<T, double, K, IS_BOX>;
     cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
-    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes, regular);
+    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes, regular, t.err.as<u32>());
   }
   else
   {
     auto kfn = codegen_kernel<T, float, K, IS_BOX>;
     cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
-    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes, regular);
+    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes, regular, t.err.as<u32>());
   }
 
   prof.mark("sort", st);
@@ -1246,6 +1259,9 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   cudaStream_t es = st;
   if (int rc = emission_stream(t, es))
     return rc;
+  // entities that the emission places in no node keep kNoOwner
+  if (IS_BOX && (e = cudaMemsetAsync(t.ownerNode.p, 0xff, sizeof(u32) * n, st)))
+    return cuda_status(e, "clearing the entity owners");
   if ((e = cudaEventRecord(t.fork, st)) || (e = cudaStreamWaitEvent(es, t.fork, 0)))
     return cuda_status(e, "ordering the emission stream");
   prof.mark("gather+emit", st);
@@ -1532,7 +1548,7 @@ template<typename T, typename K, bool IS_BOX>
 __global__ void __launch_bounds__(256) forest_codegen_kernel(const T* __restrict__ ent, const uint2* __restrict__ segTiles, const u64* __restrict__ off,
                                                              const Space<T>* __restrict__ sp, const typename Ord<T>::U* __restrict__ tabG,
                                                              const u64* __restrict__ tabOff, int tabInSmem, K* __restrict__ keys, u32* __restrict__ hist,
-                                                             u32 trees, u32 passes, bool regular)
+                                                             u32 trees, u32 passes, bool regular, u32* __restrict__ err)
 {
   using U = typename Ord<T>::U;
   constexpr int W = IS_BOX ? 6 : 3;
@@ -1570,7 +1586,15 @@ __global__ void __launch_bounds__(256) forest_codegen_kernel(const T* __restrict
       v[c] = ent[i * W + c];
     K kk;
     if constexpr (IS_BOX)
-      kk = K(regular ? regular_box_key<T>(v, s, D) : entity_key<T, IS_BOX>(v, tab, perDim, cells, minF, rastF, D));
+    {
+      u64 k64 = regular ? regular_box_key<T>(v, s, D) : entity_key<T, IS_BOX>(v, tab, perDim, cells, minF, rastF, D);
+      if (k64 == kBadRegularBox)
+      {
+        atomicOr(err, kErrArgument);
+        k64 = 0;
+      }
+      kk = K(k64);
+    }
     else
       kk = K(entity_key<T, IS_BOX>(v, tab, perDim, cells, minF, rastF, D));
     keys[i] = kk;
@@ -1686,7 +1710,7 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
     auto kfn = forest_codegen_kernel<T, K, IS_BOX>;
     cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
     kfn<<<tiles, 256, cgSmem, st>>>(ent, segTiles, off, sp, t.rasterTab.as<U>(), t.tabOff.as<u64>(), tabInSmem, t.keysA.as<K>(), hist, trees, passes,
-                                    regular);
+                                    regular, t.err.as<u32>());
   }
 
   prof.mark("sort", st);
@@ -1711,6 +1735,10 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
       ent, t.sortedIds.as<u32>(), n, t.sortedGeom.as<T>());
   prof.mark("emit", st);
   u32* parent = IS_BOX ? t.nodeParent.as<u32>() : nullptr;
+  // entities that the emission places in no node keep kNoOwner
+  if (IS_BOX && n)
+    if (cudaError_t me = cudaMemsetAsync(t.ownerNode.p, 0xff, sizeof(u32) * n, st))
+      return cuda_status(me, "clearing the entity owners");
   forest_root_init_kernel<<<grid_blocks(trees, 128), 128, 0, es>>>(t.nodeLink.as<uint4>(), t.nodeKey.as<u64>(), t.nodeDepth.as<unsigned char>(),
                                                                    t.levelCount.as<u32>(), off, trees, parent, t.nodeTree.as<u32>());
   const int emitBlocks = grid_blocks(maxNodes, 256, 152 * 16);
@@ -1907,6 +1935,12 @@ int finish_build(TreeState& t, cudaStream_t st)
   {
     set_error("node capacity exceeded during emission");
     return OTG_ERR_OUT_OF_MEMORY;
+  }
+  if (hostErr & kErrArgument)
+  {
+    set_error("a box of a regular box tree has its min corner on the max face of the space, where the reference asserts "
+              "(detail/si_grid.h:213)");
+    return OTG_ERR_INVALID_ARGUMENT;
   }
   if (t.n || t.trees)
   {

@@ -106,6 +106,7 @@ struct CollideArgs
   const T* geomA;
   u32 nA;
   const u32* order; // processing order of the A entities
+  const u32* ownerA; // node holding each A entity (kNoOwner: none reachable, skipped)
   const float4* imgB;
   const T* geomB;
   const uint4* linkB;
@@ -139,6 +140,8 @@ __global__ void __launch_bounds__(WARPS * 32) collide_box_kernel(CollideArgs<T> 
     if (item >= a.nA)
       break;
     const u32 i = a.order ? a.order[item] : item;
+    if (a.ownerA && a.ownerA[i] == kNoOwner)
+      continue; // an entity that no node reachable from the root holds takes part in no pair
     const BoxImg me = load_img(a.imgA, i);
     u32 nbuf = 0;
     if (lane == 0)
@@ -257,7 +260,8 @@ __global__ void owner_depth_key_kernel(const u32* __restrict__ owner, const unsi
 {
   for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < n; i += u64(gridDim.x) * blockDim.x)
   {
-    keys[i] = depth[owner[i]];
+    const u32 o = owner[i];
+    keys[i] = o == kNoOwner ? 31u : depth[o]; // entities in no node last (the collision skips them)
     idx[i] = u32(i);
   }
 }
@@ -319,6 +323,7 @@ static int collide_search_impl(TreeState& A, TreeState& B, bool self, bool swapO
   }
   CollideArgs<T> a{};
   a.order = s.order.as<u32>();
+  a.ownerA = A.ownerNode.as<u32>();
   a.imgA = s.imgA.as<float4>();
   a.geomA = A.sortedGeom.as<T>();
   a.nA = u32(A.n);

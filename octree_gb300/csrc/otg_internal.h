@@ -81,6 +81,9 @@ struct DevBuf
   }
 };
 
+// ownerNode of an entity that no node reachable from the root holds (a location outside the grid:
+// the reference keeps it in a node the root does not link, so no query or collision sees it)
+constexpr u32 kNoOwner = 0xffffffffu;
 constexpr u32 kChildShift = 28;
 constexpr u32 kFirstChildMask = (1u << kChildShift) - 1;
 

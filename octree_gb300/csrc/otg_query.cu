@@ -863,7 +863,7 @@ __device__ __forceinline__ bool sweep_pair(const T* o, const StructTree<T>& ti, 
   if (o[3] < r[0]) // the inner loop breaks at the first inner min-x above o.maxX
     return false;
   if (r[3] < o[0])
-    return sweep_reaches(ti, ti.owner[ip], ip, o[0]);
+    return ti.owner[ip] != kNoOwner && sweep_reaches(ti, ti.owner[ip], ip, o[0]);
   return true;
 }
 
@@ -880,7 +880,9 @@ __global__ void __launch_bounds__(128) collide_filter_kernel(StructTree<T> A, St
     const T* gb = B.geom + u64(j) * 6;
     u32 ancA[21], ancB[21];
     bool keep = true;
-    if (!selfMode)
+    if (xa == kNoOwner || xb == kNoOwner)
+      keep = false; // an entity in no node reachable from the root is in no pair of the reference's walk
+    else if (!selfMode)
     {
       // CollisionDetection(left = A, right = B): node-pair walk from the roots, then the sweep
       keep = sweep_pair(ga, B, j);

@@ -241,7 +241,9 @@ def _edge_boxes():
         "boxes_outside_box": (b, KIND_LOOSE_BOXES, np.array([10.0, 10, 10, 40, 40, 40])),
         "regular_boxes_on_cell_boundaries": (on_grid, KIND_BOXES, np.array([0.0, 0, 0, 50, 50, 50])),
     }
-    for name in ("boxes_degenerate", "box_spans_space", "boxes_on_max_corner", "boxes_outside_box"):
+    # (a regular tree refuses a box with its min corner on the max face of the space, where the
+    # reference asserts: test_regular_boxes_on_max_face_are_refused)
+    for name in ("box_spans_space", "boxes_outside_box"):
         ent, _, box = cases[name]
         cases["regular_" + name] = (ent, KIND_BOXES, box)
     return cases
@@ -271,6 +273,24 @@ def test_edge_cases(name, max_depth, max_elem):
     assert_csr_equal(t.pick_search(q)[:2], o.pick_search(q), f"{name} pick")
     if kind != KIND_POINTS:
         assert np.array_equal(t.collision_self(), o.collide_self())
+
+
+def test_regular_boxes_on_max_face_are_refused():
+    """A regular (non-loose) box tree refuses a box whose min corner rasterises to cell 2^D (on the
+    max face of the space within the tolerance): the reference asserts there (detail/si_grid.h:213)
+    and its location's depth would wrap. Loose trees take such boxes (they hold them in no node)."""
+    rng = np.random.default_rng(9)
+    cen = rng.random((2000, 3)) * 50
+    degenerate = np.concatenate([cen, cen], 1)  # its bounding box puts one of them on the max face
+    corner = np.concatenate([cen - 1, cen + 1], 1)
+    corner[1] = [50, 50, 50, 50, 50, 50]
+    for ent, box in ((degenerate, None), (corner, np.array([0.0, 0, 0, 50, 50, 50]))):
+        with pytest.raises(otg.OtgError):
+            _gpu_tree(ent, KIND_BOXES, 5, box, 8)
+        _gpu_tree(ent, KIND_LOOSE_BOXES, 5, box, 8)  # the loose tree takes them
+    # the refusal comes from the same arithmetic the oracle restates: its location has a wrapped depth
+    keys = oracle().create(degenerate, KIND_BOXES, 5, None, 8).location_keys()
+    assert ((keys & 31) > 5).any()
 
 
 def test_empty_tree():
