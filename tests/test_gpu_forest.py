@@ -7,7 +7,7 @@ import pytest
 
 import octree_gb300 as otg
 from _compare import GPU_KIND, assert_csr_equal, assert_dist_close, assert_nodes_equal, node_dict
-from _oracle_lib import KIND_LOOSE_BOXES, KIND_POINTS, oracle
+from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, oracle
 
 pytestmark = pytest.mark.gpu
 RAY_REL = 1e-12
@@ -69,6 +69,8 @@ def _queries(rng, trees, per, dtype):
         (KIND_POINTS, np.float64, 0, False),
         (KIND_POINTS, np.float32, 5, True),
         (KIND_LOOSE_BOXES, np.float64, 6, True),
+        (KIND_BOXES, np.float32, 0, False),
+        (KIND_BOXES, np.float64, 6, True),
     ],
 )
 def test_forest_matches_oracle_trees(kind, dtype, max_depth, given_box):
