@@ -243,6 +243,25 @@ int main()
     oro_destroy(oo);
   }
   oro_destroy(ob);
+  // ---- regular (non-loose) boxes: OctreeBoxMs<false>
+  {
+    OctreeBoxMs<false> tr(boxes, 7, std::nullopt, 16);
+    void* orr = oro_create(0, 2, boxes.data(), boxes.size(), 7, nullptr, 16);
+    void* r = oro_range(orr, ranges.data(), nq, 1, -1.0);
+    for (int q = 0; q < nq; ++q)
+      expect(tr.RangeSearch(ranges[q], RangeSearchMode::Overlap), r, q, "RangeSearch (regular boxes)");
+    oro_res_free(r);
+    std::vector<uint32_t> flat;
+    for (auto [a, b] : tr.CollisionDetection())
+    {
+      flat.push_back(a);
+      flat.push_back(b);
+    }
+    r = oro_collide_self(orr, -1.0);
+    expect(flat, r, 0, "CollisionDetection (regular boxes)");
+    oro_res_free(r);
+    oro_destroy(orr);
+  }
   if (g_fail)
     return 1;
   std::printf("OK\n");
