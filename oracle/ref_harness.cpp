@@ -580,6 +580,34 @@ extern "C"
     return bytes.size();
   }
 
+  // The reference's own dynamicTree.IsEqualTo(staticTree) (core/ot_query.h:2149-2266) for its
+  // dynamic tree and the static tree of the same entities; -1 where the static tree is not built
+  // (point trees with points outside their space, see oro_static)
+  int oro_dynamic_equals_static(void* h)
+  {
+    auto* a = (AnyRef*)h;
+    if (a->kind == 0)
+      for (auto k : a->locKeys)
+        if ((k & 31u) != a->D)
+          return -1;
+    return with_static(a, [&]<typename ST>(auto ents, auto const& box, bool) -> int {
+      std::optional<typename ST::TBox> ob;
+      std::optional<depth_t> od;
+      static_args<ST>(a, box, ob, od);
+      ST st(PAR_EXEC, ents, od, ob, a->maxElem);
+      return with_tree(a, [&](auto& dyn, auto, auto, auto) -> int {
+        if constexpr (std::is_same_v<typename std::decay_t<decltype(dyn)>::GA, typename ST::GA>)
+        {
+          if (dyn.GetNodeCount() == 0 || st.GetNodeCount() == 0)
+            return dyn.GetNodeCount() == st.GetNodeCount() ? 1 : 0;
+          return dyn.IsEqualTo(st) ? 1 : 0;
+        }
+        else
+          return -1;
+      });
+    });
+  }
+
   // Archive bytes loaded by the reference (see static_load); null when they do not load.
   void* oro_static_load(void* h, const uint8_t* buf, uint64_t size, int managed)
   {

@@ -231,3 +231,56 @@ def space_of(ent, is_box, box=None):
         mn = ent[:, :3].min(axis=0)
         mx = (ent[:, 3:] if is_box else ent).max(axis=0)
     return mn, (mx - mn).astype(T)
+
+
+def tree_is_equal_to_static(dyn, st, tol):
+    """OrthoTreeQueryBase::IsEqualTo (core/ot_query.h:2149-2266) between a dynamic tree (nodes():
+    keys with sentinel bit, min, size, entity offsets and ids) and a static linear layout: equal
+    node counts, then from the roots: the same entity set per node, node boxes equal within `tol`,
+    the same number of children, and children matched by the octant of their centre against the
+    parent's centre, recursively."""
+    keys = [int(k) for k in dyn["keys"]]
+    idx = {k: i for i, k in enumerate(keys)}
+    m = len(st["depth"])
+    if len(keys) != m:
+        return False
+    cb = np.asarray(st["child_begins"], np.int64)
+    seg = np.asarray(st["segments"], np.int64)
+    es = np.asarray(st["entity_storage"])
+    geo = np.asarray(st["geometry"], np.float64)
+    if geo.shape[1] == 3:
+        # MinPoint trees store no size: GetNodeSize(depth) is the tree size halved per depth
+        # (core/ot_base.h:121-134; a power-of-two factor, so exact), the dynamic root's size
+        root = dyn["size"][idx[1]] if 1 in idx else np.zeros(3)
+        sizes = root[None, :] * (0.5 ** np.asarray(st["depth"], np.float64))[:, None]
+        geo = np.concatenate([geo, sizes], 1)
+
+    def dyn_children(k):
+        return [idx[(k << 3) | c] for c in range(8) if ((k << 3) | c) in idx]
+
+    def st_children(i):
+        return list(range(cb[i], cb[i + 1])) if i + 1 < len(cb) else []
+
+    def octant(cmin, csize, pmin, psize):
+        cc, pc = cmin + csize * 0.5, pmin + psize * 0.5
+        return sum(1 << d for d in range(3) if cc[d] > pc[d])
+
+    def rec(di, si):
+        a = np.sort(dyn["eids"][int(dyn["eoff"][di]) : int(dyn["eoff"][di + 1])])
+        b = np.sort(es[seg[si, 0] : seg[si, 0] + seg[si, 1]])
+        if not np.array_equal(a, b):
+            return False
+        dmin, dsize = dyn["min"][di], dyn["size"][di]
+        smin, ssize = geo[si, :3], geo[si, 3:]
+        if np.any(np.abs(dmin - smin) > tol) or np.any(np.abs((dmin + dsize) - (smin + ssize)) > tol):
+            return False
+        dc, sc = dyn_children(keys[di]), st_children(si)
+        if len(dc) != len(sc):
+            return False
+        md = {octant(dyn["min"][c], dyn["size"][c], dmin, dsize): c for c in dc}
+        ms = {octant(geo[c, :3], geo[c, 3:], smin, ssize): c for c in sc}
+        if md.keys() != ms.keys():
+            return False
+        return all(rec(md[o], ms[o]) for o in md)
+
+    return m == 0 or rec(idx[1], 0)

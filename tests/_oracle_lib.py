@@ -77,6 +77,8 @@ class OracleLib:
             lib.oro_static_load.argtypes = [_vp, _vp, _u64, _int]
             lib.oro_static_equal.restype = _int
             lib.oro_static_equal.argtypes = [_vp]
+            lib.oro_dynamic_equals_static.restype = _int
+            lib.oro_dynamic_equals_static.argtypes = [_vp]
         if hasattr(lib, "oro_collide_self_par"):
             lib.oro_collide_self_par.restype = _vp
             lib.oro_collide_self_par.argtypes = [_vp, _dbl]

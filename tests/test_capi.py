@@ -52,9 +52,18 @@ def test_no_gpu_fails_loudly():
     rc = lib.otg_tree_create(h, pts.ctypes.data_as(ctypes.c_void_p), 4, 3, None, 16, otg.MEM_HOST, None)
     assert rc == 7  # OTG_ERR_NO_DEVICE
     assert b"no CUDA device" in lib.otg_last_error()
+    # the export, archive and resume calls fail loudly too (no CPU path behind them)
+    lay = otg.StaticLayout()
+    assert lib.otg_tree_export_static(h, ctypes.byref(lay), None) == 7
+    size = ctypes.c_uint64()
+    assert lib.otg_tree_save_static(h, 1, None, 0, ctypes.byref(size), None) == 7
+    blob = np.zeros(16, np.uint8)
+    assert lib.otg_tree_load_static(h, blob.ctypes.data_as(ctypes.c_void_p), 16, None, None) == 7
     lib.otg_tree_free(h)
     with pytest.raises(otg.OtgError):
         otg.Tree("points").create(pts)
+    with pytest.raises(otg.OtgError):
+        otg.Tree("regular_boxes").create(np.zeros((4, 6)))
 
 
 def test_invalid_arguments_rejected():
@@ -62,3 +71,7 @@ def test_invalid_arguments_rejected():
     h = ctypes.c_void_p()
     assert lib.otg_tree_new(ctypes.byref(h), 5, otg.KIND_POINTS) == 1
     assert lib.otg_tree_new(ctypes.byref(h), otg.SCALAR_F64, 9) == 1
+    assert lib.otg_tree_new(ctypes.byref(h), otg.SCALAR_F64, otg.KIND_BOXES_REGULAR) == 0
+    lib.otg_tree_free(h)
+    with pytest.raises(ValueError):
+        otg.Tree("cones")

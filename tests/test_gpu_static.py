@@ -18,6 +18,7 @@ from _compare import (
     space_of,
     static_archive_bytes,
     static_from_golden,
+    tree_is_equal_to_static,
 )
 from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, oracle
 
@@ -233,3 +234,38 @@ def test_archive_of_a_tree_built_from_device_memory():
     dev.fill_(0.0)  # the archive must not read the caller's array
     torch.cuda.synchronize()
     assert td.save_static(True) == th.save_static(True)
+
+
+@pytest.mark.parametrize("kind", [KIND_LOOSE_BOXES, KIND_BOXES])
+def test_dynamic_vs_static_known_answer(kind):
+    """DynamicVsStaticTest (tests/unittests/general.tests.cpp:5313-5397) on the GPU trees: the GPU
+    tree and its static export of the five boxes have the same node count and are IsEqualTo each
+    other (tests/_compare.py restates IsEqualTo); the export of the modified boxes is not."""
+    boxes = np.array(
+        [
+            [1.0, 1.0, 1.0, 2.0, 2.0, 2.0],
+            [1.1, 1.1, 1.1, 2.1, 2.1, 2.1],
+            [4.5, 4.5, 4.5, 5.5, 5.5, 5.5],
+            [8.0, 8.0, 8.0, 9.0, 9.0, 9.0],
+            [8.1, 8.1, 8.1, 9.1, 9.1, 9.1],
+        ]
+    )
+    domain = np.array([0.0, 0, 0, 10, 10, 10])
+    t = _gpu_tree(boxes, kind, 10, domain, 2)
+    st = t.export_static()
+    tol = float(np.finfo(np.float64).eps * 100)
+    assert len(st["depth"]) == t.node_count
+    assert tree_is_equal_to_static(t.nodes(), st, tol)
+    modified = boxes.copy()
+    modified[0, 0] -= 1.5
+    assert not tree_is_equal_to_static(t.nodes(), _gpu_tree(modified, kind, 10, domain, 2).export_static(), tol)
+
+
+@pytest.mark.parametrize("case", ["points", "clustered_estimated_depth", "boxes", "regular_boxes", "duplicate_boxes"])
+def test_is_equal_to_matches_oracle(case):
+    """IsEqualTo between the GPU tree and its static export answers as it does for the oracle's."""
+    ent, kind, depth, box, me = _cases()[case]
+    tol = float(np.finfo(ent.dtype).eps * 100)
+    t = _gpu_tree(ent, kind, depth, box, me)
+    o = oracle().create(ent, kind, depth, box, me)
+    assert tree_is_equal_to_static(t.nodes(), t.export_static(), tol) == tree_is_equal_to_static(o.nodes(), o.static_layout(), tol)

@@ -6,8 +6,10 @@ tests/unittests/general.tests.cpp:182-204 (3-D Morton codes), example.tests.cpp:
 z in [0, 1], which leaves each predicate's answer unchanged (all boxes overlap strictly in z).
 """
 import numpy as np
+import pytest
 
-from _oracle_lib import KIND_LOOSE_BOXES, KIND_POINTS, oracle
+from _compare import tree_is_equal_to_static
+from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, oracle
 
 
 def _morton(x, y, z):
@@ -63,3 +65,36 @@ def test_example2_boxes_extruded():
     assert sorted(t.range_search(rng, 0)[1].tolist()) == [1, 2, 4]
     assert sorted(t.range_search(rng, 1)[1].tolist()) == [1, 2, 3, 4]
     assert sorted(t.pick_search(np.array([[2.5, 2.5, 0.5]]))[1].tolist()) == [2, 4]
+
+
+def _dynamic_vs_static_boxes():
+    """The entities of DynamicVsStaticTest (tests/unittests/general.tests.cpp:5313-5377): five boxes
+    in the domain [0, 10]^3, max depth 10, max 2 elements per node; the modified set moves the first
+    box's min x by -1.5."""
+    boxes = np.array(
+        [
+            [1.0, 1.0, 1.0, 2.0, 2.0, 2.0],
+            [1.1, 1.1, 1.1, 2.1, 2.1, 2.1],
+            [4.5, 4.5, 4.5, 5.5, 5.5, 5.5],
+            [8.0, 8.0, 8.0, 9.0, 9.0, 9.0],
+            [8.1, 8.1, 8.1, 9.1, 9.1, 9.1],
+        ]
+    )
+    modified = boxes.copy()
+    modified[0, 0] -= 1.5
+    return boxes, modified, np.array([0.0, 0, 0, 10, 10, 10])
+
+
+@pytest.mark.parametrize("kind", [KIND_LOOSE_BOXES, KIND_BOXES])
+def test_dynamic_vs_static_structure(kind):
+    """ComparisonTest_MBR_Loose / _NotLoose (general.tests.cpp:5379-5397): the dynamic and the static
+    tree of the five boxes have the same node count and are IsEqualTo each other; the static tree of
+    the modified boxes is not equal to the dynamic one."""
+    boxes, modified, domain = _dynamic_vs_static_boxes()
+    dyn = oracle().create(boxes, kind, 10, domain, 2)
+    st = dyn.static_layout()
+    assert len(st["depth"]) == dyn.node_count
+    tol = float(np.finfo(np.float64).eps * 100)
+    assert tree_is_equal_to_static(dyn.nodes(), st, tol)
+    st_mod = oracle().create(modified, kind, 10, domain, 2).static_layout()
+    assert not tree_is_equal_to_static(dyn.nodes(), st_mod, tol)

@@ -4,7 +4,7 @@ the committed golden fixtures carry the pin."""
 import numpy as np
 import pytest
 
-from _compare import assert_static_equal, space_of, static_archive_bytes
+from _compare import assert_static_equal, space_of, static_archive_bytes, tree_is_equal_to_static
 from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, oracle, reference
 
 pytestmark = pytest.mark.skipif(reference() is None, reason="reference harness not built here")
@@ -208,3 +208,16 @@ def test_reference_loads_oracle_archive(case):
     assert_static_equal(arrays, lay, case, exact_storage=True)
     # a cut archive does not load
     assert reference().create(ent, kind, depth, box, max_elem).static_load(data[:-1]) is None
+
+
+@pytest.mark.parametrize("case", list(_static_cases()))
+def test_is_equal_to_restatement(case):
+    """tests/_compare.py: tree_is_equal_to_static answers as the reference's own IsEqualTo between
+    its dynamic tree and its static tree of the same entities (equal where no node passes its
+    entities through, unequal where the static tree contracts such nodes)."""
+    ent, kind, depth, box, max_elem = _static_cases()[case]
+    r = reference().create(ent, kind, depth, box, max_elem)
+    want = r.lib.oro_dynamic_equals_static(r.h)
+    assert want in (0, 1)
+    tol = float(np.finfo(ent.dtype).eps * 100)
+    assert tree_is_equal_to_static(r.nodes(), r.static_layout(), tol) == bool(want)
