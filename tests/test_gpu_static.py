@@ -269,3 +269,42 @@ def test_is_equal_to_matches_oracle(case):
     t = _gpu_tree(ent, kind, depth, box, me)
     o = oracle().create(ent, kind, depth, box, me)
     assert tree_is_equal_to_static(t.nodes(), t.export_static(), tol) == tree_is_equal_to_static(o.nodes(), o.static_layout(), tol)
+
+
+def _fuzz_case(seed):
+    # the random small trees of tests/test_oracle_vs_reference.py: test_static_fuzz (same seeds)
+    rng = np.random.default_rng(1000 + seed)
+    kind = int(rng.integers(0, 3))
+    dtype = np.float64 if rng.random() < 0.6 else np.float32
+    n = int(rng.integers(1, 3000))
+    depth = int(rng.integers(1, 13)) if rng.random() < 0.8 else 0
+    max_elem = int(rng.integers(1, 33))
+    scale = 10.0 ** rng.uniform(-2, 3)
+    style = rng.integers(0, 3)
+    if style == 0:
+        c = rng.random((n, 3))
+    elif style == 1:
+        c = np.clip(rng.normal(0.5, 0.02, (n, 3)), 0, 1)
+    else:
+        c = np.repeat(rng.random((max(1, n // 20), 3)), 20, 0)[:n]
+    c = c * scale
+    box = None
+    if kind == KIND_POINTS:
+        ent = c
+    else:
+        h = rng.random((len(c), 3)) * scale * 0.02 + scale * 1e-4
+        ent = np.concatenate([c - h, c + h], 1)
+        if rng.random() < 0.3:
+            box = np.array([-0.1, -0.1, -0.1, 1.1, 1.1, 1.1]) * scale
+    return ent.astype(dtype), kind, depth, box, max_elem
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_static_fuzz(seed):
+    """Random small trees: the GPU's static layout equals the oracle's (entity order included) and its
+    archive equals the writer's bytes."""
+    ent, kind, depth, box, max_elem = _fuzz_case(seed)
+    t = _gpu_tree(ent, kind, depth, box, max_elem)
+    lay = t.export_static()
+    assert_static_equal(lay, oracle().create(ent, kind, depth, box, max_elem).static_layout(), f"fuzz {seed}", exact_storage=True)
+    assert t.save_static(True) == _writer_bytes(t, lay, ent, kind, box, max_elem, True)

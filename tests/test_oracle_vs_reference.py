@@ -221,3 +221,50 @@ def test_is_equal_to_restatement(case):
     assert want in (0, 1)
     tol = float(np.finfo(ent.dtype).eps * 100)
     assert tree_is_equal_to_static(r.nodes(), r.static_layout(), tol) == bool(want)
+
+
+def _fuzz_case(seed):
+    rng = np.random.default_rng(1000 + seed)
+    kind = int(rng.integers(0, 3))
+    dtype = np.float64 if rng.random() < 0.6 else np.float32
+    n = int(rng.integers(1, 3000))
+    depth = int(rng.integers(1, 13)) if rng.random() < 0.8 else 0
+    max_elem = int(rng.integers(1, 33))
+    scale = 10.0 ** rng.uniform(-2, 3)
+    style = rng.integers(0, 3)
+    if style == 0:
+        c = rng.random((n, 3))
+    elif style == 1:
+        c = np.clip(rng.normal(0.5, 0.02, (n, 3)), 0, 1)
+    else:
+        c = np.repeat(rng.random((max(1, n // 20), 3)), 20, 0)[:n]
+    c = c * scale
+    box = None
+    if kind == KIND_POINTS:
+        ent = c
+    else:
+        h = rng.random((len(c), 3)) * scale * 0.02 + scale * 1e-4  # every box has extent
+        ent = np.concatenate([c - h, c + h], 1)
+        if rng.random() < 0.3:
+            box = np.array([-0.1, -0.1, -0.1, 1.1, 1.1, 1.1]) * scale
+    return ent.astype(dtype), kind, depth, box, max_elem
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_static_fuzz(seed):
+    """Random small trees (kind, scalar, depth, max elements, distribution, given box): the oracle's
+    static layout, the archive writer and the IsEqualTo restatement against the reference."""
+    ent, kind, depth, box, max_elem = _fuzz_case(seed)
+    r = reference().create(ent, kind, depth, box, max_elem)
+    o = oracle().create(ent, kind, depth, box, max_elem)
+    ref = r.static_layout()
+    got = o.static_layout()
+    assert (ref is None) == (got is None)
+    if ref is None:
+        return
+    assert_static_equal(got, ref, f"fuzz {seed}")
+    is_box = kind != KIND_POINTS
+    mn, size = space_of(ent, is_box, box)
+    assert static_archive_bytes(ref, is_box, ent.dtype, len(ent), r.max_depth, max_elem, mn, size, ent) == r.static_archive(True)
+    tol = float(np.finfo(ent.dtype).eps * 100)
+    assert tree_is_equal_to_static(r.nodes(), ref, tol) == bool(r.lib.oro_dynamic_equals_static(r.h))
