@@ -18,6 +18,7 @@
 #include "otg_internal.h"
 
 #include <cstring>
+#include <limits>
 
 static_assert(__BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__, "the archive is little-endian and written as the host stores scalars");
 
@@ -161,11 +162,34 @@ int gather_static(TreeState& t, bool managed, StaticHost<T>& h, cudaStream_t st)
                 { h.storage.data(), L.entity_storage, sizeof(u32) * h.storage.size() },
                 { h.geometry.data(), L.geometry, sizeof(T) * h.geometry.size() },
                 { sorted.data(), t.sortedGeom.p, sizeof(T) * sorted.size() },
-                { &h.sp, t.space.p, t.space.p ? sizeof(Space<T>) : 0 } };
+                { &h.sp, t.space.p, (n && t.space.p) ? sizeof(Space<T>) : 0 } };
   for (const Part& p : parts)
     if (p.bytes)
       if (cudaError_t e = cudaMemcpy(p.dst, p.src, p.bytes, cudaMemcpyDeviceToHost))
         return cuda_status(e, "copying the tree for its archive");
+  if (n == 0)
+  {
+    // a build of no entities computes no space: Create still runs InitBase on the given box, or on
+    // the bounding box of nothing (inverted: min = +max, max = -max, so the size overflows)
+    T box[6];
+    if (t.boxGiven && t.boxDev.p)
+    {
+      if (cudaError_t e = cudaMemcpy(box, t.boxDev.p, sizeof(box), cudaMemcpyDeviceToHost))
+        return cuda_status(e, "copying the space box");
+    }
+    else
+      for (int d = 0; d < 3; ++d)
+      {
+        box[d] = std::numeric_limits<T>::max();
+        box[3 + d] = -std::numeric_limits<T>::max();
+      }
+    for (int d = 0; d < 3; ++d)
+    {
+      h.sp.min[d] = box[d];
+      h.sp.max[d] = box[3 + d];
+      h.sp.size[d] = T(box[3 + d] - box[d]);
+    }
+  }
   if (managed)
   {
     h.entities.resize(n * W);

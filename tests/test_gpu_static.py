@@ -308,3 +308,13 @@ def test_static_fuzz(seed):
     lay = t.export_static()
     assert_static_equal(lay, oracle().create(ent, kind, depth, box, max_elem).static_layout(), f"fuzz {seed}", exact_storage=True)
     assert t.save_static(True) == _writer_bytes(t, lay, ent, kind, box, max_elem, True)
+
+
+@pytest.mark.parametrize("kind,box", [(KIND_POINTS, None), (KIND_POINTS, [0.0, 0, 0, 4, 5, 6]), (KIND_LOOSE_BOXES, [1.0, 1, 1, 9, 9, 9])])
+def test_archive_of_an_empty_tree(kind, box):
+    """A Create of no entities still writes the base fields of its space (the given box, or the
+    inverted bounding box of nothing) and empty arrays, as the reference's archive holds them."""
+    ent = np.zeros((0, 3 if kind == KIND_POINTS else 6))
+    b = None if box is None else np.array(box)
+    t = _gpu_tree(ent, kind, 4, b, 16)
+    assert t.save_static(True) == _writer_bytes(t, t.export_static(), ent, kind, b, 16, True)
