@@ -29,6 +29,10 @@ N_POINTS = 16_000_000
 MAX_DEPTH = 10
 MAX_ELEM = 20
 METRIC = "M entities/s build (OctreePoint Create, 16M FP64 points, depth 10, max 20 per node)"
+# single-thread Create time of the oracle port over that of the reference itself on the same 1M
+# and 2M shell points (x86 container, both built with g++ -O2): the port is this much slower, so a
+# CPU figure of kind "port" understates the reference's speed by about this factor
+PORT_VS_REFERENCE = {"1M": 1.39, "2M": 1.27}
 # mean dram__bytes_read.sum + dram__bytes_write.sum of the four radix passes of this build (one ncu capture)
 SORT_PASS_DRAM_BYTES = 191.7e6
 
@@ -53,6 +57,19 @@ def shell_points(n, seed):
     r = rng.normal(0.4, 0.005, (n_shell, 1))
     pts[n - n_shell :] = 0.5 + d * r
     return pts[rng.permutation(n)]
+
+
+def c1_workload(n_ranges=10_000, n_knn=10_000):
+    """The 1M-point query workload: 1,000,000 FP64 points uniform in [0,100)^3 (seed 101); range
+    boxes with centres uniform in the domain (seed 102) and edge lengths uniform in [0.5, 5] per
+    axis drawn from their own stream (seed 105), so size and position are independent; kNN query
+    points uniform in the domain (seed 103). Returns (points, ranges (n, 6), knn points (n, 3))."""
+    pts = np.random.default_rng(101).random((1_000_000, 3)) * 100
+    c = np.random.default_rng(102).random((10_000, 3)) * 100
+    e = np.random.default_rng(105).uniform(0.5, 5, (10_000, 3))
+    ranges = np.concatenate([c - e / 2, c + e / 2], 1)[:n_ranges]
+    q = (np.random.default_rng(103).random((10_000, 3)) * 100)[:n_knn]
+    return pts, ranges, q
 
 
 class ClockSampler:
@@ -242,22 +259,35 @@ def cpu_build_rate(pts, reps):
     return len(pts) * reps / secs / 1e6, kind, threads
 
 
+def headline_config(nodes, world):
+    """The `config` object of the headline line, the same for the GPU and the reference arm."""
+    return {
+        "workload": "OctreePoint Create, 16M FP64 points (70% uniform, 30% noisy shell r=0.4), bounding box of the data",
+        "max_depth": MAX_DEPTH,
+        "max_elements": MAX_ELEM,
+        "nodes": nodes,
+        "l2": "inputs (384 MB of points) larger than L2 (129 MB); no flush",
+        "parallelism": f"replicas x{world}",
+    }
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
         return
+    # the whole 16M-point workload every step, as the GPU arm builds it
     pts = shell_points(N_POINTS, 301)
     lib, kind = oracle_lib()
     threads = cpu_threads(lib)
-    sample_n = 2_000_000
-    sample = np.ascontiguousarray(pts[:sample_n])
-    for _ in range(max(0, args.warmup)):
-        time_cpu_create(lib, sample, 1, threads)
+    # the first warm-up Create also gives the node count of the workload's tree
+    nodes = int(lib.create(pts, 0, MAX_DEPTH, None, MAX_ELEM, threads=threads).node_count)
+    for _ in range(max(0, args.warmup - 1)):
+        time_cpu_create(lib, pts, 1, threads)
     times = []
     for _ in range(args.steps):
-        times.append(time_cpu_create(lib, sample, 1, threads))
+        times.append(time_cpu_create(lib, pts, 1, threads))
     ms = statistics.mean(times) * 1e3
-    value = sample_n / (ms / 1e3) / 1e6
+    value = N_POINTS / (ms / 1e3) / 1e6
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -272,14 +302,15 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": "OctreePoint Create of 2M of the 16M shell/uniform FP64 points per step", "max_depth": MAX_DEPTH, "max_elements": MAX_ELEM},
+        "config": headline_config(nodes, world),
         "cpu_baseline": {
             "value": value,
             "unit": "M entities/s",
             "cores": threads,
             "kind": kind,
-            "sample": f"{sample_n} points per step (bounded sample of the 16M workload), Create with the location transform and sort "
+            "sample": f"all {N_POINTS} points every step (the GPU arm's workload), Create with the location transform and sort "
             f"on {threads} threads, BuildSubtree sequential as in the reference",
+            "port_vs_reference_time": PORT_VS_REFERENCE if kind == "port" else None,
         },
         "e2e": {"value": value, "unit": "M entities/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -397,14 +428,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {
-            "workload": "OctreePoint Create, 16M FP64 points (70% uniform, 30% noisy shell r=0.4), bounding box of the data",
-            "max_depth": MAX_DEPTH,
-            "max_elements": MAX_ELEM,
-            "nodes": int(info.node_count),
-            "l2": "inputs (384 MB of points) larger than L2 (129 MB); no flush",
-            "parallelism": f"replicas x{world}",
-        },
+        "config": headline_config(int(info.node_count), world),
         "phases_ms": mean_phase,
         "roofline": roofline,
         "e2e": {"value": e2e_value, "unit": "M entities/s", "h2d_bytes_per_step": N_POINTS * 24, "d2h_bytes_per_step": 4 + 32 * 4},
@@ -417,20 +441,21 @@ def run_gpu(args):
     # depth 0..D-1
     line["gpu_launches"] = args.steps * (6 + passes + 1 + 1 + 1 + MAX_DEPTH)
     if rank == 0 and not args.no_cpu_baseline:
-        sample = pts_h[:1_000_000]
-        rate, kind, threads = cpu_build_rate(sample, 3)
+        rate, kind, threads = cpu_build_rate(pts_h, 2)
         line["cpu_baseline"] = {
             "value": rate,
             "unit": "M entities/s",
             "cores": threads,
             "kind": kind,
-            "sample": f"1M of the 16M points, 3 Creates, location transform and sort on {threads} threads",
+            "sample": f"all 16M points, 2 Creates, location transform and sort on {threads} threads",
+            "port_vs_reference_time": PORT_VS_REFERENCE if kind == "port" else None,
         }
     if not args.no_queries:
         line["static_layout"] = run_static_export(tree, pts_h)
+        cpu_results = None
         if rank == 0 and not args.no_cpu_baseline:
-            line["cpu_configs"] = run_cpu_configs()
-        line["queries"] = run_queries(tree, pts_d, stream)
+            line["cpu_configs"], cpu_results = run_cpu_configs()
+        line["queries"] = run_queries(tree, pts_d, stream, cpu_results)
         line["many_trees"] = run_many_trees()
         line["two_trees"] = run_two_trees()
         line["autotune"] = otg.autotune_entries()
@@ -509,27 +534,30 @@ def run_cpu_configs():
     build_threads = threads if hasattr(lib.lib, "oro_create_threads") else 1
     pool = ThreadPoolExecutor(threads)
 
-    def par_queries(fn, arrays):
-        # fn(slice arrays...) for `threads` contiguous slices, concurrently; returns seconds
+    results = {}
+
+    def par_queries(fn, arrays, keep=None):
+        # fn(slice arrays...) for `threads` contiguous slices, concurrently; returns seconds. keep:
+        # the name under which the CSR result of all slices, in query order, is kept for the
+        # comparison with the GPU lines
         n = len(arrays[0])
         cuts = [n * i // threads for i in range(threads + 1)]
         t0 = time.perf_counter()
-        list(pool.map(lambda i: fn(*[a[cuts[i] : cuts[i + 1]] for a in arrays]), range(threads)))
-        return time.perf_counter() - t0
+        parts = list(pool.map(lambda i: fn(*[a[cuts[i] : cuts[i + 1]] for a in arrays]), range(threads)))
+        s = time.perf_counter() - t0
+        if keep:
+            results[keep] = concat_csr(parts)
+        return s
 
     out = {"kind": kind, "query_threads": threads, "build_threads": build_threads}
     # C1: 1M uniform points (depth 10, max 20); 2000 of the 10k range boxes and 2000 kNN(k=8) queries
-    p1 = np.random.default_rng(101).random((1_000_000, 3)) * 100
+    p1, ranges, q = c1_workload(2000, 2000)
     t0 = time.perf_counter()
     t1 = lib.create(p1, 0, 10, None, 20, threads=build_threads)
     out["c1_create_1M_s"] = time.perf_counter() - t0
-    c = np.random.default_rng(102).random((10_000, 3)) * 100
-    e = np.random.default_rng(102).uniform(0.5, 5, (10_000, 3))
-    ranges = np.concatenate([c - e / 2, c + e / 2], 1)[:2000]
-    s = par_queries(lambda r: t1.range_search(r), [ranges])
+    s = par_queries(lambda r: t1.range_search(r), [ranges], keep="c1_range")
     out["c1_range_Mq_per_s"] = 2000 / s / 1e6
-    q = np.random.default_rng(103).random((2000, 3)) * 100
-    s = par_queries(lambda x: t1.knn(x, 8), [q])
+    s = par_queries(lambda x: t1.knn(x, 8), [q], keep="c1_knn8")
     out["c1_knn8_Mq_per_s"] = 2000 / s / 1e6
     out["c1_sample"] = "2000 of the 10k range boxes, 2000 kNN(k=8) queries"
     del t1
@@ -540,7 +568,7 @@ def run_cpu_configs():
     out["c3_create_16M_s"] = time.perf_counter() - t0
     qk = shell_points(1_000_000, 302)[:2000]
     ks = np.random.default_rng(303).integers(1, 65, 1_000_000).astype(np.uint32)[:2000]
-    s = par_queries(lambda x, k: t3.knn(x, k), [qk, ks])
+    s = par_queries(lambda x, k: t3.knn(x, k), [qk, ks], keep="c3_knn_uneven")
     out["c3_knn_uneven_Mq_per_s"] = 2000 / s / 1e6
     out["c3_sample"] = "2000 of the 1M queries, k in 1..64"
     del t3, pts
@@ -551,6 +579,7 @@ def run_cpu_configs():
     t0 = time.perf_counter()
     pairs = tb.collide_self()
     s = time.perf_counter() - t0
+    results["c2_collide_self_500k"] = pairs
     out["c2_collide_self_500k_ms"] = s * 1e3
     out["c2_collide_self_500k_Mpairs_per_s"] = len(pairs) / s / 1e6
     out["c2_sample"] = "every 8th of the 4M boxes (500k, one eighth of the density), one thread"
@@ -567,7 +596,45 @@ def run_cpu_configs():
     out["c4_trees_per_s"] = 16 / s
     out["c4_sample"] = "16 trees of the same distribution, one after another"
     pool.shutdown()
-    return out
+    return out, results
+
+
+def concat_csr(parts):
+    """One CSR result (offsets, ids[, distances]) from the results of consecutive query slices."""
+    offs, ids, dists = [np.zeros(1, np.uint64)], [], []
+    base = 0
+    for p in parts:
+        o = np.asarray(p[0], np.uint64)
+        offs.append(o[1:] + np.uint64(base))
+        base += int(o[-1])
+        ids.append(p[1])
+        if len(p) > 2 and p[2] is not None:
+            dists.append(p[2])
+    out = (np.concatenate(offs), np.concatenate(ids) if ids else np.zeros(0, np.uint32))
+    return out + (np.concatenate(dists),) if dists else out
+
+
+def csr_mismatches(a, b):
+    """Queries whose id lists (and distances, where both carry them) differ between two CSR results."""
+    oa, ob = np.asarray(a[0], np.int64), np.asarray(b[0], np.int64)
+    if len(oa) != len(ob):
+        return max(len(oa), len(ob)) - 1
+    dist = len(a) > 2 and len(b) > 2 and a[2] is not None and b[2] is not None
+    bad = 0
+    for qi in range(len(oa) - 1):
+        x, y = slice(oa[qi], oa[qi + 1]), slice(ob[qi], ob[qi + 1])
+        if not np.array_equal(a[1][x], b[1][y]) or (dist and not np.array_equal(a[2][x], b[2][y])):
+            bad += 1
+    return bad
+
+
+def pair_mismatches(a, b):
+    """Pairs in one canonically sorted (i < j) pair list and not in the other."""
+    ka = np.asarray(a, np.uint64).reshape(-1, 2)
+    kb = np.asarray(b, np.uint64).reshape(-1, 2)
+    ka = ka[:, 0] << np.uint64(32) | ka[:, 1]
+    kb = kb[:, 0] << np.uint64(32) | kb[:, 1]
+    return int(len(np.setxor1d(ka, kb)))
 
 
 def time_query(fn, reps=3):
@@ -613,27 +680,31 @@ def mismatched_queries(a, b):
     return bad
 
 
-def run_queries(tree16, pts16_d, stream):
+def run_queries(tree16, pts16_d, stream, cpu=None):
+    """cpu: the CPU results of run_cpu_configs on its samples; each is compared with the GPU's
+    result on the same sample (mismatched_ids_vs_cpu: queries, or pairs, that differ)."""
     import torch
 
     import octree_gb300 as otg
 
     out = {}
     algos = ((otg.ALGO_PLAIN_FP64, "plain_fp64"), (otg.ALGO_FILTERED, "filtered_fp32"))
-    rng = np.random.default_rng(103)
+    rng = np.random.default_rng(104)
     # 1M uniform points in [0,100]^3, 10k range boxes (edges U[0.5,5]), 10k kNN k=8
-    p1 = np.random.default_rng(101).random((1_000_000, 3)) * 100
+    p1, ranges_h, q_h = c1_workload()
     t1 = otg.Tree("points").create(p1, max_depth=10, max_elements=20)
-    c = np.random.default_rng(102).random((10_000, 3)) * 100
-    e = np.random.default_rng(102).uniform(0.5, 5, (10_000, 3))
-    ranges = torch.as_tensor(np.concatenate([c - e / 2, c + e / 2], 1), device="cuda")
-    q = torch.as_tensor(rng.random((10_000, 3)) * 100, device="cuda")
+    ranges = torch.as_tensor(ranges_h, device="cuda")
+    q = torch.as_tensor(q_h, device="cuda")
+    mism = {}
+    if cpu:
+        mism["c1_range_2000"] = csr_mismatches(t1.range_search(ranges_h[:2000])[:2], cpu["c1_range"])
+        mism["c1_knn8_2000"] = csr_mismatches(t1.knn(q_h[:2000], 8), cpu["c1_knn8"])
     s = time_query(lambda: t1.range_search(ranges, algo=otg.ALGO_PLAIN_FP64, raw=True))
     out["range_1M_10k_plain_fp64_Mq_per_s"] = 10_000 / s / 1e6
     s = time_query(lambda: t1.range_search(ranges, raw=True))
     out["range_1M_10k_batched_Mq_per_s"] = 10_000 / s / 1e6
     # 10k PickSearch at points of the tree (each finds its point)
-    picks = torch.as_tensor(p1[np.random.default_rng(104).integers(0, len(p1), 10_000)], device="cuda")
+    picks = torch.as_tensor(p1[rng.integers(0, len(p1), 10_000)], device="cuda")
     for algo, name in ((otg.ALGO_PLAIN_FP64, "plain_fp64"), (otg.ALGO_DEFAULT, "batched")):
         s = time_query(lambda: t1.pick_search(picks, algo=algo, raw=True))
         out[f"pick_1M_10k_{name}_Mq_per_s"] = 10_000 / s / 1e6
@@ -669,6 +740,8 @@ def run_queries(tree16, pts16_d, stream):
     tests, rechecks = tree16.knn(qk, ks, algo=otg.ALGO_FILTERED, raw=True).stats()
     out["knn_uneven_recheck_fraction"] = rechecks / max(tests, 1)
     out["knn_uneven_mismatched_queries_filtered_vs_plain"] = mismatched_queries(res["plain_fp64"], res["filtered_fp32"])
+    if cpu:
+        mism["c3_knn_uneven_2000"] = csr_mismatches(tree16.knn(qk[:2000], ks[:2000]), cpu["c3_knn_uneven"])
     out["knn_uneven_speedup_filtered_vs_plain"] = out["knn_uneven_16M_1Mq_filtered_fp32_Mq_per_s"] / out["knn_uneven_16M_1Mq_plain_fp64_Mq_per_s"]
     # self-collision of 4M clustered FP64 boxes, depth 12, max 32 per node
     boxes = torch.as_tensor(cluster_boxes(4_000_000, 201), device="cuda")
@@ -688,6 +761,11 @@ def run_queries(tree16, pts16_d, stream):
     out["collide_self_4M_pairs"] = int(pairs)
     out["collide_self_4M_pair_lists_equal"] = bool(np.array_equal(pair_lists["plain_fp64"], pair_lists["filtered_fp32"]))
     out["collide_self_4M_speedup_filtered_vs_plain"] = out["collide_self_4M_plain_fp64_ms"] / out["collide_self_4M_filtered_fp32_ms"]
+    if cpu:
+        sub = otg.Tree("boxes").create(np.ascontiguousarray(cluster_boxes(4_000_000, 201)[::8]), max_depth=12, max_elements=32)
+        mism["c2_collide_self_500k_pairs"] = pair_mismatches(sub.collision_self(), cpu["c2_collide_self_500k"])
+        out["mismatched_ids_vs_cpu"] = mism
+        out["mismatched_ids_vs_cpu_samples"] = "the CPU samples of cpu_configs (C1: 2000 ranges, 2000 kNN k=8; C3: 2000 uneven kNN; C2: self-collision of every 8th box), run again on the GPU with the default kernels"
     return out
 
 

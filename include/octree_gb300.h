@@ -266,7 +266,8 @@ int otg_collision_pair(const otg_tree* left, const otg_tree* right, double tol, 
    array's device address (with that device current); make that first call, for instance with
    n_queries = 0, which only does this set-up, before any stream capture begins. All calls on a
    device share the one scratch array: calls that overlap on the GPU (from several host threads
-   or streams) race on it, so the caller must serialise them. */
+   or streams) race on it, so the caller must serialise them. When the call returns an error,
+   counts, ids and distances hold no defined values. */
 int otg_knn_noalloc(const otg_tree* tree, const void* points, uint64_t n_queries, uint32_t k, double max_distance, double tol,
                     uint32_t slot_capacity, uint32_t* counts, uint32_t* ids, double* distances, void* stream);
 

@@ -376,7 +376,9 @@ __global__ void __launch_bounds__(128) query_plain_kernel(TreeView<T> tv, QueryP
 // Pass 1: the k-th smallest distance d_k (points) -> F = U(d_k), the reference's final
 // farthestEntityDistance. Box trees keep the reference's optimistic/pessimistic pair:
 // the pessimistic (minMax) k-th distance sets F, entities qualify by their min distance.
-template<typename T>
+// KMAX: the heap's capacity, a bucket at or above every k of the launch (8, 16, ..., 256), so a
+// query with small k keeps a small heap.
+template<typename T, int KMAX>
 __global__ void __launch_bounds__(128) knn_threshold_kernel(TreeView<T> tv, const T* __restrict__ pts, u32 nq, const u32* __restrict__ kArr, u32 kAll,
                                                             T F0, T tol, T* __restrict__ Fout, u32* err)
 {
@@ -392,16 +394,16 @@ __global__ void __launch_bounds__(128) knn_threshold_kernel(TreeView<T> tv, cons
     Fout[q] = T(0);
     return;
   }
-  if (k > kKnnMaxK)
+  if (k > u32(KMAX))
   {
     atomicOr(err, kErrCapacity);
-    k = kKnnMaxK;
+    k = KMAX;
   }
   T p[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
     p[c] = pts[u64(q) * 3 + c];
-  T heap[kKnnMaxK]; // max-heap of the k smallest (pessimistic) distances
+  T heap[KMAX]; // max-heap of the k smallest (pessimistic) distances
   u32 hs = 0;
   T F = F0;
   u32 stack[kStack];
@@ -419,8 +421,11 @@ __global__ void __launch_bounds__(128) knn_threshold_kernel(TreeView<T> tv, cons
     const uint4 L = tv.link[node];
     if (L.z > tv.n || L.w > tv.n || L.y > L.z)
     {
+      // a broken node record: the call fails; the threshold is still written (0: no entity
+      // qualifies), so the collect pass never reads an unwritten value
       atomicOr(err, kErrStack);
-      return;
+      F = T(0);
+      break;
     }
     for (u32 e = L.y; e < L.z; ++e)
     {
@@ -552,6 +557,43 @@ __global__ void __launch_bounds__(128) knn_collect_kernel(TreeView<T> tv, const 
     for (u32 c = 0; c < cc; ++c)
       stack[sp++] = fc + c;
   }
+}
+
+// The heap bucket of the plain kNN threshold pass for a largest k of kMax.
+static int knn_heap_bucket(u32 kMax)
+{
+  int b = 8;
+  while (b < kKnnMaxK && u32(b) < kMax)
+    b *= 2;
+  return b;
+}
+
+template<typename T>
+static void launch_knn_threshold(int bucket, u32 blocks, cudaStream_t st, TreeView<T> tv, const T* pts, u32 nq, const u32* kArr, u32 kAll, T F0,
+                                 T tol, T* Fout, u32* err)
+{
+  switch (bucket)
+  {
+  case 8: knn_threshold_kernel<T, 8><<<blocks, 128, 0, st>>>(tv, pts, nq, kArr, kAll, F0, tol, Fout, err); break;
+  case 16: knn_threshold_kernel<T, 16><<<blocks, 128, 0, st>>>(tv, pts, nq, kArr, kAll, F0, tol, Fout, err); break;
+  case 32: knn_threshold_kernel<T, 32><<<blocks, 128, 0, st>>>(tv, pts, nq, kArr, kAll, F0, tol, Fout, err); break;
+  case 64: knn_threshold_kernel<T, 64><<<blocks, 128, 0, st>>>(tv, pts, nq, kArr, kAll, F0, tol, Fout, err); break;
+  case 128: knn_threshold_kernel<T, 128><<<blocks, 128, 0, st>>>(tv, pts, nq, kArr, kAll, F0, tol, Fout, err); break;
+  default: knn_threshold_kernel<T, kKnnMaxK><<<blocks, 128, 0, st>>>(tv, pts, nq, kArr, kAll, F0, tol, Fout, err); break;
+  }
+}
+
+// largest value of a device array (0 for n = 0) into *out, which the caller zeroed
+__global__ void max_u32_kernel(const u32* __restrict__ a, u64 n, u32* __restrict__ out)
+{
+  u32 m = 0;
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < n; i += u64(gridDim.x) * blockDim.x)
+    m = max(m, a[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m)
+    atomicMax(out, m);
 }
 
 // ---------------------------------------------------------------- rays (plain)
@@ -1504,11 +1546,24 @@ static int knn_impl(const TreeState& t, const void* pts, u64 nq, const u32* k, u
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
   T F0 = maxDist < 0 ? Lim<T>::max() : upper_tol_host(T(maxDist), tl);
+  // the heap bucket: the largest k of the batch (per-query k is reduced on the device)
+  u32 kMax = kAll;
+  if (dk)
+  {
+    DevBuf m;
+    cudaError_t e;
+    if ((e = m.ensure(sizeof(u32))) || (e = cudaMemsetAsync(m.p, 0, sizeof(u32), st)))
+      return cuda_status(e, "finding the largest k");
+    max_u32_kernel<<<u32(std::min<u64>((nq + 255) / 256, 152 * 8)), 256, 0, st>>>((const u32*)dk, nq, m.as<u32>());
+    if ((e = cudaMemcpyAsync(&kMax, m.p, sizeof(u32), cudaMemcpyDeviceToHost, st)) || (e = cudaStreamSynchronize(st)))
+      return cuda_status(e, "finding the largest k");
+  }
+  const int bucket = knn_heap_bucket(kMax);
   Collected c;
   int rc = collect(
     c, true, nq * 16,
     [&](Appender a, u32* err) {
-      knn_threshold_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), (const u32*)dk, kAll, F0, tl, F.as<T>(), err);
+      launch_knn_threshold<T>(bucket, u32((nq + 127) / 128), st, tv, (const T*)d, u32(nq), (const u32*)dk, kAll, F0, tl, F.as<T>(), err);
       knn_collect_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), F.as<T>(), tl, a, err);
     },
     st);
@@ -1892,7 +1947,7 @@ static int knn_noalloc_impl(const TreeState& t, const void* pts, u64 nq, u32 k, 
   const T tl = tol_of<T>(tol);
   const T F0 = maxDist < 0 ? Lim<T>::max() : upper_tol_host(T(maxDist), tl);
   const u32 blocks = u32((nq + 127) / 128);
-  knn_threshold_kernel<T><<<blocks, 128, 0, st>>>(tv, (const T*)pts, u32(nq), nullptr, k, F0, tl, F, err);
+  launch_knn_threshold<T>(knn_heap_bucket(k), blocks, st, tv, (const T*)pts, u32(nq), nullptr, k, F0, tl, F, err);
   knn_collect_slots_kernel<T><<<blocks, 128, 0, st>>>(tv, (const T*)pts, u32(nq), F, tl, cap, counts, ids, dist, err);
   if ((e = cudaGetLastError()))
     return cuda_status(e, "launching the kNN query");

@@ -483,6 +483,7 @@ public:
   std::unordered_map<u64, Node> nodes;
   std::vector<u64> locationKeys; // per entity, input order
   std::vector<u32> sortedOrder;  // entity ids in sorted-location order (ties by id)
+  std::vector<u64> sortedKeys;   // location keys in sorted order (only while Create emits nodes)
 
   const T* ent(u32 id) const { return &geom[size_t(id) * (isBox ? 6 : 3)]; }
 
@@ -706,30 +707,47 @@ public:
         locationKeys[i] = rasterDouble ? location_key<double>(ent(u32(i)), rsizeD, rastD) : location_key<float>(ent(u32(i)), rsizeF, rastF);
     });
 
-    // :791-796 sort by location (ParExec path). Ties are ordered by id here; the reference's
-    // std::sort leaves them unspecified, so every comparison is made on canonical (sorted) id sets.
-    // With several workers: sorted chunks merged pairwise, each round's merges in parallel.
-    std::vector<u32> order(n);
-    std::iota(order.begin(), order.end(), 0u);
-    auto less = [&](u32 a, u32 b) { return locationKeys[a] < locationKeys[b] || (locationKeys[a] == locationKeys[b] && a < b); };
+    // :791-796 sort by location (ParExec path): contiguous (location, id) records, as the
+    // reference sorts its zip of Location and EntityID. Ties are ordered by id here; the
+    // reference's std::sort leaves them unspecified, so every comparison is made on canonical
+    // (sorted) id sets. With several workers: sorted chunks merged pairwise, each round's merges
+    // in parallel.
+    std::vector<std::pair<u64, u32>> kv(n);
+    parallel_ranges(n, [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i)
+        kv[i] = { locationKeys[i], u32(i) };
+    });
     const size_t chunks = std::min<size_t>(threads, std::max<size_t>(1, n / 4096));
     std::vector<size_t> cut(chunks + 1);
     for (size_t c = 0; c <= chunks; ++c)
       cut[c] = n * c / chunks;
-    run_workers(chunks, [&](size_t c) { std::sort(order.begin() + cut[c], order.begin() + cut[c + 1], less); });
-    std::vector<u32> tmp(chunks > 1 ? n : 0);
+    run_workers(chunks, [&](size_t c) { std::sort(kv.begin() + cut[c], kv.begin() + cut[c + 1]); });
+    std::vector<std::pair<u64, u32>> tmp(chunks > 1 ? n : 0);
     for (size_t width = 1; width < chunks; width *= 2)
     {
       run_workers((chunks + 2 * width - 1) / (2 * width), [&](size_t m) {
         const size_t lo = cut[2 * width * m], mid = cut[std::min(chunks, 2 * width * m + width)], hi = cut[std::min(chunks, 2 * width * (m + 1))];
-        std::merge(order.begin() + lo, order.begin() + mid, order.begin() + mid, order.begin() + hi, tmp.begin() + lo, less);
-        std::copy(tmp.begin() + lo, tmp.begin() + hi, order.begin() + lo);
+        std::merge(kv.begin() + lo, kv.begin() + mid, kv.begin() + mid, kv.begin() + hi, tmp.begin() + lo);
+        std::copy(tmp.begin() + lo, tmp.begin() + hi, kv.begin() + lo);
       });
     }
+    std::vector<u32> order(n);
+    sortedKeys.resize(n);
+    parallel_ranges(n, [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i)
+      {
+        sortedKeys[i] = kv[i].first;
+        order[i] = kv[i].second;
+      }
+    });
+    std::vector<std::pair<u64, u32>>().swap(kv);
 
-    // :717-747 BuildSubtree (depth-first emission)
-    build_subtree(root, 0, order, 0, n);
+    // :800 the node map is reserved for EstimateNodeNumber nodes; :717-747 BuildSubtree
+    // (depth-first emission) over the sorted records
+    nodes.reserve(estimate_node_number(n, D, maxElem));
+    build_subtree(std::move(root), 0, order, 0, n);
     sortedOrder = std::move(order);
+    std::vector<u64>().swap(sortedKeys);
 
     // :803-806 node geometry
     if (isBox)
@@ -767,6 +785,24 @@ public:
     run_workers(parts, [&](size_t p) { f(n * p / parts, n * (p + 1) / parts); });
   }
 
+  // detail/utils.h:587-611 EstimateNodeNumber (3-D): the node map's reserved size in Create
+  static size_t estimate_node_number(size_t elementNo, u32 maxDepthID, size_t maxElementNo)
+  {
+    if (elementNo < 10)
+      return 10;
+    if ((maxDepthID + 1) * 3 < 64)
+    {
+      const size_t nMaxChild = size_t(1) << (maxDepthID * 3);
+      if (elementNo / nMaxChild > maxElementNo / 2)
+        return nMaxChild;
+    }
+    const float nElementInNodeAvg = float(elementNo) / float(maxElementNo);
+    const u32 nDepthEstimated = std::min(maxDepthID, u32(std::ceil((std::log2(nElementInNodeAvg) + 1.0) / 3.0f)));
+    if (nDepthEstimated * 3 < 64)
+      return size_t(1.05 * double(u64(1) << (nDepthEstimated * 3)));
+    return size_t(1.5 * nElementInNodeAvg);
+  }
+
   // ot_dynamic_hash_core.h:647-747 (ProcessNode / CreateProcessingData / BuildSubtree)
   void build_subtree(Node node, u32 depth, const std::vector<u32>& order, size_t b, size_t e)
   {
@@ -780,7 +816,7 @@ public:
       {
         // :660-666 partition_point on "entity depth == node depth" (stuck entities come first)
         stuckEnd = b;
-        while (stuckEnd < e && key_loc_depth(locationKeys[order[stuckEnd]]) == depth)
+        while (stuckEnd < e && key_loc_depth(sortedKeys[stuckEnd]) == depth)
           ++stuckEnd;
       }
       for (size_t i = b; i < stuckEnd; ++i)
@@ -790,12 +826,12 @@ public:
       {
         // :695-714 child id from bits [3(D-d-1), 3(D-d-1)+3)
         u32 examined = D - (depth + 1);
-        u64 loc = key_loc(locationKeys[order[it]]);
+        u64 loc = key_loc(sortedKeys[it]);
         u64 mask = u64(7) << (examined * 3);
         u64 flag = loc & mask;
         u64 childID = flag >> (examined * 3);
         size_t end = it;
-        while (end < e && (key_loc(locationKeys[order[end]]) & mask) == flag)
+        while (end < e && (key_loc(sortedKeys[end]) & mask) == flag)
           ++end;
         Node child;
         child.key = (node.key << 3) | childID;
@@ -808,7 +844,7 @@ public:
         // in nodes that are not reachable from the root. The restatement does the same.
         if (std::find(node.children.begin(), node.children.end(), child.key) == node.children.end())
           node.children.push_back(child.key);
-        build_subtree(child, depth + 1, order, it, end);
+        build_subtree(std::move(child), depth + 1, order, it, end);
         it = end;
       }
     }

@@ -58,6 +58,26 @@ def assert_nodes_equal(gpu, ref, what):
         assert not (set(re.tolist()) & reached), f"{what}: orphan node shares entities"
 
 
+def assert_nodes_equal_exact(gpu, ref, what):
+    """assert_nodes_equal for trees of millions of nodes, vectorised: the GPU's reachable nodes
+    (any order) must be exactly the reference's nodes (sorted by key, entity ids ascending per
+    node), with the same min points, sizes and entity sets. Trees with orphan nodes (locations
+    outside the grid) need assert_nodes_equal."""
+    order = np.argsort(gpu["keys"], kind="stable")
+    assert np.array_equal(gpu["keys"][order], ref["keys"]), f"{what}: node keys differ ({len(order)} vs {len(ref['keys'])} nodes)"
+    assert np.array_equal(gpu["min"][order], ref["min"]), f"{what}: node min points differ"
+    assert np.array_equal(gpu["size"][order], ref["size"]), f"{what}: node sizes differ"
+    geoff = gpu["eoff"].astype(np.int64)
+    cnt = np.diff(geoff)[order]
+    assert np.array_equal(cnt, np.diff(ref["eoff"].astype(np.int64))), f"{what}: entity counts per node differ"
+    # the GPU's entity ids node by node in key order, then sorted inside each node
+    first = np.repeat(geoff[:-1][order] - np.concatenate([[0], np.cumsum(cnt)[:-1]]), cnt)
+    ge = gpu["eids"][first + np.arange(int(cnt.sum()))]
+    seg = np.repeat(np.arange(len(cnt)), cnt)
+    ge = ge[np.lexsort((ge, seg))]
+    assert np.array_equal(ge, ref["eids"]), f"{what}: entity sets of some nodes differ"
+
+
 def node_dict(prefix, g):
     return {k: g[prefix + k] for k in ("keys", "min", "size", "eoff", "eids")}
 

@@ -151,6 +151,9 @@ def _static_cases():
         "max_elem_1": (pts[:900], KIND_POINTS, 8, None, 1),
         "single_leaf": (pts[:10], KIND_POINTS, 6, None, 16),
         "empty": (np.zeros((0, 3)), KIND_POINTS, 4, None, 16),
+        # the empty trees of the GPU archive test: a given box instead of the inverted one
+        "empty_points_box": (np.zeros((0, 3)), KIND_POINTS, 4, np.array([0.0, 0, 0, 4, 5, 6]), 16),
+        "empty_loose_boxes_box": (np.zeros((0, 6)), KIND_LOOSE_BOXES, 4, np.array([1.0, 1, 1, 9, 9, 9]), 16),
         "loose_boxes": (boxes, KIND_LOOSE_BOXES, 7, None, 4),
         "loose_boxes_f32": (boxes.astype(np.float32), KIND_LOOSE_BOXES, 7, None, 4),
         "loose_boxes_outside_space": (outside, KIND_LOOSE_BOXES, 6, space, 3),

@@ -101,3 +101,24 @@ def test_noalloc_knn_limits():
     # slot_capacity 0: counts only
     rc = lib.otg_knn_noalloc(tree.h, _ptr(one), 1, 4, -1.0, -1.0, 0, _ptr(counts), None, None, None)
     assert rc == 0 and int(counts[0]) == int(np.diff(tree.knn(one.cpu().numpy(), 4)[0].astype(np.int64))[0])
+
+
+def test_noalloc_knn_empty_tree_and_k0():
+    """An empty tree answers every query with count 0 (its own branch: no kernel runs), and k = 0
+    gives empty lists on a non-empty tree; both over counts pre-filled with 0xDEAD, twice, and
+    equal to otg_knn."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(44)
+    q = rng.random((500, 3)) * 10
+    qd = torch.as_tensor(q, device="cuda")
+    empty = otg.Tree("points").create(np.zeros((0, 3)))
+    empty.sync()
+    full = otg.Tree("points").create(rng.random((50_000, 3)) * 10, max_depth=6, max_elements=16)
+    full.sync()
+    for tree, k, what in ((empty, 8, "empty tree"), (full, 0, "k = 0")):
+        ref = tree.knn(q, k)
+        assert int(ref[0][-1]) == 0
+        for call in range(2):
+            counts, ids, dist = _noalloc(tree, qd, k, 4)
+            assert np.array_equal(counts, np.zeros(len(q), np.uint32)), f"{what} call {call}: counts not cleared"
+            _expect_slots(ref, counts, ids, dist, 4, f"{what} call {call}")
