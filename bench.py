@@ -455,7 +455,7 @@ def run_gpu(args):
         cpu_results = None
         if rank == 0 and not args.no_cpu_baseline:
             line["cpu_configs"], cpu_results = run_cpu_configs()
-        line["queries"] = run_queries(tree, pts_d, stream, cpu_results)
+        line["queries"] = run_queries(tree, pts_d, stream, cpu_results, pts_h)
         line["many_trees"] = run_many_trees()
         line["two_trees"] = run_two_trees()
         line["autotune"] = otg.autotune_entries()
@@ -680,9 +680,70 @@ def mismatched_queries(a, b):
     return bad
 
 
-def run_queries(tree16, pts16_d, stream, cpu=None):
+# bytes the query kernels read per unit of the reference's traversal work (FP64 point trees): a node
+# record is its link (uint4) and its box (6 doubles), an entity record one point, an id 4 bytes
+NODE_RECORD_BYTES, POINT_RECORD_BYTES, ID_BYTES = 16 + 48, 24, 4
+
+
+def l2_copy_gbs(reps=50):
+    """Read + write GB/s of a device copy whose 2 x 32 MB stay in L2 (the roof of L2-resident query
+    working sets; the HBM roof is MEASURED_PEAKS.json's)."""
+    import torch
+
+    x = torch.ones(8 << 20, device="cuda")
+    y = torch.empty_like(x)
+    for _ in range(5):
+        y.copy_(x)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(reps):
+        y.copy_(x)
+    b.record()
+    b.synchronize()
+    return 2 * x.numel() * 4 * reps / (a.elapsed_time(b) / 1e3) / 1e9
+
+
+def query_work(p1, ranges, q8, pts16, q16, k16):
+    """Per-query work of the reference's traversal on the measured inputs, counted by the oracle
+    restatement (node records read, entity records read, ids returned): C1 range and kNN(k=8) on
+    the 1M tree (all 10k queries), C3 uneven kNN on the 16M tree (the first 20k of the 1M
+    queries). Returns {name: (nodes, entities, ids) per query}."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _oracle_lib import oracle
+
+    threads = os.cpu_count() or 1
+    o1 = oracle().create(p1, 0, 10, None, 20, threads=threads)
+    out = {}
+    for name, fn, nq in (("c1_range", lambda t: t.range_search(ranges), len(ranges)), ("c1_knn8", lambda t: t.knn(q8, 8), len(q8))):
+        out[name] = tuple(v / nq for v in o1.work(fn))
+    del o1
+    o3 = oracle().create(pts16, 0, 10, None, 20, threads=threads)
+    out["c3_knn_uneven"] = tuple(v / len(q16) for v in o3.work(lambda t: t.knn(q16, k16)))
+    return out
+
+
+def query_roofline(work, mq_per_s, peak_gbs, bound):
+    """roofline object of a query line: algorithmic bytes per query (the reference traversal's
+    work x record sizes) x queries/s against the roof of its working set."""
+    nodes, ents, ids = work
+    per_query = nodes * NODE_RECORD_BYTES + ents * POINT_RECORD_BYTES + ids * ID_BYTES
+    achieved = per_query * mq_per_s * 1e6 / 1e9
+    return {
+        "bound": bound,
+        "achieved": achieved,
+        "peak": peak_gbs,
+        "unit": "GB/s",
+        "frac": achieved / peak_gbs,
+        "bytes_per_query": per_query,
+        "work_per_query": {"node_records": nodes, "entity_records": ents, "ids": ids},
+    }
+
+
+def run_queries(tree16, pts16_d, stream, cpu=None, pts16_h=None):
     """cpu: the CPU results of run_cpu_configs on its samples; each is compared with the GPU's
-    result on the same sample (mismatched_ids_vs_cpu: queries, or pairs, that differ)."""
+    result on the same sample (mismatched_ids_vs_cpu: queries, or pairs, that differ).
+    pts16_h: the host copy of the 16M points, for the traversal work counts of the rooflines."""
     import torch
 
     import octree_gb300 as otg
@@ -743,6 +804,25 @@ def run_queries(tree16, pts16_d, stream, cpu=None):
     if cpu:
         mism["c3_knn_uneven_2000"] = csr_mismatches(tree16.knn(qk[:2000], ks[:2000]), cpu["c3_knn_uneven"])
     out["knn_uneven_speedup_filtered_vs_plain"] = out["knn_uneven_16M_1Mq_filtered_fp32_Mq_per_s"] / out["knn_uneven_16M_1Mq_plain_fp64_Mq_per_s"]
+    if pts16_h is not None:
+        # rooflines of the query lines: the 1M tree and its points (42 MB) stay in L2; the 16M tree
+        # (384 MB of points) does not
+        work = query_work(p1, ranges_h, q_h, pts16_h, qk.cpu().numpy()[:20_000], ks.cpu().numpy().astype(np.uint32)[:20_000])
+        l2 = l2_copy_gbs()
+        hbm, hbm_kind = peaks()
+        rl = {}
+        for key, wname, peak, bound in (
+            ("range_1M_10k_batched", "c1_range", l2, "l2"),
+            ("range_1M_10k_plain_fp64", "c1_range", l2, "l2"),
+            ("knn8_1M_10k_filtered_fp32", "c1_knn8", l2, "l2"),
+            ("knn8_1M_10k_plain_fp64", "c1_knn8", l2, "l2"),
+            ("knn_uneven_16M_1Mq_filtered_fp32", "c3_knn_uneven", hbm, "hbm"),
+            ("knn_uneven_16M_1Mq_plain_fp64", "c3_knn_uneven", hbm, "hbm"),
+        ):
+            rl[key] = query_roofline(work[wname], out[key + "_Mq_per_s"], peak, bound)
+        out["roofline"] = rl
+        out["roofline_peaks"] = {"l2_copy_gbs": l2, "hbm_gbs": hbm, "hbm_kind": hbm_kind, "l2_how": "device copy of 2 x 32 MB kept in L2, 50 reps, CUDA events"}
+        out["roofline_work_source"] = "oracle restatement counters of the reference's traversal on the measured queries (C3: the first 20k queries)"
     # self-collision of 4M clustered FP64 boxes, depth 12, max 32 per node
     boxes = torch.as_tensor(cluster_boxes(4_000_000, 201), device="cuda")
     tb = otg.Tree("boxes").create(boxes, max_depth=12, max_elements=32)

@@ -101,6 +101,15 @@ void otg_tree_free(otg_tree* tree);
 int otg_tree_create(otg_tree* tree, const void* entities, uint64_t n, uint32_t max_depth, const void* box, uint64_t max_elements, int mem,
                     void* stream);
 
+/* Core (non-owning) form: the geometry that the tree's queries test from now on. The reference's
+   Core trees take the entity span on every query (core/ot_query.h:424-427, 477-482, 1209-1215,
+   1902-1906, with EntityContainerView = std::span<T const>, core/entity_adapter.h:171-174) and
+   test the geometry of that span against the nodes that Create built from the earlier span. This
+   call makes the GPU tree do the same: the nodes (and their boxes) stay as the last Create built
+   them, and `entities` (n must equal the tree's entity count; the same layout as Create's) becomes
+   the tested geometry. Host memory is copied; device memory is read once, here. Not for forests. */
+int otg_tree_set_entities(otg_tree* tree, const void* entities, uint64_t n, int mem, void* stream);
+
 /* Waits for the tree's last build on `stream` and reports device-side errors (OTG_ERR_TIMEOUT). */
 int otg_tree_sync(otg_tree* tree, void* stream);
 
@@ -147,7 +156,7 @@ typedef struct otg_static_layout
 int otg_tree_export_static(otg_tree* tree, otg_static_layout* out, void* stream);
 
 /* The tree as the reference's BinaryOutputArchive writes its static tree (`ar & tree`,
-   serialization.h:359-385 with serialization/binary_archive.h and serialization/stl/*.h):
+   serialization.h:359-385 with serialization/binary_archive.h and the headers of serialization/stl):
    StaticOctreePoint / StaticOctreeBox, or with with_entities != 0 the Managed
    StaticOctreePointM / StaticOctreeBoxM, which also holds the entities (serialization.h:433-438).
    The reference's BinaryInputArchive loads the bytes into that type. Little-endian scalars and

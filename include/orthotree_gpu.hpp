@@ -1,11 +1,20 @@
-// orthotree_gpu.hpp — C++20 drop-in types for OrthoTree's Managed octrees, backed by the GB300
-// library through its C-ABI (octree_gb300.h).
+// orthotree_gpu.hpp — C++20 drop-in types for OrthoTree's octrees (Core and Managed forms), backed
+// by the GB300 library through its C-ABI (octree_gb300.h).
 //
+//   OrthoTreeGPU::OctreePoint    ~ OrthoTree::OctreePoint  (core/ot_aliases.h:119), Core: non-owning
+//   OrthoTreeGPU::OctreeBox      ~ OrthoTree::OctreeBox    (core/ot_aliases.h:122), Core
+//   OrthoTreeGPU::OctreeBoxs<L>  ~ OrthoTree::OctreeBoxs<L> (core/ot_aliases.h:144-145), Core
+//   (and the FP32 Core variants OctreePointF / OctreeBoxF / OctreeBoxsF)
 //   OrthoTreeGPU::OctreePointM   ~ OrthoTree::OctreePointM (core/ot_aliases.h:364)
 //   OrthoTreeGPU::OctreeBoxM     ~ OrthoTree::OctreeBoxM   (core/ot_aliases.h:369)
 //   OrthoTreeGPU::OctreeBoxMs<L> ~ OrthoTree::OctreeBoxMs<L> (core/ot_aliases.h:367-368; false: regular boxes)
 //   (and the FP32 variants OctreePointMF / OctreeBoxMF / OctreeBoxMsF)
 //
+// The Core types take the entity span on Create and on every query, as the reference's do
+// (core/ot_dynamic_hash_core.h:348-373, 812-822; core/ot_query.h:424-2146): the GPU keeps a device
+// copy of the span it last saw and uploads another span (or the same one after
+// NotifyEntitiesChanged) before a query, keeping the nodes, which is what the reference answers
+// when it is given another span. The Managed types own their entities.
 // Construction and Create take the reference's arguments (core/ot_managed.h:169-228, 318-360):
 // entities, optional max depth, optional space box, max elements per node (default 16,
 // core/configuration.h:83). Queries have the reference's names, argument order and defaults
@@ -44,6 +53,7 @@
 #include <optional>
 #include <span>
 #include <stdexcept>
+#include <type_traits>
 #include <string>
 #include <utility>
 #include <vector>
@@ -232,6 +242,7 @@ public:
 
   // CUDA stream (cudaStream_t) the tree's work is ordered on; nullptr = legacy default stream
   void SetStream(void* stream) noexcept { m_stream = stream; }
+  void* Stream() const noexcept { return m_stream; }
   const otg_tree* Handle() const noexcept { return m_tree; }
 
   // Create(entities, maxDepthID, boxSpace, maxElementNoInNode) — core/ot_dynamic_hash_core.h:751-822
@@ -567,5 +578,222 @@ template<bool IS_LOOSE_TREE>
 using OctreeBoxMs = OrthoTreeManagedGPU<BoundingBox3<double>, double, IS_LOOSE_TREE ? OTG_KIND_BOXES : OTG_KIND_BOXES_REGULAR>;
 template<bool IS_LOOSE_TREE>
 using OctreeBoxMsF = OrthoTreeManagedGPU<BoundingBox3<float>, float, IS_LOOSE_TREE ? OTG_KIND_BOXES : OTG_KIND_BOXES_REGULAR>;
+
+// Core tree: non-owning, as OrthoTree's Core types (OctreePoint, OctreeBox, OctreeBoxs<L>;
+// core/ot_aliases.h:119-145). Create takes the entities, and so does every query
+// (EntityContainerView = std::span<T const>, core/entity_adapter.h:171-174); the reference tests
+// the geometry of the span it is given against the nodes Create built
+// (core/ot_dynamic_hash_core.h:812-822, core/ot_query.h:424-427, 477-482, 1209-1215, 1902-1906).
+// The GPU needs that geometry in device memory, so the tree keeps a device copy of the span it
+// last saw, identified by (pointer, size, generation):
+//   * a query with the same span and generation uses the device copy as it is;
+//   * a query with another span of the same size, or after NotifyEntitiesChanged() (the caller
+//     changed the span's contents in place), uploads that span first and keeps the nodes, exactly
+//     as the reference answers with a span other than the one it was created from;
+//   * a span of another size is refused (OTG_ERR_INVALID_ARGUMENT): it does not fit the nodes.
+// The check makes queries on one tree object unsafe to call concurrently with different spans.
+template<typename TEntity, typename TScalar, int KIND>
+class OrthoTreeCoreGPU
+{
+  using Impl = OrthoTreeManagedGPU<TEntity, TScalar, KIND>;
+
+public:
+  using Entity = TEntity;
+  using EntityContainerView = std::span<const TEntity>;
+  using TBox = typename Impl::TBox;
+  using TVector = typename Impl::TVector;
+  using TRay = typename Impl::TRay;
+  using TPlane = typename Impl::TPlane;
+  using QueryCondition = typename Impl::QueryCondition;
+  static constexpr std::size_t DEFAULT_TARGET_ELEMENT_NUM_IN_NODES = Impl::DEFAULT_TARGET_ELEMENT_NUM_IN_NODES;
+
+  OrthoTreeCoreGPU() = default;
+
+  // DynamicHashOrthoTreeCore(entities, maxDepthID, boxSpace, maxElementNoInNode, execMode) (:348-358)
+  template<typename TExecMode = std::nullptr_t>
+  explicit OrthoTreeCoreGPU(EntityContainerView entities, std::optional<depth_t> maxDepthID = std::nullopt, std::optional<TBox> boxSpace = std::nullopt,
+                            std::size_t maxElementNoInNode = DEFAULT_TARGET_ELEMENT_NUM_IN_NODES, TExecMode = {})
+  {
+    Create(entities, maxDepthID, boxSpace, maxElementNoInNode);
+  }
+  // DynamicHashOrthoTreeCore(execMode, entities, maxDepthID, boxSpace, maxElementNoInNode) (:362-373)
+  template<typename TExecMode>
+    requires(!std::is_convertible_v<TExecMode, EntityContainerView>)
+  OrthoTreeCoreGPU(TExecMode, EntityContainerView entities, std::optional<depth_t> maxDepthID = std::nullopt, std::optional<TBox> boxSpace = std::nullopt,
+                   std::size_t maxElementNoInNode = DEFAULT_TARGET_ELEMENT_NUM_IN_NODES)
+  {
+    Create(entities, maxDepthID, boxSpace, maxElementNoInNode);
+  }
+
+  void SetStream(void* stream) noexcept { m_impl.SetStream(stream); }
+  const otg_tree* Handle() const noexcept { return m_impl.Handle(); }
+
+  // Create(entities, maxDepthID, boxSpace, maxElementNoInNode, execMode) (:751-809); errors throw
+  template<typename TExecMode = std::nullptr_t>
+  bool Create(EntityContainerView entities, std::optional<depth_t> maxDepthID = std::nullopt, std::optional<TBox> boxSpace = std::nullopt,
+              std::size_t maxElementNoInNode = DEFAULT_TARGET_ELEMENT_NUM_IN_NODES, TExecMode = {})
+  {
+    m_impl.Create(entities, maxDepthID, boxSpace, maxElementNoInNode);
+    m_data = entities.data();
+    m_size = entities.size();
+    m_boundGeneration = m_generation;
+    return true;
+  }
+  // static Create(tree, entities, maxDepthID, boxSpace, maxElementNoInNode, execMode) (:812-822)
+  template<typename TExecMode = std::nullptr_t>
+  static bool Create(OrthoTreeCoreGPU& tree, EntityContainerView entities, std::optional<depth_t> maxDepthID = std::nullopt,
+                     std::optional<TBox> boxSpace = std::nullopt, std::size_t maxElementNoInNode = DEFAULT_TARGET_ELEMENT_NUM_IN_NODES, TExecMode = {})
+  {
+    return tree.Create(entities, maxDepthID, boxSpace, maxElementNoInNode);
+  }
+
+  // The caller changed the contents of the span in place: the next query uploads it again.
+  void NotifyEntitiesChanged() noexcept { ++m_generation; }
+
+  std::size_t GetNodeCount() const { return m_impl.GetNodeCount(); }
+  depth_t GetMaxDepthID() const { return m_impl.GetMaxDepthID(); }
+
+  // ---------------------------------------------------------------- queries (reference form)
+  std::vector<EntityID> PickSearch(const TVector& pickPoint, EntityContainerView entities, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return bind(entities).PickSearch(pickPoint, tolerance);
+  }
+  std::vector<EntityID> RangeSearch(const TBox& range, EntityContainerView entities, RangeSearchMode mode = RangeSearchMode::Inside,
+                                    double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return bind(entities).RangeSearch(range, mode, tolerance);
+  }
+  std::vector<EntityID> PlaneSearch(TScalar distanceOfOrigo, const TVector& planeNormal, EntityContainerView entities,
+                                    double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return bind(entities).PlaneSearch(distanceOfOrigo, planeNormal, tolerance);
+  }
+  std::vector<EntityID> PlaneSearch(const TPlane& plane, EntityContainerView entities, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return bind(entities).PlaneSearch(plane, tolerance);
+  }
+  std::vector<EntityID> PlaneIntersection(TScalar distanceOfOrigo, const TVector& planeNormal, EntityContainerView entities,
+                                          double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return PlaneSearch(distanceOfOrigo, planeNormal, entities, tolerance);
+  }
+  std::vector<EntityID> PlaneIntersection(const TPlane& plane, EntityContainerView entities, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return PlaneSearch(plane, entities, tolerance);
+  }
+  std::vector<EntityID> PlanePositiveSegmentation(TScalar distanceOfOrigo, const TVector& planeNormal, EntityContainerView entities,
+                                                  double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return bind(entities).PlanePositiveSegmentation(distanceOfOrigo, planeNormal, tolerance);
+  }
+  std::vector<EntityID> PlanePositiveSegmentation(const TPlane& plane, EntityContainerView entities, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return bind(entities).PlanePositiveSegmentation(plane, tolerance);
+  }
+  std::vector<EntityID> FrustumCulling(std::span<const TPlane> boundaryPlanes, EntityContainerView entities,
+                                       double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return bind(entities).FrustumCulling(boundaryPlanes, tolerance);
+  }
+  static QueryCondition ByWithin(const TBox& range) { return Impl::ByWithin(range); }
+  static QueryCondition ByOverlaps(const TBox& range) { return Impl::ByOverlaps(range); }
+  static QueryCondition ByInFrustum(std::vector<std::pair<TPlane, bool>> boundaryPlanes) { return Impl::ByInFrustum(std::move(boundaryPlanes)); }
+  static QueryCondition ByIntersecting(const TPlane& plane, double tolerance = detail::base_tolerance<TScalar>())
+  {
+    return Impl::ByIntersecting(plane, tolerance);
+  }
+  template<LogicalOperator OP = LogicalOperator::And, typename TConditions>
+  std::vector<EntityID> Query(const TConditions& conditions, EntityContainerView entities, double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return bind(entities).template Query<OP>(conditions, tolerance);
+  }
+  std::vector<EntityID> GetNearestNeighbors(const TVector& searchPoint, std::size_t neighborCount, TScalar maxDistanceWithin, EntityContainerView entities,
+                                            double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return bind(entities).GetNearestNeighbors(searchPoint, neighborCount, maxDistanceWithin, tolerance);
+  }
+  std::vector<EntityID> GetNearestNeighbors(const TVector& searchPoint, std::size_t neighborNo, EntityContainerView entities,
+                                            double tolerance = detail::base_tolerance<TScalar>()) const
+  {
+    return bind(entities).GetNearestNeighbors(searchPoint, neighborNo, std::numeric_limits<TScalar>::max(), tolerance);
+  }
+  std::vector<EntityID> RayIntersectedAll(const TVector& rayBasePoint, const TVector& rayHeading, EntityContainerView entities,
+                                          double tolerance = detail::base_tolerance<TScalar>(), double toleranceIncrement = 0.0,
+                                          TScalar maxExaminationDistance = std::numeric_limits<TScalar>::max()) const
+  {
+    return bind(entities).RayIntersectedAll(rayBasePoint, rayHeading, tolerance, toleranceIncrement, maxExaminationDistance);
+  }
+  std::vector<EntityID> RayIntersectedAll(const TRay& ray, EntityContainerView entities, double tolerance = detail::base_tolerance<TScalar>(),
+                                          double toleranceIncrement = 0.0, TScalar maxExaminationDistance = std::numeric_limits<TScalar>::max()) const
+  {
+    return bind(entities).RayIntersectedAll(ray, tolerance, toleranceIncrement, maxExaminationDistance);
+  }
+  std::vector<EntityID> RayIntersectedFirst(const TVector& rayBasePoint, const TVector& rayHeading, EntityContainerView entities,
+                                            double tolerance = detail::base_tolerance<TScalar>(), double toleranceIncrement = 0.0,
+                                            TScalar maxDistance = std::numeric_limits<TScalar>::max()) const
+  {
+    return bind(entities).RayIntersectedFirst(rayBasePoint, rayHeading, tolerance, toleranceIncrement, maxDistance);
+  }
+  std::vector<EntityID> RayIntersectedFirst(const TRay& ray, EntityContainerView entities, double tolerance = detail::base_tolerance<TScalar>(),
+                                            double toleranceIncrement = 0.0, TScalar maxDistance = std::numeric_limits<TScalar>::max()) const
+  {
+    return bind(entities).RayIntersectedFirst(ray, tolerance, toleranceIncrement, maxDistance);
+  }
+
+  // CollisionDetection(entities, tolerance, execMode) (core/ot_query.h:1902-1906)
+  template<typename TExecMode = std::nullptr_t>
+  std::vector<std::pair<EntityID, EntityID>> CollisionDetection(EntityContainerView entities, double tolerance = detail::base_tolerance<TScalar>(),
+                                                                TExecMode = {}) const
+    requires(KIND != OTG_KIND_POINTS)
+  {
+    return bind(entities).CollisionDetection(tolerance);
+  }
+  // CollisionDetection(entities, otherTree, otherEntities, tolerance) (core/ot_query.h:1489-1497)
+  std::vector<std::pair<EntityID, EntityID>> CollisionDetection(EntityContainerView entities, const OrthoTreeCoreGPU& otherTree,
+                                                                EntityContainerView otherEntities, double tolerance = detail::base_tolerance<TScalar>()) const
+    requires(KIND != OTG_KIND_POINTS)
+  {
+    const Impl& left = bind(entities);
+    return left.CollisionDetection(otherTree.bind(otherEntities), tolerance);
+  }
+  // static CollisionDetection(leftTree, leftEntities, rightTree, rightEntities, tolerance) (:1462-1485)
+  static std::vector<std::pair<EntityID, EntityID>> CollisionDetection(const OrthoTreeCoreGPU& leftTree, EntityContainerView leftEntities,
+                                                                       const OrthoTreeCoreGPU& rightTree, EntityContainerView rightEntities,
+                                                                       double tolerance = detail::base_tolerance<TScalar>())
+    requires(KIND != OTG_KIND_POINTS)
+  {
+    return leftTree.CollisionDetection(leftEntities, rightTree, rightEntities, tolerance);
+  }
+
+private:
+  // the Managed tree behind the Core interface, its device entities made to be `entities`
+  const Impl& bind(EntityContainerView entities) const
+  {
+    if (entities.data() != m_data || entities.size() != m_size || m_boundGeneration != m_generation)
+    {
+      detail::check(otg_tree_set_entities(const_cast<otg_tree*>(m_impl.Handle()), entities.data(), entities.size(), OTG_MEM_HOST, m_impl.Stream()));
+      m_data = entities.data();
+      m_size = entities.size();
+      m_boundGeneration = m_generation;
+    }
+    return m_impl;
+  }
+
+  Impl m_impl;
+  mutable const TEntity* m_data = nullptr;
+  mutable std::size_t m_size = 0;
+  std::uint64_t m_generation = 0;
+  mutable std::uint64_t m_boundGeneration = 0;
+};
+
+using OctreePoint = OrthoTreeCoreGPU<Vector3<double>, double, OTG_KIND_POINTS>;
+using OctreeBox = OrthoTreeCoreGPU<BoundingBox3<double>, double, OTG_KIND_BOXES>;
+using OctreePointF = OrthoTreeCoreGPU<Vector3<float>, float, OTG_KIND_POINTS>;
+using OctreeBoxF = OrthoTreeCoreGPU<BoundingBox3<float>, float, OTG_KIND_BOXES>;
+// OctreeBoxs<IS_LOOSE_TREE> (core/ot_aliases.h:144-145): false = the regular box tree
+template<bool IS_LOOSE_TREE>
+using OctreeBoxs = OrthoTreeCoreGPU<BoundingBox3<double>, double, IS_LOOSE_TREE ? OTG_KIND_BOXES : OTG_KIND_BOXES_REGULAR>;
+template<bool IS_LOOSE_TREE>
+using OctreeBoxsF = OrthoTreeCoreGPU<BoundingBox3<float>, float, IS_LOOSE_TREE ? OTG_KIND_BOXES : OTG_KIND_BOXES_REGULAR>;
 
 } // namespace OrthoTreeGPU

@@ -42,6 +42,7 @@ EXPORTS = [
     ("otg_tree_new", _int, [C.POINTER(_vp), _int, _int]),
     ("otg_tree_free", None, [_vp]),
     ("otg_tree_create", _int, [_vp, _vp, _u64, _u32, _vp, _u64, _int, _vp]),
+    ("otg_tree_set_entities", _int, [_vp, _vp, _u64, _int, _vp]),
     ("otg_tree_sync", _int, [_vp, _vp]),
     ("otg_tree_info_get", _int, [_vp, _vp]),
     ("otg_tree_export_locations", _int, [_vp, _vp, _int, _vp]),
@@ -284,6 +285,15 @@ class Tree:
                 bp = bb.ctypes.data_as(_vp)
         _check(library().otg_tree_create(self.h, p, n, max_depth, bp, max_elements, mem, _stream_ptr(stream)))
         self._keep = (keep, bkeep)
+        return self
+
+    def set_entities(self, entities, stream=None):
+        """Core form: the geometry that later queries test, as the reference's Core queries take the
+        entity span on every call; the nodes stay as the last create() built them."""
+        p, mem, keep = _arg(entities, self.dtype)
+        n = int(entities.shape[0]) if len(entities.shape) else 0
+        _check(library().otg_tree_set_entities(self.h, p, n, mem, _stream_ptr(stream)))
+        self._keep_span = keep  # device input is read by the stream-ordered gather of this call
         return self
 
     def sync(self, stream=None):

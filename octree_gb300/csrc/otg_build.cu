@@ -25,9 +25,11 @@
 #include "otg_internal.h"
 #include "otg_raster.cuh"
 #include "otg_sort.cuh"
+#include "otg_sort_chunked.cuh"
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 namespace otg
@@ -1114,6 +1116,26 @@ __global__ void __launch_bounds__(256) root_box_kernel(const uint4* __restrict__
 }
 
 // ---------------------------------------------------------------- host orchestration
+// The single-tree sort: decoupled look-back passes (otg_sort.cuh), or with OTG_SORT=chunked the
+// chunked persistent passes (otg_sort_chunked.cuh); forests and recorded builds use the former.
+static bool chunked_sort_enabled()
+{
+  static const bool on = [] {
+    const char* v = std::getenv("OTG_SORT");
+    return v && std::strcmp(v, "chunked") == 0;
+  }();
+  return on;
+}
+// widest digit of the chunked passes (OTG_SORT_BITS, 8-11)
+static int chunked_sort_bits()
+{
+  static const int b = [] {
+    const char* v = std::getenv("OTG_SORT_BITS");
+    return v ? std::atoi(v) : kChunkMaxBits;
+  }();
+  return b;
+}
+
 static int grid_blocks(u64 n, int perBlock = 256, int maxBlocks = 152 * 16)
 {
   u64 b = (n + perBlock - 1) / perBlock;
@@ -1166,7 +1188,13 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   const bool regular = t.kind == OTG_KIND_BOXES_REGULAR; // GetBoxGridID instead of the loose grid data
   const u32 D = t.D;
   const u32 bits = IS_BOX ? 3 * D + 5 : 3 * D + 1;
-  const u32 passes = (bits + kRadixBits - 1) / kRadixBits;
+  const bool chunked = chunked_sort_enabled();
+  // histogram passes computed by codegen: the onesweep passes need them, the chunked ones count
+  // their own digits
+  // sorted key bits: a loose box centred on the max face of its space has the out-of-grid cell 2^D
+  // in up to three dimensions, so its key can hold three bits above 3D + 5
+  const u32 sortBits = IS_BOX ? std::min(3 * D + 8, u32(8 * sizeof(K))) : bits;
+  const u32 passes = chunked ? 0u : (sortBits + kRadixBits - 1) / kRadixBits;
   const u32 cells = IS_BOX ? (1u << D) + 2 : (1u << D);
   const size_t tabBytes = RasterLayout<T>::bytes(cells);
   const u64 minTabEntries = IS_BOX ? 1 : 3 * ((u64(2) << D) - 1);
@@ -1180,7 +1208,7 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
       (e = t.nodeKey.ensure(sizeof(u64) * maxNodes)) || (e = t.nodeBox.ensure(sizeof(T) * 6 * maxNodes)) ||
       (e = t.nodeDepth.ensure(maxNodes)) || (e = t.levelCount.ensure(sizeof(u32) * 64)) ||
       (e = t.splitQueue.ensure(2 * sizeof(u32) * (n / (t.maxElem + 1) + 2))) || (e = t.space.ensure(sizeof(Space<T>))) ||
-      (e = t.sortScratch.ensure(SortScratch::bytes(n, passes))) || (e = t.bboxBits.ensure(sizeof(U) * 6)) ||
+      (e = t.sortScratch.ensure(chunked ? ChunkScratch::bytes() : SortScratch::bytes(n, passes))) || (e = t.bboxBits.ensure(sizeof(U) * 6)) ||
       (e = t.rasterTab.ensure(tabBytes)) || (e = t.minTab.ensure(sizeof(T) * minTabEntries)) ||
       (IS_BOX && ((e = t.nodeMax.ensure(sizeof(T) * 3 * maxNodes)) || (e = t.ownerNode.ensure(sizeof(u32) * n)) ||
                   (e = t.nodeParent.ensure(sizeof(u32) * maxNodes)))))
@@ -1190,8 +1218,17 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   prof.reset();
   prof.mark("setup", st);
   SortScratch ss;
-  ss.carve(t.sortScratch.p, n, passes);
-  cudaMemsetAsync(t.sortScratch.p, 0, SortScratch::bytes(n, passes), st);
+  ChunkScratch cs;
+  if (chunked)
+  {
+    cs.carve(t.sortScratch.p);
+    cudaMemsetAsync(static_cast<unsigned char*>(t.sortScratch.p) + ChunkScratch::zero_offset(), 0, ChunkScratch::zero_bytes(), st);
+  }
+  else
+  {
+    ss.carve(t.sortScratch.p, n, passes);
+    cudaMemsetAsync(t.sortScratch.p, 0, SortScratch::bytes(n, passes), st);
+  }
   cudaMemsetAsync(t.levelCount.p, 0, sizeof(u32) * 64, st);
 
   const bool vec = (reinterpret_cast<uintptr_t>(ent) & 15) == 0;
@@ -1244,7 +1281,15 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   }
 
   prof.mark("sort", st);
-  bool inB = onesweep_passes<K>(t.keysA.as<K>(), t.sortedIds.as<u32>(), t.keysB.as<K>(), t.valsB.as<u32>(), n, 0, passes, true, ss, t.err.as<u32>(), st);
+  bool inB = false;
+  if (chunked)
+  {
+    if (int rc = chunk_sort<K>(t.keysA.as<K>(), t.sortedIds.as<u32>(), t.keysB.as<K>(), t.valsB.as<u32>(), n, sortBits, true, cs, t.err.as<u32>(), st,
+                               &inB, chunked_sort_bits()))
+      return rc;
+  }
+  else
+    inB = onesweep_passes<K>(t.keysA.as<K>(), t.sortedIds.as<u32>(), t.keysB.as<K>(), t.valsB.as<u32>(), n, 0, passes, true, ss, t.err.as<u32>(), st);
   if (inB)
   {
     std::swap(t.sortedIds, t.valsB);
@@ -1313,8 +1358,22 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
   return cuda_status(cudaGetLastError(), "launching build kernels");
 }
 
+// OTG_L2_FETCH_BYTES (32-128): this process's L2 fetch granularity limit (cudaLimitMaxL2FetchGranularity,
+// a per-context hint), set once before the first build
+static void apply_l2_fetch_limit()
+{
+  static const bool done = [] {
+    if (const char* v = std::getenv("OTG_L2_FETCH_BYTES"))
+      cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, size_t(std::atoi(v)));
+    cudaGetLastError();
+    return true;
+  }();
+  (void)done;
+}
+
 int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const void* box, u64 maxElem, int mem, cudaStream_t st)
 {
+  apply_l2_fetch_limit();
   const bool isBox = t.kind != OTG_KIND_POINTS;
   const int W = isBox ? 6 : 3;
   const size_t esz = t.scalar == OTG_SCALAR_F64 ? 8 : 4;
@@ -1394,7 +1453,9 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
     return OTG_OK;
   }
   const u32 bits = isBox ? 3 * D + 5 : 3 * D + 1;
-  t.keys32 = bits <= 32;
+  // a loose box's location can lie one cell outside the grid (3 more key bits), which a 32-bit
+  // key would cut off
+  t.keys32 = bits + (isBox ? 3 : 0) <= 32;
   int rc;
   if (t.scalar == OTG_SCALAR_F64)
   {
@@ -1635,7 +1696,8 @@ static int forest_build_impl(TreeState& t, const T* ent, const T* boxes, cudaStr
   const u32 trees = t.trees;
   const u64 n = t.n;
   const u32 Dmax = t.D;
-  const u32 bits = IS_BOX ? 3 * Dmax + 5 : 3 * Dmax + 1;
+  // sorted key bits (out-of-grid loose-box locations: three bits above 3D + 5)
+  const u32 bits = IS_BOX ? std::min(3 * Dmax + 8, u32(8 * sizeof(K))) : 3 * Dmax + 1;
   const u32 passes = (bits + kRadixBits - 1) / kRadixBits;
   const u32 tiles = u32(t.segTilesHost.size());
   const u64 tabEntries = t.tabOffHost.back();
@@ -1853,7 +1915,7 @@ int build_forest(TreeState& t, const void* entities, const u64* treeOffsets, u32
     dboxes = t.boxDev.p;
   }
   const u32 bits = isBox ? 3 * Dmax + 5 : 3 * Dmax + 1;
-  t.keys32 = bits <= 32;
+  t.keys32 = bits + (isBox ? 3 : 0) <= 32; // out-of-grid loose-box locations need 3 more bits
   int rc;
   if (t.scalar == OTG_SCALAR_F64)
   {
@@ -1951,6 +2013,56 @@ int finish_build(TreeState& t, cudaStream_t st)
     t.nodeCount = s;
   }
   t.countsKnown = true;
+  return OTG_OK;
+}
+
+// The Core form's entity span (otg_tree_set_entities): the new geometry in tree order, gathered by
+// the ids of the last Create; nodes, node boxes and MBRs stay as that Create built them.
+int set_entities(TreeState& t, const void* entities, u64 n, int mem, cudaStream_t st)
+{
+  if (t.trees)
+  {
+    set_error("otg_tree_set_entities: not for forests");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
+  if (n != t.n)
+  {
+    set_error("otg_tree_set_entities: the entity count differs from the tree's");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  if (n == 0)
+    return OTG_OK;
+  const bool isBox = t.kind != OTG_KIND_POINTS;
+  const int W = isBox ? 6 : 3;
+  const size_t esz = t.scalar == OTG_SCALAR_F64 ? 8 : 4;
+  cudaError_t e;
+  const void* src = entities;
+  if (mem == OTG_MEM_HOST)
+  {
+    if ((e = t.entities.ensure(esz * W * n)) || (e = cudaMemcpyAsync(t.entities.p, entities, esz * W * n, cudaMemcpyHostToDevice, st)))
+      return cuda_status(e, "copying entities");
+    src = t.entities.p;
+  }
+  const int blocks = grid_blocks((n + kGatherPerThread - 1) / kGatherPerThread, 256, 152 * 16);
+  if (t.scalar == OTG_SCALAR_F64)
+  {
+    if (isBox)
+      gather_kernel<double, 6, kGatherPerThread><<<blocks, 256, 0, st>>>((const double*)src, t.sortedIds.as<u32>(), n, t.sortedGeom.as<double>());
+    else
+      gather_kernel<double, 3, kGatherPerThread><<<blocks, 256, 0, st>>>((const double*)src, t.sortedIds.as<u32>(), n, t.sortedGeom.as<double>());
+  }
+  else
+  {
+    if (isBox)
+      gather_kernel<float, 6, kGatherPerThread><<<blocks, 256, 0, st>>>((const float*)src, t.sortedIds.as<u32>(), n, t.sortedGeom.as<float>());
+    else
+      gather_kernel<float, 3, kGatherPerThread><<<blocks, 256, 0, st>>>((const float*)src, t.sortedIds.as<u32>(), n, t.sortedGeom.as<float>());
+  }
+  t.image32 = false; // the FP32 filter images follow the geometry
+  if ((e = cudaGetLastError()))
+    return cuda_status(e, "gathering entities");
+  if (mem == OTG_MEM_HOST && (e = cudaStreamSynchronize(st)))
+    return cuda_status(e, "gathering entities");
   return OTG_OK;
 }
 

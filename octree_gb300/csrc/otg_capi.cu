@@ -4,6 +4,8 @@
 // There is no CPU path: without a CUDA device every compute call returns OTG_ERR_NO_DEVICE.
 #include "otg_internal.h"
 
+#include <mutex>
+
 #include <cstring>
 #include <new>
 #include <string>
@@ -14,6 +16,25 @@ namespace otg
 static thread_local std::string g_lastError;
 
 void set_error(const std::string& msg) { g_lastError = msg; }
+
+void keep_pool_memory(int device)
+{
+  static std::mutex lock;
+  static bool done[64] = {};
+  if (device < 0 || device >= 64)
+    return;
+  std::lock_guard<std::mutex> g(lock);
+  if (done[device])
+    return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess)
+  {
+    unsigned long long threshold = 1ull << 30;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+  }
+  cudaGetLastError();
+  done[device] = true;
+}
 
 int cuda_status(cudaError_t e, const char* what)
 {
@@ -204,6 +225,20 @@ extern "C"
     if (int rc = require_device())
       return rc;
     return build_tree(t->s, entities, n, max_depth, box, max_elements, mem, (cudaStream_t)stream);
+  }
+
+  int otg_tree_set_entities(otg_tree* t, const void* entities, uint64_t n, int mem, void* stream)
+  {
+    if (int rc = ready(t, (cudaStream_t)stream))
+      return rc;
+    if ((n && !entities) || (mem != OTG_MEM_HOST && mem != OTG_MEM_DEVICE))
+    {
+      set_error("otg_tree_set_entities: invalid argument");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+    if (int rc = require_device())
+      return rc;
+    return set_entities(t->s, entities, n, mem, (cudaStream_t)stream);
   }
 
   int otg_tree_sync(otg_tree* t, void* stream)

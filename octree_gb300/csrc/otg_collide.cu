@@ -313,8 +313,8 @@ static int collide_search_impl(TreeState& A, TreeState& B, bool self, bool swapO
   }
   if (!s.orderReady)
   {
-    DevBuf keys;
-    if ((e = keys.ensure(sizeof(u32) * std::max<u64>(A.n, 1))) || (e = s.order.ensure(sizeof(u32) * std::max<u64>(A.n, 1))))
+    TmpBuf keys;
+    if ((e = keys.ensure(sizeof(u32) * std::max<u64>(A.n, 1), st)) || (e = s.order.ensure(sizeof(u32) * std::max<u64>(A.n, 1))))
       return cuda_status(e, "allocating the collision order");
     owner_depth_key_kernel<<<blocks_for(A.n), 256, 0, st>>>(A.ownerNode.as<u32>(), A.nodeDepth.as<unsigned char>(), A.n, keys.as<u32>(), s.order.as<u32>());
     if (int rc = sort_pairs_u32(keys.as<u32>(), s.order.as<u32>(), A.n, 5, st, err))

@@ -81,6 +81,56 @@ struct DevBuf
   }
 };
 
+// Per-call device scratch of the query paths, stream ordered (cudaMallocAsync / cudaFreeAsync on the
+// call's stream, from the device's default memory pool, which keeps up to 1 GiB of freed blocks for
+// reuse): a small batch of queries pays no cudaMalloc / cudaFree, and a block is reused only after the
+// work queued before its release on that stream.
+void keep_pool_memory(int device);
+struct TmpBuf
+{
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaStream_t st = nullptr;
+  TmpBuf() = default;
+  TmpBuf(const TmpBuf&) = delete;
+  TmpBuf& operator=(const TmpBuf&) = delete;
+  ~TmpBuf() { release(); }
+  cudaError_t ensure(size_t need, cudaStream_t stream)
+  {
+    if (need <= bytes)
+      return cudaSuccess;
+    release();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    keep_pool_memory(dev);
+    st = stream;
+    cudaError_t e = cudaMallocAsync(&p, need ? need : 16, stream);
+    if (e == cudaSuccess)
+      bytes = need ? need : 16;
+    else
+      p = nullptr;
+    return e;
+  }
+  void release()
+  {
+    if (p)
+      cudaFreeAsync(p, st);
+    p = nullptr;
+    bytes = 0;
+  }
+  template<typename X>
+  X* as() const
+  {
+    return reinterpret_cast<X*>(p);
+  }
+  friend void swap(TmpBuf& a, TmpBuf& b) noexcept
+  {
+    std::swap(a.p, b.p);
+    std::swap(a.bytes, b.bytes);
+    std::swap(a.st, b.st);
+  }
+};
+
 // ownerNode of an entity that no node reachable from the root holds (a location outside the grid:
 // the reference keeps it in a node the root does not link, so no query or collision sees it)
 constexpr u32 kNoOwner = 0xffffffffu;
@@ -198,6 +248,7 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
 int build_forest(TreeState& t, const void* entities, const u64* treeOffsets, u32 trees, u32 maxDepth, const void* boxes, u64 maxElem, int mem,
                  cudaStream_t st);
 int finish_build(TreeState& t, cudaStream_t st);
+int set_entities(TreeState& t, const void* entities, u64 n, int mem, cudaStream_t st);
 int forest_relaunch(TreeState& t, const void* entities, const void* boxes, cudaStream_t st);
 int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st);
 int export_nodes(const TreeState& t, u64* keys, double* minSize, u64* eoff, u32* eids, u32* childCount);

@@ -762,10 +762,10 @@ static int knn_filtered_impl(TreeState& t, const T* pts, const u32* dk, u64 nq, 
   // k statistics: the buffer size follows the largest k, the output guess the sum of k
   u32 kmax = kAll;
   u64 ksum = u64(kAll) * nq;
-  DevBuf stats;
+  TmpBuf stats;
   if (dk)
   {
-    if ((e = stats.ensure(16)))
+    if ((e = stats.ensure(16, st)))
       return cuda_status(e, "allocating k statistics");
     cudaMemsetAsync(stats.p, 0, 16, st);
     k_stats_kernel<<<blocks_for(nq), 256, 0, st>>>(dk, nq, stats.as<u32>(), reinterpret_cast<unsigned long long*>(stats.as<unsigned char>() + 8));
@@ -780,13 +780,13 @@ static int knn_filtered_impl(TreeState& t, const T* pts, const u32* dk, u64 nq, 
   }
   const bool big = kmax > 112;
   // spatial order of the queries
-  DevBuf qkeys, order;
-  if ((e = qkeys.ensure(sizeof(u32) * nq)) || (e = order.ensure(sizeof(u32) * nq)))
+  TmpBuf qkeys, order;
+  if ((e = qkeys.ensure(sizeof(u32) * nq, st)) || (e = order.ensure(sizeof(u32) * nq, st)))
     return cuda_status(e, "allocating the query order");
   query_key_kernel<T><<<blocks_for(nq), 256, 0, st>>>(pts, nq, t.space.as<Space<T>>(), qkeys.as<u32>(), order.as<u32>());
-  DevBuf ctr, fb, start, cnt, oIds, oDist;
-  if ((e = ctr.ensure(sizeof(KnnCounters))) || (e = fb.ensure(sizeof(u32) * nq)) || (e = start.ensure(sizeof(u64) * nq)) ||
-      (e = cnt.ensure(sizeof(u32) * nq)))
+  TmpBuf ctr, fb, start, cnt, oIds, oDist;
+  if ((e = ctr.ensure(sizeof(KnnCounters), st)) || (e = fb.ensure(sizeof(u32) * nq, st)) || (e = start.ensure(sizeof(u64) * nq, st)) ||
+      (e = cnt.ensure(sizeof(u32) * nq, st)))
     return cuda_status(e, "allocating kNN buffers");
   cudaMemsetAsync(ctr.p, 0, sizeof(KnnCounters), st);
   if (int rc = sort_pairs_u32(qkeys.as<u32>(), order.as<u32>(), nq, 30, st, &ctr.as<KnnCounters>()->err))
@@ -832,7 +832,7 @@ static int knn_filtered_impl(TreeState& t, const T* pts, const u32* dk, u64 nq, 
   KnnCounters h{};
   for (int attempt = 0; attempt < 2; ++attempt)
   {
-    if ((e = oIds.ensure(sizeof(u32) * cap)) || (e = oDist.ensure(sizeof(double) * cap)))
+    if ((e = oIds.ensure(sizeof(u32) * cap, st)) || (e = oDist.ensure(sizeof(double) * cap, st)))
       return cuda_status(e, "allocating the kNN output");
     a.outIds = oIds.as<u32>();
     a.outDist = oDist.as<double>();
@@ -867,8 +867,8 @@ static int knn_filtered_impl(TreeState& t, const T* pts, const u32* dk, u64 nq, 
   ResultState fbr;
   if (h.fallbacks)
   {
-    DevBuf fpts, fk;
-    if ((e = fpts.ensure(sizeof(T) * 3 * h.fallbacks)) || (e = fk.ensure(sizeof(u32) * h.fallbacks)))
+    TmpBuf fpts, fk;
+    if ((e = fpts.ensure(sizeof(T) * 3 * h.fallbacks, st)) || (e = fk.ensure(sizeof(u32) * h.fallbacks, st)))
       return cuda_status(e, "allocating fallback queries");
     fallback_points_kernel<<<blocks_for(h.fallbacks), 256, 0, st>>>(fb.as<u32>(), h.fallbacks, pts, u32(sizeof(T) * 3), dk, kAll,
                                                                    fpts.as<unsigned char>(), fk.as<u32>());
@@ -878,8 +878,8 @@ static int knn_filtered_impl(TreeState& t, const T* pts, const u32* dk, u64 nq, 
   }
   // CSR: offsets by scan of the counts, then entries moved into query order
   const u64 tiles = (nq + kScanTile - 1) / kScanTile;
-  DevBuf tileSums;
-  if ((e = tileSums.ensure(sizeof(u64) * (tiles + 1))) || (e = r.offsets.ensure(sizeof(u64) * (nq + 1))))
+  TmpBuf tileSums;
+  if ((e = tileSums.ensure(sizeof(u64) * (tiles + 1), st)) || (e = r.offsets.ensure(sizeof(u64) * (nq + 1))))
     return cuda_status(e, "allocating result offsets");
   scan_reduce_kernel<<<u32(tiles), kScanThreads, 0, st>>>(cnt.as<u32>(), nq, tileSums.as<u64>());
   scan_tiles_kernel<<<1, kScanThreads, 0, st>>>(tileSums.as<u64>(), tiles);

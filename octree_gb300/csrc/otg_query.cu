@@ -1051,11 +1051,11 @@ __global__ void item_ids_kernel(const u64* __restrict__ items, u64 m, u32* __res
 
 struct Collected
 {
-  DevBuf items, dist, count, err;
+  TmpBuf items, dist, count, err;
   u64 m = 0;
 };
 
-static int check_err(const DevBuf& err, cudaStream_t st)
+static int check_err(const TmpBuf& err, cudaStream_t st)
 {
   u32 h = 0;
   cudaError_t e = cudaMemcpyAsync(&h, err.p, sizeof(u32), cudaMemcpyDeviceToHost, st);
@@ -1091,12 +1091,12 @@ template<typename F>
 static int collect(Collected& c, bool withDist, u64 guess, F&& launch, cudaStream_t st)
 {
   cudaError_t e;
-  if ((e = c.count.ensure(sizeof(unsigned long long))) || (e = c.err.ensure(sizeof(u32))))
+  if ((e = c.count.ensure(sizeof(unsigned long long), st)) || (e = c.err.ensure(sizeof(u32), st)))
     return cuda_status(e, "allocating counters");
   u64 cap = std::max<u64>(guess, 1024);
   for (int attempt = 0; attempt < 3; ++attempt)
   {
-    if ((e = c.items.ensure(sizeof(u64) * cap)) || (withDist && (e = c.dist.ensure(sizeof(double) * cap))))
+    if ((e = c.items.ensure(sizeof(u64) * cap, st)) || (withDist && (e = c.dist.ensure(sizeof(double) * cap, st))))
       return cuda_status(e, "allocating result buffer");
     cudaMemsetAsync(c.count.p, 0, sizeof(unsigned long long), st);
     cudaMemsetAsync(c.err.p, 0, sizeof(u32), st);
@@ -1135,8 +1135,8 @@ static int finish_sorted_ids(Collected& c, u64 nq, ResultState& r, cudaStream_t 
     return cuda_status(e, "allocating result");
   if (m == 0)
     return cuda_status(cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * (nq + 1), st), "result offsets");
-  DevBuf vals, qid;
-  if ((e = vals.ensure(sizeof(u32) * m)) || (e = qid.ensure(sizeof(u32) * m)))
+  TmpBuf vals, qid;
+  if ((e = vals.ensure(sizeof(u32) * m, st)) || (e = qid.ensure(sizeof(u32) * m, st)))
     return cuda_status(e, "allocating sort values");
   if (int rc = sort_pairs_u64(c.items.as<u64>(), vals.as<u32>(), m, 32 + bit_count(nq), st, c.err.as<u32>()))
     return rc;
@@ -1159,8 +1159,8 @@ static int finish_by_distance(Collected& c, u64 nq, u64 nEntities, ResultState& 
     return cuda_status(e, "allocating result");
   if (m == 0)
     return cuda_status(cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * (nq + 1), st), "result offsets");
-  DevBuf perm, k32, k64;
-  if ((e = perm.ensure(sizeof(u32) * m)) || (e = k32.ensure(sizeof(u32) * m)) || (e = k64.ensure(sizeof(u64) * m)))
+  TmpBuf perm, k32, k64;
+  if ((e = perm.ensure(sizeof(u32) * m, st)) || (e = k32.ensure(sizeof(u32) * m, st)) || (e = k64.ensure(sizeof(u64) * m, st)))
     return cuda_status(e, "allocating sort buffers");
   u32* err = c.err.as<u32>();
   iota_kernel<<<blocks_for(m), 256, 0, st>>>(perm.as<u32>(), m);
@@ -1194,8 +1194,8 @@ static int finish_pairs(Collected& c, ResultState& r, cudaStream_t st)
     return cuda_status(e, "result offsets");
   if (m)
   {
-    DevBuf vals;
-    if ((e = vals.ensure(sizeof(u32) * m)))
+    TmpBuf vals;
+    if ((e = vals.ensure(sizeof(u32) * m, st)))
       return cuda_status(e, "allocating sort values");
     if (int rc = sort_pairs_u64(c.items.as<u64>(), vals.as<u32>(), m, 64, st, c.err.as<u32>()))
       return rc;
@@ -1219,14 +1219,14 @@ __global__ void swap_pair_halves_kernel(u32* ids, u64 m)
 
 // ---------------------------------------------------------------- host entry points
 // stage a caller array in device memory
-static int stage_input(DevBuf& buf, const void* src, size_t bytes, int mem, cudaStream_t st, const void*& dptr)
+static int stage_input(TmpBuf& buf, const void* src, size_t bytes, int mem, cudaStream_t st, const void*& dptr)
 {
   if (mem == OTG_MEM_DEVICE)
   {
     dptr = src;
     return OTG_OK;
   }
-  if (cudaError_t e = buf.ensure(bytes))
+  if (cudaError_t e = buf.ensure(bytes, st))
     return cuda_status(e, "allocating query input");
   if (bytes)
     if (cudaError_t e = cudaMemcpyAsync(buf.p, src, bytes, cudaMemcpyHostToDevice, st))
@@ -1266,7 +1266,7 @@ template<typename T>
 static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
                       const u32* qTree)
 {
-  DevBuf in;
+  TmpBuf in;
   const void* d;
   if (int rc = stage_input(in, ranges, sizeof(T) * 6 * nq, mem, st, d))
     return rc;
@@ -1275,8 +1275,8 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
   Collected c;
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
-  DevBuf work;
-  if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
+  TmpBuf work;
+  if (cudaError_t e = work.ensure(batch_work_bytes(nq), st))
     return cuda_status(e, "allocating the work counter");
   int launchRc = OTG_OK;
   int rc = collect(
@@ -1307,7 +1307,7 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
 template<typename T>
 static int pick_impl(const TreeState& t, const void* pts, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st, const u32* qTree)
 {
-  DevBuf in;
+  TmpBuf in;
   const void* d;
   if (int rc = stage_input(in, pts, sizeof(T) * 3 * nq, mem, st, d))
     return rc;
@@ -1316,8 +1316,8 @@ static int pick_impl(const TreeState& t, const void* pts, u64 nq, double tol, in
   Collected c;
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
-  DevBuf work;
-  if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
+  TmpBuf work;
+  if (cudaError_t e = work.ensure(batch_work_bytes(nq), st))
     return cuda_status(e, "allocating the work counter");
   int launchRc = OTG_OK;
   int rc = collect(
@@ -1349,7 +1349,7 @@ template<typename T>
 static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
                         const u32* qTree)
 {
-  DevBuf in;
+  TmpBuf in;
   const void* d;
   if (int rc = stage_input(in, planes, sizeof(T) * 4 * np * nq, mem, st, d))
     return rc;
@@ -1358,8 +1358,8 @@ static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, 
   Collected c;
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
-  DevBuf work;
-  if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
+  TmpBuf work;
+  if (cudaError_t e = work.ensure(batch_work_bytes(nq), st))
     return cuda_status(e, "allocating the work counter");
   int launchRc = OTG_OK;
   int rc = collect(
@@ -1391,7 +1391,7 @@ template<typename T>
 static int plane_impl(const TreeState& t, const void* planes, u64 nq, bool positive, double tol, int algo, ResultState& r, int mem, cudaStream_t st,
                       const u32* qTree)
 {
-  DevBuf in;
+  TmpBuf in;
   const void* d;
   if (int rc = stage_input(in, planes, sizeof(T) * 4 * nq, mem, st, d))
     return rc;
@@ -1400,8 +1400,8 @@ static int plane_impl(const TreeState& t, const void* planes, u64 nq, bool posit
   Collected c;
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
-  DevBuf work;
-  if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
+  TmpBuf work;
+  if (cudaError_t e = work.ensure(batch_work_bytes(nq), st))
     return cuda_status(e, "allocating the work counter");
   int launchRc = OTG_OK;
   int rc = collect(
@@ -1477,7 +1477,7 @@ static int query_impl(const TreeState& t, const QueryCond* conds, const u64* off
         return cuda_status(e, "reading the condition count");
     }
   }
-  DevBuf inC, inO, inP, inX, inB;
+  TmpBuf inC, inO, inP, inX, inB;
   const void *dC, *dO, *dP, *dX, *dB;
   if (int rc = stage_input(inC, conds, sizeof(QueryCond) * nConds, mem, st, dC))
     return rc;
@@ -1495,8 +1495,8 @@ static int query_impl(const TreeState& t, const QueryCond* conds, const u64* off
   Collected c;
   auto tv = view<T>(t, nullptr);
   T tl = tol_of<T>(tol);
-  DevBuf work;
-  if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
+  TmpBuf work;
+  if (cudaError_t e = work.ensure(batch_work_bytes(nq), st))
     return cuda_status(e, "allocating the work counter");
   int launchRc = OTG_OK;
   int rc = collect(
@@ -1529,7 +1529,7 @@ template<typename T>
 static int knn_impl(const TreeState& t, const void* pts, u64 nq, const u32* k, u32 kAll, double maxDist, double tol, int algo, ResultState& r, int mem,
                     cudaStream_t st, const u32* qTree)
 {
-  DevBuf in, kin, F;
+  TmpBuf in, kin, F;
   const void* d;
   const void* dk = nullptr;
   if (int rc = stage_input(in, pts, sizeof(T) * 3 * nq, mem, st, d))
@@ -1541,7 +1541,7 @@ static int knn_impl(const TreeState& t, const void* pts, u64 nq, const u32* k, u
     return empty_result(nq, r, true, st);
   if (algo != OTG_ALGO_PLAIN_FP64 && t.kind == OTG_KIND_POINTS && !qTree)
     return knn_filtered(const_cast<TreeState&>(t), d, (const u32*)dk, nq, kAll, maxDist, tol, r, st);
-  if (cudaError_t e = F.ensure(sizeof(T) * nq))
+  if (cudaError_t e = F.ensure(sizeof(T) * nq, st))
     return cuda_status(e, "allocating kNN thresholds");
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
@@ -1550,9 +1550,9 @@ static int knn_impl(const TreeState& t, const void* pts, u64 nq, const u32* k, u
   u32 kMax = kAll;
   if (dk)
   {
-    DevBuf m;
+    TmpBuf m;
     cudaError_t e;
-    if ((e = m.ensure(sizeof(u32))) || (e = cudaMemsetAsync(m.p, 0, sizeof(u32), st)))
+    if ((e = m.ensure(sizeof(u32), st)) || (e = cudaMemsetAsync(m.p, 0, sizeof(u32), st)))
       return cuda_status(e, "finding the largest k");
     max_u32_kernel<<<u32(std::min<u64>((nq + 255) / 256, 152 * 8)), 256, 0, st>>>((const u32*)dk, nq, m.as<u32>());
     if ((e = cudaMemcpyAsync(&kMax, m.p, sizeof(u32), cudaMemcpyDeviceToHost, st)) || (e = cudaStreamSynchronize(st)))
@@ -1576,7 +1576,7 @@ template<typename T>
 static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, double tolInc, double maxDist, bool first, int algo, ResultState& r,
                     int mem, cudaStream_t st, const u32* qTree)
 {
-  DevBuf in, M;
+  TmpBuf in, M;
   const void* d;
   if (int rc = stage_input(in, rays, sizeof(T) * 6 * nq, mem, st, d))
     return rc;
@@ -1590,8 +1590,8 @@ static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, do
   int rc;
   if (!first)
   {
-    DevBuf work;
-    if (cudaError_t e = work.ensure(batch_work_bytes(nq)))
+    TmpBuf work;
+    if (cudaError_t e = work.ensure(batch_work_bytes(nq), st))
       return cuda_status(e, "allocating the work counter");
     int launchRc = OTG_OK;
     rc = collect(
@@ -1617,7 +1617,7 @@ static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, do
   }
   else
   {
-    if (cudaError_t e = M.ensure(sizeof(T) * nq))
+    if (cudaError_t e = M.ensure(sizeof(T) * nq, st))
       return cuda_status(e, "allocating ray thresholds");
     rc = collect(
       c, true, nq * 4,
@@ -1674,9 +1674,9 @@ static int collide_impl(const TreeState& a, const TreeState& b, bool self, doubl
   if (filtered && (rc = collide_search_stats(search, tests, rechecks, st)))
     return rc;
   const u64 m = c.m;
-  DevBuf keys, rej;
+  TmpBuf keys, rej;
   cudaError_t e;
-  if ((e = keys.ensure(sizeof(u64) * std::max<u64>(m, 1))) || (e = rej.ensure(sizeof(unsigned long long))))
+  if ((e = keys.ensure(sizeof(u64) * std::max<u64>(m, 1), st)) || (e = rej.ensure(sizeof(unsigned long long), st)))
     return cuda_status(e, "allocating pair filter");
   cudaMemsetAsync(rej.p, 0, sizeof(unsigned long long), st);
   if (m)
@@ -1688,7 +1688,7 @@ static int collide_impl(const TreeState& a, const TreeState& b, bool self, doubl
     e = cudaStreamSynchronize(st);
   if (e)
     return cuda_status(e, "filtering pairs");
-  std::swap(c.items, keys);
+  swap(c.items, keys);
   rc = finish_pairs(c, r, st); // rejected pairs carry key ~0 and sort last
   if (rc)
     return rc;

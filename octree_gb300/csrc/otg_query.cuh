@@ -237,9 +237,9 @@ static inline int sort_pairs_u64(u64* keys, u32* vals, u64 m, u32 bits, cudaStre
   if (m <= 1 || bits == 0)
     return OTG_OK;
   const u32 passes = (bits + kRadixBits - 1) / kRadixBits;
-  DevBuf k1, v1, scratch;
+  TmpBuf k1, v1, scratch;
   cudaError_t e;
-  if ((e = k1.ensure(sizeof(u64) * m)) || (e = v1.ensure(sizeof(u32) * m)) || (e = scratch.ensure(SortScratch::bytes(m, passes))))
+  if ((e = k1.ensure(sizeof(u64) * m, st)) || (e = v1.ensure(sizeof(u32) * m, st)) || (e = scratch.ensure(SortScratch::bytes(m, passes), st)))
     return cuda_status(e, "allocating sort buffers");
   cudaMemsetAsync(scratch.p, 0, SortScratch::bytes(m, passes), st);
   SortScratch ss;
@@ -251,10 +251,7 @@ static inline int sort_pairs_u64(u64* keys, u32* vals, u64 m, u32 bits, cudaStre
     cudaMemcpyAsync(keys, k1.p, sizeof(u64) * m, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(vals, v1.p, sizeof(u32) * m, cudaMemcpyDeviceToDevice, st);
   }
-  cudaStreamSynchronize(st);
-  k1.release();
-  v1.release();
-  scratch.release();
+  // the scratch is released in stream order after the copies above
   return cuda_status(cudaGetLastError(), "sorting results");
 }
 
@@ -263,9 +260,9 @@ static inline int sort_pairs_u32(u32* keys, u32* vals, u64 m, u32 bits, cudaStre
   if (m <= 1 || bits == 0)
     return OTG_OK;
   const u32 passes = (bits + kRadixBits - 1) / kRadixBits;
-  DevBuf k1, v1, scratch;
+  TmpBuf k1, v1, scratch;
   cudaError_t e;
-  if ((e = k1.ensure(sizeof(u32) * m)) || (e = v1.ensure(sizeof(u32) * m)) || (e = scratch.ensure(SortScratch::bytes(m, passes))))
+  if ((e = k1.ensure(sizeof(u32) * m, st)) || (e = v1.ensure(sizeof(u32) * m, st)) || (e = scratch.ensure(SortScratch::bytes(m, passes), st)))
     return cuda_status(e, "allocating sort buffers");
   cudaMemsetAsync(scratch.p, 0, SortScratch::bytes(m, passes), st);
   SortScratch ss;
@@ -277,10 +274,7 @@ static inline int sort_pairs_u32(u32* keys, u32* vals, u64 m, u32 bits, cudaStre
     cudaMemcpyAsync(keys, k1.p, sizeof(u32) * m, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(vals, v1.p, sizeof(u32) * m, cudaMemcpyDeviceToDevice, st);
   }
-  cudaStreamSynchronize(st);
-  k1.release();
-  v1.release();
-  scratch.release();
+  // the scratch is released in stream order after the copies above
   return cuda_status(cudaGetLastError(), "sorting results");
 }
 

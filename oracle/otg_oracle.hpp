@@ -1065,6 +1065,17 @@ public:
     return true;
   }
 
+  // ------------------------------------------------------------------ query work counters
+  // The work of the reference's traversal, counted while `countWork` is set (single-threaded use):
+  // node records read (node tests), entity records read (entity tests) and ids returned. They give
+  // the algorithmic bytes of a query batch: nodes x node record + entities x entity record + ids x 4.
+  struct QueryWork
+  {
+    u64 nodes = 0, entities = 0, ids = 0;
+  };
+  mutable QueryWork work;
+  bool countWork = false;
+
   // ------------------------------------------------------------------ node accessors
   // ot_dynamic_hash_core.h:491-529
   const T* node_min(const Node& n) const { return n.minPoint; }
@@ -1133,6 +1144,8 @@ public:
       [&](const Node& n) {
         const T* mn = node_min(n);
         const T* sz = node_size(n);
+        if (countWork)
+          ++work.nodes;
         if (!G::overlap_by_min_point(rmin, rsize, mn, sz, tol))
           return false;
         if (G::range_contains_min_size(range, mn, sz, tol))
@@ -1140,6 +1153,8 @@ public:
           collect_subtree(n, found);
           return false;
         }
+        if (countWork)
+          work.entities += n.entities.size();
         for (u32 id : n.entities)
         {
           const T* e = ent(id);
@@ -1156,6 +1171,8 @@ public:
         return true;
       },
       root());
+    if (countWork)
+      work.ids += found.size();
     return found;
   }
 
@@ -1180,6 +1197,8 @@ public:
         return true;
       },
       root());
+    if (countWork)
+      work.ids += found.size();
     return found;
   }
 
@@ -1345,6 +1364,8 @@ public:
         return true;
       },
       root());
+    if (countWork)
+      work.ids += found.size();
     return found;
   }
 
@@ -1519,16 +1540,22 @@ public:
       [&](const Node& n, T nodeDistance) -> int {
         if (nodeDistance >= farthest)
           return 2;
+        if (countWork)
+          work.entities += n.entities.size();
         add_entity_distance(k, q, n.entities, tol, opt, pes, farthest);
         return 0;
       },
       [&](const Node& n) -> std::optional<T> {
+        if (countWork)
+          ++work.nodes;
         T w = G::wall_distance(q, node_min(n), node_size(n));
         if (w >= farthest)
           return std::nullopt;
         return w;
       });
     // ot_query.h:1166-1191 ConvertEntityDistanceToList
+    if (countWork)
+      work.ids += opt.size();
     if (opt.empty())
       return opt;
     if (opt.size() < k)

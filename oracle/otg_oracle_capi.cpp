@@ -246,11 +246,51 @@ extern "C"
     }
     return a;
   }
+  // Work counters of the reference's traversal (Tree::QueryWork): on = 1 clears them and starts
+  // counting the tree's range and kNN queries (single-threaded calls only); oro_work reads them as
+  // {node records, entity records, ids}.
+  void oro_count_work(void* h, int on)
+  {
+    auto* a = (AnyTree*)h;
+    if (a->scalar == 0)
+    {
+      a->d->countWork = on != 0;
+      a->d->work = {};
+    }
+    else
+    {
+      a->f->countWork = on != 0;
+      a->f->work = {};
+    }
+  }
+  void oro_work(void* h, uint64_t* out3)
+  {
+    auto* a = (AnyTree*)h;
+    auto put = [&](const auto& w) {
+      out3[0] = w.nodes;
+      out3[1] = w.entities;
+      out3[2] = w.ids;
+    };
+    if (a->scalar == 0)
+      put(a->d->work);
+    else
+      put(a->f->work);
+  }
   void* oro_create(int scalar, int kind, const void* ent, uint64_t n, uint32_t maxDepth, const void* box, uint64_t maxElem)
   {
     return oro_create_threads(scalar, kind, ent, n, maxDepth, box, maxElem, 1);
   }
   void oro_destroy(void* h) { delete (AnyTree*)h; }
+  // Core form: `ent` (n entities, the Create layout) becomes the geometry the tree's queries test;
+  // the nodes stay as Create built them (the reference's Core queries take the span per call)
+  void oro_set_entities(void* h, const void* ent, uint64_t n)
+  {
+    auto* a = (AnyTree*)h;
+    if (a->scalar == 0)
+      a->d->geom.assign((const double*)ent, (const double*)ent + n * (a->d->isBox ? 6 : 3));
+    else
+      a->f->geom.assign((const float*)ent, (const float*)ent + n * (a->f->isBox ? 6 : 3));
+  }
   uint32_t oro_max_depth(void* h)
   {
     auto* a = (AnyTree*)h;

@@ -733,6 +733,19 @@ extern "C"
   }
   void oro_res_free(void* r) { delete (Result*)r; }
 
+  // Core form: the entity span that every later query passes (the tree is not rebuilt): the
+  // reference's Core queries test the geometry of the span they are given against the nodes
+  // Create built from the earlier one
+  void oro_set_entities(void* h, const void* ent, uint64_t n)
+  {
+    auto* a = (AnyRef*)h;
+    const uint64_t w = n * (a->kind == 0 ? 3 : 6);
+    if (a->scalar == 0)
+      a->ed.assign((const double*)ent, (const double*)ent + w);
+    else
+      a->ef.assign((const float*)ent, (const float*)ent + w);
+  }
+
   // Timed reference Create (OctreePoint, PAR_EXEC) — used for the CPU baseline where the reference is built.
   double oro_time_create_points(const double* pts, uint64_t n, uint32_t maxDepth, uint64_t maxElem, int reps)
   {

@@ -304,3 +304,24 @@ def tree_is_equal_to_static(dyn, st, tol):
         return all(rec(md[o], ms[o]) for o in md)
 
     return m == 0 or rec(idx[1], 0)
+
+
+def moved_span(ent, rng, is_box):
+    """A new span for the same tree: a fifth of the entities moved a little, a few moved far (out of
+    their nodes and out of the space), and boxes resized."""
+    out = ent.copy()
+    n = len(ent)
+    idx = rng.choice(n, n // 5, replace=False)
+    shift = rng.normal(0, 0.02, (len(idx), 3)).astype(ent.dtype)
+    far = rng.choice(n, max(1, n // 100), replace=False)
+    fshift = rng.normal(0, 30, (len(far), 3)).astype(ent.dtype)
+    if is_box:
+        out[idx, :3] += shift
+        out[idx, 3:] += shift * 1.5
+        out[far, :3] += fshift
+        out[far, 3:] += fshift
+        out[:, 3:] = np.maximum(out[:, 3:], out[:, :3])
+    else:
+        out[idx] += shift
+        out[far] += fshift
+    return out

@@ -79,6 +79,14 @@ class OracleLib:
             lib.oro_static_equal.argtypes = [_vp]
             lib.oro_dynamic_equals_static.restype = _int
             lib.oro_dynamic_equals_static.argtypes = [_vp]
+        if hasattr(lib, "oro_set_entities"):
+            lib.oro_set_entities.restype = None
+            lib.oro_set_entities.argtypes = [_vp, _vp, _u64]
+        if hasattr(lib, "oro_count_work"):  # the restatement only
+            lib.oro_count_work.restype = None
+            lib.oro_count_work.argtypes = [_vp, _int]
+            lib.oro_work.restype = None
+            lib.oro_work.argtypes = [_vp, _vp]
         if hasattr(lib, "oro_collide_self_par"):
             lib.oro_collide_self_par.restype = _vp
             lib.oro_collide_self_par.argtypes = [_vp, _dbl]
@@ -187,6 +195,26 @@ class OracleTree:
         finally:
             self.lib.oro_static_free(h)
         return dict(child_begins=cb[:nb], segments=seg[:m], depth=dep[:m], entity_storage=es[:ne], geometry=geo[:m]), equal
+
+    def set_entities(self, ent):
+        """Core form: the geometry later queries test (same count and layout; the tree keeps its nodes)."""
+        ent = np.ascontiguousarray(ent, dtype=self.ent.dtype)
+        assert ent.shape == self.ent.shape
+        self.ent = ent
+        self.lib.oro_set_entities(self.h, _ptr(ent), ent.shape[0] if ent.size else 0)
+        return self
+
+    def work(self, fn):
+        """(node records, entity records, ids) that the reference's traversal reads and returns for
+        the queries fn(self) runs (the restatement's counters; single-threaded)."""
+        self.lib.oro_count_work(self.h, 1)
+        try:
+            fn(self)
+            out = np.zeros(3, np.uint64)
+            self.lib.oro_work(self.h, _ptr(out))
+        finally:
+            self.lib.oro_count_work(self.h, 0)
+        return tuple(int(v) for v in out)
 
     def location_keys(self):
         out = np.zeros(self.n, np.uint64)

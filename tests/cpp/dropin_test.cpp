@@ -25,6 +25,7 @@ extern "C"
                   int or_op, double tol);
   void* oro_collide_self(void* h, double tol);
   void* oro_collide_pair(void* h1, void* h2, double tol);
+  void oro_set_entities(void* h, const void* ent, uint64_t n);
   uint64_t oro_res_nq(void* r);
   uint64_t oro_res_total(void* r);
   void oro_res_copy(void* r, uint64_t* offsets, uint32_t* ids, double* dist);
@@ -261,6 +262,94 @@ int main()
     expect(flat, r, 0, "CollisionDetection (regular boxes)");
     oro_res_free(r);
     oro_destroy(orr);
+  }
+  // ---- the Core form (non-owning): the entity span on Create and on every query
+  {
+    std::vector<Point3D> span1(pts.begin(), pts.begin() + 30000);
+    OctreePoint tc(std::span<const Point3D>(span1), 8, std::nullopt, 20);
+    void* oc = oro_create(0, 0, span1.data(), span1.size(), 8, nullptr, 20);
+    auto check_span = [&](std::span<const Point3D> span, const char* what) {
+      oro_set_entities(oc, span.data(), span.size());
+      void* r = oro_range(oc, ranges.data(), nq, 0, -1.0);
+      for (int i = 0; i < nq; ++i)
+        expect(tc.RangeSearch(ranges[i], span), r, i, what);
+      oro_res_free(r);
+      std::vector<uint32_t> k(nq, 7);
+      r = oro_knn(oc, qp.data(), nq, k.data(), -1.0, -1.0);
+      for (int i = 0; i < nq; ++i)
+        expect(tc.GetNearestNeighbors(qp[i], 7, span), r, i, what);
+      oro_res_free(r);
+      r = oro_pick(oc, qp.data(), nq, -1.0);
+      for (int i = 0; i < nq; ++i)
+        expect(tc.PickSearch(qp[i], span), r, i, what);
+      oro_res_free(r);
+    };
+    check_span(span1, "Core: the Create span");
+    // another span of the same size: the nodes stay, the new geometry is tested
+    std::vector<Point3D> span2(span1);
+    for (std::size_t i = 0; i < span2.size(); i += 3)
+      for (int c = 0; c < 3; ++c)
+        span2[i][c] += 0.7 * N(rng);
+    check_span(span2, "Core: another span");
+    // the first span changed in place: uploaded again after NotifyEntitiesChanged
+    for (std::size_t i = 1; i < span1.size(); i += 5)
+      span1[i][0] += 1.3;
+    tc.NotifyEntitiesChanged();
+    check_span(span1, "Core: span changed in place");
+    // a span of another size does not fit the nodes
+    bool refused = false;
+    try
+    {
+      tc.RangeSearch(ranges[0], std::span<const Point3D>(span1.data(), span1.size() - 1));
+    }
+    catch (const Error& e)
+    {
+      refused = e.status() == OTG_ERR_INVALID_ARGUMENT;
+    }
+    if (!refused)
+    {
+      std::printf("MISMATCH Core: a span of another size was not refused\n");
+      ++g_fail;
+    }
+    oro_destroy(oc);
+    // box trees: collisions with the span, and the two-tree form
+    std::vector<BoundingBox3D> bspan(boxes.begin(), boxes.begin() + 8000);
+    OctreeBox tbc(std::span<const BoundingBox3D>(bspan), 7, std::nullopt, 16);
+    OctreeBox tbo;
+    std::vector<BoundingBox3D> ospan(boxes.begin() + 8000, boxes.begin() + 12000);
+    OctreeBox::Create(tbo, std::span<const BoundingBox3D>(ospan), 6, std::nullopt, 12);
+    void* obc = oro_create(0, 1, bspan.data(), bspan.size(), 7, nullptr, 16);
+    void* obo = oro_create(0, 1, ospan.data(), ospan.size(), 6, nullptr, 12);
+    auto flat = [](const std::vector<std::pair<EntityID, EntityID>>& p) {
+      std::vector<uint32_t> v;
+      for (auto [a, b] : p)
+      {
+        v.push_back(a);
+        v.push_back(b);
+      }
+      return v;
+    };
+    for (int round = 0; round < 2; ++round)
+    {
+      void* r = oro_collide_self(obc, -1.0);
+      expect(flat(tbc.CollisionDetection(std::span<const BoundingBox3D>(bspan))), r, 0, "Core: CollisionDetection");
+      oro_res_free(r);
+      r = oro_collide_pair(obc, obo, -1.0);
+      expect(flat(OctreeBox::CollisionDetection(tbc, std::span<const BoundingBox3D>(bspan), tbo, std::span<const BoundingBox3D>(ospan))), r, 0,
+             "Core: CollisionDetection(two trees)");
+      oro_res_free(r);
+      // move some boxes of the first span (same size): the next round tests the new geometry
+      for (std::size_t i = 0; i < bspan.size(); i += 4)
+        for (int c = 0; c < 3; ++c)
+        {
+          bspan[i].Min[c] += 0.5;
+          bspan[i].Max[c] += 0.5;
+        }
+      tbc.NotifyEntitiesChanged();
+      oro_set_entities(obc, bspan.data(), bspan.size());
+    }
+    oro_destroy(obc);
+    oro_destroy(obo);
   }
   if (g_fail)
     return 1;

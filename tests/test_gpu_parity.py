@@ -5,7 +5,17 @@ import numpy as np
 import pytest
 
 import octree_gb300 as otg
-from _compare import GPU_KIND, assert_csr_equal, assert_dist_close, assert_nodes_equal, golden_cases, load_golden, node_dict
+from _compare import (
+    GPU_KIND,
+    assert_csr_equal,
+    assert_dist_close,
+    assert_nodes_equal,
+    assert_nodes_equal_exact,
+    golden_cases,
+    load_golden,
+    moved_span,
+    node_dict,
+)
 from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, oracle
 
 pytestmark = pytest.mark.gpu
@@ -489,3 +499,54 @@ def test_build_from_pinned_host_memory(kind, dtype, offset):
     assert_nodes_equal(t.nodes(), o.nodes(), "pinned")
     q = _queries(rng, dtype, 100)
     assert_csr_equal(t.range_search(q["ranges"], 1)[:2], o.range_search(q["ranges"], 1), "pinned range")
+
+
+@pytest.mark.parametrize("n", [1, 7, 4095, 4096, 4097, 3 * 4096 + 1, 1_000_003])
+@pytest.mark.parametrize("kind,depth", [(KIND_POINTS, 10), (KIND_POINTS, 19), (KIND_POINTS, 3), (KIND_LOOSE_BOXES, 12), (KIND_LOOSE_BOXES, 10)])
+def test_sort_sizes_and_digit_widths(n, kind, depth):
+    """Sizes around the radix sort's 4096-key tiles (one partial tile, exact tiles, a partial last
+    tile, chunks of unequal tile counts) and key widths that give 1 to 6 passes of 8-11-bit
+    digits (points at depth 3, 10, 19: 10, 31, 58 bits; boxes at depth 10 and 12: 35 and 41
+    bits): keys and node sets equal the oracle's."""
+    rng = np.random.default_rng(n * 31 + depth)
+    if kind == KIND_POINTS:
+        ent = rng.random((n, 3)) * 100
+        ent[: n // 3] = np.round(ent[: n // 3])  # repeated locations: equal keys keep id order
+    else:
+        c = rng.random((n, 3)) * 100
+        ent = np.concatenate([c - rng.random((n, 3)) * 0.3, c + rng.random((n, 3)) * 0.3], 1)
+    t = _gpu_tree(ent, kind, depth, None, 8)
+    o = oracle().create(ent, kind, depth, None, 8)
+    assert np.array_equal(t.location_keys(), o.location_keys())
+    assert_nodes_equal_exact(t.nodes(), o.nodes(), f"n={n} depth={depth}")
+
+
+@pytest.mark.parametrize("kind", [KIND_POINTS, KIND_LOOSE_BOXES, KIND_BOXES])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("device_span", [False, True])
+def test_core_form_set_entities(kind, dtype, device_span):
+    """The Core form (otg_tree_set_entities): a tree created from one span answers with another span
+    of the same size as the reference's Core queries do (the oracle pins that against the
+    reference in test_oracle_vs_reference.py), then with the first span again; a span of another
+    size is refused."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(71 + kind)
+    n = 60_000
+    if kind == KIND_POINTS:
+        ent = (rng.random((n, 3)) * 10).astype(dtype)
+    else:
+        c = rng.random((n, 3)) * 10
+        h = rng.random((n, 3)) * 0.05
+        ent = np.concatenate([c - h, c + h], 1).astype(dtype)
+    t = _gpu_tree(ent, kind, 8, None, 12)
+    o = oracle().create(ent, kind, 8, None, 12)
+    qs = _queries(rng, dtype, 10, nq=300)
+    new = moved_span(ent, rng, kind != KIND_POINTS)
+    for span in (new, ent):
+        t.set_entities(torch.as_tensor(span, device="cuda") if device_span else span)
+        o.set_entities(span)
+        _check_queries(t, o, qs, kind, 0.05, f"core span kind={kind}")
+        if kind != KIND_POINTS:
+            assert np.array_equal(t.collision_self(), o.collide_self())
+    with pytest.raises(otg.OtgError):
+        t.set_entities(ent[:-1])

@@ -4,7 +4,7 @@ the committed golden fixtures carry the pin."""
 import numpy as np
 import pytest
 
-from _compare import assert_static_equal, space_of, static_archive_bytes, tree_is_equal_to_static
+from _compare import assert_static_equal, moved_span, space_of, static_archive_bytes, tree_is_equal_to_static
 from _oracle_lib import KIND_BOXES, KIND_LOOSE_BOXES, KIND_POINTS, oracle, reference
 
 pytestmark = pytest.mark.skipif(reference() is None, reason="reference harness not built here")
@@ -271,3 +271,37 @@ def test_static_fuzz(seed):
     assert static_archive_bytes(ref, is_box, ent.dtype, len(ent), r.max_depth, max_elem, mn, size, ent) == r.static_archive(True)
     tol = float(np.finfo(ent.dtype).eps * 100)
     assert tree_is_equal_to_static(r.nodes(), ref, tol) == bool(r.lib.oro_dynamic_equals_static(r.h))
+
+
+@pytest.mark.parametrize("kind", [KIND_POINTS, KIND_LOOSE_BOXES, KIND_BOXES])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_core_form_queries_with_another_span(kind, dtype):
+    """The Core form: a tree created from one span answers queries with another span of the same
+    size (set_entities) as the reference's Core queries answer with the span they are given; the
+    oracle restatement equals the reference on every query kind."""
+    rng = np.random.default_rng(61 + kind)
+    n = 3000
+    if kind == KIND_POINTS:
+        ent = (rng.random((n, 3)) * 10).astype(dtype)
+    else:
+        c = rng.random((n, 3)) * 10
+        h = rng.random((n, 3)) * 0.2
+        ent = np.concatenate([c - h, c + h], 1).astype(dtype)
+    o = oracle().create(ent, kind, 6, None, 8)
+    r = reference().create(ent, kind, 6, None, 8)
+    new = moved_span(ent, rng, kind != KIND_POINTS)
+    o.set_entities(new)
+    r.set_entities(new)
+    c = rng.random((80, 3)) * 10
+    e = rng.random((80, 3)) * 1.5
+    ranges = np.concatenate([c - e, c + e], 1).astype(dtype)
+    for mode in (0, 1):
+        for x, y in zip(o.range_search(ranges, mode), r.range_search(ranges, mode)):
+            assert np.array_equal(x, y)
+    q = (rng.random((80, 3)) * 10).astype(dtype)
+    for x, y in zip(o.knn(q, 6), r.knn(q, 6)):
+        assert np.array_equal(x, y)
+    for x, y in zip(o.pick_search(q), r.pick_search(q)):
+        assert np.array_equal(x, y)
+    if kind != KIND_POINTS:
+        assert np.array_equal(o.collide_self(), r.collide_self())
