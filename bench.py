@@ -882,7 +882,8 @@ def many_trees(trees, seed):
 
 def run_many_trees(trees=4096, sample=48):
     """The many-small-trees workload: one forest (one build + three batched query launches for all
-    trees) against per-tree Create + queries with the one-query-per-thread kernels, on a sample."""
+    trees) against per-tree Create + queries, on a sample of trees, with the one-query-per-thread
+    kernels and with the batched (warp-per-query) kernels."""
     import torch
 
     import octree_gb300 as otg
@@ -958,6 +959,24 @@ def run_many_trees(trees=4096, sample=48):
             same = np.array_equal(got[1], fi[o0:o1]) and np.array_equal(np.diff(got[0].astype(np.int64)), np.diff(fo[qi : qi + nper + 1].astype(np.int64)))
             mism += 0 if same else 1
     per_tree_s = t_plain / sample
+    # the same per-tree calls with the batched (warp-per-query) kernels, after one untimed pass that
+    # lets the autotuner settle the size classes of the sample
+    def per_tree_batched(t):
+        a, b = int(off[t]), int(off[t + 1])
+        q = slice(t * 256, (t + 1) * 256)
+        tr = otg.Tree("boxes", np.float32).create(d_boxes[a:b], max_elements=16)
+        tr.range_search(d_ranges[q], raw=True)
+        tr.ray_all(d_rays[q], raw=True)
+        tr.frustum_culling(d_planes[t : t + 1], raw=True)
+
+    for t in idx:
+        per_tree_batched(t)
+    torch.cuda.synchronize()
+    s0 = time.perf_counter()
+    for t in idx:
+        per_tree_batched(t)
+    torch.cuda.synchronize()
+    per_tree_batched_s = (time.perf_counter() - s0) / sample
     return {
         "trees": trees,
         "entities": int(off[-1]),
@@ -976,6 +995,9 @@ def run_many_trees(trees=4096, sample=48):
         "per_tree_plain_trees_per_s": 1.0 / per_tree_s,
         "per_tree_plain_sample_trees": int(sample),
         "speedup_forest_vs_per_tree": (1.0 / per_tree_s) and (trees / step_s) / (1.0 / per_tree_s),
+        "per_tree_batched_trees_per_s": 1.0 / per_tree_batched_s,
+        "speedup_forest_vs_per_tree_batched": (trees / step_s) * per_tree_batched_s,
+        "speedup_graph_vs_per_tree_batched": (trees / graph_step_s) * per_tree_batched_s,
         "mismatched_query_groups_in_sample": int(mism),
     }
 

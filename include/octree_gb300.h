@@ -97,7 +97,10 @@ void otg_tree_free(otg_tree* tree);
    max_depth 0 = estimate (EstimateMaxDepth); box NULL = the entities' bounding box.
    The entity array is copied into the tree (the Managed form's ownership, ot_managed.h:70-71);
    queries therefore need no entity argument. Asynchronous on `stream` unless mem == OTG_MEM_HOST,
-   in which case the call returns after the build finished and reports device-side errors. */
+   in which case the call returns after the build finished and reports device-side errors.
+   The first build of the process sets its CUDA context's L2 fetch granularity limit
+   (cudaLimitMaxL2FetchGranularity) to 64 bytes, which makes the build's random entity reads cheaper;
+   the environment variable OTG_L2_FETCH_BYTES chooses another value, 0 leaves the limit unchanged. */
 int otg_tree_create(otg_tree* tree, const void* entities, uint64_t n, uint32_t max_depth, const void* box, uint64_t max_elements, int mem,
                     void* stream);
 
@@ -343,13 +346,19 @@ void otg_result_free(otg_result* r);
 
 /* ---------------------------------------------------------------- kernel-shape autotuning
    No counterpart in the reference. Query kernels exist in shapes that return identical results
-   (one query per thread or per warp; 2, 4 or 8 warps per block). With autotuning on (the default)
-   the first call of a query kind on a size class (kind, scalar, log2 entity count, log2 query
-   count) times every shape on that call's own work and keeps the fastest for the class.
+   (one query per thread or per warp; 2, 4 or 8 warps per block; for the batched range, pick,
+   frustum, plane, Query and ray kernels also the depth, none or 1-3, at which a batch's subtrees
+   become separate work items). With autotuning on (the default) the first call of a query kind on
+   a size class (kind, scalar, log2 entity count, log2 query count) times every shape on that
+   call's own work and keeps the fastest for the class.
    otg_autotune_entry describes entry `index`: the class, each shape's time and the choice. */
 int otg_autotune_enable(int on);
 int otg_autotune_count(void);
 int otg_autotune_entry(int index, char* text, int capacity);
+/* Diagnostic: every tuned call whose candidate shapes include `shape` runs that shape (shape -1:
+   back to tuning). Shapes of the batched query kernels: warps per block (2, 4, 8) | split << 8,
+   split 1 = no split, 2-4 = subtrees at depth 1-3 become work items; 0 = one query per thread. */
+int otg_autotune_force_shape(int shape);
 
 /* ---------------------------------------------------------------- instrumentation
    No counterpart in the reference. When enabled, each otg_tree_create records a CUDA event on

@@ -585,12 +585,19 @@ using OctreeBoxMsF = OrthoTreeManagedGPU<BoundingBox3<float>, float, IS_LOOSE_TR
 // the geometry of the span it is given against the nodes Create built
 // (core/ot_dynamic_hash_core.h:812-822, core/ot_query.h:424-427, 477-482, 1209-1215, 1902-1906).
 // The GPU needs that geometry in device memory, so the tree keeps a device copy of the span it
-// last saw, identified by (pointer, size, generation):
-//   * a query with the same span and generation uses the device copy as it is;
-//   * a query with another span of the same size, or after NotifyEntitiesChanged() (the caller
-//     changed the span's contents in place), uploads that span first and keeps the nodes, exactly
-//     as the reference answers with a span other than the one it was created from;
-//   * a span of another size is refused (OTG_ERR_INVALID_ARGUMENT): it does not fit the nodes.
+// last saw, identified by (pointer, size, generation). A query with the same span and generation
+// uses the device copy as it is. A query with another span, or after NotifyEntitiesChanged() (the
+// caller changed the span's contents in place), uploads that span first, by the tree's SpanChange
+// policy:
+//   * Rebuild (default): the tree is created again from the new span with the arguments of the last
+//     Create, so every query answers as the reference's tree of that span does. The reference
+//     instead keeps the nodes it built from the earlier span.
+//   * KeepNodes: the nodes stay and only the tested geometry changes (otg_tree_set_entities), as the
+//     reference does; a span of another size is refused (OTG_ERR_INVALID_ARGUMENT). Where
+//     entities moved outside the nodes they were built into, the reference's kNN,
+//     RayIntersectedFirst and collision answers depend on the order of its own traversal, and the
+//     GPU's may differ from them; RangeSearch, PickSearch, FrustumCulling, the plane queries, Query
+//     and RayIntersectedAll test a fixed set of nodes and entities and answer as the reference does.
 // The check makes queries on one tree object unsafe to call concurrently with different spans.
 template<typename TEntity, typename TScalar, int KIND>
 class OrthoTreeCoreGPU
@@ -606,6 +613,12 @@ public:
   using TPlane = typename Impl::TPlane;
   using QueryCondition = typename Impl::QueryCondition;
   static constexpr std::size_t DEFAULT_TARGET_ELEMENT_NUM_IN_NODES = Impl::DEFAULT_TARGET_ELEMENT_NUM_IN_NODES;
+
+  enum class SpanChange
+  {
+    Rebuild,
+    KeepNodes
+  };
 
   OrthoTreeCoreGPU() = default;
 
@@ -634,6 +647,9 @@ public:
               std::size_t maxElementNoInNode = DEFAULT_TARGET_ELEMENT_NUM_IN_NODES, TExecMode = {})
   {
     m_impl.Create(entities, maxDepthID, boxSpace, maxElementNoInNode);
+    m_maxDepth = maxDepthID;
+    m_box = boxSpace;
+    m_maxElem = maxElementNoInNode;
     m_data = entities.data();
     m_size = entities.size();
     m_boundGeneration = m_generation;
@@ -649,6 +665,7 @@ public:
 
   // The caller changed the contents of the span in place: the next query uploads it again.
   void NotifyEntitiesChanged() noexcept { ++m_generation; }
+  void SetSpanChange(SpanChange policy) noexcept { m_policy = policy; }
 
   std::size_t GetNodeCount() const { return m_impl.GetNodeCount(); }
   depth_t GetMaxDepthID() const { return m_impl.GetMaxDepthID(); }
@@ -771,7 +788,10 @@ private:
   {
     if (entities.data() != m_data || entities.size() != m_size || m_boundGeneration != m_generation)
     {
-      detail::check(otg_tree_set_entities(const_cast<otg_tree*>(m_impl.Handle()), entities.data(), entities.size(), OTG_MEM_HOST, m_impl.Stream()));
+      if (m_policy == SpanChange::Rebuild)
+        const_cast<Impl&>(m_impl).Create(entities, m_maxDepth, m_box, m_maxElem);
+      else
+        detail::check(otg_tree_set_entities(const_cast<otg_tree*>(m_impl.Handle()), entities.data(), entities.size(), OTG_MEM_HOST, m_impl.Stream()));
       m_data = entities.data();
       m_size = entities.size();
       m_boundGeneration = m_generation;
@@ -780,6 +800,10 @@ private:
   }
 
   Impl m_impl;
+  std::optional<depth_t> m_maxDepth;
+  std::optional<TBox> m_box;
+  std::size_t m_maxElem = DEFAULT_TARGET_ELEMENT_NUM_IN_NODES;
+  SpanChange m_policy = SpanChange::Rebuild;
   mutable const TEntity* m_data = nullptr;
   mutable std::size_t m_size = 0;
   std::uint64_t m_generation = 0;

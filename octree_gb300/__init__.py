@@ -84,6 +84,7 @@ EXPORTS = [
     ("otg_autotune_enable", _int, [_int]),
     ("otg_autotune_count", _int, []),
     ("otg_autotune_entry", _int, [_int, C.c_char_p, _int]),
+    ("otg_autotune_force_shape", _int, [_int]),
     ("otg_profile_enable", _int, [_int]),
     ("otg_profile_phase_count", _int, []),
     ("otg_profile_phase", _int, [_int, C.c_char_p, _int, C.POINTER(C.c_float)]),
@@ -155,6 +156,12 @@ def device_count():
 
 def autotune_enable(on=True):
     _check(library().otg_autotune_enable(1 if on else 0))
+
+
+def autotune_force_shape(shape):
+    """Runs `shape` in every tuned call that offers it (-1: back to tuning); shapes of the batched
+    query kernels are warps per block (2, 4, 8) | split << 8 (1: no split, 2-4: split depth 1-3)."""
+    _check(library().otg_autotune_force_shape(int(shape)))
 
 
 def autotune_entries():

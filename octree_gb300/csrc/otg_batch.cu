@@ -93,6 +93,7 @@ struct BatchArgs
   QueryProgram<T> qp; // combined queries
   int phase;          // 0: whole queries; 1: top levels, deeper subtrees become items; 2: the items
   u32 splitCap;       // item capacity of the work buffer
+  u32 splitDepth;     // depth of the subtrees that become items
 };
 
 template<typename T, int KIND, int WARPS>
@@ -427,7 +428,7 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
           if (a.phase == 1)
           {
             // subtrees at the split depth become items for any warp
-            const bool defer = keep && tv.nodeDepth[child] >= kSplitDepth;
+            const bool defer = keep && tv.nodeDepth[child] >= a.splitDepth;
             const u32 dbal = __ballot_sync(~0u, defer);
             if (dbal)
             {
@@ -497,9 +498,8 @@ static int launch_batch_w(const BatchArgs<T, KIND>& a, cudaStream_t st)
   return cuda_status(cudaGetLastError(), "launching the batched query kernel");
 }
 
-// shape: warps per block, 2, 4 or 8 (autotuned)
-// workBytes: size of the work buffer; a batch of at most kSplitQueries queries is split when the
-// buffer holds its items (batch_work_bytes)
+// shape: warps per block (2, 4 or 8) | split code << 8 (otg_query.cuh: shape_split_depth), autotuned
+// workBytes: size of the work buffer; a batch is split only when the buffer holds its items
 template<typename T, int KIND>
 static int launch_batch(const BatchArgs<T, KIND>& a0, int shape, cudaStream_t st, size_t workBytes)
 {
@@ -510,10 +510,13 @@ static int launch_batch(const BatchArgs<T, KIND>& a0, int shape, cudaStream_t st
   }
   BatchArgs<T, KIND> a = a0;
   a.phase = 0;
-  a.splitCap = (a.nq <= kSplitQueries && a.tv.nodeDepth && workBytes >= batch_work_bytes(a.nq)) ? a.nq * kSplitItemsPerQuery : 0u;
-  if (shape == 2)
+  a.splitDepth = shape_split_depth(shape, a.nq);
+  const u64 items = a.splitDepth ? u64(a.nq) * split_items_per_query(a.splitDepth) : 0;
+  a.splitCap = (items && a.tv.nodeDepth && workBytes >= 16 + sizeof(u64) * items) ? u32(items) : 0u;
+  const int warps = shape & 0xff;
+  if (warps == 2)
     return launch_batch_w<T, KIND, 2>(a, st);
-  if (shape == 8)
+  if (warps == 8)
     return launch_batch_w<T, KIND, 8>(a, st);
   return launch_batch_w<T, KIND, 4>(a, st);
 }

@@ -592,6 +592,12 @@ extern "C"
 
   int otg_autotune_count(void) { return tune_count(); }
 
+  int otg_autotune_force_shape(int shape)
+  {
+    tune_force(shape);
+    return OTG_OK;
+  }
+
   int otg_autotune_entry(int index, char* text, int capacity)
   {
     if (!text || capacity <= 0 || index < 0 || index >= tune_count())

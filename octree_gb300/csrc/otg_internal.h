@@ -240,6 +240,7 @@ int tune_run(const std::string& key, const std::vector<std::pair<int, const char
              const std::function<int(int)>& launch);
 int tune_lookup(const std::string& key, int fallback);
 void tune_enable(bool on);
+void tune_force(int shape); // -1: none
 int tune_count();
 std::string tune_entry(int i);
 

@@ -1251,15 +1251,27 @@ static int empty_result(u64 nq, ResultState& r, bool dist, cudaStream_t st)
   return cuda_status(e, "empty result");
 }
 
-// shapes of the batched query kernels: 0 = one query per thread, 2/4/8 = warps per block of the
-// warp-per-query kernel. OTG_ALGO_DEFAULT lets the autotuner choose among all of them,
-// OTG_ALGO_FILTERED among the warp shapes.
-static std::vector<std::pair<int, const char*>> query_shapes(int algo)
+// shapes of the batched query kernels: 0 = one query per thread; else warps per block (2, 4, 8) of
+// the warp-per-query kernel | split code << 8 (no split, or the subtrees at depth 1, 2 or 3 become
+// work items; otg_query.cuh). OTG_ALGO_DEFAULT lets the autotuner choose among all of them,
+// OTG_ALGO_FILTERED among the warp shapes; the split depths offered depend on the batch size.
+static std::vector<std::pair<int, const char*>> query_shapes(int algo, u64 nq)
 {
+  static const char* names[3][4] = { { "warp x2", "warp x2 split 1", "warp x2 split 2", "warp x2 split 3" },
+                                     { "warp x4", "warp x4 split 1", "warp x4 split 2", "warp x4 split 3" },
+                                     { "warp x8", "warp x8 split 1", "warp x8 split 2", "warp x8 split 3" } };
+  std::vector<std::pair<int, const char*>> out;
   if (algo == OTG_ALGO_DEFAULT)
-    return { { 0, "thread" }, { 2, "warp x2" }, { 4, "warp x4" }, { 8, "warp x8" } };
-  return { { 2, "warp x2" }, { 4, "warp x4" }, { 8, "warp x8" } };
+    out.push_back({ 0, "thread" });
+  const u32 maxDepth = split_depth_limit(nq);
+  const int warps[3] = { 2, 4, 8 };
+  for (int w = 0; w < 3; ++w)
+    for (u32 d = 0; d <= maxDepth; ++d)
+      out.push_back({ warps[w] | int((d + 1) << 8), names[w][d] });
+  return out;
 }
+// the shape used when the autotuner is off: 4 warps, the default split
+constexpr int kDefaultQueryShape = 4;
 
 
 template<typename T>
@@ -1285,7 +1297,7 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
       if (algo == OTG_ALGO_PLAIN_FP64)
         range_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), mode, tl, a, err);
       else
-        launchRc = tune_run(query_key("range", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st, [&](int shape) {
+        launchRc = tune_run(query_key("range", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo, nq), kDefaultQueryShape, st, [&](int shape) {
           cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
           cudaMemsetAsync(err, 0, sizeof(u32), st);
           if (shape == 0)
@@ -1326,7 +1338,7 @@ static int pick_impl(const TreeState& t, const void* pts, u64 nq, double tol, in
       if (algo == OTG_ALGO_PLAIN_FP64)
         pick_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, a, err);
       else
-        launchRc = tune_run(query_key("pick", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st, [&](int shape) {
+        launchRc = tune_run(query_key("pick", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo, nq), kDefaultQueryShape, st, [&](int shape) {
           cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
           cudaMemsetAsync(err, 0, sizeof(u32), st);
           if (shape == 0)
@@ -1368,7 +1380,7 @@ static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, 
       if (algo == OTG_ALGO_PLAIN_FP64)
         frustum_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(np), u32(nq), tl, a, err);
       else
-        launchRc = tune_run(query_key("frustum", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st, [&](int shape) {
+        launchRc = tune_run(query_key("frustum", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo, nq), kDefaultQueryShape, st, [&](int shape) {
           cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
           cudaMemsetAsync(err, 0, sizeof(u32), st);
           if (shape == 0)
@@ -1410,7 +1422,7 @@ static int plane_impl(const TreeState& t, const void* planes, u64 nq, bool posit
       if (algo == OTG_ALGO_PLAIN_FP64)
         plane_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), positive ? 1 : 0, tl, a, err);
       else
-        launchRc = tune_run(query_key(positive ? "plane positive" : "plane", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st,
+        launchRc = tune_run(query_key(positive ? "plane positive" : "plane", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo, nq), kDefaultQueryShape, st,
                             [&](int shape) {
                               cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
                               cudaMemsetAsync(err, 0, sizeof(u32), st);
@@ -1505,7 +1517,7 @@ static int query_impl(const TreeState& t, const QueryCond* conds, const u64* off
       if (algo == OTG_ALGO_PLAIN_FP64)
         query_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, qp, u32(nq), tl, a, err);
       else
-        launchRc = tune_run(query_key(orOp ? "query or" : "query and", algo, false, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st,
+        launchRc = tune_run(query_key(orOp ? "query or" : "query and", algo, false, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo, nq), kDefaultQueryShape, st,
                             [&](int shape) {
                               cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
                               cudaMemsetAsync(err, 0, sizeof(u32), st);
@@ -1600,7 +1612,7 @@ static int ray_impl(const TreeState& t, const void* rays, u64 nq, double tol, do
         if (algo == OTG_ALGO_PLAIN_FP64)
           ray_all_plain_kernel<T><<<u32((nq + 127) / 128), 128, 0, st>>>(tv, (const T*)d, u32(nq), tl, ti, md, a, err);
         else
-          launchRc = tune_run(query_key("ray all", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo), 4, st, [&](int shape) {
+          launchRc = tune_run(query_key("ray all", algo, qTree, sizeof(T) == 8, t.kind, t.n, nq), query_shapes(algo, nq), kDefaultQueryShape, st, [&](int shape) {
             cudaMemsetAsync(a.count, 0, sizeof(unsigned long long), st);
             cudaMemsetAsync(err, 0, sizeof(u32), st);
             if (shape == 0)

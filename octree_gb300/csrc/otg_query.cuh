@@ -304,15 +304,31 @@ static inline T tol_of(double tol)
 template<typename T>
 int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4, size_t workBytes = 0);
 // Work buffer of the batched kernels: four counters, then the (query, subtree) items of a split
-// batch. A batch of at most kSplitQueries queries is split: each query runs its top levels, and the
-// subtrees at depth kSplitDepth it enters become items that any warp takes, so that a few costly
-// queries (large trees of a forest, wide frusta) spread over the whole GPU.
+// batch. A split batch runs in two launches: each query runs its levels above the split depth, and
+// the subtrees at the split depth that it enters become items that any warp takes, so that a few
+// costly queries (large trees of a forest, wide frusta) spread over the whole GPU.
+// The split depth is part of a batched kernel's shape (shape = warps per block | code << 8):
+//   code 0: the default, depth 2 for batches of at most kSplitQueries queries, else no split;
+//   code 1: no split; code 2, 3, 4: split depth 1, 2, 3.
+// The autotuner chooses among the depths that the batch's size allows (split_depth_limit).
 constexpr u32 kSplitQueries = 8192;
-constexpr u32 kSplitDepth = 2;
-constexpr u32 kSplitItemsPerQuery = 1u << (3 * kSplitDepth);
+constexpr u32 kSplitDefaultDepth = 2;
+constexpr u32 kSplitMaxQueries = 65536;
+inline u64 split_items_per_query(u32 depth) { return u64(1) << (3 * depth); }
+// deepest split a batch of nq queries may use (its items fit 32 MB): 3 up to 8192 queries, 2 up to
+// 65536, else none
+inline u32 split_depth_limit(u64 nq) { return nq <= kSplitQueries ? 3u : nq <= kSplitMaxQueries ? 2u : 0u; }
 inline size_t batch_work_bytes(u64 nq)
 {
-  return 16 + (nq <= kSplitQueries ? sizeof(u64) * kSplitItemsPerQuery * nq : 0);
+  const u32 d = split_depth_limit(nq);
+  return 16 + (d ? sizeof(u64) * split_items_per_query(d) * nq : 0);
+}
+// split depth (0: none) of a shape for a batch of nq queries
+inline u32 shape_split_depth(int shape, u64 nq)
+{
+  const int code = shape >> 8;
+  const u32 d = code == 0 ? (nq <= kSplitQueries ? kSplitDefaultDepth : 0u) : u32(code - 1);
+  return d <= split_depth_limit(nq) ? d : 0u;
 }
 template<typename T>
 int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape = 4, size_t workBytes = 0);

@@ -5,7 +5,9 @@
 // sort is unstable, this one is stable, so equal keys keep ascending entity id).
 //
 // Per pass, every CTA takes the next tile id from a counter (so tiles start in launch order),
-// counts its 4096 keys per digit and publishes the counts, ranks the keys stably with warp
+// receives its tile's keys and values by bulk copies (cp.async.bulk into shared memory, completion
+// on an mbarrier; plain loads for a partial tile), counts its 4096 keys per digit and publishes the
+// counts, ranks the keys stably with warp
 // ballots, looks back over earlier tiles' published counts (decoupled look-back) to get its global
 // offsets, stages the tile in shared memory in digit order and writes it out in runs. Look-back spins are bounded:
 // on timeout the CTA sets an error bit and finishes, so a broken invariant can never hang the GPU.
@@ -32,6 +34,53 @@ constexpr u32 kErrTimeout = 1u;
 constexpr u32 kErrCapacity = 2u;
 constexpr u32 kErrStack = 4u;
 constexpr u32 kErrArgument = 8u; // an input index out of range (reported, never followed)
+
+// ---- bulk copies (cp.async.bulk) into shared memory, completing on an mbarrier
+constexpr u32 kCopySpinLimit = 1u << 20; // mbarrier polls for one tile's bulk copies
+
+__device__ __forceinline__ u32 smem_addr(const void* p) { return u32(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init(u64* bar, u32 count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(u64* bar, u32 bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+// true once the phase of the given parity has completed
+__device__ __forceinline__ bool mbar_try_wait(u64* bar, u32 parity)
+{
+  u32 done;
+  asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+               : "=r"(done)
+               : "r"(smem_addr(bar)), "r"(parity)
+               : "memory");
+  return done != 0;
+}
+
+// bulk copy global -> this CTA's shared memory (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, u32 bytes, u64* bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)), "l"(src), "r"(bytes),
+               "r"(smem_addr(bar))
+               : "memory");
+}
+
+// orders this thread's earlier generic-proxy shared-memory accesses before later bulk copies
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// bounded wait for the phase `parity` of bar, by every thread; false on timeout
+__device__ __forceinline__ bool mbar_wait_bounded(u64* bar, u32 parity)
+{
+  for (u32 spins = 0; spins < kCopySpinLimit; ++spins)
+    if (mbar_try_wait(bar, parity))
+      return true;
+  return false;
+}
 
 __device__ __forceinline__ u32 lanemask_lt()
 {
@@ -128,10 +177,18 @@ __global__ void __launch_bounds__(kSortThreads, 3) onesweep_pass_kernel(const K*
   __shared__ u32 s_globalBase[kRadix];
   __shared__ u32 s_scan[kSortWarps];
   __shared__ u32 s_tile;
+  __shared__ __align__(8) u64 s_bar; // completion of the tile's bulk copies
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0)
+  {
     s_tile = atomicAdd(tileCounter, 1u);
+    if constexpr (!SEG && !DEVN)
+    {
+      mbar_init(&s_bar, 1);
+      fence_mbar_init();
+    }
+  }
   for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads)
     (&s_cnt[0][0])[i] = 0;
   __syncthreads();
@@ -159,13 +216,45 @@ __global__ void __launch_bounds__(kSortThreads, 3) onesweep_pass_kernel(const K*
   u32 vals[kSortItems];
   u32 dig[kSortItems];
   const u32 wbase = base + u32(warp) * (32 * kSortItems);
+  // A whole tile of the single sort arrives by bulk copies (16-byte aligned: tiles start at
+  // multiples of 4096 elements of buffers from cudaMalloc) into the staging area, which takes the
+  // digit-ordered tile later; a partial last tile and the segmented / device-count forms read
+  // global memory directly. One load loop serves both through generic pointers.
+  const K* ksrc = kin + wbase;
+  const u32* vsrc = vin ? vin + wbase : nullptr;
+  if constexpr (!SEG && !DEVN)
+  {
+    if (u64(base) + kSortTile <= u64(segEnd))
+    {
+      if (tid == 0)
+      {
+        const u32 bytes = u32(sizeof(K) * kSortTile) + (vin ? u32(sizeof(u32) * kSortTile) : 0u);
+        mbar_arrive_expect_tx(&s_bar, bytes);
+        bulk_load(s_keys, kin + base, u32(sizeof(K) * kSortTile), &s_bar);
+        if (vin)
+          bulk_load(s_vals, vin + base, u32(sizeof(u32) * kSortTile), &s_bar);
+      }
+      // every thread waits on the mbarrier, which makes the copied bytes visible to it; copies that
+      // do not complete in time leave the tile unsorted (the error bit fails the sort)
+      const bool ok = mbar_wait_bounded(&s_bar, 0);
+      if (__syncthreads_or(!ok))
+      {
+        if (tid == 0)
+          atomicOr(err, kErrTimeout);
+        mbar_wait_bounded(&s_bar, 0); // the copies land before this CTA's shared memory goes away
+        return;
+      }
+      ksrc = s_keys + (wbase - base);
+      vsrc = vin ? s_vals + (wbase - base) : nullptr;
+    }
+  }
 #pragma unroll
   for (int i = 0; i < kSortItems; ++i)
   {
     const u32 idx = wbase + i * 32 + lane;
     const bool valid = idx < segEnd;
-    keys[i] = valid ? kin[idx] : K(0);
-    vals[i] = vin ? (valid ? vin[idx] : 0u) : idx;
+    keys[i] = valid ? ksrc[i * 32 + lane] : K(0);
+    vals[i] = vsrc ? (valid ? vsrc[i * 32 + lane] : 0u) : idx;
     dig[i] = valid ? u32((keys[i] >> shift) & (kRadix - 1)) : u32(kRadix);
   }
 #pragma unroll

@@ -33,51 +33,6 @@ constexpr int kChunkWarps = kChunkThreads / 32;
 constexpr int kChunkMaxGrid = 512;   // the column scan gives one chunk per thread
 constexpr int kChunkMaxBits = 11;    // widest digit
 constexpr u32 kGridSpinLimit = 1u << 22;  // grid barrier spins (each with a short sleep)
-constexpr u32 kCopySpinLimit = 1u << 20;  // mbarrier polls for one tile's bulk copies
-
-__device__ __forceinline__ u32 smem_addr(const void* p) { return u32(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ void mbar_init(u64* bar, u32 count)
-{
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(u64* bar, u32 bytes)
-{
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-}
-
-// true once the phase of the given parity has completed
-__device__ __forceinline__ bool mbar_try_wait(u64* bar, u32 parity)
-{
-  u32 done;
-  asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
-               : "=r"(done)
-               : "r"(smem_addr(bar)), "r"(parity)
-               : "memory");
-  return done != 0;
-}
-
-// bulk copy global -> this CTA's shared memory (16-byte aligned addresses, size a multiple of 16)
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, u32 bytes, u64* bar)
-{
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)), "l"(src), "r"(bytes),
-               "r"(smem_addr(bar))
-               : "memory");
-}
-
-// orders this thread's earlier generic-proxy shared-memory accesses before later bulk copies
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-
-// bounded wait for the phase `parity` of bar, by every thread; false on timeout
-__device__ __forceinline__ bool mbar_wait_bounded(u64* bar, u32 parity)
-{
-  for (u32 spins = 0; spins < kCopySpinLimit; ++spins)
-    if (mbar_try_wait(bar, parity))
-      return true;
-  return false;
-}
 
 // Grid barrier of a co-resident grid: arrival count `target` (monotonic counter per pass).
 // Returns false (and sets the error bit) when the other CTAs do not arrive in time.

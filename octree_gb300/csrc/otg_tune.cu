@@ -20,6 +20,7 @@ struct TuneEntry
 {
   std::string key;
   int best = 0;
+  std::string bestName;
   std::vector<std::pair<std::string, float>> timings;
 };
 
@@ -27,6 +28,7 @@ struct Tuner
 {
   std::mutex m;
   bool enabled = true;
+  int forced = -1; // a shape every call that offers it runs (diagnostics)
   std::map<std::string, size_t> index;
   std::vector<TuneEntry> entries;
 };
@@ -62,6 +64,10 @@ int tune_run(const std::string& key, const std::vector<std::pair<int, const char
   Tuner& T = tuner();
   {
     std::lock_guard<std::mutex> g(T.m);
+    if (T.forced >= 0)
+      for (const auto& c : cands)
+        if (c.first == T.forced)
+          return launch(T.forced);
     if (!T.enabled || cands.size() < 2)
       return launch(cands.size() == 1 ? cands[0].first : fallback);
     auto it = T.index.find(key);
@@ -105,6 +111,7 @@ int tune_run(const std::string& key, const std::vector<std::pair<int, const char
     {
       bestMs = ms;
       best = c.first;
+      entry.bestName = c.second;
     }
   }
   cudaEventDestroy(a);
@@ -128,6 +135,12 @@ int tune_lookup(const std::string& key, int fallback)
   std::lock_guard<std::mutex> g(tuner().m);
   auto it = tuner().index.find(key);
   return it == tuner().index.end() ? fallback : tuner().entries[it->second].best;
+}
+
+void tune_force(int shape)
+{
+  std::lock_guard<std::mutex> g(tuner().m);
+  tuner().forced = shape;
 }
 
 void tune_enable(bool on)
@@ -156,9 +169,7 @@ std::string tune_entry(int i)
     std::snprintf(buf, sizeof(buf), " %s %.3f ms", t.first.c_str(), t.second);
     s += buf;
   }
-  char buf[32];
-  std::snprintf(buf, sizeof(buf), " -> %d", en.best);
-  s += buf;
+  s += " -> " + en.bestName;
   return s;
 }
 

@@ -267,9 +267,9 @@ int main()
   {
     std::vector<Point3D> span1(pts.begin(), pts.begin() + 30000);
     OctreePoint tc(std::span<const Point3D>(span1), 8, std::nullopt, 20);
-    void* oc = oro_create(0, 0, span1.data(), span1.size(), 8, nullptr, 20);
+    // the span's tree, as the oracle builds it; kNN, range and pick of the Core type against it
     auto check_span = [&](std::span<const Point3D> span, const char* what) {
-      oro_set_entities(oc, span.data(), span.size());
+      void* oc = oro_create(0, 0, span.data(), span.size(), 8, nullptr, 20);
       void* r = oro_range(oc, ranges.data(), nq, 0, -1.0);
       for (int i = 0; i < nq; ++i)
         expect(tc.RangeSearch(ranges[i], span), r, i, what);
@@ -283,9 +283,10 @@ int main()
       for (int i = 0; i < nq; ++i)
         expect(tc.PickSearch(qp[i], span), r, i, what);
       oro_res_free(r);
+      oro_destroy(oc);
     };
     check_span(span1, "Core: the Create span");
-    // another span of the same size: the nodes stay, the new geometry is tested
+    // another span (SpanChange::Rebuild, the default): the tree of that span
     std::vector<Point3D> span2(span1);
     for (std::size_t i = 0; i < span2.size(); i += 3)
       for (int c = 0; c < 3; ++c)
@@ -296,29 +297,44 @@ int main()
       span1[i][0] += 1.3;
     tc.NotifyEntitiesChanged();
     check_span(span1, "Core: span changed in place");
-    // a span of another size does not fit the nodes
-    bool refused = false;
-    try
+    // SpanChange::KeepNodes: the nodes of the last Create stay and the new geometry is tested, as the
+    // reference answers with a span other than its Create's (queries that test a fixed set of nodes)
     {
-      tc.RangeSearch(ranges[0], std::span<const Point3D>(span1.data(), span1.size() - 1));
+      OctreePoint tk(std::span<const Point3D>(span1), 8, std::nullopt, 20);
+      tk.SetSpanChange(OctreePoint::SpanChange::KeepNodes);
+      void* ok = oro_create(0, 0, span1.data(), span1.size(), 8, nullptr, 20);
+      oro_set_entities(ok, span2.data(), span2.size());
+      void* r = oro_range(ok, ranges.data(), nq, 0, -1.0);
+      for (int i = 0; i < nq; ++i)
+        expect(tk.RangeSearch(ranges[i], std::span<const Point3D>(span2)), r, i, "Core KeepNodes: RangeSearch");
+      oro_res_free(r);
+      r = oro_pick(ok, qp.data(), nq, -1.0);
+      for (int i = 0; i < nq; ++i)
+        expect(tk.PickSearch(qp[i], std::span<const Point3D>(span2)), r, i, "Core KeepNodes: PickSearch");
+      oro_res_free(r);
+      oro_destroy(ok);
+      // a span of another size does not fit the nodes
+      bool refused = false;
+      try
+      {
+        tk.RangeSearch(ranges[0], std::span<const Point3D>(span1.data(), span1.size() - 1));
+      }
+      catch (const Error& e)
+      {
+        refused = e.status() == OTG_ERR_INVALID_ARGUMENT;
+      }
+      if (!refused)
+      {
+        std::printf("MISMATCH Core KeepNodes: a span of another size was not refused\n");
+        ++g_fail;
+      }
     }
-    catch (const Error& e)
-    {
-      refused = e.status() == OTG_ERR_INVALID_ARGUMENT;
-    }
-    if (!refused)
-    {
-      std::printf("MISMATCH Core: a span of another size was not refused\n");
-      ++g_fail;
-    }
-    oro_destroy(oc);
     // box trees: collisions with the span, and the two-tree form
     std::vector<BoundingBox3D> bspan(boxes.begin(), boxes.begin() + 8000);
     OctreeBox tbc(std::span<const BoundingBox3D>(bspan), 7, std::nullopt, 16);
     OctreeBox tbo;
     std::vector<BoundingBox3D> ospan(boxes.begin() + 8000, boxes.begin() + 12000);
     OctreeBox::Create(tbo, std::span<const BoundingBox3D>(ospan), 6, std::nullopt, 12);
-    void* obc = oro_create(0, 1, bspan.data(), bspan.size(), 7, nullptr, 16);
     void* obo = oro_create(0, 1, ospan.data(), ospan.size(), 6, nullptr, 12);
     auto flat = [](const std::vector<std::pair<EntityID, EntityID>>& p) {
       std::vector<uint32_t> v;
@@ -331,6 +347,7 @@ int main()
     };
     for (int round = 0; round < 2; ++round)
     {
+      void* obc = oro_create(0, 1, bspan.data(), bspan.size(), 7, nullptr, 16);
       void* r = oro_collide_self(obc, -1.0);
       expect(flat(tbc.CollisionDetection(std::span<const BoundingBox3D>(bspan))), r, 0, "Core: CollisionDetection");
       oro_res_free(r);
@@ -338,7 +355,8 @@ int main()
       expect(flat(OctreeBox::CollisionDetection(tbc, std::span<const BoundingBox3D>(bspan), tbo, std::span<const BoundingBox3D>(ospan))), r, 0,
              "Core: CollisionDetection(two trees)");
       oro_res_free(r);
-      // move some boxes of the first span (same size): the next round tests the new geometry
+      oro_destroy(obc);
+      // move some boxes of the first span in place: the next round answers for the moved span
       for (std::size_t i = 0; i < bspan.size(); i += 4)
         for (int c = 0; c < 3; ++c)
         {
@@ -346,9 +364,7 @@ int main()
           bspan[i].Max[c] += 0.5;
         }
       tbc.NotifyEntitiesChanged();
-      oro_set_entities(obc, bspan.data(), bspan.size());
     }
-    oro_destroy(obc);
     oro_destroy(obo);
   }
   if (g_fail)

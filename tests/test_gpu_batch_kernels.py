@@ -1,7 +1,7 @@
 """The batched warp-per-query kernels (default algorithm) against the one-query-per-thread kernels
 (OTG_ALGO_PLAIN_FP64) for RangeSearch, FrustumCulling, RayIntersectedAll and PickSearch: identical id lists and
 ray distances, on point and box trees of both scalar types and on a forest. Batches of at most
-8192 queries run split (top levels per query, then their depth-2 subtrees as separate work items);
+8192 queries run split by default (top levels per query, then their depth-2 subtrees as separate work items);
 larger ones run whole, and both sizes are covered. (Both kernels are checked against the oracle by
 the parity tests; this pins them to each other on larger inputs.)"""
 import numpy as np
@@ -72,3 +72,28 @@ def test_batch_kernels_match_plain_on_forest():
         assert_csr_equal(f.range_search(ranges, qoff, mode), f.range_search(ranges, qoff, mode, algo=otg.ALGO_PLAIN_FP64), f"forest range {mode}")
     assert_csr_equal(f.frustum_culling(planes, poff)[:2], f.frustum_culling(planes, poff, algo=otg.ALGO_PLAIN_FP64)[:2], "forest frustum")
     assert_csr_equal(f.ray_all(rays, qoff), f.ray_all(rays, qoff, algo=otg.ALGO_PLAIN_FP64), "forest ray_all")
+
+
+@pytest.mark.parametrize("split", [1, 2, 3, 4])
+@pytest.mark.parametrize("warps", [2, 8])
+def test_every_split_depth_matches_plain(warps, split):
+    """Each shape the autotuner chooses among (warps per block, and no split or the subtrees at depth
+    1-3 as separate work items) gives the plain kernel's results, on a point and a box tree, for a
+    batch that allows every split depth and one that allows depths 1-2 only."""
+    rng = np.random.default_rng(113)
+    n = 120_000
+    c = rng.random((n, 3)) * 100
+    e = rng.uniform(0.05, 1.0, (n, 3))
+    boxes = np.concatenate([c - e, c + e], 1)
+    trees = [otg.Tree("points").create(c, max_depth=8, max_elements=20), otg.Tree("boxes").create(boxes, max_depth=8, max_elements=20)]
+    otg.autotune_force_shape(warps | (split << 8))
+    try:
+        for nq in (2000, 20_000):
+            ranges, rays, planes = _inputs(rng, nq, np.float64)
+            for t in trees:
+                ref = t.range_search(ranges, otg.RANGE_OVERLAP, algo=otg.ALGO_PLAIN_FP64)
+                assert_csr_equal(t.range_search(ranges, otg.RANGE_OVERLAP), ref, f"range nq={nq}")
+                assert_csr_equal(t.frustum_culling(planes)[:2], t.frustum_culling(planes, algo=otg.ALGO_PLAIN_FP64)[:2], f"frustum nq={nq}")
+                assert_csr_equal(t.ray_all(rays), t.ray_all(rays, algo=otg.ALGO_PLAIN_FP64), f"ray_all nq={nq}")
+    finally:
+        otg.autotune_force_shape(-1)

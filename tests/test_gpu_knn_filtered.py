@@ -121,3 +121,38 @@ def test_filtered_device_inputs_and_rebuild():
     t.create(pts2, max_depth=9, max_elements=20)
     o2 = oracle().create(pts2, KIND_POINTS, 9, None, 20)
     assert_csr_equal(t.knn(q, k), o2.knn(q, k), "after rebuild")
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("layout", ["far_offset", "near_ties"])
+def test_filtered_margin_at_large_coordinates(dtype, layout):
+    """The FP32 filter's margins where an FP32 ulp approaches the gap at the k-th distance:
+    coordinates around 1e6-1e7 (an FP32 ulp there is 0.06-1), and (near_ties) query points whose
+    neighbours lie at distances differing by about one FP32 ulp of the coordinates. Filtered,
+    plain and oracle agree id for id and distance for distance."""
+    rng = np.random.default_rng(91)
+    n = 200_000
+    if layout == "far_offset":
+        # a cube of side 100 placed at 2.5e6 .. 7.5e6 + 100, points on a 1/16 lattice with jitter
+        # (many near-equal distances)
+        base = np.array([5.0e6, 7.5e6, 2.5e6])
+        pts = base + np.round(rng.random((n, 3)) * 1600) / 16 + rng.normal(0, 1e-3, (n, 3))
+        q = base + rng.random((2000, 3)) * 100
+    else:
+        # per query, 100 points at radius 3 +- up to one FP32 ulp of 8e6 around it
+        base = 8.0e6
+        c = base + rng.random((2000, 3)) * 1000
+        dirs = rng.normal(size=(2000, 100, 3))
+        dirs /= np.linalg.norm(dirs, axis=2, keepdims=True)
+        r = 3.0 + rng.integers(-2, 3, (2000, 100, 1)) * float(np.spacing(np.float32(base))) * 0.5
+        pts = (c[:, None, :] + dirs * r).reshape(-1, 3)
+        q = c
+    pts = pts.astype(dtype)
+    q = q.astype(dtype)
+    k = np.random.default_rng(92).integers(1, 33, len(q)).astype(np.uint32)
+    t = otg.Tree("points", dtype).create(pts, max_depth=10, max_elements=20)
+    o = oracle().create(pts, KIND_POINTS, 10, None, 20)
+    f, p = _both(t, q, k)
+    ref = o.knn(q, k)
+    assert_csr_equal(p, ref, "plain vs oracle")
+    assert_csr_equal(f, ref, "filtered vs oracle")

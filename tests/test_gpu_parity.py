@@ -525,10 +525,10 @@ def test_sort_sizes_and_digit_widths(n, kind, depth):
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("device_span", [False, True])
 def test_core_form_set_entities(kind, dtype, device_span):
-    """The Core form (otg_tree_set_entities): a tree created from one span answers with another span
-    of the same size as the reference's Core queries do (the oracle pins that against the
-    reference in test_oracle_vs_reference.py), then with the first span again; a span of another
-    size is refused."""
+    """The Core form's entity span (otg_tree_set_entities): a tree created from one span answers with
+    another span of the same size as the reference's Core queries do, for the queries that test a
+    fixed set of nodes (the oracle pins that against the reference in test_oracle_vs_reference.py),
+    then answers every query with a copy of its Create span; a span of another size is refused."""
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(71 + kind)
     n = 60_000
@@ -542,11 +542,24 @@ def test_core_form_set_entities(kind, dtype, device_span):
     o = oracle().create(ent, kind, 8, None, 12)
     qs = _queries(rng, dtype, 10, nq=300)
     new = moved_span(ent, rng, kind != KIND_POINTS)
-    for span in (new, ent):
-        t.set_entities(torch.as_tensor(span, device="cuda") if device_span else span)
-        o.set_entities(span)
-        _check_queries(t, o, qs, kind, 0.05, f"core span kind={kind}")
-        if kind != KIND_POINTS:
-            assert np.array_equal(t.collision_self(), o.collide_self())
+    # a moved span: the queries that test a fixed set of nodes and entities (where entities left
+    # the nodes they were built into, the reference's kNN, first-hit and collision answers depend
+    # on the order of its own traversal)
+    t.set_entities(torch.as_tensor(new, device="cuda") if device_span else new)
+    o.set_entities(new)
+    for mode in (0, 1):
+        assert_csr_equal(t.range_search(qs["ranges"], mode)[:2], o.range_search(qs["ranges"], mode), f"moved span range{mode}")
+    assert_csr_equal(t.pick_search(qs["qpts"])[:2], o.pick_search(qs["qpts"]), "moved span pick")
+    assert_csr_equal(t.frustum_culling(qs["planes"])[:2], o.frustum(qs["planes"]), "moved span frustum")
+    g = t.ray_all(qs["rays"], tol=0.05)
+    r = o.ray(qs["rays"], first=False, tol=0.05)
+    assert_csr_equal(g[:2], r[:2], "moved span ray all")
+    assert_dist_close(g[2], r[2], RAY_REL, "moved span ray all")
+    # the Create span again (a copy: another pointer, the same geometry): every query
+    t.set_entities(torch.as_tensor(ent.copy(), device="cuda") if device_span else ent.copy())
+    o.set_entities(ent)
+    _check_queries(t, o, qs, kind, 0.05, f"core span kind={kind}")
+    if kind != KIND_POINTS:
+        assert np.array_equal(t.collision_self(), o.collide_self())
     with pytest.raises(otg.OtgError):
         t.set_entities(ent[:-1])
