@@ -1065,6 +1065,201 @@ public:
     return true;
   }
 
+  // ------------------------------------------------------------------ bulk Insert (point trees)
+  // ot_dynamic_hash_core.h:1012-1333 Insert(newEntities, existingEntities) for OctreePoint (location
+  // depth is not element specific: LowestCommonAncestorCalculator<false>, no stuck entities), then
+  // LinkOrphanNodes (:826-863); MinPoint trees need no geometry update (UpdateNodeGeometry, :866-1005,
+  // only unites MBRs). New entity i gets id N + i.
+  // The reference partitions its buffer in place (MSD radix partition, 9-bit digits, :1102-1199) and
+  // sorts ranges of at most 256 (:1310-1320). Every bucket is a run of the buffer sorted by location,
+  // and a bucket's fold (the lowest common ancestor of its locations, :1153-1191) and a walk's
+  // clusters depend only on the locations of the run, so this restatement sorts the buffer once
+  // (ties by id) and runs the same work stack (LIFO, buckets pushed in ascending digit order) over it.
+  // Returns false without inserting anything when a new point lies outside the tree's space (the
+  // reference would give it the root's location with a code of 0).
+  static u64 node_lca(u64 a, u64 b) // si_morton.h:307-325
+  {
+    if (a == b)
+      return a;
+    const u32 da = key_depth(a), db = key_depth(b);
+    if (da > db)
+      a >>= 3 * (da - db);
+    else if (db > da)
+      b >>= 3 * (db - da);
+    const u32 levels = u32((std::bit_width(a ^ b) + 2) / 3);
+    return a >> (3 * levels);
+  }
+  static u32 nondirect_child_id(u64 parent, u64 child) // si_morton.h:651-658
+  {
+    return u32((child >> (3 * (key_depth(child) - key_depth(parent) - 1))) & 7u);
+  }
+  // LinkChild with a non-direct child: the child of `slot` becomes `child` (children kept in slot order)
+  void link_child(Node& p, u64 child)
+  {
+    const u32 slot = nondirect_child_id(p.key, child);
+    for (auto& c : p.children)
+      if (nondirect_child_id(p.key, c) == slot)
+      {
+        c = child;
+        return;
+      }
+    p.children.push_back(child);
+    std::sort(p.children.begin(), p.children.end(), [&](u64 a, u64 b) { return nondirect_child_id(p.key, a) < nondirect_child_id(p.key, b); });
+  }
+  u64 child_in_slot(const Node& p, u32 slot) const
+  {
+    for (u64 c : p.children)
+      if (nondirect_child_id(p.key, c) == slot)
+        return c;
+    return 0;
+  }
+
+  bool insert_points(const T* ent, size_t n2)
+  {
+    if (isBox)
+      return false;
+    if (n2 == 0)
+      return true;
+    std::vector<u64> keys(n2);
+    for (size_t i = 0; i < n2; ++i)
+    {
+      keys[i] = rasterDouble ? location_key<double>(ent + 3 * i, rsizeD, rastD) : location_key<float>(ent + 3 * i, rsizeF, rastF);
+      if (key_loc_depth(keys[i]) != D)
+        return false;
+    }
+    std::vector<std::pair<u64, u32>> buf(n2); // (location code, entity id)
+    for (size_t i = 0; i < n2; ++i)
+      buf[i] = { key_loc(keys[i]), u32(N + i) };
+    geom.insert(geom.end(), ent, ent + 3 * n2);
+    locationKeys.insert(locationKeys.end(), keys.begin(), keys.end());
+    N += n2;
+    std::sort(buf.begin(), buf.end());
+
+    constexpr u32 kRadixBits = 9, kSortThreshold = 256; // :1097-1099, :1028
+    auto fold_depth = [&](u64 diff) { return std::min(D, D - u32((std::bit_width(diff) + 2) / 3)); };
+    std::vector<u64> orphans;
+    // emitCluster (:1203-1234): the entities join the node of the location, created if missing
+    auto emit = [&](size_t b, size_t e, u64 loc, u32 depth) {
+      if (e == b)
+        return;
+      const u64 key = (u64(1) << (3 * depth)) | (loc >> (3 * (D - depth)));
+      auto [it, inserted] = nodes.try_emplace(key);
+      if (inserted)
+      {
+        it->second.key = key;
+        init_min_point(it->second);
+        orphans.push_back(key);
+      }
+      for (size_t i = b; i < e; ++i)
+        it->second.entities.push_back(buf[i].second);
+    };
+    // emitSortedRange (:1237-1291): greedy clusters over a sorted run
+    auto walk = [&](size_t b, size_t e) {
+      size_t cb = b;
+      while (cb < e)
+      {
+        const u64 base = buf[cb].first;
+        u64 diff = 0;
+        size_t ce = cb + 1;
+        while (ce < e)
+        {
+          const u64 nd = diff | (base ^ buf[ce].first);
+          const u32 newDepth = fold_depth(nd);
+          if (ce - cb + 1 > maxElem && newDepth < D && newDepth < fold_depth(diff))
+            break;
+          diff = nd;
+          ++ce;
+        }
+        emit(cb, ce, base, fold_depth(diff));
+        cb = ce;
+      }
+    };
+    struct Work
+    {
+      size_t b, e;
+      u32 bits;
+      u64 loc;
+      u32 depth;
+    };
+    std::vector<Work> stack{ { 0, n2, 3 * D, 0, 0 } }; // the root location (:1295)
+    while (!stack.empty())
+    {
+      const Work w = stack.back();
+      stack.pop_back();
+      const size_t num = w.e - w.b;
+      if (num == 0)
+        continue;
+      if (num <= maxElem) // :1304-1308
+      {
+        emit(w.b, w.e, w.loc, w.depth);
+        continue;
+      }
+      if (num <= kSortThreshold || w.bits == 0) // :1310-1317
+      {
+        walk(w.b, w.e);
+        continue;
+      }
+      // radixPartition (:1153-1199): buckets of the next min(9, bits) bits, each with its fold
+      const u32 numBits = std::min(kRadixBits, w.bits);
+      const u32 shift = w.bits - numBits;
+      const u64 mask = (u64(1) << numBits) - 1;
+      size_t bb = w.b;
+      while (bb < w.e)
+      {
+        const u64 dig = (buf[bb].first >> shift) & mask;
+        size_t be = bb + 1;
+        u64 diff = 0;
+        while (be < w.e && ((buf[be].first >> shift) & mask) == dig)
+        {
+          diff |= buf[bb].first ^ buf[be].first;
+          ++be;
+        }
+        const u32 depth = fold_depth(diff);
+        stack.push_back({ bb, be, std::min((D - depth) * 3, shift), buf[bb].first, depth });
+        bb = be;
+      }
+    }
+
+    // LinkOrphanNodes (:826-863)
+    for (size_t i = 0; i < orphans.size(); ++i)
+    {
+      const u64 o = orphans[i];
+      u64 pk = o >> 3; // GetParentIt (:1379-1390): the nearest ancestor in the node map
+      while (pk > 1 && !nodes.count(pk))
+        pk >>= 3;
+      Node& parent = nodes.at(pk);
+      const u64 c = child_in_slot(parent, nondirect_child_id(pk, o));
+      if (!c)
+      {
+        link_child(parent, o);
+        continue;
+      }
+      const u64 lca = node_lca(c, o);
+      if (lca == o)
+      {
+        link_child(parent, o);
+        Node& on = nodes.at(o);
+        const u64 prev = child_in_slot(on, nondirect_child_id(o, c));
+        if (prev)
+          orphans.push_back(prev);
+        link_child(on, c);
+      }
+      else
+      {
+        link_child(parent, lca);
+        auto [it, inserted] = nodes.try_emplace(lca);
+        if (inserted)
+        {
+          it->second.key = lca;
+          init_min_point(it->second);
+        }
+        link_child(it->second, c);
+        link_child(it->second, o);
+      }
+    }
+    return true;
+  }
+
   // ------------------------------------------------------------------ query work counters
   // The work of the reference's traversal, counted while `countWork` is set (single-threaded use):
   // node records read (node tests), entity records read (entity tests) and ids returned. They give

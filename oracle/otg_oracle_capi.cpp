@@ -221,6 +221,23 @@ void export_nodes_impl(Tree<T>& t, uint64_t* keys, double* minp, double* size, u
   }
   eoff[ks.size()] = off;
 }
+// the key of every node's parent (0 for the root and for nodes no link holds), ascending key order
+template<typename T>
+void export_parents_impl(Tree<T>& t, uint64_t* parents)
+{
+  std::vector<uint64_t> ks;
+  for (auto& [k, n] : t.nodes)
+    ks.push_back(k);
+  std::sort(ks.begin(), ks.end());
+  std::fill(parents, parents + ks.size(), 0);
+  for (uint64_t k : ks)
+    for (uint64_t c : t.nodes.at(k).children)
+    {
+      const auto it = std::lower_bound(ks.begin(), ks.end(), c);
+      if (it != ks.end() && *it == c)
+        parents[it - ks.begin()] = k;
+    }
+}
 } // namespace
 
 extern "C"
@@ -281,6 +298,12 @@ extern "C"
     return oro_create_threads(scalar, kind, ent, n, maxDepth, box, maxElem, 1);
   }
   void oro_destroy(void* h) { delete (AnyTree*)h; }
+  // Bulk Insert of n new points (Tree::insert_points); 1 when they were inserted, 0 when refused
+  int oro_insert(void* h, const void* ent, uint64_t n)
+  {
+    auto* a = (AnyTree*)h;
+    return a->scalar == 0 ? int(a->d->insert_points((const double*)ent, n)) : int(a->f->insert_points((const float*)ent, n));
+  }
   // Core form: `ent` (n entities, the Create layout) becomes the geometry the tree's queries test;
   // the nodes stay as Create built them (the reference's Core queries take the span per call)
   void oro_set_entities(void* h, const void* ent, uint64_t n)
@@ -361,6 +384,14 @@ extern "C"
       export_nodes_impl(*a->f, keys, minp, size, eoff, eids, subtree);
   }
 
+  void oro_node_parents(void* h, uint64_t* parents)
+  {
+    auto* a = (AnyTree*)h;
+    if (a->scalar == 0)
+      export_parents_impl(*a->d, parents);
+    else
+      export_parents_impl(*a->f, parents);
+  }
   void* oro_range(void* h, const void* ranges, uint64_t nq, int mode, double tol)
   {
     auto* a = (AnyTree*)h;

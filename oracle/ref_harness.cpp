@@ -268,6 +268,25 @@ void export_nodes(Tree const& t, uint64_t* keys, double* minp, double* size, uin
   eoff[ks.size()] = off;
 }
 
+// the key of every node's parent (the node whose child links hold it; 0 for the root and for nodes
+// no link holds), nodes in ascending key order
+template<typename Tree>
+void export_parents(Tree const& t, uint64_t* parents)
+{
+  std::vector<uint64_t> ks;
+  for (auto const& kv : t.GetNodes())
+    ks.push_back(uint64_t(kv.first));
+  std::sort(ks.begin(), ks.end());
+  std::fill(parents, parents + ks.size(), 0);
+  for (uint64_t k : ks)
+    for (auto c : t.GetNodeChildren(t.GetNodeValue(k)))
+    {
+      const auto it = std::lower_bound(ks.begin(), ks.end(), uint64_t(c));
+      if (it != ks.end() && *it == uint64_t(c))
+        parents[it - ks.begin()] = k;
+    }
+}
+
 template<typename F>
 Result* run_queries(uint64_t nq, F&& one)
 {
@@ -631,6 +650,13 @@ extern "C"
       return 0;
     });
   }
+  void oro_node_parents(void* h, uint64_t* parents)
+  {
+    with_tree((AnyRef*)h, [&](auto& t, auto, auto, auto) {
+      export_parents(t, parents);
+      return 0;
+    });
+  }
   void* oro_range(void* h, const void* ranges, uint64_t nq, int mode, double tol)
   {
     return with_tree((AnyRef*)h, [&](auto& t, auto ents, auto s, auto) -> Result* {
@@ -732,6 +758,27 @@ extern "C"
       std::memcpy(dist, r->dist.data(), r->dist.size() * sizeof(double));
   }
   void oro_res_free(void* r) { delete (Result*)r; }
+
+  // Bulk Insert of n new points into a point tree (Insert(newEntities, existingEntities),
+  // core/ot_dynamic_hash_core.h:1012-1333); the new entities get ids N .. N + n - 1 and join the span
+  // that later queries pass. Returns the reference's result (all inserted).
+  int oro_insert(void* h, const void* ent, uint64_t n)
+  {
+    auto* a = (AnyRef*)h;
+    if (a->kind != 0)
+      return 0;
+    if (a->scalar == 0)
+    {
+      std::vector<double> add((const double*)ent, (const double*)ent + 3 * n);
+      const bool ok = a->pd->Insert(pts_span(add), pts_span(a->ed));
+      a->ed.insert(a->ed.end(), add.begin(), add.end());
+      return ok ? 1 : 0;
+    }
+    std::vector<float> add((const float*)ent, (const float*)ent + 3 * n);
+    const bool ok = a->pf->Insert(pts_span(add), pts_span(a->ef));
+    a->ef.insert(a->ef.end(), add.begin(), add.end());
+    return ok ? 1 : 0;
+  }
 
   // Core form: the entity span that every later query passes (the tree is not rebuilt): the
   // reference's Core queries test the geometry of the span they are given against the nodes

@@ -79,6 +79,12 @@ class OracleLib:
             lib.oro_static_equal.argtypes = [_vp]
             lib.oro_dynamic_equals_static.restype = _int
             lib.oro_dynamic_equals_static.argtypes = [_vp]
+        if hasattr(lib, "oro_node_parents"):
+            lib.oro_node_parents.restype = None
+            lib.oro_node_parents.argtypes = [_vp, _vp]
+        if hasattr(lib, "oro_insert"):
+            lib.oro_insert.restype = _int
+            lib.oro_insert.argtypes = [_vp, _vp, _u64]
         if hasattr(lib, "oro_set_entities"):
             lib.oro_set_entities.restype = None
             lib.oro_set_entities.argtypes = [_vp, _vp, _u64]
@@ -195,6 +201,22 @@ class OracleTree:
         finally:
             self.lib.oro_static_free(h)
         return dict(child_begins=cb[:nb], segments=seg[:m], depth=dep[:m], entity_storage=es[:ne], geometry=geo[:m]), equal
+
+    def parents(self):
+        """Parent key of every node (0 for the root), nodes in ascending key order (as nodes())."""
+        out = np.zeros(self.node_count, np.uint64)
+        self.lib.oro_node_parents(self.h, _ptr(out))
+        return out
+
+    def insert(self, ent):
+        """Bulk Insert of new points (point trees); they get ids n .. n + len(ent) - 1. Returns the
+        library's result (False: refused, nothing inserted)."""
+        ent = np.ascontiguousarray(ent, dtype=self.ent.dtype)
+        ok = bool(self.lib.oro_insert(self.h, _ptr(ent), ent.shape[0]))
+        if ok:
+            self.ent = np.concatenate([self.ent, ent])
+            self.n = self.ent.shape[0]
+        return ok
 
     def set_entities(self, ent):
         """Core form: the geometry later queries test (same count and layout; the tree keeps its nodes)."""

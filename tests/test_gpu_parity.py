@@ -551,14 +551,17 @@ def test_core_form_set_entities(kind, dtype, device_span):
         assert_csr_equal(t.range_search(qs["ranges"], mode)[:2], o.range_search(qs["ranges"], mode), f"moved span range{mode}")
     assert_csr_equal(t.pick_search(qs["qpts"])[:2], o.pick_search(qs["qpts"]), "moved span pick")
     assert_csr_equal(t.frustum_culling(qs["planes"])[:2], o.frustum(qs["planes"]), "moved span frustum")
-    g = t.ray_all(qs["rays"], tol=0.05)
-    r = o.ray(qs["rays"], first=False, tol=0.05)
+    g = t.ray_all(qs["rays"], tol=0.005)
+    r = o.ray(qs["rays"], first=False, tol=0.005)
     assert_csr_equal(g[:2], r[:2], "moved span ray all")
     assert_dist_close(g[2], r[2], RAY_REL, "moved span ray all")
-    # the Create span again (a copy: another pointer, the same geometry): every query
+    # the Create span again (a copy: another pointer, the same geometry): every query. The ray
+    # tolerance scales with the domain (10 here, 100 in the random tests): with a tolerance near the
+    # points' spacing, RayIntersectedFirst's bound can grow back while the reference examines entities,
+    # and its answer depends on that order
     t.set_entities(torch.as_tensor(ent.copy(), device="cuda") if device_span else ent.copy())
     o.set_entities(ent)
-    _check_queries(t, o, qs, kind, 0.05, f"core span kind={kind}")
+    _check_queries(t, o, qs, kind, 0.005, f"core span kind={kind}")
     if kind != KIND_POINTS:
         assert np.array_equal(t.collision_self(), o.collide_self())
     with pytest.raises(otg.OtgError):
