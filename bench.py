@@ -458,6 +458,7 @@ def run_gpu(args):
         line["queries"] = run_queries(tree, pts_d, stream, cpu_results, pts_h)
         line["many_trees"] = run_many_trees()
         line["two_trees"] = run_two_trees()
+        line["insert"] = run_insert(cpu=rank == 0 and not args.no_cpu_baseline)
         line["autotune"] = otg.autotune_entries()
     if rank == 0:
         print(json.dumps(line))
@@ -1069,6 +1070,87 @@ def run_two_trees(steps=10):
         "pair_lists_equal_step0": equal_step0,
         "recheck_fraction": rechecks / max(tests, 1),
     }
+
+
+def inside(pts, ref):
+    """The rows of pts inside the bounding box of ref (new points that a tree of ref can take)."""
+    lo, hi = ref.min(0), ref.max(0)
+    return pts[np.all((pts >= lo) & (pts <= hi), 1)]
+
+
+def run_insert(reps=3, cpu=True):
+    """Bulk Insert (DynamicHashOrthoTreeCore::Insert) of 1M new shell points into the 16M shell tree
+    (depth 10, max 20): each repetition inserts into a fresh Create (untimed); the synchronous insert
+    call is timed by the host clock, from device and from host memory; a full Create of all 17M points
+    is timed beside it. On the CPU, the oracle's Insert (one thread, as the reference's SeqExec) of
+    62.5k points into a 1M-point tree is timed against the GPU on the same case, and the two trees'
+    node sets and parent links are compared."""
+    import torch
+
+    import octree_gb300 as otg
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _insert_cases import parent_keys
+    from _oracle_lib import KIND_POINTS, oracle
+
+    pts = shell_points(16_000_000, 301)
+    add = inside(shell_points(1_050_000, 311), pts)[:1_000_000]
+    pts_d = torch.as_tensor(pts, device="cuda")
+    add_d = torch.as_tensor(add, device="cuda")
+    add_pinned = torch.as_tensor(add).pin_memory()
+    out = {"insert_points": len(add), "into_tree_points": len(pts)}
+    dev_ms, host_ms, nodes = [], [], 0
+    for r in range(reps + 1):
+        for src, acc in ((add_d, dev_ms), (add_pinned.numpy(), host_ms)):
+            t = otg.Tree("points").create(pts_d, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
+            t.sync()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            t.insert(src)
+            ms = (time.perf_counter() - t0) * 1e3
+            if r:
+                acc.append(ms)
+            nodes = t.node_count
+            del t
+    allp = torch.cat([pts_d, add_d])
+    rebuild = []
+    for r in range(reps + 1):
+        t = otg.Tree("points")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t.create(allp, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
+        t.sync()
+        if r:
+            rebuild.append((time.perf_counter() - t0) * 1e3)
+        del t
+    out["insert_1M_into_16M_device_ms"] = statistics.median(dev_ms)
+    out["insert_1M_into_16M_host_input_ms"] = statistics.median(host_ms)
+    out["insert_Mpts_per_s"] = len(add) / statistics.median(dev_ms) / 1e3
+    out["nodes_after_insert"] = int(nodes)
+    out["create_17M_ms"] = statistics.median(rebuild)
+    # the same small case on the GPU and in the oracle
+    small, small_add = pts[::16], add[::16]
+    g = []
+    for r in range(reps + 1):
+        t = otg.Tree("points").create(small, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
+        t.sync()
+        t0 = time.perf_counter()
+        t.insert(small_add)
+        if r:
+            g.append((time.perf_counter() - t0) * 1e3)
+    out["insert_62k_into_1M_gpu_ms"] = statistics.median(g)
+    if cpu:
+        o = oracle().create(small, KIND_POINTS, MAX_DEPTH, None, MAX_ELEM, threads=os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        ok = o.insert(small_add)
+        out["insert_62k_into_1M_cpu_ms"] = (time.perf_counter() - t0) * 1e3
+        out["insert_cpu_kind"] = "port"
+        out["insert_cpu_threads"] = 1
+        out["insert_speedup_gpu_vs_cpu_same_case"] = out["insert_62k_into_1M_cpu_ms"] / out["insert_62k_into_1M_gpu_ms"]
+        gn, on = t.nodes(), o.nodes()
+        same = ok and np.array_equal(np.sort(gn["keys"]), on["keys"]) and np.array_equal(parent_keys(gn), o.parents())
+        out["insert_sample_nodes_and_links_equal_to_cpu"] = bool(same)
+    return out
 
 
 PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m", "build_4m_clustered", "forest_frustum_1024")

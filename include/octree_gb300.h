@@ -98,9 +98,9 @@ void otg_tree_free(otg_tree* tree);
    The entity array is copied into the tree (the Managed form's ownership, ot_managed.h:70-71);
    queries therefore need no entity argument. Asynchronous on `stream` unless mem == OTG_MEM_HOST,
    in which case the call returns after the build finished and reports device-side errors.
-   The first build of the process sets its CUDA context's L2 fetch granularity limit
-   (cudaLimitMaxL2FetchGranularity) to 64 bytes, which makes the build's random entity reads cheaper;
-   the environment variable OTG_L2_FETCH_BYTES chooses another value, 0 leaves the limit unchanged. */
+   With the environment variable OTG_L2_FETCH_BYTES set to a byte count, the first build of the
+   process sets its CUDA context's L2 fetch granularity limit (cudaLimitMaxL2FetchGranularity) to it;
+   unset or 0 leaves the limit unchanged. */
 int otg_tree_create(otg_tree* tree, const void* entities, uint64_t n, uint32_t max_depth, const void* box, uint64_t max_elements, int mem,
                     void* stream);
 
@@ -112,6 +112,20 @@ int otg_tree_create(otg_tree* tree, const void* entities, uint64_t n, uint32_t m
    them, and `entities` (n must equal the tree's entity count; the same layout as Create's) becomes
    the tested geometry. Host memory is copied; device memory is read once, here. Not for forests. */
 int otg_tree_set_entities(otg_tree* tree, const void* entities, uint64_t n, int mem, void* stream);
+
+/* Bulk Insert of points into a point tree, as DynamicHashOrthoTreeCore::Insert(newEntities,
+   existingEntities) (core/ot_dynamic_hash_core.h:1012-1333; OrthoTreeManaged::Add(newEntities),
+   core/ot_managed.h:421-455, calls it): the new points get the ids entity_count .. entity_count +
+   n - 1 and join the tree without a rebuild. They are clustered by the reference's rule (sorted by
+   location, split by 9 bits at a time, runs of at most 256 walked greedily, at most max_elements per
+   new node where locations differ), each cluster joins the node at its location, created where
+   missing, and new nodes are linked under their nearest ancestor with branch nodes where two of them
+   claim one child slot (LinkOrphanNodes, :826-863). The tree keeps its space and max depth.
+   entities: n * 3 scalars of the tree's type, host or device memory. Synchronises `stream`.
+   OTG_ERR_INVALID_ARGUMENT (nothing inserted) when a point lies outside the tree's space, where the
+   reference stores it with location code 0; OTG_ERR_NOT_SUPPORTED for box trees, forests and
+   empty trees. A tree changed by Insert is refused by otg_tree_export_static. */
+int otg_tree_insert(otg_tree* tree, const void* entities, uint64_t n, int mem, void* stream);
 
 /* Waits for the tree's last build on `stream` and reports device-side errors (OTG_ERR_TIMEOUT). */
 int otg_tree_sync(otg_tree* tree, void* stream);

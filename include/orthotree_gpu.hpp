@@ -54,6 +54,7 @@
 #include <span>
 #include <stdexcept>
 #include <type_traits>
+#include <unordered_set>
 #include <string>
 #include <utility>
 #include <vector>
@@ -253,6 +254,24 @@ public:
     detail::check(otg_tree_create(m_tree, entities.data(), entities.size(), maxDepthID.value_or(0), boxSpace ? &*boxSpace : nullptr,
                                   maxElementNoInNode, OTG_MEM_HOST, m_stream));
   }
+
+  // Add(newEntities, execMode): bulk Insert (core/ot_managed.h:421-455, which calls
+  // DynamicHashOrthoTreeCore::Insert, core/ot_dynamic_hash_core.h:1012-1333). The new entities get the
+  // ids GetEntityCount() .. GetEntityCount() + n - 1, as the reference numbers a contiguous span
+  // (:1061-1064). false, and nothing added, when one lies outside the tree's space (the reference's
+  // answer for non-keyed entities when out-of-space insertion is off; with it on, the reference
+  // stores such a point with location code 0). Point trees.
+  template<typename TExecMode = std::nullptr_t>
+  bool Add(std::span<const Entity> newEntities, TExecMode = {})
+    requires(KIND == OTG_KIND_POINTS)
+  {
+    const int rc = otg_tree_insert(m_tree, newEntities.data(), newEntities.size(), OTG_MEM_HOST, m_stream);
+    if (rc == OTG_ERR_INVALID_ARGUMENT && newEntities.data())
+      return false;
+    detail::check(rc);
+    return true;
+  }
+  std::size_t GetEntityCount() const { return std::size_t(Info().entity_count); }
 
   otg_tree_info Info() const
   {
@@ -663,6 +682,45 @@ public:
     return tree.Create(entities, maxDepthID, boxSpace, maxElementNoInNode);
   }
 
+  // Insert(newEntities, existingEntities, execMode, failedEntities) (core/ot_dynamic_hash_core.h:
+  // 1012-1333): bulk Insert of points with the ids existingEntities.size() + i (:1061-1064);
+  // existingEntities is the span the tree was built for (its size is the tree's entity count). The
+  // next query's span of the grown size (existing then new entities, as the caller appends them)
+  // is taken as the tree's geometry without a rebuild. false, nothing inserted and the ids of the
+  // points outside the tree's space in failedEntities, when any lies outside it.
+  template<typename TExecMode = std::nullptr_t>
+  bool Insert(EntityContainerView newEntities, EntityContainerView existingEntities, TExecMode = {},
+              std::unordered_set<EntityID>* failedEntities = nullptr)
+    requires(KIND == OTG_KIND_POINTS)
+  {
+    const std::size_t n = m_impl.GetEntityCount();
+    if (existingEntities.size() != n)
+      throw Error(OTG_ERR_INVALID_ARGUMENT, "Insert: existingEntities must be the span the tree holds");
+    if (!m_impl.Add(newEntities))
+    {
+      if (failedEntities)
+      {
+        const otg_tree_info info = m_impl.Info();
+        for (std::size_t i = 0; i < newEntities.size(); ++i)
+        {
+          bool in = true;
+          for (int d = 0; d < 3; ++d)
+          {
+            const double v = double(newEntities[i][d]);
+            in = in && v >= info.space_min[d] && v <= info.space_max[d];
+          }
+          if (!in)
+            failedEntities->insert(EntityID(n + i));
+        }
+      }
+      return false;
+    }
+    m_data = nullptr;
+    m_size = n + newEntities.size();
+    m_grown = true;
+    return true;
+  }
+
   // The caller changed the contents of the span in place: the next query uploads it again.
   void NotifyEntitiesChanged() noexcept { ++m_generation; }
   void SetSpanChange(SpanChange policy) noexcept { m_policy = policy; }
@@ -788,7 +846,10 @@ private:
   {
     if (entities.data() != m_data || entities.size() != m_size || m_boundGeneration != m_generation)
     {
-      if (m_policy == SpanChange::Rebuild)
+      // after an Insert the grown span (the old entities, then the new ones) is the tree's geometry
+      const bool grown = m_grown && entities.size() == m_size;
+      m_grown = false;
+      if (m_policy == SpanChange::Rebuild && !grown)
         const_cast<Impl&>(m_impl).Create(entities, m_maxDepth, m_box, m_maxElem);
       else
         detail::check(otg_tree_set_entities(const_cast<otg_tree*>(m_impl.Handle()), entities.data(), entities.size(), OTG_MEM_HOST, m_impl.Stream()));
@@ -808,6 +869,7 @@ private:
   mutable std::size_t m_size = 0;
   std::uint64_t m_generation = 0;
   mutable std::uint64_t m_boundGeneration = 0;
+  mutable bool m_grown = false;
 };
 
 using OctreePoint = OrthoTreeCoreGPU<Vector3<double>, double, OTG_KIND_POINTS>;

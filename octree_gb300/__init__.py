@@ -43,6 +43,7 @@ EXPORTS = [
     ("otg_tree_free", None, [_vp]),
     ("otg_tree_create", _int, [_vp, _vp, _u64, _u32, _vp, _u64, _int, _vp]),
     ("otg_tree_set_entities", _int, [_vp, _vp, _u64, _int, _vp]),
+    ("otg_tree_insert", _int, [_vp, _vp, _u64, _int, _vp]),
     ("otg_tree_sync", _int, [_vp, _vp]),
     ("otg_tree_info_get", _int, [_vp, _vp]),
     ("otg_tree_export_locations", _int, [_vp, _vp, _int, _vp]),
@@ -301,6 +302,16 @@ class Tree:
         n = int(entities.shape[0]) if len(entities.shape) else 0
         _check(library().otg_tree_set_entities(self.h, p, n, mem, _stream_ptr(stream)))
         self._keep_span = keep  # device input is read by the stream-ordered gather of this call
+        return self
+
+    def insert(self, entities, stream=None):
+        """Bulk Insert of points (DynamicHashOrthoTreeCore::Insert, core/ot_dynamic_hash_core.h:1012):
+        the new points get ids entity_count .. entity_count + len - 1. Raises (nothing inserted) when
+        a point lies outside the tree's space."""
+        p, mem, keep = _arg(entities, self.dtype)
+        n = int(entities.shape[0]) if len(entities.shape) else 0
+        _check(library().otg_tree_insert(self.h, p, n, mem, _stream_ptr(stream)))
+        del keep  # the call synchronises its stream
         return self
 
     def sync(self, stream=None):

@@ -26,6 +26,7 @@
 #include "otg_raster.cuh"
 #include "otg_sort.cuh"
 #include "otg_sort_chunked.cuh"
+#include "otg_query.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -1365,10 +1366,13 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
 // measured at 16M points). Measured on the 16M-point build: 1.340 ms per build at the default, 1.303
 // ms at 64 bytes, 1.316 ms at 32 bytes. OTG_L2_FETCH_BYTES chooses another value; 0 leaves the
 // context's limit as it is.
+// OTG_L2_FETCH_BYTES=b sets the context's L2 fetch granularity limit before the first build (0 or
+// unset: unchanged). Measured on the 16M-point build: unchanged 1.359 ms, 32 B 1.394 ms, 64 B
+// 1.365 ms, 128 B 1.360 ms; the gather's extra sectors cost no time, so the default leaves it.
 static void apply_l2_fetch_limit()
 {
   static const bool done = [] {
-    size_t bytes = 64;
+    size_t bytes = 0;
     if (const char* v = std::getenv("OTG_L2_FETCH_BYTES"))
       bytes = size_t(std::atoi(v));
     if (bytes)
@@ -1414,6 +1418,7 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
   t.built = false;
   t.countsKnown = false;
   t.image32 = false;
+  t.inserted = false;
   t.trees = 0;
   t.boxGiven = box != nullptr;
   cudaError_t e;
@@ -1898,6 +1903,7 @@ int build_forest(TreeState& t, const void* entities, const u64* treeOffsets, u32
   t.built = false;
   t.countsKnown = false;
   t.image32 = false;
+  t.inserted = false;
   t.trees = trees;
   t.boxGiven = boxes != nullptr;
   cudaError_t e;
@@ -2178,6 +2184,740 @@ int export_nodes(const TreeState& t, u64* keys, double* minSize, u64* eoff, u32*
   }
   eoff[m] = off;
   return OTG_OK;
+}
+
+} // namespace otg
+
+// ================================================================ bulk Insert (point trees)
+// Insert(newEntities, existingEntities) of DynamicHashOrthoTreeCore (core/ot_dynamic_hash_core.h:
+// 1012-1333) and LinkOrphanNodes (:826-863) for point trees; MinPoint trees need no geometry
+// update (UpdateNodeGeometry :866-1005 only unites MBRs). New entity i gets id n + i.
+//  1. keys of the new points from the tree's own grid (the rasterisation tables of its Create), and
+//     a stable radix sort of them;
+//  2. the reference's clustering of the sorted new points, in rounds, one warp per work item:
+//     an item of at most maxElementNo points becomes one cluster at its location (:1304-1308), an
+//     item of at most 256 (or one whose remaining bits are 0: identical locations) is walked
+//     greedily (:1237-1291, one lane), a larger one is split by the next 9 bits into buckets found
+//     by binary search, each with the fold of its locations (lowest common ancestor, :1153-1199);
+//  3. the node set after LinkOrphanNodes: the old nodes, the clusters' nodes and the lowest common
+//     ancestors of DFS-adjacent keys (the branch nodes the linking creates where two nodes claim
+//     the same child slot), each node's parent its nearest ancestor in the set (a child link may
+//     skip levels);
+//  4. the tree laid out again: nodes breadth first by link level (children contiguous, in slot
+//     order), entities ordered by their node in depth-first order (own entities and subtrees
+//     contiguous), MinPoint geometry from the node keys.
+// A new point outside the tree's space is refused (OTG_ERR_INVALID_ARGUMENT, nothing inserted): the
+// reference would store it with a location code of 0.
+namespace otg
+{
+namespace
+{
+struct InsItem
+{
+  u32 b, e, bits, depth;
+  u64 loc;
+};
+struct InsCluster
+{
+  u32 b, e;
+  u64 key;
+};
+
+__device__ __forceinline__ u32 ins_fold_depth(u64 diff, u32 D)
+{
+  const u32 levels = (u32(64 - __clzll(diff)) + 2u) / 3u;
+  return levels >= D ? 0u : D - levels;
+}
+__device__ __forceinline__ u64 ins_node_key(u64 loc, u32 depth, u32 D) { return (u64(1) << (3 * depth)) | (loc >> (3 * (D - depth))); }
+__device__ __forceinline__ u32 ins_key_depth(u64 key) { return u32(63 - __clzll(key)) / 3u; }
+// depth-first (pre-order) sort key of a node: its location left-aligned to the max depth, then depth
+__device__ __forceinline__ u64 ins_dfs_key(u64 key, u32 D)
+{
+  const u32 d = ins_key_depth(key);
+  return (((key ^ (u64(1) << (3 * d))) << (3 * (D - d))) << 5) | d;
+}
+__device__ __forceinline__ u64 ins_key_of_dfs(u64 c, u32 D)
+{
+  const u32 d = u32(c & 31u);
+  return (u64(1) << (3 * d)) | ((c >> 5) >> (3 * (D - d)));
+}
+__device__ __forceinline__ u64 ins_node_lca(u64 a, u64 b) // si_morton.h:307-325
+{
+  if (a == b)
+    return a;
+  const u32 da = ins_key_depth(a), db = ins_key_depth(b);
+  if (da > db)
+    a >>= 3 * (da - db);
+  else if (db > da)
+    b >>= 3 * (db - da);
+  const u32 levels = (u32(64 - __clzll(a ^ b)) + 2u) / 3u;
+  return a >> (3 * levels);
+}
+__device__ __forceinline__ u32 ins_lower_bound(const u64* a, u32 lo, u32 hi, u64 v)
+{
+  while (lo < hi)
+  {
+    const u32 mid = lo + ((hi - lo) >> 1);
+    if (a[mid] < v)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ u32 ins_lower_bound32(const u32* a, u32 lo, u32 hi, u32 v)
+{
+  while (lo < hi)
+  {
+    const u32 mid = lo + ((hi - lo) >> 1);
+    if (a[mid] < v)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+} // namespace
+
+template<typename T, typename R, typename K>
+__global__ void __launch_bounds__(256) insert_keys_kernel(const T* __restrict__ pts, u64 n2, const Space<T>* __restrict__ spg,
+                                                          const typename Ord<T>::U* __restrict__ tab, u32 cells, K* __restrict__ keys, u32* __restrict__ vals,
+                                                          u32* __restrict__ err)
+{
+  const Space<T>& s = *spg;
+  float minF[3], rastF[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    minF[d] = to_f(s.min[d]);
+    rastF[d] = float(Raster<R, T>::rast(s, d));
+  }
+  const size_t perDim = RasterLayout<T>::per_dim(cells);
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < n2; i += u64(gridDim.x) * blockDim.x)
+  {
+    const T e[3] = { pts[3 * i], pts[3 * i + 1], pts[3 * i + 2] };
+    const u64 k = entity_key<T, false>(e, tab, perDim, cells, minF, rastF, s.D);
+    if (k == 0)
+      atomicOr(err, kErrArgument); // outside the space
+    keys[i] = K(k);
+    vals[i] = u32(i);
+  }
+}
+
+// One round of the clustering: a warp per item. keys: the sorted new keys (location + 1).
+template<typename K>
+__global__ void __launch_bounds__(256) insert_round_kernel(const K* __restrict__ keys, u32 D, u64 maxElem, const InsItem* __restrict__ in, u32 nIn,
+                                                           InsItem* __restrict__ out, u32* __restrict__ nOut, u32 outCap, InsCluster* __restrict__ cl,
+                                                           u32* __restrict__ nCl, u32 clCap, u32* __restrict__ err)
+{
+  const u32 lane = threadIdx.x & 31;
+  const u32 warps = (gridDim.x * blockDim.x) >> 5;
+  auto push_cluster = [&](u32 b, u32 e, u64 key) {
+    const u32 slot = atomicAdd(nCl, 1u);
+    if (slot < clCap)
+      cl[slot] = InsCluster{ b, e, key };
+    else
+      atomicOr(err, kErrCapacity);
+  };
+  for (u32 it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < nIn; it += warps)
+  {
+    const InsItem w = in[it];
+    const u32 num = w.e - w.b;
+    if (num == 0)
+      continue;
+    if (num <= maxElem) // :1304-1308 one cluster at the item's fold
+    {
+      if (lane == 0)
+        push_cluster(w.b, w.e, ins_node_key(w.loc, w.depth, D));
+      continue;
+    }
+    if (w.bits == 0) // identical locations: the walk makes one cluster of them at the max depth
+    {
+      if (lane == 0)
+        push_cluster(w.b, w.e, ins_node_key(u64(keys[w.b]) - 1, D, D));
+      continue;
+    }
+    if (num <= 256) // :1310-1317 emitSortedRange (:1237-1291), sequential on one lane
+    {
+      if (lane == 0)
+      {
+        u32 cb = w.b;
+        while (cb < w.e)
+        {
+          const u64 base = u64(keys[cb]) - 1;
+          u64 diff = 0;
+          u32 ce = cb + 1;
+          while (ce < w.e)
+          {
+            const u64 nd = diff | (base ^ (u64(keys[ce]) - 1));
+            const u32 newDepth = ins_fold_depth(nd, D);
+            if (u64(ce - cb + 1) > maxElem && newDepth < D && newDepth < ins_fold_depth(diff, D))
+              break;
+            diff = nd;
+            ++ce;
+          }
+          push_cluster(cb, ce, ins_node_key(base, ins_fold_depth(diff, D), D));
+          cb = ce;
+        }
+      }
+      continue;
+    }
+    // radixPartition (:1153-1199): buckets of the next min(9, bits) bits; all locations of the item
+    // share the bits above w.bits
+    const u32 numBits = min(9u, w.bits);
+    const u32 shift = w.bits - numBits;
+    const u32 nd = 1u << numBits;
+    const u64 prefix = w.bits >= 64 ? 0 : (((u64(keys[w.b]) - 1) >> w.bits) << w.bits);
+    for (u32 d0 = 0; d0 < nd; d0 += 32)
+    {
+      const u32 d = d0 + lane;
+      if (d >= nd)
+        break;
+      const u64 lo = prefix | (u64(d) << shift);
+      const u64 hi = lo + (u64(1) << shift);
+      const u32 bb = lower_bound_key(keys, w.b, w.e, lo + 1);
+      const u32 be = lower_bound_key(keys, bb, w.e, hi + 1);
+      if (be > bb)
+      {
+        const u64 l0 = u64(keys[bb]) - 1, l1 = u64(keys[be - 1]) - 1;
+        const u32 depth = ins_fold_depth(l0 ^ l1, D);
+        const u32 slot = atomicAdd(nOut, 1u);
+        if (slot < outCap)
+          out[slot] = InsItem{ bb, be, min((D - depth) * 3u, shift), depth, l0 };
+        else
+          atomicOr(err, kErrCapacity);
+      }
+    }
+  }
+}
+
+// entries of the node-set merge: (depth-first key, tag): old nodes (tag = old index), clusters
+// (tag = M + cluster), branch candidates (tag = M + C + i, from the first merge pass)
+__global__ void insert_entries_kernel(const u64* __restrict__ nodeKey, u32 M, const InsCluster* __restrict__ cl, u32 C, u32 D, u64* __restrict__ ek,
+                                      u32* __restrict__ ev)
+{
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < M + C; i += gridDim.x * blockDim.x)
+  {
+    ek[i] = ins_dfs_key(i < M ? nodeKey[i] : cl[i - M].key, D);
+    ev[i] = i;
+  }
+}
+
+// the lowest common ancestor of each adjacent pair of sorted entries, as a candidate entry without a
+// tag (the first entry repeats itself; equal keys give the key again)
+__global__ void insert_lca_kernel(u64* __restrict__ ek, u32* __restrict__ ev, u32 m, u32 D)
+{
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+  {
+    ek[m + i] = i == 0 ? ek[0] : ins_dfs_key(ins_node_lca(ins_key_of_dfs(ek[i - 1], D), ins_key_of_dfs(ek[i], D)), D);
+    ev[m + i] = 0xffffffffu;
+  }
+}
+
+__global__ void insert_first_kernel(const u64* __restrict__ ek, u32 m, u32* __restrict__ first)
+{
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    first[i] = (i == 0 || ek[i] != ek[i - 1]) ? 1u : 0u;
+}
+
+// exclusive scan of u32 values (three launches: block sums, their scan, the adds)
+constexpr u32 kScanBlock = 1024;
+__global__ void __launch_bounds__(kScanBlock) scan_block_sums_kernel(const u32* __restrict__ v, u32 m, u32* __restrict__ sums)
+{
+  __shared__ u32 s[32];
+  const u32 i = blockIdx.x * kScanBlock + threadIdx.x;
+  u32 x = i < m ? v[i] : 0u;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    x += __shfl_xor_sync(0xffffffffu, x, o);
+  if ((threadIdx.x & 31) == 0)
+    s[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x < 32)
+  {
+    u32 y = s[threadIdx.x];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      y += __shfl_xor_sync(0xffffffffu, y, o);
+    if (threadIdx.x == 0)
+      sums[blockIdx.x] = y;
+  }
+}
+__global__ void __launch_bounds__(kScanBlock) scan_sums_kernel(u32* __restrict__ sums, u32 nb, u32* __restrict__ total)
+{
+  __shared__ u32 s[32];
+  __shared__ u32 carry;
+  if (threadIdx.x == 0)
+    carry = 0;
+  __syncthreads();
+  for (u32 base = 0; base < nb; base += kScanBlock)
+  {
+    const u32 i = base + threadIdx.x;
+    const u32 v = i < nb ? sums[i] : 0u;
+    u32 x = v;
+    const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      const u32 y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= u32(o))
+        x += y;
+    }
+    if (lane == 31)
+      s[w] = x;
+    __syncthreads();
+    if (w == 0)
+    {
+      u32 y = s[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1)
+      {
+        const u32 z = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= u32(o))
+          y += z;
+      }
+      s[lane] = y;
+    }
+    __syncthreads();
+    const u32 incl = x + (w ? s[w - 1] : 0u);
+    if (i < nb)
+      sums[i] = carry + incl - v;
+    __syncthreads();
+    if (threadIdx.x == kScanBlock - 1)
+      carry += incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    *total = carry;
+}
+__global__ void __launch_bounds__(kScanBlock) scan_add_kernel(const u32* __restrict__ v, u32 m, const u32* __restrict__ sums, u32* __restrict__ out)
+{
+  __shared__ u32 s[32];
+  const u32 i = blockIdx.x * kScanBlock + threadIdx.x;
+  const u32 val = i < m ? v[i] : 0u;
+  u32 x = val;
+  const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    const u32 y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= u32(o))
+      x += y;
+  }
+  if (lane == 31)
+    s[w] = x;
+  __syncthreads();
+  if (w == 0)
+  {
+    u32 y = s[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      const u32 z = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= u32(o))
+        y += z;
+    }
+    s[lane] = y;
+  }
+  __syncthreads();
+  if (i < m)
+    out[i] = sums[blockIdx.x] + x - val + (w ? s[w - 1] : 0u);
+}
+
+// the distinct keys of the sorted entries, and where each old node and each cluster went
+__global__ void insert_compact_kernel(const u64* __restrict__ ek, const u32* __restrict__ ev, const u32* __restrict__ first, const u32* __restrict__ idx, u32 m,
+                                      u32 M, u32 C, u64* __restrict__ fk, u32* __restrict__ oldToNew, u32* __restrict__ clusterNode)
+{
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+  {
+    const u32 u = idx[i] + first[i] - 1; // index of this entry's distinct key
+    if (first[i])
+      fk[u] = ek[i];
+    const u32 tag = ev[i];
+    if (tag < M)
+      oldToNew[tag] = u;
+    else if (tag < M + C)
+      clusterNode[tag - M] = u;
+  }
+}
+
+// parent (nearest ancestor in the set) and link level of every node, nodes in depth-first order;
+// nodes per depth counted in depthCount
+__global__ void insert_parents_kernel(const u64* __restrict__ fk, u32 F, u32 D, u32* __restrict__ parent, u32* __restrict__ level, u32* __restrict__ depthCount)
+{
+  for (u32 u = blockIdx.x * blockDim.x + threadIdx.x; u < F; u += gridDim.x * blockDim.x)
+  {
+    u64 key = ins_key_of_dfs(fk[u], D);
+    u32 p = 0xffffffffu, lv = 0;
+    while (key > 1)
+    {
+      key >>= 3;
+      const u64 c = ins_dfs_key(key, D);
+      const u32 j = ins_lower_bound(fk, 0, u, c);
+      if (j < u && fk[j] == c)
+      {
+        if (p == 0xffffffffu)
+          p = j;
+        ++lv;
+      }
+    }
+    parent[u] = p;
+    level[u] = lv;
+    atomicAdd(&depthCount[u32(fk[u] & 31u)], 1u);
+  }
+}
+
+__global__ void insert_bfs_keys_kernel(const u32* __restrict__ level, u32 F, u64* __restrict__ bk, u32* __restrict__ bv)
+{
+  for (u32 u = blockIdx.x * blockDim.x + threadIdx.x; u < F; u += gridDim.x * blockDim.x)
+  {
+    bk[u] = (u64(level[u]) << 32) | u;
+    bv[u] = u;
+  }
+}
+
+__global__ void insert_bfs_index_kernel(const u32* __restrict__ bfsToDfs, u32 F, u32* __restrict__ dfsToBfs)
+{
+  for (u32 b = blockIdx.x * blockDim.x + threadIdx.x; b < F; b += gridDim.x * blockDim.x)
+    dfsToBfs[bfsToDfs[b]] = b;
+}
+__global__ void insert_links_kernel(const u32* __restrict__ dfsToBfs, u32 F, const u32* __restrict__ parent, u32* __restrict__ firstChild,
+                                    u32* __restrict__ childCount)
+{
+  for (u32 u = blockIdx.x * blockDim.x + threadIdx.x; u < F; u += gridDim.x * blockDim.x)
+  {
+    const u32 p = parent[u];
+    if (p == 0xffffffffu)
+      continue;
+    const u32 pb = dfsToBfs[p];
+    atomicMin(&firstChild[pb], dfsToBfs[u]);
+    atomicAdd(&childCount[pb], 1u);
+  }
+}
+
+// owner (depth-first node index) of every entity position: old entities by their old node's own
+// range, new ones by their cluster
+__global__ void insert_old_owner_kernel(const uint4* __restrict__ link, u32 M, const u32* __restrict__ oldToNew, u32* __restrict__ owner)
+{
+  for (u32 j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x)
+  {
+    const uint4 L = link[j];
+    for (u32 p = L.y; p < L.z; ++p)
+      owner[p] = oldToNew[j];
+  }
+}
+// every entity position starts without a node (owner F sorts after every node) and as itself
+__global__ void insert_owner_init_kernel(u64 nt, u32 F, u32* __restrict__ owner, u32* __restrict__ src)
+{
+  for (u64 p = blockIdx.x * u64(blockDim.x) + threadIdx.x; p < nt; p += u64(gridDim.x) * blockDim.x)
+  {
+    owner[p] = F;
+    src[p] = u32(p);
+  }
+}
+__global__ void insert_new_owner_kernel(const InsCluster* __restrict__ cl, u32 C, const u32* __restrict__ clusterNode, u32 n, u32* __restrict__ owner)
+{
+  for (u32 c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x)
+  {
+    const InsCluster k = cl[c];
+    for (u32 p = k.b; p < k.e; ++p)
+      owner[n + p] = clusterNode[c];
+  }
+}
+
+template<typename T>
+__global__ void insert_entities_kernel(const u32* __restrict__ src, u64 nTotal, u32 n, const u32* __restrict__ oldIds, const T* __restrict__ oldGeom,
+                                       const u32* __restrict__ newIdx, const T* __restrict__ newPts, u32* __restrict__ ids, T* __restrict__ geom)
+{
+  for (u64 k = blockIdx.x * u64(blockDim.x) + threadIdx.x; k < nTotal; k += u64(gridDim.x) * blockDim.x)
+  {
+    const u32 s = src[k];
+    const T* g;
+    if (s < n)
+    {
+      ids[k] = oldIds[s];
+      g = oldGeom + u64(s) * 3;
+    }
+    else
+    {
+      const u32 j = newIdx[s - n];
+      ids[k] = n + j;
+      g = newPts + u64(j) * 3;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      geom[k * 3 + c] = g[c];
+  }
+}
+
+template<typename T>
+__global__ void insert_nodes_kernel(const u32* __restrict__ bfsToDfs, u32 F, const u64* __restrict__ fk, u32 D, const u32* __restrict__ owner, u32 nTotal,
+                                    const u32* __restrict__ firstChild, const u32* __restrict__ childCount, const T* __restrict__ oldRootBox,
+                                    const T* __restrict__ minTab, const Space<T>* __restrict__ spg, uint4* __restrict__ link, u64* __restrict__ nodeKey,
+                                    T* __restrict__ nodeBox, unsigned char* __restrict__ nodeDepth)
+{
+  for (u32 b = blockIdx.x * blockDim.x + threadIdx.x; b < F; b += gridDim.x * blockDim.x)
+  {
+    const u32 u = bfsToDfs[b];
+    const u64 key = ins_key_of_dfs(fk[u], D);
+    const u32 d = ins_key_depth(key);
+    const u32 ownBegin = ins_lower_bound32(owner, 0, nTotal, u);
+    const u32 ownEnd = ins_lower_bound32(owner, ownBegin, nTotal, u + 1);
+    // the subtree: the depth-first keys from this node's up to the next cell of its depth
+    const u64 loc = key ^ (u64(1) << (3 * d));
+    const u64 endKey = ((loc + 1) << (3 * (D - d))) << 5;
+    const u32 j = ins_lower_bound(fk, u + 1, F, endKey);
+    const u32 subtreeEnd = j < F ? ins_lower_bound32(owner, ownEnd, nTotal, j) : nTotal;
+    const u32 cc = childCount[b];
+    link[b] = make_uint4((cc ? firstChild[b] : 0u) | (cc << kChildShift), ownBegin, ownEnd, subtreeEnd);
+    nodeKey[b] = key;
+    nodeDepth[b] = (unsigned char)d;
+    if (b == 0)
+    {
+#pragma unroll
+      for (int c = 0; c < 6; ++c)
+        nodeBox[c] = oldRootBox[c];
+    }
+    else
+      write_node_min(nodeBox, b, key, d, minTab, (u64(2) << D) - 1, spg->nodeSize);
+  }
+}
+
+template<typename T, typename R>
+static int insert_impl(TreeState& t, const T* pts, u64 n2, cudaStream_t st)
+{
+  using U = typename Ord<T>::U;
+  const u32 D = t.D;
+  const u64 n = t.n;
+  const u32 M = u32(t.nodeCount);
+  const u64 nt = n + n2;
+  u32* err = t.err.as<u32>();
+  cudaError_t e;
+  u32 hostErr = 0;
+  auto read_err = [&](const char* what) -> int {
+    cudaError_t ce = cudaMemcpyAsync(&hostErr, err, sizeof(u32), cudaMemcpyDeviceToHost, st);
+    if (!ce)
+      ce = cudaStreamSynchronize(st);
+    if (ce)
+      return cuda_status(ce, what);
+    return OTG_OK;
+  };
+  cudaMemsetAsync(err, 0, sizeof(u32), st);
+
+  // 1. keys of the new points, sorted (stable: equal locations keep their input order)
+  TmpBuf nk, nv;
+  if ((e = nk.ensure(sizeof(u64) * n2, st)) || (e = nv.ensure(sizeof(u32) * n2, st)))
+    return cuda_status(e, "allocating insert keys");
+  insert_keys_kernel<T, R, u64><<<blocks_for(n2), 256, 0, st>>>(pts, n2, t.space.as<Space<T>>(), t.rasterTab.as<U>(), 1u << D, nk.as<u64>(),
+                                                                nv.as<u32>(), err);
+  if (int rc = read_err("computing insert keys"))
+    return rc;
+  if (hostErr & kErrArgument)
+  {
+    set_error("otg_tree_insert: a point lies outside the tree's space (nothing inserted)");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  if (int rc = sort_pairs_u64(nk.as<u64>(), nv.as<u32>(), n2, 3 * D + 1, st, err))
+    return rc;
+
+  // 2. clustering rounds
+  TmpBuf itemsA, itemsB, clusters, counters;
+  if ((e = itemsA.ensure(sizeof(InsItem) * n2, st)) || (e = itemsB.ensure(sizeof(InsItem) * n2, st)) ||
+      (e = clusters.ensure(sizeof(InsCluster) * n2, st)) || (e = counters.ensure(sizeof(u32) * 2, st)))
+    return cuda_status(e, "allocating insert work");
+  const InsItem root{ 0, u32(n2), 3 * D, 0, 0 };
+  if ((e = cudaMemcpyAsync(itemsA.p, &root, sizeof(root), cudaMemcpyHostToDevice, st)))
+    return cuda_status(e, "starting insert work");
+  u32* dCount = counters.as<u32>(); // [0] items of the next round, [1] clusters
+  cudaMemsetAsync(dCount, 0, sizeof(u32) * 2, st);
+  u32 nIn = 1, hc[2] = { 0, 0 };
+  for (u32 round = 0; nIn; ++round)
+  {
+    if (round > 3 * D + 2) // every round takes at least 3 bits off the items' remaining bits
+    {
+      set_error("otg_tree_insert: clustering did not converge");
+      return OTG_ERR_CUDA;
+    }
+    cudaMemsetAsync(dCount, 0, sizeof(u32), st);
+    insert_round_kernel<u64><<<grid_blocks(u64(nIn) * 32, 256), 256, 0, st>>>(nk.as<u64>(), D, t.maxElem, itemsA.as<InsItem>(), nIn, itemsB.as<InsItem>(),
+                                                                             dCount, u32(n2), clusters.as<InsCluster>(), dCount + 1, u32(n2), err);
+    if ((e = cudaMemcpyAsync(hc, dCount, sizeof(hc), cudaMemcpyDeviceToHost, st)) || (e = cudaStreamSynchronize(st)))
+      return cuda_status(e, "clustering inserted points");
+    if (hc[0] > n2 || hc[1] > n2)
+    {
+      set_error("otg_tree_insert: clustering work exceeded its capacity");
+      return OTG_ERR_OUT_OF_MEMORY;
+    }
+    nIn = hc[0];
+    swap(itemsA, itemsB);
+  }
+  const u32 C = hc[1];
+  itemsA.release();
+  itemsB.release();
+
+  // 3. node set: old nodes, cluster nodes and the lowest common ancestors of adjacent keys
+  const u64 m = u64(M) + C;
+  if (2 * m + 1 >= (u64(1) << kChildShift))
+  {
+    set_error("otg_tree_insert: node count too large for the 28-bit node index of this build");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
+  const u32 keyBits = 3 * D + 5;
+  TmpBuf ek, ev, first, idx, blockSums, total;
+  const u32 m2 = u32(2 * m);
+  const u32 nScanBlocks = (m2 + kScanBlock - 1) / kScanBlock;
+  if ((e = ek.ensure(sizeof(u64) * m2, st)) || (e = ev.ensure(sizeof(u32) * m2, st)) || (e = first.ensure(sizeof(u32) * m2, st)) ||
+      (e = idx.ensure(sizeof(u32) * m2, st)) || (e = blockSums.ensure(sizeof(u32) * nScanBlocks, st)) || (e = total.ensure(sizeof(u32), st)))
+    return cuda_status(e, "allocating insert node merge");
+  insert_entries_kernel<<<blocks_for(m), 256, 0, st>>>(t.nodeKey.as<u64>(), M, clusters.as<InsCluster>(), C, D, ek.as<u64>(), ev.as<u32>());
+  if (int rc = sort_pairs_u64(ek.as<u64>(), ev.as<u32>(), m, keyBits, st, err))
+    return rc;
+  insert_lca_kernel<<<blocks_for(m), 256, 0, st>>>(ek.as<u64>(), ev.as<u32>(), u32(m), D);
+  if (int rc = sort_pairs_u64(ek.as<u64>(), ev.as<u32>(), m2, keyBits, st, err))
+    return rc;
+  insert_first_kernel<<<blocks_for(m2), 256, 0, st>>>(ek.as<u64>(), m2, first.as<u32>());
+  scan_block_sums_kernel<<<nScanBlocks, kScanBlock, 0, st>>>(first.as<u32>(), m2, blockSums.as<u32>());
+  scan_sums_kernel<<<1, kScanBlock, 0, st>>>(blockSums.as<u32>(), nScanBlocks, total.as<u32>());
+  scan_add_kernel<<<nScanBlocks, kScanBlock, 0, st>>>(first.as<u32>(), m2, blockSums.as<u32>(), idx.as<u32>());
+  u32 F = 0;
+  if ((e = cudaMemcpyAsync(&F, total.p, sizeof(u32), cudaMemcpyDeviceToHost, st)) || (e = cudaStreamSynchronize(st)))
+    return cuda_status(e, "merging insert nodes");
+  TmpBuf fk, oldToNew, clusterNode;
+  if ((e = fk.ensure(sizeof(u64) * F, st)) || (e = oldToNew.ensure(sizeof(u32) * M, st)) || (e = clusterNode.ensure(sizeof(u32) * std::max<u32>(C, 1), st)))
+    return cuda_status(e, "allocating insert nodes");
+  insert_compact_kernel<<<blocks_for(m2), 256, 0, st>>>(ek.as<u64>(), ev.as<u32>(), first.as<u32>(), idx.as<u32>(), m2, M, C, fk.as<u64>(),
+                                                        oldToNew.as<u32>(), clusterNode.as<u32>());
+  ek.release();
+  ev.release();
+  first.release();
+  idx.release();
+
+  // 4. parents, link levels, breadth-first order
+  TmpBuf parent, level, depthCount, bk, bv, dfsToBfs, firstChild, childCount;
+  if ((e = parent.ensure(sizeof(u32) * F, st)) || (e = level.ensure(sizeof(u32) * F, st)) || (e = depthCount.ensure(sizeof(u32) * 64, st)) ||
+      (e = bk.ensure(sizeof(u64) * F, st)) || (e = bv.ensure(sizeof(u32) * F, st)) || (e = dfsToBfs.ensure(sizeof(u32) * F, st)) ||
+      (e = firstChild.ensure(sizeof(u32) * F, st)) || (e = childCount.ensure(sizeof(u32) * F, st)))
+    return cuda_status(e, "allocating insert links");
+  cudaMemsetAsync(depthCount.p, 0, sizeof(u32) * 64, st);
+  insert_parents_kernel<<<blocks_for(F), 256, 0, st>>>(fk.as<u64>(), F, D, parent.as<u32>(), level.as<u32>(), depthCount.as<u32>());
+  insert_bfs_keys_kernel<<<blocks_for(F), 256, 0, st>>>(level.as<u32>(), F, bk.as<u64>(), bv.as<u32>());
+  if (int rc = sort_pairs_u64(bk.as<u64>(), bv.as<u32>(), F, 40, st, err))
+    return rc;
+  const u32* bfsToDfs = bv.as<u32>();
+  insert_bfs_index_kernel<<<blocks_for(F), 256, 0, st>>>(bfsToDfs, F, dfsToBfs.as<u32>());
+  cudaMemsetAsync(firstChild.p, 0xff, sizeof(u32) * F, st);
+  cudaMemsetAsync(childCount.p, 0, sizeof(u32) * F, st);
+  insert_links_kernel<<<blocks_for(F), 256, 0, st>>>(dfsToBfs.as<u32>(), F, parent.as<u32>(), firstChild.as<u32>(), childCount.as<u32>());
+
+  // 5. entities ordered by their node (depth-first), old ones first within a node
+  TmpBuf owner, src;
+  if ((e = owner.ensure(sizeof(u32) * nt, st)) || (e = src.ensure(sizeof(u32) * nt, st)))
+    return cuda_status(e, "allocating insert owners");
+  insert_owner_init_kernel<<<blocks_for(nt), 256, 0, st>>>(nt, F, owner.as<u32>(), src.as<u32>());
+  insert_old_owner_kernel<<<blocks_for(M), 256, 0, st>>>(t.nodeLink.as<uint4>(), M, oldToNew.as<u32>(), owner.as<u32>());
+  insert_new_owner_kernel<<<blocks_for(std::max<u32>(C, 1)), 256, 0, st>>>(clusters.as<InsCluster>(), C, clusterNode.as<u32>(), u32(n), owner.as<u32>());
+  if (int rc = sort_pairs_u32(owner.as<u32>(), src.as<u32>(), nt, bit_count(F), st, err)) // owners 0 .. F
+    return rc;
+
+  // 6. the new tree
+  DevBuf ids, geom, link, key, box, depth;
+  if ((e = ids.ensure(sizeof(u32) * nt)) || (e = geom.ensure(sizeof(T) * 3 * nt)) || (e = link.ensure(sizeof(uint4) * F)) ||
+      (e = key.ensure(sizeof(u64) * F)) || (e = box.ensure(sizeof(T) * 6 * F)) || (e = depth.ensure(F)))
+    return cuda_status(e, "allocating the inserted tree");
+  insert_entities_kernel<T><<<blocks_for(nt), 256, 0, st>>>(src.as<u32>(), nt, u32(n), t.sortedIds.as<u32>(), t.sortedGeom.as<T>(), nv.as<u32>(), pts,
+                                                            ids.as<u32>(), geom.as<T>());
+  insert_nodes_kernel<T><<<blocks_for(F), 256, 0, st>>>(bfsToDfs, F, fk.as<u64>(), D, owner.as<u32>(), u32(nt), firstChild.as<u32>(),
+                                                        childCount.as<u32>(), t.nodeBox.as<T>(), t.minTab.as<T>(), t.space.as<Space<T>>(),
+                                                        link.as<uint4>(), key.as<u64>(), box.as<T>(), depth.as<unsigned char>());
+  std::vector<u32> dc(64);
+  if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(dc.data(), depthCount.p, sizeof(u32) * 64, cudaMemcpyDeviceToHost, st)))
+    return cuda_status(e, "inserting points");
+  if (int rc = read_err("inserting points"))
+    return rc;
+  if (hostErr & kErrTimeout)
+  {
+    set_error("radix sort look-back wait ran out of its iteration limit");
+    return OTG_ERR_TIMEOUT;
+  }
+  if (hostErr & kErrCapacity)
+  {
+    set_error("otg_tree_insert: clustering work exceeded its capacity");
+    return OTG_ERR_OUT_OF_MEMORY;
+  }
+  std::swap(t.sortedIds, ids);
+  std::swap(t.sortedGeom, geom);
+  std::swap(t.nodeLink, link);
+  std::swap(t.nodeKey, key);
+  std::swap(t.nodeBox, box);
+  std::swap(t.nodeDepth, depth);
+  t.n = nt;
+  t.nodeCount = F;
+  t.maxNodes = F;
+  t.levelCountsHost.assign(dc.begin(), dc.begin() + D + 1);
+  t.sortedKeys = nullptr;
+  t.inserted = true;
+  t.image32 = false;
+  return OTG_OK;
+}
+
+int insert_points(TreeState& t, const void* entities, u64 n2, int mem, cudaStream_t st)
+{
+  if (t.trees)
+  {
+    set_error("otg_tree_insert: not for forests");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
+  if (t.kind != OTG_KIND_POINTS)
+  {
+    set_error("otg_tree_insert: point trees only (box trees would also need their node geometry updated)");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
+  if (n2 == 0)
+    return OTG_OK;
+  if (t.n == 0)
+  {
+    set_error("otg_tree_insert: the tree is empty (its space is defined by a Create with entities)");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
+  if (t.n + n2 >= (u64(1) << 30))
+  {
+    set_error("entity count must be below 2^30");
+    return OTG_ERR_INVALID_ARGUMENT;
+  }
+  cudaError_t e;
+  if (!t.inserted && t.sortedKeys)
+  {
+    // a point outside a given space has the location key 0 and sorts first; the reference keeps it
+    // in a node that the root does not link
+    u64 first = 0;
+    if ((e = cudaMemcpyAsync(&first, t.sortedKeys, t.keys32 ? 4 : 8, cudaMemcpyDeviceToHost, st)) || (e = cudaStreamSynchronize(st)))
+      return cuda_status(e, "reading the first location");
+    if (first == 0)
+    {
+      set_error("otg_tree_insert: the tree holds points outside its space, which no node reachable from the root holds");
+      return OTG_ERR_NOT_SUPPORTED;
+    }
+  }
+  const size_t esz = t.scalar == OTG_SCALAR_F64 ? 8 : 4;
+  TmpBuf hostCopy;
+  const void* src = entities;
+  if (mem == OTG_MEM_HOST)
+  {
+    if ((e = hostCopy.ensure(esz * 3 * n2, st)) || (e = cudaMemcpyAsync(hostCopy.p, entities, esz * 3 * n2, cudaMemcpyHostToDevice, st)))
+      return cuda_status(e, "copying inserted points");
+    src = hostCopy.p;
+  }
+  const bool rasterDouble = t.scalar == OTG_SCALAR_F64 || t.D >= 16;
+  int rc;
+  if (t.scalar == OTG_SCALAR_F64)
+    rc = insert_impl<double, double>(t, static_cast<const double*>(src), n2, st);
+  else if (rasterDouble)
+    rc = insert_impl<float, double>(t, static_cast<const float*>(src), n2, st);
+  else
+    rc = insert_impl<float, float>(t, static_cast<const float*>(src), n2, st);
+  if (rc == OTG_OK && (e = cudaStreamSynchronize(st)))
+    return cuda_status(e, "inserting points");
+  return rc;
 }
 
 } // namespace otg

@@ -241,6 +241,20 @@ extern "C"
     return set_entities(t->s, entities, n, mem, (cudaStream_t)stream);
   }
 
+  int otg_tree_insert(otg_tree* t, const void* entities, uint64_t n, int mem, void* stream)
+  {
+    if (int rc = ready(t, (cudaStream_t)stream))
+      return rc;
+    if ((n && !entities) || (mem != OTG_MEM_HOST && mem != OTG_MEM_DEVICE))
+    {
+      set_error("otg_tree_insert: invalid argument");
+      return OTG_ERR_INVALID_ARGUMENT;
+    }
+    if (int rc = require_device())
+      return rc;
+    return insert_points(t->s, entities, n, mem, (cudaStream_t)stream);
+  }
+
   int otg_tree_sync(otg_tree* t, void* stream)
   {
     if (int rc = require_tree(t))

@@ -198,6 +198,9 @@ struct TreeState
   DevBuf geom32;     // FP32 image of sortedGeom for the query filters (built on first use)
   DevBuf nodeBox32;  // FP32 outward-rounded node boxes for the query filters
   bool image32 = false;
+  // a bulk Insert changed the tree: nodes may own entities beside their children and child links
+  // may skip levels, which the static array layout cannot hold
+  bool inserted = false;
 
   // cached after the build (host copies, filled by sync)
   u64 nodeCount = 0;
@@ -250,6 +253,7 @@ int build_forest(TreeState& t, const void* entities, const u64* treeOffsets, u32
                  cudaStream_t st);
 int finish_build(TreeState& t, cudaStream_t st);
 int set_entities(TreeState& t, const void* entities, u64 n, int mem, cudaStream_t st);
+int insert_points(TreeState& t, const void* entities, u64 n, int mem, cudaStream_t st);
 int forest_relaunch(TreeState& t, const void* entities, const void* boxes, cudaStream_t st);
 int export_locations(const TreeState& t, u64* keys, int mem, cudaStream_t st);
 int export_nodes(const TreeState& t, u64* keys, double* minSize, u64* eoff, u32* eids, u32* childCount);

@@ -414,6 +414,13 @@ int export_static(TreeState& t, otg_static_layout* out, cudaStream_t st)
     set_error("otg_tree_export_static: the static layout is defined for a single tree, not a forest");
     return OTG_ERR_INVALID_ARGUMENT;
   }
+  if (t.inserted)
+  {
+    // the reference's static tree has no Insert, and its layout is a Create's (one child segment per
+    // node, entities only in leaves)
+    set_error("otg_tree_export_static: the tree was changed by Insert; create it from all its entities instead");
+    return OTG_ERR_NOT_SUPPORTED;
+  }
   int rc = finish_build(t, st);
   if (rc)
     return rc;

@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <random>
+#include <unordered_set>
 #include <vector>
 
 extern "C"
@@ -26,6 +27,7 @@ extern "C"
   void* oro_collide_self(void* h, double tol);
   void* oro_collide_pair(void* h1, void* h2, double tol);
   void oro_set_entities(void* h, const void* ent, uint64_t n);
+  int oro_insert(void* h, const void* ent, uint64_t n);
   uint64_t oro_res_nq(void* r);
   uint64_t oro_res_total(void* r);
   void oro_res_copy(void* r, uint64_t* offsets, uint32_t* ids, double* dist);
@@ -326,6 +328,55 @@ int main()
       if (!refused)
       {
         std::printf("MISMATCH Core KeepNodes: a span of another size was not refused\n");
+        ++g_fail;
+      }
+    }
+    // bulk Insert: Managed Add and Core Insert of new points, against the oracle's Insert
+    {
+      std::vector<Point3D> base(pts.begin(), pts.begin() + 20000), add(pts.begin() + 20000, pts.begin() + 26000);
+      for (std::size_t i = 0; i < add.size(); i += 2)
+        add[i] = { 40.0 + 0.01 * N(rng), 60.0 + 0.01 * N(rng), 20.0 + 0.01 * N(rng) }; // a deep cluster
+      OctreePointM tm(base, 8, std::nullopt, 20);
+      OctreePoint ti(std::span<const Point3D>(base), 8, std::nullopt, 20);
+      void* oi = oro_create(0, 0, base.data(), base.size(), 8, nullptr, 20);
+      const bool ok = oro_insert(oi, add.data(), add.size()) && tm.Add(std::span<const Point3D>(add)) &&
+                      ti.Insert(std::span<const Point3D>(add), std::span<const Point3D>(base));
+      if (!ok || tm.GetEntityCount() != base.size() + add.size() || tm.GetNodeCount() != ti.GetNodeCount())
+      {
+        std::printf("MISMATCH Insert: refused or counts differ\n");
+        ++g_fail;
+      }
+      std::vector<Point3D> all(base);
+      all.insert(all.end(), add.begin(), add.end());
+      std::span<const Point3D> allSpan(all);
+      void* r = oro_range(oi, ranges.data(), nq, 0, -1.0);
+      for (int i = 0; i < nq; ++i)
+      {
+        expect(tm.RangeSearch(ranges[i]), r, i, "Managed Add: RangeSearch");
+        expect(ti.RangeSearch(ranges[i], allSpan), r, i, "Core Insert: RangeSearch");
+      }
+      oro_res_free(r);
+      std::vector<uint32_t> k(nq, 11);
+      r = oro_knn(oi, qp.data(), nq, k.data(), -1.0, -1.0);
+      for (int i = 0; i < nq; ++i)
+      {
+        expect(tm.GetNearestNeighbors(qp[i], 11), r, i, "Managed Add: GetNearestNeighbors");
+        expect(ti.GetNearestNeighbors(qp[i], 11, allSpan), r, i, "Core Insert: GetNearestNeighbors");
+      }
+      oro_res_free(r);
+      r = oro_pick(oi, add.data(), nq, -1.0);
+      for (int i = 0; i < nq; ++i)
+        expect(tm.PickSearch(add[i]), r, i, "Managed Add: PickSearch");
+      oro_res_free(r);
+      oro_destroy(oi);
+      // a point outside the space: nothing inserted, its id in failedEntities
+      const std::vector<Point3D> bad{ { 50.0, 50.0, 50.0 }, { 150.0, 50.0, 50.0 } };
+      std::unordered_set<EntityID> failed;
+      const std::size_t nodes = ti.GetNodeCount();
+      if (tm.Add(std::span<const Point3D>(bad)) || ti.Insert(std::span<const Point3D>(bad), allSpan, nullptr, &failed) || failed.size() != 1 ||
+          !failed.count(EntityID(all.size() + 1)) || ti.GetNodeCount() != nodes || tm.GetEntityCount() != all.size())
+      {
+        std::printf("MISMATCH Insert: a point outside the space was not refused\n");
         ++g_fail;
       }
     }

@@ -6,28 +6,10 @@ import numpy as np
 import pytest
 
 from _compare import assert_csr_equal, assert_nodes_equal
+from _insert_cases import insert_case
 from _oracle_lib import KIND_POINTS, oracle, reference
 
 pytestmark = pytest.mark.skipif(reference() is None, reason="reference harness not built here")
-
-
-def _new_points(rng, n, dtype):
-    """Points inside [0, 10)^3: half uniform, half in a few tight clusters (deep new nodes)."""
-    u = rng.random((n // 2, 3)) * 10
-    c = rng.random((6, 3)) * 9.5 + 0.2
-    cl = c[rng.integers(0, 6, n - n // 2)] + rng.normal(0, 0.01, (n - n // 2, 3))
-    return np.clip(np.concatenate([u, cl]), 0.0, 9.999).astype(dtype)
-
-
-def insert_case(seed):
-    rng = np.random.default_rng(seed)
-    dtype = np.float32 if seed % 3 == 2 else np.float64
-    base = (rng.random((int(rng.integers(200, 6000)), 3)) * 10).astype(dtype)
-    depth = int(rng.integers(3, 11))
-    max_elem = int(rng.choice([1, 4, 8, 20, 64]))
-    box = np.array([0.0, 0, 0, 10, 10, 10], dtype)
-    batches = [_new_points(rng, int(rng.integers(1, 5000)), dtype) for _ in range(1 + seed % 2)]
-    return base, depth, box, max_elem, batches
 
 
 @pytest.mark.parametrize("seed", range(12))
