@@ -1099,7 +1099,8 @@ def run_insert(reps=3, cpu=True):
     add_d = torch.as_tensor(add, device="cuda")
     add_pinned = torch.as_tensor(add).pin_memory()
     out = {"insert_points": len(add), "into_tree_points": len(pts)}
-    dev_ms, host_ms, nodes = [], [], 0
+    dev_ms, host_ms, nodes, phases = [], [], 0, []
+    otg.profile_enable(True)
     for r in range(reps + 1):
         for src, acc in ((add_d, dev_ms), (add_pinned.numpy(), host_ms)):
             t = otg.Tree("points").create(pts_d, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
@@ -1110,8 +1111,11 @@ def run_insert(reps=3, cpu=True):
             ms = (time.perf_counter() - t0) * 1e3
             if r:
                 acc.append(ms)
+                if src is add_d:
+                    phases.append(dict(otg.profile_phases()))
             nodes = t.node_count
             del t
+    otg.profile_enable(False)
     allp = torch.cat([pts_d, add_d])
     rebuild = []
     for r in range(reps + 1):
@@ -1127,6 +1131,8 @@ def run_insert(reps=3, cpu=True):
     out["insert_1M_into_16M_host_input_ms"] = statistics.median(host_ms)
     out["insert_Mpts_per_s"] = len(add) / statistics.median(dev_ms) / 1e3
     out["nodes_after_insert"] = int(nodes)
+    if phases and phases[0]:
+        out["insert_phases_ms"] = {k: statistics.median(p[k] for p in phases) for k in phases[0]}
     out["create_17M_ms"] = statistics.median(rebuild)
     # the same small case on the GPU and in the oracle
     small, small_add = pts[::16], add[::16]
@@ -1153,7 +1159,7 @@ def run_insert(reps=3, cpu=True):
     return out
 
 
-PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m", "build_4m_clustered", "forest_frustum_1024")
+PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m", "build_4m_clustered", "forest_frustum_1024", "insert_16m_1m", "insert_4m_250k")
 
 
 def run_profile_case(name):
@@ -1200,6 +1206,16 @@ def run_profile_case(name):
         for _ in range(2):
             t.create(pts, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
         t.sync()
+        print(json.dumps({"case": name, "nodes": int(t.node_count)}))
+    elif name in ("insert_16m_1m", "insert_4m_250k"):
+        # Insert of new shell points into a fresh shell tree, twice (the launch list covers both)
+        n, m = (16_000_000, 1_000_000) if name == "insert_16m_1m" else (4_000_000, 250_000)
+        pts = shell_points(n, 301)
+        add = torch.as_tensor(inside(shell_points(m + m // 20, 311), pts)[:m], device="cuda")
+        pts = torch.as_tensor(pts, device="cuda")
+        for _ in range(2):
+            t = otg.Tree("points").create(pts, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
+            t.insert(add)
         print(json.dumps({"case": name, "nodes": int(t.node_count)}))
     elif name == "build_4m":
         pts = torch.as_tensor(shell_points(4_000_000, 301), device="cuda")

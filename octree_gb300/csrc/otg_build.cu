@@ -1419,6 +1419,7 @@ int build_tree(TreeState& t, const void* entities, u64 n, u32 maxDepth, const vo
   t.countsKnown = false;
   t.image32 = false;
   t.inserted = false;
+  t.retired.clear();
   t.trees = 0;
   t.boxGiven = box != nullptr;
   cudaError_t e;
@@ -1904,6 +1905,7 @@ int build_forest(TreeState& t, const void* entities, const u64* treeOffsets, u32
   t.countsKnown = false;
   t.image32 = false;
   t.inserted = false;
+  t.retired.clear();
   t.trees = trees;
   t.boxGiven = boxes != nullptr;
   cudaError_t e;
@@ -2194,33 +2196,30 @@ int export_nodes(const TreeState& t, u64* keys, double* minSize, u64* eoff, u32*
 // update (UpdateNodeGeometry :866-1005 only unites MBRs). New entity i gets id n + i.
 //  1. keys of the new points from the tree's own grid (the rasterisation tables of its Create), and
 //     a stable radix sort of them;
-//  2. the reference's clustering of the sorted new points, in rounds, one warp per work item:
-//     an item of at most maxElementNo points becomes one cluster at its location (:1304-1308), an
-//     item of at most 256 (or one whose remaining bits are 0: identical locations) is walked
-//     greedily (:1237-1291, one lane), a larger one is split by the next 9 bits into buckets found
-//     by binary search, each with the fold of its locations (lowest common ancestor, :1153-1199);
+//  2. the reference's clustering of the sorted new points, in rounds: an item of at most
+//     maxElementNo points becomes one cluster at its location (:1304-1308), an item of at most 256
+//     (or one whose remaining bits are 0: identical locations) is walked greedily (:1237-1291, one
+//     lane), a larger one is split by the next 9 bits into buckets found by binary search, each with
+//     the fold of its locations (lowest common ancestor, :1153-1199). Items and clusters partition
+//     the sorted points, so each is stored at the sorted position where it begins: no counters, and
+//     a fixed number of rounds (every split takes at least min(9, bits) bits off an item);
 //  3. the node set after LinkOrphanNodes: the old nodes, the clusters' nodes and the lowest common
-//     ancestors of DFS-adjacent keys (the branch nodes the linking creates where two nodes claim
-//     the same child slot), each node's parent its nearest ancestor in the set (a child link may
-//     skip levels);
+//     ancestors of depth-first neighbours (the branch nodes the linking creates where two nodes
+//     claim one child slot); each node's parent is its nearest ancestor in the set (a child link
+//     may skip levels);
 //  4. the tree laid out again: nodes breadth first by link level (children contiguous, in slot
 //     order), entities ordered by their node in depth-first order (own entities and subtrees
-//     contiguous), MinPoint geometry from the node keys.
+//     contiguous, old entities before new ones in a node), MinPoint geometry from the node keys.
 // A new point outside the tree's space is refused (OTG_ERR_INVALID_ARGUMENT, nothing inserted): the
 // reference would store it with a location code of 0.
 namespace otg
 {
 namespace
 {
-struct InsItem
+struct InsItem // a run [b, e) of sorted new points; e == 0: an empty slot
 {
   u32 b, e, bits, depth;
   u64 loc;
-};
-struct InsCluster
-{
-  u32 b, e;
-  u64 key;
 };
 
 __device__ __forceinline__ u32 ins_fold_depth(u64 diff, u32 D)
@@ -2265,18 +2264,6 @@ __device__ __forceinline__ u32 ins_lower_bound(const u64* a, u32 lo, u32 hi, u64
   }
   return lo;
 }
-__device__ __forceinline__ u32 ins_lower_bound32(const u32* a, u32 lo, u32 hi, u32 v)
-{
-  while (lo < hi)
-  {
-    const u32 mid = lo + ((hi - lo) >> 1);
-    if (a[mid] < v)
-      lo = mid + 1;
-    else
-      hi = mid;
-  }
-  return lo;
-}
 } // namespace
 
 template<typename T, typename R, typename K>
@@ -2304,86 +2291,84 @@ __global__ void __launch_bounds__(256) insert_keys_kernel(const T* __restrict__ 
   }
 }
 
-// One round of the clustering: a warp per item. keys: the sorted new keys (location + 1).
-template<typename K>
-__global__ void __launch_bounds__(256) insert_round_kernel(const K* __restrict__ keys, u32 D, u64 maxElem, const InsItem* __restrict__ in, u32 nIn,
-                                                           InsItem* __restrict__ out, u32* __restrict__ nOut, u32 outCap, InsCluster* __restrict__ cl,
-                                                           u32* __restrict__ nCl, u32 clCap, u32* __restrict__ err)
+// One round of the clustering over the item slots `in` (n2 of them, most empty): clusters go to
+// (clEnd, clKey) at their first position, items to split to the list `splits` (their buckets are
+// searched by insert_split_kernel, one thread per bucket). The 32 slots of a warp are taken in
+// turn, each valid one by the whole warp. keys: the sorted new keys (location + 1).
+__global__ void __launch_bounds__(256) insert_round_kernel(const u64* __restrict__ keys, u32 n2, u32 D, u64 maxElem, const InsItem* __restrict__ in,
+                                                           u32* __restrict__ clEnd, u64* __restrict__ clKey, InsItem* __restrict__ splits,
+                                                           u32* __restrict__ nSplits, u32 splitCap, u32* __restrict__ err)
 {
   const u32 lane = threadIdx.x & 31;
   const u32 warps = (gridDim.x * blockDim.x) >> 5;
-  auto push_cluster = [&](u32 b, u32 e, u64 key) {
-    const u32 slot = atomicAdd(nCl, 1u);
-    if (slot < clCap)
-      cl[slot] = InsCluster{ b, e, key };
-    else
-      atomicOr(err, kErrCapacity);
-  };
-  for (u32 it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < nIn; it += warps)
+  for (u32 base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < n2; base += warps * 32)
   {
-    const InsItem w = in[it];
-    const u32 num = w.e - w.b;
-    if (num == 0)
-      continue;
-    if (num <= maxElem) // :1304-1308 one cluster at the item's fold
+    const u32 p = base + lane;
+    InsItem mine{ 0, 0, 0, 0, 0 };
+    if (p < n2)
+      mine = in[p];
+    u32 todo = __ballot_sync(0xffffffffu, mine.e != 0);
+    while (todo)
     {
-      if (lane == 0)
-        push_cluster(w.b, w.e, ins_node_key(w.loc, w.depth, D));
-      continue;
-    }
-    if (w.bits == 0) // identical locations: the walk makes one cluster of them at the max depth
-    {
-      if (lane == 0)
-        push_cluster(w.b, w.e, ins_node_key(u64(keys[w.b]) - 1, D, D));
-      continue;
-    }
-    if (num <= 256) // :1310-1317 emitSortedRange (:1237-1291), sequential on one lane
-    {
-      if (lane == 0)
+      const int src = __ffs(todo) - 1;
+      todo &= todo - 1;
+      InsItem w;
+      w.b = __shfl_sync(0xffffffffu, mine.b, src);
+      w.e = __shfl_sync(0xffffffffu, mine.e, src);
+      w.bits = __shfl_sync(0xffffffffu, mine.bits, src);
+      w.depth = __shfl_sync(0xffffffffu, mine.depth, src);
+      w.loc = __shfl_sync(0xffffffffu, mine.loc, src);
+      const u32 num = w.e - w.b;
+      if (num <= maxElem) // :1304-1308 one cluster at the item's fold
       {
-        u32 cb = w.b;
-        while (cb < w.e)
+        if (lane == 0)
         {
-          const u64 base = u64(keys[cb]) - 1;
-          u64 diff = 0;
-          u32 ce = cb + 1;
-          while (ce < w.e)
-          {
-            const u64 nd = diff | (base ^ (u64(keys[ce]) - 1));
-            const u32 newDepth = ins_fold_depth(nd, D);
-            if (u64(ce - cb + 1) > maxElem && newDepth < D && newDepth < ins_fold_depth(diff, D))
-              break;
-            diff = nd;
-            ++ce;
-          }
-          push_cluster(cb, ce, ins_node_key(base, ins_fold_depth(diff, D), D));
-          cb = ce;
+          clEnd[w.b] = w.e;
+          clKey[w.b] = ins_node_key(w.loc, w.depth, D);
         }
+        continue;
       }
-      continue;
-    }
-    // radixPartition (:1153-1199): buckets of the next min(9, bits) bits; all locations of the item
-    // share the bits above w.bits
-    const u32 numBits = min(9u, w.bits);
-    const u32 shift = w.bits - numBits;
-    const u32 nd = 1u << numBits;
-    const u64 prefix = w.bits >= 64 ? 0 : (((u64(keys[w.b]) - 1) >> w.bits) << w.bits);
-    for (u32 d0 = 0; d0 < nd; d0 += 32)
-    {
-      const u32 d = d0 + lane;
-      if (d >= nd)
-        break;
-      const u64 lo = prefix | (u64(d) << shift);
-      const u64 hi = lo + (u64(1) << shift);
-      const u32 bb = lower_bound_key(keys, w.b, w.e, lo + 1);
-      const u32 be = lower_bound_key(keys, bb, w.e, hi + 1);
-      if (be > bb)
+      if (w.bits == 0) // identical locations: the walk makes one cluster of them at the max depth
       {
-        const u64 l0 = u64(keys[bb]) - 1, l1 = u64(keys[be - 1]) - 1;
-        const u32 depth = ins_fold_depth(l0 ^ l1, D);
-        const u32 slot = atomicAdd(nOut, 1u);
-        if (slot < outCap)
-          out[slot] = InsItem{ bb, be, min((D - depth) * 3u, shift), depth, l0 };
+        if (lane == 0)
+        {
+          clEnd[w.b] = w.e;
+          clKey[w.b] = ins_node_key(keys[w.b] - 1, D, D);
+        }
+        continue;
+      }
+      if (num <= 256) // :1310-1317 emitSortedRange (:1237-1291), sequential on one lane
+      {
+        if (lane == 0)
+        {
+          u32 cb = w.b;
+          while (cb < w.e)
+          {
+            const u64 first = keys[cb] - 1;
+            u64 diff = 0;
+            u32 ce = cb + 1;
+            while (ce < w.e)
+            {
+              const u64 nd = diff | (first ^ (keys[ce] - 1));
+              const u32 newDepth = ins_fold_depth(nd, D);
+              if (u64(ce - cb + 1) > maxElem && newDepth < D && newDepth < ins_fold_depth(diff, D))
+                break;
+              diff = nd;
+              ++ce;
+            }
+            clEnd[cb] = ce;
+            clKey[cb] = ins_node_key(first, ins_fold_depth(diff, D), D);
+            cb = ce;
+          }
+        }
+        continue;
+      }
+      // radixPartition (:1153-1199): to the list of items to split
+      if (lane == 0)
+      {
+        const u32 slot = atomicAdd(nSplits, 1u);
+        if (slot < splitCap)
+          splits[slot] = w;
         else
           atomicOr(err, kErrCapacity);
       }
@@ -2391,33 +2376,40 @@ __global__ void __launch_bounds__(256) insert_round_kernel(const K* __restrict__
   }
 }
 
-// entries of the node-set merge: (depth-first key, tag): old nodes (tag = old index), clusters
-// (tag = M + cluster), branch candidates (tag = M + C + i, from the first merge pass)
-__global__ void insert_entries_kernel(const u64* __restrict__ nodeKey, u32 M, const InsCluster* __restrict__ cl, u32 C, u32 D, u64* __restrict__ ek,
-                                      u32* __restrict__ ev)
+// radixPartition (:1153-1199) of the listed items, one thread per (item, bucket of the next
+// min(9, bits) bits): the bucket's run by two binary searches, its fold from its first and last
+// location, the child item written to `out` at its first position. All locations of an item share
+// the bits above its remaining bits.
+__global__ void __launch_bounds__(256) insert_split_kernel(const u64* __restrict__ keys, u32 D, const InsItem* __restrict__ splits,
+                                                           const u32* __restrict__ nSplits, u32 splitCap, InsItem* __restrict__ out)
 {
-  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < M + C; i += gridDim.x * blockDim.x)
+  const u64 tasks = u64(min(*nSplits, splitCap)) << 9;
+  for (u64 t = blockIdx.x * u64(blockDim.x) + threadIdx.x; t < tasks; t += u64(gridDim.x) * blockDim.x)
   {
-    ek[i] = ins_dfs_key(i < M ? nodeKey[i] : cl[i - M].key, D);
-    ev[i] = i;
+    const InsItem w = splits[t >> 9];
+    const u32 d = u32(t & 511u);
+    const u32 numBits = min(9u, w.bits);
+    if (d >= (1u << numBits))
+      continue;
+    const u32 shift = w.bits - numBits;
+    const u64 prefix = w.bits >= 64 ? 0 : (((keys[w.b] - 1) >> w.bits) << w.bits);
+    const u64 lo = prefix | (u64(d) << shift);
+    const u64 hi = lo + (u64(1) << shift);
+    const u32 bb = ins_lower_bound(keys, w.b, w.e, lo + 1);
+    const u32 be = ins_lower_bound(keys, bb, w.e, hi + 1);
+    if (be > bb)
+    {
+      const u64 l0 = keys[bb] - 1, l1 = keys[be - 1] - 1;
+      const u32 depth = ins_fold_depth(l0 ^ l1, D);
+      out[bb] = InsItem{ bb, be, min((D - depth) * 3u, shift), depth, l0 };
+    }
   }
 }
 
-// the lowest common ancestor of each adjacent pair of sorted entries, as a candidate entry without a
-// tag (the first entry repeats itself; equal keys give the key again)
-__global__ void insert_lca_kernel(u64* __restrict__ ek, u32* __restrict__ ev, u32 m, u32 D)
+__global__ void insert_root_item_kernel(InsItem* items, u32 n2, u32 D)
 {
-  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
-  {
-    ek[m + i] = i == 0 ? ek[0] : ins_dfs_key(ins_node_lca(ins_key_of_dfs(ek[i - 1], D), ins_key_of_dfs(ek[i], D)), D);
-    ev[m + i] = 0xffffffffu;
-  }
-}
-
-__global__ void insert_first_kernel(const u64* __restrict__ ek, u32 m, u32* __restrict__ first)
-{
-  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
-    first[i] = (i == 0 || ek[i] != ek[i - 1]) ? 1u : 0u;
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    items[0] = InsItem{ 0, n2, 3 * D, 0, 0 };
 }
 
 // exclusive scan of u32 values (three launches: block sums, their scan, the adds)
@@ -2524,152 +2516,312 @@ __global__ void __launch_bounds__(kScanBlock) scan_add_kernel(const u32* __restr
     out[i] = sums[blockIdx.x] + x - val + (w ? s[w - 1] : 0u);
 }
 
-// the distinct keys of the sorted entries, and where each old node and each cluster went
-__global__ void insert_compact_kernel(const u64* __restrict__ ek, const u32* __restrict__ ev, const u32* __restrict__ first, const u32* __restrict__ idx, u32 m,
-                                      u32 M, u32 C, u64* __restrict__ fk, u32* __restrict__ oldToNew, u32* __restrict__ clusterNode)
+// exclusive scan of v[0, m) into out; *total (device) the sum
+static int exclusive_scan_u32(const u32* v, u32 m, u32* out, u32* total, cudaStream_t st)
+{
+  const u32 nb = std::max<u32>(1, (m + kScanBlock - 1) / kScanBlock);
+  TmpBuf sums;
+  if (cudaError_t e = sums.ensure(sizeof(u32) * nb, st))
+    return cuda_status(e, "allocating scan sums");
+  scan_block_sums_kernel<<<nb, kScanBlock, 0, st>>>(v, m, sums.as<u32>());
+  scan_sums_kernel<<<1, kScanBlock, 0, st>>>(sums.as<u32>(), nb, total);
+  scan_add_kernel<<<nb, kScanBlock, 0, st>>>(v, m, sums.as<u32>(), out);
+  return cuda_status(cudaGetLastError(), "scanning");
+}
+
+__global__ void insert_cluster_flags_kernel(const u32* __restrict__ clEnd, u32 n2, u32* __restrict__ flag)
+{
+  for (u32 p = blockIdx.x * blockDim.x + threadIdx.x; p < n2; p += gridDim.x * blockDim.x)
+    flag[p] = clEnd[p] != 0 ? 1u : 0u;
+}
+
+// node-set entries: old nodes (tag = old index), then clusters (tag = M + cluster), as depth-first
+// keys; the clusters are compacted from their slots on the way
+__global__ void insert_entries_kernel(const u64* __restrict__ nodeKey, u32 M, const u32* __restrict__ clEnd, const u64* __restrict__ clKey,
+                                      const u32* __restrict__ clIdx, u32 n2, u32 D, u64* __restrict__ ek, u32* __restrict__ ev, u32* __restrict__ clBegin)
+{
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < M + n2; i += gridDim.x * blockDim.x)
+  {
+    if (i < M)
+    {
+      ek[i] = ins_dfs_key(nodeKey[i], D);
+      ev[i] = i;
+    }
+    else if (clEnd[i - M] != 0)
+    {
+      const u32 p = i - M, c = clIdx[p];
+      ek[M + c] = ins_dfs_key(clKey[p], D);
+      ev[M + c] = M + c;
+      clBegin[c] = p;
+    }
+  }
+}
+
+__global__ void insert_first_kernel(const u64* __restrict__ ek, u32 m, u32* __restrict__ first)
+{
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    first[i] = (i == 0 || ek[i] != ek[i - 1]) ? 1u : 0u;
+}
+
+// the distinct keys s0 of the sorted entries, and the distinct index of each old node and cluster
+__global__ void insert_unique_kernel(const u64* __restrict__ ek, const u32* __restrict__ ev, const u32* __restrict__ first, const u32* __restrict__ idx,
+                                     u32 m, u64* __restrict__ s0, u32* __restrict__ s0Of)
 {
   for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
   {
-    const u32 u = idx[i] + first[i] - 1; // index of this entry's distinct key
+    const u32 u = idx[i] + first[i] - 1;
     if (first[i])
-      fk[u] = ek[i];
-    const u32 tag = ev[i];
-    if (tag < M)
-      oldToNew[tag] = u;
-    else if (tag < M + C)
-      clusterNode[tag - M] = u;
+      s0[u] = ek[i];
+    s0Of[ev[i]] = u;
   }
 }
 
-// parent (nearest ancestor in the set) and link level of every node, nodes in depth-first order;
-// nodes per depth counted in depthCount
-__global__ void insert_parents_kernel(const u64* __restrict__ fk, u32 F, u32 D, u32* __restrict__ parent, u32* __restrict__ level, u32* __restrict__ depthCount)
+// the lowest common ancestor of each pair of depth-first neighbours that is missing from s0
+// (a neighbour that is an ancestor of the next one gives nothing new)
+__global__ void insert_lca_kernel(const u64* __restrict__ s0, u32 U, u32 D, u64* __restrict__ cand, u32* __restrict__ flag)
 {
-  for (u32 u = blockIdx.x * blockDim.x + threadIdx.x; u < F; u += gridDim.x * blockDim.x)
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < U; i += gridDim.x * blockDim.x)
   {
-    u64 key = ins_key_of_dfs(fk[u], D);
-    u32 p = 0xffffffffu, lv = 0;
-    while (key > 1)
+    u32 f = 0;
+    if (i > 0)
     {
-      key >>= 3;
-      const u64 c = ins_dfs_key(key, D);
-      const u32 j = ins_lower_bound(fk, 0, u, c);
-      if (j < u && fk[j] == c)
+      const u64 a = ins_key_of_dfs(s0[i - 1], D);
+      const u64 l = ins_node_lca(a, ins_key_of_dfs(s0[i], D));
+      if (l != a)
       {
-        if (p == 0xffffffffu)
-          p = j;
-        ++lv;
+        const u64 c = ins_dfs_key(l, D);
+        const u32 j = ins_lower_bound(s0, 0, i - 1, c); // an ancestor of s0[i - 1] precedes it
+        if (s0[j] != c)
+        {
+          cand[i] = c;
+          f = 1;
+        }
       }
     }
-    parent[u] = p;
-    level[u] = lv;
-    atomicAdd(&depthCount[u32(fk[u] & 31u)], 1u);
+    flag[i] = f;
+  }
+}
+__global__ void insert_compact_u64_kernel(const u64* __restrict__ v, const u32* __restrict__ flag, const u32* __restrict__ idx, u32 m, u64* __restrict__ out)
+{
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    if (flag[i])
+      out[idx[i]] = v[i];
+}
+
+// The node set fk = s0 and the new branch nodes nw (sorted, distinct, none in s0), merged: every key
+// goes to its index plus the count of the other list's keys below it.
+__global__ void insert_place_s0_kernel(const u64* __restrict__ s0, u32 U, const u64* __restrict__ nw, u32 L, u64* __restrict__ fk, u32* __restrict__ map)
+{
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < U; i += gridDim.x * blockDim.x)
+  {
+    const u32 k = i + ins_lower_bound(nw, 0, L, s0[i]);
+    fk[k] = s0[i];
+    map[i] = k;
+  }
+}
+__global__ void insert_place_new_kernel(const u64* __restrict__ s0, u32 U, const u64* __restrict__ nw, u32 L, u64* __restrict__ fk)
+{
+  for (u32 q = blockIdx.x * blockDim.x + threadIdx.x; q < L; q += gridDim.x * blockDim.x)
+    fk[q + ins_lower_bound(s0, 0, U, nw[q])] = nw[q];
+}
+// the node index of every old node and every cluster
+__global__ void insert_node_index_kernel(const u32* __restrict__ s0Of, const u32* __restrict__ map, u32 M, u32 C, u32* __restrict__ oldToNew,
+                                         u32* __restrict__ clusterNode)
+{
+  for (u32 t = blockIdx.x * blockDim.x + threadIdx.x; t < M + C; t += gridDim.x * blockDim.x)
+  {
+    const u32 v = map[s0Of[t]];
+    if (t < M)
+      oldToNew[t] = v;
+    else
+      clusterNode[t - M] = v;
   }
 }
 
-__global__ void insert_bfs_keys_kernel(const u32* __restrict__ level, u32 F, u64* __restrict__ bk, u32* __restrict__ bv)
+// Parent of every node, nodes in depth-first order (fk sorted, closed under lowest common
+// ancestors): the parent of node u > 0 is the lowest common ancestor of nodes u - 1 and u. (Any
+// ancestor w of u in the set precedes u, and every node between w and u in depth-first order lies
+// in w's subtree; so u - 1 is w or below it, and no set node lies between that ancestor and u.)
+// slot: u's child slot in its parent; occupied: the parent's slots as a bit mask; depthCount: nodes
+// per depth.
+__global__ void insert_parents_kernel(const u64* __restrict__ fk, u32 F, u32 D, u32* __restrict__ parent, unsigned char* __restrict__ slot,
+                                      u32* __restrict__ occupied, u32* __restrict__ depthCount, u32* __restrict__ err)
 {
+  __shared__ u32 sDepth[32]; // nodes per depth of this block, added to depthCount once per block
+  if (threadIdx.x < 32)
+    sDepth[threadIdx.x] = 0;
+  __syncthreads();
   for (u32 u = blockIdx.x * blockDim.x + threadIdx.x; u < F; u += gridDim.x * blockDim.x)
   {
-    bk[u] = (u64(level[u]) << 32) | u;
-    bv[u] = u;
+    atomicAdd(&sDepth[u32(fk[u] & 31u)], 1u);
+    if (u == 0)
+    {
+      parent[0] = 0xffffffffu;
+      slot[0] = 0;
+      continue;
+    }
+    const u64 key = ins_key_of_dfs(fk[u], D);
+    const u64 pk = ins_node_lca(ins_key_of_dfs(fk[u - 1], D), key);
+    const u64 pc = ins_dfs_key(pk, D);
+    const u32 p = ins_lower_bound(fk, 0, u, pc);
+    // a parent missing from the set would be a broken closure: reported, never followed
+    if (p >= u || fk[p] != pc || pk == key)
+    {
+      atomicOr(err, kErrCapacity);
+      parent[u] = 0xffffffffu;
+      slot[u] = 0;
+      continue;
+    }
+    const u32 s = u32((key >> (3 * (ins_key_depth(key) - ins_key_depth(pk) - 1))) & 7u); // si_morton.h:651-658
+    parent[u] = p;
+    slot[u] = (unsigned char)s;
+    atomicOr(&occupied[p], 1u << s);
   }
+  __syncthreads();
+  if (threadIdx.x < 32 && sDepth[threadIdx.x])
+    atomicAdd(&depthCount[threadIdx.x], sDepth[threadIdx.x]);
 }
 
-__global__ void insert_bfs_index_kernel(const u32* __restrict__ bfsToDfs, u32 F, u32* __restrict__ dfsToBfs)
-{
-  for (u32 b = blockIdx.x * blockDim.x + threadIdx.x; b < F; b += gridDim.x * blockDim.x)
-    dfsToBfs[bfsToDfs[b]] = b;
-}
-__global__ void insert_links_kernel(const u32* __restrict__ dfsToBfs, u32 F, const u32* __restrict__ parent, u32* __restrict__ firstChild,
-                                    u32* __restrict__ childCount)
+// Link level (ancestors in the set) of every node by pointer jumping: after round r, lvl[u] counts
+// u's ancestors up to (not including) anc[u], its 2^r-th ancestor or the root. Reads one buffer
+// pair and writes the other.
+__global__ void insert_level_init_kernel(const u32* __restrict__ parent, u32 F, u32* __restrict__ lvl, u32* __restrict__ anc)
 {
   for (u32 u = blockIdx.x * blockDim.x + threadIdx.x; u < F; u += gridDim.x * blockDim.x)
   {
     const u32 p = parent[u];
-    if (p == 0xffffffffu)
-      continue;
-    const u32 pb = dfsToBfs[p];
-    atomicMin(&firstChild[pb], dfsToBfs[u]);
-    atomicAdd(&childCount[pb], 1u);
+    const bool top = u == 0 || p >= F; // the root (or a node whose parent went missing, reported)
+    lvl[u] = top ? 0u : 1u;
+    anc[u] = top ? 0u : p;
+  }
+}
+__global__ void insert_level_jump_kernel(const u32* __restrict__ lvl, const u32* __restrict__ anc, u32 F, u32* __restrict__ lvlOut, u32* __restrict__ ancOut)
+{
+  for (u32 u = blockIdx.x * blockDim.x + threadIdx.x; u < F; u += gridDim.x * blockDim.x)
+  {
+    const u32 a = anc[u];
+    lvlOut[u] = lvl[u] + lvl[a];
+    ancOut[u] = anc[a];
+  }
+}
+__global__ void iota_u32_kernel(u32* __restrict__ a, u32 n)
+{
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    a[i] = i;
+}
+
+// breadth-first position of every node from the stable order by (level, depth-first index), and each
+// node's first child: its child of the lowest occupied slot
+__global__ void insert_positions_kernel(const u32* __restrict__ bfsToDfs, u32 F, u32* __restrict__ pos)
+{
+  for (u32 b = blockIdx.x * blockDim.x + threadIdx.x; b < F; b += gridDim.x * blockDim.x)
+    pos[bfsToDfs[b]] = b;
+}
+__global__ void insert_first_child_kernel(const u32* __restrict__ parent, const unsigned char* __restrict__ slot, const u32* __restrict__ occupied,
+                                          const u32* __restrict__ pos, u32 F, u32* __restrict__ firstChild)
+{
+  for (u32 u = 1 + blockIdx.x * blockDim.x + threadIdx.x; u < F; u += gridDim.x * blockDim.x)
+  {
+    const u32 p = parent[u];
+    if (p < F && (occupied[p] & ((1u << slot[u]) - 1u)) == 0)
+      firstChild[p] = pos[u];
   }
 }
 
-// owner (depth-first node index) of every entity position: old entities by their old node's own
-// range, new ones by their cluster
-__global__ void insert_old_owner_kernel(const uint4* __restrict__ link, u32 M, const u32* __restrict__ oldToNew, u32* __restrict__ owner)
+// owner (depth-first node index) of every old entity position, from the old nodes' own ranges; in
+// the old order, which is the depth-first order of the old nodes and so non-decreasing
+__global__ void insert_old_owner_kernel(const uint4* __restrict__ link, u32 M, u32 n, const u32* __restrict__ oldToNew, u32* __restrict__ owner)
 {
   for (u32 j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x)
   {
     const uint4 L = link[j];
-    for (u32 p = L.y; p < L.z; ++p)
+    for (u32 p = L.y; p < min(L.z, n); ++p)
       owner[p] = oldToNew[j];
   }
 }
-// every entity position starts without a node (owner F sorts after every node) and as itself
-__global__ void insert_owner_init_kernel(u64 nt, u32 F, u32* __restrict__ owner, u32* __restrict__ src)
+__global__ void insert_fill_kernel(u32* __restrict__ a, u64 n, u32 v)
 {
-  for (u64 p = blockIdx.x * u64(blockDim.x) + threadIdx.x; p < nt; p += u64(gridDim.x) * blockDim.x)
-  {
-    owner[p] = F;
-    src[p] = u32(p);
-  }
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < n; i += u64(gridDim.x) * blockDim.x)
+    a[i] = v;
 }
-__global__ void insert_new_owner_kernel(const InsCluster* __restrict__ cl, u32 C, const u32* __restrict__ clusterNode, u32 n, u32* __restrict__ owner)
+// owner of every new entity (sorted position) and its position, for a stable sort by owner
+__global__ void insert_new_owner_kernel(const u32* __restrict__ clBegin, const u32* __restrict__ clEnd, u32 C, const u32* __restrict__ clusterNode,
+                                        u32* __restrict__ owner, u32* __restrict__ idx)
 {
   for (u32 c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x)
   {
-    const InsCluster k = cl[c];
-    for (u32 p = k.b; p < k.e; ++p)
-      owner[n + p] = clusterNode[c];
+    const u32 b = clBegin[c], e = clEnd[b];
+    for (u32 p = b; p < e; ++p)
+    {
+      owner[p] = clusterNode[c];
+      idx[p] = p;
+    }
   }
 }
 
-template<typename T>
-__global__ void insert_entities_kernel(const u32* __restrict__ src, u64 nTotal, u32 n, const u32* __restrict__ oldIds, const T* __restrict__ oldGeom,
-                                       const u32* __restrict__ newIdx, const T* __restrict__ newPts, u32* __restrict__ ids, T* __restrict__ geom)
+// start[v] = the first position in owner[0, m) (sorted, below F) whose owner is at least v, for v in
+// [0, F]: the change of owner at position k covers the owners it passes
+__global__ void insert_starts_kernel(const u32* __restrict__ owner, u64 m, u32 F, u32* __restrict__ start)
 {
-  for (u64 k = blockIdx.x * u64(blockDim.x) + threadIdx.x; k < nTotal; k += u64(gridDim.x) * blockDim.x)
+  for (u64 k = blockIdx.x * u64(blockDim.x) + threadIdx.x; k <= m; k += u64(gridDim.x) * blockDim.x)
   {
-    const u32 s = src[k];
-    const T* g;
-    if (s < n)
-    {
-      ids[k] = oldIds[s];
-      g = oldGeom + u64(s) * 3;
-    }
-    else
-    {
-      const u32 j = newIdx[s - n];
-      ids[k] = n + j;
-      g = newPts + u64(j) * 3;
-    }
+    const u32 lo = k == 0 ? 0u : min(owner[k - 1], F) + 1u; // owners up to owner[k - 1] start earlier
+    const u32 hi = k == m ? F : min(owner[k], F);           // owners up to owner[k] start here at the latest
+    for (u32 v = lo; v <= hi; ++v)
+      start[v] = u32(k);
+  }
+}
+
+// Entities in their new order (by node, old before new within a node): old entity i goes to
+// i + (new entities of earlier nodes), new entity j (sorted by node) to j + (old entities of its
+// node and earlier ones).
+template<typename T>
+__global__ void insert_old_entities_kernel(const u32* __restrict__ oldOwner, u32 n, const u32* __restrict__ startNew, const u32* __restrict__ oldIds,
+                                           const T* __restrict__ oldGeom, u32* __restrict__ ids, T* __restrict__ geom)
+{
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  {
+    const u64 k = u64(i) + startNew[oldOwner[i]];
+    ids[k] = oldIds[i];
 #pragma unroll
     for (int c = 0; c < 3; ++c)
-      geom[k * 3 + c] = g[c];
+      geom[k * 3 + c] = oldGeom[u64(i) * 3 + c];
+  }
+}
+template<typename T>
+__global__ void insert_new_entities_kernel(const u32* __restrict__ newOwner, const u32* __restrict__ newPos, u32 n2, const u32* __restrict__ startOld,
+                                           const u32* __restrict__ newIdx, const T* __restrict__ newPts, u32 n, u32* __restrict__ ids, T* __restrict__ geom)
+{
+  for (u32 j = blockIdx.x * blockDim.x + threadIdx.x; j < n2; j += gridDim.x * blockDim.x)
+  {
+    const u64 k = u64(j) + startOld[newOwner[j] + 1];
+    const u32 q = newIdx[newPos[j]]; // input index of the new point at sorted position newPos[j]
+    ids[k] = n + q;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      geom[k * 3 + c] = newPts[u64(q) * 3 + c];
   }
 }
 
+// node records at their positions: links, keys, MinPoint geometry (the root keeps its box)
 template<typename T>
-__global__ void insert_nodes_kernel(const u32* __restrict__ bfsToDfs, u32 F, const u64* __restrict__ fk, u32 D, const u32* __restrict__ owner, u32 nTotal,
-                                    const u32* __restrict__ firstChild, const u32* __restrict__ childCount, const T* __restrict__ oldRootBox,
-                                    const T* __restrict__ minTab, const Space<T>* __restrict__ spg, uint4* __restrict__ link, u64* __restrict__ nodeKey,
-                                    T* __restrict__ nodeBox, unsigned char* __restrict__ nodeDepth)
+__global__ void insert_nodes_kernel(const u32* __restrict__ pos, u32 F, const u64* __restrict__ fk, u32 D, const u32* __restrict__ startOld,
+                                    const u32* __restrict__ startNew, const u32* __restrict__ firstChild, const u32* __restrict__ occupied,
+                                    const T* __restrict__ oldRootBox, const T* __restrict__ minTab, const Space<T>* __restrict__ spg,
+                                    uint4* __restrict__ link, u64* __restrict__ nodeKey, T* __restrict__ nodeBox, unsigned char* __restrict__ nodeDepth)
 {
-  for (u32 b = blockIdx.x * blockDim.x + threadIdx.x; b < F; b += gridDim.x * blockDim.x)
+  for (u32 u = blockIdx.x * blockDim.x + threadIdx.x; u < F; u += gridDim.x * blockDim.x)
   {
-    const u32 u = bfsToDfs[b];
+    const u32 b = pos[u];
     const u64 key = ins_key_of_dfs(fk[u], D);
     const u32 d = ins_key_depth(key);
-    const u32 ownBegin = ins_lower_bound32(owner, 0, nTotal, u);
-    const u32 ownEnd = ins_lower_bound32(owner, ownBegin, nTotal, u + 1);
     // the subtree: the depth-first keys from this node's up to the next cell of its depth
     const u64 loc = key ^ (u64(1) << (3 * d));
     const u64 endKey = ((loc + 1) << (3 * (D - d))) << 5;
     const u32 j = ins_lower_bound(fk, u + 1, F, endKey);
-    const u32 subtreeEnd = j < F ? ins_lower_bound32(owner, ownEnd, nTotal, j) : nTotal;
-    const u32 cc = childCount[b];
-    link[b] = make_uint4((cc ? firstChild[b] : 0u) | (cc << kChildShift), ownBegin, ownEnd, subtreeEnd);
+    const u32 cc = __popc(occupied[u]);
+    link[b] = make_uint4((cc ? firstChild[u] : 0u) | (cc << kChildShift), startOld[u] + startNew[u], startOld[u + 1] + startNew[u + 1],
+                         startOld[j] + startNew[j]);
     nodeKey[b] = key;
     nodeDepth[b] = (unsigned char)d;
     if (b == 0)
@@ -2702,6 +2854,23 @@ static int insert_impl(TreeState& t, const T* pts, u64 n2, cudaStream_t st)
       return cuda_status(ce, what);
     return OTG_OK;
   };
+  // counts read back by the host: [0] clusters, [1] distinct keys, [2] new branch nodes, [3] spare
+  u32* hostCounts = nullptr;
+  TmpBuf counts;
+  if ((e = counts.ensure(sizeof(u32) * 4, st)))
+    return cuda_status(e, "allocating insert counts");
+  u32* dCounts = counts.as<u32>();
+  u32 hc[4] = { 0, 0, 0, 0 };
+  (void)hostCounts;
+  auto read_count = [&](int i, const char* what) -> int {
+    cudaError_t ce = cudaMemcpyAsync(&hc[i], dCounts + i, sizeof(u32), cudaMemcpyDeviceToHost, st);
+    if (!ce)
+      ce = cudaStreamSynchronize(st);
+    return ce ? cuda_status(ce, what) : OTG_OK;
+  };
+  Profiler& prof = profiler();
+  prof.reset();
+  prof.mark("keys", st);
   cudaMemsetAsync(err, 0, sizeof(u32), st);
 
   // 1. keys of the new points, sorted (stable: equal locations keep their input order)
@@ -2720,42 +2889,47 @@ static int insert_impl(TreeState& t, const T* pts, u64 n2, cudaStream_t st)
   if (int rc = sort_pairs_u64(nk.as<u64>(), nv.as<u32>(), n2, 3 * D + 1, st, err))
     return rc;
 
-  // 2. clustering rounds
-  TmpBuf itemsA, itemsB, clusters, counters;
-  if ((e = itemsA.ensure(sizeof(InsItem) * n2, st)) || (e = itemsB.ensure(sizeof(InsItem) * n2, st)) ||
-      (e = clusters.ensure(sizeof(InsCluster) * n2, st)) || (e = counters.ensure(sizeof(u32) * 2, st)))
+  // 2. clustering rounds over item slots: at most ceil(3D / 9) splits, then the emitting round
+  prof.mark("cluster", st);
+  TmpBuf itemsA, itemsB, clEnd, clKey, clIdx, splits, nSplits;
+  const u32 splitCap = u32(n2 / 257 + 1); // items split in one round hold more than 256 points each
+  if ((e = itemsA.ensure(sizeof(InsItem) * n2, st)) || (e = itemsB.ensure(sizeof(InsItem) * n2, st)) || (e = clEnd.ensure(sizeof(u32) * n2, st)) ||
+      (e = clKey.ensure(sizeof(u64) * n2, st)) || (e = clIdx.ensure(sizeof(u32) * n2, st)) || (e = splits.ensure(sizeof(InsItem) * splitCap, st)) ||
+      (e = nSplits.ensure(sizeof(u32), st)))
     return cuda_status(e, "allocating insert work");
-  const InsItem root{ 0, u32(n2), 3 * D, 0, 0 };
-  if ((e = cudaMemcpyAsync(itemsA.p, &root, sizeof(root), cudaMemcpyHostToDevice, st)))
-    return cuda_status(e, "starting insert work");
-  u32* dCount = counters.as<u32>(); // [0] items of the next round, [1] clusters
-  cudaMemsetAsync(dCount, 0, sizeof(u32) * 2, st);
-  u32 nIn = 1, hc[2] = { 0, 0 };
-  for (u32 round = 0; nIn; ++round)
+  cudaMemsetAsync(itemsA.p, 0, sizeof(InsItem) * n2, st);
+  cudaMemsetAsync(clEnd.p, 0, sizeof(u32) * n2, st);
+  insert_root_item_kernel<<<1, 32, 0, st>>>(itemsA.as<InsItem>(), u32(n2), D);
+  const u32 rounds = (3 * D + 8) / 9 + 1;
+  const int roundBlocks = grid_blocks((n2 + 31) / 32 * 32, 256);
+  for (u32 r = 0; r < rounds; ++r)
   {
-    if (round > 3 * D + 2) // every round takes at least 3 bits off the items' remaining bits
-    {
-      set_error("otg_tree_insert: clustering did not converge");
-      return OTG_ERR_CUDA;
-    }
-    cudaMemsetAsync(dCount, 0, sizeof(u32), st);
-    insert_round_kernel<u64><<<grid_blocks(u64(nIn) * 32, 256), 256, 0, st>>>(nk.as<u64>(), D, t.maxElem, itemsA.as<InsItem>(), nIn, itemsB.as<InsItem>(),
-                                                                             dCount, u32(n2), clusters.as<InsCluster>(), dCount + 1, u32(n2), err);
-    if ((e = cudaMemcpyAsync(hc, dCount, sizeof(hc), cudaMemcpyDeviceToHost, st)) || (e = cudaStreamSynchronize(st)))
-      return cuda_status(e, "clustering inserted points");
-    if (hc[0] > n2 || hc[1] > n2)
-    {
-      set_error("otg_tree_insert: clustering work exceeded its capacity");
-      return OTG_ERR_OUT_OF_MEMORY;
-    }
-    nIn = hc[0];
+    cudaMemsetAsync(itemsB.p, 0, sizeof(InsItem) * n2, st);
+    cudaMemsetAsync(nSplits.p, 0, sizeof(u32), st);
+    insert_round_kernel<<<roundBlocks, 256, 0, st>>>(nk.as<u64>(), u32(n2), D, t.maxElem, itemsA.as<InsItem>(), clEnd.as<u32>(), clKey.as<u64>(),
+                                                     splits.as<InsItem>(), nSplits.as<u32>(), splitCap, err);
+    insert_split_kernel<<<grid_blocks(u64(splitCap) << 9, 256), 256, 0, st>>>(nk.as<u64>(), D, splits.as<InsItem>(), nSplits.as<u32>(), splitCap,
+                                                                             itemsB.as<InsItem>());
     swap(itemsA, itemsB);
   }
-  const u32 C = hc[1];
   itemsA.release();
   itemsB.release();
+  splits.release();
+  // cluster c: the c-th occupied slot (a scan of the slot flags)
+  if (int rc = [&] {
+        TmpBuf flag;
+        if (cudaError_t fe = flag.ensure(sizeof(u32) * n2, st))
+          return cuda_status(fe, "allocating cluster flags");
+        insert_cluster_flags_kernel<<<blocks_for(n2), 256, 0, st>>>(clEnd.as<u32>(), u32(n2), flag.as<u32>());
+        return exclusive_scan_u32(flag.as<u32>(), u32(n2), clIdx.as<u32>(), dCounts + 0, st);
+      }())
+    return rc;
+  if (int rc = read_count(0, "clustering inserted points"))
+    return rc;
+  const u32 C = hc[0];
 
-  // 3. node set: old nodes, cluster nodes and the lowest common ancestors of adjacent keys
+  // 3. node set: old nodes, cluster nodes and the lowest common ancestors of depth-first neighbours
+  prof.mark("node set", st);
   const u64 m = u64(M) + C;
   if (2 * m + 1 >= (u64(1) << kChildShift))
   {
@@ -2763,72 +2937,137 @@ static int insert_impl(TreeState& t, const T* pts, u64 n2, cudaStream_t st)
     return OTG_ERR_NOT_SUPPORTED;
   }
   const u32 keyBits = 3 * D + 5;
-  TmpBuf ek, ev, first, idx, blockSums, total;
-  const u32 m2 = u32(2 * m);
-  const u32 nScanBlocks = (m2 + kScanBlock - 1) / kScanBlock;
-  if ((e = ek.ensure(sizeof(u64) * m2, st)) || (e = ev.ensure(sizeof(u32) * m2, st)) || (e = first.ensure(sizeof(u32) * m2, st)) ||
-      (e = idx.ensure(sizeof(u32) * m2, st)) || (e = blockSums.ensure(sizeof(u32) * nScanBlocks, st)) || (e = total.ensure(sizeof(u32), st)))
+  TmpBuf ek, ev, first, idx, s0, s0Of, clBegin;
+  if ((e = ek.ensure(sizeof(u64) * m, st)) || (e = ev.ensure(sizeof(u32) * m, st)) || (e = first.ensure(sizeof(u32) * m, st)) ||
+      (e = idx.ensure(sizeof(u32) * m, st)) || (e = s0.ensure(sizeof(u64) * m, st)) || (e = s0Of.ensure(sizeof(u32) * m, st)) ||
+      (e = clBegin.ensure(sizeof(u32) * std::max<u32>(C, 1), st)))
     return cuda_status(e, "allocating insert node merge");
-  insert_entries_kernel<<<blocks_for(m), 256, 0, st>>>(t.nodeKey.as<u64>(), M, clusters.as<InsCluster>(), C, D, ek.as<u64>(), ev.as<u32>());
+  insert_entries_kernel<<<blocks_for(M + n2), 256, 0, st>>>(t.nodeKey.as<u64>(), M, clEnd.as<u32>(), clKey.as<u64>(), clIdx.as<u32>(), u32(n2), D,
+                                                            ek.as<u64>(), ev.as<u32>(), clBegin.as<u32>());
+  clKey.release();
+  clIdx.release();
   if (int rc = sort_pairs_u64(ek.as<u64>(), ev.as<u32>(), m, keyBits, st, err))
     return rc;
-  insert_lca_kernel<<<blocks_for(m), 256, 0, st>>>(ek.as<u64>(), ev.as<u32>(), u32(m), D);
-  if (int rc = sort_pairs_u64(ek.as<u64>(), ev.as<u32>(), m2, keyBits, st, err))
+  insert_first_kernel<<<blocks_for(m), 256, 0, st>>>(ek.as<u64>(), u32(m), first.as<u32>());
+  if (int rc = exclusive_scan_u32(first.as<u32>(), u32(m), idx.as<u32>(), dCounts + 1, st))
     return rc;
-  insert_first_kernel<<<blocks_for(m2), 256, 0, st>>>(ek.as<u64>(), m2, first.as<u32>());
-  scan_block_sums_kernel<<<nScanBlocks, kScanBlock, 0, st>>>(first.as<u32>(), m2, blockSums.as<u32>());
-  scan_sums_kernel<<<1, kScanBlock, 0, st>>>(blockSums.as<u32>(), nScanBlocks, total.as<u32>());
-  scan_add_kernel<<<nScanBlocks, kScanBlock, 0, st>>>(first.as<u32>(), m2, blockSums.as<u32>(), idx.as<u32>());
-  u32 F = 0;
-  if ((e = cudaMemcpyAsync(&F, total.p, sizeof(u32), cudaMemcpyDeviceToHost, st)) || (e = cudaStreamSynchronize(st)))
-    return cuda_status(e, "merging insert nodes");
-  TmpBuf fk, oldToNew, clusterNode;
-  if ((e = fk.ensure(sizeof(u64) * F, st)) || (e = oldToNew.ensure(sizeof(u32) * M, st)) || (e = clusterNode.ensure(sizeof(u32) * std::max<u32>(C, 1), st)))
+  insert_unique_kernel<<<blocks_for(m), 256, 0, st>>>(ek.as<u64>(), ev.as<u32>(), first.as<u32>(), idx.as<u32>(), u32(m), s0.as<u64>(), s0Of.as<u32>());
+  if (int rc = read_count(1, "merging insert nodes"))
+    return rc;
+  const u32 Un = hc[1];
+  // branch nodes missing from the set: found per neighbour pair, compacted, sorted, made distinct
+  TmpBuf cand, candIdx, nw, nwVals;
+  if ((e = cand.ensure(sizeof(u64) * Un, st)) || (e = candIdx.ensure(sizeof(u32) * Un, st)))
+    return cuda_status(e, "allocating insert branch nodes");
+  insert_lca_kernel<<<blocks_for(Un), 256, 0, st>>>(s0.as<u64>(), Un, D, cand.as<u64>(), first.as<u32>());
+  if (int rc = exclusive_scan_u32(first.as<u32>(), Un, candIdx.as<u32>(), dCounts + 2, st))
+    return rc;
+  if (int rc = read_count(2, "finding insert branch nodes"))
+    return rc;
+  const u32 L0 = hc[2];
+  u32 L = 0;
+  if (L0)
+  {
+    if ((e = nw.ensure(sizeof(u64) * L0, st)) || (e = nwVals.ensure(sizeof(u32) * L0, st)))
+      return cuda_status(e, "allocating insert branch nodes");
+    insert_compact_u64_kernel<<<blocks_for(Un), 256, 0, st>>>(cand.as<u64>(), first.as<u32>(), candIdx.as<u32>(), Un, nw.as<u64>());
+    iota_u32_kernel<<<blocks_for(L0), 256, 0, st>>>(nwVals.as<u32>(), L0);
+    if (int rc = sort_pairs_u64(nw.as<u64>(), nwVals.as<u32>(), L0, keyBits, st, err))
+      return rc;
+    // one node may be the branch of several neighbour pairs: keep each once
+    insert_first_kernel<<<blocks_for(L0), 256, 0, st>>>(nw.as<u64>(), L0, first.as<u32>());
+    if (int rc = exclusive_scan_u32(first.as<u32>(), L0, candIdx.as<u32>(), dCounts + 3, st))
+      return rc;
+    insert_compact_u64_kernel<<<blocks_for(L0), 256, 0, st>>>(nw.as<u64>(), first.as<u32>(), candIdx.as<u32>(), L0, cand.as<u64>());
+    if (int rc = read_count(3, "finding insert branch nodes"))
+      return rc;
+    L = hc[3];
+  }
+  const u32 F = Un + L;
+  TmpBuf fk, map, oldToNew, clusterNode;
+  if ((e = fk.ensure(sizeof(u64) * F, st)) || (e = map.ensure(sizeof(u32) * Un, st)) || (e = oldToNew.ensure(sizeof(u32) * M, st)) ||
+      (e = clusterNode.ensure(sizeof(u32) * std::max<u32>(C, 1), st)))
     return cuda_status(e, "allocating insert nodes");
-  insert_compact_kernel<<<blocks_for(m2), 256, 0, st>>>(ek.as<u64>(), ev.as<u32>(), first.as<u32>(), idx.as<u32>(), m2, M, C, fk.as<u64>(),
-                                                        oldToNew.as<u32>(), clusterNode.as<u32>());
+  insert_place_s0_kernel<<<blocks_for(Un), 256, 0, st>>>(s0.as<u64>(), Un, cand.as<u64>(), L, fk.as<u64>(), map.as<u32>());
+  if (L)
+    insert_place_new_kernel<<<blocks_for(L), 256, 0, st>>>(s0.as<u64>(), Un, cand.as<u64>(), L, fk.as<u64>());
+  insert_node_index_kernel<<<blocks_for(m), 256, 0, st>>>(s0Of.as<u32>(), map.as<u32>(), M, C, oldToNew.as<u32>(), clusterNode.as<u32>());
   ek.release();
   ev.release();
-  first.release();
   idx.release();
+  s0.release();
+  s0Of.release();
+  cand.release();
+  candIdx.release();
+  nw.release();
+  nwVals.release();
+  map.release();
 
-  // 4. parents, link levels, breadth-first order
-  TmpBuf parent, level, depthCount, bk, bv, dfsToBfs, firstChild, childCount;
-  if ((e = parent.ensure(sizeof(u32) * F, st)) || (e = level.ensure(sizeof(u32) * F, st)) || (e = depthCount.ensure(sizeof(u32) * 64, st)) ||
-      (e = bk.ensure(sizeof(u64) * F, st)) || (e = bv.ensure(sizeof(u32) * F, st)) || (e = dfsToBfs.ensure(sizeof(u32) * F, st)) ||
-      (e = firstChild.ensure(sizeof(u32) * F, st)) || (e = childCount.ensure(sizeof(u32) * F, st)))
+  // 4. parents, child slots, link levels and breadth-first positions
+  prof.mark("links", st);
+  TmpBuf parent, slot, occupied, depthCount, lvlA, lvlB, ancA, ancB, order, pos, firstChild;
+  if ((e = parent.ensure(sizeof(u32) * F, st)) || (e = slot.ensure(F, st)) || (e = occupied.ensure(sizeof(u32) * F, st)) ||
+      (e = depthCount.ensure(sizeof(u32) * 64, st)) || (e = lvlA.ensure(sizeof(u32) * F, st)) || (e = lvlB.ensure(sizeof(u32) * F, st)) ||
+      (e = ancA.ensure(sizeof(u32) * F, st)) || (e = ancB.ensure(sizeof(u32) * F, st)) || (e = order.ensure(sizeof(u32) * F, st)) ||
+      (e = pos.ensure(sizeof(u32) * F, st)) || (e = firstChild.ensure(sizeof(u32) * F, st)))
     return cuda_status(e, "allocating insert links");
   cudaMemsetAsync(depthCount.p, 0, sizeof(u32) * 64, st);
-  insert_parents_kernel<<<blocks_for(F), 256, 0, st>>>(fk.as<u64>(), F, D, parent.as<u32>(), level.as<u32>(), depthCount.as<u32>());
-  insert_bfs_keys_kernel<<<blocks_for(F), 256, 0, st>>>(level.as<u32>(), F, bk.as<u64>(), bv.as<u32>());
-  if (int rc = sort_pairs_u64(bk.as<u64>(), bv.as<u32>(), F, 40, st, err))
+  cudaMemsetAsync(occupied.p, 0, sizeof(u32) * F, st);
+  insert_parents_kernel<<<blocks_for(F), 256, 0, st>>>(fk.as<u64>(), F, D, parent.as<u32>(), slot.as<unsigned char>(), occupied.as<u32>(),
+                                                       depthCount.as<u32>(), err);
+  insert_level_init_kernel<<<blocks_for(F), 256, 0, st>>>(parent.as<u32>(), F, lvlA.as<u32>(), ancA.as<u32>());
+  for (u32 r = 0; (1u << r) <= D; ++r) // link levels are at most D
+  {
+    insert_level_jump_kernel<<<blocks_for(F), 256, 0, st>>>(lvlA.as<u32>(), ancA.as<u32>(), F, lvlB.as<u32>(), ancB.as<u32>());
+    swap(lvlA, lvlB);
+    swap(ancA, ancB);
+  }
+  iota_u32_kernel<<<blocks_for(F), 256, 0, st>>>(order.as<u32>(), F);
+  if (int rc = sort_pairs_u32(lvlA.as<u32>(), order.as<u32>(), F, 5, st, err)) // stable: depth-first order within a level
     return rc;
-  const u32* bfsToDfs = bv.as<u32>();
-  insert_bfs_index_kernel<<<blocks_for(F), 256, 0, st>>>(bfsToDfs, F, dfsToBfs.as<u32>());
-  cudaMemsetAsync(firstChild.p, 0xff, sizeof(u32) * F, st);
-  cudaMemsetAsync(childCount.p, 0, sizeof(u32) * F, st);
-  insert_links_kernel<<<blocks_for(F), 256, 0, st>>>(dfsToBfs.as<u32>(), F, parent.as<u32>(), firstChild.as<u32>(), childCount.as<u32>());
+  insert_positions_kernel<<<blocks_for(F), 256, 0, st>>>(order.as<u32>(), F, pos.as<u32>());
+  insert_first_child_kernel<<<blocks_for(F), 256, 0, st>>>(parent.as<u32>(), slot.as<unsigned char>(), occupied.as<u32>(), pos.as<u32>(), F,
+                                                           firstChild.as<u32>());
+  parent.release();
+  slot.release();
+  lvlA.release();
+  lvlB.release();
+  ancA.release();
+  ancB.release();
+  order.release();
 
-  // 5. entities ordered by their node (depth-first), old ones first within a node
-  TmpBuf owner, src;
-  if ((e = owner.ensure(sizeof(u32) * nt, st)) || (e = src.ensure(sizeof(u32) * nt, st)))
+  // 5. entities ordered by their node (depth-first), old ones first within a node: the old entities
+  // are in that order already, the new ones are sorted by node; each goes to its index plus the
+  // count of the other group's entities before it
+  prof.mark("entity order", st);
+  TmpBuf oldOwner, newOwner, newPos, startOld, startNew;
+  if ((e = oldOwner.ensure(sizeof(u32) * n, st)) || (e = newOwner.ensure(sizeof(u32) * n2, st)) || (e = newPos.ensure(sizeof(u32) * n2, st)) ||
+      (e = startOld.ensure(sizeof(u32) * (u64(F) + 1), st)) || (e = startNew.ensure(sizeof(u32) * (u64(F) + 1), st)))
     return cuda_status(e, "allocating insert owners");
-  insert_owner_init_kernel<<<blocks_for(nt), 256, 0, st>>>(nt, F, owner.as<u32>(), src.as<u32>());
-  insert_old_owner_kernel<<<blocks_for(M), 256, 0, st>>>(t.nodeLink.as<uint4>(), M, oldToNew.as<u32>(), owner.as<u32>());
-  insert_new_owner_kernel<<<blocks_for(std::max<u32>(C, 1)), 256, 0, st>>>(clusters.as<InsCluster>(), C, clusterNode.as<u32>(), u32(n), owner.as<u32>());
-  if (int rc = sort_pairs_u32(owner.as<u32>(), src.as<u32>(), nt, bit_count(F), st, err)) // owners 0 .. F
+  insert_fill_kernel<<<blocks_for(n), 256, 0, st>>>(oldOwner.as<u32>(), n, 0u);
+  insert_old_owner_kernel<<<blocks_for(M), 256, 0, st>>>(t.nodeLink.as<uint4>(), M, u32(n), oldToNew.as<u32>(), oldOwner.as<u32>());
+  insert_new_owner_kernel<<<blocks_for(std::max<u32>(C, 1)), 256, 0, st>>>(clBegin.as<u32>(), clEnd.as<u32>(), C, clusterNode.as<u32>(),
+                                                                          newOwner.as<u32>(), newPos.as<u32>());
+  if (int rc = sort_pairs_u32(newOwner.as<u32>(), newPos.as<u32>(), n2, bit_count(F), st, err))
     return rc;
+  insert_starts_kernel<<<blocks_for(n + 1), 256, 0, st>>>(oldOwner.as<u32>(), n, F, startOld.as<u32>());
+  insert_starts_kernel<<<blocks_for(n2 + 1), 256, 0, st>>>(newOwner.as<u32>(), n2, F, startNew.as<u32>());
 
   // 6. the new tree
+  prof.mark("write", st);
   DevBuf ids, geom, link, key, box, depth;
-  if ((e = ids.ensure(sizeof(u32) * nt)) || (e = geom.ensure(sizeof(T) * 3 * nt)) || (e = link.ensure(sizeof(uint4) * F)) ||
-      (e = key.ensure(sizeof(u64) * F)) || (e = box.ensure(sizeof(T) * 6 * F)) || (e = depth.ensure(F)))
+  if ((e = ids.ensure_pooled(sizeof(u32) * nt, st)) || (e = geom.ensure_pooled(sizeof(T) * 3 * nt, st)) ||
+      (e = link.ensure_pooled(sizeof(uint4) * F, st)) || (e = key.ensure_pooled(sizeof(u64) * F, st)) ||
+      (e = box.ensure_pooled(sizeof(T) * 6 * F, st)) || (e = depth.ensure_pooled(F, st)))
     return cuda_status(e, "allocating the inserted tree");
-  insert_entities_kernel<T><<<blocks_for(nt), 256, 0, st>>>(src.as<u32>(), nt, u32(n), t.sortedIds.as<u32>(), t.sortedGeom.as<T>(), nv.as<u32>(), pts,
-                                                            ids.as<u32>(), geom.as<T>());
-  insert_nodes_kernel<T><<<blocks_for(F), 256, 0, st>>>(bfsToDfs, F, fk.as<u64>(), D, owner.as<u32>(), u32(nt), firstChild.as<u32>(),
-                                                        childCount.as<u32>(), t.nodeBox.as<T>(), t.minTab.as<T>(), t.space.as<Space<T>>(),
-                                                        link.as<uint4>(), key.as<u64>(), box.as<T>(), depth.as<unsigned char>());
+  insert_old_entities_kernel<T><<<blocks_for(n), 256, 0, st>>>(oldOwner.as<u32>(), u32(n), startNew.as<u32>(), t.sortedIds.as<u32>(), t.sortedGeom.as<T>(),
+                                                               ids.as<u32>(), geom.as<T>());
+  insert_new_entities_kernel<T><<<blocks_for(n2), 256, 0, st>>>(newOwner.as<u32>(), newPos.as<u32>(), u32(n2), startOld.as<u32>(), nv.as<u32>(), pts,
+                                                                u32(n), ids.as<u32>(), geom.as<T>());
+  insert_nodes_kernel<T><<<blocks_for(F), 256, 0, st>>>(pos.as<u32>(), F, fk.as<u64>(), D, startOld.as<u32>(), startNew.as<u32>(), firstChild.as<u32>(),
+                                                        occupied.as<u32>(), t.nodeBox.as<T>(), t.minTab.as<T>(), t.space.as<Space<T>>(), link.as<uint4>(),
+                                                        key.as<u64>(), box.as<T>(), depth.as<unsigned char>());
+  prof.mark("end", st);
   std::vector<u32> dc(64);
   if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(dc.data(), depthCount.p, sizeof(u32) * 64, cudaMemcpyDeviceToHost, st)))
     return cuda_status(e, "inserting points");
@@ -2841,8 +3080,8 @@ static int insert_impl(TreeState& t, const T* pts, u64 n2, cudaStream_t st)
   }
   if (hostErr & kErrCapacity)
   {
-    set_error("otg_tree_insert: clustering work exceeded its capacity");
-    return OTG_ERR_OUT_OF_MEMORY;
+    set_error("otg_tree_insert: a clustering list overflowed, or a node of the merged set lost its parent");
+    return OTG_ERR_CUDA;
   }
   std::swap(t.sortedIds, ids);
   std::swap(t.sortedGeom, geom);
@@ -2850,6 +3089,14 @@ static int insert_impl(TreeState& t, const T* pts, u64 n2, cudaStream_t st)
   std::swap(t.nodeKey, key);
   std::swap(t.nodeBox, box);
   std::swap(t.nodeDepth, depth);
+  // the replaced arrays: pooled ones freed in stream order, a Create's kept until the next Create
+  for (DevBuf* b : { &ids, &geom, &link, &key, &box, &depth })
+  {
+    if (b->pooled)
+      b->release_async(st);
+    else if (b->p)
+      t.retired.push_back(std::move(*b));
+  }
   t.n = nt;
   t.nodeCount = F;
   t.maxNodes = F;

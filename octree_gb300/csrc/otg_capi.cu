@@ -4,6 +4,7 @@
 // There is no CPU path: without a CUDA device every compute call returns OTG_ERR_NO_DEVICE.
 #include "otg_internal.h"
 
+#include <algorithm>
 #include <mutex>
 
 #include <cstring>
@@ -29,7 +30,11 @@ void keep_pool_memory(int device)
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess)
   {
-    unsigned long long threshold = 1ull << 30;
+    // freed blocks up to 8 GiB stay in the pool (a 16M-point tree's arrays after an Insert take
+    // about 1.1 GB), at most a sixteenth of the device's memory
+    size_t freeB = 0, totalB = 0;
+    cudaMemGetInfo(&freeB, &totalB);
+    unsigned long long threshold = std::min<unsigned long long>(8ull << 30, totalB / 16);
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
   }
   cudaGetLastError();
@@ -129,6 +134,7 @@ static void release_tree(TreeState& s)
                      &s.stOrder, &s.stChildBegin, &s.stSeg, &s.stDepth, &s.stGeom, &s.stCtl };
   for (DevBuf* b : bufs)
     b->release();
+  s.retired.clear();
 }
 
 // forest: the query addresses the trees of a forest (per-query trees) rather than a single tree

@@ -28,18 +28,26 @@
 namespace otg
 {
 
-// Owning device allocation (move-only; freed on destruction).
+void keep_pool_memory(int device);
+
+// Owning device allocation (move-only; freed on destruction). `ensure` allocates with cudaMalloc;
+// `ensure_pooled` allocates in stream order from the device's default memory pool (which keeps
+// freed blocks for reuse), for arrays that are replaced often, such as a tree's arrays after an
+// Insert: a pooled allocation or free costs microseconds where cudaMalloc / cudaFree of hundreds
+// of megabytes cost hundreds.
 struct DevBuf
 {
   void* p = nullptr;
   size_t bytes = 0;
+  bool pooled = false;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
-  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes)
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes), pooled(o.pooled)
   {
     o.p = nullptr;
     o.bytes = 0;
+    o.pooled = false;
   }
   DevBuf& operator=(DevBuf&& o) noexcept
   {
@@ -48,8 +56,10 @@ struct DevBuf
       release();
       p = o.p;
       bytes = o.bytes;
+      pooled = o.pooled;
       o.p = nullptr;
       o.bytes = 0;
+      o.pooled = false;
     }
     return *this;
   }
@@ -58,21 +68,62 @@ struct DevBuf
   {
     if (need <= bytes)
       return cudaSuccess;
-    if (p)
-      cudaFree(p);
-    p = nullptr;
-    bytes = 0;
+    release();
     cudaError_t e = cudaMalloc(&p, need ? need : 16);
     if (e == cudaSuccess)
       bytes = need ? need : 16;
+    else
+      p = nullptr;
     return e;
   }
+  cudaError_t ensure_pooled(size_t need, cudaStream_t st)
+  {
+    if (need <= bytes)
+      return cudaSuccess;
+    release_async(st);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    keep_pool_memory(dev);
+    cudaError_t e = cudaMallocAsync(&p, need ? need : 16, st);
+    if (e == cudaSuccess)
+    {
+      bytes = need ? need : 16;
+      pooled = true;
+    }
+    else
+      p = nullptr;
+    return e;
+  }
+  // freed after the work queued on st (a cudaMalloc allocation is freed at once)
+  void release_async(cudaStream_t st)
+  {
+    if (p)
+    {
+      if (pooled)
+        cudaFreeAsync(p, st);
+      else
+        cudaFree(p);
+    }
+    p = nullptr;
+    bytes = 0;
+    pooled = false;
+  }
+  // a pooled allocation is freed after all work on the device, as cudaFree does for the others
   void release()
   {
     if (p)
-      cudaFree(p);
+    {
+      if (pooled)
+      {
+        cudaDeviceSynchronize();
+        cudaFreeAsync(p, nullptr);
+      }
+      else
+        cudaFree(p);
+    }
     p = nullptr;
     bytes = 0;
+    pooled = false;
   }
   template<typename X>
   X* as() const
@@ -82,10 +133,9 @@ struct DevBuf
 };
 
 // Per-call device scratch of the query paths, stream ordered (cudaMallocAsync / cudaFreeAsync on the
-// call's stream, from the device's default memory pool, which keeps up to 1 GiB of freed blocks for
+// call's stream, from the device's default memory pool, which keeps up to 8 GiB of freed blocks for
 // reuse): a small batch of queries pays no cudaMalloc / cudaFree, and a block is reused only after the
 // work queued before its release on that stream.
-void keep_pool_memory(int device);
 struct TmpBuf
 {
   void* p = nullptr;
@@ -201,6 +251,9 @@ struct TreeState
   // a bulk Insert changed the tree: nodes may own entities beside their children and child links
   // may skip levels, which the static array layout cannot hold
   bool inserted = false;
+  // arrays an Insert replaced that were allocated with cudaMalloc: kept until the next Create or the
+  // tree's end, so that the Insert itself waits for no cudaFree
+  std::vector<DevBuf> retired;
 
   // cached after the build (host copies, filled by sync)
   u64 nodeCount = 0;

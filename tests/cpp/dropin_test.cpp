@@ -336,9 +336,11 @@ int main()
       std::vector<Point3D> base(pts.begin(), pts.begin() + 20000), add(pts.begin() + 20000, pts.begin() + 26000);
       for (std::size_t i = 0; i < add.size(); i += 2)
         add[i] = { 40.0 + 0.01 * N(rng), 60.0 + 0.01 * N(rng), 20.0 + 0.01 * N(rng) }; // a deep cluster
-      OctreePointM tm(base, 8, std::nullopt, 20);
-      OctreePoint ti(std::span<const Point3D>(base), 8, std::nullopt, 20);
-      void* oi = oro_create(0, 0, base.data(), base.size(), 8, nullptr, 20);
+      // a given space, so that every new point lies inside it
+      const BoundingBox3D space{ { 0.0, 0.0, 0.0 }, { 100.0, 100.0, 100.0 } };
+      OctreePointM tm(base, 8, space, 20);
+      OctreePoint ti(std::span<const Point3D>(base), 8, space, 20);
+      void* oi = oro_create(0, 0, base.data(), base.size(), 8, &space, 20);
       const bool ok = oro_insert(oi, add.data(), add.size()) && tm.Add(std::span<const Point3D>(add)) &&
                       ti.Insert(std::span<const Point3D>(add), std::span<const Point3D>(base));
       if (!ok || tm.GetEntityCount() != base.size() + add.size() || tm.GetNodeCount() != ti.GetNodeCount())
