@@ -1159,7 +1159,7 @@ def run_insert(reps=3, cpu=True):
     return out
 
 
-PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m", "build_4m_clustered", "forest_frustum_1024", "insert_16m_1m", "insert_4m_250k")
+PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m", "build_4m_clustered", "forest_frustum_1024", "insert_16m_1m", "insert_4m_250k", "range_1m_10k")
 
 
 def run_profile_case(name):
@@ -1207,6 +1207,16 @@ def run_profile_case(name):
             t.create(pts, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
         t.sync()
         print(json.dumps({"case": name, "nodes": int(t.node_count)}))
+    elif name == "range_1m_10k":
+        # C1 RangeSearch (Inside) through the batched kernel at its default shape (autotuning off)
+        pts, ranges, _ = c1_workload()
+        t = otg.Tree("points").create(torch.as_tensor(pts, device="cuda"), max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
+        t.sync()
+        otg.autotune_enable(False)
+        rd = torch.as_tensor(ranges, device="cuda")
+        for _ in range(2):
+            r = t.range_search(rd, otg.RANGE_INSIDE, raw=True)
+        print(json.dumps({"case": name, "ids": r.sizes()[1]}))
     elif name in ("insert_16m_1m", "insert_4m_250k"):
         # Insert of new shell points into a fresh shell tree, twice (the launch list covers both)
         n, m = (16_000_000, 1_000_000) if name == "insert_16m_1m" else (4_000_000, 250_000)

@@ -78,6 +78,91 @@ __device__ __forceinline__ void sink_put(WarpSink& s, Appender& out, u32 lane, b
 // query kinds
 constexpr int kRange = 0, kFrustum = 1, kRayAll = 2, kPlane = 3, kPlanePositive = 4, kQuery = 5, kPick = 6;
 
+// ---- FP32 pre-tests of RangeSearch on FP64 point trees
+// The FP64 tests (core/ot_query.h:476-583 with internal_geometry_module.h:190-252, :398-422):
+//   node pruned  : some d with  maxL <= RN(nmin - tol)  or  maxR <= P        (overlap_by_min_point)
+//   node inside  : every d with P <= nmin and maxR <= Q                      (range_contains_min_size)
+//   point inside : every d with P < x < Q (tol != 0), or rmin <= x <= rmax (tol == 0)
+// with P = RN(rmin - tol), Q = RN(rmax + tol), maxL = RN(rmin + RN(rmax - rmin)) per query and
+// maxR = RN(nmin + nsize) per node. The images bound the FP64 values: a node's image holds
+// lo = rd(nmin) and hi = ru(maxR), so nmin lies in [lo, succ(lo)) and maxR in (pred(hi), hi]; a
+// point's image holds x32 = RN32(x), so x lies in (pred(x32), succ(x32)). Because floats are
+// discrete, "succ(a) <= b" is "a < b" and "pred(a) >= b" is "a > b" for floats a, b, and each test
+// below is decided where these bounds settle it, with per-query thresholds rounded down (lo) and up
+// (hi) from the exact FP64 values:
+//   P < x  : true if x32 > P.hi, false if x32 < P.lo      x < Q  : true if x32 < Q.lo, false if x32 > Q.hi
+//   (the same for rmin <= x and x <= rmax with P = rmin, Q = rmax when tol == 0)
+//   maxR <= P : true if hi <= P.lo, false if hi > P.hi   maxR <= Q : true if hi <= Q.lo, false if hi > Q.hi
+//   P <= nmin : true if P.hi <= lo, false if lo < P.lo
+//   maxL <= RN(nmin - tol) : true if ru(W + g) <= lo, false if lo < rd(W - g), W = RN(maxL + tol),
+//     where the slack g = 2^-46 (M + tol) exceeds every FP64 rounding involved (M bounds the range's
+//     and the root box's coordinates, so also every node's). RN is monotone, so maxL + tol <= nmin
+//     gives maxL <= RN(nmin - tol); and nmin + g/2 < maxL + tol gives RN(nmin - tol) < maxL.
+// Undecided tests run in FP64, so every answer is the FP64 answer.
+struct RangeF32
+{
+  float w[3], s[3], plo[3], phi[3], qlo[3], qhi[3];
+};
+
+__device__ __forceinline__ void range_thresholds(const double* r, const double* rsize, const double* rootBox, double tol, RangeF32& f)
+{
+  double M = 0.0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    M = fmax(M, fmax(fabs(r[d]), fabs(r[3 + d])));
+    M = fmax(M, fmax(fabs(rootBox[d]), fabs(rootBox[d] + rootBox[3 + d])));
+  }
+  const double g = (M + fabs(tol)) * 0x1p-46;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    const double maxL = r[d] + rsize[d];
+    const double P = r[d] - tol, Q = r[3 + d] + tol;
+    const double W = maxL + tol;
+    f.w[d] = __double2float_ru(W + g);
+    f.s[d] = __double2float_rd(W - g);
+    f.plo[d] = __double2float_rd(P);
+    f.phi[d] = __double2float_ru(P);
+    f.qlo[d] = __double2float_rd(Q);
+    f.qhi[d] = __double2float_ru(Q);
+  }
+}
+
+// node: enter 0 (pruned) / 1 (entered) / 2 (undecided); inside 0 / 1 / 2 likewise
+__device__ __forceinline__ void range_node_f32(const float4* __restrict__ img, u32 node, const RangeF32& f, int& enter, int& inside)
+{
+  const float4 mn = img[2 * size_t(node)], mx = img[2 * size_t(node) + 1];
+  const float lo[3] = { mn.x, mn.y, mn.z }, hi[3] = { mx.x, mx.y, mx.z };
+  bool anyPrune = false, allKeep = true, allIn = true, anyOut = false;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    anyPrune |= (f.w[d] <= lo[d]) | (hi[d] <= f.plo[d]);
+    allKeep &= (lo[d] < f.s[d]) & (hi[d] > f.phi[d]);
+    allIn &= (f.phi[d] <= lo[d]) & (hi[d] <= f.qlo[d]);
+    anyOut |= (lo[d] < f.plo[d]) | (hi[d] > f.qhi[d]);
+  }
+  enter = anyPrune ? 0 : (allKeep ? 1 : 2);
+  inside = anyOut ? 0 : (allIn ? 1 : 2);
+}
+
+// point: 0 outside, 1 inside, 2 undecided (also for a point without a finite image)
+__device__ __forceinline__ int range_point_f32(const float4 p, const RangeF32& f)
+{
+  if (!(p.w < INFINITY))
+    return 2;
+  const float x[3] = { p.x, p.y, p.z };
+  bool allIn = true, anyOut = false;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    allIn &= (x[d] > f.phi[d]) & (x[d] < f.qlo[d]);
+    anyOut |= (x[d] < f.plo[d]) | (x[d] > f.qhi[d]);
+  }
+  return anyOut ? 0 : (allIn ? 1 : 2);
+}
+
 template<typename T, int KIND>
 struct BatchArgs
 {
@@ -101,6 +186,8 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
 {
   static_assert(KIND >= kRange && KIND <= kPick, "every query kind has its own setup, node test and entity test below");
   using G = GeoD<T>;
+  constexpr bool kRangeF32 = KIND == kRange && sizeof(T) == 8;
+  __shared__ RangeF32 rangeF[kRangeF32 ? WARPS : 1];
   __shared__ u32 stackMem[WARPS][kWideStack];
   __shared__ u64 itemMem[WARPS][kItemBuf];
   __shared__ double distMem[KIND == kRayAll ? WARPS : 1][KIND == kRayAll ? kItemBuf : 1];
@@ -205,6 +292,16 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
     }
     if (skip)
       continue;
+    // FP32 pre-tests (range on FP64 point trees): the query's thresholds, shared by the warp
+    bool useF32 = false;
+    if constexpr (kRangeF32)
+    {
+      useF32 = tv.nodeImg != nullptr && tv.pointImg != nullptr && !tv.isBox;
+      __syncwarp(); // the previous query's thresholds are read by every lane before they change
+      if (useF32 && lane == 0)
+        range_thresholds(r, rsize, tv.nodeBox + u64(root) * 6, double(a.tol), rangeF[w]);
+      __syncwarp();
+    }
     // ---- node test of one node (run by one lane per child)
     auto enters = [&](u32 node, bool& contained) -> bool {
       const T* nb = tv.nodeBox + u64(node) * 6;
@@ -212,6 +309,18 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
       if constexpr (KIND == kRange)
       {
         T nmin[3] = { nb[0], nb[1], nb[2] }, nsize[3] = { nb[3], nb[4], nb[5] };
+        if constexpr (kRangeF32)
+        {
+          if (useF32)
+          {
+            int en, in;
+            range_node_f32(tv.nodeImg, node, rangeF[w], en, in);
+            if (en == 0 || (en == 2 && !G::overlap_by_min_point(r, rsize, nmin, nsize, a.tol)))
+              return false;
+            contained = in == 2 ? G::range_contains_min_size(r, nmin, nsize, a.tol) : in == 1;
+            return true;
+          }
+        }
         if (!G::overlap_by_min_point(r, rsize, nmin, nsize, a.tol))
           return false;
         contained = G::range_contains_min_size(r, nmin, nsize, a.tol);
@@ -347,7 +456,13 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
             if constexpr (KIND == kRange)
             {
               if (!tv.isBox)
-                hit = G::box_contains_point(r, tv.geom + u64(e) * 3, a.tol);
+              {
+                int dec = 2;
+                if constexpr (kRangeF32)
+                  if (useF32)
+                    dec = range_point_f32(tv.pointImg[e], rangeF[w]);
+                hit = dec == 2 ? G::box_contains_point(r, tv.geom + u64(e) * 3, a.tol) : dec == 1;
+              }
               else
               {
                 T bx[6];

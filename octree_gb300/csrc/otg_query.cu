@@ -1287,6 +1287,14 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
   Collected c;
   auto tv = view<T>(t, qTree);
   T tl = tol_of<T>(tol);
+  if (sizeof(T) == 8 && t.kind == OTG_KIND_POINTS && algo != OTG_ALGO_PLAIN_FP64)
+  {
+    // the batched kernel decides most node and point tests on FP32 images, the rest in FP64
+    if (int rc = ensure_image32(const_cast<TreeState&>(t), st))
+      return rc;
+    tv.nodeImg = t.nodeBox32.as<float4>();
+    tv.pointImg = t.geom32.as<float4>();
+  }
   TmpBuf work;
   if (cudaError_t e = work.ensure(batch_work_bytes(nq), st))
     return cuda_status(e, "allocating the work counter");

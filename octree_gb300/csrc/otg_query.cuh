@@ -27,6 +27,10 @@ struct TreeView
   const u32* qTree;   // forest: tree (= root node) of each query; null for a single tree
   const u64* treeOff; // forest: first entity of each tree (ids are returned relative to it)
   const unsigned char* nodeDepth; // depth of each node below its tree's root
+  // FP32 images (point trees of FP64 entities, built on demand): outward-rounded node boxes (two
+  // float4 per node) and round-to-nearest entities; null where a kernel takes the FP64 tests only
+  const float4* nodeImg = nullptr;
+  const float4* pointImg = nullptr;
 };
 
 // root node and id base of query q (node t is the root of tree t in a forest)

@@ -566,3 +566,27 @@ def test_core_form_set_entities(kind, dtype, device_span):
         assert np.array_equal(t.collision_self(), o.collide_self())
     with pytest.raises(otg.OtgError):
         t.set_entities(ent[:-1])
+
+
+@pytest.mark.parametrize("tol", [0.0, -1.0, 1e-9, 0.5])
+def test_range_on_exact_boundaries(tol):
+    """Points on an integer lattice and one ulp either side of it, ranges whose faces lie on lattice
+    values or one ulp off them: the batched kernel's FP32 pre-tests must leave every such case to
+    the FP64 test and answer exactly as the reference."""
+    rng = np.random.default_rng(31)
+    lat = rng.integers(0, 64, (60_000, 3)).astype(np.float64)
+    wiggle = rng.integers(-1, 2, lat.shape)
+    pts = np.where(wiggle < 0, np.nextafter(lat, -np.inf), np.where(wiggle > 0, np.nextafter(lat, np.inf), lat))
+    pts = np.concatenate([pts, lat[:20_000] * 1e-3, lat[:20_000] + 1e6])  # small and large magnitudes
+    lo = rng.integers(0, 60, (3000, 3)).astype(np.float64)
+    hi = lo + rng.integers(0, 6, (3000, 3))
+    lo = np.where(rng.random(lo.shape) < 0.3, np.nextafter(lo, np.inf), lo)
+    hi = np.where(rng.random(hi.shape) < 0.3, np.nextafter(hi, -np.inf), hi)
+    ranges = np.concatenate([lo, hi], 1)
+    ranges = np.concatenate([ranges, ranges[:500] * 1e-3, ranges[:500] + 1e6])
+    t = _gpu_tree(pts, KIND_POINTS, 10, None, 8)
+    o = oracle().create(pts, KIND_POINTS, 10, None, 8)
+    for mode in (0, 1):
+        ref = o.range_search(ranges, mode, tol)
+        for algo in (otg.ALGO_DEFAULT, otg.ALGO_PLAIN_FP64):
+            assert_csr_equal(t.range_search(ranges, mode, tol=tol, algo=algo)[:2], ref, f"range mode {mode} tol {tol} algo {algo}")
