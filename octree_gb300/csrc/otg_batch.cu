@@ -129,6 +129,25 @@ __device__ __forceinline__ void range_thresholds(const double* r, const double* 
   }
 }
 
+// The FP64 tests of the undecided cases, out of line: inlined, the compiler may evaluate them for
+// every node and point beside the FP32 tests (predicated), which kept the FP64 pipe busy.
+struct RangeD // the query box and its size, passed by value (no address of the caller's arrays escapes)
+{
+  double r[6], rsize[3];
+};
+__device__ __noinline__ bool range_node_enters_fp64(const RangeD q, const double* nb, double tol)
+{
+  return GeoD<double>::overlap_by_min_point(q.r, q.rsize, nb, nb + 3, tol);
+}
+__device__ __noinline__ bool range_node_inside_fp64(const RangeD q, const double* nb, double tol)
+{
+  return GeoD<double>::range_contains_min_size(q.r, nb, nb + 3, tol);
+}
+__device__ __noinline__ bool range_point_inside_fp64(const RangeD q, const double* p, double tol)
+{
+  return GeoD<double>::box_contains_point(q.r, p, tol);
+}
+
 // node: enter 0 (pruned) / 1 (entered) / 2 (undecided); inside 0 / 1 / 2 likewise
 __device__ __forceinline__ void range_node_f32(const float4* __restrict__ img, u32 node, const RangeF32& f, int& enter, int& inside)
 {
@@ -315,9 +334,13 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
           {
             int en, in;
             range_node_f32(tv.nodeImg, node, rangeF[w], en, in);
-            if (en == 0 || (en == 2 && !G::overlap_by_min_point(r, rsize, nmin, nsize, a.tol)))
+            if (en == 0)
               return false;
-            contained = in == 2 ? G::range_contains_min_size(r, nmin, nsize, a.tol) : in == 1;
+            if (en == 2 && !range_node_enters_fp64(RangeD{ { r[0], r[1], r[2], r[3], r[4], r[5] }, { rsize[0], rsize[1], rsize[2] } }, nb, a.tol))
+              return false;
+            contained = in == 1;
+            if (in == 2)
+              contained = range_node_inside_fp64(RangeD{ { r[0], r[1], r[2], r[3], r[4], r[5] }, { rsize[0], rsize[1], rsize[2] } }, nb, a.tol);
             return true;
           }
         }
@@ -461,7 +484,15 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
                 if constexpr (kRangeF32)
                   if (useF32)
                     dec = range_point_f32(tv.pointImg[e], rangeF[w]);
-                hit = dec == 2 ? G::box_contains_point(r, tv.geom + u64(e) * 3, a.tol) : dec == 1;
+                hit = dec == 1;
+                if (dec == 2)
+                {
+                  if constexpr (kRangeF32)
+                    hit = range_point_inside_fp64(RangeD{ { r[0], r[1], r[2], r[3], r[4], r[5] }, { rsize[0], rsize[1], rsize[2] } }, tv.geom + u64(e) * 3,
+                                                  a.tol);
+                  else
+                    hit = G::box_contains_point(r, tv.geom + u64(e) * 3, a.tol);
+                }
               }
               else
               {

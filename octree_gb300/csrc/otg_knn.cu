@@ -504,6 +504,12 @@ __global__ void __launch_bounds__(WARPS * 32) knn_filtered_kernel(KnnArgs<T> a)
 // ---------------------------------------------------------------- query order, k statistics
 // Morton order of the query points in the tree's space (10 bits per dimension): neighbouring
 // queries then walk the same nodes, which keeps the traversal in L2.
+__global__ void iota_order_kernel(u32* __restrict__ order, u64 nq)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < nq; i += u64(gridDim.x) * blockDim.x)
+    order[i] = u32(i);
+}
+
 template<typename T>
 __global__ void query_key_kernel(const T* __restrict__ pts, u64 nq, const Space<T>* __restrict__ sp, u32* __restrict__ keys, u32* __restrict__ idx)
 {
@@ -783,14 +789,21 @@ static int knn_filtered_impl(TreeState& t, const T* pts, const u32* dk, u64 nq, 
   TmpBuf qkeys, order;
   if ((e = qkeys.ensure(sizeof(u32) * nq, st)) || (e = order.ensure(sizeof(u32) * nq, st)))
     return cuda_status(e, "allocating the query order");
-  query_key_kernel<T><<<blocks_for(nq), 256, 0, st>>>(pts, nq, t.space.as<Space<T>>(), qkeys.as<u32>(), order.as<u32>());
+  // below 64k queries the batch takes the queries in input order: four radix passes over a few
+  // tiles cost more than the locality gains, the tree's upper levels sitting in L2 anyway
+  const bool sortQueries = nq >= (u64(1) << 16);
+  if (sortQueries)
+    query_key_kernel<T><<<blocks_for(nq), 256, 0, st>>>(pts, nq, t.space.as<Space<T>>(), qkeys.as<u32>(), order.as<u32>());
+  else
+    iota_order_kernel<<<blocks_for(nq), 256, 0, st>>>(order.as<u32>(), nq);
   TmpBuf ctr, fb, start, cnt, oIds, oDist;
   if ((e = ctr.ensure(sizeof(KnnCounters), st)) || (e = fb.ensure(sizeof(u32) * nq, st)) || (e = start.ensure(sizeof(u64) * nq, st)) ||
       (e = cnt.ensure(sizeof(u32) * nq, st)))
     return cuda_status(e, "allocating kNN buffers");
   cudaMemsetAsync(ctr.p, 0, sizeof(KnnCounters), st);
-  if (int rc = sort_pairs_u32(qkeys.as<u32>(), order.as<u32>(), nq, 30, st, &ctr.as<KnnCounters>()->err))
-    return rc;
+  if (sortQueries)
+    if (int rc = sort_pairs_u32(qkeys.as<u32>(), order.as<u32>(), nq, 30, st, &ctr.as<KnnCounters>()->err))
+      return rc;
   qkeys.release();
   KnnArgs<T> a{};
   a.link = t.nodeLink.as<uint4>();

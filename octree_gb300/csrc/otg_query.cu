@@ -985,14 +985,26 @@ __global__ void __launch_bounds__(128) collide_filter_kernel(StructTree<T> A, St
 }
 
 // ---------------------------------------------------------------- result finishing
-__global__ void split_items_kernel(const u64* __restrict__ items, const u32* __restrict__ perm, u64 m, u32* __restrict__ qOut, u32* __restrict__ idOut)
+// items (query << idBits | id) into query and id arrays
+__global__ void split_items_kernel(const u64* __restrict__ items, const u32* __restrict__ perm, u64 m, u32* __restrict__ qOut, u32* __restrict__ idOut,
+                                   u32 idBits = 32)
 {
   for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
   {
     u64 it = items[perm ? perm[i] : i];
     if (qOut)
-      qOut[i] = u32(it >> 32);
-    idOut[i] = u32(it);
+      qOut[i] = u32(it >> idBits);
+    idOut[i] = u32(it & ((u64(1) << idBits) - 1));
+  }
+}
+// items (query << 32 | id) repacked as (query << idBits | id), so that their sort takes only the
+// bits that queries and ids use
+__global__ void pack_items_kernel(u64* __restrict__ items, u64 m, u32 idBits)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+  {
+    const u64 it = items[i];
+    items[i] = ((it >> 32) << idBits) | (it & 0xffffffffull);
   }
 }
 __global__ void gather_u64_kernel(const u64* __restrict__ src, const u32* __restrict__ perm, u64 m, u64* __restrict__ dst)
@@ -1123,8 +1135,8 @@ static int collect(Collected& c, bool withDist, u64 guess, F&& launch, cudaStrea
   return OTG_ERR_OUT_OF_MEMORY;
 }
 
-// CSR result with ids ascending per query
-static int finish_sorted_ids(Collected& c, u64 nq, ResultState& r, cudaStream_t st)
+// CSR result with ids ascending per query; ids are below idLimit
+static int finish_sorted_ids(Collected& c, u64 nq, ResultState& r, cudaStream_t st, u64 idLimit = u64(1) << 32)
 {
   const u64 m = c.m;
   r.nq = nq;
@@ -1138,9 +1150,12 @@ static int finish_sorted_ids(Collected& c, u64 nq, ResultState& r, cudaStream_t 
   TmpBuf vals, qid;
   if ((e = vals.ensure(sizeof(u32) * m, st)) || (e = qid.ensure(sizeof(u32) * m, st)))
     return cuda_status(e, "allocating sort values");
-  if (int rc = sort_pairs_u64(c.items.as<u64>(), vals.as<u32>(), m, 32 + bit_count(nq), st, c.err.as<u32>()))
+  const u32 idBits = std::min<u32>(32, std::max<u32>(1, bit_count(std::max<u64>(idLimit, 1) - 1)));
+  if (idBits < 32)
+    pack_items_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), m, idBits);
+  if (int rc = sort_pairs_u64(c.items.as<u64>(), vals.as<u32>(), m, idBits + bit_count(nq), st, c.err.as<u32>()))
     return rc;
-  split_items_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), nullptr, m, qid.as<u32>(), r.ids.as<u32>());
+  split_items_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), nullptr, m, qid.as<u32>(), r.ids.as<u32>(), idBits);
   offsets_kernel<<<blocks_for(nq + 1), 256, 0, st>>>(qid.as<u32>(), m, nq, r.offsets.as<u64>());
   e = cudaStreamSynchronize(st);
   return cuda_status(e ? e : cudaGetLastError(), "finishing result");
@@ -1321,7 +1336,7 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
     return launchRc;
   if (rc)
     return rc;
-  return finish_sorted_ids(c, nq, r, st);
+  return finish_sorted_ids(c, nq, r, st, t.n);
 }
 
 template<typename T>
@@ -1362,7 +1377,7 @@ static int pick_impl(const TreeState& t, const void* pts, u64 nq, double tol, in
     return launchRc;
   if (rc)
     return rc;
-  return finish_sorted_ids(c, nq, r, st);
+  return finish_sorted_ids(c, nq, r, st, t.n);
 }
 
 template<typename T>
@@ -1404,7 +1419,7 @@ static int frustum_impl(const TreeState& t, const void* planes, u64 np, u64 nq, 
     return launchRc;
   if (rc)
     return rc;
-  return finish_sorted_ids(c, nq, r, st);
+  return finish_sorted_ids(c, nq, r, st, t.n);
 }
 
 template<typename T>
@@ -1447,7 +1462,7 @@ static int plane_impl(const TreeState& t, const void* planes, u64 nq, bool posit
     return launchRc;
   if (rc)
     return rc;
-  return finish_sorted_ids(c, nq, r, st);
+  return finish_sorted_ids(c, nq, r, st, t.n);
 }
 
 // conditions given in host memory are checked here; device conditions are checked by the kernels
@@ -1542,7 +1557,7 @@ static int query_impl(const TreeState& t, const QueryCond* conds, const u64* off
     return launchRc;
   if (rc)
     return rc;
-  return finish_sorted_ids(c, nq, r, st);
+  return finish_sorted_ids(c, nq, r, st, t.n);
 }
 
 template<typename T>
