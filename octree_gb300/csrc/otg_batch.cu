@@ -131,21 +131,74 @@ __device__ __forceinline__ void range_thresholds(const double* r, const double* 
 
 // The FP64 tests of the undecided cases, out of line: inlined, the compiler may evaluate them for
 // every node and point beside the FP32 tests (predicated), which kept the FP64 pipe busy.
-struct RangeD // the query box and its size, passed by value (no address of the caller's arrays escapes)
+// the query's range as the caller passed it (6 doubles), and its size
+__device__ __forceinline__ void range_load(const double* q, double r[6], double rsize[3])
+{
+#pragma unroll
+  for (int c = 0; c < 6; ++c)
+    r[c] = q[c];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    rsize[c] = r[3 + c] - r[c];
+}
+__device__ __noinline__ bool range_node_enters_fp64(const double* q, const double* nb, double tol)
 {
   double r[6], rsize[3];
+  range_load(q, r, rsize);
+  return GeoD<double>::overlap_by_min_point(r, rsize, nb, nb + 3, tol);
+}
+__device__ __noinline__ bool range_node_inside_fp64(const double* q, const double* nb, double tol)
+{
+  double r[6], rsize[3];
+  range_load(q, r, rsize);
+  return GeoD<double>::range_contains_min_size(r, nb, nb + 3, tol);
+}
+__device__ __noinline__ bool range_point_inside_fp64(const double* q, const double* p, double tol)
+{
+  double r[6], rsize[3];
+  range_load(q, r, rsize);
+  return GeoD<double>::box_contains_point(r, p, tol);
+}
+
+// One query's FP64 setup, done beforehand by one thread per query (an FP64 instruction of a warp
+// occupies this GPU's FP64 pipe for many cycles, so a warp doing one query's setup costs 32 times as
+// much): the FP32 thresholds, and the flags of the root shortcut and of an empty range.
+constexpr u32 kRangeAll = 1u, kRangeEmpty = 2u;
+struct RangeQ
+{
+  RangeF32 f;
+  u32 flags, pad;
 };
-__device__ __noinline__ bool range_node_enters_fp64(const RangeD q, const double* nb, double tol)
+static_assert(sizeof(RangeQ) == 80, "RangeQ: 20 words");
+
+__global__ void __launch_bounds__(128) range_prepare_kernel(TreeView<double> tv, const double* __restrict__ ranges, u32 nq, double tol,
+                                                            RangeQ* __restrict__ out)
 {
-  return GeoD<double>::overlap_by_min_point(q.r, q.rsize, nb, nb + 3, tol);
-}
-__device__ __noinline__ bool range_node_inside_fp64(const RangeD q, const double* nb, double tol)
-{
-  return GeoD<double>::range_contains_min_size(q.r, nb, nb + 3, tol);
-}
-__device__ __noinline__ bool range_point_inside_fp64(const RangeD q, const double* p, double tol)
-{
-  return GeoD<double>::box_contains_point(q.r, p, tol);
+  using G = GeoD<double>;
+  for (u32 q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x)
+  {
+    const u32 root = query_root(tv, q);
+    double r[6], rsize[3], rb[6];
+    range_load(ranges + u64(q) * 6, r, rsize);
+    const double* nb = tv.nodeBox + u64(root) * 6;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+    {
+      rb[c] = nb[c];
+      rb[3 + c] = nb[c] + nb[3 + c];
+    }
+    RangeQ o;
+    o.flags = G::range_contains_box(r, rb, tol) ? kRangeAll : 0u; // root shortcut (:488-511)
+    double vol = 1.0;                                             // zero-volume range -> empty (:514-519)
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      vol *= rsize[c];
+    if (vol <= 0.0)
+      o.flags |= kRangeEmpty;
+    range_thresholds(r, rsize, nb, tol, o.f);
+    o.pad = 0;
+    out[q] = o;
+  }
 }
 
 // node: enter 0 (pruned) / 1 (entered) / 2 (undecided); inside 0 / 1 / 2 likewise
@@ -198,6 +251,7 @@ struct BatchArgs
   int phase;          // 0: whole queries; 1: top levels, deeper subtrees become items; 2: the items
   u32 splitCap;       // item capacity of the work buffer
   u32 splitDepth;     // depth of the subtrees that become items
+  const void* prep = nullptr; // range on FP64 point trees: one RangeQ per query (FP32 pre-tests)
 };
 
 template<typename T, int KIND, int WARPS>
@@ -248,8 +302,38 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
     const T* pl = nullptr;
     RayD<T> ray;
     bool skip = false;
+    bool useF32 = false;
+    if constexpr (kRangeF32)
+    {
+      if (a.prep)
+      {
+        // the query's prepared thresholds into the warp's shared copy, its flags to every lane
+        const u32* src = reinterpret_cast<const u32*>(static_cast<const RangeQ*>(a.prep) + q);
+        __syncwarp(); // the previous query's thresholds are read by every lane before they change
+        if (lane < 18)
+          reinterpret_cast<u32*>(&rangeF[w])[lane] = src[lane];
+        const u32 flags = src[18];
+        __syncwarp();
+        useF32 = true;
+        if (a.phase != 2 && (flags & kRangeAll))
+        {
+          const u32 nt = tv.qTree ? u32(tv.treeOff[root + 1] - tv.treeOff[root]) : tv.n;
+          unsigned long long base = 0;
+          if (lane == 0)
+            base = a.out.reserve(nt);
+          base = __shfl_sync(~0u, base, 0);
+          for (u32 i = lane; i < nt; i += 32)
+            if (base + i < a.out.capacity)
+              a.out.items[base + i] = (u64(q) << 32) | i;
+          continue;
+        }
+        skip = (flags & kRangeEmpty) != 0;
+      }
+    }
     if constexpr (KIND == kRange)
     {
+      if (!useF32)
+      {
       load_box(a.q + u64(q) * 6, r);
       if (a.phase != 2) // items continue queries that passed this setup in the first phase
       {
@@ -281,6 +365,7 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
         vol *= rsize[c];
       }
       skip = vol <= T(0);
+      }
     }
     else if constexpr (KIND == kFrustum)
     {
@@ -311,23 +396,12 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
     }
     if (skip)
       continue;
-    // FP32 pre-tests (range on FP64 point trees): the query's thresholds, shared by the warp
-    bool useF32 = false;
-    if constexpr (kRangeF32)
-    {
-      useF32 = tv.nodeImg != nullptr && tv.pointImg != nullptr && !tv.isBox;
-      __syncwarp(); // the previous query's thresholds are read by every lane before they change
-      if (useF32 && lane == 0)
-        range_thresholds(r, rsize, tv.nodeBox + u64(root) * 6, double(a.tol), rangeF[w]);
-      __syncwarp();
-    }
     // ---- node test of one node (run by one lane per child)
     auto enters = [&](u32 node, bool& contained) -> bool {
       const T* nb = tv.nodeBox + u64(node) * 6;
       contained = false;
       if constexpr (KIND == kRange)
       {
-        T nmin[3] = { nb[0], nb[1], nb[2] }, nsize[3] = { nb[3], nb[4], nb[5] };
         if constexpr (kRangeF32)
         {
           if (useF32)
@@ -336,14 +410,15 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
             range_node_f32(tv.nodeImg, node, rangeF[w], en, in);
             if (en == 0)
               return false;
-            if (en == 2 && !range_node_enters_fp64(RangeD{ { r[0], r[1], r[2], r[3], r[4], r[5] }, { rsize[0], rsize[1], rsize[2] } }, nb, a.tol))
+            if (en == 2 && !range_node_enters_fp64(a.q + u64(q) * 6, nb, a.tol))
               return false;
             contained = in == 1;
             if (in == 2)
-              contained = range_node_inside_fp64(RangeD{ { r[0], r[1], r[2], r[3], r[4], r[5] }, { rsize[0], rsize[1], rsize[2] } }, nb, a.tol);
+              contained = range_node_inside_fp64(a.q + u64(q) * 6, nb, a.tol);
             return true;
           }
         }
+        T nmin[3] = { nb[0], nb[1], nb[2] }, nsize[3] = { nb[3], nb[4], nb[5] };
         if (!G::overlap_by_min_point(r, rsize, nmin, nsize, a.tol))
           return false;
         contained = G::range_contains_min_size(r, nmin, nsize, a.tol);
@@ -488,8 +563,7 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
                 if (dec == 2)
                 {
                   if constexpr (kRangeF32)
-                    hit = range_point_inside_fp64(RangeD{ { r[0], r[1], r[2], r[3], r[4], r[5] }, { rsize[0], rsize[1], rsize[2] } }, tv.geom + u64(e) * 3,
-                                                  a.tol);
+                    hit = range_point_inside_fp64(a.q + u64(q) * 6, tv.geom + u64(e) * 3, a.tol);
                   else
                     hit = G::box_contains_point(r, tv.geom + u64(e) * 3, a.tol);
                 }
@@ -670,7 +744,20 @@ static int launch_batch(const BatchArgs<T, KIND>& a0, int shape, cudaStream_t st
 template<typename T>
 int batch_range(const TreeView<T>& tv, const T* ranges, u32 nq, int mode, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape, size_t workBytes)
 {
-  return launch_batch<T, kRange>(BatchArgs<T, kRange>{ tv, ranges, 0, nq, mode, tol, T(0), T(0), out, work, err }, shape, st, workBytes);
+  BatchArgs<T, kRange> a{ tv, ranges, 0, nq, mode, tol, T(0), T(0), out, work, err };
+  TmpBuf prep;
+  if constexpr (sizeof(T) == 8)
+  {
+    // FP64 point trees with FP32 images: the per-query setup by one thread per query
+    if (tv.nodeImg && tv.pointImg && !tv.isBox && nq)
+    {
+      if (cudaError_t e = prep.ensure(sizeof(RangeQ) * nq, st))
+        return cuda_status(e, "allocating the range setup");
+      range_prepare_kernel<<<u32((nq + 127) / 128), 128, 0, st>>>(tv, ranges, nq, double(tol), prep.as<RangeQ>());
+      a.prep = prep.p;
+    }
+  }
+  return launch_batch<T, kRange>(a, shape, st, workBytes);
 }
 template<typename T>
 int batch_frustum(const TreeView<T>& tv, const T* planes, u32 np, u32 nq, T tol, Appender out, u32* work, u32* err, cudaStream_t st, int shape, size_t workBytes)
