@@ -251,7 +251,9 @@ struct BatchArgs
   int phase;          // 0: whole queries; 1: top levels, deeper subtrees become items; 2: the items
   u32 splitCap;       // item capacity of the work buffer
   u32 splitDepth;     // depth of the subtrees that become items
-  const void* prep = nullptr; // range on FP64 point trees: one RangeQ per query (FP32 pre-tests)
+  // range on FP64 point trees: one RangeQ per query (FP32 pre-tests); set only where out.count has
+  // three slots (the item count, then the pre-tests and the undecided ones, added at the end)
+  const void* prep = nullptr;
 };
 
 template<typename T, int KIND, int WARPS>
@@ -269,6 +271,7 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
   WarpSink sink{ itemMem[w], KIND == kRayAll ? distMem[w] : nullptr, 0 };
   const TreeView<T>& tv = a.tv;
   u64* items = reinterpret_cast<u64*>(a.work + 4);
+  u32 f32Tests = 0, f32Undecided = 0; // FP32 pre-tests of this lane (range on FP64 point trees)
   for (;;)
   {
     u32 q = 0, start = 0;
@@ -408,6 +411,8 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
           {
             int en, in;
             range_node_f32(tv.nodeImg, node, rangeF[w], en, in);
+            ++f32Tests;
+            f32Undecided += (en == 2 || (en != 0 && in == 2)) ? 1u : 0u;
             if (en == 0)
               return false;
             if (en == 2 && !range_node_enters_fp64(a.q + u64(q) * 6, nb, a.tol))
@@ -417,6 +422,12 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
               contained = range_node_inside_fp64(a.q + u64(q) * 6, nb, a.tol);
             return true;
           }
+          // FP64 trees without the pre-tests (box trees): the same tests, out of line, so that none of
+          // their FP64 arithmetic is evaluated beside the FP32 path
+          if (!range_node_enters_fp64(a.q + u64(q) * 6, nb, a.tol))
+            return false;
+          contained = range_node_inside_fp64(a.q + u64(q) * 6, nb, a.tol);
+          return true;
         }
         T nmin[3] = { nb[0], nb[1], nb[2] }, nsize[3] = { nb[3], nb[4], nb[5] };
         if (!G::overlap_by_min_point(r, rsize, nmin, nsize, a.tol))
@@ -558,7 +569,11 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
                 int dec = 2;
                 if constexpr (kRangeF32)
                   if (useF32)
+                  {
                     dec = range_point_f32(tv.pointImg[e], rangeF[w]);
+                    ++f32Tests;
+                    f32Undecided += dec == 2 ? 1u : 0u;
+                  }
                 hit = dec == 1;
                 if (dec == 2)
                 {
@@ -685,6 +700,24 @@ __global__ void __launch_bounds__(WARPS * 32) batch_query_kernel(BatchArgs<T, KI
     if (bad && lane == 0)
       atomicOr(a.err, kErrStack);
     sink_flush(sink, a.out, lane);
+  }
+  if constexpr (kRangeF32)
+  {
+    if (a.prep)
+    {
+      // the warp's counts, after the item count of the appender
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        f32Tests += __shfl_xor_sync(~0u, f32Tests, o);
+        f32Undecided += __shfl_xor_sync(~0u, f32Undecided, o);
+      }
+      if (lane == 0)
+      {
+        atomicAdd(a.out.count + 1, (unsigned long long)f32Tests);
+        atomicAdd(a.out.count + 2, (unsigned long long)f32Undecided);
+      }
+    }
   }
 }
 

@@ -1063,8 +1063,9 @@ __global__ void item_ids_kernel(const u64* __restrict__ items, u64 m, u32* __res
 
 struct Collected
 {
-  TmpBuf items, dist, count, err;
+  TmpBuf items, dist, count, err; // count: the item count, then the filter's tests and undecided tests
   u64 m = 0;
+  u64 tests = 0, rechecks = 0;
 };
 
 static int check_err(const TmpBuf& err, cudaStream_t st)
@@ -1103,21 +1104,24 @@ template<typename F>
 static int collect(Collected& c, bool withDist, u64 guess, F&& launch, cudaStream_t st)
 {
   cudaError_t e;
-  if ((e = c.count.ensure(sizeof(unsigned long long), st)) || (e = c.err.ensure(sizeof(u32), st)))
+  if ((e = c.count.ensure(sizeof(unsigned long long) * 3, st)) || (e = c.err.ensure(sizeof(u32), st)))
     return cuda_status(e, "allocating counters");
   u64 cap = std::max<u64>(guess, 1024);
   for (int attempt = 0; attempt < 3; ++attempt)
   {
     if ((e = c.items.ensure(sizeof(u64) * cap, st)) || (withDist && (e = c.dist.ensure(sizeof(double) * cap, st))))
       return cuda_status(e, "allocating result buffer");
-    cudaMemsetAsync(c.count.p, 0, sizeof(unsigned long long), st);
+    cudaMemsetAsync(c.count.p, 0, sizeof(unsigned long long) * 3, st);
     cudaMemsetAsync(c.err.p, 0, sizeof(u32), st);
     Appender a{ c.items.as<u64>(), withDist ? c.dist.as<double>() : nullptr, c.count.as<unsigned long long>(), cap };
     launch(a, c.err.as<u32>());
     if ((e = cudaGetLastError()))
       return cuda_status(e, "launching query");
-    unsigned long long m = 0;
-    e = cudaMemcpyAsync(&m, c.count.p, sizeof(m), cudaMemcpyDeviceToHost, st);
+    unsigned long long h[3] = { 0, 0, 0 };
+    e = cudaMemcpyAsync(h, c.count.p, sizeof(h), cudaMemcpyDeviceToHost, st);
+    const unsigned long long m = h[0];
+    c.tests = h[1];
+    c.rechecks = h[2];
     if (!e)
       e = cudaStreamSynchronize(st);
     if (e)
@@ -1336,6 +1340,8 @@ static int range_impl(const TreeState& t, const void* ranges, u64 nq, int mode, 
     return launchRc;
   if (rc)
     return rc;
+  r.filterTests = c.tests; // the FP32 pre-tests of the batched kernel and the ones left to FP64
+  r.rechecks = c.rechecks;
   return finish_sorted_ids(c, nq, r, st, t.n);
 }
 
