@@ -352,7 +352,10 @@ void otg_forest_plan_free(otg_plan* plan);
 int otg_result_info(const otg_result* r, uint64_t* n_queries, uint64_t* n_ids, int* has_distances);
 /* offsets[n_queries+1], ids[n_ids], distances[n_ids] (double; may be NULL). mem: destination space. */
 int otg_result_copy(const otg_result* r, uint64_t* offsets, uint32_t* ids, double* distances, int mem, void* stream);
-/* Device pointers owned by the result (valid until otg_result_free). */
+/* Device pointers owned by the result (valid until otg_result_free). The arrays come from the
+   device's stream-ordered memory pool; otg_result_free returns them in the order of the legacy
+   default stream, so work of the caller's that reads them on another stream must be complete, or
+   ordered before that stream, when the result is freed. */
 int otg_result_device_ptrs(const otg_result* r, const uint64_t** offsets, const uint32_t** ids, const double** distances);
 /* Statistics of the last query that produced r: FP32-filter tests and FP64 rechecks. */
 int otg_result_stats(const otg_result* r, uint64_t* filter_tests, uint64_t* fp64_rechecks);

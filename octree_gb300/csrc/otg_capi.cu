@@ -714,9 +714,10 @@ extern "C"
   {
     if (!r)
       return;
-    r->s.offsets.release();
-    r->s.ids.release();
-    r->s.dist.release();
+    // in stream order on the legacy default stream (the query's own stream may be gone by now)
+    r->s.offsets.release_async(nullptr);
+    r->s.ids.release_async(nullptr);
+    r->s.dist.release_async(nullptr);
     delete r;
   }
 }

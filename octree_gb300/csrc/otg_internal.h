@@ -268,9 +268,21 @@ struct ResultState
   u64 nq = 0;
   u64 nids = 0;
   bool hasDist = false;
+  // the arrays come from the stream-ordered pool on the query's stream and go back to it in that
+  // stream's order (result_alloc, otg_result_free)
+  cudaStream_t stream = nullptr;
   DevBuf offsets; // u64[nq+1]
   DevBuf ids;     // u32[nids]
   DevBuf dist;    // double[nids]
+  ResultState() = default;
+  ResultState(const ResultState&) = delete;
+  ResultState& operator=(const ResultState&) = delete;
+  ~ResultState()
+  {
+    offsets.release_async(stream);
+    ids.release_async(stream);
+    dist.release_async(stream);
+  }
   u64 filterTests = 0;
   u64 rechecks = 0;
 };
@@ -288,6 +300,19 @@ struct Profiler
 };
 Profiler& profiler();
 int cuda_status(cudaError_t e, const char* what);
+// a query result's arrays (bytes of each; 0 leaves one unallocated), from the pool on stream st
+inline cudaError_t result_alloc(ResultState& r, size_t offBytes, size_t idBytes, size_t distBytes, cudaStream_t st)
+{
+  r.stream = st;
+  cudaError_t e = cudaSuccess;
+  if (offBytes && (e = r.offsets.ensure_pooled(offBytes, st)))
+    return e;
+  if (idBytes && (e = r.ids.ensure_pooled(idBytes, st)))
+    return e;
+  if (distBytes && (e = r.dist.ensure_pooled(distBytes, st)))
+    return e;
+  return cudaSuccess;
+}
 
 // kernel-shape autotuner (otg_tune.cu): runs launch(shape) with the fastest candidate shape of the
 // key's size class, timing every candidate on the first call of the class

@@ -892,13 +892,13 @@ static int knn_filtered_impl(TreeState& t, const T* pts, const u32* dk, u64 nq, 
   // CSR: offsets by scan of the counts, then entries moved into query order
   const u64 tiles = (nq + kScanTile - 1) / kScanTile;
   TmpBuf tileSums;
-  if ((e = tileSums.ensure(sizeof(u64) * (tiles + 1), st)) || (e = r.offsets.ensure(sizeof(u64) * (nq + 1))))
+  if ((e = tileSums.ensure(sizeof(u64) * (tiles + 1), st)) || (e = result_alloc(r, sizeof(u64) * (nq + 1), 0, 0, st)))
     return cuda_status(e, "allocating result offsets");
   scan_reduce_kernel<<<u32(tiles), kScanThreads, 0, st>>>(cnt.as<u32>(), nq, tileSums.as<u64>());
   scan_tiles_kernel<<<1, kScanThreads, 0, st>>>(tileSums.as<u64>(), tiles);
   scan_apply_kernel<<<u32(tiles), kScanThreads, 0, st>>>(cnt.as<u32>(), nq, tileSums.as<u64>(), r.offsets.as<u64>());
   const u64 total = h.out + fbr.nids;
-  if ((e = r.ids.ensure(sizeof(u32) * std::max<u64>(total, 1))) || (e = r.dist.ensure(sizeof(double) * std::max<u64>(total, 1))))
+  if ((e = result_alloc(r, 0, sizeof(u32) * std::max<u64>(total, 1), sizeof(double) * std::max<u64>(total, 1), st)))
     return cuda_status(e, "allocating the result");
   csr_move_kernel<<<blocks_for(nq * 32), 256, 0, st>>>(start.as<u64>(), cnt.as<u32>(), r.offsets.as<u64>(), nq, oIds.as<u32>(), oDist.as<double>(),
                                                         fbr.ids.as<u32>(), fbr.dist.as<double>(), r.ids.as<u32>(), r.dist.as<double>());

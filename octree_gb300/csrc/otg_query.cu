@@ -1063,19 +1063,16 @@ __global__ void item_ids_kernel(const u64* __restrict__ items, u64 m, u32* __res
 
 struct Collected
 {
-  TmpBuf items, dist, count, err; // count: the item count, then the filter's tests and undecided tests
+  // count: four words read back together: the item count, the filter's tests, the undecided tests,
+  // and the error bits (the low half of the fourth)
+  TmpBuf items, dist, count;
   u64 m = 0;
   u64 tests = 0, rechecks = 0;
+  u32* errp() const { return reinterpret_cast<u32*>(count.as<unsigned long long>() + 3); }
 };
 
-static int check_err(const TmpBuf& err, cudaStream_t st)
+static int status_of(u32 h)
 {
-  u32 h = 0;
-  cudaError_t e = cudaMemcpyAsync(&h, err.p, sizeof(u32), cudaMemcpyDeviceToHost, st);
-  if (!e)
-    e = cudaStreamSynchronize(st);
-  if (e)
-    return cuda_status(e, "reading query status");
   if (h & kErrStack)
   {
     set_error("traversal stack bound exceeded");
@@ -1104,29 +1101,28 @@ template<typename F>
 static int collect(Collected& c, bool withDist, u64 guess, F&& launch, cudaStream_t st)
 {
   cudaError_t e;
-  if ((e = c.count.ensure(sizeof(unsigned long long) * 3, st)) || (e = c.err.ensure(sizeof(u32), st)))
+  if ((e = c.count.ensure(sizeof(unsigned long long) * 4, st)))
     return cuda_status(e, "allocating counters");
   u64 cap = std::max<u64>(guess, 1024);
   for (int attempt = 0; attempt < 3; ++attempt)
   {
     if ((e = c.items.ensure(sizeof(u64) * cap, st)) || (withDist && (e = c.dist.ensure(sizeof(double) * cap, st))))
       return cuda_status(e, "allocating result buffer");
-    cudaMemsetAsync(c.count.p, 0, sizeof(unsigned long long) * 3, st);
-    cudaMemsetAsync(c.err.p, 0, sizeof(u32), st);
+    cudaMemsetAsync(c.count.p, 0, sizeof(unsigned long long) * 4, st);
     Appender a{ c.items.as<u64>(), withDist ? c.dist.as<double>() : nullptr, c.count.as<unsigned long long>(), cap };
-    launch(a, c.err.as<u32>());
+    launch(a, c.errp());
     if ((e = cudaGetLastError()))
       return cuda_status(e, "launching query");
-    unsigned long long h[3] = { 0, 0, 0 };
+    unsigned long long h[4] = { 0, 0, 0, 0 };
     e = cudaMemcpyAsync(h, c.count.p, sizeof(h), cudaMemcpyDeviceToHost, st);
-    const unsigned long long m = h[0];
-    c.tests = h[1];
-    c.rechecks = h[2];
     if (!e)
       e = cudaStreamSynchronize(st);
     if (e)
       return cuda_status(e, "running query");
-    if (int rc = check_err(c.err, st))
+    const unsigned long long m = h[0];
+    c.tests = h[1];
+    c.rechecks = h[2];
+    if (int rc = status_of(u32(h[3])))
       return rc;
     if (m <= cap)
     {
@@ -1147,7 +1143,7 @@ static int finish_sorted_ids(Collected& c, u64 nq, ResultState& r, cudaStream_t 
   r.nids = m;
   r.hasDist = false;
   cudaError_t e;
-  if ((e = r.offsets.ensure(sizeof(u64) * (nq + 1))) || (e = r.ids.ensure(sizeof(u32) * std::max<u64>(m, 1))))
+  if ((e = result_alloc(r, sizeof(u64) * (nq + 1), sizeof(u32) * std::max<u64>(m, 1), 0, st)))
     return cuda_status(e, "allocating result");
   if (m == 0)
     return cuda_status(cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * (nq + 1), st), "result offsets");
@@ -1157,7 +1153,7 @@ static int finish_sorted_ids(Collected& c, u64 nq, ResultState& r, cudaStream_t 
   const u32 idBits = std::min<u32>(32, std::max<u32>(1, bit_count(std::max<u64>(idLimit, 1) - 1)));
   if (idBits < 32)
     pack_items_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), m, idBits);
-  if (int rc = sort_pairs_u64(c.items.as<u64>(), vals.as<u32>(), m, idBits + bit_count(nq), st, c.err.as<u32>()))
+  if (int rc = sort_pairs_u64(c.items.as<u64>(), vals.as<u32>(), m, idBits + bit_count(nq), st, c.errp()))
     return rc;
   split_items_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), nullptr, m, qid.as<u32>(), r.ids.as<u32>(), idBits);
   offsets_kernel<<<blocks_for(nq + 1), 256, 0, st>>>(qid.as<u32>(), m, nq, r.offsets.as<u64>());
@@ -1173,15 +1169,14 @@ static int finish_by_distance(Collected& c, u64 nq, u64 nEntities, ResultState& 
   r.nids = m;
   r.hasDist = true;
   cudaError_t e;
-  if ((e = r.offsets.ensure(sizeof(u64) * (nq + 1))) || (e = r.ids.ensure(sizeof(u32) * std::max<u64>(m, 1))) ||
-      (e = r.dist.ensure(sizeof(double) * std::max<u64>(m, 1))))
+  if ((e = result_alloc(r, sizeof(u64) * (nq + 1), sizeof(u32) * std::max<u64>(m, 1), sizeof(double) * std::max<u64>(m, 1), st)))
     return cuda_status(e, "allocating result");
   if (m == 0)
     return cuda_status(cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * (nq + 1), st), "result offsets");
   TmpBuf perm, k32, k64;
   if ((e = perm.ensure(sizeof(u32) * m, st)) || (e = k32.ensure(sizeof(u32) * m, st)) || (e = k64.ensure(sizeof(u64) * m, st)))
     return cuda_status(e, "allocating sort buffers");
-  u32* err = c.err.as<u32>();
+  u32* err = c.errp();
   iota_kernel<<<blocks_for(m), 256, 0, st>>>(perm.as<u32>(), m);
   item_ids_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), m, k32.as<u32>());
   if (int rc = sort_pairs_u32(k32.as<u32>(), perm.as<u32>(), m, bit_count(nEntities), st, err))
@@ -1206,7 +1201,7 @@ static int finish_pairs(Collected& c, ResultState& r, cudaStream_t st)
   r.nids = 2 * m;
   r.hasDist = false;
   cudaError_t e;
-  if ((e = r.offsets.ensure(sizeof(u64) * 2)) || (e = r.ids.ensure(sizeof(u32) * std::max<u64>(2 * m, 1))))
+  if ((e = result_alloc(r, sizeof(u64) * 2, sizeof(u32) * std::max<u64>(2 * m, 1), 0, st)))
     return cuda_status(e, "allocating result");
   u64 offs[2] = { 0, 2 * m };
   if ((e = cudaMemcpyAsync(r.offsets.p, offs, sizeof(offs), cudaMemcpyHostToDevice, st)))
@@ -1216,7 +1211,7 @@ static int finish_pairs(Collected& c, ResultState& r, cudaStream_t st)
     TmpBuf vals;
     if ((e = vals.ensure(sizeof(u32) * m, st)))
       return cuda_status(e, "allocating sort values");
-    if (int rc = sort_pairs_u64(c.items.as<u64>(), vals.as<u32>(), m, 64, st, c.err.as<u32>()))
+    if (int rc = sort_pairs_u64(c.items.as<u64>(), vals.as<u32>(), m, 64, st, c.errp()))
       return rc;
     // (a << 32 | b) in little-endian memory is {b, a}: swap into {a, b}
     e = cudaMemcpyAsync(r.ids.p, c.items.p, sizeof(u64) * m, cudaMemcpyDeviceToDevice, st);
@@ -1259,11 +1254,8 @@ static int empty_result(u64 nq, ResultState& r, bool dist, cudaStream_t st)
   r.nq = nq;
   r.nids = 0;
   r.hasDist = dist;
-  if (cudaError_t e = r.offsets.ensure(sizeof(u64) * (nq + 1)))
+  if (cudaError_t e = result_alloc(r, sizeof(u64) * (nq + 1), 4, dist ? 8 : 0, st))
     return cuda_status(e, "allocating result");
-  r.ids.ensure(4);
-  if (dist)
-    r.dist.ensure(8);
   cudaError_t e = cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * (nq + 1), st);
   if (!e)
     e = cudaStreamSynchronize(st);
@@ -1688,8 +1680,8 @@ static int collide_impl(const TreeState& a, const TreeState& b, bool self, doubl
     r.nq = 1;
     r.nids = 0;
     r.hasDist = false;
-    r.offsets.ensure(sizeof(u64) * 2);
-    r.ids.ensure(4);
+    if (cudaError_t e = result_alloc(r, sizeof(u64) * 2, 4, 0, st))
+      return cuda_status(e, "allocating result");
     return cuda_status(cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * 2, st), "empty result");
   }
   Collected c;
