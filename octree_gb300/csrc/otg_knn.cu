@@ -576,9 +576,6 @@ __global__ void fallback_slots_kernel(const u32* __restrict__ fb, u32 nfb, const
   }
 }
 
-constexpr int kScanThreads = 256;
-constexpr int kScanItems = 8;
-constexpr int kScanTile = kScanThreads * kScanItems;
 
 __device__ __forceinline__ u64 block_scan_u64(u64 v, u64* warpSums, u64& total)
 {

@@ -1135,6 +1135,90 @@ static int collect(Collected& c, bool withDist, u64 guess, F&& launch, cudaStrea
   return OTG_ERR_OUT_OF_MEMORY;
 }
 
+// ---- canonical order of (query, id) results by counting: each query's run, sorted by one warp
+// items (query << 32 | id): the count of every query and each item's slot in its query's run
+__global__ void query_slots_kernel(const u64* __restrict__ items, u64 m, u32* __restrict__ cnt, u32* __restrict__ slot)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+    slot[i] = atomicAdd(&cnt[u32(items[i] >> 32)], 1u);
+}
+__global__ void query_scatter_kernel(const u64* __restrict__ items, const u32* __restrict__ slot, u64 m, const u64* __restrict__ off, u32* __restrict__ ids)
+{
+  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
+  {
+    const u64 it = items[i];
+    ids[off[u32(it >> 32)] + slot[i]] = u32(it);
+  }
+}
+// One warp per query sorts its run of ids ascending: up to 32 in registers, up to kRunSortMax in
+// shared memory (bitonic networks, padded with ~0); longer runs are only counted in *longRuns (the
+// caller then orders the whole result another way).
+constexpr u32 kRunSortMax = 1024;
+constexpr int kRunSortWarps = 8;
+__global__ void __launch_bounds__(kRunSortWarps * 32) run_sort_kernel(const u64* __restrict__ off, u64 nq, u32* __restrict__ ids, u32* __restrict__ longRuns)
+{
+  __shared__ u32 buf[kRunSortWarps][kRunSortMax];
+  const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const u64 warps = u64(gridDim.x) * kRunSortWarps;
+  for (u64 q = u64(blockIdx.x) * kRunSortWarps + w; q < nq; q += warps)
+  {
+    const u64 b = off[q];
+    const u32 len = u32(off[q + 1] - b);
+    if (len <= 1)
+      continue;
+    if (len > kRunSortMax)
+    {
+      if (lane == 0)
+        atomicAdd(longRuns, 1u);
+      continue;
+    }
+    if (len <= 32)
+    {
+      u32 v = lane < len ? ids[b + lane] : ~0u;
+#pragma unroll
+      for (u32 k = 2; k <= 32; k <<= 1)
+#pragma unroll
+        for (u32 j = k >> 1; j > 0; j >>= 1)
+        {
+          const u32 o = __shfl_xor_sync(~0u, v, j);
+          const bool up = (lane & k) == 0, lower = (lane & j) == 0;
+          v = (lower == up) ? min(v, o) : max(v, o);
+        }
+      if (lane < len)
+        ids[b + lane] = v;
+      continue;
+    }
+    u32 P = 64;
+    while (P < len)
+      P <<= 1;
+    u32* s = buf[w];
+    for (u32 i = lane; i < P; i += 32)
+      s[i] = i < len ? ids[b + i] : ~0u;
+    __syncwarp();
+    for (u32 k = 2; k <= P; k <<= 1)
+      for (u32 j = k >> 1; j > 0; j >>= 1)
+      {
+        for (u32 i = lane; i < P; i += 32)
+        {
+          const u32 x = i ^ j;
+          if (x > i)
+          {
+            const u32 a = s[i], c = s[x];
+            if ((a > c) == ((i & k) == 0))
+            {
+              s[i] = c;
+              s[x] = a;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    for (u32 i = lane; i < len; i += 32)
+      ids[b + i] = s[i];
+    __syncwarp();
+  }
+}
+
 // CSR result with ids ascending per query; ids are below idLimit
 static int finish_sorted_ids(Collected& c, u64 nq, ResultState& r, cudaStream_t st, u64 idLimit = u64(1) << 32)
 {
@@ -1147,6 +1231,31 @@ static int finish_sorted_ids(Collected& c, u64 nq, ResultState& r, cudaStream_t 
     return cuda_status(e, "allocating result");
   if (m == 0)
     return cuda_status(cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * (nq + 1), st), "result offsets");
+  if (m < (u64(1) << 32) && nq < (u64(1) << 31))
+  {
+    // counting order: counts and slots, offsets, ids into their runs, each run sorted by a warp
+    TmpBuf cnt, slot, tileSums, longRuns;
+    const u64 tiles = (nq + kScanTile - 1) / kScanTile;
+    if ((e = cnt.ensure(sizeof(u32) * nq, st)) || (e = slot.ensure(sizeof(u32) * m, st)) || (e = tileSums.ensure(sizeof(u64) * (tiles + 1), st)) ||
+        (e = longRuns.ensure(sizeof(u32), st)))
+      return cuda_status(e, "allocating the result order");
+    cudaMemsetAsync(cnt.p, 0, sizeof(u32) * nq, st);
+    cudaMemsetAsync(longRuns.p, 0, sizeof(u32), st);
+    query_slots_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), m, cnt.as<u32>(), slot.as<u32>());
+    scan_reduce_kernel<<<u32(tiles), kScanThreads, 0, st>>>(cnt.as<u32>(), nq, tileSums.as<u64>());
+    scan_tiles_kernel<<<1, kScanThreads, 0, st>>>(tileSums.as<u64>(), tiles);
+    scan_apply_kernel<<<u32(tiles), kScanThreads, 0, st>>>(cnt.as<u32>(), nq, tileSums.as<u64>(), r.offsets.as<u64>());
+    query_scatter_kernel<<<blocks_for(m), 256, 0, st>>>(c.items.as<u64>(), slot.as<u32>(), m, r.offsets.as<u64>(), r.ids.as<u32>());
+    run_sort_kernel<<<u32(std::min<u64>((nq + kRunSortWarps - 1) / kRunSortWarps, 152 * 8)), kRunSortWarps * 32, 0, st>>>(r.offsets.as<u64>(), nq,
+                                                                                                                          r.ids.as<u32>(), longRuns.as<u32>());
+    u32 hl = 0;
+    if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&hl, longRuns.p, sizeof(u32), cudaMemcpyDeviceToHost, st)) || (e = cudaStreamSynchronize(st)))
+      return cuda_status(e, "finishing result");
+    if (hl == 0)
+      return OTG_OK;
+    // some query holds more than kRunSortMax ids: the whole result by radix sort instead (the items
+    // are unchanged)
+  }
   TmpBuf vals, qid;
   if ((e = vals.ensure(sizeof(u32) * m, st)) || (e = qid.ensure(sizeof(u32) * m, st)))
     return cuda_status(e, "allocating sort values");

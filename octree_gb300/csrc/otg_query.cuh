@@ -219,6 +219,16 @@ __device__ __forceinline__ T entity_distance(const TreeView<T>& tv, u32 e, const
 }
 
 constexpr int kKnnMaxK = 256;
+
+// u64 offsets from u32 counts (otg_knn.cu): per-tile sums, their scan in one block (the grand total
+// at tileSums[tiles]), and the offsets; off holds n + 1 entries
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const u32* __restrict__ cnt, u64 n, u64* __restrict__ tileSums);
+__global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(u64* __restrict__ tileSums, u64 tiles);
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const u32* __restrict__ cnt, u64 n, const u64* __restrict__ tileSums,
+                                                                  u64* __restrict__ off);
 static inline int blocks_for(u64 n, int per = 256)
 {
   return int(std::max<u64>(1, std::min<u64>((n + per - 1) / per, 152 * 16)));

@@ -590,3 +590,32 @@ def test_range_on_exact_boundaries(tol):
         ref = o.range_search(ranges, mode, tol)
         for algo in (otg.ALGO_DEFAULT, otg.ALGO_PLAIN_FP64):
             assert_csr_equal(t.range_search(ranges, mode, tol=tol, algo=algo)[:2], ref, f"range mode {mode} tol {tol} algo {algo}")
+
+
+@pytest.mark.parametrize("sizes", ["small", "medium", "with_long"])
+def test_result_runs_of_every_length(sizes):
+    """Results are put in canonical order per query by counting and a sort of each query's run:
+    runs of at most 32 ids, runs of 33-1024 ids, and batches holding a longer run (which take the
+    radix sort of the whole result instead) all give the oracle's ids."""
+    rng = np.random.default_rng({"small": 41, "medium": 42, "with_long": 43}[sizes])
+    pts = rng.random((100_000, 3)) * 100
+    c = rng.random((400, 3)) * 100
+    half = {"small": 1.0, "medium": 5.0, "with_long": 5.0}[sizes] * (0.5 + rng.random((400, 1)))
+    if sizes == "with_long":
+        half[:3] = 30.0  # tens of thousands of ids each
+    ranges = np.concatenate([c - half, c + half], 1)
+    t = _gpu_tree(pts, KIND_POINTS, 8, None, 16)
+    o = oracle().create(pts, KIND_POINTS, 8, None, 16)
+    ref = o.range_search(ranges, 0)
+    counts = np.diff(ref[0].astype(np.int64))
+    if sizes == "small":
+        assert counts.max() <= 32
+    elif sizes == "medium":
+        assert counts.max() <= 1024 and counts.max() > 32
+    else:
+        assert counts.max() > 1024
+    for algo in (otg.ALGO_DEFAULT, otg.ALGO_PLAIN_FP64):
+        assert_csr_equal(t.range_search(ranges, 0, algo=algo)[:2], ref, f"range runs {sizes} algo {algo}")
+    planes = np.concatenate([rng.random((50, 1)) * 60 + 20, rng.normal(size=(50, 3))], 1)
+    planes[:, 1:] /= np.linalg.norm(planes[:, 1:], axis=1, keepdims=True)
+    assert_csr_equal(t.plane_search(planes, tol=0.05)[:2], o.plane_search(planes, 0.05), f"plane runs {sizes}")
