@@ -1137,10 +1137,25 @@ static int collect(Collected& c, bool withDist, u64 guess, F&& launch, cudaStrea
 
 // ---- canonical order of (query, id) results by counting: each query's run, sorted by one warp
 // items (query << 32 | id): the count of every query and each item's slot in its query's run
+// (the lanes of a warp that hold the same query take their slots with one atomic)
 __global__ void query_slots_kernel(const u64* __restrict__ items, u64 m, u32* __restrict__ cnt, u32* __restrict__ slot)
 {
-  for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < m; i += u64(gridDim.x) * blockDim.x)
-    slot[i] = atomicAdd(&cnt[u32(items[i] >> 32)], 1u);
+  const u32 lane = threadIdx.x & 31;
+  const u64 stride = u64(gridDim.x) * blockDim.x;
+  for (u64 base = blockIdx.x * u64(blockDim.x) + (threadIdx.x & ~31u); base < m; base += stride)
+  {
+    const u64 i = base + lane;
+    const bool v = i < m;
+    const u32 q = v ? u32(items[i] >> 32) : 0xffffffffu;
+    const u32 peers = __match_any_sync(~0u, q);
+    const int leader = __ffs(int(peers)) - 1;
+    u32 b = 0;
+    if (v && int(lane) == leader)
+      b = atomicAdd(&cnt[q], u32(__popc(peers)));
+    b = __shfl_sync(~0u, b, leader);
+    if (v)
+      slot[i] = b + __popc(peers & ((1u << lane) - 1u));
+  }
 }
 __global__ void query_scatter_kernel(const u64* __restrict__ items, const u32* __restrict__ slot, u64 m, const u64* __restrict__ off, u32* __restrict__ ids)
 {
@@ -1231,7 +1246,9 @@ static int finish_sorted_ids(Collected& c, u64 nq, ResultState& r, cudaStream_t 
     return cuda_status(e, "allocating result");
   if (m == 0)
     return cuda_status(cudaMemsetAsync(r.offsets.p, 0, sizeof(u64) * (nq + 1), st), "result offsets");
-  if (m < (u64(1) << 32) && nq < (u64(1) << 31))
+  // runs longer than kRunSortMax on average certainly include long ones: straight to the radix sort
+  // (counting them would also put every item's atomic on a few counters)
+  if (m < (u64(1) << 32) && nq < (u64(1) << 31) && m <= u64(kRunSortMax) * nq)
   {
     // counting order: counts and slots, offsets, ids into their runs, each run sorted by a warp
     TmpBuf cnt, slot, tileSums, longRuns;
