@@ -437,9 +437,9 @@ def run_gpu(args):
     }
     # kernel launches per build of this workload (as in the ncu launch list of
     # profiles/build16m_launch_list.md): bbox init, bbox, space setup, raster tables, MinPoint table,
-    # codegen, the radix passes, gather, root init, the root's classify launch and a split launch per
-    # depth 0..D-1
-    line["gpu_launches"] = args.steps * (6 + passes + 1 + 1 + 1 + MAX_DEPTH)
+    # codegen, the digit bases, the radix passes, gather, root init, the root's classify launch and a
+    # split launch per depth 0..D-1
+    line["gpu_launches"] = args.steps * (6 + 1 + passes + 1 + 1 + 1 + MAX_DEPTH)
     if rank == 0 and not args.no_cpu_baseline:
         rate, kind, threads = cpu_build_rate(pts_h, 2)
         line["cpu_baseline"] = {
@@ -1159,7 +1159,7 @@ def run_insert(reps=3, cpu=True):
     return out
 
 
-PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m", "build_4m_clustered", "forest_frustum_1024", "insert_16m_1m", "insert_4m_250k", "range_1m_10k")
+PROFILE_CASES = ("knn_4m_200k", "collide_1m", "build_4m", "build_16m", "build_4m_clustered", "forest_frustum_1024", "insert_16m_1m", "insert_4m_250k", "range_1m_10k")
 
 
 def run_profile_case(name):
@@ -1227,8 +1227,10 @@ def run_profile_case(name):
             t = otg.Tree("points").create(pts, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)
             t.insert(add)
         print(json.dumps({"case": name, "nodes": int(t.node_count)}))
-    elif name == "build_4m":
-        pts = torch.as_tensor(shell_points(4_000_000, 301), device="cuda")
+    elif name in ("build_4m", "build_16m"):
+        # build_16m: the measured workload (384 MB of points, above the L2), about 2 GB on the device
+        n = 4_000_000 if name == "build_4m" else N_POINTS
+        pts = torch.as_tensor(shell_points(n, 301), device="cuda")
         t = otg.Tree("points")
         for _ in range(2):
             t.create(pts, max_depth=MAX_DEPTH, max_elements=MAX_ELEM)

@@ -153,6 +153,77 @@ __global__ void __launch_bounds__(256) radix_histogram_kernel(const K* __restric
         atomicAdd(&hist[p * kRadix + d], sh[p][d]);
 }
 
+// Rows of 256 digit counts (one per pass, or per pass and segment) turned into their exclusive
+// prefix sums in place: the global base of every digit, scanned once per pass instead of in every
+// tile.
+static __global__ void __launch_bounds__(kRadix) digit_base_kernel(u32* __restrict__ hist)
+{
+  __shared__ u32 s_warp[kRadix / 32];
+  u32* row = hist + u64(blockIdx.x) * kRadix;
+  const int d = threadIdx.x, lane = d & 31, warp = d >> 5;
+  const u32 v = row[d];
+  u32 x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    const u32 y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o)
+      x += y;
+  }
+  if (lane == 31)
+    s_warp[warp] = x;
+  __syncthreads();
+  u32 before = 0;
+#pragma unroll
+  for (int w = 0; w < kRadix / 32; ++w)
+    before += w < warp ? s_warp[w] : 0u;
+  row[d] = before + x - v;
+}
+
+// Decoupled look-back for digit d of tile `tile`: the sum of the counts of the earlier tiles
+// (down to firstTile) from their published statuses, eight predecessors per round trip. A wait
+// that runs out of its iteration limit sets kErrTimeout and returns what it has.
+__device__ __forceinline__ u32 lookback_prefix(volatile u32* vstatus, u32 tile, u32 firstTile, u32 d, u32* err)
+{
+  u32 prefix = 0;
+  long long j = (long long)tile - 1;
+  u32 spins = 0;
+  while (j >= (long long)firstTile)
+  {
+    u32 sv[kLookbackBatch];
+#pragma unroll
+    for (int k = 0; k < kLookbackBatch; ++k)
+      sv[k] = (j - k >= (long long)firstTile) ? vstatus[u64(j - k) * kRadix + d] : u32(kStatusInclusive);
+    int used = 0;
+    bool done = false;
+#pragma unroll
+    for (int k = 0; k < kLookbackBatch; ++k)
+    {
+      if (done || used < k)
+        continue;
+      const u32 flag = sv[k] & ~kStatusValueMask;
+      if (flag == 0)
+        continue; // not published yet: re-read from here
+      prefix += sv[k] & kStatusValueMask;
+      used = k + 1;
+      done = flag == kStatusInclusive;
+    }
+    if (done)
+      break;
+    j -= used;
+    if (used < kLookbackBatch)
+    {
+      if (++spins > kLookbackSpinLimit)
+      {
+        atomicOr(err, kErrTimeout);
+        break;
+      }
+      __nanosleep(32);
+    }
+  }
+  return prefix;
+}
+
 // One onesweep pass. vin == nullptr means values are the input positions (iota).
 // Order of work in a tile: per-warp digit counts (shared-memory atomics without return values),
 // publication of the tile's counts as an aggregate right away, then the ranking, and only then
@@ -162,16 +233,18 @@ __global__ void __launch_bounds__(256) radix_histogram_kernel(const K* __restric
 // atomic, and each lane adds its rank among lower lanes.
 // Segmented form (segTiles != null): independent sorts of the segments [segOff[s], segOff[s+1])
 // in one launch. Tile i covers tile segTiles[i].y of segment segTiles[i].x (the tiles of a segment
-// are consecutive, in order), the look-back stops at the segment's first tile, and hist holds
-// 256 digit counts per segment. Positions are below 2^30, so they are kept in 32 bits.
+// are consecutive, in order), the look-back stops at the segment's first tile, and digitBase holds
+// 256 digit bases per segment. Positions are below 2^30, so they are kept in 32 bits.
 // DEVN: the element count is read from device memory (segOff[0] as unsigned long long, at most n);
 // tiles that start past it end at once (no later tile looks back at them).
+// digitBase: the pass's global digit bases (digit_base_kernel), per segment in the segmented form
+// (16M points: 0.444 ms for the four passes, against 0.453 ms scanning the counts in every tile).
 // STAGE (single sort only): whole tiles arrive by bulk copies instead of plain loads. Measured on
 // 16M points (4 passes, 31-bit keys): 0.522 ms staged against 0.517 ms with plain loads, so plain
 // loads are the default and OTG_SORT_STAGE=1 selects the staged form.
 template<typename K, bool SEG = false, bool DEVN = false, bool STAGE = false>
 __global__ void __launch_bounds__(kSortThreads, 3) onesweep_pass_kernel(const K* __restrict__ kin, const u32* __restrict__ vin, K* __restrict__ kout,
-                                                                     u32* __restrict__ vout, u32 n, u32 shift, const u32* __restrict__ hist,
+                                                                     u32* __restrict__ vout, u32 n, u32 shift, const u32* __restrict__ digitBase,
                                                                      u32* __restrict__ status, u32* __restrict__ tileCounter, u32* __restrict__ err,
                                                                      const uint2* __restrict__ segTiles = nullptr, const u64* __restrict__ segOff = nullptr)
 {
@@ -212,7 +285,7 @@ __global__ void __launch_bounds__(kSortThreads, 3) onesweep_pass_kernel(const K*
     segBase = u32(segOff[st.x]);
     segEnd = u32(segOff[st.x + 1]);
     tileInSeg = st.y;
-    hist += u64(st.x) * kRadix;
+    digitBase += u64(st.x) * kRadix;
   }
   const u32 base = segBase + tileInSeg * u32(kSortTile);
   const u32 firstTile = tile - tileInSeg;
@@ -292,8 +365,11 @@ __global__ void __launch_bounds__(kSortThreads, 3) onesweep_pass_kernel(const K*
   }
   __syncthreads();
 
+  // Ranking, and each key straight into shared memory at its rank in the tile's digit order (the
+  // loads from a staged tile ended at the barrier after the counts), so the look-back holds no keys
+  // in registers. 16M points, the four passes: 0.453 ms, against 0.498 ms scattering from a rank
+  // array after the ranking and 0.515 ms scattering after the look-back.
   const u32 ltmask = lanemask_lt();
-  u32 pos[kSortItems];
 #pragma unroll
   for (int i = 0; i < kSortItems; ++i)
   {
@@ -312,63 +388,25 @@ __global__ void __launch_bounds__(kSortThreads, 3) onesweep_pass_kernel(const K*
     if (d < kRadix && lane == leader)
       old = atomicAdd(&s_cnt[warp][d], u32(__popc(peers)));
     old = __shfl_sync(0xffffffffu, old, leader);
-    pos[i] = old + __popc(peers & ltmask);
-  }
-
-  // decoupled look-back over earlier tiles of the segment for digit tid, eight predecessors per round trip
-  u32 prefix = 0;
-  if (tid < kRadix && tileInSeg > 0)
-  {
-    long long j = (long long)tile - 1;
-    u32 spins = 0;
-    while (j >= (long long)firstTile)
+    if (d < kRadix)
     {
-      u32 sv[kLookbackBatch];
-#pragma unroll
-      for (int k = 0; k < kLookbackBatch; ++k)
-        sv[k] = (j - k >= (long long)firstTile) ? vstatus[u64(j - k) * kRadix + tid] : u32(kStatusInclusive);
-      int used = 0;
-      bool done = false;
-#pragma unroll
-      for (int k = 0; k < kLookbackBatch; ++k)
-      {
-        if (done || used < k)
-          continue;
-        const u32 flag = sv[k] & ~kStatusValueMask;
-        if (flag == 0)
-          continue; // not published yet: re-read from here
-        prefix += sv[k] & kStatusValueMask;
-        used = k + 1;
-        done = flag == kStatusInclusive;
-      }
-      if (done)
-        break;
-      j -= used;
-      if (used < kLookbackBatch)
-      {
-        if (++spins > kLookbackSpinLimit)
-        {
-          atomicOr(err, kErrTimeout);
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-    vstatus[u64(tile) * kRadix + tid] = kStatusInclusive | ((prefix + total) & kStatusValueMask);
-  }
-  u32 hcount = tid < kRadix ? hist[tid] : 0u;
-  u32 hsum;
-  const u32 histPrefix = block_exclusive_scan(hcount, s_scan, hsum); // its barriers also end the ranking
-  if (tid < kRadix)
-    s_globalBase[tid] = segBase + histPrefix + prefix - digitStart;
-#pragma unroll
-  for (int i = 0; i < kSortItems; ++i)
-    if (dig[i] < kRadix)
-    {
-      const u32 p = pos[i] & (kSortTile - 1); // ranks of a tile are below kSortTile by construction
+      const u32 p = (old + __popc(peers & ltmask)) & (kSortTile - 1); // ranks of a tile are below kSortTile by construction
       s_keys[p] = keys[i];
       s_vals[p] = vals[i];
     }
+  }
+
+  // The look-back after the ranking: predecessors have had the ranking's duration to publish
+  // (looking back first, beside the other warps' ranking: 0.447 against 0.444 ms). Eight
+  // predecessors per round trip measured best (16: 0.511 ms, 32: 0.562 ms, before the changes above).
+  u32 prefix = 0;
+  if (tid < kRadix && tileInSeg > 0)
+  {
+    prefix = lookback_prefix(vstatus, tile, firstTile, u32(tid), err);
+    vstatus[u64(tile) * kRadix + tid] = kStatusInclusive | ((prefix + total) & kStatusValueMask);
+  }
+  if (tid < kRadix)
+    s_globalBase[tid] = segBase + digitBase[tid] + prefix - digitStart;
   __syncthreads();
 
   const u32 tileCount = min(u32(kSortTile), segEnd - base);
@@ -430,6 +468,8 @@ inline bool onesweep_passes(K* k0, u32* v0, K* k1, u32* v1, u64 n, u32 shift0, u
   auto kfn = stage ? onesweep_pass_kernel<K, false, false, true> : onesweep_pass_kernel<K>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(onesweep_smem_bytes<K>()));
   const u32 tiles = u32(SortScratch::tiles(n));
+  if (passes)
+    digit_base_kernel<<<passes, kRadix, 0, st>>>(s.hist);
   for (u32 p = 0; p < passes; ++p)
   {
     const bool even = (p % 2) == 0;
@@ -450,6 +490,8 @@ inline bool onesweep_passes_devn(K* k0, u32* v0, K* k1, u32* v1, u64 n, const un
 {
   cudaFuncSetAttribute(onesweep_pass_kernel<K, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(onesweep_smem_bytes<K>()));
   const u32 tiles = u32(SortScratch::tiles(n));
+  if (passes)
+    digit_base_kernel<<<passes, kRadix, 0, st>>>(s.hist);
   for (u32 p = 0; p < passes; ++p)
   {
     const bool even = (p % 2) == 0;
@@ -467,9 +509,11 @@ inline bool onesweep_passes_devn(K* k0, u32* v0, K* k1, u32* v1, u64 n, const un
 // Segmented passes: `tiles` tiles listed in segTiles; hist holds [pass][segment][256] counts.
 template<typename K>
 inline bool onesweep_passes_segmented(K* k0, u32* v0, K* k1, u32* v1, u64 n, u32 passes, bool iotaValues, const uint2* segTiles, u32 tiles,
-                                      const u64* segOff, u32 segments, const u32* hist, u32* status, u32* counters, u32* err, cudaStream_t st)
+                                      const u64* segOff, u32 segments, u32* hist, u32* status, u32* counters, u32* err, cudaStream_t st)
 {
   cudaFuncSetAttribute(onesweep_pass_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(onesweep_smem_bytes<K>()));
+  if (tiles && passes && segments)
+    digit_base_kernel<<<passes * segments, kRadix, 0, st>>>(hist);
   for (u32 p = 0; p < passes; ++p)
   {
     const bool even = (p % 2) == 0;

@@ -163,6 +163,23 @@ def test_point_emission_layouts(dtype, name):
     assert_csr_equal(t.knn(q, 9), o.knn(q, 9), f"{name} knn")
 
 
+@pytest.mark.parametrize("max_depth", [8, 9, 10])
+@pytest.mark.parametrize("n", [1, 2, 100, 4095, 4096, 4097, 12289, 70_001])
+def test_point_sort_tile_boundaries(max_depth, n):
+    """Radix-sort tiles of 4096 keys: one key, one tile, a partial last tile, sizes either side of
+    a tile boundary, and a run of identical keys across tiles, in the data's bounding box and in a
+    given box, against the oracle."""
+    rng = np.random.default_rng(n * 16 + max_depth)
+    pts = rng.random((n, 3))
+    if n > 10:
+        pts[: n // 10] = pts[n // 2]  # a run of identical keys across tiles
+    for box in (None, np.array([0.0, 0, 0, 1, 1, 1])):
+        t = _gpu_tree(pts, KIND_POINTS, max_depth, box, 4)
+        o = oracle().create(pts, KIND_POINTS, max_depth, box, 4)
+        assert np.array_equal(t.location_keys(), o.location_keys())
+        assert_nodes_equal(t.nodes(), o.nodes(), f"n={n} depth {max_depth} box {box is not None}")
+
+
 @pytest.mark.parametrize("kind", [KIND_LOOSE_BOXES, KIND_BOXES])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("max_depth,max_elem", [(8, 32), (0, 16), (4, 2)])
