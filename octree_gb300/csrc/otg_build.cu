@@ -441,7 +441,8 @@ __device__ __forceinline__ float to_f(float v) { return v; }
 
 // Location key of one entity from the threshold tables (layout in otg_raster.cuh): integer
 // compares only, around an FP32 estimate of the cell.
-template<typename T, bool IS_BOX>
+// NARROW (points with 32-bit keys, depth up to 10): the Morton code in 32-bit arithmetic.
+template<typename T, bool IS_BOX, bool NARROW = false>
 __device__ __forceinline__ u64 entity_key(const T* e, const typename Ord<T>::U* __restrict__ tab, size_t perDim, u32 cells, const float* minF,
                                           const float* rastF, u32 D)
 {
@@ -460,7 +461,10 @@ __device__ __forceinline__ u64 entity_key(const T* e, const typename Ord<T>::U* 
       const float est = (approx_f(e[d]) - minF[d]) * rastF[d];
       g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, o, est > 2.0e9f ? 2000000000 : int(est));
     }
-    return valid ? encode3(g[0], g[1], g[2]) + 1 : 0;
+    if constexpr (NARROW)
+      return valid ? u64(encode3_10(g[0], g[1], g[2]) + 1u) : 0;
+    else
+      return valid ? encode3(g[0], g[1], g[2]) + 1 : 0;
   }
   else
   {
@@ -545,7 +549,7 @@ __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent,
         kk = K(k64);
       }
       else
-        kk = K(entity_key<T, IS_BOX>(v + k * W, tab, perDim, cells, minF, rastF, D));
+        kk = K(entity_key<T, IS_BOX, sizeof(K) == 4>(v + k * W, tab, perDim, cells, minF, rastF, D));
       keys[c * E + k] = kk;
       for (u32 p = 0; p < passes; ++p)
         atomicAdd(&sh[p][(kk >> (kRadixBits * p)) & (kRadix - 1)], 1u);
@@ -1671,7 +1675,7 @@ __global__ void __launch_bounds__(256) forest_codegen_kernel(const T* __restrict
       kk = K(k64);
     }
     else
-      kk = K(entity_key<T, IS_BOX>(v, tab, perDim, cells, minF, rastF, D));
+      kk = K(entity_key<T, IS_BOX, sizeof(K) == 4>(v, tab, perDim, cells, minF, rastF, D));
     keys[i] = kk;
     for (u32 p = 0; p < passes; ++p)
       atomicAdd(&sh[p][(kk >> (kRadixBits * p)) & (kRadix - 1)], 1u);

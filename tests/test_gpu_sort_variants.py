@@ -1,6 +1,7 @@
 """The opt-in forms of the build's radix sort give the default form's trees: tiles staged by bulk
 copies (OTG_SORT_STAGE=1) and the chunked persistent passes (OTG_SORT=chunked). The switches are
-read once per process, so each form builds in a child process."""
+read once per process, so each form builds in a child process, which prints a digest of its
+location keys and of its nodes in canonical order (node order follows the emission's scheduling)."""
 import os
 import subprocess
 import sys
@@ -23,9 +24,13 @@ out = []
 for kind, ent, depth in (("points", pts, 10), ("points", pts[:4097], 9), ("boxes", boxes, 8)):
     t = otg.Tree(kind).create(ent, max_depth=depth, max_elements=12)
     h = hashlib.sha256(np.ascontiguousarray(t.location_keys()).tobytes())
-    nodes = t.nodes()
-    for k in sorted(nodes):
-        h.update(np.ascontiguousarray(nodes[k]).tobytes())
+    g = t.nodes()  # nodes in emission order: canonical form by key, entity ids ascending per node
+    order = np.argsort(g["keys"], kind="stable")
+    eoff = g["eoff"].astype(np.int64)
+    for a in (g["keys"][order], g["min"][order], g["size"][order]):
+        h.update(np.ascontiguousarray(a).tobytes())
+    for i in order:
+        h.update(np.sort(g["eids"][eoff[i] : eoff[i + 1]]).tobytes())
     out.append(h.hexdigest())
 print(" ".join(out))
 """
