@@ -441,25 +441,66 @@ __device__ __forceinline__ float to_f(float v) { return v; }
 
 // Location key of one entity from the threshold tables (layout in otg_raster.cuh): integer
 // compares only, around an FP32 estimate of the cell.
+// Margin of the FP32 cell estimate est = (approx_f(x) - float(min)) * float(rast) of a point
+// coordinate x inside the space, against the reference's cell value v = (x - min) * rast (FP64, or
+// FP32 for FP32 trees below depth 16). approx_f truncates to 23 mantissa bits (relative error
+// below 2^-23), float(min) and float(rast) round to nearest (2^-24 each), and the subtraction and
+// the product round to nearest (2^-24 each). With M = max(|min|, |max|) and est, v below `cells`:
+//   |est - v| <= rast * M * (2^-23 + 2^-24) + cells * 3 * 2^-24 (+ the reference's own 2^-52 terms)
+//             <  rast * M * 2^-22 + cells * 2^-22 + 2^-20.
+// A coordinate whose estimate lies more than that margin from every integer, inside (0, cells),
+// has the reference's cell trunc(est) and lies inside the space, so it needs no threshold lookup.
+// Margins of 1/4 or more switch the shortcut off (2.0 never passes). One thread per dimension.
+template<typename T>
+__device__ __forceinline__ float cell_estimate_margin(const Space<T>& s, int d, double rast, u32 cells)
+{
+  const double M = fmax(fabs(double(s.min[d])), fabs(double(s.max[d])));
+  const double m = rast * M * 0x1p-22 + double(cells) * 0x1p-22 + 0x1p-20;
+  return m < 0.25 ? __double2float_ru(m) : 2.0f;
+}
+
 // NARROW (points with 32-bit keys, depth up to 10): the Morton code in 32-bit arithmetic.
+// margF (points, optional): the cell-estimate margins of cell_estimate_margin; coordinates whose
+// estimates clear them take their cell from the estimate, the others from the threshold tables.
 template<typename T, bool IS_BOX, bool NARROW = false>
 __device__ __forceinline__ u64 entity_key(const T* e, const typename Ord<T>::U* __restrict__ tab, size_t perDim, u32 cells, const float* minF,
-                                          const float* rastF, u32 D)
+                                          const float* rastF, u32 D, const float* margF = nullptr)
 {
   using O = Ord<T>;
   using U = typename O::U;
   if constexpr (!IS_BOX)
   {
-    bool valid = true;
+    float est[3];
+    bool clear = margF != nullptr;
     u32 g[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+      est[d] = (approx_f(e[d]) - minF[d]) * rastF[d];
+      if (margF)
+      {
+        const float m = margF[d];
+        const bool inside = est[d] > m && est[d] < float(cells) - m;
+        g[d] = inside ? u32(est[d]) : 0u;
+        const float f = est[d] - float(g[d]);
+        clear = clear && inside && f > m && f < 1.0f - m;
+      }
+    }
+    if (clear)
+    {
+      if constexpr (NARROW)
+        return u64(encode3_10(g[0], g[1], g[2]) + 1u);
+      else
+        return encode3(g[0], g[1], g[2]) + 1;
+    }
+    bool valid = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d)
     {
       const U* td = tab + d * perDim;
       const U o = ord_bits(e[d]);
       valid = valid && o >= td[0] && o <= td[1];
-      const float est = (approx_f(e[d]) - minF[d]) * rastF[d];
-      g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, o, est > 2.0e9f ? 2000000000 : int(est));
+      g[d] = cell_from_table(td + 2 + kLevelThresholds, cells, o, est[d] > 2.0e9f ? 2000000000 : int(est[d]));
     }
     if constexpr (NARROW)
       return valid ? u64(encode3_10(g[0], g[1], g[2]) + 1u) : 0;
@@ -507,7 +548,7 @@ __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent,
   constexpr int E = Chunk<T, W>::E;
   extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ u32 sh[8][kRadix];
-  __shared__ float minF[3], rastF[3];
+  __shared__ float minF[3], rastF[3], margF[3];
   __shared__ u32 sD;
   const size_t perDim = RasterLayout<T>::per_dim(cells);
   U* stab = reinterpret_cast<U*>(s_dyn);
@@ -521,6 +562,7 @@ __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent,
     const Space<T>& s = *spg;
     minF[threadIdx.x] = to_f(s.min[threadIdx.x]);
     rastF[threadIdx.x] = float(Raster<R, T>::rast(s, threadIdx.x));
+    margF[threadIdx.x] = cell_estimate_margin(s, threadIdx.x, double(Raster<R, T>::rast(s, threadIdx.x)), cells);
     if (threadIdx.x == 0)
       sD = s.D;
   }
@@ -549,7 +591,7 @@ __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent,
         kk = K(k64);
       }
       else
-        kk = K(entity_key<T, IS_BOX, sizeof(K) == 4>(v + k * W, tab, perDim, cells, minF, rastF, D));
+        kk = K(entity_key<T, IS_BOX, sizeof(K) == 4>(v + k * W, tab, perDim, cells, minF, rastF, D, margF));
       keys[c * E + k] = kk;
       for (u32 p = 0; p < passes; ++p)
         atomicAdd(&sh[p][(kk >> (kRadixBits * p)) & (kRadix - 1)], 1u);
@@ -1633,7 +1675,7 @@ __global__ void __launch_bounds__(256) forest_codegen_kernel(const T* __restrict
   constexpr int W = IS_BOX ? 6 : 3;
   extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ u32 sh[8][kRadix];
-  __shared__ float minF[3], rastF[3];
+  __shared__ float minF[3], rastF[3], margF[3];
   const uint2 st = segTiles[blockIdx.x];
   const u32 tr = st.x;
   const Space<T>& s = sp[tr];
@@ -1651,6 +1693,8 @@ __global__ void __launch_bounds__(256) forest_codegen_kernel(const T* __restrict
   {
     minF[threadIdx.x] = to_f(s.min[threadIdx.x]);
     rastF[threadIdx.x] = s.rasterDouble ? float(s.rastD[threadIdx.x]) : s.rastF[threadIdx.x];
+    margF[threadIdx.x] =
+      cell_estimate_margin(s, threadIdx.x, s.rasterDouble ? s.rastD[threadIdx.x] : double(s.rastF[threadIdx.x]), cells);
   }
   __syncthreads();
   if (tabInSmem)
@@ -1675,7 +1719,7 @@ __global__ void __launch_bounds__(256) forest_codegen_kernel(const T* __restrict
       kk = K(k64);
     }
     else
-      kk = K(entity_key<T, IS_BOX, sizeof(K) == 4>(v, tab, perDim, cells, minF, rastF, D));
+      kk = K(entity_key<T, IS_BOX, sizeof(K) == 4>(v, tab, perDim, cells, minF, rastF, D, margF));
     keys[i] = kk;
     for (u32 p = 0; p < passes; ++p)
       atomicAdd(&sh[p][(kk >> (kRadixBits * p)) & (kRadix - 1)], 1u);
@@ -2276,18 +2320,21 @@ __global__ void __launch_bounds__(256) insert_keys_kernel(const T* __restrict__ 
                                                           u32* __restrict__ err)
 {
   const Space<T>& s = *spg;
-  float minF[3], rastF[3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d)
+  __shared__ float minF[3], rastF[3], margF[3];
+  if (threadIdx.x < 3)
   {
+    const int d = threadIdx.x;
     minF[d] = to_f(s.min[d]);
     rastF[d] = float(Raster<R, T>::rast(s, d));
+    margF[d] = cell_estimate_margin(s, d, double(Raster<R, T>::rast(s, d)), cells);
   }
+  __syncthreads();
   const size_t perDim = RasterLayout<T>::per_dim(cells);
+  const u32 D = s.D;
   for (u64 i = blockIdx.x * u64(blockDim.x) + threadIdx.x; i < n2; i += u64(gridDim.x) * blockDim.x)
   {
     const T e[3] = { pts[3 * i], pts[3 * i + 1], pts[3 * i + 2] };
-    const u64 k = entity_key<T, false>(e, tab, perDim, cells, minF, rastF, s.D);
+    const u64 k = entity_key<T, false>(e, tab, perDim, cells, minF, rastF, D, margF);
     if (k == 0)
       atomicOr(err, kErrArgument); // outside the space
     keys[i] = K(k);
