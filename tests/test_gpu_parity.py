@@ -180,6 +180,33 @@ def test_point_sort_tile_boundaries(max_depth, n):
         assert_nodes_equal(t.nodes(), o.nodes(), f"n={n} depth {max_depth} box {box is not None}")
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("max_depth", [10, 12])
+@pytest.mark.parametrize("offset", [0.0, 819.0, 1e6])
+def test_point_cells_near_boundaries(dtype, max_depth, offset):
+    """Point cells from the FP32 estimate where it clears its rounding margin, from the threshold
+    tables elsewhere: coordinates exactly on cell boundaries, a few ulps either side, and at
+    distances around the margin (which grows with the coordinates' magnitude; at an offset of 1e6
+    it switches the estimate off), in a given box and in the points' own box, against the oracle."""
+    rng = np.random.default_rng(int(offset) + max_depth)
+    cells = 1 << max_depth
+    width = 1000.0 / cells
+    j = rng.integers(0, cells + 1, (60_000, 3)).astype(np.float64)
+    x = j * width
+    k = rng.integers(-4, 5, x.shape)
+    for step in range(4):  # up to four ulps either side
+        x = np.where(k > step, np.nextafter(x, np.inf), np.where(k < -step, np.nextafter(x, -np.inf), x))
+    margin = (1000.0 + offset) * (cells / 1000.0) * 2.0**-22 + cells * 2.0**-22
+    near = (j + rng.choice([-2.0, -1.0, -0.5, 0.5, 1.0, 2.0], j.shape) * margin) * width
+    pts = np.concatenate([x, near, rng.random((60_000, 3)) * 1000.0]) + offset
+    pts = np.clip(pts, offset, offset + 1000.0).astype(dtype)
+    for box in (None, np.array([offset] * 3 + [offset + 1000.0] * 3, dtype)):
+        t = _gpu_tree(pts, KIND_POINTS, max_depth, box, 16)
+        o = oracle().create(pts, KIND_POINTS, max_depth, box, 16)
+        assert np.array_equal(t.location_keys(), o.location_keys()), f"box {box is not None}"
+        assert_nodes_equal(t.nodes(), o.nodes(), f"offset {offset} box {box is not None}")
+
+
 @pytest.mark.parametrize("kind", [KIND_LOOSE_BOXES, KIND_BOXES])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("max_depth,max_elem", [(8, 32), (0, 16), (4, 2)])
