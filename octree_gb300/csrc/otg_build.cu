@@ -1406,12 +1406,9 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
 }
 
 // The L2 fetch granularity limit of this process's CUDA context (cudaLimitMaxL2FetchGranularity, a
-// per-context performance hint that ends with the process), set once before the first build: 64
-// bytes. The gather of a build reads one 24-byte point at a random position per output; with the
-// default granularity each such read brought about a whole 128-byte line from DRAM (125 B per point
-// measured at 16M points). Measured on the 16M-point build: 1.340 ms per build at the default, 1.303
-// ms at 64 bytes, 1.316 ms at 32 bytes. OTG_L2_FETCH_BYTES chooses another value; 0 leaves the
-// context's limit as it is.
+// per-context performance hint that ends with the process). The gather of a build reads one 24-byte
+// point at a random position per output, and each such read brings about a whole 128-byte line from
+// DRAM (125 B per point measured at 16M points).
 // OTG_L2_FETCH_BYTES=b sets the context's L2 fetch granularity limit before the first build (0 or
 // unset: unchanged). Measured on the 16M-point build: unchanged 1.359 ms, 32 B 1.394 ms, 64 B
 // 1.365 ms, 128 B 1.360 ms; the gather's extra sectors cost no time, so the default leaves it.
