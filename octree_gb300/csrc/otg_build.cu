@@ -537,10 +537,17 @@ __device__ __forceinline__ u64 entity_key(const T* e, const typename Ord<T>::U* 
   }
 }
 
-template<typename T, typename R, typename K, bool IS_BOX>
+// STAGED (16-byte aligned entities): whole tiles of 256 chunks (12 KB) arrive in shared memory by
+// bulk copies (cp.async.bulk, completion on an mbarrier), two buffers deep, while the previous tile
+// is coded; each thread reads its 48-byte chunk from shared memory. The chunks after the last whole
+// tile take the direct loads. stageOff: byte offset of the two buffers in dynamic shared memory.
+constexpr u32 kCodegenTileChunks = 256;
+constexpr u32 kCodegenTileBytes = kCodegenTileChunks * 48;
+template<typename T, typename R, typename K, bool IS_BOX, bool STAGED = false>
 __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent, u64 n, bool vec, const Space<T>* __restrict__ spg,
                                                       const typename Ord<T>::U* __restrict__ tabG, u32 cells, int tabInSmem,
-                                                      K* __restrict__ keys, u32* __restrict__ hist, u32 passes, bool regular, u32* __restrict__ err)
+                                                      K* __restrict__ keys, u32* __restrict__ hist, u32 passes, bool regular, u32* __restrict__ err,
+                                                      u32 stageOff = 0)
 {
   using O = Ord<T>;
   using U = typename O::U;
@@ -570,10 +577,7 @@ __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent,
   const U* tab = tabInSmem ? stab : tabG;
   const u32 D = sD;
   const u64 chunks = (n + E - 1) / E;
-  for (u64 c = blockIdx.x * u64(blockDim.x) + threadIdx.x; c < chunks; c += u64(gridDim.x) * blockDim.x)
-  {
-    T v[E * W];
-    const int cnt = load_chunk<T, W>(ent, n, c * E, vec, v);
+  auto code = [&](const T* v, u64 c, int cnt) {
 #pragma unroll
     for (int k = 0; k < E; ++k)
     {
@@ -596,6 +600,88 @@ __global__ void __launch_bounds__(256) codegen_kernel(const T* __restrict__ ent,
       for (u32 p = 0; p < passes; ++p)
         atomicAdd(&sh[p][(kk >> (kRadixBits * p)) & (kRadix - 1)], 1u);
     }
+  };
+  u64 firstDirect = 0;
+  if constexpr (STAGED)
+  {
+    __shared__ __align__(8) u64 s_bar[2];
+    unsigned char* stage = s_dyn + stageOff;
+    const u64 fullTiles = chunks == 0 ? 0 : (n / E) / kCodegenTileChunks; // tiles of whole chunks only
+    const unsigned char* src = reinterpret_cast<const unsigned char*>(ent);
+    if (threadIdx.x == 0)
+    {
+      mbar_init(&s_bar[0], 1);
+      mbar_init(&s_bar[1], 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](u64 tile, int b) {
+      mbar_arrive_expect_tx(&s_bar[b], kCodegenTileBytes);
+      bulk_load(stage + b * kCodegenTileBytes, src + tile * kCodegenTileBytes, kCodegenTileBytes, &s_bar[b]);
+    };
+    u64 t = blockIdx.x;
+    u32 it = 0;
+    if (threadIdx.x == 0 && t < fullTiles)
+      issue(t, 0);
+    bool failed = false;
+    for (; t < fullTiles; t += gridDim.x, ++it)
+    {
+      const int b = int(it & 1u);
+      if (threadIdx.x == 0 && t + gridDim.x < fullTiles)
+      {
+        fence_proxy_async(); // buffer b ^ 1 was read before the barrier that ended the last tile
+        issue(t + gridDim.x, b ^ 1);
+      }
+      const bool ok = mbar_wait_bounded(&s_bar[b], (it >> 1) & 1u);
+      if (__syncthreads_or(!ok))
+      {
+        failed = true;
+        break;
+      }
+      T v[E * W];
+      const T* mine = reinterpret_cast<const T*>(stage + b * kCodegenTileBytes) + threadIdx.x * (E * W);
+      if constexpr (sizeof(T) == 8)
+      {
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+        {
+          const double2 x = reinterpret_cast<const double2*>(mine)[j];
+          v[2 * j] = x.x;
+          v[2 * j + 1] = x.y;
+        }
+      }
+      else
+      {
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+        {
+          const float4 x = reinterpret_cast<const float4*>(mine)[j];
+          v[4 * j] = x.x;
+          v[4 * j + 1] = x.y;
+          v[4 * j + 2] = x.z;
+          v[4 * j + 3] = x.w;
+        }
+      }
+      code(v, t * kCodegenTileChunks + threadIdx.x, E);
+      __syncthreads(); // buffer b is read: the copy two tiles on may overwrite it
+    }
+    if (failed)
+    {
+      // the copies in flight land before this block's shared memory goes away; the error bit fails
+      // the build
+      if (threadIdx.x == 0)
+        atomicOr(err, kErrTimeout);
+      mbar_wait_bounded(&s_bar[it & 1u], (it >> 1) & 1u);
+      mbar_wait_bounded(&s_bar[(it + 1) & 1u], ((it + 1) >> 1) & 1u);
+      return;
+    }
+    firstDirect = fullTiles * kCodegenTileChunks;
+  }
+  for (u64 c = firstDirect + blockIdx.x * u64(blockDim.x) + threadIdx.x; c < chunks; c += u64(gridDim.x) * blockDim.x)
+  {
+    T v[E * W];
+    const int cnt = load_chunk<T, W>(ent, n, c * E, vec, v);
+    code(v, c, cnt);
   }
   __syncthreads();
   for (u32 p = 0; p < passes; ++p)
@@ -1310,22 +1396,29 @@ static int build_impl(TreeState& t, const T* ent, const void* box, u64 n, cudaSt
 
   prof.mark("codegen", st);
   const int tabInSmem = tabBytes <= 64 * 1024 ? 1 : 0;
-  const size_t cgSmem = tabInSmem ? tabBytes : 0;
+  static const bool cgStage = [] {
+    const char* v = std::getenv("OTG_CODEGEN_STAGE");
+    return v && v[0] == '1';
+  }();
+  const bool staged = cgStage && vec;
+  const u32 stageOff = u32((tabInSmem ? tabBytes : 0) + 15) & ~15u;
+  const size_t cgSmem = staged ? stageOff + 2 * kCodegenTileBytes : (tabInSmem ? tabBytes : 0);
   // up to 16 blocks per SM: more blocks in flight than fit at once balance the grid-stride loop
   // (16M points: 0.184 ms at 4 per SM, 0.168 ms at 16, 0.186 ms at 64)
-  const int cgBlocks = grid_blocks((n + Chunk<T, W>::E - 1) / Chunk<T, W>::E, 256, 152 * 16);
-  if (rasterDouble)
+  int cgBlocks = grid_blocks((n + Chunk<T, W>::E - 1) / Chunk<T, W>::E, 256, 152 * 16);
+  auto kfn = rasterDouble ? (staged ? codegen_kernel<T, double, K, IS_BOX, true> : codegen_kernel<T, double, K, IS_BOX>)
+                          : (staged ? codegen_kernel<T, float, K, IS_BOX, true> : codegen_kernel<T, float, K, IS_BOX>);
+  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
+  if (staged)
   {
-    auto kfn = codegen_kernel<T, double, K, IS_BOX>;
-    cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
-    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes, regular, t.err.as<u32>());
+    // the tiles are shared out over the blocks that fit at once
+    int perSm = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kfn, 256, cgSmem);
+    cgBlocks = std::max(1, std::min(cgBlocks, std::max(perSm, 1) * std::max(sms, 1)));
   }
-  else
-  {
-    auto kfn = codegen_kernel<T, float, K, IS_BOX>;
-    cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cgSmem));
-    kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes, regular, t.err.as<u32>());
-  }
+  kfn<<<cgBlocks, 256, cgSmem, st>>>(ent, n, vec, sp, tab, cells, tabInSmem, t.keysA.as<K>(), ss.hist, passes, regular, t.err.as<u32>(), stageOff);
 
   prof.mark("sort", st);
   bool inB = false;

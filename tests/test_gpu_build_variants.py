@@ -1,7 +1,8 @@
-"""The opt-in forms of the build's radix sort give the default form's trees: tiles staged by bulk
-copies (OTG_SORT_STAGE=1) and the chunked persistent passes (OTG_SORT=chunked). The switches are
-read once per process, so each form builds in a child process, which prints a digest of its
-location keys and of its nodes in canonical order (node order follows the emission's scheduling)."""
+"""The opt-in forms of the build give the default form's trees: radix-sort tiles staged by bulk
+copies (OTG_SORT_STAGE=1), the chunked persistent sort passes (OTG_SORT=chunked), and codegen
+tiles staged by bulk copies (OTG_CODEGEN_STAGE=1). The switches are read once per process, so each
+form builds in a child process, which prints a digest of its location keys and of its nodes in
+canonical order (node order follows the emission's scheduling)."""
 import os
 import subprocess
 import sys
@@ -40,6 +41,7 @@ def _digests(env_extra):
     env = dict(os.environ)
     env.pop("OTG_SORT", None)
     env.pop("OTG_SORT_STAGE", None)
+    env.pop("OTG_CODEGEN_STAGE", None)
     env.update(env_extra)
     env["PYTHONPATH"] = ROOT + os.pathsep + env.get("PYTHONPATH", "")
     p = subprocess.run([sys.executable, "-c", CHILD], env=env, cwd=ROOT, capture_output=True, text=True, timeout=600)
@@ -47,6 +49,6 @@ def _digests(env_extra):
     return p.stdout.split()
 
 
-@pytest.mark.parametrize("variant", [{"OTG_SORT_STAGE": "1"}, {"OTG_SORT": "chunked"}])
-def test_sort_variant_builds_the_same_trees(variant):
+@pytest.mark.parametrize("variant", [{"OTG_SORT_STAGE": "1"}, {"OTG_SORT": "chunked"}, {"OTG_CODEGEN_STAGE": "1"}])
+def test_build_variant_builds_the_same_trees(variant):
     assert _digests(variant) == _digests({})
