@@ -185,22 +185,28 @@ def test_point_sort_tile_boundaries(max_depth, n):
 @pytest.mark.parametrize("offset", [0.0, 819.0, 1e6])
 def test_point_cells_near_boundaries(dtype, max_depth, offset):
     """Point cells from the FP32 estimate where it clears its rounding margin, from the threshold
-    tables elsewhere: coordinates exactly on cell boundaries, a few ulps either side, and at
-    distances around the margin (which grows with the coordinates' magnitude; at an offset of 1e6
-    it switches the estimate off), in a given box and in the points' own box, against the oracle."""
+    tables elsewhere: coordinates on cell boundaries, a few ulps either side, at distances around
+    the margin, and full-mantissa values within two margins of a boundary, in a space whose
+    boundaries are not short binary fractions. The margin grows with the coordinates' magnitude: at
+    an offset of 1e6 it leaves about half of the coordinates to the tables at depth 10 and switches
+    the estimate off at depth 12. In a given box and in the points' own box, against the oracle
+    (tests/test_cell_estimate_margin.py checks the same estimate on the CPU, and that these inputs
+    need the margin)."""
     rng = np.random.default_rng(int(offset) + max_depth)
     cells = 1 << max_depth
-    width = 1000.0 / cells
+    size, low = 1000.123456789, offset + 0.3712345
+    width = size / cells
     j = rng.integers(0, cells + 1, (60_000, 3)).astype(np.float64)
-    x = j * width
+    x = low + j * width
     k = rng.integers(-4, 5, x.shape)
     for step in range(4):  # up to four ulps either side
         x = np.where(k > step, np.nextafter(x, np.inf), np.where(k < -step, np.nextafter(x, -np.inf), x))
-    margin = (1000.0 + offset) * (cells / 1000.0) * 2.0**-22 + cells * 2.0**-22
-    near = (j + rng.choice([-2.0, -1.0, -0.5, 0.5, 1.0, 2.0], j.shape) * margin) * width
-    pts = np.concatenate([x, near, rng.random((60_000, 3)) * 1000.0]) + offset
-    pts = np.clip(pts, offset, offset + 1000.0).astype(dtype)
-    for box in (None, np.array([offset] * 3 + [offset + 1000.0] * 3, dtype)):
+    margin = (size + offset) * (cells / size) * 2.0**-22 + cells * 2.0**-22
+    near = low + (j + rng.choice([-2.0, -1.0, -0.5, 0.5, 1.0, 2.0], j.shape) * margin) * width
+    band = low + (j + (rng.random(j.shape) * 2.0 - 1.0) * 2.0 * margin) * width
+    pts = np.concatenate([x, near, band, low + rng.random((60_000, 3)) * size])
+    pts = np.clip(pts, low, low + size).astype(dtype)
+    for box in (None, np.array([low] * 3 + [low + size] * 3, dtype)):
         t = _gpu_tree(pts, KIND_POINTS, max_depth, box, 16)
         o = oracle().create(pts, KIND_POINTS, max_depth, box, 16)
         assert np.array_equal(t.location_keys(), o.location_keys()), f"box {box is not None}"
