@@ -409,7 +409,7 @@ int main()
              "Core: CollisionDetection(two trees)");
       oro_res_free(r);
       oro_destroy(obc);
-      // move some boxes of the first span in place: the next round answers for the moved span
+      // move some boxes of the first span in place: the next pass of the loop answers for the moved span
       for (std::size_t i = 0; i < bspan.size(); i += 4)
         for (int c = 0; c < 3; ++c)
         {
