@@ -7,8 +7,10 @@
 //      core/ot_base.h:121-134), exact rasterisation thresholds and the
 //      MinPoint node table (otg_raster.cuh)                              -> space_setup / raster_tables / node_min_table
 //   3. one location key per entity (si_mortongrid.h:69-97) fused with the radix digit
-//      histograms of the sort; integer compares against the thresholds   -> codegen_kernel
-//   4. stable radix sort of (key, id) (replaces std::sort(par), :791-796)  -> otg_sort.cuh
+//      histograms of the sort; a point coordinate's cell from its FP32 estimate where that clears
+//      the estimate's rounding margin, else integer compares against the thresholds -> codegen_kernel
+//   4. stable radix sort of (key, id) (replaces std::sort(par), :791-796): digit bases
+//      per pass, then one onesweep launch per 8-bit digit             -> digit_base / onesweep (otg_sort.cuh)
 //   5. entities gathered into tree order                                   -> gather_kernel
 //   6. node emission, one launch per depth (BuildSubtree/ProcessNode,
 //      :647-747): a node whose subtree holds more than maxElem entities and
